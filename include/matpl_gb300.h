@@ -1,0 +1,141 @@
+/*
+ * matpl_gb300 — C ABI of the GB300-native (sm_103a) DP / NEP evaluation path of MatPL.
+ *
+ * Every entry point takes raw device pointers, sizes, a dtype code and a cudaStream_t
+ * (passed as void*), launches asynchronously on that stream, allocates nothing (scratch is
+ * a caller-provided workspace whose size a *_workspace_bytes() query returns) and returns a
+ * matpl_status.  Errors found by a kernel (neighbor overflow ...) are written to a
+ * caller-provided device int32 (err_dev); the caller reads it after the stream is done.
+ * matpl_last_error() gives a message for the last failing call on the calling thread.
+ *
+ * Layout conventions follow the reference's tensors (row-major, contiguous):
+ *   B = configurations in the batch, N = local atoms, S = neighbor slots per atom
+ *   (= ntypes * m, per-type blocks of m slots), nghost = ghost atoms (LAMMPS).
+ */
+#ifndef MATPL_GB300_H
+#define MATPL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    MATPL_OK = 0,
+    MATPL_ERR_INVALID = 1,      /* bad size / pointer / unsupported shape */
+    MATPL_ERR_DTYPE = 2,        /* dtype code not supported by this entry point */
+    MATPL_ERR_WORKSPACE = 3,    /* workspace smaller than *_workspace_bytes() */
+    MATPL_ERR_CUDA = 4,         /* a CUDA runtime call failed (launch, memset) */
+    MATPL_ERR_UNSUPPORTED = 5   /* model shape outside the compiled kernels */
+} matpl_status;
+
+/* Codes a kernel writes to err_dev (0 = fine). */
+#define MATPL_KERR_NEIGHBOR_OVERFLOW 1   /* a type block exceeds m (NeighConst.f90:75-78) */
+#define MATPL_KERR_BAD_TYPE 2            /* atom type index outside [0, ntypes) */
+
+typedef enum { MATPL_F32 = 0, MATPL_F64 = 1, MATPL_MIXED = 2 } matpl_dtype;
+
+const char *matpl_last_error(void);
+int matpl_version(void);
+
+/* ------------------------------------------------------------------------------------
+ * Force / virial custom ops.
+ * Replaces CalcOps_cuda::calculateForce (src/op/src/CalcOps.cpp:6-22 -> kernel
+ * src/op/kernel/calculateForce.cu:49-142) and its backward (calculateForceGrad.cu:10-90),
+ * CalcOps_cuda::calculateVirial (CalcOps.cpp:170-185 -> calculateVirial.cu:19-120) and its
+ * backward (calculateVirialGrad.cu:16-92).
+ *   list_neigh [B,N,S] int32, 0-based neighbor index, -1 = empty slot
+ *   dE         [B,N,4S]    dE/dRi of the normalised environment matrix
+ *   Ri_d       [B,N,4S,3]  dRi/dr_i
+ *   Rij        [B,N,S,3]   pair vectors (ImageDR[...,1:])
+ * Batch stride of force / atom_virial is N+nghost (the shape of the returned tensor).
+ * ---------------------------------------------------------------------------------- */
+int matpl_calc_force(int dtype, const int32_t *list_neigh, const void *dE, const void *Ri_d,
+                     const void *F_center, int batch, int natoms, int nslots, int nghost,
+                     void *force_out, void *stream);
+
+int matpl_calc_virial(int dtype, const int32_t *list_neigh, const void *dE, const void *Rij,
+                      const void *Ri_d, int batch, int natoms, int nslots, int nghost,
+                      void *virial_out, void *atom_virial_out, void *stream);
+
+/* grad_dE [B,N,4S] = d(force . grad_force)/d(dE); grad_force [B,N+nghost,3]. */
+int matpl_calc_force_grad(int dtype, const int32_t *list_neigh, const void *Ri_d,
+                          const void *grad_force, int batch, int natoms, int nslots, int nghost,
+                          void *grad_dE, void *stream);
+
+/* grad_dE [B,N,4S] = d(virial . grad_virial)/d(dE); grad_virial [B,9]. */
+int matpl_calc_virial_grad(int dtype, const int32_t *list_neigh, const void *Rij,
+                           const void *Ri_d, const void *grad_virial, int batch, int natoms,
+                           int nslots, void *grad_dE, void *stream);
+
+/* ------------------------------------------------------------------------------------
+ * DP neighbor search.  Replaces the Fortran NeighConst.find_neighbore
+ * (src/pre_data/gen_feature/NeighConst.f90:14-149) as called by
+ * src/pre_data/dpuni_data_loader.py:595-650, plus the r column of compute_Ri (:652-716).
+ *   frac_pos   [B,N,3] f64 fractional coordinates (wrapped with mod(x+10,1) internally)
+ *   lattice    [B,3,3] f64 row vectors
+ *   type_map   [N] int32 0-based type of each atom
+ *   Rc_type    host array [ntypes] per centre-type cutoff
+ * Outputs (fully written):
+ *   list_neigh [B,N,ntypes*m] int32, 1-based, 0 = empty; per type ascending j (then image)
+ *   image_dr   [B,N,ntypes*m,4] (r, dx, dy, dz), f64 or f32 per out_dtype
+ *   num_neigh  [B,N,ntypes] int32 or NULL
+ * Index sets and f64 dR are bit-identical to the restatement of the Fortran source.
+ * ---------------------------------------------------------------------------------- */
+size_t matpl_neighbor_workspace_bytes(int batch, int natoms);
+int matpl_neighbor_build(int batch, int natoms, int ntypes, int m_neigh, double Rc_M,
+                         const double *Rc_type, const int32_t *type_map, const double *lattice,
+                         const double *frac_pos, int out_dtype, int32_t *list_neigh,
+                         void *image_dr, int32_t *num_neigh, int32_t *err_dev,
+                         void *workspace, size_t workspace_bytes, void *stream);
+
+/* ------------------------------------------------------------------------------------
+ * Environment matrix.  Replaces DP.calculate_Ri (src/model/dp_dp.py:217-302):
+ *   Ri [B,N,S,4] = (Ri_raw - davg[t_i]) / dstd[t_i],  Ri_d [B,N,S,4,3] = -dRi/d(dR) / dstd
+ * davg/dstd [ntypes, S*4] (the model buffers), type_map [N] 0-based model type.
+ * ---------------------------------------------------------------------------------- */
+int matpl_env_mat(int dtype, int batch, int natoms, int nslots, const int32_t *type_map,
+                  const void *image_dr, const void *davg, const void *dstd, double rmin,
+                  double rmax, void *Ri, void *Ri_d, void *stream);
+
+/* ------------------------------------------------------------------------------------
+ * Fused DP se_e2_a energy + force + virial.  Replaces DP.forward + calculate_force_virial
+ * (src/model/dp_dp.py:167-215, 304-530): environment matrix, embedding nets, descriptor
+ * contraction, fitting nets, the adjoint dE/dRi and the force / virial scatter, with the
+ * environment matrix and all network activations kept on chip.
+ *
+ * Compiled network shape: embedding 1->25->25->25 (tanh, residual on equal widths),
+ * M2 = 16, fitting 400->50->50->50->1 (tanh, residual layers 2-3).
+ * params: device buffer in matpl_dp_pack_layout order (see matpl_gb300/dp.py: pack_params),
+ * in the compute dtype (f64 for MATPL_F64, f32 for MATPL_F32 and MATPL_MIXED).
+ * ---------------------------------------------------------------------------------- */
+typedef struct {
+    int ntypes;             /* model types */
+    int m;                  /* maxNeighborNum (slots per neighbor type) */
+    int npresent;           /* number of image types (type_nums of dp_dp.py:197) */
+    int present[8];         /* model type index of each image type, in image order */
+    double rmin, rmax;      /* Rmin, Rmax (config Rm, Rc_M) */
+    const void *params;     /* packed network parameters (device) */
+    const void *davg;       /* [ntypes,4] per centre type (device, compute dtype) */
+    const void *dstd;       /* [ntypes,4] */
+} matpl_dp_model;
+
+size_t matpl_dp_param_count(int ntypes);
+size_t matpl_dp_workspace_bytes(int dtype, int batch, int natoms);
+
+/* type_map [N]: model type index of each atom (atoms whose type is not in present[] get
+ * Ei = 0 and contribute nothing, like dp_dp.py:304-342).  list_neigh [B,N,S] int32 1-based,
+ * 0 = empty; image_dr [B,N,S,4] in the compute dtype (f32 for MIXED).
+ * Outputs: Ei [B,N] (atom order, compute dtype), Etot [B] f64, force [B,N+nghost,3]
+ * (compute dtype), virial [B,9] f64 with virial[a*3+c] = sum f_a * Rij_c. */
+int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, int natoms, int nslots,
+                  int nghost, const int32_t *list_neigh, const void *image_dr,
+                  const int32_t *type_map, void *Ei, double *Etot, void *force, double *virial,
+                  void *workspace, size_t workspace_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MATPL_GB300_H */

@@ -1,0 +1,82 @@
+"""ctypes binding of ``libmatpl_gb300.so`` (the C ABI declared in ``include/matpl_gb300.h``).
+
+The library is built in-tree by ``matpl_gb300.build``.  There is no fallback: when the library
+is missing or a call fails, a ``MatplError`` is raised.
+"""
+import ctypes
+import os
+
+from . import build as _build
+
+MATPL_F32, MATPL_F64, MATPL_MIXED = 0, 1, 2
+KERR_NEIGHBOR_OVERFLOW = 1
+KERR_BAD_TYPE = 2
+
+_c = ctypes
+_vp, _i, _d, _sz = _c.c_void_p, _c.c_int, _c.c_double, _c.c_size_t
+
+
+class MatplDpModel(ctypes.Structure):
+    """Mirror of ``matpl_dp_model``."""
+    _fields_ = [("ntypes", _i), ("m", _i), ("npresent", _i), ("present", _i * 8),
+                ("rmin", _d), ("rmax", _d), ("params", _vp), ("davg", _vp), ("dstd", _vp)]
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "matpl_last_error": (_c.c_char_p, []),
+    "matpl_version": (_i, []),
+    "matpl_calc_force": (_i, [_i, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp, _vp]),
+    "matpl_calc_virial": (_i, [_i, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp, _vp, _vp]),
+    "matpl_calc_force_grad": (_i, [_i, _vp, _vp, _vp, _i, _i, _i, _i, _vp, _vp]),
+    "matpl_calc_virial_grad": (_i, [_i, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp]),
+    "matpl_neighbor_workspace_bytes": (_sz, [_i, _i]),
+    "matpl_neighbor_build": (_i, [_i, _i, _i, _i, _d, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp,
+                                  _vp, _vp, _sz, _vp]),
+    "matpl_env_mat": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _d, _d, _vp, _vp, _vp]),
+    "matpl_dp_param_count": (_sz, [_i]),
+    "matpl_dp_workspace_bytes": (_sz, [_i, _i, _i]),
+    "matpl_dp_eval": (_i, [_i, _c.POINTER(MatplDpModel), _i, _i, _i, _i, _vp, _vp, _vp, _vp,
+                           _vp, _vp, _vp, _vp, _sz, _vp]),
+}
+
+
+class MatplError(RuntimeError):
+    pass
+
+
+_LIB = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load (building first if needed) the native library and bind every entry point."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if build_if_missing:
+        path = _build.build()
+    if not os.path.exists(path):
+        raise MatplError(f"native library not built: {path} (run matpl_gb300.build.build())")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def check(status: int, what: str):
+    if status != 0:
+        msg = load().matpl_last_error().decode(errors="replace")
+        raise MatplError(f"{what} failed (status {status}): {msg}")
+
+
+def ptr(t) -> int:
+    """Device pointer of a torch tensor (None -> NULL)."""
+    return 0 if t is None else t.data_ptr()

@@ -1,0 +1,48 @@
+// Shared helpers for the matpl_gb300 kernels (sm_103a only).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include "../../include/matpl_gb300.h"
+
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ < 1000)
+#error "matpl_gb300 is built for sm_103a (GB300) only"
+#endif
+
+namespace matpl {
+
+void set_error(const std::string &msg);
+
+#define MATPL_REQUIRE(cond, code, msg)                 \
+    do {                                               \
+        if (!(cond)) {                                 \
+            ::matpl::set_error(msg);                   \
+            return (code);                             \
+        }                                              \
+    } while (0)
+
+inline int check_launch(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error(std::string(what) + ": " + cudaGetErrorString(e));
+        return MATPL_ERR_CUDA;
+    }
+    return MATPL_OK;
+}
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Device math wrappers: the plain forms use CUDA's correctly-rounded-library tanh.
+__device__ __forceinline__ float dev_tanh(float x) { return tanhf(x); }
+__device__ __forceinline__ double dev_tanh(double x) { return tanh(x); }
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace matpl

@@ -1,0 +1,518 @@
+// DP neighbor search and environment matrix.
+//
+// Semantics: src/pre_data/gen_feature/NeighConst.f90:14-149 (find_neighbore), applied to
+// each image on its own (MatPL's loader always calls it with images = 1,
+// dpuni_data_loader.py:619), then the r column of compute_Ri (dpuni_data_loader.py:669-673).
+//
+//  * Per-type slot blocks of m slots, filled in ascending neighbor index j and, for small
+//    cells (any |a_v| < 2 Rc), in the Fortran image order (i1, i2, i3) inside each j.
+//  * Cells with all |a_v| >= 2 Rc use the per-component nearest-image rule of
+//    NeighConst.f90:98-108.  Candidates come from a cell list whose bins (in fractional
+//    coordinates) are at least Rc/h_k wide (h_k = cell thickness along reciprocal direction
+//    k), so every pair within Rc under that rule sits in one of the 27 (or fewer, distinct)
+//    adjacent bins.  The candidate order does not matter: the warp rank-sorts the accepted
+//    neighbors by (j, image) to reproduce the Fortran slot order exactly.
+//  * All pair arithmetic is evaluated in the Fortran source order with explicit
+//    round-to-nearest intrinsics (no FMA contraction), so dR and the accept / reject
+//    decisions are bit-identical to the restatement in plain C.
+#include "common.cuh"
+
+namespace matpl {
+namespace {
+
+constexpr int kWarps = 4;
+constexpr int kMaxTypes = 16;
+
+struct NbImage {
+    double L[9];
+    int iflag;       // 1: enumerate periodic images (NeighConst.f90:55-92)
+    int nper[3];     // nperiod (NeighConst.f90:42)
+    int nb[3];       // cell bins per fractional axis (minimum-image branch)
+    int ncells;
+};
+
+struct NbParams {
+    int batch, natoms, ntypes, m;
+    double rc2;                    // Rc_M**2
+    double rct2[kMaxTypes];        // Rc_type(t)**2
+    int cell_cap;                  // cell capacity per image
+};
+
+__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
+
+__device__ __forceinline__ void mic(double &d) {
+    if (fabs(da(d, 1.0)) < fabs(d)) d = da(d, 1.0);
+    if (fabs(da(d, -1.0)) < fabs(d)) d = da(d, -1.0);
+}
+
+__device__ __forceinline__ void cart(const double *L, double d1, double d2, double d3, double &x,
+                                     double &y, double &z, double &dd) {
+    x = da(da(dm(L[0], d1), dm(L[3], d2)), dm(L[6], d3));
+    y = da(da(dm(L[1], d1), dm(L[4], d2)), dm(L[7], d3));
+    z = da(da(dm(L[2], d1), dm(L[5], d2)), dm(L[8], d3));
+    dd = da(da(dm(x, x), dm(y, y)), dm(z, z));
+}
+
+__global__ void nb_setup(const double *__restrict__ lattice, NbImage *__restrict__ img,
+                         int batch, double Rc, int cell_cap) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < batch; b += gridDim.x * blockDim.x) {
+        NbImage im;
+        const double *L = lattice + 9 * b;
+        for (int q = 0; q < 9; ++q) im.L[q] = L[q];
+        im.iflag = 0;
+        for (int v = 0; v < 3; ++v) {
+            double d = sqrt(da(da(dm(L[3 * v], L[3 * v]), dm(L[3 * v + 1], L[3 * v + 1])),
+                               dm(L[3 * v + 2], L[3 * v + 2])));
+            im.nper[v] = (int)(Rc / d) + 1;
+            if (d < 2 * Rc) im.iflag = 1;
+        }
+        // thickness h_k = V / |a_i x a_j|
+        const double *a = L, *bb = L + 3, *c = L + 6;
+        double cr[3][3];
+        const double *vv[3][2] = {{bb, c}, {c, a}, {a, bb}};
+        for (int k = 0; k < 3; ++k) {
+            const double *p = vv[k][0], *q = vv[k][1];
+            cr[k][0] = p[1] * q[2] - p[2] * q[1];
+            cr[k][1] = p[2] * q[0] - p[0] * q[2];
+            cr[k][2] = p[0] * q[1] - p[1] * q[0];
+        }
+        const double V = fabs(a[0] * cr[0][0] + a[1] * cr[0][1] + a[2] * cr[0][2]);
+        long long prod = 1;
+        for (int k = 0; k < 3; ++k) {
+            double area = sqrt(cr[k][0] * cr[k][0] + cr[k][1] * cr[k][1] + cr[k][2] * cr[k][2]);
+            double h = V / area;
+            int n = (int)floor(h / (Rc * 1.0000001));
+            im.nb[k] = n < 1 ? 1 : (n > 1024 ? 1024 : n);
+        }
+        for (;;) {
+            prod = (long long)im.nb[0] * im.nb[1] * im.nb[2];
+            if (prod <= cell_cap) break;
+            int kmax = 0;
+            for (int k = 1; k < 3; ++k)
+                if (im.nb[k] > im.nb[kmax]) kmax = k;
+            im.nb[kmax] = (im.nb[kmax] + 1) / 2;
+        }
+        im.ncells = im.iflag ? 0 : (int)prod;
+        img[b] = im;
+    }
+}
+
+__global__ void nb_bin(const double *__restrict__ frac, const NbImage *__restrict__ img,
+                       double *__restrict__ wpos, int *__restrict__ cell_of,
+                       int *__restrict__ cell_count, NbParams P) {
+    const long long total = (long long)P.batch * P.natoms;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int b = (int)(t / P.natoms);
+        double f[3];
+        for (int k = 0; k < 3; ++k) {
+            f[k] = fmod(da(frac[3 * t + k], 10.0), 1.0);   // NeighConst.f90:46-50
+            wpos[3 * t + k] = f[k];
+        }
+        const NbImage &im = img[b];
+        if (im.iflag) {
+            cell_of[t] = -1;
+            continue;
+        }
+        int c[3];
+        for (int k = 0; k < 3; ++k) {
+            int q = (int)(f[k] * im.nb[k]);
+            c[k] = q >= im.nb[k] ? im.nb[k] - 1 : (q < 0 ? 0 : q);
+        }
+        const int cell = (c[0] * im.nb[1] + c[1]) * im.nb[2] + c[2];
+        cell_of[t] = cell;
+        atomicAdd(cell_count + (long long)b * P.cell_cap + cell, 1);
+    }
+}
+
+// Exclusive scan of cell counts, one block per image.
+__global__ void nb_scan(const NbImage *__restrict__ img, const int *__restrict__ cell_count,
+                        int *__restrict__ cell_start, NbParams P) {
+    const int b = blockIdx.x;
+    const int n = img[b].ncells;
+    const int *cnt = cell_count + (long long)b * P.cell_cap;
+    int *st = cell_start + (long long)b * (P.cell_cap + 1);
+    __shared__ int wsum[32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += blockDim.x) {
+        const int i = base + threadIdx.x;
+        int v = i < n ? cnt[i] : 0;
+        int x = v;
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            int s = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += y;
+            }
+            wsum[lane] = s;
+        }
+        __syncthreads();
+        const int excl = carry + x - v + (w > 0 ? wsum[w - 1] : 0);
+        if (i < n) st[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) st[n] = carry;
+}
+
+__global__ void nb_fill(const int *__restrict__ cell_of, const int *__restrict__ cell_start,
+                        int *__restrict__ cell_fill, int *__restrict__ cell_atoms, NbParams P) {
+    const long long total = (long long)P.batch * P.natoms;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int cell = cell_of[t];
+        if (cell < 0) continue;
+        const int b = (int)(t / P.natoms);
+        const int pos = atomicAdd(cell_fill + (long long)b * P.cell_cap + cell, 1);
+        cell_atoms[(long long)b * P.natoms + cell_start[(long long)b * (P.cell_cap + 1) + cell] +
+                   pos] = (int)(t - (long long)b * P.natoms);
+    }
+}
+
+template <typename TO>
+__global__ void __launch_bounds__(kWarps * 32)
+nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
+          const int32_t *__restrict__ type_map, const int *__restrict__ cell_start,
+          const int *__restrict__ cell_atoms, int32_t *__restrict__ list_neigh,
+          TO *__restrict__ image_dr, int32_t *__restrict__ num_neigh, int32_t *__restrict__ err,
+          NbParams P) {
+    extern __shared__ unsigned char smem_raw[];
+    const int S = P.ntypes * P.m;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int *keys = reinterpret_cast<int *>(smem_raw) + warp * S;
+    unsigned char *ktype =
+        reinterpret_cast<unsigned char *>(reinterpret_cast<int *>(smem_raw) + kWarps * S) +
+        warp * S;
+    const long long total = (long long)P.batch * P.natoms;
+    for (long long t = (long long)blockIdx.x * kWarps + warp; t < total;
+         t += (long long)gridDim.x * kWarps) {
+        const int b = (int)(t / P.natoms);
+        const int i = (int)(t - (long long)b * P.natoms);
+        const NbImage &im = img[b];
+        const double *pos = wpos + (long long)b * P.natoms * 3;
+        const double pi0 = pos[3 * i], pi1 = pos[3 * i + 1], pi2 = pos[3 * i + 2];
+        const int ti = type_map[i];
+        if (ti < 0 || ti >= P.ntypes) {
+            if (lane == 0) atomicMax(err, MATPL_KERR_BAD_TYPE);
+            continue;
+        }
+        const double rct2 = P.rct2[ti];
+        int n_acc = 0;                       // accepted (within Rc_type) entries in keys[]
+        int cntM[kMaxTypes];                 // within Rc_M, per type (overflow test)
+        for (int q = 0; q < P.ntypes; ++q) cntM[q] = 0;
+        bool overflow = false;
+        const int nimg1 = 2 * im.nper[2] + 1, nimg2 = 2 * im.nper[1] + 1;
+        const int nimg = im.iflag ? (2 * im.nper[0] + 1) * nimg2 * nimg1 : 1;
+
+        auto consider = [&](bool valid, int j, int img_idx, double d1, double d2, double d3) {
+            double x, y, z, dd;
+            cart(im.L, d1, d2, d3, x, y, z, dd);
+            const bool inM = valid && dd < P.rc2 && dd > 1.0e-8;
+            const bool inT = inM && dd < rct2;
+            const int tj = valid ? type_map[j] : 0;
+            if (valid && (tj < 0 || tj >= P.ntypes)) atomicMax(err, MATPL_KERR_BAD_TYPE);
+            for (int q = 0; q < P.ntypes; ++q) {
+                const unsigned mq = __ballot_sync(0xffffffffu, inM && tj == q);
+                cntM[q] += __popc(mq);
+            }
+            const unsigned ma = __ballot_sync(0xffffffffu, inT);
+            const int at = n_acc + __popc(ma & ((1u << lane) - 1u));
+            if (inT && at < S) {
+                keys[at] = j * nimg + img_idx;
+                ktype[at] = (unsigned char)tj;
+            }
+            n_acc += __popc(ma);
+        };
+
+        if (im.iflag) {
+            for (int j0 = 0; j0 < P.natoms; j0 += 32) {
+                const int j = j0 + lane;
+                const bool valid = j < P.natoms;
+                const double pj0 = valid ? pos[3 * j] : 0.0, pj1 = valid ? pos[3 * j + 1] : 0.0,
+                             pj2 = valid ? pos[3 * j + 2] : 0.0;
+                int idx = 0;
+                for (int i1 = -im.nper[0]; i1 <= im.nper[0]; ++i1)
+                    for (int i2 = -im.nper[1]; i2 <= im.nper[1]; ++i2)
+                        for (int i3 = -im.nper[2]; i3 <= im.nper[2]; ++i3, ++idx) {
+                            const double d1 = da(da(pj0, -pi0), (double)i1);
+                            const double d2 = da(da(pj1, -pi1), (double)i2);
+                            const double d3 = da(da(pj2, -pi2), (double)i3);
+                            consider(valid, j, idx, d1, d2, d3);
+                        }
+            }
+        } else {
+            int ci[3];
+            for (int k = 0; k < 3; ++k) {
+                const double f = k == 0 ? pi0 : (k == 1 ? pi1 : pi2);
+                int q = (int)(f * im.nb[k]);
+                ci[k] = q >= im.nb[k] ? im.nb[k] - 1 : (q < 0 ? 0 : q);
+            }
+            int noff[3], off0[3];
+            for (int k = 0; k < 3; ++k) {
+                noff[k] = im.nb[k] >= 3 ? 3 : im.nb[k];
+                off0[k] = im.nb[k] >= 3 ? -1 : 0;
+            }
+            const int *cs = cell_start + (long long)b * (P.cell_cap + 1);
+            const int *ca = cell_atoms + (long long)b * P.natoms;
+            for (int ox = 0; ox < noff[0]; ++ox)
+                for (int oy = 0; oy < noff[1]; ++oy)
+                    for (int oz = 0; oz < noff[2]; ++oz) {
+                        const int cx = (ci[0] + off0[0] + ox + im.nb[0]) % im.nb[0];
+                        const int cy = (ci[1] + off0[1] + oy + im.nb[1]) % im.nb[1];
+                        const int cz = (ci[2] + off0[2] + oz + im.nb[2]) % im.nb[2];
+                        const int cell = (cx * im.nb[1] + cy) * im.nb[2] + cz;
+                        const int s0 = cs[cell], s1 = cs[cell + 1];
+                        for (int p = s0; p < s1; p += 32) {
+                            const bool valid = p + lane < s1;
+                            const int j = valid ? ca[p + lane] : 0;
+                            double d1 = 0, d2 = 0, d3 = 0;
+                            if (valid) {
+                                d1 = da(pos[3 * j], -pi0); mic(d1);
+                                d2 = da(pos[3 * j + 1], -pi1); mic(d2);
+                                d3 = da(pos[3 * j + 2], -pi2); mic(d3);
+                            }
+                            consider(valid, j, 0, d1, d2, d3);
+                        }
+                    }
+        }
+        for (int q = 0; q < P.ntypes; ++q) overflow |= cntM[q] > P.m;
+        if (overflow && lane == 0) atomicMax(err, MATPL_KERR_NEIGHBOR_OVERFLOW);
+        const int nst = n_acc < S ? n_acc : S;
+        __syncwarp();
+        // per-type accepted counts (capped at m)
+        int ncount[kMaxTypes];
+        for (int q = 0; q < P.ntypes; ++q) {
+            int c = 0;
+            for (int e = lane; e < nst; e += 32) c += ktype[e] == q;
+            c = warp_sum(c);
+            ncount[q] = c < P.m ? c : P.m;
+        }
+        const long long row = t * (long long)S;
+        // rank sort by key within each type block, write the accepted slots
+        for (int e = lane; e < nst; e += 32) {
+            const int key = keys[e];
+            const int ty = ktype[e];
+            int rank = 0;
+            for (int f = 0; f < nst; ++f) rank += (ktype[f] == ty) & (keys[f] < key);
+            if (rank >= P.m) continue;
+            const int j = key / nimg, idx = key - j * nimg;
+            double d1, d2, d3;
+            if (im.iflag) {
+                const int i3 = idx % nimg1 - im.nper[2];
+                const int i2 = (idx / nimg1) % nimg2 - im.nper[1];
+                const int i1 = idx / (nimg1 * nimg2) - im.nper[0];
+                d1 = da(da(pos[3 * j], -pi0), (double)i1);
+                d2 = da(da(pos[3 * j + 1], -pi1), (double)i2);
+                d3 = da(da(pos[3 * j + 2], -pi2), (double)i3);
+            } else {
+                d1 = da(pos[3 * j], -pi0); mic(d1);
+                d2 = da(pos[3 * j + 1], -pi1); mic(d2);
+                d3 = da(pos[3 * j + 2], -pi2); mic(d3);
+            }
+            double x, y, z, dd;
+            cart(im.L, d1, d2, d3, x, y, z, dd);
+            const long long slot = row + (long long)ty * P.m + rank;
+            list_neigh[slot] = j + 1;
+            image_dr[4 * slot + 0] = (TO)__dsqrt_rn(dd);
+            image_dr[4 * slot + 1] = (TO)x;
+            image_dr[4 * slot + 2] = (TO)y;
+            image_dr[4 * slot + 3] = (TO)z;
+        }
+        // clear the remaining slots
+        for (int s = lane; s < S; s += 32) {
+            const int ty = s / P.m;
+            if (s - ty * P.m < ncount[ty]) continue;
+            list_neigh[row + s] = 0;
+            image_dr[4 * (row + s) + 0] = TO(0);
+            image_dr[4 * (row + s) + 1] = TO(0);
+            image_dr[4 * (row + s) + 2] = TO(0);
+            image_dr[4 * (row + s) + 3] = TO(0);
+        }
+        if (num_neigh != nullptr && lane < P.ntypes) {
+            int c = 0;
+            for (int q = 0; q < P.ntypes; ++q)
+                if (q == lane) c = ncount[q];
+            num_neigh[t * P.ntypes + lane] = c;
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Environment matrix (dp_dp.py:217-302).  One thread per slot.
+template <typename T>
+__global__ void env_mat_kernel(const int32_t *__restrict__ type_map, const T *__restrict__ idr,
+                               const T *__restrict__ davg, const T *__restrict__ dstd, T rmin,
+                               T rmax, T *__restrict__ Ri, T *__restrict__ Rid, int batch,
+                               int natoms, int nslots) {
+    const long long total = (long long)batch * natoms * nslots;
+    for (long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x; s < total;
+         s += (long long)gridDim.x * blockDim.x) {
+        const long long bi = s / nslots;
+        const int i = (int)(bi % natoms);
+        const int k = (int)(s - bi * nslots);
+        const int ti = type_map[i];
+        const T R = idr[4 * s], x = idr[4 * s + 1], y = idr[4 * s + 2], z = idr[4 * s + 3];
+        T sr = 0, ds = 0;
+        if (R > 0 && R < rmin) {
+            sr = T(1) / R;
+            ds = -T(1) / (R * R);
+        } else if (R > rmin && R < rmax) {
+            const T u = (R - rmin) / (rmax - rmin);
+            const T poly = u * u * u * (T(-6) * u * u + T(15) * u - T(10)) + T(1);
+            const T dpoly = (T(3) * u * u * (T(-6) * u * u + T(15) * u - T(10)) +
+                             u * u * u * (T(-12) * u + T(15))) / (rmax - rmin);
+            sr = poly / R;
+            ds = dpoly / R - poly / (R * R);
+        }
+        const bool mask = fabs((double)R) > 1e-5;
+        const T *av = davg + ((long long)ti * nslots + k) * 4;
+        const T *sd = dstd + ((long long)ti * nslots + k) * 4;
+        const T raw[4] = {sr, mask ? sr * x / R : T(0), mask ? sr * y / R : T(0),
+                          mask ? sr * z / R : T(0)};
+        for (int c = 0; c < 4; ++c) Ri[4 * s + c] = (raw[c] - av[c]) / sd[c];
+        T d[4][3];
+        const T xyz[3] = {x, y, z};
+        const T common = mask ? (ds - sr / R) / (R * R) : T(0);
+        for (int bcol = 0; bcol < 3; ++bcol) {
+            d[0][bcol] = mask ? ds * xyz[bcol] / R : T(0);
+            for (int a = 0; a < 3; ++a) {
+                T v = common * xyz[a] * xyz[bcol];
+                if (a == bcol) v += mask ? sr / R : T(0);
+                d[a + 1][bcol] = mask ? v : T(0);
+            }
+        }
+        for (int c = 0; c < 4; ++c)
+            for (int bcol = 0; bcol < 3; ++bcol) Rid[12 * s + 3 * c + bcol] = -d[c][bcol] / sd[c];
+    }
+}
+
+struct NbLayout {
+    size_t img, wpos, cell_of, cell_count, cell_fill, cell_start, cell_atoms, total;
+};
+
+NbLayout nb_layout(int batch, int natoms) {
+    NbLayout l;
+    const size_t cap = (size_t)natoms + 27;
+    size_t o = 0;
+    l.img = o;        o = align_up(o + sizeof(NbImage) * batch, 256);
+    l.wpos = o;       o = align_up(o + 8 * 3 * (size_t)batch * natoms, 256);
+    l.cell_of = o;    o = align_up(o + 4 * (size_t)batch * natoms, 256);
+    l.cell_count = o; o = align_up(o + 4 * cap * batch, 256);
+    l.cell_fill = o;  o = align_up(o + 4 * cap * batch, 256);
+    l.cell_start = o; o = align_up(o + 4 * (cap + 1) * batch, 256);
+    l.cell_atoms = o; o = align_up(o + 4 * (size_t)batch * natoms, 256);
+    l.total = o;
+    return l;
+}
+
+inline int grid_for(long long work, int per_block) {
+    long long g = (work + per_block - 1) / per_block;
+    if (g > 152LL * 32) g = 152LL * 32;
+    return (int)(g < 1 ? 1 : g);
+}
+
+}  // namespace
+}  // namespace matpl
+
+using namespace matpl;
+
+extern "C" size_t matpl_neighbor_workspace_bytes(int batch, int natoms) {
+    if (batch < 0 || natoms < 0) return 0;
+    return nb_layout(batch, natoms).total;
+}
+
+extern "C" int matpl_neighbor_build(int batch, int natoms, int ntypes, int m_neigh, double Rc_M,
+                                    const double *Rc_type, const int32_t *type_map,
+                                    const double *lattice, const double *frac_pos, int out_dtype,
+                                    int32_t *list_neigh, void *image_dr, int32_t *num_neigh,
+                                    int32_t *err_dev, void *workspace, size_t workspace_bytes,
+                                    void *stream) {
+    MATPL_REQUIRE(batch >= 0 && natoms >= 0, MATPL_ERR_INVALID, "negative size");
+    MATPL_REQUIRE(ntypes >= 1 && ntypes <= kMaxTypes, MATPL_ERR_UNSUPPORTED,
+                  "ntypes must be in [1, 16]");
+    MATPL_REQUIRE(m_neigh >= 1, MATPL_ERR_INVALID, "m_neigh must be >= 1");
+    MATPL_REQUIRE((long long)ntypes * m_neigh <= 2048, MATPL_ERR_UNSUPPORTED,
+                  "ntypes * m_neigh must be <= 2048");
+    MATPL_REQUIRE(Rc_M > 0 && Rc_type != nullptr, MATPL_ERR_INVALID, "bad cutoff");
+    MATPL_REQUIRE(out_dtype == MATPL_F32 || out_dtype == MATPL_F64, MATPL_ERR_DTYPE,
+                  "image_dr dtype must be f32 or f64");
+    MATPL_REQUIRE(err_dev != nullptr, MATPL_ERR_INVALID, "err_dev is required");
+    const NbLayout lay = nb_layout(batch, natoms);
+    MATPL_REQUIRE(workspace != nullptr && workspace_bytes >= lay.total, MATPL_ERR_WORKSPACE,
+                  "neighbor workspace too small");
+    if (batch == 0 || natoms == 0) return MATPL_OK;
+    // key = j * nimages + image must fit in int32; nimages <= (2*(int(Rc/|a|)+1)+1)^3
+    cudaStream_t s = as_stream(stream);
+    NbParams P;
+    P.batch = batch; P.natoms = natoms; P.ntypes = ntypes; P.m = m_neigh;
+    P.rc2 = Rc_M * Rc_M;
+    for (int q = 0; q < kMaxTypes; ++q) P.rct2[q] = q < ntypes ? Rc_type[q] * Rc_type[q] : 0.0;
+    P.cell_cap = natoms + 27;
+    char *ws = static_cast<char *>(workspace);
+    NbImage *img = reinterpret_cast<NbImage *>(ws + lay.img);
+    double *wpos = reinterpret_cast<double *>(ws + lay.wpos);
+    int *cell_of = reinterpret_cast<int *>(ws + lay.cell_of);
+    int *cell_count = reinterpret_cast<int *>(ws + lay.cell_count);
+    int *cell_fill = reinterpret_cast<int *>(ws + lay.cell_fill);
+    int *cell_start = reinterpret_cast<int *>(ws + lay.cell_start);
+    int *cell_atoms = reinterpret_cast<int *>(ws + lay.cell_atoms);
+    if (cudaMemsetAsync(ws + lay.cell_count, 0, lay.cell_start - lay.cell_count, s) !=
+        cudaSuccess) {
+        set_error("matpl_neighbor_build: memset failed");
+        return MATPL_ERR_CUDA;
+    }
+    const long long na = (long long)batch * natoms;
+    nb_setup<<<(batch + 127) / 128, 128, 0, s>>>(lattice, img, batch, Rc_M, P.cell_cap);
+    nb_bin<<<grid_for(na, 256), 256, 0, s>>>(frac_pos, img, wpos, cell_of, cell_count, P);
+    nb_scan<<<batch, 1024, 0, s>>>(img, cell_count, cell_start, P);
+    nb_fill<<<grid_for(na, 256), 256, 0, s>>>(cell_of, cell_start, cell_fill, cell_atoms, P);
+    const int S = ntypes * m_neigh;
+    const size_t smem = (size_t)kWarps * S * 5;
+    if (out_dtype == MATPL_F64) {
+        cudaFuncSetAttribute(nb_search<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        nb_search<double><<<grid_for(na, kWarps), kWarps * 32, smem, s>>>(
+            img, wpos, type_map, cell_start, cell_atoms, list_neigh, (double *)image_dr,
+            num_neigh, err_dev, P);
+    } else {
+        cudaFuncSetAttribute(nb_search<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        nb_search<float><<<grid_for(na, kWarps), kWarps * 32, smem, s>>>(
+            img, wpos, type_map, cell_start, cell_atoms, list_neigh, (float *)image_dr,
+            num_neigh, err_dev, P);
+    }
+    return check_launch("matpl_neighbor_build");
+}
+
+extern "C" int matpl_env_mat(int dtype, int batch, int natoms, int nslots,
+                             const int32_t *type_map, const void *image_dr, const void *davg,
+                             const void *dstd, double rmin, double rmax, void *Ri, void *Ri_d,
+                             void *stream) {
+    MATPL_REQUIRE(dtype == MATPL_F32 || dtype == MATPL_F64, MATPL_ERR_DTYPE,
+                  "env_mat supports f32 and f64");
+    MATPL_REQUIRE(batch >= 0 && natoms >= 0 && nslots >= 0, MATPL_ERR_INVALID, "negative size");
+    const long long total = (long long)batch * natoms * nslots;
+    if (total == 0) return MATPL_OK;
+    cudaStream_t s = as_stream(stream);
+    if (dtype == MATPL_F64)
+        env_mat_kernel<double><<<grid_for(total, 256), 256, 0, s>>>(
+            type_map, (const double *)image_dr, (const double *)davg, (const double *)dstd, rmin,
+            rmax, (double *)Ri, (double *)Ri_d, batch, natoms, nslots);
+    else
+        env_mat_kernel<float><<<grid_for(total, 256), 256, 0, s>>>(
+            type_map, (const float *)image_dr, (const float *)davg, (const float *)dstd,
+            (float)rmin, (float)rmax, (float *)Ri, (float *)Ri_d, batch, natoms, nslots);
+    return check_launch("matpl_env_mat");
+}

@@ -1,0 +1,201 @@
+"""Drop-in replacements for MatPL's ``CalcOps_cuda`` DP ops and data-path builders.
+
+``calculateForce`` / ``calculateVirial`` keep the reference signatures and return lists like
+``torch.ops.CalcOps_cuda.*`` (src/op/src/CalcOps_bind.cpp:6-16, CalcOps.cpp:6-236) and are
+differentiable w.r.t. ``dE`` exactly like the reference ``autograd::Function``s.  ``find_neighbore``
+mirrors ``src/pre_data/dpuni_data_loader.py:595-650`` on the GPU and ``env_mat`` mirrors
+``DP.calculate_Ri`` (``src/model/dp_dp.py:217-302``).
+
+Every op runs on the current CUDA stream of its inputs' device, goes through the C ABI of
+``libmatpl_gb300.so`` and raises ``MatplError`` on failure; there is no CPU fallback.
+"""
+from typing import List, Optional, Sequence, Tuple, Union
+
+import torch
+
+from . import _lib
+from ._lib import MATPL_F32, MATPL_F64, check, ptr
+
+_DT = {torch.float32: MATPL_F32, torch.float64: MATPL_F64}
+
+
+def _stream(dev: torch.device) -> int:
+    return torch.cuda.current_stream(dev).cuda_stream
+
+
+def _dtype_code(t: torch.Tensor) -> int:
+    if t.dtype not in _DT:
+        raise _lib.MatplError(f"unsupported dtype {t.dtype}; MatPL DP ops take float32/float64")
+    return _DT[t.dtype]
+
+
+def _require_cuda(*ts):
+    for t in ts:
+        if t is not None and not t.is_cuda:
+            raise _lib.MatplError("matpl_gb300 ops take CUDA tensors (no CPU fallback)")
+
+
+def _nghost(n) -> int:
+    return int(n.item()) if isinstance(n, torch.Tensor) else int(n)
+
+
+class _CalculateForce(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, list_neigh, dE, Ri_d, F, nghost: int):
+        B, N = list_neigh.shape[0], list_neigh.shape[1]
+        S = list_neigh[0, 0].numel() if N > 0 else 0
+        nl = list_neigh.contiguous().to(torch.int32)
+        dE_c, Rd = dE.contiguous(), Ri_d.contiguous()
+        out = torch.empty(B, N + nghost, 3, dtype=dE.dtype, device=dE.device)
+        lib = _lib.load()
+        check(lib.matpl_calc_force(_dtype_code(dE), ptr(nl), ptr(dE_c), ptr(Rd),
+                                   ptr(F.contiguous().to(dE.dtype)), B, N, S, nghost, ptr(out),
+                                   _stream(dE.device)), "matpl_calc_force")
+        ctx.save_for_backward(nl, Rd)
+        ctx.meta = (B, N, S, nghost, dE.shape)
+        return out
+
+    @staticmethod
+    def backward(ctx, grad_force):
+        nl, Rd = ctx.saved_tensors
+        B, N, S, nghost, dshape = ctx.meta
+        g = grad_force.contiguous()
+        grad = torch.empty(dshape, dtype=Rd.dtype, device=Rd.device)
+        lib = _lib.load()
+        check(lib.matpl_calc_force_grad(_dtype_code(Rd), ptr(nl), ptr(Rd), ptr(g), B, N, S,
+                                        nghost, ptr(grad), _stream(Rd.device)),
+              "matpl_calc_force_grad")
+        return None, grad, None, None, None
+
+
+class _CalculateVirial(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, list_neigh, dE, Rij, Ri_d, nghost: int):
+        B, N = list_neigh.shape[0], list_neigh.shape[1]
+        S = list_neigh[0, 0].numel() if N > 0 else 0
+        nl = list_neigh.contiguous().to(torch.int32)
+        dE_c, Rj, Rd = dE.contiguous(), Rij.contiguous().to(dE.dtype), Ri_d.contiguous()
+        vir = torch.empty(B, 9, dtype=dE.dtype, device=dE.device)
+        avir = torch.empty(B, N + nghost, 9, dtype=dE.dtype, device=dE.device)
+        lib = _lib.load()
+        check(lib.matpl_calc_virial(_dtype_code(dE), ptr(nl), ptr(dE_c), ptr(Rj), ptr(Rd), B, N,
+                                    S, nghost, ptr(vir), ptr(avir), _stream(dE.device)),
+              "matpl_calc_virial")
+        ctx.save_for_backward(nl, Rj, Rd)
+        ctx.meta = (B, N, S, dE.shape)
+        ctx.mark_non_differentiable(avir)
+        return vir, avir
+
+    @staticmethod
+    def backward(ctx, grad_vir, grad_avir):
+        nl, Rj, Rd = ctx.saved_tensors
+        B, N, S, dshape = ctx.meta
+        grad = torch.empty(dshape, dtype=Rd.dtype, device=Rd.device)
+        g = grad_vir.contiguous() if grad_vir is not None else torch.zeros(
+            B, 9, dtype=Rd.dtype, device=Rd.device)
+        lib = _lib.load()
+        check(lib.matpl_calc_virial_grad(_dtype_code(Rd), ptr(nl), ptr(Rj), ptr(Rd), ptr(g), B, N,
+                                         S, ptr(grad), _stream(Rd.device)),
+              "matpl_calc_virial_grad")
+        return None, grad, None, None, None
+
+
+def calculateForce(list_neigh: torch.Tensor, dE: torch.Tensor, Ri_d: torch.Tensor,
+                   F: torch.Tensor, nghost_tensor) -> List[torch.Tensor]:
+    """``CalcOps_cuda.calculateForce`` (CalcOps.cpp:6-72).
+
+    list_neigh [B,N,1,S] int32 0-based (-1 empty), dE [B,N,1,4S], Ri_d [B,N,4S,3],
+    F [B,N,3] (centre term), nghost 0-d int64 tensor or int -> [force [B,N+nghost,3]]."""
+    _require_cuda(list_neigh, dE, Ri_d, F)
+    return [_CalculateForce.apply(list_neigh, dE, Ri_d, F, _nghost(nghost_tensor))]
+
+
+def calculateVirial(list_neigh: torch.Tensor, dE: torch.Tensor, Rij: torch.Tensor,
+                    Ri_d: torch.Tensor, nghost_tensor) -> List[torch.Tensor]:
+    """``CalcOps_cuda.calculateVirial`` (CalcOps.cpp:170-236) -> [virial [B,9],
+    atom_virial [B,N+nghost,9]], virial[a*3+c] = sum f_a Rij_c."""
+    _require_cuda(list_neigh, dE, Rij, Ri_d)
+    v, av = _CalculateVirial.apply(list_neigh, dE, Rij, Ri_d, _nghost(nghost_tensor))
+    return [v, av]
+
+
+def env_mat(ImageDR: torch.Tensor, Imagetype_map: torch.Tensor, davg: torch.Tensor,
+            dstd: torch.Tensor, Rmin: float, Rmax: float) -> Tuple[torch.Tensor, torch.Tensor]:
+    """``DP.calculate_Ri`` (dp_dp.py:217-302): normalised Ri [B,N,S,4] and Ri_d [B,N,S,4,3]."""
+    _require_cuda(ImageDR, Imagetype_map)
+    B, N, S, _ = ImageDR.shape
+    dt = ImageDR.dtype
+    idr = ImageDR.contiguous()
+    tm = Imagetype_map.to(device=ImageDR.device, dtype=torch.int32).contiguous()
+    av = davg.to(device=ImageDR.device, dtype=dt).contiguous()
+    sd = dstd.to(device=ImageDR.device, dtype=dt).contiguous()
+    Ri = torch.empty(B, N, S, 4, dtype=dt, device=ImageDR.device)
+    Rid = torch.empty(B, N, S, 4, 3, dtype=dt, device=ImageDR.device)
+    lib = _lib.load()
+    check(lib.matpl_env_mat(_dtype_code(ImageDR), B, N, S, ptr(tm), ptr(idr), ptr(av), ptr(sd),
+                            float(Rmin), float(Rmax), ptr(Ri), ptr(Rid), _stream(ImageDR.device)),
+          "matpl_env_mat")
+    return Ri, Rid
+
+
+class NeighborOverflow(_lib.MatplError):
+    """A type block needs more than maxNeighborNum slots (NeighConst.f90:75-78)."""
+
+
+_ws_cache = {}
+
+
+def workspace(device: torch.device, nbytes: int, tag: str) -> torch.Tensor:
+    """Grow-only per-device scratch buffer (the C ABI itself never allocates)."""
+    key = (str(device), tag)
+    buf = _ws_cache.get(key)
+    if buf is None or buf.numel() < nbytes:
+        buf = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=device)
+        _ws_cache[key] = buf
+    return buf
+
+
+def find_neighbore(type_maps: torch.Tensor, frac_position: torch.Tensor, lattice: torch.Tensor,
+                   ntypes: int, m_neigh: int, Rc_M: float, Rc_type: Union[float, Sequence[float]],
+                   out_dtype: torch.dtype = torch.float64, with_counts: bool = False,
+                   check_overflow: bool = True):
+    """GPU DP neighbor search (dpuni_data_loader.py:595-650 + compute_Ri's r column).
+
+    type_maps [N] 0-based types; frac_position [B,N,3] (or [N,3]) f64 fractional; lattice
+    [B,3,3] (or [3,3]) f64 row vectors.  Returns list_neigh [B,N,ntypes*m] int32 (1-based,
+    0 = empty) and ImageDR [B,N,ntypes*m,4] = (r, dx, dy, dz) (plus num_neigh [B,N,ntypes]
+    when ``with_counts``).  Raises NeighborOverflow like the Fortran "stop" when
+    ``check_overflow`` (that reads one device flag and synchronises the stream)."""
+    _require_cuda(frac_position)
+    dev = frac_position.device
+    pos = frac_position.to(torch.float64)
+    N = type_maps.shape[0]
+    pos = pos.reshape(-1, N, 3).contiguous()
+    B = pos.shape[0]
+    lat = lattice.to(device=dev, dtype=torch.float64).reshape(B, 3, 3).contiguous()
+    tm = type_maps.to(device=dev, dtype=torch.int32).contiguous()
+    rct = [float(Rc_type)] * ntypes if isinstance(Rc_type, (int, float)) else [float(x) for x in Rc_type]
+    if len(rct) != ntypes:
+        raise _lib.MatplError("Rc_type must have ntypes entries")
+    import ctypes
+    rct_c = (ctypes.c_double * ntypes)(*rct)
+    S = ntypes * m_neigh
+    ln = torch.empty(B, N, S, dtype=torch.int32, device=dev)
+    idr = torch.empty(B, N, S, 4, dtype=out_dtype, device=dev)
+    cnt = torch.empty(B, N, ntypes, dtype=torch.int32, device=dev) if with_counts else None
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    lib = _lib.load()
+    nbytes = lib.matpl_neighbor_workspace_bytes(B, N)
+    ws = workspace(dev, nbytes, "neighbor")
+    check(lib.matpl_neighbor_build(B, N, ntypes, m_neigh, float(Rc_M), rct_c, ptr(tm), ptr(lat),
+                                   ptr(pos), _DT[out_dtype], ptr(ln), ptr(idr), ptr(cnt), ptr(err),
+                                   ptr(ws), ws.numel(), _stream(dev)), "matpl_neighbor_build")
+    if check_overflow:
+        code = int(err.item())
+        if code == _lib.KERR_NEIGHBOR_OVERFLOW:
+            raise NeighborOverflow(f"Error! maxNeighborNum too small {m_neigh}")
+        if code != 0:
+            raise _lib.MatplError(f"matpl_neighbor_build kernel error {code} (bad atom type)")
+    if with_counts:
+        return ln, idr, cnt
+    return ln, idr

@@ -1,0 +1,84 @@
+"""CPU-side checks of the C ABI: the library builds for sm_103a, loads, and exports every
+function that include/matpl_gb300.h declares; host-side packing logic."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+import torch
+
+from matpl_gb300 import _lib, dp, params as P
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    txt = open(os.path.join(REPO, "include", "matpl_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(matpl_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    names = header_functions()
+    assert len(names) >= 12
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in the header but not exported"
+        assert n in _lib.SIGNATURES, f"{n} has no ctypes signature"
+
+
+def test_version_and_error_string():
+    lib = _lib.load()
+    assert lib.matpl_version() >= 1
+    assert isinstance(lib.matpl_last_error(), bytes)
+
+
+def test_host_side_validation_needs_no_gpu():
+    """Argument errors are caught on the host before any CUDA call."""
+    lib = _lib.load()
+    st = lib.matpl_calc_force(7, None, None, None, None, 1, 1, 1, 0, None, None)
+    assert st == 2  # MATPL_ERR_DTYPE
+    assert b"f32" in lib.matpl_last_error()
+    st = lib.matpl_neighbor_build(1, 4, 1, 10, 6.0, (ctypes.c_double * 1)(6.0), None, None, None,
+                                  0, None, None, None, None, None, 0, None)
+    assert st in (1, 3)  # missing err_dev / workspace
+    m = _lib.MatplDpModel()
+    m.ntypes, m.m, m.npresent = 1, 100, 0
+    st = lib.matpl_dp_eval(1, ctypes.byref(m), 1, 1, 100, 0, None, None, None, None, None, None,
+                           None, None, 0, None)
+    assert st == 1
+
+
+def test_workspace_queries():
+    lib = _lib.load()
+    assert lib.matpl_neighbor_workspace_bytes(1, 32000) > 32000 * 24
+    assert lib.matpl_dp_workspace_bytes(0, 1, 32000) >= 32000 * 100 * 4 * 2
+    assert lib.matpl_dp_param_count(2) == 4 * dp.EMB_SIZE + 2 * dp.FIT_SIZE
+
+
+def test_pack_params_layout_roundtrip():
+    cfg = P.DPConfig(atom_type=[3, 14])
+    prm = P.init_params(cfg, seed=1)
+    flat = dp.pack_params(cfg, prm)
+    assert flat.numel() == _lib.load().matpl_dp_param_count(2)
+    k = 3  # embedding net (1, 1)
+    base = k * dp.EMB_SIZE
+    w1 = flat[base + 2 * dp.E: base + 2 * dp.E + dp.E * dp.E].reshape(dp.E, dp.E)
+    assert torch.equal(w1, prm["embedding_net.3.layers.1.weight"])
+    # no resnet_dt in the embedding -> packed as ones
+    dt1 = flat[base + 3 * dp.E + dp.E * dp.E: base + 4 * dp.E + dp.E * dp.E]
+    assert torch.equal(dt1, torch.ones(dp.E, dtype=torch.float64))
+    fb = 4 * dp.EMB_SIZE + dp.FIT_SIZE   # fitting net 1
+    W0 = prm["fitting_net.1.layers.0.weight"]
+    assert torch.equal(flat[fb:fb + dp.DIN * dp.F].reshape(dp.DIN, dp.F), W0)
+    assert torch.equal(flat[fb + dp.FIT_W0T: fb + dp.FIT_W1T].reshape(dp.F, dp.DIN), W0.t())
+    assert flat[fb + dp.FIT_B3] == prm["fitting_net.1.layers.3.bias"].reshape(-1)[0]
+
+
+def test_per_type_stats_rejects_untiled():
+    cfg = P.DPConfig(atom_type=[29])
+    a = torch.zeros(1, cfg.nslots * 4)
+    a[0, 4] = 1.0
+    with pytest.raises(_lib.MatplError):
+        dp.per_type_stats(a, 1)
