@@ -1,0 +1,339 @@
+"""Benchmark: DP se_e2_a energy + force + virial throughput (atom-steps/s) on GB300.
+
+Workload (the headline configuration): 32,000 atoms, Li:Si 1:1, random-packed periodic cube at
+0.05 atoms/A^3 (minimum pair distance 2.0 A, seeded), Rc = 6.0 A, Rmin = 0.5 A, 150 neighbor
+slots per type (S = 300); embedding 1->25->25->25, M2 = 16, fitting 400->50->50->50->1, random
+weights W ~ N(0, 1/fan_in).  One step = neighbor search from fractional positions + energy,
+forces and virial (what an MD step needs).  Synthetic data: no dataset is involved.
+
+  value : step with inputs resident in HBM (per-step working set ~230 MB > 129 MB L2)
+  e2e   : the same step through the public API with host (pinned) positions copied in and
+          energy / forces / virial copied out every step
+  roofline : the dominant kernel, timed live with CUDA events on its stream
+  cpu_baseline : MatPL's DP algorithm (oracle port of dp_dp_script.DP, torch FP64) on the
+          host cores, on a bounded 4,000-atom sample of the same workload
+
+--impl reference runs only that CPU implementation and prints its line.
+For N > 1 (torchrun) every rank runs its own replica (replicas only, weak scaling).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+NATOMS, DENSITY, M_NEIGH, RC, RMIN = 32000, 0.05, 150, 6.0, 0.5
+ELEMENTS = [3, 14]
+SEED_STRUCT, SEED_W = 2024, 11
+METRIC = "E+F+virial atom-steps/s, mixed vs plain FP32 at force err ≤1e-4 eV/Å"
+CPU_SAMPLE = 4000
+
+# algorithmic FLOPs (no recompute): per occupied pair / per atom, see the design doc
+FLOP_EMB_FWD_PAIR = 2 * (25 + 625 + 625) + 2 * 4 * 25          # 2750
+FLOP_EMB_BWD_PAIR = 2 * 2 * 100 + 2 * (625 + 625 + 25) + 42     # 2992
+FLOP_FIT_ATOM = 2 * 4 * 25 * 16 + 2 * 2 * (400 * 50 + 50 * 50 + 50 * 50 + 50) + 2 * 3200
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.item()
+
+
+def make_workload(natoms=NATOMS, seed=SEED_STRUCT):
+    from matpl_gb300 import params as P, structures
+    st = structures.random_packed(natoms, DENSITY, ELEMENTS, [0.5, 0.5], seed=seed)
+    cfg = P.DPConfig(atom_type=list(ELEMENTS), maxNeighborNum=M_NEIGH, Rmax=RC, Rmin=RMIN)
+    prm = P.init_params(cfg, SEED_W)
+    return st, cfg, prm
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.gpu = gpu_index
+        self.path = os.path.join(HERE, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100", "-i", str(self.gpu)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = [l.split(",") for l in open(self.path).read().splitlines() if l.strip()]
+        sm, mx, pw, reasons = [], None, [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1])); mx = float(r[2]); pw.append(float(r[3]))
+                for k, n in enumerate(names):
+                    if r[5 + k].strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "power_w_max": max(pw) if pw else None, "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def cpu_baseline_run(steps, warmup):
+    """MatPL's DP algorithm on the host cores (oracle port), bounded 4,000-atom sample."""
+    from oracle import dp_oracle, neigh
+    from matpl_gb300 import params as P
+    ncores = os.cpu_count() or 1
+    torch.set_num_threads(ncores)
+    st, cfg, prm = make_workload(CPU_SAMPLE, seed=SEED_STRUCT + 1)
+    ln, idr = neigh.find_neighbore(st.types, st.frac, st.lattice, 2, M_NEIGH, RC, [RC, RC])
+    davg, dstd = P.calc_stat(cfg, ln, idr, st.types)
+    args = (cfg, prm, torch.tensor(davg), torch.tensor(dstd))
+    at = torch.tensor(cfg.atom_type)
+    tm = torch.tensor(st.types)
+
+    def step():
+        l, r = neigh.find_neighbore(st.types, st.frac, st.lattice, 2, M_NEIGH, RC, [RC, RC])
+        out = dp_oracle.dp_eval(*args, torch.tensor(l), tm, at, torch.tensor(r), 0)
+        return out["Etot"].item()
+
+    for _ in range(warmup):
+        step()
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        step()
+        ts.append(time.perf_counter() - t0)
+    med = statistics.median(ts)
+    return {"value": CPU_SAMPLE / med, "unit": "atom-steps/s", "cores": ncores, "kind": "port",
+            "sample": f"{CPU_SAMPLE}-atom Li/Si box of the same density, m=150/type, FP64, "
+                      f"neighbor search + E/F/V per step, median of {steps}",
+            "sec_per_step": med, "steps": steps}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return
+    steps = max(3, min(args.steps, 10))
+    warm = 1
+    cb = cpu_baseline_run(steps, warm)
+    line = {"metric": METRIC, "value": cb["value"], "unit": "atom-steps/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": warm, "ms_per_step": cb["sec_per_step"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"DP se_e2_a Li/Si, {CPU_SAMPLE}-atom sample of the 32k-atom "
+                                   "0.05/A^3 box, m=150/type", "device": "host CPU"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args, ws, rank, local):
+    from matpl_gb300 import _lib, dp, ops, params as P
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    _lib.load()
+    st, cfg, prm = make_workload()
+    prec = args.precision
+    types_d = torch.tensor(st.types, device=dev)
+    frac_d = torch.tensor(st.frac, device=dev)
+    lat_d = torch.tensor(st.lattice, device=dev)
+    ln, idr = ops.find_neighbore(types_d, frac_d, lat_d, 2, M_NEIGH, RC, RC)   # overflow checked
+    n_pairs = int((ln > 0).sum())
+    sub = slice(0, 4000)
+    davg, dstd = P.calc_stat(cfg, ln[:, sub].cpu().numpy(), idr[:, sub].cpu().numpy(), st.types[sub])
+    model = dp.DP(cfg, prm, davg, dstd, precision=prec, device=dev)
+    m64 = dp.DP(cfg, prm, davg, dstd, precision="float64", device=dev)
+    present = model.present_types(cfg.atom_type)
+    tm32 = types_d.to(torch.int32)
+    out_dt = model.dtype
+
+    def step(frac, lat):
+        l, r = ops.find_neighbore(types_d, frac, lat, 2, M_NEIGH, RC, RC, out_dtype=out_dt,
+                                  check_overflow=False)
+        return model.evaluate(l, tm32, present, r, 0)
+
+    # accuracy of this form against the FP64 GPU path (itself checked against the reference)
+    r64 = m64.evaluate(ln, tm32, present, idr, 0)
+    rr = step(frac_d, lat_d)
+    torch.cuda.synchronize()
+    f_rmse = (rr["Force"].double() - r64["Force"]).pow(2).mean().sqrt().item()
+    e_err = abs(rr["Etot"].item() - r64["Etot"].item()) / NATOMS
+    v_err = (rr["Virial"] - r64["Virial"]).abs().max().item()
+
+    # ---- device-resident timed region
+    for _ in range(args.warmup):
+        step(frac_d, lat_d)
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    torch.cuda.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    _lib.profile_begin(max(4096, args.steps * 16))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step(frac_d, lat_d)
+    e1.record()
+    torch.cuda.synchronize()
+    prof = _lib.profile_collect()
+    barrier(ws)
+    ms = e0.elapsed_time(e1) / args.steps
+    clocks = sampler.stop()
+    ms = max_over_ranks(ms, ws)
+    value = ws * NATOMS / (ms * 1e-3)
+
+    # ---- end to end through host buffers
+    frac_h = torch.tensor(st.frac).pin_memory()
+    lat_h = torch.tensor(st.lattice).pin_memory()
+    F_h = torch.empty(1, NATOMS, 3, dtype=out_dt).pin_memory()
+    E_h = torch.empty(1, dtype=torch.float64).pin_memory()
+    V_h = torch.empty(1, 9, dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        f = frac_h.to(dev, non_blocking=True)
+        l = lat_h.to(dev, non_blocking=True)
+        r = step(f, l)
+        F_h.copy_(r["Force"], non_blocking=True)
+        E_h.copy_(r["Etot"], non_blocking=True)
+        V_h.copy_(r["Virial"], non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+    for _ in range(max(3, args.warmup // 2)):
+        e2e_step()
+    e2e_steps = max(10, args.steps // 2)
+    barrier(ws)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    t1 = time.perf_counter()
+    barrier(ws)
+    e2e_ms = max_over_ranks((t1 - t0) * 1e3 / e2e_steps, ws)
+    h2d = frac_h.numel() * 8 + lat_h.numel() * 8
+    d2h = F_h.numel() * F_h.element_size() + 8 + 72
+
+    # ---- roofline of the dominant kernel
+    per_kernel = {k: {"ms_per_launch": v[0] / v[1], "launches": v[1],
+                      "share": None} for k, v in prof.items()}
+    tot = sum(v[0] for v in prof.values())
+    for k, v in prof.items():
+        per_kernel[k]["share"] = v[0] / tot if tot else None
+    dom = max(prof, key=lambda k: prof[k][0]) if prof else None
+    flops = {"dp_embed_bwd": FLOP_EMB_BWD_PAIR * n_pairs, "dp_embed_fwd": FLOP_EMB_FWD_PAIR * n_pairs,
+             "dp_fit": FLOP_FIT_ATOM * NATOMS}
+    peaks = {}
+    pk_path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(pk_path):
+        peaks = json.load(open(pk_path))
+    bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    roof = None
+    if dom in flops:
+        t_launch = per_kernel[dom]["ms_per_launch"] * 1e-3
+        ach = flops[dom] / t_launch / 1e12
+        sm_mhz = clocks.get("sm_mhz") or 2070.0
+        simt_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+        roof = {"kernel": dom, "bound": "tensor", "achieved": ach, "peak": bf16_peak,
+                "unit": "TFLOP/s", "frac": ach / bf16_peak, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks else "fallback",
+                "simt_fp32": {"achieved": ach, "peak_nominal_at_sm_clock": simt_peak,
+                              "frac": ach / simt_peak}}
+        tp = os.path.join(HERE, "profiles", "traffic.json")
+        if os.path.exists(tp):
+            tr = json.load(open(tp)).get(f"{dom}:{prec}")
+            if tr:
+                roof["traffic"] = tr["bytes_per_launch"]
+                roof["traffic_note"] = tr.get("note")
+    launches = sum(v[1] for k, v in prof.items()) + 3 * prof.get("nb_cells", (0, 0))[1]
+
+    cb = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cb = cpu_baseline_run(steps=8, warmup=1)
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": {"float32": "f32", "float64": "f64"}.get(prec, prec), "data": "synthetic",
+            "config": {"workload": "DP se_e2_a, 32,000-atom Li/Si (1:1) random-packed box, "
+                                   "0.05 atoms/A^3, Rc 6.0, m=150/type (S=300), emb 25-25-25, "
+                                   "M2 16, fit 50-50-50-1; step = neighbor search + E/F/V",
+                       "precision_form": prec, "natoms": NATOMS, "pairs": n_pairs,
+                       "parallelism": "replicas" if ws > 1 else "single GPU",
+                       "l2": "no flush: per-step working set ~230 MB (neighbor list + ImageDR) "
+                             "exceeds the 129 MB L2",
+                       "force_rmse_vs_f64_eV_per_A": f_rmse, "energy_err_per_atom_eV": e_err,
+                       "virial_max_abs_err_eV": v_err},
+            "e2e": {"value": ws * NATOMS / (e2e_ms * 1e-3), "unit": "atom-steps/s",
+                    "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "kernels": per_kernel, "roofline": roof,
+            "clocks": clocks, "cpu_baseline": cb}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="float32", choices=["float32", "float64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        ws = int(os.environ.get("WORLD_SIZE", "1"))
+        rank = int(os.environ.get("RANK", "0"))
+        run_reference(args, ws, rank)
+        return
+    ws, rank, local = dist_setup()
+    run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -40,6 +40,14 @@ typedef enum { MATPL_F32 = 0, MATPL_F64 = 1, MATPL_MIXED = 2 } matpl_dtype;
 const char *matpl_last_error(void);
 int matpl_version(void);
 
+/* Per-kernel timing.  After matpl_profile_begin(max_launches), every kernel launch of this
+ * library records a CUDA event pair on its stream (up to max_launches launches).
+ * matpl_profile_collect() waits for those events, switches timing off and returns, per kernel
+ * name (NUL-terminated, name_len bytes each), the summed milliseconds and launch count. */
+int matpl_profile_begin(int max_launches);
+int matpl_profile_collect(int max_names, char *names, int name_len, double *total_ms,
+                          int *launches, int *n_out);
+
 /* ------------------------------------------------------------------------------------
  * Force / virial custom ops.
  * Replaces CalcOps_cuda::calculateForce (src/op/src/CalcOps.cpp:6-22 -> kernel

@@ -26,6 +26,9 @@ class MatplDpModel(ctypes.Structure):
 SIGNATURES = {
     "matpl_last_error": (_c.c_char_p, []),
     "matpl_version": (_i, []),
+    "matpl_profile_begin": (_i, [_i]),
+    "matpl_profile_collect": (_i, [_i, _c.c_char_p, _i, _c.POINTER(_d), _c.POINTER(_i),
+                                   _c.POINTER(_i)]),
     "matpl_calc_force": (_i, [_i, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp, _vp]),
     "matpl_calc_virial": (_i, [_i, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp, _vp, _vp]),
     "matpl_calc_force_grad": (_i, [_i, _vp, _vp, _vp, _i, _i, _i, _i, _vp, _vp]),
@@ -75,6 +78,26 @@ def check(status: int, what: str):
     if status != 0:
         msg = load().matpl_last_error().decode(errors="replace")
         raise MatplError(f"{what} failed (status {status}): {msg}")
+
+
+def profile_begin(max_launches: int = 65536):
+    check(load().matpl_profile_begin(max_launches), "matpl_profile_begin")
+
+
+def profile_collect():
+    """{kernel: (total_ms, launches)} for launches since profile_begin()."""
+    n = 64
+    names = ctypes.create_string_buffer(n * 64)
+    ms = (ctypes.c_double * n)()
+    cnt = (ctypes.c_int * n)()
+    nout = ctypes.c_int()
+    check(load().matpl_profile_collect(n, names, 64, ms, cnt, ctypes.byref(nout)),
+          "matpl_profile_collect")
+    out = {}
+    for k in range(nout.value):
+        nm = names.raw[k * 64:(k + 1) * 64].split(b"\0", 1)[0].decode()
+        out[nm] = (ms[k], cnt[k])
+    return out
 
 
 def ptr(t) -> int:

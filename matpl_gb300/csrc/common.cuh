@@ -32,9 +32,34 @@ inline int check_launch(const char *what) {
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Optional per-kernel timing (matpl_profile_begin / matpl_profile_collect): when enabled,
+// every launch site records a CUDA event pair on its own stream.
+bool profiling_enabled();
+void profile_record(const char *name, cudaEvent_t start, cudaEvent_t stop);
+cudaEvent_t profile_event();
+
+struct ProfScope {
+    const char *name;
+    cudaStream_t stream;
+    cudaEvent_t a = nullptr, b = nullptr;
+    ProfScope(const char *n, cudaStream_t s) : name(n), stream(s) {
+        if (profiling_enabled()) {
+            a = profile_event();
+            b = profile_event();
+            if (a && b) cudaEventRecord(a, stream);
+        }
+    }
+    ~ProfScope() {
+        if (a && b) {
+            cudaEventRecord(b, stream);
+            profile_record(name, a, b);
+        }
+    }
+};
+
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-// Device math wrappers: the plain forms use CUDA's correctly-rounded-library tanh.
+// Device math wrappers: the plain forms call CUDA's tanhf / tanh.
 __device__ __forceinline__ float dev_tanh(float x) { return tanhf(x); }
 __device__ __forceinline__ double dev_tanh(double x) { return tanh(x); }
 

@@ -700,7 +700,10 @@ int launch_eval(const matpl_dp_model *M, const EvalParams &P, const int32_t *lis
         return MATPL_ERR_CUDA;
     }
     const int nnet = P.ntypes * P.ntypes;
-    dp_pad<T><<<(nnet + 31) / 32, 32, 0, s>>>(params, davg, dstd, pad, P.ntypes);
+    {
+        ProfScope ps("dp_pad", s);
+        dp_pad<T><<<(nnet + 31) / 32, 32, 0, s>>>(params, davg, dstd, pad, P.ntypes);
+    }
 
     const size_t wbytes = sizeof(T) * (size_t)nnet * EmbOff::SIZE;
     const bool ws_ok = wbytes <= 128 * 1024;
@@ -715,16 +718,28 @@ int launch_eval(const matpl_dp_model *M, const EvalParams &P, const int32_t *lis
     auto kb = ws_ok ? dp_embed_bwd<T, true> : dp_embed_bwd<T, false>;
     cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f);
     cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
-    kf<<<gridw, kWarps * 32, smem_f, s>>>(list_neigh, idr, type_map, params, davg, dstd, pad, A, P);
+    {
+        ProfScope ps("dp_embed_fwd", s);
+        kf<<<gridw, kWarps * 32, smem_f, s>>>(list_neigh, idr, type_map, params, davg, dstd, pad, A, P);
+    }
     constexpr int TILE = sizeof(T) == 8 ? 32 : 64;
     const size_t smem_fit = sizeof(T) * (size_t)TILE * (NA + DIN + 4 * F);
     cudaFuncSetAttribute(dp_fit<T, TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_fit);
     const long long ntiles = (total + TILE - 1) / TILE;
     const int gridf = (int)(ntiles < 152LL * 4 ? ntiles : 152LL * 4);
-    dp_fit<T, TILE><<<gridf, 256, smem_fit, s>>>(A, type_map, params, Ei, dA, P);
-    kb<<<gridw, kWarps * 32, smem_b, s>>>(list_neigh, idr, type_map, params, davg, dstd, dA,
-                                          force, avir, P);
-    dp_reduce<T><<<P.batch, 256, 0, s>>>(Ei, avir, Etot, virial, P.natoms);
+    {
+        ProfScope ps("dp_fit", s);
+        dp_fit<T, TILE><<<gridf, 256, smem_fit, s>>>(A, type_map, params, Ei, dA, P);
+    }
+    {
+        ProfScope ps("dp_embed_bwd", s);
+        kb<<<gridw, kWarps * 32, smem_b, s>>>(list_neigh, idr, type_map, params, davg, dstd, dA,
+                                              force, avir, P);
+    }
+    {
+        ProfScope ps("dp_reduce", s);
+        dp_reduce<T><<<P.batch, 256, 0, s>>>(Ei, avir, Etot, virial, P.natoms);
+    }
     return check_launch("matpl_dp_eval");
 }
 

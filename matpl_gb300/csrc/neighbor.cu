@@ -474,10 +474,14 @@ extern "C" int matpl_neighbor_build(int batch, int natoms, int ntypes, int m_nei
         return MATPL_ERR_CUDA;
     }
     const long long na = (long long)batch * natoms;
-    nb_setup<<<(batch + 127) / 128, 128, 0, s>>>(lattice, img, batch, Rc_M, P.cell_cap);
-    nb_bin<<<grid_for(na, 256), 256, 0, s>>>(frac_pos, img, wpos, cell_of, cell_count, P);
-    nb_scan<<<batch, 1024, 0, s>>>(img, cell_count, cell_start, P);
-    nb_fill<<<grid_for(na, 256), 256, 0, s>>>(cell_of, cell_start, cell_fill, cell_atoms, P);
+    {
+        ProfScope ps("nb_cells", s);
+        nb_setup<<<(batch + 127) / 128, 128, 0, s>>>(lattice, img, batch, Rc_M, P.cell_cap);
+        nb_bin<<<grid_for(na, 256), 256, 0, s>>>(frac_pos, img, wpos, cell_of, cell_count, P);
+        nb_scan<<<batch, 1024, 0, s>>>(img, cell_count, cell_start, P);
+        nb_fill<<<grid_for(na, 256), 256, 0, s>>>(cell_of, cell_start, cell_fill, cell_atoms, P);
+    }
+    ProfScope ps("nb_search", s);
     const int S = ntypes * m_neigh;
     const size_t smem = (size_t)kWarps * S * 5;
     if (out_dtype == MATPL_F64) {

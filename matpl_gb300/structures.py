@@ -51,49 +51,62 @@ def fcc(a: float, reps: Sequence[int], sigma: float, seed: int, element: int = 2
 def random_packed(natoms: int, density: float, elements: Sequence[int],
                   fractions: Sequence[float], seed: int, min_dist: float = 2.0,
                   strain: float = 0.0) -> Structure:
-    """Random sequential insertion of ``natoms`` atoms in a cube of the given number density
-    (atoms / A^3) with all pair distances >= ``min_dist`` (periodic), then an optional
-    symmetric strain eps with entries N(0, strain) applied to the cell (cell = cube (I + eps)).
+    """Random insertion of ``natoms`` atoms in a cube of the given number density
+    (atoms / A^3) with all periodic pair distances >= ``min_dist``, then an optional symmetric
+    strain eps with entries N(0, strain) applied to the cell (cell = cube (I + eps)).
+
+    Candidates are drawn in seeded batches and checked on a grid of cells of edge
+    <= min_dist/sqrt(3) (at most one atom per cell): a candidate is rejected if an accepted
+    atom, or an earlier candidate of its own batch, lies closer than ``min_dist``.
     Element counts follow ``fractions`` (rounded, remainder to the last element)."""
     rng = np.random.default_rng(seed)
     L = (natoms / density) ** (1.0 / 3.0)
-    nb = max(1, int(L // min_dist))
+    nb = max(1, int(np.ceil(L / (min_dist / np.sqrt(3.0)))))
     w = L / nb
-    grid = {}
+    reach = int(np.ceil(min_dist / w))
+    rr = np.arange(-reach, reach + 1)
+    offs = np.stack(np.meshgrid(rr, rr, rr, indexing="ij"), -1).reshape(-1, 3)
+    grid = -np.ones((nb, nb, nb), dtype=np.int64)
     pts = np.empty((natoms, 3), dtype=np.float64)
-    n = 0
     md2 = min_dist * min_dist
-    attempts = 0
+    n = 0
+    rounds = 0
+
+    def conflicts(cand, cells, g, src):
+        nc = (cells[:, None, :] + offs[None, :, :]) % nb
+        occ = g[nc[..., 0], nc[..., 1], nc[..., 2]]                 # [B, K]
+        ok = occ >= 0
+        d = src[np.where(ok, occ, 0)] - cand[:, None, :]
+        d -= L * np.round(d / L)
+        close = ok & (np.einsum("bkj,bkj->bk", d, d) < md2)
+        return close, occ
+
     while n < natoms:
-        cand = rng.random((256, 3)) * L
-        for p in cand:
-            attempts += 1
-            if attempts > 200 * natoms + 10000:
-                raise RuntimeError("random_packed: insertion stalled; lower density or min_dist")
-            c = np.floor(p / w).astype(int) % nb
-            ok = True
-            for dx in (-1, 0, 1):
-                if not ok:
-                    break
-                for dy in (-1, 0, 1):
-                    if not ok:
-                        break
-                    for dz in (-1, 0, 1):
-                        key = ((c[0] + dx) % nb, (c[1] + dy) % nb, (c[2] + dz) % nb)
-                        lst = grid.get(key)
-                        if not lst:
-                            continue
-                        d = pts[lst] - p
-                        d -= L * np.round(d / L)
-                        if np.any(np.einsum("ij,ij->i", d, d) < md2):
-                            ok = False
-                            break
-            if ok:
-                pts[n] = p
-                grid.setdefault((c[0], c[1], c[2]), []).append(n)
-                n += 1
-                if n == natoms:
-                    break
+        rounds += 1
+        if rounds > 10000:
+            raise RuntimeError("random_packed: insertion stalled; lower density or min_dist")
+        bsz = int(min(8192, max(64, 2 * (natoms - n))))
+        cand = rng.random((bsz, 3)) * L
+        cells = np.minimum((cand / w).astype(np.int64), nb - 1)
+        close, _ = conflicts(cand, cells, grid, pts)
+        keep = ~close.any(1)
+        cand, cells = cand[keep], cells[keep]
+        if len(cand) == 0:
+            continue
+        # intra-batch: drop a candidate that conflicts with an earlier one of the batch
+        tg = -np.ones((nb, nb, nb), dtype=np.int64)
+        order = np.arange(len(cand))
+        tg[cells[::-1, 0], cells[::-1, 1], cells[::-1, 2]] = order[::-1]   # earliest wins a cell
+        same_cell_loser = tg[cells[:, 0], cells[:, 1], cells[:, 2]] != order
+        close_b, occ_b = conflicts(cand, cells, tg, cand)
+        earlier = close_b & (occ_b < order[:, None])
+        keep = ~(earlier.any(1) | same_cell_loser)
+        cand, cells = cand[keep], cells[keep]
+        take = min(len(cand), natoms - n)
+        cand, cells = cand[:take], cells[:take]
+        pts[n:n + take] = cand
+        grid[cells[:, 0], cells[:, 1], cells[:, 2]] = np.arange(n, n + take)
+        n += take
     counts = [int(round(f * natoms)) for f in fractions[:-1]]
     counts.append(natoms - sum(counts))
     types = np.concatenate([np.full(c, t, dtype=np.int32) for t, c in enumerate(counts)])
