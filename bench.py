@@ -265,31 +265,45 @@ def run_ours(args, ws, rank, local):
     for k, v in prof.items():
         per_kernel[k]["share"] = v[0] / tot if tot else None
     dom = max(prof, key=lambda k: prof[k][0]) if prof else None
+    es = 8 if prec == "float64" else 4
+    S = 2 * M_NEIGH
     flops = {"dp_embed_bwd": FLOP_EMB_BWD_PAIR * n_pairs, "dp_embed_fwd": FLOP_EMB_FWD_PAIR * n_pairs,
              "dp_fit": FLOP_FIT_ATOM * NATOMS}
+    # HBM-bound kernels: algorithmic bytes per launch (reads positions + types, writes the
+    # reference-layout list_neigh [N,S] int32 and ImageDR [N,S,4])
+    hbm_bytes = {"nb_search": NATOMS * (24 + 4 + S * (4 + 4 * es))}
     peaks = {}
     pk_path = os.path.join(HERE, "MEASURED_PEAKS.json")
     if os.path.exists(pk_path):
         peaks = json.load(open(pk_path))
     bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    src = "of measured (MEASURED_PEAKS.json)" if peaks else "of fallback"
     roof = None
-    if dom in flops:
+    if dom is not None and (dom in flops or dom in hbm_bytes):
         t_launch = per_kernel[dom]["ms_per_launch"] * 1e-3
-        ach = flops[dom] / t_launch / 1e12
-        sm_mhz = clocks.get("sm_mhz") or 2070.0
-        simt_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
-        roof = {"kernel": dom, "bound": "tensor", "achieved": ach, "peak": bf16_peak,
-                "unit": "TFLOP/s", "frac": ach / bf16_peak, "traffic": None,
-                "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peaks else "fallback",
-                "simt_fp32": {"achieved": ach, "peak_nominal_at_sm_clock": simt_peak,
-                              "frac": ach / simt_peak}}
+        if dom in hbm_bytes:
+            ach = hbm_bytes[dom] / t_launch / 1e9
+            roof = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": hbm_peak,
+                    "unit": "GB/s", "frac": ach / hbm_peak, "traffic": None,
+                    "algorithmic_bytes_per_launch": hbm_bytes[dom], "peak_source": src}
+        else:
+            ach = flops[dom] / t_launch / 1e12
+            sm_mhz = clocks.get("sm_mhz") or 2070.0
+            simt_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+            roof = {"kernel": dom, "bound": "tensor", "achieved": ach, "peak": bf16_peak,
+                    "unit": "TFLOP/s", "frac": ach / bf16_peak, "traffic": None,
+                    "algorithmic_flops_per_launch": flops[dom], "peak_source": src + " bf16 burst",
+                    "simt_fp32": {"achieved": ach, "peak_nominal_at_sm_clock": simt_peak,
+                                  "frac": ach / simt_peak}}
         tp = os.path.join(HERE, "profiles", "traffic.json")
         if os.path.exists(tp):
             tr = json.load(open(tp)).get(f"{dom}:{prec}")
             if tr:
                 roof["traffic"] = tr["bytes_per_launch"]
                 roof["traffic_note"] = tr.get("note")
-    launches = sum(v[1] for k, v in prof.items()) + 3 * prof.get("nb_cells", (0, 0))[1]
+    per_scope = {"nb_cells": 4, "dp_reduce": 2}
+    launches = sum(v[1] * per_scope.get(k, 1) for k, v in prof.items())
 
     cb = None
     if rank == 0 and not args.no_cpu_baseline:

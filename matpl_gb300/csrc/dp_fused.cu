@@ -19,6 +19,7 @@
 //                fixed order (deterministic).
 #include "common.cuh"
 #include "dp_layout.cuh"
+#include <algorithm>
 
 namespace matpl {
 namespace {
@@ -640,15 +641,19 @@ dp_embed_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
 }
 
 // --------------------------------------------------------------------------- dp_reduce
+// Two fixed-order passes (deterministic): kReduceBlocks partial sums per configuration, then
+// one warp per configuration adds the partials in index order.
+constexpr int kReduceBlocks = 64;
+
 template <typename T>
-__global__ void dp_reduce(const T *__restrict__ Ei, const double *__restrict__ atom_vir,
-                          double *__restrict__ Etot, double *__restrict__ virial, int natoms) {
-    const int b = blockIdx.x;
-    __shared__ double part[10][32];
+__global__ void dp_reduce_partial(const T *__restrict__ Ei, const double *__restrict__ atom_vir,
+                                  double *__restrict__ part_out, int natoms) {
+    const int b = blockIdx.y;
+    __shared__ double part[10][8];
     double acc[10];
 #pragma unroll
     for (int q = 0; q < 10; ++q) acc[q] = 0.0;
-    for (int i = threadIdx.x; i < natoms; i += blockDim.x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < natoms; i += gridDim.x * blockDim.x) {
         const long long t = (long long)b * natoms + i;
         acc[0] += (double)Ei[t];
 #pragma unroll
@@ -664,13 +669,23 @@ __global__ void dp_reduce(const T *__restrict__ Ei, const double *__restrict__ a
     if (threadIdx.x < 10) {
         double v = 0.0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += part[threadIdx.x][w];
+        part_out[((long long)b * gridDim.x + blockIdx.x) * 10 + threadIdx.x] = v;
+    }
+}
+
+__global__ void dp_reduce_final(const double *__restrict__ part, double *__restrict__ Etot,
+                                double *__restrict__ virial, int nblk) {
+    const int b = blockIdx.x;
+    if (threadIdx.x < 10) {
+        double v = 0.0;
+        for (int k = 0; k < nblk; ++k) v += part[((long long)b * nblk + k) * 10 + threadIdx.x];
         if (threadIdx.x == 0) Etot[b] = v;
         else virial[b * 9 + threadIdx.x - 1] = v;
     }
 }
 
 struct DpLayout {
-    size_t A, dA, pad, vir, total;
+    size_t A, dA, pad, vir, red, total;
 };
 
 DpLayout dp_layout(size_t es, int batch, int natoms, int ntypes) {
@@ -681,6 +696,7 @@ DpLayout dp_layout(size_t es, int batch, int natoms, int ntypes) {
     l.dA = o;  o = align_up(o + es * na * NA, 256);
     l.pad = o; o = align_up(o + es * (size_t)ntypes * ntypes * NA, 256);
     l.vir = o; o = align_up(o + 8 * na * 9, 256);
+    l.red = o; o = align_up(o + 8 * (size_t)batch * kReduceBlocks * 10, 256);
     l.total = o;
     return l;
 }
@@ -738,7 +754,10 @@ int launch_eval(const matpl_dp_model *M, const EvalParams &P, const int32_t *lis
     }
     {
         ProfScope ps("dp_reduce", s);
-        dp_reduce<T><<<P.batch, 256, 0, s>>>(Ei, avir, Etot, virial, P.natoms);
+        const int nblk = (int)std::min<long long>(kReduceBlocks, (P.natoms + 255) / 256);
+        double *red = (double *)(ws + lay.red);
+        dp_reduce_partial<T><<<dim3(nblk, P.batch), 256, 0, s>>>(Ei, avir, red, P.natoms);
+        dp_reduce_final<<<P.batch, 32, 0, s>>>(red, Etot, virial, nblk);
     }
     return check_launch("matpl_dp_eval");
 }

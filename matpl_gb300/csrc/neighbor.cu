@@ -54,6 +54,14 @@ __device__ __forceinline__ void cart(const double *L, double d1, double d2, doub
     dd = da(da(dm(x, x), dm(y, y)), dm(z, z));
 }
 
+__device__ __forceinline__ void store4(float *p, float a, float b, float c, float d) {
+    *reinterpret_cast<float4 *>(p) = make_float4(a, b, c, d);
+}
+__device__ __forceinline__ void store4(double *p, double a, double b, double c, double d) {
+    reinterpret_cast<double2 *>(p)[0] = make_double2(a, b);
+    reinterpret_cast<double2 *>(p)[1] = make_double2(c, d);
+}
+
 __global__ void nb_setup(const double *__restrict__ lattice, NbImage *__restrict__ img,
                          int batch, double Rc, int cell_cap) {
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < batch; b += gridDim.x * blockDim.x) {
@@ -99,8 +107,8 @@ __global__ void nb_setup(const double *__restrict__ lattice, NbImage *__restrict
 }
 
 __global__ void nb_bin(const double *__restrict__ frac, const NbImage *__restrict__ img,
-                       double *__restrict__ wpos, int *__restrict__ cell_of,
-                       int *__restrict__ cell_count, NbParams P) {
+                       double *__restrict__ wpos, float4 *__restrict__ wpos32,
+                       int *__restrict__ cell_of, int *__restrict__ cell_count, NbParams P) {
     const long long total = (long long)P.batch * P.natoms;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
@@ -110,6 +118,7 @@ __global__ void nb_bin(const double *__restrict__ frac, const NbImage *__restric
             f[k] = fmod(da(frac[3 * t + k], 10.0), 1.0);   // NeighConst.f90:46-50
             wpos[3 * t + k] = f[k];
         }
+        wpos32[t] = make_float4((float)f[0], (float)f[1], (float)f[2], 0.f);
         const NbImage &im = img[b];
         if (im.iflag) {
             cell_of[t] = -1;
@@ -180,20 +189,39 @@ __global__ void nb_fill(const int *__restrict__ cell_of, const int *__restrict__
     }
 }
 
+// FP32 pre-filter: a candidate whose single-precision distance is clearly beyond Rc (by a
+// margin far larger than the FP32 rounding error of the pair vector) is dropped; everything
+// else, including nearest-image ties, goes to the exact FP64 test below.
+__device__ __forceinline__ bool maybe_within(const float *Lf, float d1, float d2, float d3,
+                                             float thr2) {
+    const float x = Lf[0] * d1 + Lf[3] * d2 + Lf[6] * d3;
+    const float y = Lf[1] * d1 + Lf[4] * d2 + Lf[7] * d3;
+    const float z = Lf[2] * d1 + Lf[5] * d2 + Lf[8] * d3;
+    return x * x + y * y + z * z < thr2;
+}
+
+__device__ __forceinline__ float mic_f(float d, bool &tie) {
+    if (fabsf(d + 1.f) < fabsf(d)) d += 1.f;
+    if (fabsf(d - 1.f) < fabsf(d)) d -= 1.f;
+    tie |= fabsf(fabsf(d) - 0.5f) < 1e-5f;
+    return d;
+}
+
 template <typename TO>
 __global__ void __launch_bounds__(kWarps * 32)
 nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
-          const int32_t *__restrict__ type_map, const int *__restrict__ cell_start,
-          const int *__restrict__ cell_atoms, int32_t *__restrict__ list_neigh,
-          TO *__restrict__ image_dr, int32_t *__restrict__ num_neigh, int32_t *__restrict__ err,
-          NbParams P) {
+          const float4 *__restrict__ wpos32, const int32_t *__restrict__ type_map,
+          const int *__restrict__ cell_start, const int *__restrict__ cell_atoms,
+          int32_t *__restrict__ list_neigh, TO *__restrict__ image_dr,
+          int32_t *__restrict__ num_neigh, int32_t *__restrict__ err, NbParams P) {
     extern __shared__ unsigned char smem_raw[];
     const int S = P.ntypes * P.m;
+    const int CAP = 2 * S;                         // pre-filtered candidates per atom
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int *keys = reinterpret_cast<int *>(smem_raw) + warp * S;
-    unsigned char *ktype =
-        reinterpret_cast<unsigned char *>(reinterpret_cast<int *>(smem_raw) + kWarps * S) +
-        warp * S;
+    int *cand = reinterpret_cast<int *>(smem_raw) + warp * (CAP + S);
+    int *keys = cand + CAP;
+    unsigned char *ktype = reinterpret_cast<unsigned char *>(
+                               reinterpret_cast<int *>(smem_raw) + kWarps * (CAP + S)) + warp * S;
     const long long total = (long long)P.batch * P.natoms;
     for (long long t = (long long)blockIdx.x * kWarps + warp; t < total;
          t += (long long)gridDim.x * kWarps) {
@@ -201,105 +229,200 @@ nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
         const int i = (int)(t - (long long)b * P.natoms);
         const NbImage &im = img[b];
         const double *pos = wpos + (long long)b * P.natoms * 3;
+        const float4 *pos32 = wpos32 + (long long)b * P.natoms;
         const double pi0 = pos[3 * i], pi1 = pos[3 * i + 1], pi2 = pos[3 * i + 2];
+        const float4 fi = pos32[i];
         const int ti = type_map[i];
         if (ti < 0 || ti >= P.ntypes) {
             if (lane == 0) atomicMax(err, MATPL_KERR_BAD_TYPE);
             continue;
         }
-        const double rct2 = P.rct2[ti];
-        int n_acc = 0;                       // accepted (within Rc_type) entries in keys[]
-        int cntM[kMaxTypes];                 // within Rc_M, per type (overflow test)
-        for (int q = 0; q < P.ntypes; ++q) cntM[q] = 0;
-        bool overflow = false;
+        float Lf[9], lsum = 0.f;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            Lf[q] = (float)im.L[q];
+            lsum += fabsf(Lf[q]);
+        }
+        const float rc2f = (float)P.rc2;
+        const float thr2 = rc2f + 0.01f + 1e-5f * lsum * sqrtf(rc2f);
         const int nimg1 = 2 * im.nper[2] + 1, nimg2 = 2 * im.nper[1] + 1;
         const int nimg = im.iflag ? (2 * im.nper[0] + 1) * nimg2 * nimg1 : 1;
 
-        auto consider = [&](bool valid, int j, int img_idx, double d1, double d2, double d3) {
-            double x, y, z, dd;
-            cart(im.L, d1, d2, d3, x, y, z, dd);
-            const bool inM = valid && dd < P.rc2 && dd > 1.0e-8;
-            const bool inT = inM && dd < rct2;
-            const int tj = valid ? type_map[j] : 0;
-            if (valid && (tj < 0 || tj >= P.ntypes)) atomicMax(err, MATPL_KERR_BAD_TYPE);
-            for (int q = 0; q < P.ntypes; ++q) {
-                const unsigned mq = __ballot_sync(0xffffffffu, inM && tj == q);
-                cntM[q] += __popc(mq);
-            }
-            const unsigned ma = __ballot_sync(0xffffffffu, inT);
-            const int at = n_acc + __popc(ma & ((1u << lane) - 1u));
-            if (inT && at < S) {
-                keys[at] = j * nimg + img_idx;
-                ktype[at] = (unsigned char)tj;
-            }
-            n_acc += __popc(ma);
-        };
-
+        // ---- phase A: enumerate candidates (flattened over cell ranges / images), FP32 filter
+        int ncand = 0;
+        bool cap_hit = false;
         if (im.iflag) {
-            for (int j0 = 0; j0 < P.natoms; j0 += 32) {
-                const int j = j0 + lane;
-                const bool valid = j < P.natoms;
-                const double pj0 = valid ? pos[3 * j] : 0.0, pj1 = valid ? pos[3 * j + 1] : 0.0,
-                             pj2 = valid ? pos[3 * j + 2] : 0.0;
-                int idx = 0;
-                for (int i1 = -im.nper[0]; i1 <= im.nper[0]; ++i1)
-                    for (int i2 = -im.nper[1]; i2 <= im.nper[1]; ++i2)
-                        for (int i3 = -im.nper[2]; i3 <= im.nper[2]; ++i3, ++idx) {
-                            const double d1 = da(da(pj0, -pi0), (double)i1);
-                            const double d2 = da(da(pj1, -pi1), (double)i2);
-                            const double d3 = da(da(pj2, -pi2), (double)i3);
-                            consider(valid, j, idx, d1, d2, d3);
-                        }
+            const long long T = (long long)P.natoms * nimg;
+            for (long long c0 = 0; c0 < T; c0 += 32) {
+                const long long c = c0 + lane;
+                bool keep = false;
+                int key = 0;
+                if (c < T) {
+                    const int j = (int)(c / nimg), idx = (int)(c - (long long)j * nimg);
+                    const int i3 = idx % nimg1 - im.nper[2];
+                    const int i2 = (idx / nimg1) % nimg2 - im.nper[1];
+                    const int i1 = idx / (nimg1 * nimg2) - im.nper[0];
+                    const float4 fj = pos32[j];
+                    keep = maybe_within(Lf, fj.x - fi.x + i1, fj.y - fi.y + i2, fj.z - fi.z + i3, thr2);
+                    key = j * nimg + idx;
+                }
+                const unsigned mk = __ballot_sync(0xffffffffu, keep);
+                const int at = ncand + __popc(mk & ((1u << lane) - 1u));
+                if (keep && at < CAP) cand[at] = key;
+                ncand += __popc(mk);
             }
         } else {
+            // up to 9 (x, y) columns x 2 z-ranges; lane q < nr holds range q
             int ci[3];
-            for (int k = 0; k < 3; ++k) {
-                const double f = k == 0 ? pi0 : (k == 1 ? pi1 : pi2);
-                int q = (int)(f * im.nb[k]);
-                ci[k] = q >= im.nb[k] ? im.nb[k] - 1 : (q < 0 ? 0 : q);
-            }
-            int noff[3], off0[3];
-            for (int k = 0; k < 3; ++k) {
-                noff[k] = im.nb[k] >= 3 ? 3 : im.nb[k];
-                off0[k] = im.nb[k] >= 3 ? -1 : 0;
+            ci[0] = min((int)(fi.x * im.nb[0]), im.nb[0] - 1);
+            ci[1] = min((int)(fi.y * im.nb[1]), im.nb[1] - 1);
+            ci[2] = min((int)(fi.z * im.nb[2]), im.nb[2] - 1);
+            // the FP32 bin may differ from the FP64 bin at a bin edge: use the FP64 one
+            {
+                const double f[3] = {pi0, pi1, pi2};
+                for (int k = 0; k < 3; ++k) {
+                    int q = (int)(f[k] * im.nb[k]);
+                    ci[k] = q >= im.nb[k] ? im.nb[k] - 1 : (q < 0 ? 0 : q);
+                }
             }
             const int *cs = cell_start + (long long)b * (P.cell_cap + 1);
             const int *ca = cell_atoms + (long long)b * P.natoms;
-            for (int ox = 0; ox < noff[0]; ++ox)
-                for (int oy = 0; oy < noff[1]; ++oy)
-                    for (int oz = 0; oz < noff[2]; ++oz) {
-                        const int cx = (ci[0] + off0[0] + ox + im.nb[0]) % im.nb[0];
-                        const int cy = (ci[1] + off0[1] + oy + im.nb[1]) % im.nb[1];
-                        const int cz = (ci[2] + off0[2] + oz + im.nb[2]) % im.nb[2];
-                        const int cell = (cx * im.nb[1] + cy) * im.nb[2] + cz;
-                        const int s0 = cs[cell], s1 = cs[cell + 1];
-                        for (int p = s0; p < s1; p += 32) {
-                            const bool valid = p + lane < s1;
-                            const int j = valid ? ca[p + lane] : 0;
-                            double d1 = 0, d2 = 0, d3 = 0;
-                            if (valid) {
-                                d1 = da(pos[3 * j], -pi0); mic(d1);
-                                d2 = da(pos[3 * j + 1], -pi1); mic(d2);
-                                d3 = da(pos[3 * j + 2], -pi2); mic(d3);
-                            }
-                            consider(valid, j, 0, d1, d2, d3);
-                        }
+            const int nx = im.nb[0] >= 3 ? 3 : im.nb[0], ny = im.nb[1] >= 3 ? 3 : im.nb[1];
+            const int nz = im.nb[2] >= 3 ? 3 : im.nb[2];
+            const int ox0 = im.nb[0] >= 3 ? -1 : 0, oy0 = im.nb[1] >= 3 ? -1 : 0;
+            const int oz0 = im.nb[2] >= 3 ? -1 : 0;
+            // lane q (< 18) builds range q: column q/2, part q%2
+            int rs = 0, rl = 0;
+            if (lane < 18) {
+                const int col = lane >> 1, part = lane & 1;
+                if (col < nx * ny) {
+                    const int cx = (ci[0] + ox0 + col / ny + im.nb[0]) % im.nb[0];
+                    const int cy = (ci[1] + oy0 + col % ny + im.nb[1]) % im.nb[1];
+                    const int base = (cx * im.nb[1] + cy) * im.nb[2];
+                    const int zlo = ci[2] + oz0;                // may be -1
+                    const int zhi = zlo + nz - 1;               // may be nb
+                    int a0, a1;                                 // z-cell interval of this part
+                    if (part == 0) {
+                        a0 = zlo < 0 ? 0 : zlo;
+                        a1 = zhi >= im.nb[2] ? im.nb[2] - 1 : zhi;
+                    } else if (zlo < 0) {
+                        a0 = im.nb[2] - 1; a1 = im.nb[2] - 1;
+                    } else if (zhi >= im.nb[2]) {
+                        a0 = 0; a1 = 0;
+                    } else {
+                        a0 = 1; a1 = 0;                          // empty
                     }
+                    if (a0 <= a1) {
+                        rs = cs[base + a0];
+                        rl = cs[base + a1 + 1] - rs;
+                    }
+                }
+            }
+            int incl = rl;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const int T = __shfl_sync(0xffffffffu, incl, 31);
+            const int excl = incl - rl;
+            for (int c0 = 0; c0 < T; c0 += 32) {
+                const int c = c0 + lane;
+                // find the range holding flat index c: last q with excl_q <= c and rl_q > 0
+                int q = 0;
+#pragma unroll
+                for (int r = 0; r < 18; ++r) {
+                    const int e_r = __shfl_sync(0xffffffffu, excl, r);
+                    const int l_r = __shfl_sync(0xffffffffu, rl, r);
+                    if (l_r > 0 && e_r <= c) q = r;
+                }
+                const int s_q = __shfl_sync(0xffffffffu, rs, q);
+                const int e_q = __shfl_sync(0xffffffffu, excl, q);
+                bool keep = false;
+                int j = 0;
+                if (c < T) {
+                    j = ca[s_q + c - e_q];
+                    const float4 fj = pos32[j];
+                    bool tie = false;
+                    const float d1 = mic_f(fj.x - fi.x, tie), d2 = mic_f(fj.y - fi.y, tie),
+                                d3 = mic_f(fj.z - fi.z, tie);
+                    keep = tie || maybe_within(Lf, d1, d2, d3, thr2);
+                }
+                const unsigned mk = __ballot_sync(0xffffffffu, keep);
+                const int at = ncand + __popc(mk & ((1u << lane) - 1u));
+                if (keep && at < CAP) cand[at] = j;
+                ncand += __popc(mk);
+            }
         }
-        for (int q = 0; q < P.ntypes; ++q) overflow |= cntM[q] > P.m;
+        if (ncand > CAP) { cap_hit = true; ncand = CAP; }
+        __syncwarp();
+
+        // ---- phase B: exact FP64 test (NeighConst.f90 arithmetic) on the survivors
+        int cntM[kMaxTypes];
+#pragma unroll
+        for (int q = 0; q < kMaxTypes; ++q) cntM[q] = 0;
+        int n_acc = 0;
+        const double rct2 = P.rct2[ti];
+        for (int c0 = 0; c0 < ncand; c0 += 32) {
+            const int c = c0 + lane;
+            bool inM = false, inT = false;
+            int tj = 0, key = 0;
+            if (c < ncand) {
+                key = cand[c];
+                const int j = key / nimg, idx = key - (key / nimg) * nimg;
+                double d1, d2, d3;
+                if (im.iflag) {
+                    const int i3 = idx % nimg1 - im.nper[2];
+                    const int i2 = (idx / nimg1) % nimg2 - im.nper[1];
+                    const int i1 = idx / (nimg1 * nimg2) - im.nper[0];
+                    d1 = da(da(pos[3 * j], -pi0), (double)i1);
+                    d2 = da(da(pos[3 * j + 1], -pi1), (double)i2);
+                    d3 = da(da(pos[3 * j + 2], -pi2), (double)i3);
+                } else {
+                    d1 = da(pos[3 * j], -pi0); mic(d1);
+                    d2 = da(pos[3 * j + 1], -pi1); mic(d2);
+                    d3 = da(pos[3 * j + 2], -pi2); mic(d3);
+                }
+                double x, y, z, dd;
+                cart(im.L, d1, d2, d3, x, y, z, dd);
+                inM = dd < P.rc2 && dd > 1.0e-8;
+                inT = inM && dd < rct2;
+                tj = type_map[j];
+                if (tj < 0 || tj >= P.ntypes) {
+                    atomicMax(err, MATPL_KERR_BAD_TYPE);
+                    inM = inT = false;
+                    tj = 0;
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kMaxTypes; ++q)
+                if (q < P.ntypes) cntM[q] += __popc(__ballot_sync(0xffffffffu, inM && tj == q));
+            const unsigned ma = __ballot_sync(0xffffffffu, inT);
+            const int at = n_acc + __popc(ma & ((1u << lane) - 1u));
+            if (inT && at < S) {
+                keys[at] = key;
+                ktype[at] = (unsigned char)tj;
+            }
+            n_acc += __popc(ma);
+        }
+        bool overflow = cap_hit;
+#pragma unroll
+        for (int q = 0; q < kMaxTypes; ++q) overflow |= (q < P.ntypes) && cntM[q] > P.m;
         if (overflow && lane == 0) atomicMax(err, MATPL_KERR_NEIGHBOR_OVERFLOW);
         const int nst = n_acc < S ? n_acc : S;
         __syncwarp();
-        // per-type accepted counts (capped at m)
         int ncount[kMaxTypes];
-        for (int q = 0; q < P.ntypes; ++q) {
+#pragma unroll
+        for (int q = 0; q < kMaxTypes; ++q) {
             int c = 0;
-            for (int e = lane; e < nst; e += 32) c += ktype[e] == q;
-            c = warp_sum(c);
+            if (q < P.ntypes) {
+                for (int e = lane; e < nst; e += 32) c += ktype[e] == q;
+                c = warp_sum(c);
+            }
             ncount[q] = c < P.m ? c : P.m;
         }
         const long long row = t * (long long)S;
-        // rank sort by key within each type block, write the accepted slots
+        // ---- phase C: rank sort by (j, image) inside each type block, write occupied slots
         for (int e = lane; e < nst; e += 32) {
             const int key = keys[e];
             const int ty = ktype[e];
@@ -324,24 +447,23 @@ nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
             cart(im.L, d1, d2, d3, x, y, z, dd);
             const long long slot = row + (long long)ty * P.m + rank;
             list_neigh[slot] = j + 1;
-            image_dr[4 * slot + 0] = (TO)__dsqrt_rn(dd);
-            image_dr[4 * slot + 1] = (TO)x;
-            image_dr[4 * slot + 2] = (TO)y;
-            image_dr[4 * slot + 3] = (TO)z;
+            store4(image_dr + 4 * slot, (TO)__dsqrt_rn(dd), (TO)x, (TO)y, (TO)z);
         }
-        // clear the remaining slots
+        // ---- phase D: clear the empty slots
         for (int s = lane; s < S; s += 32) {
             const int ty = s / P.m;
-            if (s - ty * P.m < ncount[ty]) continue;
+            int nt = 0;
+#pragma unroll
+            for (int q = 0; q < kMaxTypes; ++q)
+                if (q == ty) nt = ncount[q];
+            if (s - ty * P.m < nt) continue;
             list_neigh[row + s] = 0;
-            image_dr[4 * (row + s) + 0] = TO(0);
-            image_dr[4 * (row + s) + 1] = TO(0);
-            image_dr[4 * (row + s) + 2] = TO(0);
-            image_dr[4 * (row + s) + 3] = TO(0);
+            store4(image_dr + 4 * (row + s), TO(0), TO(0), TO(0), TO(0));
         }
         if (num_neigh != nullptr && lane < P.ntypes) {
             int c = 0;
-            for (int q = 0; q < P.ntypes; ++q)
+#pragma unroll
+            for (int q = 0; q < kMaxTypes; ++q)
                 if (q == lane) c = ncount[q];
             num_neigh[t * P.ntypes + lane] = c;
         }
@@ -399,7 +521,7 @@ __global__ void env_mat_kernel(const int32_t *__restrict__ type_map, const T *__
 }
 
 struct NbLayout {
-    size_t img, wpos, cell_of, cell_count, cell_fill, cell_start, cell_atoms, total;
+    size_t img, wpos, wpos32, cell_of, cell_count, cell_fill, cell_start, cell_atoms, total;
 };
 
 NbLayout nb_layout(int batch, int natoms) {
@@ -408,6 +530,7 @@ NbLayout nb_layout(int batch, int natoms) {
     size_t o = 0;
     l.img = o;        o = align_up(o + sizeof(NbImage) * batch, 256);
     l.wpos = o;       o = align_up(o + 8 * 3 * (size_t)batch * natoms, 256);
+    l.wpos32 = o;     o = align_up(o + 16 * (size_t)batch * natoms, 256);
     l.cell_of = o;    o = align_up(o + 4 * (size_t)batch * natoms, 256);
     l.cell_count = o; o = align_up(o + 4 * cap * batch, 256);
     l.cell_fill = o;  o = align_up(o + 4 * cap * batch, 256);
@@ -463,6 +586,7 @@ extern "C" int matpl_neighbor_build(int batch, int natoms, int ntypes, int m_nei
     char *ws = static_cast<char *>(workspace);
     NbImage *img = reinterpret_cast<NbImage *>(ws + lay.img);
     double *wpos = reinterpret_cast<double *>(ws + lay.wpos);
+    float4 *wpos32 = reinterpret_cast<float4 *>(ws + lay.wpos32);
     int *cell_of = reinterpret_cast<int *>(ws + lay.cell_of);
     int *cell_count = reinterpret_cast<int *>(ws + lay.cell_count);
     int *cell_fill = reinterpret_cast<int *>(ws + lay.cell_fill);
@@ -477,24 +601,24 @@ extern "C" int matpl_neighbor_build(int batch, int natoms, int ntypes, int m_nei
     {
         ProfScope ps("nb_cells", s);
         nb_setup<<<(batch + 127) / 128, 128, 0, s>>>(lattice, img, batch, Rc_M, P.cell_cap);
-        nb_bin<<<grid_for(na, 256), 256, 0, s>>>(frac_pos, img, wpos, cell_of, cell_count, P);
+        nb_bin<<<grid_for(na, 256), 256, 0, s>>>(frac_pos, img, wpos, wpos32, cell_of, cell_count, P);
         nb_scan<<<batch, 1024, 0, s>>>(img, cell_count, cell_start, P);
         nb_fill<<<grid_for(na, 256), 256, 0, s>>>(cell_of, cell_start, cell_fill, cell_atoms, P);
     }
     ProfScope ps("nb_search", s);
     const int S = ntypes * m_neigh;
-    const size_t smem = (size_t)kWarps * S * 5;
+    const size_t smem = (size_t)kWarps * (3 * S * 4 + S);
     if (out_dtype == MATPL_F64) {
         cudaFuncSetAttribute(nb_search<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
         nb_search<double><<<grid_for(na, kWarps), kWarps * 32, smem, s>>>(
-            img, wpos, type_map, cell_start, cell_atoms, list_neigh, (double *)image_dr,
+            img, wpos, wpos32, type_map, cell_start, cell_atoms, list_neigh, (double *)image_dr,
             num_neigh, err_dev, P);
     } else {
         cudaFuncSetAttribute(nb_search<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
         nb_search<float><<<grid_for(na, kWarps), kWarps * 32, smem, s>>>(
-            img, wpos, type_map, cell_start, cell_atoms, list_neigh, (float *)image_dr,
+            img, wpos, wpos32, type_map, cell_start, cell_atoms, list_neigh, (float *)image_dr,
             num_neigh, err_dev, P);
     }
     return check_launch("matpl_neighbor_build");
