@@ -185,7 +185,7 @@ def run_ours(args, ws, rank, local):
     n_pairs = int((ln > 0).sum())
     sub = slice(0, 4000)
     davg, dstd = P.calc_stat(cfg, ln[:, sub].cpu().numpy(), idr[:, sub].cpu().numpy(), st.types[sub])
-    model = dp.DP(cfg, prm, davg, dstd, precision=prec, device=dev)
+    model = dp.DP(cfg, prm, davg, dstd, precision=prec, device=dev, check_errors=False)
     m64 = dp.DP(cfg, prm, davg, dstd, precision="float64", device=dev)
     present = model.present_types(cfg.atom_type)
     tm32 = types_d.to(torch.int32)
@@ -336,7 +336,8 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="float32", choices=["float32", "float64"])
+    ap.add_argument("--precision", default="float32",
+                    choices=["float32", "float64", "mixed", "mixed_fast", "mixed_x3fast"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

@@ -34,8 +34,20 @@ typedef enum {
 /* Codes a kernel writes to err_dev (0 = fine). */
 #define MATPL_KERR_NEIGHBOR_OVERFLOW 1   /* a type block exceeds m (NeighConst.f90:75-78) */
 #define MATPL_KERR_BAD_TYPE 2            /* atom type index outside [0, ntypes) */
+#define MATPL_KERR_TIMEOUT 3             /* a bounded tensor-core completion wait gave up */
 
-typedef enum { MATPL_F32 = 0, MATPL_F64 = 1, MATPL_MIXED = 2 } matpl_dtype;
+/* Compute forms.  MIXED*: FP32 data, embedding GEMMs on the tensor cores (tcgen05, BF16
+ * operands, FP32 accumulation in TMEM), FP64 energy / virial reductions.
+ *   MATPL_MIXED         BF16x3 split operands (hi*hi + hi*lo + lo*hi), CUDA tanhf
+ *   MATPL_MIXED_FAST    single BF16 operands, hardware tanh.approx.f32
+ *   MATPL_MIXED_X3FAST  BF16x3 split operands, hardware tanh.approx.f32 */
+typedef enum {
+    MATPL_F32 = 0,
+    MATPL_F64 = 1,
+    MATPL_MIXED = 2,
+    MATPL_MIXED_FAST = 3,
+    MATPL_MIXED_X3FAST = 4
+} matpl_dtype;
 
 const char *matpl_last_error(void);
 int matpl_version(void);
@@ -116,8 +128,8 @@ int matpl_env_mat(int dtype, int batch, int natoms, int nslots, const int32_t *t
  *
  * Compiled network shape: embedding 1->25->25->25 (tanh, residual on equal widths),
  * M2 = 16, fitting 400->50->50->50->1 (tanh, residual layers 2-3).
- * params: device buffer in matpl_dp_pack_layout order (see matpl_gb300/dp.py: pack_params),
- * in the compute dtype (f64 for MATPL_F64, f32 for MATPL_F32 and MATPL_MIXED).
+ * params: device buffer in the packed layout of matpl_gb300/dp.py: pack_params, in the
+ * compute dtype (f64 for MATPL_F64, f32 for MATPL_F32 and the MATPL_MIXED* forms).
  * ---------------------------------------------------------------------------------- */
 typedef struct {
     int ntypes;             /* model types */
@@ -128,6 +140,7 @@ typedef struct {
     const void *params;     /* packed network parameters (device) */
     const void *davg;       /* [ntypes,4] per centre type (device, compute dtype) */
     const void *dstd;       /* [ntypes,4] */
+    int32_t *err_dev;       /* device int32 for kernel error codes (MATPL_KERR_*), or NULL */
 } matpl_dp_model;
 
 size_t matpl_dp_param_count(int ntypes);

@@ -8,9 +8,10 @@ import os
 
 from . import build as _build
 
-MATPL_F32, MATPL_F64, MATPL_MIXED = 0, 1, 2
+MATPL_F32, MATPL_F64, MATPL_MIXED, MATPL_MIXED_FAST, MATPL_MIXED_X3FAST = 0, 1, 2, 3, 4
 KERR_NEIGHBOR_OVERFLOW = 1
 KERR_BAD_TYPE = 2
+KERR_TIMEOUT = 3
 
 _c = ctypes
 _vp, _i, _d, _sz = _c.c_void_p, _c.c_int, _c.c_double, _c.c_size_t
@@ -19,7 +20,8 @@ _vp, _i, _d, _sz = _c.c_void_p, _c.c_int, _c.c_double, _c.c_size_t
 class MatplDpModel(ctypes.Structure):
     """Mirror of ``matpl_dp_model``."""
     _fields_ = [("ntypes", _i), ("m", _i), ("npresent", _i), ("present", _i * 8),
-                ("rmin", _d), ("rmax", _d), ("params", _vp), ("davg", _vp), ("dstd", _vp)]
+                ("rmin", _d), ("rmax", _d), ("params", _vp), ("davg", _vp), ("dstd", _vp),
+                ("err_dev", _vp)]
 
 
 # name -> (restype, argtypes)

@@ -22,6 +22,18 @@
 #include <algorithm>
 
 namespace matpl {
+int mixed_ga(int S);
+size_t mixed_smem(int ntypes, int S);
+size_t mixed_tile_bytes(int ntypes);
+int prep_mixed_tiles(const float *params, unsigned char *out, int ntypes, cudaStream_t s);
+template <int SPLIT, bool FAST>
+int launch_mixed_embed(bool backward, const int32_t *list_neigh, const float *idr,
+                       const int32_t *type_map, const float *params, const unsigned char *wtiles,
+                       const float *davg, const float *dstd, const float *pad_or_dA,
+                       float *A_or_force, double *atom_vir, int32_t *err, int batch, int natoms,
+                       int nslots, int nghost, int ntypes, int m, int present_mask, double rmin,
+                       double rmax, double inv_mT, cudaStream_t s);
+
 namespace {
 
 using namespace dp;
@@ -685,7 +697,7 @@ __global__ void dp_reduce_final(const double *__restrict__ part, double *__restr
 }
 
 struct DpLayout {
-    size_t A, dA, pad, vir, red, total;
+    size_t A, dA, pad, vir, red, tiles, total;
 };
 
 DpLayout dp_layout(size_t es, int batch, int natoms, int ntypes) {
@@ -697,18 +709,46 @@ DpLayout dp_layout(size_t es, int batch, int natoms, int ntypes) {
     l.pad = o; o = align_up(o + es * (size_t)ntypes * ntypes * NA, 256);
     l.vir = o; o = align_up(o + 8 * na * 9, 256);
     l.red = o; o = align_up(o + 8 * (size_t)batch * kReduceBlocks * 10, 256);
+    l.tiles = o; o = align_up(o + mixed_tile_bytes(ntypes), 256);
     l.total = o;
     return l;
 }
 
 template <typename T>
-int launch_eval(const matpl_dp_model *M, const EvalParams &P, const int32_t *list_neigh,
-                const T *idr, const int32_t *type_map, T *Ei, double *Etot, T *force,
-                double *virial, char *ws, const DpLayout &lay, cudaStream_t s) {
+int run_mixed(int mode, bool backward, const EvalParams &P, const int32_t *ln, const T *idr,
+              const int32_t *tm, const T *params, const unsigned char *wt, const T *davg,
+              const T *dstd, const T *in, T *out, double *avir, int32_t *err, cudaStream_t s) {
+    if (sizeof(T) != 4) return MATPL_ERR_DTYPE;
+    const float *fi = (const float *)idr;
+    const float *fp = (const float *)params, *fa = (const float *)davg, *fs = (const float *)dstd;
+    const float *fin = (const float *)in;
+    float *fo = (float *)out;
+    switch (mode) {
+        case MATPL_MIXED:
+            return launch_mixed_embed<3, false>(backward, ln, fi, tm, fp, wt, fa, fs, fin, fo, avir, err,
+                                                P.batch, P.natoms, P.nslots, P.nghost, P.ntypes,
+                                                P.m, P.present_mask, P.rmin, P.rmax, P.inv_mT, s);
+        case MATPL_MIXED_FAST:
+            return launch_mixed_embed<1, true>(backward, ln, fi, tm, fp, wt, fa, fs, fin, fo, avir, err,
+                                               P.batch, P.natoms, P.nslots, P.nghost, P.ntypes,
+                                               P.m, P.present_mask, P.rmin, P.rmax, P.inv_mT, s);
+        default:
+            return launch_mixed_embed<3, true>(backward, ln, fi, tm, fp, wt, fa, fs, fin, fo, avir, err,
+                                               P.batch, P.natoms, P.nslots, P.nghost, P.ntypes,
+                                               P.m, P.present_mask, P.rmin, P.rmax, P.inv_mT, s);
+    }
+}
+
+template <typename T>
+int launch_eval(int mode, const matpl_dp_model *M, const EvalParams &P,
+                const int32_t *list_neigh, const T *idr, const int32_t *type_map, T *Ei,
+                double *Etot, T *force, double *virial, char *ws, const DpLayout &lay,
+                cudaStream_t s) {
     const T *params = (const T *)M->params;
     const T *davg = (const T *)M->davg, *dstd = (const T *)M->dstd;
     T *A = (T *)(ws + lay.A), *dA = (T *)(ws + lay.dA), *pad = (T *)(ws + lay.pad);
     double *avir = (double *)(ws + lay.vir);
+    unsigned char *wt = (unsigned char *)(ws + lay.tiles);
     const long long total = (long long)P.batch * P.natoms;
     const size_t nall3 = (size_t)P.batch * (P.natoms + P.nghost) * 3;
     if (cudaMemsetAsync(force, 0, sizeof(T) * nall3, s) != cudaSuccess) {
@@ -721,6 +761,8 @@ int launch_eval(const matpl_dp_model *M, const EvalParams &P, const int32_t *lis
         dp_pad<T><<<(nnet + 31) / 32, 32, 0, s>>>(params, davg, dstd, pad, P.ntypes);
     }
 
+    const long long nwarp_blocks = (total + kWarps - 1) / kWarps;
+    const int gridw = (int)(nwarp_blocks < 152LL * 8 ? (nwarp_blocks < 1 ? 1 : nwarp_blocks) : 152LL * 8);
     const size_t wbytes = sizeof(T) * (size_t)nnet * EmbOff::SIZE;
     const bool ws_ok = wbytes <= 128 * 1024;
     const size_t wpart = ws_ok ? wbytes : 0;
@@ -728,15 +770,20 @@ int launch_eval(const matpl_dp_model *M, const EvalParams &P, const int32_t *lis
                           sizeof(int) * kWarps * P.nslots;
     const size_t smem_b = wpart + sizeof(T) * kWarps * (2 * E * 32 + NA) +
                           sizeof(int) * kWarps * P.nslots;
-    const long long nwarp_blocks = (total + kWarps - 1) / kWarps;
-    const int gridw = (int)(nwarp_blocks < 152LL * 8 ? (nwarp_blocks < 1 ? 1 : nwarp_blocks) : 152LL * 8);
     auto kf = ws_ok ? dp_embed_fwd<T, true> : dp_embed_fwd<T, false>;
     auto kb = ws_ok ? dp_embed_bwd<T, true> : dp_embed_bwd<T, false>;
-    cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f);
-    cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
-    {
+    int st = MATPL_OK;
+    if (mode == MATPL_F32 || mode == MATPL_F64) {
+        cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f);
+        cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
         ProfScope ps("dp_embed_fwd", s);
         kf<<<gridw, kWarps * 32, smem_f, s>>>(list_neigh, idr, type_map, params, davg, dstd, pad, A, P);
+    } else {
+        st = prep_mixed_tiles((const float *)params, wt, P.ntypes, s);
+        if (st) return st;
+        st = run_mixed(mode, false, P, list_neigh, idr, type_map, params, wt, davg, dstd, pad, A,
+                       nullptr, M->err_dev, s);
+        if (st) return st;
     }
     constexpr int TILE = sizeof(T) == 8 ? 32 : 64;
     const size_t smem_fit = sizeof(T) * (size_t)TILE * (NA + DIN + 4 * F);
@@ -747,10 +794,14 @@ int launch_eval(const matpl_dp_model *M, const EvalParams &P, const int32_t *lis
         ProfScope ps("dp_fit", s);
         dp_fit<T, TILE><<<gridf, 256, smem_fit, s>>>(A, type_map, params, Ei, dA, P);
     }
-    {
+    if (mode == MATPL_F32 || mode == MATPL_F64) {
         ProfScope ps("dp_embed_bwd", s);
         kb<<<gridw, kWarps * 32, smem_b, s>>>(list_neigh, idr, type_map, params, davg, dstd, dA,
                                               force, avir, P);
+    } else {
+        st = run_mixed(mode, true, P, list_neigh, idr, type_map, params, wt, davg, dstd, dA,
+                       force, avir, M->err_dev, s);
+        if (st) return st;
     }
     {
         ProfScope ps("dp_reduce", s);
@@ -782,8 +833,8 @@ extern "C" int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, 
                              double *Etot, void *force, double *virial, void *workspace,
                              size_t workspace_bytes, void *stream) {
     MATPL_REQUIRE(model != nullptr, MATPL_ERR_INVALID, "model is NULL");
-    MATPL_REQUIRE(dtype == MATPL_F32 || dtype == MATPL_F64, MATPL_ERR_DTYPE,
-                  "matpl_dp_eval: dtype must be MATPL_F32 or MATPL_F64 for this entry point");
+    MATPL_REQUIRE(dtype >= MATPL_F32 && dtype <= MATPL_MIXED_X3FAST, MATPL_ERR_DTYPE,
+                  "matpl_dp_eval: unknown dtype / compute form");
     MATPL_REQUIRE(model->ntypes >= 1 && model->ntypes <= 16, MATPL_ERR_UNSUPPORTED,
                   "ntypes must be in [1, 16]");
     MATPL_REQUIRE(model->npresent >= 1 && model->npresent <= kMaxPresent, MATPL_ERR_INVALID,
@@ -817,10 +868,17 @@ extern "C" int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, 
         if (nghost) cudaMemsetAsync(force, 0, es * 3 * (size_t)batch * nghost, s);
         return check_launch("matpl_dp_eval");
     }
+    if (dtype >= MATPL_MIXED) {
+        MATPL_REQUIRE(model->ntypes <= 15, MATPL_ERR_UNSUPPORTED,
+                      "mixed-precision forms support up to 15 types");
+        MATPL_REQUIRE(mixed_smem(model->ntypes, nslots) <= 220 * 1024, MATPL_ERR_UNSUPPORTED,
+                      "mixed-precision form: too many slots for the shared-memory pair list");
+    }
     if (dtype == MATPL_F64)
-        return launch_eval<double>(model, P, list_neigh, (const double *)image_dr, type_map,
-                                   (double *)Ei, Etot, (double *)force, virial,
+        return launch_eval<double>(dtype, model, P, list_neigh, (const double *)image_dr,
+                                   type_map, (double *)Ei, Etot, (double *)force, virial,
                                    (char *)workspace, lay, s);
-    return launch_eval<float>(model, P, list_neigh, (const float *)image_dr, type_map,
-                              (float *)Ei, Etot, (float *)force, virial, (char *)workspace, lay, s);
+    return launch_eval<float>(dtype, model, P, list_neigh, (const float *)image_dr, type_map,
+                              (float *)Ei, Etot, (float *)force, virial, (char *)workspace, lay,
+                              s);
 }

@@ -20,7 +20,17 @@ from typing import Dict, List, Optional
 import torch
 
 from . import _lib
-from ._lib import MATPL_F32, MATPL_F64, MatplDpModel, check, ptr
+from ._lib import (MATPL_F32, MATPL_F64, MATPL_MIXED, MATPL_MIXED_FAST, MATPL_MIXED_X3FAST,
+                   MatplDpModel, check, ptr)
+
+# precision name -> (C ABI compute form, storage dtype)
+PRECISIONS = {
+    "float64": (MATPL_F64, torch.float64),
+    "float32": (MATPL_F32, torch.float32),
+    "mixed": (MATPL_MIXED, torch.float32),              # tcgen05 BF16x3 GEMMs, tanhf
+    "mixed_fast": (MATPL_MIXED_FAST, torch.float32),    # tcgen05 BF16 GEMMs, tanh.approx
+    "mixed_x3fast": (MATPL_MIXED_X3FAST, torch.float32),  # tcgen05 BF16x3 GEMMs, tanh.approx
+}
 from .params import DPConfig
 
 E, M2, DIN, F = 25, 16, 400, 50
@@ -107,17 +117,25 @@ def per_type_stats(arr: torch.Tensor, ntypes: int) -> torch.Tensor:
 
 
 class DP(torch.nn.Module):
-    """Inference DP se_e2_a on GB300.  ``precision``: "float64" | "float32"."""
+    """Inference DP se_e2_a on GB300.
+
+    ``precision``: "float64" | "float32" (plain SIMT forms) | "mixed" | "mixed_fast" |
+    "mixed_x3fast" (embedding GEMMs on the tcgen05 tensor cores, FP32 data, FP64 energy /
+    virial sums).  ``check_errors`` reads the kernels' error word after every call (one
+    device sync); the benchmark turns it off inside its timed loop."""
 
     def __init__(self, cfg: DPConfig, params: Dict[str, torch.Tensor], davg, dstd,
-                 precision: str = "float64", device="cuda"):
+                 precision: str = "float64", device="cuda", check_errors: bool = True):
         super().__init__()
         check_shape(cfg)
+        if precision not in PRECISIONS:
+            raise _lib.MatplError(f"unknown precision {precision!r}; one of {list(PRECISIONS)}")
         self.cfg = cfg
         self.precision = precision
-        self.dtype = {"float64": torch.float64, "float32": torch.float32}[precision]
-        self.code = MATPL_F64 if self.dtype == torch.float64 else MATPL_F32
+        self.code, self.dtype = PRECISIONS[precision]
+        self.check_errors = check_errors
         dev = torch.device(device)
+        self.register_buffer("err", torch.zeros(1, dtype=torch.int32, device=dev))
         self.device = dev
         self.register_buffer("packed", pack_params(cfg, params, self.dtype).to(dev))
         davg = torch.as_tensor(davg)
@@ -140,6 +158,7 @@ class DP(torch.nn.Module):
             m.present[q] = t
         m.rmin, m.rmax = float(self.cfg.Rmin), float(self.cfg.Rmax)
         m.params, m.davg, m.dstd = ptr(self.packed), ptr(self.davg4), ptr(self.dstd4)
+        m.err_dev = ptr(self.err)
         return m
 
     def _grouped_perm(self, tmap: torch.Tensor, present: List[int]) -> torch.Tensor:
@@ -178,6 +197,11 @@ class DP(torch.nn.Module):
                                 ptr(tm), ptr(out["Ei_atom"]), ptr(out["Etot"]), ptr(out["Force"]),
                                 ptr(out["Virial"]), ptr(ws), ws.numel(),
                                 torch.cuda.current_stream(dev).cuda_stream), "matpl_dp_eval")
+        if self.check_errors:
+            code = int(self.err.item())
+            if code:
+                self.err.zero_()
+                raise _lib.MatplError(f"matpl_dp_eval kernel error code {code}")
         return out
 
     def forward(self, list_neigh, Imagetype_map, atom_type, ImageDR, nghost: int = 0,

