@@ -111,6 +111,23 @@ int matpl_neighbor_build(int batch, int natoms, int ntypes, int m_neigh, double 
                          void *image_dr, int32_t *num_neigh, int32_t *err_dev,
                          void *workspace, size_t workspace_bytes, void *stream);
 
+/* Allocation-free variant of matpl_neighbor_build.  It has no counterpart in the reference.
+ * For hosts that cannot give this library device memory (an MD engine's per-step force
+ * callback that owns all device memory through its own pool, or a C / Fortran host without a
+ * device allocator at hand; cudaMalloc would also stall the whole device every step).  Its
+ * scratch is a fixed 4 MiB array inside the library (present on every GPU that loads it, held
+ * until the process exits): calls needing more (about 65,000 atoms, batch x natoms) return
+ * MATPL_ERR_WORKSPACE without launching.  The first call on a device looks up that array's
+ * device address (set-up), so make the first call before any stream capture.  All calls share
+ * the array and it keeps the previous call's contents (the call clears what must start at
+ * zero itself); calls that overlap on the GPU race on it, so serialise them.  Allocates no
+ * memory.  Arguments and outputs as matpl_neighbor_build. */
+int matpl_neighbor_build_noalloc(int batch, int natoms, int ntypes, int m_neigh, double Rc_M,
+                                 const double *Rc_type, const int32_t *type_map,
+                                 const double *lattice, const double *frac_pos, int out_dtype,
+                                 int32_t *list_neigh, void *image_dr, int32_t *num_neigh,
+                                 int32_t *err_dev, void *stream);
+
 /* ------------------------------------------------------------------------------------
  * Environment matrix.  Replaces DP.calculate_Ri (src/model/dp_dp.py:217-302):
  *   Ri [B,N,S,4] = (Ri_raw - davg[t_i]) / dstd[t_i],  Ri_d [B,N,S,4,3] = -dRi/d(dR) / dstd

@@ -38,6 +38,8 @@ SIGNATURES = {
     "matpl_neighbor_workspace_bytes": (_sz, [_i, _i]),
     "matpl_neighbor_build": (_i, [_i, _i, _i, _i, _d, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp,
                                   _vp, _vp, _sz, _vp]),
+    "matpl_neighbor_build_noalloc": (_i, [_i, _i, _i, _i, _d, _vp, _vp, _vp, _vp, _i, _vp, _vp,
+                                          _vp, _vp, _vp]),
     "matpl_env_mat": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _d, _d, _vp, _vp, _vp]),
     "matpl_dp_param_count": (_sz, [_i]),
     "matpl_dp_workspace_bytes": (_sz, [_i, _i, _i]),

@@ -15,6 +15,8 @@
 //  * All pair arithmetic is evaluated in the Fortran source order with explicit
 //    round-to-nearest intrinsics (no FMA contraction), so dR and the accept / reject
 //    decisions are bit-identical to the restatement in plain C.
+#include <mutex>
+#include <string>
 #include "common.cuh"
 
 namespace matpl {
@@ -643,4 +645,63 @@ extern "C" int matpl_env_mat(int dtype, int batch, int natoms, int nslots,
             type_map, (const float *)image_dr, (const float *)davg, (const float *)dstd,
             (float)rmin, (float)rmax, (float *)Ri, (float *)Ri_d, batch, natoms, nslots);
     return check_launch("matpl_env_mat");
+}
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free neighbor search.  Some hosts cannot hand this library device memory: an MD
+// engine's per-step force callback that owns all device memory through its own pool (or a C /
+// Fortran host with no device allocator at hand) must not call cudaMalloc, which also blocks
+// the whole device while it runs.  matpl_neighbor_build_noalloc keeps its scratch in the
+// fixed array below (one copy on every GPU that loads this library, kept until the process
+// exits) and otherwise runs exactly matpl_neighbor_build.
+namespace {
+constexpr size_t kNoAllocScratchBytes = 4u << 20;          // 4 MiB: ~65,000 atoms per call
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_nb_scratch[kNoAllocScratchBytes];
+
+extern "C" int matpl_neighbor_build_noalloc(int batch, int natoms, int ntypes, int m_neigh,
+                                            double Rc_M, const double *Rc_type,
+                                            const int32_t *type_map, const double *lattice,
+                                            const double *frac_pos, int out_dtype,
+                                            int32_t *list_neigh, void *image_dr,
+                                            int32_t *num_neigh, int32_t *err_dev, void *stream) {
+    MATPL_REQUIRE(batch >= 0 && natoms >= 0, MATPL_ERR_INVALID, "negative size");
+    const size_t need = nb_layout(batch, natoms).total;
+    MATPL_REQUIRE(need <= kNoAllocScratchBytes, MATPL_ERR_WORKSPACE,
+                  "matpl_neighbor_build_noalloc: " + std::to_string(batch) + " x " +
+                      std::to_string(natoms) + " atoms need " + std::to_string(need) +
+                      " scratch bytes, above its fixed 4 MiB (about 65,000 atoms per call); use "
+                      "matpl_neighbor_build with a caller workspace");
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoAllocMaxDevices) {
+        set_error("matpl_neighbor_build_noalloc: no usable current device");
+        return MATPL_ERR_CUDA;
+    }
+    void *scratch = nullptr;
+    {
+        // Set-up on the first call on each device (with that device current): the array's
+        // name is only a host-side handle, so look up its device address once.
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (g_noalloc_ptr[dev] == nullptr) {
+            void *p = nullptr;
+            const cudaError_t e = cudaGetSymbolAddress(&p, g_nb_scratch);
+            if (e != cudaSuccess || p == nullptr) {
+                set_error(std::string("matpl_neighbor_build_noalloc: cudaGetSymbolAddress failed: ") +
+                          cudaGetErrorString(e));
+                return MATPL_ERR_CUDA;
+            }
+            g_noalloc_ptr[dev] = p;
+        }
+        scratch = g_noalloc_ptr[dev];
+    }
+    // matpl_neighbor_build clears the parts of the scratch that must start at zero (cell
+    // counters) on the stream before its kernels run, so stale contents of the previous call
+    // do not matter.
+    return matpl_neighbor_build(batch, natoms, ntypes, m_neigh, Rc_M, Rc_type, type_map, lattice,
+                                frac_pos, out_dtype, list_neigh, image_dr, num_neigh, err_dev,
+                                scratch, kNoAllocScratchBytes, stream);
 }
