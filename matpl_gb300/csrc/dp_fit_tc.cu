@@ -1,0 +1,403 @@
+// Mixed-precision DP fitting net (and its adjoint) on the tcgen05 tensor cores.
+//
+// Same math as dp_fused.cu's dp_fit (src/model/dp_embedding.py:140-163 and dp_dp.py:304-342 plus
+// the autograd adjoint down to dE/dA): per atom D = A^T A[:, :16] (400), Ei = fit(D), dE/dA.
+// A CTA of 128 threads owns a tile of 128 atoms (thread r = atom r, MMA M = 128):
+//
+//   layer 1  h1 = D W0: 13 K-chunks of 32; each chunk of D is built on the SIMT cores from the
+//            atom's A (kept in shared memory) and double-buffered into the MMA (N = 64, the 50
+//            outputs padded), FP32 accumulator in 64 TMEM columns.
+//   layers 2, 3 (50 x 50 padded to 64 x 64) and the two transposed GEMMs of the adjoint run as
+//            single MMAs (K = 64); tanh / residual / bias on SIMT; tanh outputs kept in shared
+//            memory for the adjoint.
+//   dE/dD = g1 W0^T (N = 400) in 7 chunks of 64 columns, each consumed straight from TMEM into
+//            dE/dA = sum_q dD[p][q] A[c][q] + sum_p' dD[p'][p] A[c][p'].
+// BF16x3 (hi/lo split) operands keep FP32-level accuracy; weight tiles are prepared once per
+// call in global memory (prep_fit_tiles).  Every mbarrier wait is bounded (MATPL_KERR_TIMEOUT).
+#include "common.cuh"
+#include "dp_layout.cuh"
+#include "tc.cuh"
+
+namespace matpl {
+namespace {
+
+using namespace dp;
+constexpr int FM = 128;                   // atoms per tile = threads
+constexpr int FN = 64;                    // padded fitting width
+constexpr int K1C = 13;                   // K chunks of layer 1 (32 each; 400 padded to 416)
+constexpr int NDC = 7;                    // N chunks of dE/dD (64 each; 400 padded to 448)
+constexpr int XKS = FM / 8 * 128;         // K-chunk stride of a 128-row activation tile (2048 B)
+constexpr int BKS = FN / 8 * 128;         // K-chunk stride of a 64-row weight tile (1024 B)
+constexpr int X32 = FM * 32 * 2;          // 128 x 32 bf16 tile (8 KB)
+constexpr int X64 = FM * 64 * 2;          // 128 x 64 bf16 tile (16 KB)
+constexpr int W32 = FN * 32 * 2;          // 64 x 32 bf16 weight tile (4 KB)
+constexpr int W64 = FN * 64 * 2;          // 64 x 64 bf16 weight tile (8 KB)
+constexpr int ASTR = NA + 1;              // A row stride in shared memory (floats)
+constexpr int kWait = 1 << 24;
+
+// Per-net tile offsets in the prepared buffer (each entry is a hi tile followed by a lo tile).
+constexpr size_t OFF_F0 = 0;                                  // [13] 64 x 32: B[n=o][k] = W0[32c+k][o]
+constexpr size_t OFF_F1 = OFF_F0 + (size_t)K1C * 2 * W32;     // 64 x 64: B[n=o][k=i] = W1[i][o]
+constexpr size_t OFF_F2 = OFF_F1 + 2 * W64;                   // W2 likewise
+constexpr size_t OFF_B2 = OFF_F2 + 2 * W64;                   // B[n=i][k=o] = W2[i][o]
+constexpr size_t OFF_B1 = OFF_B2 + 2 * W64;                   // B[n=i][k=o] = W1[i][o]
+constexpr size_t OFF_B0 = OFF_B1 + 2 * W64;                   // [7] 64 x 64: B[n=kD][k=o] = W0[64c+n][o]
+constexpr size_t FIT_TILE_BYTES = OFF_B0 + (size_t)NDC * 2 * W64;
+
+__device__ __forceinline__ void put_hilo(unsigned char *hi, unsigned char *lo, uint32_t off,
+                                         float v) {
+    const __nv_bfloat16 h = __float2bfloat16_rn(v);
+    *reinterpret_cast<__nv_bfloat16 *>(hi + off) = h;
+    *reinterpret_cast<__nv_bfloat16 *>(lo + off) = __float2bfloat16_rn(v - __bfloat162float(h));
+}
+
+__global__ void prep_fit_tiles(const float *__restrict__ params, unsigned char *__restrict__ out,
+                               int ntypes) {
+    const long long woff = (long long)ntypes * ntypes * EmbOff::SIZE;
+    // work items: per net, (13 + 7) chunks x 64 x 64 elements + 4 matrices x 64 x 64
+    const int per_net = (K1C * 32 + NDC * 64 + 4 * 64) * FN;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+         q < (long long)ntypes * per_net; q += (long long)gridDim.x * blockDim.x) {
+        const int t = (int)(q / per_net);
+        int r = (int)(q - (long long)t * per_net);
+        const float *fw = params + woff + (long long)t * FitOff::SIZE;
+        unsigned char *base = out + (size_t)t * FIT_TILE_BYTES;
+        const int n = r % FN;                 // weight-tile row
+        int k = r / FN;                       // running K index over all tiles of the net
+        if (k < K1C * 32) {                   // layer-1 chunks (K = 32 each)
+            const int c = k / 32, kk = k % 32, kD = 32 * c + kk;
+            const float v = (kD < DIN && n < F) ? fw[FitOff::W0 + kD * F + n] : 0.f;
+            unsigned char *hi = base + OFF_F0 + (size_t)c * 2 * W32;
+            put_hilo(hi, hi + W32, tc::tile_off(n, kk, BKS), v);
+            continue;
+        }
+        k -= K1C * 32;
+        if (k < 4 * 64) {                     // the four 64 x 64 hidden-layer tiles
+            const int mat = k / 64, kk = k % 64;
+            float v = 0.f;
+            if (n < F && kk < F) {
+                switch (mat) {
+                    case 0: v = fw[FitOff::W1 + kk * F + n]; break;   // F1: W1[i=kk][o=n]
+                    case 1: v = fw[FitOff::W2 + kk * F + n]; break;   // F2
+                    case 2: v = fw[FitOff::W2 + n * F + kk]; break;   // B2: W2[i=n][o=kk]
+                    default: v = fw[FitOff::W1 + n * F + kk]; break;  // B1
+                }
+            }
+            const size_t offs[4] = {OFF_F1, OFF_F2, OFF_B2, OFF_B1};
+            unsigned char *hi = base + offs[mat];
+            put_hilo(hi, hi + W64, tc::tile_off(n, kk, BKS), v);
+            continue;
+        }
+        k -= 4 * 64;                          // dE/dD chunks: N = 64 rows of D index, K = o
+        const int c = k / 64, kk = k % 64, kD = 64 * c + n;
+        const float v = (kD < DIN && kk < F) ? fw[FitOff::W0 + kD * F + kk] : 0.f;
+        unsigned char *hi = base + OFF_B0 + (size_t)c * 2 * W64;
+        put_hilo(hi, hi + W64, tc::tile_off(n, kk, BKS), v);
+    }
+}
+
+__device__ __forceinline__ void copy_tiles(const unsigned char *__restrict__ src, unsigned char *dst,
+                                           int bytes) {
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
+    uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+    for (int q = threadIdx.x; q < bytes / 16; q += blockDim.x) d4[q] = __ldg(s4 + q);
+}
+
+// Row r of a 128-row K-major tile: NK values as BF16 hi and lo halves.
+template <int NK>
+__device__ __forceinline__ void store_row_hilo(unsigned char *hi, unsigned char *lo, int r,
+                                               const float *v) {
+#pragma unroll
+    for (int c = 0; c < NK / 8; ++c) {
+        float h[8], l[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            h[q] = v[8 * c + q];
+            l[q] = v[8 * c + q] - __bfloat162float(__float2bfloat16_rn(v[8 * c + q]));
+        }
+        tc::store_row8(hi, r, c, XKS, h);
+        tc::store_row8(lo, r, c, XKS, l);
+    }
+}
+
+// Shared memory written by the threads becomes visible to the tensor core, and prior TMEM
+// reads are ordered before the next MMA.
+__device__ __forceinline__ void mma_sync_point() {
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+}
+
+// D[128 x 64] (+)= X W with BF16x3 operands; KCH K-steps of 16.
+template <int KCH>
+__device__ __forceinline__ void issue_split3(uint32_t tmem, const unsigned char *xh,
+                                             const unsigned char *xl, const unsigned char *wh,
+                                             const unsigned char *wl, bool accumulate) {
+    const uint32_t id = tc::idesc_bf16(FM, FN);
+    const uint32_t a[2] = {tc::smem_u32(xh), tc::smem_u32(xl)};
+    const uint32_t b[2] = {tc::smem_u32(wh), tc::smem_u32(wl)};
+    uint32_t acc = accumulate ? 1u : 0u;
+#pragma unroll
+    for (int p = 0; p < 3; ++p) {
+        const uint32_t xa = a[p == 2 ? 1 : 0], wb = b[p == 1 ? 1 : 0];
+#pragma unroll
+        for (int kk = 0; kk < KCH; ++kk) {
+            tc::mma_bf16(tmem, tc::desc_kmajor(xa + kk * 2 * XKS, XKS, 128),
+                         tc::desc_kmajor(wb + kk * 2 * BKS, BKS, 128), id, acc);
+            acc = 1u;
+        }
+    }
+}
+
+__device__ __forceinline__ void ld64(uint32_t tmem, float v[64]) {
+    const uint32_t base = tmem + ((uint32_t)((threadIdx.x >> 5) * 32) << 16);
+    tc::tmem_ld32(base, v);
+    tc::tmem_ld32(base + 32, v + 32);
+}
+
+template <bool FAST>
+__device__ __forceinline__ float fit_act(float x) {
+    if (FAST) return tc::tanh_fast(x);
+    return tanhf(x);
+}
+
+constexpr size_t FIT_SMEM = sizeof(float) * (FM * ASTR + 3 * F * FM) + 2 * X64 + 2 * W64;
+
+template <bool FAST>
+__global__ void __launch_bounds__(FM, 1)
+dp_fit_tc(const float *__restrict__ Ain, const int32_t *__restrict__ type_map,
+          const float *__restrict__ params, const unsigned char *__restrict__ ftiles,
+          float *__restrict__ Ei, float *__restrict__ dAout, int32_t *__restrict__ err,
+          int batch, int natoms, int ntypes, int present_mask) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ uint32_t tmem_base;
+    __shared__ int rtype[FM];
+    __shared__ int tflag[16];
+    __shared__ float vec[6 * FN + 4];
+    float *As = reinterpret_cast<float *>(smem_raw);
+    float *Tsm = As + FM * ASTR;                                   // [3][F][FM]
+    unsigned char *XB = reinterpret_cast<unsigned char *>(Tsm + 3 * F * FM);
+    unsigned char *WB = XB + 2 * X64;
+    const int r = threadIdx.x, warp = r >> 5;
+    if (r == 0) {
+        tc::mbar_init(&mbar[0], 1);
+        tc::mbar_init(&mbar[1], 1);
+    }
+    if (warp == 0) tc::tmem_alloc(&tmem_base, 64);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = tmem_base;
+    uint32_t ph[2] = {0u, 0u};
+    bool ok = true;
+    const long long total = (long long)batch * natoms;
+    const long long ntiles = (total + FM - 1) / FM;
+    const long long woff = (long long)ntypes * ntypes * EmbOff::SIZE;
+    const int vsrc[6] = {FitOff::B0, FitOff::B1, FitOff::DT1, FitOff::B2, FitOff::DT2, FitOff::W3};
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long long t0 = tile * FM, t = t0 + r;
+        const bool valid = t < total;
+        __syncthreads();
+        if (r < 16) tflag[r] = 0;
+        __syncthreads();
+        int ty = -1;
+        if (valid) {
+            ty = type_map[(int)(t % natoms)];
+            if (ty < 0 || ty >= ntypes || !((present_mask >> ty) & 1)) ty = -1;
+        }
+        rtype[r] = ty;
+        if (ty >= 0) tflag[ty] = 1;
+        for (int q = r; q < FM * NA; q += FM) {
+            const int row = q / NA, e = q - row * NA;
+            As[row * ASTR + e] = (t0 + row < total) ? Ain[(t0 + row) * NA + e] : 0.f;
+        }
+        __syncthreads();
+        const float *a = As + r * ASTR;
+        for (int tt = 0; tt < ntypes; ++tt) {
+            if (!tflag[tt]) continue;
+            const float *fw = params + woff + (long long)tt * FitOff::SIZE;
+            const unsigned char *tw = ftiles + (size_t)tt * FIT_TILE_BYTES;
+            __syncthreads();
+            for (int q = r; q < 6 * FN; q += FM) {
+                const int part = q / FN, o = q - part * FN;
+                vec[q] = o < F ? fw[vsrc[part] + o] : 0.f;
+            }
+            if (r == 0) vec[6 * FN] = fw[FitOff::B3];
+            __syncthreads();
+            const bool mine = valid && rtype[r] == tt;
+            // ---- layer 1: 13 double-buffered K chunks of D W0
+            for (int c = 0; c < K1C; ++c) {
+                const int b = c & 1;
+                if (c >= 2) {
+                    ok &= tc::mbar_wait(&mbar[b], ph[b], kWait);
+                    ph[b] ^= 1u;
+                }
+                copy_tiles(tw + OFF_F0 + (size_t)c * 2 * W32, WB + b * 2 * W32, 2 * W32);
+                float d[32];
+#pragma unroll
+                for (int kk = 0; kk < 32; ++kk) {
+                    const int k = 32 * c + kk, p = k >> 4, q = k & 15;
+                    d[kk] = k < DIN ? a[p] * a[q] + a[E + p] * a[E + q] + a[2 * E + p] * a[2 * E + q] +
+                                          a[3 * E + p] * a[3 * E + q]
+                                    : 0.f;
+                }
+                unsigned char *xh = XB + b * 2 * X32;
+                store_row_hilo<32>(xh, xh + X32, r, d);
+                mma_sync_point();
+                if (r == 0) {
+                    issue_split3<2>(tmem, xh, xh + X32, WB + b * 2 * W32, WB + b * 2 * W32 + W32, c > 0);
+                    tc::commit(&mbar[b]);
+                }
+            }
+            ok &= tc::mbar_wait(&mbar[1], ph[1], kWait);
+            ph[1] ^= 1u;
+            ok &= tc::mbar_wait(&mbar[0], ph[0], kWait);
+            ph[0] ^= 1u;
+            tc::fence_after_sync();
+            float h[64], x[64];
+            ld64(tmem, h);
+#pragma unroll
+            for (int o = 0; o < 64; ++o) {
+                x[o] = o < F ? fit_act<FAST>(h[o] + vec[o]) : 0.f;
+                if (o < F) Tsm[o * FM + r] = x[o];
+            }
+            // ---- layers 2, 3
+#pragma unroll 1
+            for (int l = 1; l <= 2; ++l) {
+                store_row_hilo<64>(XB, XB + X64, r, x);
+                copy_tiles(tw + (l == 1 ? OFF_F1 : OFF_F2), WB, 2 * W64);
+                mma_sync_point();
+                if (r == 0) {
+                    issue_split3<4>(tmem, XB, XB + X64, WB, WB + W64, false);
+                    tc::commit(&mbar[0]);
+                }
+                ok &= tc::mbar_wait(&mbar[0], ph[0], kWait);
+                ph[0] ^= 1u;
+                tc::fence_after_sync();
+                ld64(tmem, h);
+                const float *bias = vec + (l == 1 ? FN : 3 * FN);
+                const float *dt = vec + (l == 1 ? 2 * FN : 4 * FN);
+                float *T = Tsm + l * F * FM;
+#pragma unroll
+                for (int o = 0; o < F; ++o) {
+                    const float tv = fit_act<FAST>(h[o] + bias[o]);
+                    T[o * FM + r] = tv;
+                    x[o] = tv * dt[o] + x[o];
+                }
+            }
+            float e = vec[6 * FN];
+#pragma unroll
+            for (int o = 0; o < F; ++o) e += x[o] * vec[5 * FN + o];
+            if (mine) Ei[t] = e;
+            // ---- adjoint: dx3 = W3; through layers 3 and 2
+#pragma unroll
+            for (int o = 0; o < F; ++o) x[o] = vec[5 * FN + o];
+#pragma unroll 1
+            for (int l = 2; l >= 1; --l) {
+                const float *T = Tsm + l * F * FM;
+                const float *dt = vec + (l == 2 ? 4 * FN : 2 * FN);
+#pragma unroll
+                for (int o = 0; o < 64; ++o) {
+                    const float tv = o < F ? T[o * FM + r] : 0.f;
+                    h[o] = o < F ? x[o] * dt[o] * (1.f - tv * tv) : 0.f;
+                }
+                store_row_hilo<64>(XB, XB + X64, r, h);
+                copy_tiles(tw + (l == 2 ? OFF_B2 : OFF_B1), WB, 2 * W64);
+                mma_sync_point();
+                if (r == 0) {
+                    issue_split3<4>(tmem, XB, XB + X64, WB, WB + W64, false);
+                    tc::commit(&mbar[0]);
+                }
+                ok &= tc::mbar_wait(&mbar[0], ph[0], kWait);
+                ph[0] ^= 1u;
+                tc::fence_after_sync();
+                ld64(tmem, h);
+#pragma unroll
+                for (int o = 0; o < F; ++o) x[o] += h[o];
+            }
+#pragma unroll
+            for (int o = 0; o < 64; ++o) {
+                const float tv = o < F ? Tsm[o * FM + r] : 0.f;
+                h[o] = o < F ? x[o] * (1.f - tv * tv) : 0.f;
+            }
+            store_row_hilo<64>(XB, XB + X64, r, h);
+            // ---- dE/dD = g1 W0^T in 7 chunks of 64 D entries, folded into dE/dA
+            float acc2[4][16];
+#pragma unroll
+            for (int c4 = 0; c4 < 4; ++c4)
+#pragma unroll
+                for (int q = 0; q < 16; ++q) acc2[c4][q] = 0.f;
+#pragma unroll 1
+            for (int c = 0; c < NDC; ++c) {
+                copy_tiles(tw + OFF_B0 + (size_t)c * 2 * W64, WB, 2 * W64);
+                mma_sync_point();
+                if (r == 0) {
+                    issue_split3<4>(tmem, XB, XB + X64, WB, WB + W64, false);
+                    tc::commit(&mbar[0]);
+                }
+                ok &= tc::mbar_wait(&mbar[0], ph[0], kWait);
+                ph[0] ^= 1u;
+                tc::fence_after_sync();
+                ld64(tmem, h);                        // h[n] = dE/dD[64c + n]
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const int p = 4 * c + j;
+                    if (p >= E) break;
+#pragma unroll
+                    for (int c4 = 0; c4 < 4; ++c4) {
+                        float s = 0.f;
+                        const float ap = a[c4 * E + p];
+#pragma unroll
+                        for (int q = 0; q < M2; ++q) {
+                            s += h[16 * j + q] * a[c4 * E + q];
+                            acc2[c4][q] += h[16 * j + q] * ap;
+                        }
+                        if (mine) dAout[t * NA + c4 * E + p] = s;
+                    }
+                }
+            }
+            if (mine) {
+#pragma unroll
+                for (int c4 = 0; c4 < 4; ++c4)
+#pragma unroll
+                    for (int q = 0; q < M2; ++q) dAout[t * NA + c4 * E + q] += acc2[c4][q];
+            }
+        }
+        if (valid && rtype[r] < 0) {
+            Ei[t] = 0.f;
+            for (int q = 0; q < NA; ++q) dAout[t * NA + q] = 0.f;
+        }
+    }
+    if (!ok) atomicMax(err, MATPL_KERR_TIMEOUT);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, 64);
+}
+
+}  // namespace
+
+size_t fit_tile_bytes(int ntypes) { return (size_t)ntypes * FIT_TILE_BYTES; }
+
+// Prepares the BF16 fitting tiles of every type into `tiles`, then runs the fitting kernel.
+int launch_fit_tc(bool fast, const float *A, const int32_t *type_map, const float *params,
+                  unsigned char *tiles, float *Ei, float *dA, int32_t *err, int batch, int natoms,
+                  int ntypes, int present_mask, cudaStream_t s) {
+    {
+        ProfScope ps("prep_fit_tiles", s);
+        const long long n = (long long)ntypes * (K1C * 32 + NDC * 64 + 4 * 64) * FN;
+        prep_fit_tiles<<<(int)((n + 255) / 256), 256, 0, s>>>(params, tiles, ntypes);
+    }
+    const long long total = (long long)batch * natoms;
+    const long long ntiles = (total + FM - 1) / FM;
+    const int grid = (int)(ntiles < 152 ? ntiles : 152);
+    auto k = fast ? dp_fit_tc<true> : dp_fit_tc<false>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FIT_SMEM);
+    ProfScope ps("dp_fit_tc", s);
+    k<<<grid, FM, FIT_SMEM, s>>>(A, type_map, params, tiles, Ei, dA, err, batch, natoms, ntypes,
+                                 present_mask);
+    return check_launch("dp_fit_tc");
+}
+
+}  // namespace matpl

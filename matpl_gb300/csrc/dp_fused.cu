@@ -26,6 +26,10 @@ int mixed_ga(int S);
 size_t mixed_smem(int ntypes, int S);
 size_t mixed_tile_bytes(int ntypes);
 int prep_mixed_tiles(const float *params, unsigned char *out, int ntypes, cudaStream_t s);
+size_t fit_tile_bytes(int ntypes);
+int launch_fit_tc(bool fast, const float *A, const int32_t *type_map, const float *params,
+                  unsigned char *tiles, float *Ei, float *dA, int32_t *err, int batch, int natoms,
+                  int ntypes, int present_mask, cudaStream_t s);
 template <int SPLIT, bool FAST>
 int launch_mixed_embed(bool backward, const int32_t *list_neigh, const float *idr,
                        const int32_t *type_map, const float *params, const unsigned char *wtiles,
@@ -697,7 +701,7 @@ __global__ void dp_reduce_final(const double *__restrict__ part, double *__restr
 }
 
 struct DpLayout {
-    size_t A, dA, pad, vir, red, tiles, total;
+    size_t A, dA, pad, vir, red, tiles, ftiles, total;
 };
 
 DpLayout dp_layout(size_t es, int batch, int natoms, int ntypes) {
@@ -710,6 +714,7 @@ DpLayout dp_layout(size_t es, int batch, int natoms, int ntypes) {
     l.vir = o; o = align_up(o + 8 * na * 9, 256);
     l.red = o; o = align_up(o + 8 * (size_t)batch * kReduceBlocks * 10, 256);
     l.tiles = o; o = align_up(o + mixed_tile_bytes(ntypes), 256);
+    l.ftiles = o; o = align_up(o + fit_tile_bytes(ntypes), 256);
     l.total = o;
     return l;
 }
@@ -790,9 +795,14 @@ int launch_eval(int mode, const matpl_dp_model *M, const EvalParams &P,
     cudaFuncSetAttribute(dp_fit<T, TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_fit);
     const long long ntiles = (total + TILE - 1) / TILE;
     const int gridf = (int)(ntiles < 152LL * 4 ? ntiles : 152LL * 4);
-    {
+    if (mode == MATPL_F32 || mode == MATPL_F64) {
         ProfScope ps("dp_fit", s);
         dp_fit<T, TILE><<<gridf, 256, smem_fit, s>>>(A, type_map, params, Ei, dA, P);
+    } else {
+        st = launch_fit_tc(mode != MATPL_MIXED, (const float *)A, type_map, (const float *)params,
+                           (unsigned char *)(ws + lay.ftiles), (float *)Ei, (float *)dA,
+                           M->err_dev, P.batch, P.natoms, P.ntypes, P.present_mask, s);
+        if (st) return st;
     }
     if (mode == MATPL_F32 || mode == MATPL_F64) {
         ProfScope ps("dp_embed_bwd", s);

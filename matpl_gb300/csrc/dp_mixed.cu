@@ -190,25 +190,36 @@ __device__ __forceinline__ void load_weight_tiles(const unsigned char *__restric
     for (int q = threadIdx.x; q < 8 * WT / 16; q += blockDim.x) d4[q] = __ldg(s4 + q);
 }
 
-// Segments of the current tile: maximal runs of one atom (rows are sorted by atom).
+// Segments of the current tile: maximal runs of one atom (rows are sorted by atom).  Every
+// thread flags whether its row starts a segment; a ballot per warp and a prefix over the four
+// warps place the segment starts.  Returns the segment count (includes __syncthreads).
 __device__ __forceinline__ int tile_segments(const MixSmem &sm, int r0, int nrows) {
-    // thread 0 walks at most 128 rows; segments <= GAMAX
-    if (threadIdx.x == 0) {
-        int ns = 0, cur = -1;
-        for (int r = 0; r < nrows; ++r) {
-            const int at = sm.list[r0 + r] >> 16;
-            if (at != cur) {
-                sm.seg[ns] = r;
-                sm.seg_atom[ns] = at;
-                ++ns;
-                cur = at;
-            }
-        }
-        sm.seg[ns] = nrows;
-        sm.seg[GAMAX] = ns;
+    __shared__ unsigned ballots[TM / 32];
+    const int r = threadIdx.x, lane = r & 31, warp = r >> 5;
+    int at = -1;
+    bool start = false;
+    if (r < nrows) {
+        at = sm.list[r0 + r] >> 16;
+        start = r == 0 || (sm.list[r0 + r - 1] >> 16) != at;
     }
+    const unsigned bal = __ballot_sync(0xffffffffu, start);
+    if (lane == 0) ballots[warp] = bal;
     __syncthreads();
-    return sm.seg[GAMAX];
+    int before = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < TM / 32; ++w) {
+        const int c = __popc(ballots[w]);
+        before += w < warp ? c : 0;
+        total += c;
+    }
+    if (start) {
+        const int idx = before + __popc(bal & ((1u << lane) - 1u));
+        sm.seg[idx] = r;
+        sm.seg_atom[idx] = at;
+    }
+    if (r == 0) sm.seg[total] = nrows;
+    __syncthreads();
+    return total;
 }
 
 // Write this thread's 32-wide row (hi and, for SPLIT 3, lo halves) into the activation tiles.
@@ -268,13 +279,15 @@ __device__ __forceinline__ void run_layer(const MixSmem &sm, uint32_t tmem, int 
 }
 
 // Build the group's occupied-slot list ordered by (net, atom, slot); fills cnt / off /
-// net_start.  Returns nothing; all threads participate.
+// net_start / tia.  A 32-slot chunk spans at most a few type blocks (usually one): one ballot
+// per spanned block counts / places its occupied slots.  All threads participate.
 __device__ void build_group_list(const MixSmem &sm, const int32_t *__restrict__ list_neigh,
                                  const int32_t *__restrict__ type_map, long long g0, int ga,
                                  const MixParams &P) {
     const int S = P.nslots, nt = P.ntypes, nnet = nt * nt;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const long long total = (long long)P.batch * P.natoms;
+    const unsigned lt = (1u << lane) - 1u;
     for (int a = warp; a < ga; a += TM / 32) {
         const long long t = g0 + a;
         int ti = -1;
@@ -282,28 +295,21 @@ __device__ void build_group_list(const MixSmem &sm, const int32_t *__restrict__ 
             ti = type_map[(int)(t % P.natoms)];
             if (ti < 0 || ti >= nt || !((P.present_mask >> ti) & 1)) ti = -1;
         }
-        int c[kMaxTypes];
-#pragma unroll
-        for (int q = 0; q < kMaxTypes; ++q) c[q] = 0;
-        if (ti >= 0) {
-            const int32_t *ln = list_neigh + t * S;
-            for (int s0 = 0; s0 < S; s0 += 32) {
-                const int s = s0 + lane;
-                const int blk = s / P.m;
-                const bool active = s < S && ln[s] != 0 && blk < kMaxTypes &&
-                                    ((P.present_mask >> blk) & 1);
-#pragma unroll
-                for (int q = 0; q < kMaxTypes; ++q)
-                    if (q < nt) c[q] += __popc(__ballot_sync(0xffffffffu, active && blk == q));
+        if (lane < kMaxTypes) sm.cnt[a * kMaxTypes + lane] = 0;
+        if (lane == 0) sm.tia[a] = ti;
+        __syncwarp();
+        if (ti < 0) continue;
+        const int32_t *ln = list_neigh + t * S;
+        for (int s0 = 0; s0 < S; s0 += 32) {
+            const int s = s0 + lane;
+            const int blk = s / P.m;
+            const bool active = s < S && ln[s] != 0 && blk < nt && ((P.present_mask >> blk) & 1);
+            const int blo = s0 / P.m;
+            const int bhi = min(min(S - 1, s0 + 31) / P.m, nt - 1);
+            for (int q = blo; q <= bhi; ++q) {
+                const unsigned mq = __ballot_sync(0xffffffffu, active && blk == q);
+                if (lane == 0 && mq) sm.cnt[a * kMaxTypes + q] += __popc(mq);
             }
-        }
-        if (lane < kMaxTypes) {
-            int v = 0;
-#pragma unroll
-            for (int q = 0; q < kMaxTypes; ++q)
-                if (q == lane) v = c[q];
-            sm.cnt[a * kMaxTypes + lane] = ti >= 0 ? v : 0;
-            if (lane == 0) sm.tia[a] = ti;
         }
     }
     __syncthreads();
@@ -323,25 +329,22 @@ __device__ void build_group_list(const MixSmem &sm, const int32_t *__restrict__ 
     __syncthreads();
     for (int a = warp; a < ga; a += TM / 32) {
         const long long t = g0 + a;
-        const int ti = sm.tia[a];
-        if (ti < 0) continue;
+        if (sm.tia[a] < 0) continue;
         const int32_t *ln = list_neigh + t * S;
-        int base[kMaxTypes];
-#pragma unroll
-        for (int q = 0; q < kMaxTypes; ++q) base[q] = (q < nt) ? sm.off[a * kMaxTypes + q] : 0;
         for (int s0 = 0; s0 < S; s0 += 32) {
             const int s = s0 + lane;
             const int blk = s / P.m;
-            const bool active = s < S && ln[s] != 0 && blk < kMaxTypes &&
-                                ((P.present_mask >> blk) & 1);
-#pragma unroll
-            for (int q = 0; q < kMaxTypes; ++q) {
-                if (q < nt) {
-                    const unsigned mq = __ballot_sync(0xffffffffu, active && blk == q);
-                    if (active && blk == q)
-                        sm.list[base[q] + __popc(mq & ((1u << lane) - 1u))] = (a << 16) | s;
-                    base[q] += __popc(mq);
-                }
+            const bool active = s < S && ln[s] != 0 && blk < nt && ((P.present_mask >> blk) & 1);
+            const int blo = s0 / P.m;
+            const int bhi = min(min(S - 1, s0 + 31) / P.m, nt - 1);
+            for (int q = blo; q <= bhi; ++q) {
+                const unsigned mq = __ballot_sync(0xffffffffu, active && blk == q);
+                if (!mq) continue;
+                const int base = sm.off[a * kMaxTypes + q];
+                if (active && blk == q) sm.list[base + __popc(mq & lt)] = (a << 16) | s;
+                __syncwarp();
+                if (lane == 0) sm.off[a * kMaxTypes + q] = base + __popc(mq);
+                __syncwarp();
             }
         }
     }
