@@ -6,7 +6,9 @@ slots per type (S = 300); embedding 1->25->25->25, M2 = 16, fitting 400->50->50-
 weights W ~ N(0, 1/fan_in).  One step = neighbor search from fractional positions + energy,
 forces and virial (what an MD step needs).  Synthetic data: no dataset is involved.
 
-  value : step with inputs resident in HBM (per-step working set ~230 MB > 129 MB L2)
+  value : step with inputs resident in HBM (per-step working set ~230 MB > 129 MB L2), in the
+          mixed-precision form (tcgen05 BF16x3 GEMMs); the plain-FP32 form of the same step is
+          timed in the same run and reported beside it (config.plain_fp32, speedup)
   e2e   : the same step through the public API with host (pinned) positions copied in and
           energy / forces / virial copied out every step
   roofline : the dominant kernel, timed live with CUDA events on its stream
@@ -185,50 +187,75 @@ def run_ours(args, ws, rank, local):
     n_pairs = int((ln > 0).sum())
     sub = slice(0, 4000)
     davg, dstd = P.calc_stat(cfg, ln[:, sub].cpu().numpy(), idr[:, sub].cpu().numpy(), st.types[sub])
-    model = dp.DP(cfg, prm, davg, dstd, precision=prec, device=dev, check_errors=False)
     m64 = dp.DP(cfg, prm, davg, dstd, precision="float64", device=dev)
-    present = model.present_types(cfg.atom_type)
+    present = m64.present_types(cfg.atom_type)
     tm32 = types_d.to(torch.int32)
-    out_dt = model.dtype
-
-    def step(frac, lat):
-        l, r = ops.find_neighbore(types_d, frac, lat, 2, M_NEIGH, RC, RC, out_dtype=out_dt,
-                                  check_overflow=False)
-        return model.evaluate(l, tm32, present, r, 0)
-
-    # accuracy of this form against the FP64 GPU path (itself checked against the reference)
     r64 = m64.evaluate(ln, tm32, present, idr, 0)
-    rr = step(frac_d, lat_d)
     torch.cuda.synchronize()
-    f_rmse = (rr["Force"].double() - r64["Force"]).pow(2).mean().sqrt().item()
-    e_err = abs(rr["Etot"].item() - r64["Etot"].item()) / NATOMS
-    v_err = (rr["Virial"] - r64["Virial"]).abs().max().item()
 
-    # ---- device-resident timed region
-    for _ in range(args.warmup):
-        step(frac_d, lat_d)
-    sampler = ClockSampler(local)
-    sampler.start()
-    time.sleep(0.3)
-    torch.cuda.synchronize()
-    barrier(ws)
-    torch.cuda.synchronize()
-    _lib.profile_begin(max(4096, args.steps * 16))
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(args.steps):
-        step(frac_d, lat_d)
-    e1.record()
-    torch.cuda.synchronize()
-    prof = _lib.profile_collect()
-    barrier(ws)
-    ms = e0.elapsed_time(e1) / args.steps
-    clocks = sampler.stop()
-    ms = max_over_ranks(ms, ws)
+    def make_step(form):
+        model = dp.DP(cfg, prm, davg, dstd, precision=form, device=dev, check_errors=False)
+        out_dt = model.dtype
+
+        def step(frac, lat):
+            l, r = ops.find_neighbore(types_d, frac, lat, 2, M_NEIGH, RC, RC, out_dtype=out_dt,
+                                      check_overflow=False)
+            return model.evaluate(l, tm32, present, r, 0)
+        return model, step
+
+    def accuracy(model, step):
+        rr = step(frac_d, lat_d)
+        torch.cuda.synchronize()
+        if int(model.err.item()) != 0:
+            raise RuntimeError(f"kernel error word {int(model.err.item())}")
+        return {"force_rmse_vs_f64_eV_per_A": (rr["Force"].double() - r64["Force"]).pow(2).mean().sqrt().item(),
+                "energy_err_per_atom_eV": abs(rr["Etot"].item() - r64["Etot"].item()) / NATOMS,
+                "virial_max_abs_err_eV": (rr["Virial"] - r64["Virial"]).abs().max().item()}
+
+    def timed(step, steps, warmup, sample_clocks):
+        for _ in range(warmup):
+            step(frac_d, lat_d)
+        sampler = ClockSampler(local) if sample_clocks else None
+        if sampler:
+            sampler.start()
+            time.sleep(0.3)
+        torch.cuda.synchronize()
+        barrier(ws)
+        torch.cuda.synchronize()
+        _lib.profile_begin(max(4096, steps * 16))
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            step(frac_d, lat_d)
+        e1.record()
+        torch.cuda.synchronize()
+        prof = _lib.profile_collect()
+        barrier(ws)
+        clocks = sampler.stop() if sampler else None
+        ms = max_over_ranks(e0.elapsed_time(e1) / steps, ws)
+        return ms, prof, clocks
+
+    model, step = make_step(prec)
+    acc = accuracy(model, step)
+    ms, prof, clocks = timed(step, args.steps, args.warmup, True)
     value = ws * NATOMS / (ms * 1e-3)
+    model_ms = sum(v[0] for k, v in prof.items() if not k.startswith("nb_")) / args.steps
+
+    plain = None
+    if prec != "float32" and not args.no_plain:
+        pmodel, pstep = make_step("float32")
+        pacc = accuracy(pmodel, pstep)
+        psteps = max(10, args.steps // 3)
+        pms, pprof, _ = timed(pstep, psteps, args.warmup, False)
+        pmodel_ms = sum(v[0] for k, v in pprof.items() if not k.startswith("nb_")) / psteps
+        plain = {"form": "float32 (plain SIMT)", "value": ws * NATOMS / (pms * 1e-3),
+                 "ms_per_step": pms, "model_only_ms_per_step": pmodel_ms,
+                 "model_only_value": ws * NATOMS / (pmodel_ms * 1e-3), **pacc}
+        del pmodel
 
     # ---- end to end through host buffers
+    out_dt = model.dtype
     frac_h = torch.tensor(st.frac).pin_memory()
     lat_h = torch.tensor(st.lattice).pin_memory()
     F_h = torch.empty(1, NATOMS, 3, dtype=out_dt).pin_memory()
@@ -267,8 +294,11 @@ def run_ours(args, ws, rank, local):
     dom = max(prof, key=lambda k: prof[k][0]) if prof else None
     es = 8 if prec == "float64" else 4
     S = 2 * M_NEIGH
-    flops = {"dp_embed_bwd": FLOP_EMB_BWD_PAIR * n_pairs, "dp_embed_fwd": FLOP_EMB_FWD_PAIR * n_pairs,
-             "dp_fit": FLOP_FIT_ATOM * NATOMS}
+    flops = {}
+    for suf in ("", "_tc"):
+        flops["dp_embed_bwd" + suf] = FLOP_EMB_BWD_PAIR * n_pairs
+        flops["dp_embed_fwd" + suf] = FLOP_EMB_FWD_PAIR * n_pairs
+        flops["dp_fit" + suf] = FLOP_FIT_ATOM * NATOMS
     # HBM-bound kernels: algorithmic bytes per launch (reads positions + types, writes the
     # reference-layout list_neigh [N,S] int32 and ImageDR [N,S,4])
     hbm_bytes = {"nb_search": NATOMS * (24 + 4 + S * (4 + 4 * es))}
@@ -289,7 +319,7 @@ def run_ours(args, ws, rank, local):
                     "algorithmic_bytes_per_launch": hbm_bytes[dom], "peak_source": src}
         else:
             ach = flops[dom] / t_launch / 1e12
-            sm_mhz = clocks.get("sm_mhz") or 2070.0
+            sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
             simt_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
             roof = {"kernel": dom, "bound": "tensor", "achieved": ach, "peak": bf16_peak,
                     "unit": "TFLOP/s", "frac": ach / bf16_peak, "traffic": None,
@@ -310,19 +340,25 @@ def run_ours(args, ws, rank, local):
         cb = cpu_baseline_run(steps=8, warmup=1)
     if rank != 0:
         return
+    config = {"workload": "DP se_e2_a, 32,000-atom Li/Si (1:1) random-packed box, 0.05 atoms/A^3, "
+                          "Rc 6.0, m=150/type (S=300), emb 25-25-25, M2 16, fit 50-50-50-1; "
+                          "step = GPU neighbor search + E/F/V",
+              "precision_form": prec, "natoms": NATOMS, "pairs": n_pairs,
+              "parallelism": "replicas" if ws > 1 else "single GPU",
+              "l2": "no flush: per-step working set ~230 MB (neighbor list + ImageDR) exceeds the "
+                    "129 MB L2",
+              "model_only_ms_per_step": model_ms,
+              "model_only_value": ws * NATOMS / (model_ms * 1e-3), **acc}
+    if plain:
+        config["plain_fp32"] = plain
+        config["speedup_vs_plain_fp32"] = plain["ms_per_step"] / ms
+        config["model_only_speedup_vs_plain_fp32"] = plain["model_only_ms_per_step"] / model_ms
+    dtype = {"float32": "f32", "float64": "f64"}.get(prec, "bf16x3 tensor / f32 / f64 sums"
+                                                     if prec != "mixed_fast" else "bf16 tensor / f32")
     line = {"metric": METRIC, "value": value, "unit": "atom-steps/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": {"float32": "f32", "float64": "f64"}.get(prec, prec), "data": "synthetic",
-            "config": {"workload": "DP se_e2_a, 32,000-atom Li/Si (1:1) random-packed box, "
-                                   "0.05 atoms/A^3, Rc 6.0, m=150/type (S=300), emb 25-25-25, "
-                                   "M2 16, fit 50-50-50-1; step = neighbor search + E/F/V",
-                       "precision_form": prec, "natoms": NATOMS, "pairs": n_pairs,
-                       "parallelism": "replicas" if ws > 1 else "single GPU",
-                       "l2": "no flush: per-step working set ~230 MB (neighbor list + ImageDR) "
-                             "exceeds the 129 MB L2",
-                       "force_rmse_vs_f64_eV_per_A": f_rmse, "energy_err_per_atom_eV": e_err,
-                       "virial_max_abs_err_eV": v_err},
+            "dtype": dtype, "data": "synthetic", "config": config,
             "e2e": {"value": ws * NATOMS / (e2e_ms * 1e-3), "unit": "atom-steps/s",
                     "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "kernels": per_kernel, "roofline": roof,
@@ -336,9 +372,11 @@ def main():
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="float32",
-                    choices=["float32", "float64", "mixed", "mixed_fast", "mixed_x3fast"])
+    ap.add_argument("--precision", default="mixed",
+                    choices=["mixed", "mixed_tanhf", "mixed_fast", "float32", "float64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the plain-FP32 comparison run of a mixed form")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":

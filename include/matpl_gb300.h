@@ -36,17 +36,17 @@ typedef enum {
 #define MATPL_KERR_BAD_TYPE 2            /* atom type index outside [0, ntypes) */
 #define MATPL_KERR_TIMEOUT 3             /* a bounded tensor-core completion wait gave up */
 
-/* Compute forms.  MIXED*: FP32 data, embedding GEMMs on the tensor cores (tcgen05, BF16
- * operands, FP32 accumulation in TMEM), FP64 energy / virial reductions.
- *   MATPL_MIXED         BF16x3 split operands (hi*hi + hi*lo + lo*hi), CUDA tanhf
- *   MATPL_MIXED_FAST    single BF16 operands, hardware tanh.approx.f32
- *   MATPL_MIXED_X3FAST  BF16x3 split operands, hardware tanh.approx.f32 */
+/* Compute forms.  MIXED*: FP32 data, embedding and fitting GEMMs on the tensor cores
+ * (tcgen05, BF16 operands, FP32 accumulation in TMEM), FP64 energy / virial reductions.
+ *   MATPL_MIXED         BF16x3 split operands (hi*hi + hi*lo + lo*hi), hardware tanh.approx.f32
+ *   MATPL_MIXED_FAST    single BF16 embedding operands, hardware tanh.approx.f32
+ *   MATPL_MIXED_TANHF   BF16x3 split operands, CUDA tanhf */
 typedef enum {
     MATPL_F32 = 0,
     MATPL_F64 = 1,
     MATPL_MIXED = 2,
     MATPL_MIXED_FAST = 3,
-    MATPL_MIXED_X3FAST = 4
+    MATPL_MIXED_TANHF = 4
 } matpl_dtype;
 
 const char *matpl_last_error(void);

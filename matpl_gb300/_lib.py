@@ -8,7 +8,7 @@ import os
 
 from . import build as _build
 
-MATPL_F32, MATPL_F64, MATPL_MIXED, MATPL_MIXED_FAST, MATPL_MIXED_X3FAST = 0, 1, 2, 3, 4
+MATPL_F32, MATPL_F64, MATPL_MIXED, MATPL_MIXED_FAST, MATPL_MIXED_TANHF = 0, 1, 2, 3, 4
 KERR_NEIGHBOR_OVERFLOW = 1
 KERR_BAD_TYPE = 2
 KERR_TIMEOUT = 3

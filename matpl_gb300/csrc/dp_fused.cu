@@ -730,17 +730,18 @@ int run_mixed(int mode, bool backward, const EvalParams &P, const int32_t *ln, c
     float *fo = (float *)out;
     switch (mode) {
         case MATPL_MIXED:
-            return launch_mixed_embed<3, false>(backward, ln, fi, tm, fp, wt, fa, fs, fin, fo, avir, err,
-                                                P.batch, P.natoms, P.nslots, P.nghost, P.ntypes,
-                                                P.m, P.present_mask, P.rmin, P.rmax, P.inv_mT, s);
+            return launch_mixed_embed<3, true>(backward, ln, fi, tm, fp, wt, fa, fs, fin, fo, avir, err,
+                                               P.batch, P.natoms, P.nslots, P.nghost, P.ntypes,
+                                               P.m, P.present_mask, P.rmin, P.rmax, P.inv_mT, s);
         case MATPL_MIXED_FAST:
             return launch_mixed_embed<1, true>(backward, ln, fi, tm, fp, wt, fa, fs, fin, fo, avir, err,
                                                P.batch, P.natoms, P.nslots, P.nghost, P.ntypes,
                                                P.m, P.present_mask, P.rmin, P.rmax, P.inv_mT, s);
         default:
-            return launch_mixed_embed<3, true>(backward, ln, fi, tm, fp, wt, fa, fs, fin, fo, avir, err,
-                                               P.batch, P.natoms, P.nslots, P.nghost, P.ntypes,
-                                               P.m, P.present_mask, P.rmin, P.rmax, P.inv_mT, s);
+            return launch_mixed_embed<3, false>(backward, ln, fi, tm, fp, wt, fa, fs, fin, fo, avir,
+                                                err, P.batch, P.natoms, P.nslots, P.nghost,
+                                                P.ntypes, P.m, P.present_mask, P.rmin, P.rmax,
+                                                P.inv_mT, s);
     }
 }
 
@@ -799,7 +800,7 @@ int launch_eval(int mode, const matpl_dp_model *M, const EvalParams &P,
         ProfScope ps("dp_fit", s);
         dp_fit<T, TILE><<<gridf, 256, smem_fit, s>>>(A, type_map, params, Ei, dA, P);
     } else {
-        st = launch_fit_tc(mode != MATPL_MIXED, (const float *)A, type_map, (const float *)params,
+        st = launch_fit_tc(mode != MATPL_MIXED_TANHF, (const float *)A, type_map, (const float *)params,
                            (unsigned char *)(ws + lay.ftiles), (float *)Ei, (float *)dA,
                            M->err_dev, P.batch, P.natoms, P.ntypes, P.present_mask, s);
         if (st) return st;
@@ -843,7 +844,7 @@ extern "C" int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, 
                              double *Etot, void *force, double *virial, void *workspace,
                              size_t workspace_bytes, void *stream) {
     MATPL_REQUIRE(model != nullptr, MATPL_ERR_INVALID, "model is NULL");
-    MATPL_REQUIRE(dtype >= MATPL_F32 && dtype <= MATPL_MIXED_X3FAST, MATPL_ERR_DTYPE,
+    MATPL_REQUIRE(dtype >= MATPL_F32 && dtype <= MATPL_MIXED_TANHF, MATPL_ERR_DTYPE,
                   "matpl_dp_eval: unknown dtype / compute form");
     MATPL_REQUIRE(model->ntypes >= 1 && model->ntypes <= 16, MATPL_ERR_UNSUPPORTED,
                   "ntypes must be in [1, 16]");

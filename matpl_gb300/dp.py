@@ -20,16 +20,16 @@ from typing import Dict, List, Optional
 import torch
 
 from . import _lib
-from ._lib import (MATPL_F32, MATPL_F64, MATPL_MIXED, MATPL_MIXED_FAST, MATPL_MIXED_X3FAST,
+from ._lib import (MATPL_F32, MATPL_F64, MATPL_MIXED, MATPL_MIXED_FAST, MATPL_MIXED_TANHF,
                    MatplDpModel, check, ptr)
 
 # precision name -> (C ABI compute form, storage dtype)
 PRECISIONS = {
     "float64": (MATPL_F64, torch.float64),
     "float32": (MATPL_F32, torch.float32),
-    "mixed": (MATPL_MIXED, torch.float32),              # tcgen05 BF16x3 GEMMs, tanhf
-    "mixed_fast": (MATPL_MIXED_FAST, torch.float32),    # tcgen05 BF16 GEMMs, tanh.approx
-    "mixed_x3fast": (MATPL_MIXED_X3FAST, torch.float32),  # tcgen05 BF16x3 GEMMs, tanh.approx
+    "mixed": (MATPL_MIXED, torch.float32),              # tcgen05 BF16x3 GEMMs, tanh.approx
+    "mixed_fast": (MATPL_MIXED_FAST, torch.float32),    # tcgen05 BF16 embedding GEMMs
+    "mixed_tanhf": (MATPL_MIXED_TANHF, torch.float32),  # tcgen05 BF16x3 GEMMs, CUDA tanhf
 }
 from .params import DPConfig
 
@@ -120,8 +120,8 @@ class DP(torch.nn.Module):
     """Inference DP se_e2_a on GB300.
 
     ``precision``: "float64" | "float32" (plain SIMT forms) | "mixed" | "mixed_fast" |
-    "mixed_x3fast" (embedding GEMMs on the tcgen05 tensor cores, FP32 data, FP64 energy /
-    virial sums).  ``check_errors`` reads the kernels' error word after every call (one
+    "mixed_tanhf" (embedding and fitting GEMMs on the tcgen05 tensor cores, FP32 data, FP64
+    energy / virial sums).  ``check_errors`` reads the kernels' error word after every call (one
     device sync); the benchmark turns it off inside its timed loop."""
 
     def __init__(self, cfg: DPConfig, params: Dict[str, torch.Tensor], davg, dstd,

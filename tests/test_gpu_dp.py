@@ -161,7 +161,7 @@ def test_full_size_32k_invariants():
     assert abs(E32.item() - E64.item()) < 1e-5 * abs(E64.item()) + 1e-3
 
 
-MIXED = ["mixed", "mixed_fast", "mixed_x3fast"]
+MIXED = ["mixed", "mixed_fast", "mixed_tanhf"]
 
 
 @pytest.mark.parametrize("precision", MIXED)
@@ -173,8 +173,8 @@ def test_mixed_forms_within_tolerance_of_reference(golden_case, precision, name)
     g = c.g
     Etot, Ei, F, _, V = run_model(c, precision)
     rmse = np.sqrt(np.mean((F.cpu().double().numpy() - g["Force"]) ** 2))
-    # BF16x3 + tanhf is FP32-level; the single-BF16 + tanh.approx form carries ~1 % relative
-    # force error, which is above 1e-4 eV/A only on low-force cells (Cu: max|F| 0.012 eV/A)
+    # BF16x3 forms stay within 1e-4 eV/A; the single-BF16 embedding form carries ~1 % relative
+    # force error (2.5e-3 eV/A on the reference's HfO2 weights), reported but not held to the bar
     fmax = np.abs(g["Force"]).max()
     n = c.types.shape[0]
     e_err = abs(Etot.item() - g["Etot"].ravel()[0]) / n
@@ -182,9 +182,9 @@ def test_mixed_forms_within_tolerance_of_reference(golden_case, precision, name)
     v_err = np.abs(V.cpu().double().numpy() - g["Virial"]).max() / vs
     print(f"[accuracy] {precision} {name}: force RMSE {rmse:.3e} eV/A (max|F| {fmax:.3f}), "
           f"energy {e_err:.3e} eV/atom, virial {v_err:.3e} relative")
-    if precision == "mixed":          # meets the 1e-4 eV/A bar with margin on every case
-        assert rmse <= 3e-5 and e_err < 1e-6 and v_err < 5e-5, (rmse, e_err, v_err)
-    elif precision == "mixed_x3fast":
+    if precision == "mixed_tanhf":    # BF16x3 + tanhf: FP32-level
+        assert rmse <= 3e-5 and e_err < 2e-6 and v_err < 5e-5, (rmse, e_err, v_err)
+    elif precision == "mixed":        # BF16x3 + hardware tanh: within the 1e-4 eV/A bar
         assert rmse <= 1e-4 and e_err < 2e-4 and v_err < 2e-3, (rmse, e_err, v_err)
     else:                             # single BF16: sanity only (about 1 % relative error)
         assert rmse <= 0.02 * fmax and e_err < 2e-2 and v_err < 5e-2, (rmse, e_err, v_err)
