@@ -91,6 +91,19 @@ int matpl_calc_virial_grad(int dtype, const int32_t *list_neigh, const void *Rij
                            int nslots, void *grad_dE, void *stream);
 
 /* ------------------------------------------------------------------------------------
+ * Tabulated embedding.  Replaces CalcOps_cuda::calculateCompress (src/op/src/CalcOps.cpp:331-383,
+ * kernels src/op/kernel/calculateCompress.cu:3-55, calculateCompress_grad.cu:3-53):
+ *   f2 [nsij] (the [nsij,1] tensor), coefficient [nsij, layer_node, coe_num] highest power first,
+ *   coe_num 4 (order 3) or 6 (order 5) -> G [nsij, layer_node].
+ * The backward returns grad_f2 [nsij] = sum_i grad_G[s][i] dG[s][i]/df2 directly.
+ * ---------------------------------------------------------------------------------- */
+int matpl_calc_compress(int dtype, const void *f2, const void *coefficient, long long nsij,
+                        int layer_node, int coe_num, void *G, void *stream);
+int matpl_calc_compress_grad(int dtype, const void *f2, const void *coefficient,
+                             const void *grad_G, long long nsij, int layer_node, int coe_num,
+                             void *grad_f2, void *stream);
+
+/* ------------------------------------------------------------------------------------
  * DP neighbor search.  Replaces the Fortran NeighConst.find_neighbore
  * (src/pre_data/gen_feature/NeighConst.f90:14-149) as called by
  * src/pre_data/dpuni_data_loader.py:595-650, plus the r column of compute_Ri (:652-716).

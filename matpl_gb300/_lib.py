@@ -35,6 +35,8 @@ SIGNATURES = {
     "matpl_calc_virial": (_i, [_i, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _vp, _vp, _vp]),
     "matpl_calc_force_grad": (_i, [_i, _vp, _vp, _vp, _i, _i, _i, _i, _vp, _vp]),
     "matpl_calc_virial_grad": (_i, [_i, _vp, _vp, _vp, _vp, _i, _i, _i, _vp, _vp]),
+    "matpl_calc_compress": (_i, [_i, _vp, _vp, _c.c_longlong, _i, _i, _vp, _vp]),
+    "matpl_calc_compress_grad": (_i, [_i, _vp, _vp, _vp, _c.c_longlong, _i, _i, _vp, _vp]),
     "matpl_neighbor_workspace_bytes": (_sz, [_i, _i]),
     "matpl_neighbor_build": (_i, [_i, _i, _i, _i, _d, _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp,
                                   _vp, _vp, _sz, _vp]),

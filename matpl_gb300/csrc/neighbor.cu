@@ -216,14 +216,17 @@ nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
           const int *__restrict__ cell_start, const int *__restrict__ cell_atoms,
           int32_t *__restrict__ list_neigh, TO *__restrict__ image_dr,
           int32_t *__restrict__ num_neigh, int32_t *__restrict__ err, NbParams P) {
-    extern __shared__ unsigned char smem_raw[];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     const int S = P.ntypes * P.m;
     const int CAP = 2 * S;                         // pre-filtered candidates per atom
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int *cand = reinterpret_cast<int *>(smem_raw) + warp * (CAP + S);
+    double2 *kvec = reinterpret_cast<double2 *>(smem_raw) + 2 * warp * S;   // exact (x, y), (z, dd)
+    int *cand = reinterpret_cast<int *>(reinterpret_cast<double2 *>(smem_raw) + 2 * kWarps * S) +
+                warp * (CAP + S);
     int *keys = cand + CAP;
     unsigned char *ktype = reinterpret_cast<unsigned char *>(
-                               reinterpret_cast<int *>(smem_raw) + kWarps * (CAP + S)) + warp * S;
+                               reinterpret_cast<int *>(reinterpret_cast<double2 *>(smem_raw) +
+                                                       2 * kWarps * S) + kWarps * (CAP + S)) + warp * S;
     const long long total = (long long)P.batch * P.natoms;
     for (long long t = (long long)blockIdx.x * kWarps + warp; t < total;
          t += (long long)gridDim.x * kWarps) {
@@ -369,6 +372,7 @@ nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
             const int c = c0 + lane;
             bool inM = false, inT = false;
             int tj = 0, key = 0;
+            double px = 0.0, py = 0.0, pz = 0.0, pdd = 0.0;
             if (c < ncand) {
                 key = cand[c];
                 const int j = key / nimg, idx = key - (key / nimg) * nimg;
@@ -385,10 +389,9 @@ nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
                     d2 = da(pos[3 * j + 1], -pi1); mic(d2);
                     d3 = da(pos[3 * j + 2], -pi2); mic(d3);
                 }
-                double x, y, z, dd;
-                cart(im.L, d1, d2, d3, x, y, z, dd);
-                inM = dd < P.rc2 && dd > 1.0e-8;
-                inT = inM && dd < rct2;
+                cart(im.L, d1, d2, d3, px, py, pz, pdd);
+                inM = pdd < P.rc2 && pdd > 1.0e-8;
+                inT = inM && pdd < rct2;
                 tj = type_map[j];
                 if (tj < 0 || tj >= P.ntypes) {
                     atomicMax(err, MATPL_KERR_BAD_TYPE);
@@ -404,6 +407,8 @@ nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
             if (inT && at < S) {
                 keys[at] = key;
                 ktype[at] = (unsigned char)tj;
+                kvec[2 * at] = make_double2(px, py);
+                kvec[2 * at + 1] = make_double2(pz, pdd);
             }
             n_acc += __popc(ma);
         }
@@ -431,22 +436,9 @@ nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
             int rank = 0;
             for (int f = 0; f < nst; ++f) rank += (ktype[f] == ty) & (keys[f] < key);
             if (rank >= P.m) continue;
-            const int j = key / nimg, idx = key - j * nimg;
-            double d1, d2, d3;
-            if (im.iflag) {
-                const int i3 = idx % nimg1 - im.nper[2];
-                const int i2 = (idx / nimg1) % nimg2 - im.nper[1];
-                const int i1 = idx / (nimg1 * nimg2) - im.nper[0];
-                d1 = da(da(pos[3 * j], -pi0), (double)i1);
-                d2 = da(da(pos[3 * j + 1], -pi1), (double)i2);
-                d3 = da(da(pos[3 * j + 2], -pi2), (double)i3);
-            } else {
-                d1 = da(pos[3 * j], -pi0); mic(d1);
-                d2 = da(pos[3 * j + 1], -pi1); mic(d2);
-                d3 = da(pos[3 * j + 2], -pi2); mic(d3);
-            }
-            double x, y, z, dd;
-            cart(im.L, d1, d2, d3, x, y, z, dd);
+            const int j = key / nimg;
+            const double2 xa = kvec[2 * e], xb = kvec[2 * e + 1];
+            const double x = xa.x, y = xa.y, z = xb.x, dd = xb.y;
             const long long slot = row + (long long)ty * P.m + rank;
             list_neigh[slot] = j + 1;
             store4(image_dr + 4 * slot, (TO)__dsqrt_rn(dd), (TO)x, (TO)y, (TO)z);
@@ -568,8 +560,8 @@ extern "C" int matpl_neighbor_build(int batch, int natoms, int ntypes, int m_nei
     MATPL_REQUIRE(ntypes >= 1 && ntypes <= kMaxTypes, MATPL_ERR_UNSUPPORTED,
                   "ntypes must be in [1, 16]");
     MATPL_REQUIRE(m_neigh >= 1, MATPL_ERR_INVALID, "m_neigh must be >= 1");
-    MATPL_REQUIRE((long long)ntypes * m_neigh <= 2048, MATPL_ERR_UNSUPPORTED,
-                  "ntypes * m_neigh must be <= 2048");
+    MATPL_REQUIRE((long long)ntypes * m_neigh <= 1024, MATPL_ERR_UNSUPPORTED,
+                  "ntypes * m_neigh must be <= 1024");
     MATPL_REQUIRE(Rc_M > 0 && Rc_type != nullptr, MATPL_ERR_INVALID, "bad cutoff");
     MATPL_REQUIRE(out_dtype == MATPL_F32 || out_dtype == MATPL_F64, MATPL_ERR_DTYPE,
                   "image_dr dtype must be f32 or f64");
@@ -609,7 +601,7 @@ extern "C" int matpl_neighbor_build(int batch, int natoms, int ntypes, int m_nei
     }
     ProfScope ps("nb_search", s);
     const int S = ntypes * m_neigh;
-    const size_t smem = (size_t)kWarps * (3 * S * 4 + S);
+    const size_t smem = (size_t)kWarps * (S * 32 + 3 * S * 4 + S);
     if (out_dtype == MATPL_F64) {
         cudaFuncSetAttribute(nb_search<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);

@@ -119,6 +119,39 @@ def calculateVirial(list_neigh: torch.Tensor, dE: torch.Tensor, Rij: torch.Tenso
     return [v, av]
 
 
+class _CalculateCompress(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, f2, coefficient):
+        ns, nodes, nc = coefficient.shape
+        f = f2.contiguous().reshape(-1).to(coefficient.dtype)
+        c = coefficient.contiguous()
+        G = torch.empty(ns, nodes, dtype=c.dtype, device=c.device)
+        check(_lib.load().matpl_calc_compress(_dtype_code(c), ptr(f), ptr(c), ns, nodes, nc, ptr(G),
+                                              _stream(c.device)), "matpl_calc_compress")
+        ctx.save_for_backward(f, c)
+        ctx.f2_shape = f2.shape
+        return G
+
+    @staticmethod
+    def backward(ctx, grad_G):
+        f, c = ctx.saved_tensors
+        ns, nodes, nc = c.shape
+        g = grad_G.contiguous().to(c.dtype)
+        out = torch.empty(ns, dtype=c.dtype, device=c.device)
+        check(_lib.load().matpl_calc_compress_grad(_dtype_code(c), ptr(f), ptr(c), ptr(g), ns, nodes,
+                                                   nc, ptr(out), _stream(c.device)),
+              "matpl_calc_compress_grad")
+        return out.reshape(ctx.f2_shape), None
+
+
+def calculateCompress(f2: torch.Tensor, coefficient: torch.Tensor) -> List[torch.Tensor]:
+    """``CalcOps_cuda.calculateCompress`` (CalcOps.cpp:331-383): f2 [nsij,1], coefficient
+    [nsij, layer_node, 4 or 6] (highest power first) -> [G [nsij, layer_node]]; differentiable
+    in f2 like the reference (no gradient for the coefficients)."""
+    _require_cuda(f2, coefficient)
+    return [_CalculateCompress.apply(f2, coefficient)]
+
+
 def env_mat(ImageDR: torch.Tensor, Imagetype_map: torch.Tensor, davg: torch.Tensor,
             dstd: torch.Tensor, Rmin: float, Rmax: float) -> Tuple[torch.Tensor, torch.Tensor]:
     """``DP.calculate_Ri`` (dp_dp.py:217-302): normalised Ri [B,N,S,4] and Ri_d [B,N,S,4,3]."""

@@ -241,3 +241,20 @@ def force_virial_grads(list_neigh0, Ri_d, Rij, grad_force, grad_virial):
     gV = grad_virial.reshape(B, 3, 3)
     gvir = torch.einsum("bac,bnsc,bnswa->bnsw", gV, Rij, Rd) * ok[..., None]
     return (gf_center + gf_nei).reshape(B, N, 4 * S), gvir.reshape(B, N, 4 * S)
+
+
+def compress_oracle(f2, coefficient):
+    """Oracle for ``calculateCompress`` and its backward (``src/op/kernel/calculateCompress.cu:3-55``,
+    ``calculateCompress_grad.cu:3-53``, ``CalcOps.cpp:343-356``): G = sum_k c_k f2^(n-1-k), and
+    dG/df2, evaluated term by term in float64."""
+    f = f2.reshape(-1, 1).to(torch.float64)
+    c = coefficient.to(torch.float64)
+    n = c.shape[-1]
+    G = torch.zeros(c.shape[:2], dtype=torch.float64)
+    dG = torch.zeros(c.shape[:2], dtype=torch.float64)
+    for k in range(n):
+        p = n - 1 - k
+        G = G + c[..., k] * f ** p
+        if p > 0:
+            dG = dG + p * c[..., k] * f ** (p - 1)
+    return G, dG

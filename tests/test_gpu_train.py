@@ -1,0 +1,99 @@
+"""Force-loss training step (dp_trainer.train on the GPU with this library's env-matrix and
+force/virial kernels): parameter gradients against the FP64 oracle (second-order autograd through
+MatPL's algorithm on the CPU) and against finite differences."""
+import numpy as np
+import pytest
+import torch
+
+from matpl_gb300 import params as P, structures, train
+from oracle import dp_oracle, neigh
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+
+
+def make_case(n=48, seed=31):
+    st = structures.random_packed(n, 0.07, [72, 8], [1 / 3, 2 / 3], seed=seed, strain=0.03)
+    cfg = P.DPConfig(atom_type=[72, 8], maxNeighborNum=100)
+    ln, idr = neigh.find_neighbore(st.types, st.frac, st.lattice, 2, 100, 6.0, [6.0, 6.0])
+    davg, dstd = P.calc_stat(cfg, ln, idr, st.types)
+    prm = P.init_params(cfg, 5)
+    teacher = P.init_params(cfg, 99)
+    lab = dp_oracle.dp_eval(cfg, teacher, torch.tensor(davg), torch.tensor(dstd), torch.tensor(ln),
+                            torch.tensor(st.types), torch.tensor(cfg.atom_type), torch.tensor(idr), 0)
+    g = torch.Generator().manual_seed(seed)
+    E_lab = lab["Etot"].detach() + 0.01 * torch.randn(1, generator=g, dtype=torch.float64)
+    F_lab = lab["Force"].detach() + 0.01 * torch.randn(lab["Force"].shape, generator=g, dtype=torch.float64)
+    return cfg, st, ln, idr, davg, dstd, prm, E_lab, F_lab
+
+
+def oracle_grads(cfg, st, ln, idr, davg, dstd, prm, E_lab, F_lab):
+    p = {k: v.clone().requires_grad_() for k, v in prm.items()}
+    out = dp_oracle.dp_eval(cfg, p, torch.tensor(davg), torch.tensor(dstd), torch.tensor(ln),
+                            torch.tensor(st.types), torch.tensor(cfg.atom_type), torch.tensor(idr), 0,
+                            create_graph=True)
+    loss = torch.nn.functional.mse_loss(out["Etot"], E_lab) + \
+        torch.nn.functional.mse_loss(out["Force"], F_lab)
+    names = sorted(p)
+    gr = torch.autograd.grad(loss, [p[k] for k in names])
+    return loss.item(), dict(zip(names, gr))
+
+
+def gpu_model_and_batch(cfg, st, ln, idr, davg, dstd, prm, E_lab, F_lab):
+    model = train.DPTrainModel(cfg, prm, davg, dstd, dtype=torch.float64, device=DEV)
+    batch = {"list_neigh": torch.tensor(ln, device=DEV), "type_map": torch.tensor(st.types, device=DEV),
+             "atom_type": cfg.atom_type, "ImageDR": torch.tensor(idr, device=DEV),
+             "Etot": E_lab.to(DEV), "Force": F_lab.to(DEV)}
+    return model, batch
+
+
+def test_training_gradients_match_oracle():
+    case = make_case()
+    loss_ref, g_ref = oracle_grads(*case)
+    model, batch = gpu_model_and_batch(*case)
+    loss, _, _ = train.loss_fn(model, batch)
+    loss.backward()
+    assert abs(loss.item() - loss_ref) <= 1e-10 * abs(loss_ref)
+    worst = 0.0
+    for k, gr in g_ref.items():
+        got = model.param(k).grad.detach().cpu()
+        scale = gr.abs().max().item() + 1e-30
+        worst = max(worst, (got - gr).abs().max().item() / scale)
+    assert worst < 1e-8, worst
+
+
+def test_training_gradient_finite_difference():
+    case = make_case(n=36, seed=7)
+    model, batch = gpu_model_and_batch(*case)
+    loss, _, _ = train.loss_fn(model, batch)
+    loss.backward()
+    rng = np.random.default_rng(0)
+    for name in ["embedding_net.1.layers.1.weight", "fitting_net.0.layers.0.weight",
+                 "fitting_net.1.layers.2.resnet_dt"]:
+        p = model.param(name)
+        flat = p.detach().view(-1)
+        for q in rng.choice(flat.numel(), 2, replace=False):
+            h = 1e-6 * max(1.0, abs(flat[q].item()))
+            with torch.no_grad():
+                flat[q] += h
+            lp = train.loss_fn(model, batch)[0].item()
+            with torch.no_grad():
+                flat[q] -= 2 * h
+            lm = train.loss_fn(model, batch)[0].item()
+            with torch.no_grad():
+                flat[q] += h
+            fd = (lp - lm) / (2 * h)
+            an = p.grad.view(-1)[q].item()
+            assert abs(fd - an) <= 1e-5 * max(1e-3, abs(an)), (name, q, fd, an)
+
+
+def test_training_steps_reduce_loss():
+    """Plain gradient steps with a small step size must lower the loss (the gradient is a
+    descent direction)."""
+    case = make_case(n=48, seed=3)
+    model, batch = gpu_model_and_batch(*case)
+    opt = torch.optim.SGD(model.parameters(), lr=1e-5)
+    first = train.loss_fn(model, batch)[0].item()
+    for _ in range(5):
+        train.train_step(model, [batch], opt)
+    assert train.loss_fn(model, batch)[0].item() < first

@@ -91,3 +91,19 @@ def test_neighbor_sets_match_bruteforce_numpy():
                         if 1e-8 < dd < 36.0:
                             exp.append((j, round(np.sqrt(dd), 9)))
         assert got == sorted(exp)
+
+
+def test_compress_oracle_matches_reference_cpu_formula():
+    """The reference's CPU branch (dp_dp.py:590-597) writes the order-5 polynomial term by term;
+    the oracle's G must agree with that expression and its derivative with finite differences."""
+    g = torch.Generator().manual_seed(0)
+    f2 = torch.rand(50, 1, generator=g, dtype=torch.float64)
+    c = torch.randn(50, 25, 6, generator=g, dtype=torch.float64)
+    G, dG = dp_oracle.compress_oracle(f2, c)
+    ref = (f2 ** 5 * c[:, :, 0] + f2 ** 4 * c[:, :, 1] + f2 ** 3 * c[:, :, 2] + f2 ** 2 * c[:, :, 3]
+           + f2 * c[:, :, 4] + c[:, :, 5])
+    assert torch.allclose(G, ref, rtol=1e-14, atol=1e-14)
+    h = 1e-6
+    Gp, _ = dp_oracle.compress_oracle(f2 + h, c)
+    Gm, _ = dp_oracle.compress_oracle(f2 - h, c)
+    assert torch.allclose((Gp - Gm) / (2 * h), dG, rtol=1e-6, atol=1e-6)
