@@ -1,8 +1,9 @@
 """ORACLE build recipe (test infrastructure only).
 
-Compiles ``oracle/neighconst.c`` into ``oracle/_build/libmatpl_oracle.so`` with gcc.
-``-ffp-contract=off`` is required: the restatement's floating-point order is the Fortran
-source order with no fused multiply-add, on x86_64 and aarch64 alike.
+Compiles ``oracle/neighconst.c`` (DP neighbor list) and ``oracle/nepneigh.c`` (NEP neighbor
+lists) into ``oracle/_build/libmatpl_oracle.so`` with gcc.  ``-ffp-contract=off`` is required:
+the restatements' floating-point order is the reference source order with no fused
+multiply-add, on x86_64 and aarch64 alike.
 """
 import os
 import subprocess
@@ -13,13 +14,13 @@ LIB = os.path.join(OUT_DIR, "libmatpl_oracle.so")
 
 
 def build(force: bool = False) -> str:
-    src = os.path.join(HERE, "neighconst.c")
+    srcs = [os.path.join(HERE, f) for f in ("neighconst.c", "nepneigh.c")]
     os.makedirs(OUT_DIR, exist_ok=True)
     if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= os.path.getmtime(src)):
+            and os.path.getmtime(LIB) >= max(os.path.getmtime(s) for s in srcs)):
         return LIB
     cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-shared", "-fPIC",
-           "-o", LIB, src, "-lm"]
+           "-o", LIB, *srcs, "-lm"]
     subprocess.check_call(cmd)
     return LIB
 

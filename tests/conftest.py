@@ -69,3 +69,39 @@ def golden_case():
             cache[name] = GoldenCase(name)
         return cache[name]
     return get
+
+
+class NepCase:
+    """Rebuilds the inputs of a NEP golden fixture: frames, oracle neighbor lists, parameters
+    (seeded, with the fixture's q_scaler)."""
+
+    def __init__(self, name):
+        from matpl_gb300 import nep as NP
+        from oracle import nep_oracle as NO
+        g = load_golden(name)
+        self.g = g
+        self.name = name
+        self.cfg = NP.NepConfig(atom_type=[int(x) for x in g["atom_type"]],
+                                cutoff=tuple(float(x) for x in g["cutoff"]),
+                                n_max=tuple(int(x) for x in g["n_max"]),
+                                basis_size=tuple(int(x) for x in g["basis_size"]),
+                                l_max=tuple(int(x) for x in g["l_max"]),
+                                neuron=int(g["neuron"]), train_2b=bool(g["train_2b"]))
+        self.frames = NP.NepFrames(g["position"].copy(), g["type_map"], g["num_atom"], g["box"],
+                                   g["box_orig"], g["num_cell"])
+        self.params = NP.init_params(self.cfg, int(g["seed_w"]), energy_shift=-3.0)
+        self.params["q_scaler"] = torch.tensor(g["q_scaler"])
+        (self.NN_r, self.NN_a, self.NL_r, self.NL_a, self.Ri_r,
+         self.Ri_a) = NO.neighbor(self.frames, self.cfg.cutoff[0], self.cfg.cutoff[1],
+                                  int(g["max_r"]), int(g["max_a"]))
+
+
+@pytest.fixture(scope="session")
+def nep_case():
+    cache = {}
+
+    def get(name):
+        if name not in cache:
+            cache[name] = NepCase(name)
+        return cache[name]
+    return get
