@@ -44,6 +44,15 @@ FLOP_EMB_BWD_PAIR = 2 * 2 * 100 + 2 * (625 + 625 + 25) + 42     # 2992
 FLOP_FIT_ATOM = 2 * 4 * 25 * 16 + 2 * 2 * (400 * 50 + 50 * 50 + 50 * 50 + 50) + 2 * 3200
 
 
+# NEP workload: 100,000 atoms, four elements in equal parts, 0.06 atoms/A^3 random-packed cube;
+# radial cutoff 6 A (basis 8 -> 9 functions, n_max 4), angular cutoff 4 A (basis 8, n_max 4,
+# l_max 4 / 2 / 1), one 30-unit tanh hidden layer per element, seeded random parameters
+NEP_NATOMS, NEP_DENSITY, NEP_ELEMENTS = 100_000, 0.06, [3, 14, 8, 72]
+NEP_SEED_STRUCT, NEP_SEED_W = 2025, 12
+NEP_CPU_SAMPLE = 2000
+NEP_METRIC = "NEP E+F+virial atom-steps/s, fused FP32 vs FP64 oracle"
+
+
 def dist_setup():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

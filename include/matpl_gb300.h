@@ -186,6 +186,87 @@ int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, int natoms,
                   const int32_t *type_map, void *Ei, double *Etot, void *force, double *virial,
                   void *workspace, size_t workspace_bytes, void *stream);
 
+/* ------------------------------------------------------------------------------------
+ * NEP neighbor lists.  Replaces CalcOps calculate_neighbor / calculate_maxneigh
+ * (src/op/src/CalcOps.cpp:1025-1172, kernels src/op/kernel/calculateNepNeighbor.cu:8-380,
+ * CPU twin src/op/src/cpu_calculate_nepneighbor.cpp:6-203), bit-identical to the CPU twin.
+ * Frames are concatenated: num_atom [B] int64, position [sum N, 3] f64 (cartesian),
+ * box [B, 18] f64 (replicated cell h then h^-1, nep_data_loader.py:220-253), box_orig [B, 9]
+ * (lattice^T), num_cell [B, 3] int64.
+ * matpl_nep_neighbor writes NN_* [N] (full counts), NL_* [N, max_nn] int64 (-1 padded) and
+ * Ri_* [N, max_nn, 4] f64 = (r, x, y, z) (3 wide, no r, when with_rij = 0), zero padded.
+ * A list longer than max_nn sets MATPL_KERR_NEIGHBOR_OVERFLOW in err_dev (outputs invalid;
+ * the reference writes past the end instead).  MATPL_KERR_BAD_BOX flags num_cell < 1.
+ * matpl_nep_maxneigh writes only the counts: NN_* [N], or [N, ntypes] per neighbor element
+ * when with_type (type_map [N] int64 element index).
+ * ---------------------------------------------------------------------------------- */
+#define MATPL_KERR_BAD_BOX 4             /* num_cell entry < 1 */
+#define MATPL_KERR_BAD_COUNT 5           /* num_atom does not sum to natoms, or a list index
+                                            outside [0, natoms) */
+size_t matpl_nep_neighbor_workspace_bytes(int nframes, long long natoms);
+int matpl_nep_neighbor(int nframes, long long natoms, const long long *num_atom,
+                       const double *box, const double *box_orig, const long long *num_cell,
+                       const double *position, double cutoff_radial, double cutoff_angular,
+                       int max_nn_radial, int max_nn_angular, int with_rij,
+                       long long *NN_radial, long long *NN_angular, long long *NL_radial,
+                       long long *NL_angular, double *Ri_radial, double *Ri_angular,
+                       int *err_dev, void *workspace, size_t workspace_bytes, void *stream);
+int matpl_nep_maxneigh(int nframes, long long natoms, const long long *num_atom,
+                       const double *box, const double *box_orig, const long long *num_cell,
+                       const double *position, double cutoff_radial, double cutoff_angular,
+                       int ntypes, const long long *type_map, int with_type,
+                       long long *NN_radial, long long *NN_angular, int *err_dev,
+                       void *workspace, size_t workspace_bytes, void *stream);
+
+/* ------------------------------------------------------------------------------------
+ * Fused NEP energy + force + virial.  Replaces NEP.forward + calculate_force_virial
+ * (src/model/nep_net.py:293-438, 486-648): descriptor (calculateNepFeat / calculateNepMbFeat,
+ * CalcOps.cpp:669-1023), the per-element single-hidden-layer FittingNet
+ * (src/model/nep_fitting.py:136-160), dE/dRi and calculateNepForce / calculateNepVirial.
+ * Compiled shapes: n_max <= 7, basis_size <= 15, l_max = (4 or 0, 2 or 0, 1 or 0),
+ * neuron <= 128, ntypes <= 64.
+ * params: device buffer in the layout of matpl_gb300/nep.py: pack_params (compute dtype):
+ *   c2 [T,T,n_max_r+1,basis_r+1] | c3 [T,T,n_max_a+1,basis_a+1] | q_scaler [F] |
+ *   per element: W0 [F,H] | b0 [H] | W1 [H] | b1
+ * ---------------------------------------------------------------------------------- */
+typedef struct {
+    int ntypes;
+    int n_max_radial, basis_radial;     /* NepParam n_max[0], basis_size[0] */
+    int n_max_angular, basis_angular;   /* n_max[1], basis_size[1] */
+    int l_max_3b, l_max_4b, l_max_5b;   /* l_max */
+    int neuron;                         /* hidden units */
+    int train_2b;                       /* radial descriptor present */
+    double cutoff_radial, cutoff_angular;
+    const void *params;                 /* packed parameters (device, compute dtype) */
+    int32_t *err_dev;                   /* device int32 for MATPL_KERR_* codes */
+} matpl_nep_model;
+
+size_t matpl_nep_param_count(const matpl_nep_model *model);
+size_t matpl_nep_workspace_bytes(int dtype, int nframes, long long natoms);
+
+/* dtype MATPL_F32 (FP32 arithmetic, FP64 energy / virial sums) or MATPL_F64.
+ * Lists as matpl_nep_neighbor writes them (with_rij = 1); type_map [N] int64 element index.
+ * Outputs: Ei [N] and force [N, 3] in the compute dtype, Etot [B] f64, virial [B, 9] f64 with
+ * virial[a*3+c] = -sum_pairs (dE/dr_ij)_a (r_ij)_c (the sign NEP.forward returns). */
+int matpl_nep_eval(int dtype, const matpl_nep_model *model, int nframes, long long natoms,
+                   const long long *num_atom, const long long *type_map, int max_nn_radial,
+                   const long long *NN_radial, const long long *NL_radial,
+                   const double *Ri_radial, int max_nn_angular, const long long *NN_angular,
+                   const long long *NL_angular, const double *Ri_angular, void *Ei,
+                   double *Etot, void *force, double *virial, void *workspace,
+                   size_t workspace_bytes, void *stream);
+
+/* Descriptor only: feats [N, F] in the compute dtype, before q_scaler (the q of
+ * NEP.calculate_qn, src/model/nep_net.py:648-670; feature order [radial n] + [l = 1..4, each
+ * all n] + [4-body all n] + [5-body all n]).  Same inputs and workspace as matpl_nep_eval. */
+int matpl_nep_descriptor(int dtype, const matpl_nep_model *model, int nframes, long long natoms,
+                         const long long *num_atom, const long long *type_map, int max_nn_radial,
+                         const long long *NN_radial, const long long *NL_radial,
+                         const double *Ri_radial, int max_nn_angular,
+                         const long long *NN_angular, const long long *NL_angular,
+                         const double *Ri_angular, void *feats, void *workspace,
+                         size_t workspace_bytes, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,6 +12,8 @@ MATPL_F32, MATPL_F64, MATPL_MIXED, MATPL_MIXED_FAST, MATPL_MIXED_TANHF = 0, 1, 2
 KERR_NEIGHBOR_OVERFLOW = 1
 KERR_BAD_TYPE = 2
 KERR_TIMEOUT = 3
+KERR_BAD_BOX = 4
+KERR_BAD_COUNT = 5
 
 _c = ctypes
 _vp, _i, _d, _sz = _c.c_void_p, _c.c_int, _c.c_double, _c.c_size_t
@@ -23,6 +25,16 @@ class MatplDpModel(ctypes.Structure):
                 ("rmin", _d), ("rmax", _d), ("params", _vp), ("davg", _vp), ("dstd", _vp),
                 ("err_dev", _vp)]
 
+
+class MatplNepModel(ctypes.Structure):
+    """Mirror of ``matpl_nep_model``."""
+    _fields_ = [("ntypes", _i), ("n_max_radial", _i), ("basis_radial", _i),
+                ("n_max_angular", _i), ("basis_angular", _i), ("l_max_3b", _i), ("l_max_4b", _i),
+                ("l_max_5b", _i), ("neuron", _i), ("train_2b", _i), ("cutoff_radial", _d),
+                ("cutoff_angular", _d), ("params", _vp), ("err_dev", _vp)]
+
+
+_ll = _c.c_longlong
 
 # name -> (restype, argtypes)
 SIGNATURES = {
@@ -47,6 +59,17 @@ SIGNATURES = {
     "matpl_dp_workspace_bytes": (_sz, [_i, _i, _i]),
     "matpl_dp_eval": (_i, [_i, _c.POINTER(MatplDpModel), _i, _i, _i, _i, _vp, _vp, _vp, _vp,
                            _vp, _vp, _vp, _vp, _sz, _vp]),
+    "matpl_nep_neighbor_workspace_bytes": (_sz, [_i, _ll]),
+    "matpl_nep_neighbor": (_i, [_i, _ll, _vp, _vp, _vp, _vp, _vp, _d, _d, _i, _i, _i, _vp, _vp,
+                                _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "matpl_nep_maxneigh": (_i, [_i, _ll, _vp, _vp, _vp, _vp, _vp, _d, _d, _i, _vp, _i, _vp, _vp,
+                                _vp, _vp, _sz, _vp]),
+    "matpl_nep_param_count": (_sz, [_c.POINTER(MatplNepModel)]),
+    "matpl_nep_workspace_bytes": (_sz, [_i, _i, _ll]),
+    "matpl_nep_eval": (_i, [_i, _c.POINTER(MatplNepModel), _i, _ll, _vp, _vp, _i, _vp, _vp, _vp,
+                            _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "matpl_nep_descriptor": (_i, [_i, _c.POINTER(MatplNepModel), _i, _ll, _vp, _vp, _i, _vp, _vp,
+                                  _vp, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
 }
 
 

@@ -227,3 +227,123 @@ def pack_params(cfg: NepConfig, p: Dict[str, torch.Tensor]) -> torch.Tensor:
     flat = torch.cat([x.detach().to(torch.float64).cpu() for x in parts])
     assert flat.numel() == param_count(cfg)
     return flat
+
+
+# ----------------------------------------------------------------------------------------------
+# GPU evaluator (the NEP.forward drop-in)
+# ----------------------------------------------------------------------------------------------
+NEP_PRECISIONS = {"float64": (1, torch.float64), "float32": (0, torch.float32)}
+
+
+class NEP(torch.nn.Module):
+    """Inference NEP on GB300 through ``matpl_nep_eval``.
+
+    ``forward`` takes what ``src/model/nep_net.py:NEP.forward`` takes (the six tensors of
+    ``calculate_neighbor`` with with_rij, num_atom, atom_type_map) and returns
+    (Etot [B, 1], Ei [N], Force [N, 3], Egroup, Virial [B, 9]).  ``precision`` "float32" runs the
+    fused kernel in FP32 (FP64 energy / virial sums), "float64" in FP64."""
+
+    def __init__(self, cfg: NepConfig, params: Dict[str, torch.Tensor], precision: str = "float32",
+                 device="cuda", check_errors: bool = True):
+        super().__init__()
+        from . import _lib
+        if precision not in NEP_PRECISIONS:
+            raise _lib.MatplError(f"unknown precision {precision!r}; one of {list(NEP_PRECISIONS)}")
+        self.cfg = cfg
+        self.precision = precision
+        self.code, self.dtype = NEP_PRECISIONS[precision]
+        self.check_errors = check_errors
+        dev = torch.device(device)
+        self.device = dev
+        self.register_buffer("packed", pack_params(cfg, params).to(device=dev, dtype=self.dtype))
+        self.register_buffer("err", torch.zeros(1, dtype=torch.int32, device=dev))
+        self._model = self._model_struct()
+        lib = _lib.load()
+        n = lib.matpl_nep_param_count(self._model)
+        if n != self.packed.numel():
+            raise _lib.MatplError(f"packed parameters {self.packed.numel()} != {n} expected")
+
+    def _model_struct(self):
+        from ._lib import MatplNepModel, ptr
+        m = MatplNepModel()
+        c = self.cfg
+        m.ntypes = c.ntypes
+        m.n_max_radial, m.basis_radial = c.n_max[0], c.basis_size[0]
+        m.n_max_angular, m.basis_angular = c.n_max[1], c.basis_size[1]
+        m.l_max_3b, m.l_max_4b, m.l_max_5b = c.l_max
+        m.neuron = c.neuron
+        m.train_2b = int(c.train_2b)
+        m.cutoff_radial, m.cutoff_angular = float(c.cutoff[0]), float(c.cutoff[1])
+        m.params = ptr(self.packed)
+        m.err_dev = ptr(self.err)
+        return m
+
+    def evaluate(self, NN_radial, NL_radial, Ri_radial, NN_angular, NL_angular, Ri_angular,
+                 num_atom, atom_type_map, out=None, descriptor_only: bool = False):
+        """Raw evaluation: dict(Ei [N], Etot [B] f64, Force [N, 3], Virial [B, 9] f64)."""
+        import ctypes
+        from . import _lib
+        from ._lib import check, ptr
+        from .ops import workspace
+        if not Ri_radial.is_cuda:
+            raise _lib.MatplError("NEP.evaluate takes CUDA tensors (no CPU fallback)")
+        dev = Ri_radial.device
+        N = NL_radial.shape[0]
+        na = num_atom.to(device=dev, dtype=torch.int64).reshape(-1).contiguous()
+        B = na.shape[0]
+
+        def i64(t):
+            return t if (t.dtype == torch.int64 and t.is_contiguous()) else t.to(torch.int64).contiguous()
+
+        def f64(t):
+            return t if (t.dtype == torch.float64 and t.is_contiguous()) else t.to(torch.float64).contiguous()
+        tm = i64(atom_type_map.to(dev))
+        if Ri_radial.shape[-1] != 4 or Ri_angular.shape[-1] != 4:
+            raise _lib.MatplError("Ri_radial / Ri_angular must be (r, x, y, z) (with_rij = True)")
+        lib = _lib.load()
+        ws = workspace(dev, lib.matpl_nep_workspace_bytes(self.code, B, N), "nep")
+        lists = (NL_radial.shape[1], ptr(i64(NN_radial)), ptr(i64(NL_radial)), ptr(f64(Ri_radial)),
+                 NL_angular.shape[1], ptr(i64(NN_angular)), ptr(i64(NL_angular)),
+                 ptr(f64(Ri_angular)))
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        if descriptor_only:
+            feats = torch.empty(N, self.cfg.feature_nums, dtype=self.dtype, device=dev)
+            check(lib.matpl_nep_descriptor(self.code, ctypes.byref(self._model), B, N, ptr(na),
+                                           ptr(tm), *lists, ptr(feats), ptr(ws), ws.numel(),
+                                           stream), "matpl_nep_descriptor")
+            out = feats
+        else:
+            if out is None:
+                out = {"Ei": torch.empty(N, dtype=self.dtype, device=dev),
+                       "Etot": torch.empty(B, dtype=torch.float64, device=dev),
+                       "Force": torch.empty(N, 3, dtype=self.dtype, device=dev),
+                       "Virial": torch.empty(B, 9, dtype=torch.float64, device=dev)}
+            check(lib.matpl_nep_eval(self.code, ctypes.byref(self._model), B, N, ptr(na), ptr(tm),
+                                     *lists, ptr(out["Ei"]), ptr(out["Etot"]), ptr(out["Force"]),
+                                     ptr(out["Virial"]), ptr(ws), ws.numel(), stream),
+                  "matpl_nep_eval")
+        if self.check_errors:
+            code = int(self.err.item())
+            if code:
+                self.err.zero_()
+                raise _lib.MatplError(f"matpl_nep_eval kernel error code {code}")
+        return out
+
+    def descriptor(self, NN_radial, NL_radial, Ri_radial, NN_angular, NL_angular, Ri_angular,
+                   num_atom, atom_type_map):
+        """feats [N, F] before q_scaler (the q of NEP.calculate_qn), compute dtype."""
+        return self.evaluate(NN_radial, NL_radial, Ri_radial, NN_angular, NL_angular, Ri_angular,
+                             num_atom, atom_type_map, descriptor_only=True)
+
+    def forward(self, NN_radial, NL_radial, Ri_radial, NN_angular, NL_angular, Ri_angular,
+                num_atom, atom_type_map, Egroup_weight=None, divider=None, is_calc_f=True):
+        r = self.evaluate(NN_radial, NL_radial, Ri_radial, NN_angular, NL_angular, Ri_angular,
+                          num_atom, atom_type_map)
+        Ei = r["Ei"]
+        Egroup = None
+        if Egroup_weight is not None and divider is not None:      # nep_net.py:246-266
+            Egroup = torch.divide(torch.matmul(Egroup_weight, Ei).squeeze(-1), divider)
+        Etot = r["Etot"].to(self.dtype).unsqueeze(-1)
+        if is_calc_f is False:
+            return Etot, Ei, None, Egroup, None
+        return Etot, Ei, r["Force"], Egroup, r["Virial"].to(self.dtype)

@@ -232,3 +232,81 @@ def find_neighbore(type_maps: torch.Tensor, frac_position: torch.Tensor, lattice
     if with_counts:
         return ln, idr, cnt
     return ln, idr
+
+
+# ----------------------------------------------------------------------------------------------
+# NEP neighbor operators (CalcOps.calculate_neighbor / calculate_maxneigh, CalcOps.cpp:1025-1172)
+# ----------------------------------------------------------------------------------------------
+def _nep_frames(num_atoms, box, box_orig, num_cell, position):
+    _require_cuda(position)
+    dev = position.device
+    na = num_atoms.to(device=dev, dtype=torch.int64).reshape(-1).contiguous()
+    B = na.shape[0]
+    bx = box.to(device=dev, dtype=torch.float64).reshape(B, 18).contiguous()
+    bo = box_orig.to(device=dev, dtype=torch.float64).reshape(B, 9).contiguous()
+    nc = num_cell.to(device=dev, dtype=torch.int64).reshape(B, 3).contiguous()
+    pos = position.to(torch.float64).reshape(-1, 3).contiguous()
+    return dev, na, bx, bo, nc, pos
+
+
+def _nep_kernel_error(err: torch.Tensor, what: str):
+    code = int(err.item())
+    if code == _lib.KERR_NEIGHBOR_OVERFLOW:
+        raise NeighborOverflow(f"{what}: a neighbor list is longer than max_NN")
+    if code:
+        raise _lib.MatplError(f"{what} kernel error code {code}")
+
+
+def calculate_maxneigh(num_atoms: torch.Tensor, box: torch.Tensor, box_orig: torch.Tensor,
+                       num_cell: torch.Tensor, position: torch.Tensor, cutoff_2b: float,
+                       cutoff_3b: float, atom_type_num: int, atom_type_map: torch.Tensor,
+                       with_type: bool) -> List[torch.Tensor]:
+    """Neighbor counts [NN_radial, NN_angular], each [N] (or [N * ntypes] per neighbor element
+    when ``with_type``), as ``CalcOps.calculate_maxneigh`` returns them."""
+    dev, na, bx, bo, nc, pos = _nep_frames(num_atoms, box, box_orig, num_cell, position)
+    N = pos.shape[0]
+    nt = int(atom_type_num) if with_type else 1
+    tm = atom_type_map.to(device=dev, dtype=torch.int64).contiguous()
+    NN_r = torch.empty(N * nt, dtype=torch.int64, device=dev)
+    NN_a = torch.empty(N * nt, dtype=torch.int64, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    lib = _lib.load()
+    ws = workspace(dev, lib.matpl_nep_neighbor_workspace_bytes(na.shape[0], N), "nep_neighbor")
+    check(lib.matpl_nep_maxneigh(na.shape[0], N, ptr(na), ptr(bx), ptr(bo), ptr(nc), ptr(pos),
+                                 float(cutoff_2b), float(cutoff_3b), int(atom_type_num), ptr(tm),
+                                 int(bool(with_type)), ptr(NN_r), ptr(NN_a), ptr(err), ptr(ws),
+                                 ws.numel(), _stream(dev)), "matpl_nep_maxneigh")
+    _nep_kernel_error(err, "calculate_maxneigh")
+    return [NN_r, NN_a]
+
+
+def calculate_neighbor(num_atoms: torch.Tensor, atom_type_map: torch.Tensor,
+                       atom_types: torch.Tensor, box: torch.Tensor, box_orig: torch.Tensor,
+                       num_cell: torch.Tensor, position: torch.Tensor, cutoff_2b: float,
+                       cutoff_3b: float, max_NN_radial: int, max_NN_angular: int,
+                       with_rij: bool, check_overflow: bool = True) -> List[torch.Tensor]:
+    """[NN_radial, NN_angular, NL_radial, NL_angular, Ri_radial, Ri_angular] exactly as
+    ``CalcOps.calculate_neighbor`` returns them (atom_type_map / atom_types are accepted for
+    signature compatibility; the lists do not depend on them).  A list longer than max_NN
+    raises NeighborOverflow when ``check_overflow`` (one device read)."""
+    dev, na, bx, bo, nc, pos = _nep_frames(num_atoms, box, box_orig, num_cell, position)
+    N = pos.shape[0]
+    w = 4 if with_rij else 3
+    mr, ma = int(max_NN_radial), int(max_NN_angular)
+    NN_r = torch.empty(N, dtype=torch.int64, device=dev)
+    NN_a = torch.empty(N, dtype=torch.int64, device=dev)
+    NL_r = torch.empty(N, mr, dtype=torch.int64, device=dev)
+    NL_a = torch.empty(N, ma, dtype=torch.int64, device=dev)
+    Ri_r = torch.empty(N, mr, w, dtype=torch.float64, device=dev)
+    Ri_a = torch.empty(N, ma, w, dtype=torch.float64, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    lib = _lib.load()
+    ws = workspace(dev, lib.matpl_nep_neighbor_workspace_bytes(na.shape[0], N), "nep_neighbor")
+    check(lib.matpl_nep_neighbor(na.shape[0], N, ptr(na), ptr(bx), ptr(bo), ptr(nc), ptr(pos),
+                                 float(cutoff_2b), float(cutoff_3b), mr, ma, int(bool(with_rij)),
+                                 ptr(NN_r), ptr(NN_a), ptr(NL_r), ptr(NL_a), ptr(Ri_r), ptr(Ri_a),
+                                 ptr(err), ptr(ws), ws.numel(), _stream(dev)),
+          "matpl_nep_neighbor")
+    if check_overflow:
+        _nep_kernel_error(err, "calculate_neighbor")
+    return [NN_r, NN_a, NL_r, NL_a, Ri_r, Ri_a]
