@@ -15,7 +15,12 @@ forces and virial (what an MD step needs).  Synthetic data: no dataset is involv
   cpu_baseline : MatPL's DP algorithm (oracle port of dp_dp_script.DP, torch FP64) on the
           host cores, on a bounded 4,000-atom sample of the same workload
 
---impl reference runs only that CPU implementation and prints its line.
+A second workload, NEP (100,000 atoms, four elements, radial / angular cutoffs 6 / 4 A), is
+measured in the same run and reported in the line's "nep" object (step = calculate_neighbor with
+exact FP64 lists + the fused FP32 energy / force / virial kernel); --workload nep prints it as
+its own line.
+
+--impl reference runs only the CPU implementation (oracle port) and prints its line.
 For N > 1 (torchrun) every rank runs its own replica (replicas only, weak scaling).
 """
 import argparse
@@ -49,7 +54,7 @@ FLOP_FIT_ATOM = 2 * 4 * 25 * 16 + 2 * 2 * (400 * 50 + 50 * 50 + 50 * 50 + 50) + 
 # l_max 4 / 2 / 1), one 30-unit tanh hidden layer per element, seeded random parameters
 NEP_NATOMS, NEP_DENSITY, NEP_ELEMENTS = 100_000, 0.06, [3, 14, 8, 72]
 NEP_SEED_STRUCT, NEP_SEED_W = 2025, 12
-NEP_CPU_SAMPLE = 2000
+NEP_CPU_SAMPLE = 4000
 NEP_METRIC = "NEP E+F+virial atom-steps/s, fused FP32 vs FP64 oracle"
 
 
@@ -164,11 +169,214 @@ def cpu_baseline_run(steps, warmup):
             "sec_per_step": med, "steps": steps}
 
 
+def nep_flops(cfg, n_r_pairs, n_a_pairs, natoms):
+    """Algorithmic FLOPs of one NEP E+F+V evaluation (no recompute), from the model shape:
+    per radial pair   basis f_k and f_k' (6 kr), g_n and g_n' (4 nr kr), dE/dr (2 nr), force
+                      and virial (24);
+    per angular pair  basis (6 ka), g_n and g_n' (4 na ka), 24 harmonics (40), s_nlm (48 na),
+                      adjoint sums A_n and B_lm (96 na), harmonic gradients (80), G (144),
+                      force and virial (38);
+    per atom          features (48 na + 30 na), network forward 2 F H + H and adjoint
+                      2 F H + F + 5 H, dE/ds (10 * 24 na)."""
+    nr, kr, na, ka, F, H = cfg.nr, cfg.kr, cfg.na, cfg.ka, cfg.feature_nums, cfg.neuron
+    pr = 6 * kr + 4 * nr * kr + 2 * nr + 24
+    pa = 6 * ka + 4 * na * ka + 40 + 48 * na + 96 * na + 80 + 144 + 38
+    at = 78 * na + 2 * F * H + H + 2 * F * H + F + 5 * H + 240 * na
+    return pr * n_r_pairs + pa * n_a_pairs + at * natoms
+
+
+def nep_workload(natoms=NEP_NATOMS, seed=NEP_SEED_STRUCT):
+    from matpl_gb300 import nep as NP, structures
+    cfg = NP.NepConfig(atom_type=list(NEP_ELEMENTS))
+    st = structures.random_packed(natoms, NEP_DENSITY, NEP_ELEMENTS, [0.25] * 4, seed=seed)
+    fr = NP.frames_from_structures([st], cfg.cutoff[0])
+    prm = NP.init_params(cfg, NEP_SEED_W, energy_shift=-3.0)
+    return cfg, fr, prm
+
+
+def cpu_baseline_nep(steps, warmup):
+    """MatPL's NEP algorithm on the host cores: the oracle port (restated neighbor operator in C,
+    nep_net.NEP's CPU descriptor / network / autograd forces in torch FP64) on a bounded sample."""
+    from oracle import nep_oracle as NO
+    ncores = os.cpu_count() or 1
+    torch.set_num_threads(ncores)
+    cfg, fr, prm = nep_workload(NEP_CPU_SAMPLE, seed=NEP_SEED_STRUCT + 1)
+    cr, ca = NO.maxneigh(fr, cfg.cutoff[0], cfg.cutoff[1])
+    mr, ma = int(cr.max()), int(ca.max())
+    tm = torch.tensor(fr.type_map)
+
+    def step():
+        L = NO.neighbor(fr, cfg.cutoff[0], cfg.cutoff[1], mr, ma)
+        out = NO.nep_eval(cfg, prm, fr.num_atom, tm, torch.tensor(L[2]), torch.tensor(L[4]),
+                          torch.tensor(L[3]), torch.tensor(L[5]))
+        return float(out["Etot"].sum())
+
+    for _ in range(warmup):
+        step()
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        step()
+        ts.append(time.perf_counter() - t0)
+    med = statistics.median(ts)
+    return {"value": NEP_CPU_SAMPLE / med, "unit": "atom-steps/s", "cores": ncores, "kind": "port",
+            "sample": f"{NEP_CPU_SAMPLE}-atom four-element box of the same density and model, FP64, "
+                      f"neighbor lists + E/F/V per step, median of {steps}",
+            "sec_per_step": med, "steps": steps}
+
+
+def run_nep(args, ws, local, steps, warmup, sample_clocks=True):
+    """The NEP step on this GPU: calculate_neighbor (exact FP64 lists, the reference's layout) +
+    the fused FP32 descriptor / network / force / virial kernel, 100,000 atoms."""
+    from matpl_gb300 import _lib, nep as NP, ops
+    dev = torch.device("cuda", local)
+    cfg, fr, prm = nep_workload()
+    N = fr.natoms
+    c = lambda a, dt: torch.tensor(np.ascontiguousarray(a), dtype=dt, device=dev)  # noqa: E731
+    na, tm, bx, bo, nc = (c(fr.num_atom.reshape(-1, 1), torch.int64), c(fr.type_map, torch.int64),
+                          c(fr.box, torch.float64), c(fr.box_orig, torch.float64),
+                          c(fr.num_cell, torch.int64))
+    pos_d = c(fr.position, torch.float64)
+    at = torch.arange(cfg.ntypes, device=dev)
+    cr, ca = ops.calculate_maxneigh(na, bx, bo, nc, pos_d, cfg.cutoff[0], cfg.cutoff[1],
+                                    cfg.ntypes, tm, False)
+    mr, ma = int(cr.max()), int(ca.max())
+    n_r, n_a = int(cr.sum()), int(ca.sum())
+    lists = ops.calculate_neighbor(na, tm, at, bx, bo, nc, pos_d, cfg.cutoff[0], cfg.cutoff[1],
+                                   mr, ma, True)
+    # q_scaler from this box's descriptors (update_scaler_values, nep_net.py:1020-1058)
+    m64 = NP.NEP(cfg, prm, "float64", device=dev)
+    feats = m64.descriptor(lists[0], lists[2], lists[4], lists[1], lists[3], lists[5], na, tm)
+    prm = dict(prm)
+    prm["q_scaler"] = NP.calc_q_scaler(cfg, feats).cpu()
+    m64 = NP.NEP(cfg, prm, "float64", device=dev)
+    m32 = NP.NEP(cfg, prm, "float32", device=dev, check_errors=False)
+    r64 = m64.evaluate(lists[0], lists[2], lists[4], lists[1], lists[3], lists[5], na, tm)
+
+    def step(pos):
+        NN_r, NN_a, NL_r, NL_a, Ri_r, Ri_a = ops.calculate_neighbor(
+            na, tm, at, bx, bo, nc, pos, cfg.cutoff[0], cfg.cutoff[1], mr, ma, True,
+            check_overflow=False)
+        return m32.evaluate(NN_r, NL_r, Ri_r, NN_a, NL_a, Ri_a, na, tm)
+
+    r32 = step(pos_d)
+    torch.cuda.synchronize()
+    acc = {"force_rmse_vs_f64_eV_per_A": (r32["Force"].double() - r64["Force"]).pow(2).mean().sqrt().item(),
+           "force_max_abs_err_eV_per_A": (r32["Force"].double() - r64["Force"]).abs().max().item(),
+           "energy_err_per_atom_eV": abs(r32["Etot"].item() - r64["Etot"].item()) / N,
+           "virial_max_abs_err_eV": (r32["Virial"] - r64["Virial"]).abs().max().item()}
+    for _ in range(warmup):
+        step(pos_d)
+    sampler = ClockSampler(local) if sample_clocks else None
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    torch.cuda.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    _lib.profile_begin(max(4096, steps * 8))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        step(pos_d)
+    e1.record()
+    torch.cuda.synchronize()
+    prof = _lib.profile_collect()
+    barrier(ws)
+    clocks = sampler.stop() if sampler else None
+    ms = max_over_ranks(e0.elapsed_time(e1) / steps, ws)
+
+    # end to end: host positions in, energy / forces / virial out
+    pos_h = torch.tensor(fr.position).pin_memory()
+    F_h = torch.empty(N, 3, dtype=torch.float32).pin_memory()
+    E_h = torch.empty(1, dtype=torch.float64).pin_memory()
+    V_h = torch.empty(1, 9, dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        r = step(pos_h.to(dev, non_blocking=True))
+        F_h.copy_(r["Force"], non_blocking=True)
+        E_h.copy_(r["Etot"], non_blocking=True)
+        V_h.copy_(r["Virial"], non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+    for _ in range(3):
+        e2e_step()
+    e2e_steps = max(5, steps // 2)
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    t1 = time.perf_counter()
+    e2e_ms = max_over_ranks((t1 - t0) * 1e3 / e2e_steps, ws)
+
+    per_kernel = {k: {"ms_per_launch": v[0] / v[1], "launches": v[1]} for k, v in prof.items()}
+    tot = sum(v[0] for v in prof.values())
+    for k, v in prof.items():
+        per_kernel[k]["share"] = v[0] / tot if tot else None
+    sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    simt_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    fl = nep_flops(cfg, n_r, n_a, N)
+    t_eval = per_kernel["nep_eval"]["ms_per_launch"] * 1e-3
+    # neighbor operator: reads positions (24 B / atom), writes NN (16 B / atom) and the padded
+    # lists NL int64 + Ri f64 x 4 (40 B per slot, max_NN slots per atom, both lists)
+    nb_bytes = N * (24 + 16 + 40 * (mr + ma))
+    t_nb = per_kernel["nep_neighbor"]["ms_per_launch"] * 1e-3
+    peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(HERE, "MEASURED_PEAKS.json")) else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    # the eval kernel reads, per occupied slot, NL int64 + Ri f64 x 4 (40 B), per atom
+    # type + two counts (24 B) and writes Ei, the force accumulator and force (32 B)
+    ev_bytes = 40 * (n_r + n_a) + 56 * N
+    launches = sum(v[1] for v in prof.values())
+    return {
+        "metric": NEP_METRIC, "value": ws * N / (ms * 1e-3), "unit": "atom-steps/s",
+        "ms_per_step": ms, "steps": steps, "warmup": warmup, "dtype": "f32 (f64 lists, f64 sums)",
+        "config": {"workload": "NEP, 100,000 atoms, 4 elements (equal parts) random-packed at "
+                               "0.06 atoms/A^3; radial rc 6 A basis 8 n_max 4, angular rc 4 A "
+                               "basis 8 n_max 4 l_max 4/2/1, 30-unit tanh layer per element; "
+                               "step = calculate_neighbor + fused E/F/V",
+                   "natoms": N, "radial_pairs": n_r, "angular_pairs": n_a,
+                   "max_NN_radial": mr, "max_NN_angular": ma,
+                   "l2": "no flush: per-step lists ~0.4 GB exceed the 129 MB L2", **acc},
+        "e2e": {"value": ws * N / (e2e_ms * 1e-3), "unit": "atom-steps/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": pos_h.numel() * 8,
+                "d2h_bytes_per_step": F_h.numel() * 4 + 8 + 72},
+        "gpu_launches": launches, "kernels": per_kernel,
+        "roofline": {"kernel": "nep_eval", "bound": "simt_fp32", "achieved": fl / t_eval / 1e12,
+                     "peak": simt_peak, "unit": "TFLOP/s", "frac": fl / t_eval / 1e12 / simt_peak,
+                     "algorithmic_flops_per_launch": fl,
+                     "peak_source": "nominal FP32 SIMT at the sampled SM clock (152 SMs x 128 lanes x 2)",
+                     "hbm": {"achieved": ev_bytes / t_eval / 1e9, "peak": hbm_peak,
+                             "unit": "GB/s", "frac": ev_bytes / t_eval / 1e9 / hbm_peak,
+                             "algorithmic_bytes_per_launch": ev_bytes}},
+        "neighbor_roofline": {"kernel": "nep_neighbor", "bound": "fp64 (exact reference arithmetic)",
+                              "hbm_achieved": nb_bytes / t_nb / 1e9, "hbm_peak": hbm_peak,
+                              "unit": "GB/s", "frac": nb_bytes / t_nb / 1e9 / hbm_peak,
+                              "algorithmic_bytes_per_launch": nb_bytes},
+        "clocks": clocks,
+    }
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
     steps = max(3, min(args.steps, 10))
     warm = 1
+    if args.workload == "nep":
+        cb = cpu_baseline_nep(steps, warm)
+        line = {"metric": NEP_METRIC, "value": cb["value"], "unit": "atom-steps/s",
+                "n_gpus": args.gpus, "steps": steps, "warmup": warm,
+                "ms_per_step": cb["sec_per_step"] * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "impl": "reference",
+                "config": {"workload": f"NEP, {NEP_CPU_SAMPLE}-atom sample of the 100,000-atom "
+                                       "four-element 0.06/A^3 box", "device": "host CPU"},
+                "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
     cb = cpu_baseline_run(steps, warm)
     line = {"metric": METRIC, "value": cb["value"], "unit": "atom-steps/s", "n_gpus": args.gpus,
             "steps": steps, "warmup": warm, "ms_per_step": cb["sec_per_step"] * 1e3,
@@ -178,7 +386,8 @@ def run_reference(args, ws, rank):
                                    "0.05/A^3 box, m=150/type", "device": "host CPU"},
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+                    "d2h_bytes_per_step": 0},
+            "nep": None if args.no_nep else cpu_baseline_nep(3, 1)}
     print(json.dumps(line))
 
 
@@ -344,6 +553,12 @@ def run_ours(args, ws, rank, local):
     per_scope = {"nb_cells": 4, "dp_reduce": 2}
     launches = sum(v[1] * per_scope.get(k, 1) for k, v in prof.items())
 
+    nep = None
+    if not args.no_nep:
+        nep = run_nep(args, ws, local, steps=max(20, args.steps // 10), warmup=args.warmup,
+                      sample_clocks=False)
+        if rank == 0 and not args.no_cpu_baseline:
+            nep["cpu_baseline"] = cpu_baseline_nep(steps=8, warmup=1)
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline_run(steps=8, warmup=1)
@@ -371,7 +586,24 @@ def run_ours(args, ws, rank, local):
             "e2e": {"value": ws * NATOMS / (e2e_ms * 1e-3), "unit": "atom-steps/s",
                     "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "kernels": per_kernel, "roofline": roof,
-            "clocks": clocks, "cpu_baseline": cb}
+            "clocks": clocks, "cpu_baseline": cb, "nep": nep}
+    print(json.dumps(line))
+
+
+def run_nep_line(args, ws, rank, local):
+    torch.cuda.set_device(local)
+    from matpl_gb300 import _lib
+    _lib.load()
+    steps = args.steps if args.steps_given else 100
+    r = run_nep(args, ws, local, steps=steps, warmup=args.warmup)
+    if rank == 0 and not args.no_cpu_baseline:
+        r["cpu_baseline"] = cpu_baseline_nep(steps=8, warmup=1)
+    if rank != 0:
+        return
+    line = {"metric": r.pop("metric"), "value": r.pop("value"), "unit": r.pop("unit"),
+            "n_gpus": ws, "steps": r.pop("steps"), "warmup": r.pop("warmup"),
+            "ms_per_step": r.pop("ms_per_step"), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": r.pop("dtype"), "data": "synthetic", **r}
     print(json.dumps(line))
 
 
@@ -386,7 +618,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain-FP32 comparison run of a mixed form")
+    ap.add_argument("--no-nep", action="store_true", help="skip the NEP workload")
+    ap.add_argument("--workload", default="dp", choices=["dp", "nep"],
+                    help="dp: the headline DP line (with a nep object); nep: the NEP line alone")
+    argv = sys.argv[1:]
     args = ap.parse_args()
+    args.steps_given = any(a.startswith("--steps") for a in argv)
     args.warmup = max(3, args.warmup)
     if args.impl == "reference":
         ws = int(os.environ.get("WORLD_SIZE", "1"))
@@ -394,6 +631,9 @@ def main():
         run_reference(args, ws, rank)
         return
     ws, rank, local = dist_setup()
+    if args.workload == "nep":
+        run_nep_line(args, ws, rank, local)
+        return
     run_ours(args, ws, rank, local)
 
 

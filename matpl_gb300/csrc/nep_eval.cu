@@ -50,11 +50,15 @@ struct NepLayout {
     double rc_r_d, rc_a_d;
     int off_c2, off_c3, off_qs, off_net, net_stride;   // element offsets in params
     int nparams;
+    // shared-memory copy: hidden width padded to hp (a multiple of 4 with hp / 4 odd, so that
+    // 16-byte row loads of consecutive lanes fall in different banks), features padded to fmp
+    int hp, fmp, off_net_s, net_stride_s, nparams_s;
+    int kpr, kpa, off_c2_s, off_c3_s, off_qs_s;        // coefficient rows padded to 4
 };
 
 template <typename T> __device__ __forceinline__ void sincospi_t(T x, T *s, T *c);
 template <> __device__ __forceinline__ void sincospi_t<float>(float x, float *s, float *c) {
-    sincospif(x, s, c);
+    __sincosf(x * 3.14159265358979323846f, s, c);   // x in [0, 1): fast intrinsic suffices
 }
 template <> __device__ __forceinline__ void sincospi_t<double>(double x, double *s, double *c) {
     sincospi(x, s, c);
@@ -148,20 +152,78 @@ struct EvalArgs {
     void *facc;                     // float4 [N] (f32) or double [N, 3] (f64)
     void *feats;                    // descriptor only: q [N, F] before q_scaler, else NULL
     int *err;
+    // shared-memory layout (bytes): parameters, then one scratch area per warp
+    int smem_params, warp_bytes;
+    int o_stash_g, o_stash_b, o_s, o_dEds, o_fin, o_dq, o_dpre;
+    int o_rj, o_rv, o_rgp, o_aj, o_av, o_ag, o_agp;
 };
 
-// per-warp shared scratch (element counts, T elements)
-template <int NAM> struct WarpScratch {
-    static constexpr int FM = 8 + 6 * NAM;          // radial (<= 8) + angular features
-    static constexpr int stash_g = 0;               // [32][NAM]
-    static constexpr int stash_b = 32 * NAM;        // [32][24]
-    static constexpr int s = stash_b + 32 * 24;     // [NAM][24]
-    static constexpr int dEds = s + NAM * 24;       // [NAM][24]
-    static constexpr int fin = dEds + NAM * 24;     // [FM] scaled features
-    static constexpr int dq = fin + FM;             // [FM] dE/dq
-    static constexpr int dpre = dq + FM;            // [kMaxHidden]
-    static constexpr int size = dpre + kMaxHidden;
-};
+// descriptor constants in FP32 for the FP32 kernel (the same values as kC3B / kC4B / kC5B)
+__constant__ float kC3Bf[24] = {
+    0.238732414637843f, 0.238732414637843f, 0.238732414637843f,
+    0.099471839432435f, 1.1936620731892151f, 1.1936620731892151f, 0.2984155182973038f,
+    0.2984155182973038f,
+    0.139260575205408f, 0.20889086280811264f, 0.20889086280811264f, 2.088908628081126f,
+    2.088908628081126f, 0.34815143801352105f, 0.34815143801352105f,
+    0.01119058193614889f, 0.44762327744595565f, 0.44762327744595565f, 0.22381163872297782f,
+    0.22381163872297782f, 3.1333629421216895f, 3.1333629421216895f, 0.3916703677652112f,
+    0.3916703677652112f};
+__constant__ float kC4Bf[5] = {-0.007499480826664f, -0.134990654879954f, 0.067495327439977f,
+                               0.404971964639861f, -0.809943929279723f};
+__constant__ float kC5Bf[3] = {0.026596810706114f, 0.053193621412227f, 0.026596810706114f};
+
+template <typename T> __device__ __forceinline__ T C3(int i);
+template <> __device__ __forceinline__ float C3<float>(int i) { return kC3Bf[i]; }
+template <> __device__ __forceinline__ double C3<double>(int i) { return kC3B[i]; }
+template <typename T> __device__ __forceinline__ T C4(int i);
+template <> __device__ __forceinline__ float C4<float>(int i) { return kC4Bf[i]; }
+template <> __device__ __forceinline__ double C4<double>(int i) { return kC4B[i]; }
+template <typename T> __device__ __forceinline__ T C5(int i);
+template <> __device__ __forceinline__ float C5<float>(int i) { return kC5Bf[i]; }
+template <> __device__ __forceinline__ double C5<double>(int i) { return kC5B[i]; }
+
+// f64 -> f32, round to nearest even, with integer instructions: the FP64 pipe of this part
+// issues two lanes per clock, so the FP32 kernel keeps conversions off it.  Magnitudes below
+// 2^-126 become signed zero (inputs are pair vectors in Angstrom).
+__device__ __forceinline__ float f64_to_f32(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned sign = hi & 0x80000000u;
+    const unsigned ex = (hi >> 20) & 0x7ffu;
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    if (ex == 0x7ffu) return __uint_as_float(sign | 0x7f800000u | (m | (lo & 0x1fffffffu) ? 0x400000u : 0u));
+    const int e = (int)ex - 1023 + 127;
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+    const unsigned rest = lo & 0x1fffffffu;
+    unsigned r = ((unsigned)e << 23) | m;
+    r += (rest > 0x10000000u) || (rest == 0x10000000u && (m & 1u));
+    return __uint_as_float(sign | r);
+}
+template <typename T> __device__ __forceinline__ T ld_conv(const double *p);
+template <> __device__ __forceinline__ float ld_conv<float>(const double *p) {
+    return f64_to_f32(__ldg(p));
+}
+template <> __device__ __forceinline__ double ld_conv<double>(const double *p) { return __ldg(p); }
+
+// four consecutive elements from 16-byte aligned shared memory
+__device__ __forceinline__ void lds4(const float *p, float *o) {
+    const float4 v = *reinterpret_cast<const float4 *>(p);
+    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+}
+__device__ __forceinline__ void lds4(const double *p, double *o) {
+    const double2 a = reinterpret_cast<const double2 *>(p)[0];
+    const double2 b = reinterpret_cast<const double2 *>(p)[1];
+    o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+}
+
+__device__ __forceinline__ void sts4(float *p, float a, float b, float c, float d) {
+    *reinterpret_cast<float4 *>(p) = make_float4(a, b, c, d);
+}
+__device__ __forceinline__ void sts4(double *p, double a, double b, double c, double d) {
+    reinterpret_cast<double2 *>(p)[0] = make_double2(a, b);
+    reinterpret_cast<double2 *>(p)[1] = make_double2(c, d);
+}
 
 template <typename T>
 __device__ __forceinline__ void add_force(void *facc, long long j, T fx, T fy, T fz);
@@ -194,28 +256,68 @@ __device__ __forceinline__ void flush_frame(const EvalArgs &A, int frame, double
 template <typename T, int NRM, int KRM, int NAM, int KAM>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
-    using WS = WarpScratch<NAM>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *P = reinterpret_cast<T *>(smem_raw);
     const NepLayout &L = A.L;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const T *gp = reinterpret_cast<const T *>(A.params);
-    for (int q = threadIdx.x; q < L.nparams; q += blockDim.x) P[q] = gp[q];
-    T *W = P + ((L.nparams + 3) & ~3) + WS::size * wib;
+    T *P = reinterpret_cast<T *>(smem_raw);
+    // parameters: c2, c3, q_scaler as packed; per element W0 rows padded to Hp, b0, W1, b1
+    {
+        const T *gp = reinterpret_cast<const T *>(A.params);
+        const int T2 = L.ntypes * L.ntypes;
+        for (int q = threadIdx.x; q < T2 * L.nr * L.kpr; q += blockDim.x) {
+            const int row = q / L.kpr, k = q - row * L.kpr;
+            P[L.off_c2_s + q] = k < L.kr ? gp[L.off_c2 + row * L.kr + k] : T(0);
+        }
+        if (L.l3)
+            for (int q = threadIdx.x; q < T2 * L.na * L.kpa; q += blockDim.x) {
+                const int row = q / L.kpa, k = q - row * L.kpa;
+                P[L.off_c3_s + q] = k < L.ka ? gp[L.off_c3 + row * L.ka + k] : T(0);
+            }
+        for (int q = threadIdx.x; q < L.nfeat; q += blockDim.x) P[L.off_qs_s + q] = gp[L.off_qs + q];
+        const int Hp = L.hp;
+        for (int t = 0; t < L.ntypes; ++t) {
+            const T *src = gp + L.off_net + t * L.net_stride;
+            T *dst = P + L.off_net_s + t * L.net_stride_s;
+            for (int q = threadIdx.x; q < L.nfeat * Hp; q += blockDim.x) {
+                const int f = q / Hp, k = q - f * Hp;
+                dst[q] = k < L.hidden ? src[f * L.hidden + k] : T(0);
+            }
+            for (int q = threadIdx.x; q < Hp; q += blockDim.x) {
+                dst[L.nfeat * Hp + q] = q < L.hidden ? src[L.nfeat * L.hidden + q] : T(0);
+                dst[L.nfeat * Hp + Hp + q] = q < L.hidden ? src[L.nfeat * L.hidden + L.hidden + q] : T(0);
+            }
+            if (threadIdx.x == 0) dst[L.nfeat * Hp + 2 * Hp] = src[L.nfeat * L.hidden + 2 * L.hidden];
+        }
+    }
+    unsigned char *Wb = smem_raw + A.smem_params + (size_t)A.warp_bytes * wib;
+    T *stash_g = reinterpret_cast<T *>(Wb + A.o_stash_g);    // [32][NAM]
+    T *stash_b = reinterpret_cast<T *>(Wb + A.o_stash_b);    // [32][25]
+    T *s_sm = reinterpret_cast<T *>(Wb + A.o_s);             // [NAM][24]
+    T *dEds = reinterpret_cast<T *>(Wb + A.o_dEds);          // [NAM][24]
+    T *fin = reinterpret_cast<T *>(Wb + A.o_fin);            // [FMp] scaled features
+    T *dq = reinterpret_cast<T *>(Wb + A.o_dq);              // [FMp] dE/dq
+    T *dpre = reinterpret_cast<T *>(Wb + A.o_dpre);          // [Hp]
+    int *rj = reinterpret_cast<int *>(Wb + A.o_rj);          // radial pairs: neighbor
+    T *rv = reinterpret_cast<T *>(Wb + A.o_rv);              //   (x, y, z, 1/r)
+    T *rgp = reinterpret_cast<T *>(Wb + A.o_rgp);            //   g_n'(r)   [max_r][NRM]
+    int *aj = reinterpret_cast<int *>(Wb + A.o_aj);          // angular pairs: neighbor
+    T *av = reinterpret_cast<T *>(Wb + A.o_av);              //   (x, y, z, 1/r)
+    T *ag = reinterpret_cast<T *>(Wb + A.o_ag);              //   g_n(r)    [max_a][NAM]
+    T *agp = reinterpret_cast<T *>(Wb + A.o_agp);            //   g_n'(r)   [max_a][NAM]
+    for (int q = lane; q < L.fmp; q += 32) fin[q] = T(0);
+    for (int q = lane; q < L.hp; q += 32) dpre[q] = T(0);
     __syncthreads();
 
-    const T *c2 = P + L.off_c2, *c3 = P + L.off_c3, *qs = P + L.off_qs;
+    const T *c2 = P + L.off_c2_s, *c3 = P + L.off_c3_s, *qs = P + L.off_qs_s;
+    constexpr int KRP = (KRM + 3) / 4 * 4, KAP = (KAM + 3) / 4 * 4;
     const T rc_r = (T)L.rc_r_d, rc_a = (T)L.rc_a_d;
     const T rcinv_r = T(1) / rc_r, rcinv_a = T(1) / rc_a;
-    T *stash_g = W + WS::stash_g, *stash_b = W + WS::stash_b, *s_sm = W + WS::s,
-      *dEds = W + WS::dEds, *fin = W + WS::fin, *dq = W + WS::dq, *dpre = W + WS::dpre;
 
     const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + wib;
     const long long a_begin = gw * atoms_per_warp;
     long long a_end = a_begin + atoms_per_warp;
     if (a_end > A.natoms) a_end = A.natoms;
     if (a_begin >= a_end) return;
-    // frame of the first atom
     int frame = 0;
     {
         int lo = 0, hi = A.nframes - 1;
@@ -233,7 +335,7 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
 
     for (long long i = a_begin; i < a_end; ++i) {
         while (i >= frame_end && frame + 1 < A.nframes) {
-            flush_frame<T>(A, frame, e_frame, vir, lane);
+            if (!A.feats) flush_frame<T>(A, frame, e_frame, vir, lane);
             e_frame = 0.0;
             ++frame;
             frame_end = A.frame_start[frame + 1];
@@ -242,37 +344,55 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
         if (ti < 0 || ti >= L.ntypes) {
             if (lane == 0) {
                 atomicOr(A.err, MATPL_KERR_BAD_TYPE);
-                reinterpret_cast<T *>(A.Ei)[i] = T(0);
+                if (!A.feats) reinterpret_cast<T *>(A.Ei)[i] = T(0);
             }
             continue;
         }
-        const long long nnr = L.two ? min(A.NN_r[i], (long long)A.max_r) : 0;
-        const long long nna = L.l3 ? min(A.NN_a[i], (long long)A.max_a) : 0;
+        const int nnr = L.two ? (int)min(A.NN_r[i], (long long)A.max_r) : 0;
+        const int nna = L.l3 ? (int)min(A.NN_a[i], (long long)A.max_a) : 0;
         const long long row_r = i * A.max_r, row_a = i * A.max_a;
 
-        // ---------------- radial descriptor
+        // ---------------- radial descriptor; pair vector and g_n' kept for the force pass
         T qr[NRM];
 #pragma unroll
         for (int n = 0; n < NRM; ++n) qr[n] = T(0);
-        for (long long sl = lane; sl < nnr; sl += 32) {
+        for (int sl = lane; sl < nnr; sl += 32) {
             const long long j = A.NL_r[row_r + sl];
-            if (j < 0) continue;
-            if (j >= A.natoms) { atomicOr(A.err, MATPL_KERR_BAD_COUNT); continue; }
-            const int tj = (int)A.type_map[j];
-            if (tj < 0 || tj >= L.ntypes) { atomicOr(A.err, MATPL_KERR_BAD_TYPE); continue; }
-            const T r = (T)A.Ri_r[(row_r + sl) * 4];
-            T f[KRM], df[KRM];
+            int tj = -1;
+            if (j >= 0 && j < A.natoms) {
+                tj = (int)A.type_map[j];
+                if (tj < 0 || tj >= L.ntypes) { atomicOr(A.err, MATPL_KERR_BAD_TYPE); tj = -1; }
+            } else if (j >= A.natoms) {
+                atomicOr(A.err, MATPL_KERR_BAD_COUNT);
+            }
+            const double *rr = A.Ri_r + (row_r + sl) * 4;
+            const T r = tj >= 0 ? ld_conv<T>(rr) : T(0);
+            if (!(r > T(0))) { rj[sl] = -1; continue; }
+            const T rinv = T(1) / r;
+            sts4(rv + 4 * sl, ld_conv<T>(rr + 1), ld_conv<T>(rr + 2), ld_conv<T>(rr + 3), rinv);
+            rj[sl] = (int)j;
+            T f[KRP], df[KRP];
             basis<T, KRM>(r, rc_r, rcinv_r, L.kr, f, df);
-            const T *c = c2 + (ti * L.ntypes + tj) * L.nr * L.kr;
+#pragma unroll
+            for (int k = KRM; k < KRP; ++k) f[k] = df[k] = T(0);
+            const T *c = c2 + (ti * L.ntypes + tj) * L.nr * L.kpr;
 #pragma unroll
             for (int n = 0; n < NRM; ++n) {
+                T g = T(0), gp = T(0);
                 if (n < L.nr) {
-                    T g = T(0);
 #pragma unroll
-                    for (int k = 0; k < KRM; ++k)
-                        if (k < L.kr) g += c[n * L.kr + k] * f[k];
-                    qr[n] += g;
+                    for (int k4 = 0; k4 < KRP; k4 += 4) {
+                        T c4[4];
+                        lds4(c + n * L.kpr + k4, c4);
+#pragma unroll
+                        for (int u = 0; u < 4; ++u) {
+                            g += c4[u] * f[k4 + u];
+                            gp += c4[u] * df[k4 + u];
+                        }
+                    }
                 }
+                qr[n] += g;
+                rgp[sl * NRM + n] = gp;
             }
         }
 #pragma unroll
@@ -282,46 +402,62 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
         T sacc[NAM];
 #pragma unroll
         for (int n = 0; n < NAM; ++n) sacc[n] = T(0);
-        for (long long base = 0; base < nna; base += 32) {
-            const long long sl = base + lane;
+        for (int base = 0; base < nna; base += 32) {
+            const int sl = base + lane;
             if (sl < nna) {
-                long long j = A.NL_a[row_a + sl];
-                if (j >= A.natoms) {
+                const long long j = A.NL_a[row_a + sl];
+                int tj = -1;
+                if (j >= 0 && j < A.natoms) {
+                    tj = (int)A.type_map[j];
+                    if (tj < 0 || tj >= L.ntypes) { atomicOr(A.err, MATPL_KERR_BAD_TYPE); tj = -1; }
+                } else if (j >= A.natoms) {
                     atomicOr(A.err, MATPL_KERR_BAD_COUNT);
-                    j = -1;
                 }
-                const int tj = j >= 0 ? (int)A.type_map[j] : -1;
-                const bool ok = tj >= 0 && tj < L.ntypes;
-                if (j >= 0 && !ok) atomicOr(A.err, MATPL_KERR_BAD_TYPE);
                 const double *rr = A.Ri_a + (row_a + sl) * 4;
-                const T r = ok ? (T)rr[0] : T(0);
-                T f[KAM], df[KAM];
-                basis<T, KAM>(r, rc_a, rcinv_a, L.ka, f, df);
-                const T *c = c3 + (ok ? (ti * L.ntypes + tj) : 0) * L.na * L.ka;
+                const T r = tj >= 0 ? ld_conv<T>(rr) : T(0);
+                const bool ok = r > T(0);
+                T f[KAP], df[KAP];
+                basis<T, KAM>(ok ? r : rc_a, rc_a, rcinv_a, L.ka, f, df);
+#pragma unroll
+                for (int k = KAM; k < KAP; ++k) f[k] = df[k] = T(0);
+                const T *c = c3 + (ok ? (ti * L.ntypes + tj) : 0) * L.na * L.kpa;
 #pragma unroll
                 for (int n = 0; n < NAM; ++n) {
-                    T g = T(0);
+                    T g = T(0), gp = T(0);
                     if (n < L.na && ok) {
 #pragma unroll
-                        for (int k = 0; k < KAM; ++k)
-                            if (k < L.ka) g += c[n * L.ka + k] * f[k];
+                        for (int k4 = 0; k4 < KAP; k4 += 4) {
+                            T c4[4];
+                            lds4(c + n * L.kpa + k4, c4);
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) {
+                                g += c4[u] * f[k4 + u];
+                                gp += c4[u] * df[k4 + u];
+                            }
+                        }
                     }
                     stash_g[lane * NAM + n] = g;
+                    ag[sl * NAM + n] = g;
+                    agp[sl * NAM + n] = gp;
                 }
-                const T rinv = ok && r > T(0) ? T(1) / r : T(0);
-                const T x = (T)rr[1] * rinv, y = (T)rr[2] * rinv, z = (T)rr[3] * rinv;
+                const T rinv = ok ? T(1) / r : T(0);
+                const T x = ok ? ld_conv<T>(rr + 1) : T(0), y = ok ? ld_conv<T>(rr + 2) : T(0),
+                        z = ok ? ld_conv<T>(rr + 3) : T(0);
+                aj[sl] = ok ? (int)j : -1;
+                sts4(av + 4 * sl, x, y, z, rinv);
+                const T ux = x * rinv, uy = y * rinv, uz = z * rinv;
 #pragma unroll
                 for (int lm = 0; lm < 24; ++lm) {
                     T b, gx, gy, gz;
-                    harmonic<T>(lm, x, y, z, b, gx, gy, gz);
-                    stash_b[lane * 24 + lm] = b;
+                    harmonic<T>(lm, ux, uy, uz, b, gx, gy, gz);
+                    stash_b[lane * 25 + lm] = b;
                 }
             }
             __syncwarp();
-            const int cnt = (int)min(32LL, nna - base);
+            const int cnt = min(32, nna - base);
             if (lane < 24) {
                 for (int jj = 0; jj < cnt; ++jj) {
-                    const T b = stash_b[jj * 24 + lane];
+                    const T b = stash_b[jj * 25 + lane];
 #pragma unroll
                     for (int n = 0; n < NAM; ++n) sacc[n] += stash_g[jj * NAM + n] * b;
                 }
@@ -353,19 +489,17 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
                 q = T(0);
                 for (int lm = lo; lm < hi; ++lm) {
                     const T sv = s_sm[n * 24 + lm];
-                    q += (T)kC3B[lm] * sv * sv;
+                    q += C3<T>(lm) * sv * sv;
                 }
             } else if (L.four && fa < n3 + L.na) {
                 const T *s = s_sm + (fa - n3) * 24;
-                q = (T)kC4B[0] * s[3] * s[3] * s[3] +
-                    (T)kC4B[1] * s[3] * (s[4] * s[4] + s[5] * s[5]) +
-                    (T)kC4B[2] * s[3] * (s[6] * s[6] + s[7] * s[7]) +
-                    (T)kC4B[3] * s[6] * (s[5] * s[5] - s[4] * s[4]) +
-                    (T)kC4B[4] * s[4] * s[5] * s[7];
+                q = C4<T>(0) * s[3] * s[3] * s[3] + C4<T>(1) * s[3] * (s[4] * s[4] + s[5] * s[5]) +
+                    C4<T>(2) * s[3] * (s[6] * s[6] + s[7] * s[7]) +
+                    C4<T>(3) * s[6] * (s[5] * s[5] - s[4] * s[4]) + C4<T>(4) * s[4] * s[5] * s[7];
             } else {
                 const T *s = s_sm + (fa - n3 - (L.four ? L.na : 0)) * 24;
                 const T a0 = s[0] * s[0], a12 = s[1] * s[1] + s[2] * s[2];
-                q = (T)kC5B[0] * a0 * a0 + (T)kC5B[1] * a0 * a12 + (T)kC5B[2] * a12 * a12;
+                q = C5<T>(0) * a0 * a0 + C5<T>(1) * a0 * a12 + C5<T>(2) * a12 * a12;
             }
             fin[L.two + fa] = q * qs[L.two + fa];
             if (A.feats) reinterpret_cast<T *>(A.feats)[i * L.nfeat + L.two + fa] = q;
@@ -374,13 +508,20 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
         if (A.feats) continue;            // descriptor only
 
         // ---------------- fitting net of element ti and its adjoint
-        const T *net = P + L.off_net + ti * L.net_stride;
-        const T *W0 = net, *b0 = net + L.nfeat * L.hidden, *W1 = b0 + L.hidden;
-        const T b1 = W1[L.hidden];
+        const int Hp = L.hp;
+        const T *net = P + L.off_net_s + ti * L.net_stride_s;
+        const T *W0 = net, *b0 = net + L.nfeat * Hp, *W1 = b0 + Hp;
+        const T b1 = W1[Hp];
         T e = T(0);
         for (int k = lane; k < L.hidden; k += 32) {
             T pre = b0[k];
-            for (int f = 0; f < L.nfeat; ++f) pre += fin[f] * W0[f * L.hidden + k];
+            for (int f4 = 0; f4 < L.nfeat; f4 += 4) {
+                T x4[4];
+                lds4(fin + f4, x4);
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (f4 + u < L.nfeat) pre += x4[u] * W0[(f4 + u) * Hp + k];
+            }
             const T h = dev_tanh(pre);
             e += W1[k] * h;
             dpre[k] = W1[k] * (T(1) - h * h);
@@ -389,8 +530,13 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
         __syncwarp();
         for (int f = lane; f < L.nfeat; f += 32) {
             T d = T(0);
-            const T *w = W0 + f * L.hidden;
-            for (int k = 0; k < L.hidden; ++k) d += w[k] * dpre[k];
+            const T *w = W0 + f * Hp;
+            for (int k4 = 0; k4 < Hp; k4 += 4) {
+                T a4[4], b4[4];
+                lds4(w + k4, a4);
+                lds4(dpre + k4, b4);
+                d += a4[0] * b4[0] + a4[1] * b4[1] + a4[2] * b4[2] + a4[3] * b4[3];
+            }
             dq[f] = d * qs[f];
         }
         __syncwarp();
@@ -406,34 +552,31 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
                     continue;
                 }
                 const T *s = s_sm + n * 24;
-                T d = dq[L.two + l * L.na + n] * T(2) * (T)kC3B[lm] * s[lm];
+                T d = dq[L.two + l * L.na + n] * T(2) * C3<T>(lm) * s[lm];
                 if (L.four && lm >= 3 && lm <= 7) {
                     const T g4 = dq[L.two + n3 + n];
                     T dd;
                     if (lm == 3)
-                        dd = T(3) * (T)kC4B[0] * s[3] * s[3] +
-                             (T)kC4B[1] * (s[4] * s[4] + s[5] * s[5]) +
-                             (T)kC4B[2] * (s[6] * s[6] + s[7] * s[7]);
+                        dd = T(3) * C4<T>(0) * s[3] * s[3] + C4<T>(1) * (s[4] * s[4] + s[5] * s[5]) +
+                             C4<T>(2) * (s[6] * s[6] + s[7] * s[7]);
                     else if (lm == 4)
-                        dd = T(2) * (T)kC4B[1] * s[3] * s[4] - T(2) * (T)kC4B[3] * s[6] * s[4] +
-                             (T)kC4B[4] * s[5] * s[7];
+                        dd = T(2) * C4<T>(1) * s[3] * s[4] - T(2) * C4<T>(3) * s[6] * s[4] +
+                             C4<T>(4) * s[5] * s[7];
                     else if (lm == 5)
-                        dd = T(2) * (T)kC4B[1] * s[3] * s[5] + T(2) * (T)kC4B[3] * s[6] * s[5] +
-                             (T)kC4B[4] * s[4] * s[7];
+                        dd = T(2) * C4<T>(1) * s[3] * s[5] + T(2) * C4<T>(3) * s[6] * s[5] +
+                             C4<T>(4) * s[4] * s[7];
                     else if (lm == 6)
-                        dd = T(2) * (T)kC4B[2] * s[3] * s[6] +
-                             (T)kC4B[3] * (s[5] * s[5] - s[4] * s[4]);
+                        dd = T(2) * C4<T>(2) * s[3] * s[6] + C4<T>(3) * (s[5] * s[5] - s[4] * s[4]);
                     else
-                        dd = T(2) * (T)kC4B[2] * s[3] * s[7] + (T)kC4B[4] * s[4] * s[5];
+                        dd = T(2) * C4<T>(2) * s[3] * s[7] + C4<T>(4) * s[4] * s[5];
                     d += g4 * dd;
                 }
                 if (L.five && lm <= 2) {
                     const T g5 = dq[L.two + n3 + (L.four ? L.na : 0) + n];
                     const T a0 = s[0] * s[0], a12 = s[1] * s[1] + s[2] * s[2];
                     const T dd = lm == 0
-                                     ? T(4) * (T)kC5B[0] * a0 * s[0] + T(2) * (T)kC5B[1] * s[0] * a12
-                                     : T(2) * (T)kC5B[1] * a0 * s[lm] +
-                                           T(4) * (T)kC5B[2] * a12 * s[lm];
+                                     ? T(4) * C5<T>(0) * a0 * s[0] + T(2) * C5<T>(1) * s[0] * a12
+                                     : T(2) * C5<T>(1) * a0 * s[lm] + T(4) * C5<T>(2) * a12 * s[lm];
                     d += g5 * dd;
                 }
                 dEds[n * 24 + lm] = d;
@@ -443,29 +586,19 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
 
         // ---------------- forces: radial pairs
         T fi0 = T(0), fi1 = T(0), fi2 = T(0);
-        for (long long sl = lane; sl < nnr; sl += 32) {
-            const long long j = A.NL_r[row_r + sl];
-            if (j < 0 || j >= A.natoms) continue;
-            const int tj = (int)A.type_map[j];
-            if (tj < 0 || tj >= L.ntypes) continue;
-            const double *rr = A.Ri_r + (row_r + sl) * 4;
-            const T r = (T)rr[0], x = (T)rr[1], y = (T)rr[2], z = (T)rr[3];
-            if (!(r > T(0))) continue;
-            T f[KRM], df[KRM];
-            basis<T, KRM>(r, rc_r, rcinv_r, L.kr, f, df);
-            const T *c = c2 + (ti * L.ntypes + tj) * L.nr * L.kr;
+        T dqr[NRM];
+#pragma unroll
+        for (int n = 0; n < NRM; ++n) dqr[n] = n < L.two ? dq[n] : T(0);
+        for (int sl = lane; sl < nnr; sl += 32) {
+            const int j = rj[sl];
+            if (j < 0) continue;
             T dEdr = T(0);
 #pragma unroll
-            for (int n = 0; n < NRM; ++n) {
-                if (n < L.nr) {
-                    T gp = T(0);
-#pragma unroll
-                    for (int k = 0; k < KRM; ++k)
-                        if (k < L.kr) gp += c[n * L.kr + k] * df[k];
-                    dEdr += dq[n] * gp;
-                }
-            }
-            const T s = dEdr / r;
+            for (int n = 0; n < NRM; ++n) dEdr += dqr[n] * rgp[sl * NRM + n];
+            T v4[4];
+            lds4(rv + 4 * sl, v4);
+            const T x = v4[0], y = v4[1], z = v4[2];
+            const T s = dEdr * v4[3];
             const T fx = s * x, fy = s * y, fz = s * z;
             fi0 += fx; fi1 += fy; fi2 += fz;
             add_force<T>(A.facc, j, -fx, -fy, -fz);
@@ -475,32 +608,18 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
         }
 
         // ---------------- forces: angular pairs
-        for (long long sl = lane; sl < nna; sl += 32) {
-            const long long j = A.NL_a[row_a + sl];
-            if (j < 0 || j >= A.natoms) continue;
-            const int tj = (int)A.type_map[j];
-            if (tj < 0 || tj >= L.ntypes) continue;
-            const double *rr = A.Ri_a + (row_a + sl) * 4;
-            const T r = (T)rr[0], x = (T)rr[1], y = (T)rr[2], z = (T)rr[3];
-            if (!(r > T(0))) continue;
-            T f[KAM], df[KAM];
-            basis<T, KAM>(r, rc_a, rcinv_a, L.ka, f, df);
-            const T *c = c3 + (ti * L.ntypes + tj) * L.na * L.ka;
-            T g[NAM], gp[NAM], An[NAM];
+        for (int sl = lane; sl < nna; sl += 32) {
+            const int j = aj[sl];
+            if (j < 0) continue;
+            T v4[4];
+            lds4(av + 4 * sl, v4);
+            const T x = v4[0], y = v4[1], z = v4[2], rinv = v4[3];
+            T g[NAM], An[NAM];
 #pragma unroll
             for (int n = 0; n < NAM; ++n) {
-                T a = T(0), b = T(0);
-                if (n < L.na) {
-#pragma unroll
-                    for (int k = 0; k < KAM; ++k)
-                        if (k < L.ka) {
-                            a += c[n * L.ka + k] * f[k];
-                            b += c[n * L.ka + k] * df[k];
-                        }
-                }
-                g[n] = a; gp[n] = b; An[n] = T(0);
+                g[n] = ag[sl * NAM + n];
+                An[n] = T(0);
             }
-            const T rinv = T(1) / r;
             const T ux = x * rinv, uy = y * rinv, uz = z * rinv;
             T G0 = T(0), G1 = T(0), G2 = T(0);
 #pragma unroll
@@ -518,7 +637,7 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
             }
             T dEdr = T(0);
 #pragma unroll
-            for (int n = 0; n < NAM; ++n) dEdr += gp[n] * An[n];
+            for (int n = 0; n < NAM; ++n) dEdr += agp[sl * NAM + n] * An[n];
             const T ug = ux * G0 + uy * G1 + uz * G2;
             const T fx = dEdr * ux + (G0 - ug * ux) * rinv;
             const T fy = dEdr * uy + (G1 - ug * uy) * rinv;
@@ -539,7 +658,7 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
         }
         __syncwarp();
     }
-    flush_frame<T>(A, frame, e_frame, vir, lane);
+    if (!A.feats) flush_frame<T>(A, frame, e_frame, vir, lane);
 }
 
 __global__ void nep_frame_start(const long long *__restrict__ num_atom, int nframes,
@@ -605,6 +724,17 @@ int make_layout(const matpl_nep_model *m, NepLayout *L) {
     l.off_net = l.off_qs + l.nfeat;
     l.net_stride = l.nfeat * l.hidden + 2 * l.hidden + 1;
     l.nparams = l.off_net + l.ntypes * l.net_stride;
+    l.hp = (l.hidden + 3) / 4 * 4;
+    if ((l.hp / 4) % 2 == 0) l.hp += 4;
+    l.fmp = (l.nfeat + 3) / 4 * 4;
+    l.kpr = (l.kr + 3) / 4 * 4;
+    l.kpa = (l.ka + 3) / 4 * 4;
+    l.off_c2_s = 0;
+    l.off_c3_s = T2 * l.nr * l.kpr;
+    l.off_qs_s = l.off_c3_s + (l.l3 ? T2 * l.na * l.kpa : 0);
+    l.off_net_s = (l.off_qs_s + l.nfeat + 3) / 4 * 4;
+    l.net_stride_s = (l.nfeat * l.hp + 2 * l.hp + 1 + 3) / 4 * 4;
+    l.nparams_s = l.off_net_s + l.ntypes * l.net_stride_s;
     *L = l;
     return MATPL_OK;
 }
@@ -627,14 +757,39 @@ size_t ws_layout(int dtype, int nframes, long long natoms, unsigned char *base,
 template <typename T, int NRM, int KRM, int NAM, int KAM>
 int launch_eval(const EvalArgs &A0, cudaStream_t s) {
     EvalArgs A = A0;
+    const NepLayout &L = A.L;
     auto kern = nep_eval_kernel<T, NRM, KRM, NAM, KAM>;
-    const size_t pbytes = (size_t)((A.L.nparams + 3) & ~3) * sizeof(T);
-    const size_t wbytes = (size_t)WarpScratch<NAM>::size * sizeof(T);
+    // per-warp scratch, 16-byte aligned pieces
+    int off = 0;
+    auto take = [&](size_t bytes) {
+        const int o = off;
+        off += (int)((bytes + 15) / 16 * 16);
+        return o;
+    };
+    const size_t t = sizeof(T);
+    const int mr = A.max_r > 0 ? A.max_r : 1, ma = A.max_a > 0 ? A.max_a : 1;
+    A.o_stash_g = take(32 * NAM * t);
+    A.o_stash_b = take(32 * 25 * t);
+    A.o_s = take(NAM * 24 * t);
+    A.o_dEds = take(NAM * 24 * t);
+    A.o_fin = take(L.fmp * t);
+    A.o_dq = take(L.fmp * t);
+    A.o_dpre = take(L.hp * t);
+    A.o_rj = take(mr * 4);
+    A.o_rv = take((size_t)mr * 4 * t);
+    A.o_rgp = take((size_t)mr * NRM * t);
+    A.o_aj = take(ma * 4);
+    A.o_av = take((size_t)ma * 4 * t);
+    A.o_ag = take((size_t)ma * NAM * t);
+    A.o_agp = take((size_t)ma * NAM * t);
+    A.warp_bytes = off;
+    A.smem_params = (int)((L.nparams_s * t + 15) / 16 * 16);
     int wpb = kWarpsPerBlock;
-    while (wpb > 1 && pbytes + wpb * wbytes > 220 * 1024) --wpb;
-    const size_t smem = pbytes + wpb * wbytes;
+    while (wpb > 1 && (size_t)A.smem_params + (size_t)wpb * A.warp_bytes > 220 * 1024) --wpb;
+    const size_t smem = (size_t)A.smem_params + (size_t)wpb * A.warp_bytes;
     MATPL_REQUIRE(smem <= 220 * 1024, MATPL_ERR_UNSUPPORTED,
-                  "NEP parameters do not fit in shared memory");
+                  "NEP parameters and per-warp lists do not fit in shared memory "
+                  "(max_nn_radial / max_nn_angular too large)");
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
         return check_launch("cudaFuncSetAttribute(nep_eval)");
@@ -648,7 +803,7 @@ int launch_eval(const EvalArgs &A0, cudaStream_t s) {
     const long long nwarps = (A.natoms + apw - 1) / apw;
     const int grid = (int)((nwarps + wpb - 1) / wpb);
     {
-        ProfScope ps("nep_eval", s);
+        ProfScope ps(A.feats ? "nep_descriptor" : "nep_eval", s);
         kern<<<grid, 32 * wpb, smem, s>>>(A, apw);
     }
     return check_launch("matpl_nep_eval");

@@ -255,14 +255,18 @@ __global__ void nepnb_fill(const NepFrame *__restrict__ fr, int nframes, long lo
     }
 }
 
-// per-warp shared scratch of the list-writing search: int keys, then (x, y, z, d2) doubles
+// Per-warp shared scratch of the search: a queue of FP32-prefilter survivors, then (list mode)
+// int keys and (x, y, z, r) doubles of the kept pairs, or (typed count mode) per-element counts.
+constexpr int kQueue = 64;
+
 __host__ __device__ inline size_t key_bytes(int max_r, int max_a) {
     return ((size_t)(max_r + max_a) * 4 + 15) / 16 * 16;
 }
 __host__ __device__ inline size_t warp_scratch(bool count, bool typed, int max_r, int max_a,
                                                int ntypes) {
-    if (count) return typed ? ((size_t)2 * ntypes * 4 + 15) / 16 * 16 : 0;
-    return key_bytes(max_r, max_a) + (size_t)(max_r + max_a) * 32;
+    const size_t q = kQueue * 4;
+    if (count) return q + (typed ? ((size_t)2 * ntypes * 4 + 15) / 16 * 16 : 0);
+    return q + key_bytes(max_r, max_a) + (size_t)(max_r + max_a) * 32;
 }
 
 struct SearchArgs {
@@ -283,16 +287,23 @@ struct SearchArgs {
     int *err;
 };
 
+struct WarpLists {
+    int *queue;
+    int *key_r, *key_a;
+    double *val_r, *val_a;   // (x, y, z, r) per kept pair
+    int *tcount;             // typed counts [2 * ntypes]
+};
+
 __device__ __forceinline__ void write_entry(const SearchArgs &A, bool radial, long long n1,
                                             int slot, long long n2, double x, double y, double z,
-                                            double d2) {
+                                            double r) {
     const int mx = radial ? A.max_r : A.max_a;
     long long *NL = radial ? A.NL_r : A.NL_a;
     double *Ri = radial ? A.Ri_r : A.Ri_a;
     NL[n1 * mx + slot] = n2;
     double *o = Ri + (n1 * mx + slot) * A.width;
     if (A.width == 4) {
-        reinterpret_cast<double2 *>(o)[0] = make_double2(sqrt(d2), x);
+        reinterpret_cast<double2 *>(o)[0] = make_double2(r, x);
         reinterpret_cast<double2 *>(o)[1] = make_double2(y, z);
     } else {
         o[0] = x; o[1] = y; o[2] = z;
@@ -311,20 +322,80 @@ __device__ __forceinline__ void pad_rows(const SearchArgs &A, long long n1, int 
     }
 }
 
+template <bool TYPED>
+__device__ __forceinline__ void count_types(const SearchArgs &A, const WarpLists &W, long long n2,
+                                            bool in_r, bool in_a) {
+    if (TYPED && (in_r || in_a)) {
+        const int t2 = (int)A.type_map[n2];
+        if (t2 >= 0 && t2 < A.ntypes) {
+            if (in_r) atomicAdd(&W.tcount[t2], 1);
+            if (in_a) atomicAdd(&W.tcount[A.ntypes + t2], 1);
+        } else {
+            atomicOr(A.err, MATPL_KERR_BAD_TYPE);
+        }
+    }
+}
+
+// Exact FP64 test of the first k (<= 32) queued candidates of atom n1 (cell list: replica
+// (0, 0, 0) only), one candidate per lane so that the FP64 pipe runs full warps.  Kept pairs
+// are appended to the per-warp lists (list mode) or counted.
+template <bool COUNT, bool TYPED>
+__device__ __forceinline__ void drain(const SearchArgs &A, const NepFrame &F, const double *p1,
+                                      int k, int lane, const WarpLists &W, int &cr, int &ca) {
+    const unsigned lt = (1u << lane) - 1u;
+    bool in_r = false, in_a = false;
+    long long n2 = -1;
+    double x = 0, y = 0, z = 0, d2 = 0;
+    if (lane < k) {
+        n2 = F.atom0 + W.queue[lane];
+        const double p2[3] = {A.pos[3 * n2], A.pos[3 * n2 + 1], A.pos[3 * n2 + 2]};
+        d2 = exact_pair(F.box, p1, p2, F.zdelta, x, y, z);
+        in_r = d2 < A.rc2_r;
+        in_a = d2 < A.rc2_a;
+    }
+    const unsigned br = __ballot_sync(0xffffffffu, in_r);
+    const unsigned ba = __ballot_sync(0xffffffffu, in_a);
+    if (COUNT) {
+        count_types<TYPED>(A, W, n2, in_r, in_a);
+    } else {
+        const double r = (A.width == 4 && (in_r || in_a)) ? sqrt(d2) : 0.0;
+        if (in_r) {
+            const int slot = cr + __popc(br & lt);
+            if (slot < A.max_r) {
+                W.key_r[slot] = (int)(n2 - F.atom0);
+                double *v = W.val_r + 4 * slot;
+                v[0] = x; v[1] = y; v[2] = z; v[3] = r;
+            }
+        }
+        if (in_a) {
+            const int slot = ca + __popc(ba & lt);
+            if (slot < A.max_a) {
+                W.key_a[slot] = (int)(n2 - F.atom0);
+                double *v = W.val_a + 4 * slot;
+                v[0] = x; v[1] = y; v[2] = z; v[3] = r;
+            }
+        }
+    }
+    cr += __popc(br);
+    ca += __popc(ba);
+}
+
 // COUNT: only count neighbors (calculate_maxneigh); TYPED: counts per neighbor element.
 template <bool COUNT, bool TYPED>
 __global__ void __launch_bounds__(128) nepnb_search(SearchArgs A, int warps_per_block) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
-    // per-warp scratch: keys then (x, y, z, d2) of kept pairs, radial then angular
     const size_t per_warp = warp_scratch(COUNT, TYPED, A.max_r, A.max_a, A.ntypes);
     unsigned char *mine = smem + per_warp * wib;
-    int *key_r = reinterpret_cast<int *>(mine);
-    int *key_a = key_r + A.max_r;
-    double *val_r = reinterpret_cast<double *>(mine + key_bytes(A.max_r, A.max_a));
-    double *val_a = val_r + 4 * (size_t)A.max_r;
-    int *tcount = reinterpret_cast<int *>(mine);
+    WarpLists W;
+    W.queue = reinterpret_cast<int *>(mine);
+    unsigned char *rest = mine + kQueue * 4;
+    W.tcount = reinterpret_cast<int *>(rest);
+    W.key_r = reinterpret_cast<int *>(rest);
+    W.key_a = W.key_r + A.max_r;
+    W.val_r = reinterpret_cast<double *>(rest + key_bytes(A.max_r, A.max_a));
+    W.val_a = W.val_r + 4 * (size_t)A.max_r;
 
     const long long gw = (long long)blockIdx.x * warps_per_block + wib;
     const long long nw = (long long)gridDim.x * warps_per_block;
@@ -333,7 +404,7 @@ __global__ void __launch_bounds__(128) nepnb_search(SearchArgs A, int warps_per_
         const double p1[3] = {A.pos[3 * n1], A.pos[3 * n1 + 1], A.pos[3 * n1 + 2]};
         int cr = 0, ca = 0;
         if (TYPED) {
-            for (int t = lane; t < 2 * A.ntypes; t += 32) tcount[t] = 0;
+            for (int t = lane; t < 2 * A.ntypes; t += 32) W.tcount[t] = 0;
             __syncwarp();
         }
         if (F.mode == 0) {
@@ -344,6 +415,10 @@ __global__ void __launch_bounds__(128) nepnb_search(SearchArgs A, int warps_per_
                 const float v = sv[k] * F.nc[k];
                 c1[k] = v >= 0.f ? min((int)v, F.nc[k] - 1) : 0;   // also maps NaN to 0
             }
+            float H[9];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) H[q] = F.H[q];
+            int qn = 0;
             for (int q = 0; q < 27; ++q) {
                 int c[3], sh[3];
                 const int d[3] = {q / 9 - 1, (q / 3) % 3 - 1, q % 3 - 1};
@@ -357,65 +432,38 @@ __global__ void __launch_bounds__(128) nepnb_search(SearchArgs A, int warps_per_
                 const int beg = A.cell_start[cell], cnt = A.cell_count[cell];
                 for (int base = 0; base < cnt; base += 32) {
                     const int e = base + lane;
-                    bool in_r = false, in_a = false;
-                    long long n2 = -1;
-                    double x = 0, y = 0, z = 0, d2 = 0;
+                    bool pass = false;
+                    int loc = -1;
                     if (e < cnt) {
-                        const int loc = A.cell_atoms[F.atom0 + beg + e];
-                        n2 = F.atom0 + loc;
-                        if (n2 != n1) {
-                            const float4 s2 = A.spos[n2];
+                        loc = A.cell_atoms[F.atom0 + beg + e];
+                        if (F.atom0 + loc != n1) {
+                            const float4 s2 = A.spos[F.atom0 + loc];
                             const float f0 = s2.x + sh[0] - s1.x, f1 = s2.y + sh[1] - s1.y,
                                         f2 = s2.z + sh[2] - s1.z;
-                            const float xf = F.H[0] * f0 + F.H[1] * f1 + F.H[2] * f2;
-                            const float yf = F.H[3] * f0 + F.H[4] * f1 + F.H[5] * f2;
-                            const float zf = F.H[6] * f0 + F.H[7] * f1 + F.H[8] * f2;
-                            if (xf * xf + yf * yf + zf * zf < A.pre2) {
-                                const double p2[3] = {A.pos[3 * n2], A.pos[3 * n2 + 1],
-                                                      A.pos[3 * n2 + 2]};
-                                d2 = exact_pair(F.box, p1, p2, F.zdelta, x, y, z);
-                                in_r = d2 < A.rc2_r;
-                                in_a = d2 < A.rc2_a;
-                            }
+                            const float xf = H[0] * f0 + H[1] * f1 + H[2] * f2;
+                            const float yf = H[3] * f0 + H[4] * f1 + H[5] * f2;
+                            const float zf = H[6] * f0 + H[7] * f1 + H[8] * f2;
+                            pass = xf * xf + yf * yf + zf * zf < A.pre2;
                         }
                     }
-                    if (COUNT) {
-                        if (TYPED) {
-                            if (in_r || in_a) {
-                                const int t2 = (int)A.type_map[n2];
-                                if (t2 >= 0 && t2 < A.ntypes) {
-                                    if (in_r) atomicAdd(&tcount[t2], 1);
-                                    if (in_a) atomicAdd(&tcount[A.ntypes + t2], 1);
-                                } else {
-                                    atomicOr(A.err, MATPL_KERR_BAD_TYPE);
-                                }
-                            }
-                        }
-                        cr += __popc(__ballot_sync(0xffffffffu, in_r));
-                        ca += __popc(__ballot_sync(0xffffffffu, in_a));
-                        continue;
+                    const unsigned b = __ballot_sync(0xffffffffu, pass);
+                    if (pass) W.queue[qn + __popc(b & lt)] = loc;
+                    qn += __popc(b);
+                    if (qn >= 32) {
+                        __syncwarp();
+                        drain<COUNT, TYPED>(A, F, p1, 32, lane, W, cr, ca);
+                        const int left = qn - 32;
+                        const int v = lane < left ? W.queue[32 + lane] : 0;
+                        __syncwarp();
+                        if (lane < left) W.queue[lane] = v;
+                        __syncwarp();
+                        qn = left;
                     }
-                    const unsigned br = __ballot_sync(0xffffffffu, in_r);
-                    const unsigned ba = __ballot_sync(0xffffffffu, in_a);
-                    if (in_r) {
-                        const int slot = cr + __popc(br & lt);
-                        if (slot < A.max_r) {
-                            key_r[slot] = (int)(n2 - F.atom0);
-                            double *v = val_r + 4 * slot;
-                            v[0] = x; v[1] = y; v[2] = z; v[3] = d2;
-                        }
-                    }
-                    if (in_a) {
-                        const int slot = ca + __popc(ba & lt);
-                        if (slot < A.max_a) {
-                            key_a[slot] = (int)(n2 - F.atom0);
-                            double *v = val_a + 4 * slot;
-                            v[0] = x; v[1] = y; v[2] = z; v[3] = d2;
-                        }
-                    }
-                    cr += __popc(br);
-                    ca += __popc(ba);
                 }
+            }
+            if (qn > 0) {
+                __syncwarp();
+                drain<COUNT, TYPED>(A, F, p1, qn, lane, W, cr, ca);
             }
             if (!COUNT) {
                 __syncwarp();
@@ -423,8 +471,8 @@ __global__ void __launch_bounds__(128) nepnb_search(SearchArgs A, int warps_per_
                 for (int pass = 0; pass < 2; ++pass) {
                     const bool radial = pass == 0;
                     const int n = min(radial ? cr : ca, radial ? A.max_r : A.max_a);
-                    const int *key = radial ? key_r : key_a;
-                    const double *val = radial ? val_r : val_a;
+                    const int *key = radial ? W.key_r : W.key_a;
+                    const double *val = radial ? W.val_r : W.val_a;
                     for (int e = lane; e < n; e += 32) {
                         const int k = key[e];
                         int rank = 0;
@@ -461,29 +509,20 @@ __global__ void __launch_bounds__(128) nepnb_search(SearchArgs A, int warps_per_
                         in_a = d2 < A.rc2_a;
                     }
                 }
-                if (COUNT) {
-                    if (TYPED && (in_r || in_a)) {
-                        const int t2 = (int)A.type_map[n2];
-                        if (t2 >= 0 && t2 < A.ntypes) {
-                            if (in_r) atomicAdd(&tcount[t2], 1);
-                            if (in_a) atomicAdd(&tcount[A.ntypes + t2], 1);
-                        } else {
-                            atomicOr(A.err, MATPL_KERR_BAD_TYPE);
-                        }
-                    }
-                    cr += __popc(__ballot_sync(0xffffffffu, in_r));
-                    ca += __popc(__ballot_sync(0xffffffffu, in_a));
-                    continue;
-                }
                 const unsigned br = __ballot_sync(0xffffffffu, in_r);
                 const unsigned ba = __ballot_sync(0xffffffffu, in_a);
-                if (in_r) {
-                    const int slot = cr + __popc(br & lt);
-                    if (slot < A.max_r) write_entry(A, true, n1, slot, n2, x, y, z, d2);
-                }
-                if (in_a) {
-                    const int slot = ca + __popc(ba & lt);
-                    if (slot < A.max_a) write_entry(A, false, n1, slot, n2, x, y, z, d2);
+                if (COUNT) {
+                    count_types<TYPED>(A, W, n2, in_r, in_a);
+                } else {
+                    const double r = (A.width == 4 && (in_r || in_a)) ? sqrt(d2) : 0.0;
+                    if (in_r) {
+                        const int slot = cr + __popc(br & lt);
+                        if (slot < A.max_r) write_entry(A, true, n1, slot, n2, x, y, z, r);
+                    }
+                    if (in_a) {
+                        const int slot = ca + __popc(ba & lt);
+                        if (slot < A.max_a) write_entry(A, false, n1, slot, n2, x, y, z, r);
+                    }
                 }
                 cr += __popc(br);
                 ca += __popc(ba);
@@ -493,8 +532,8 @@ __global__ void __launch_bounds__(128) nepnb_search(SearchArgs A, int warps_per_
             if (TYPED) {
                 __syncwarp();
                 for (int t = lane; t < A.ntypes; t += 32) {
-                    A.NN_r[n1 * A.ntypes + t] = tcount[t];
-                    A.NN_a[n1 * A.ntypes + t] = tcount[A.ntypes + t];
+                    A.NN_r[n1 * A.ntypes + t] = W.tcount[t];
+                    A.NN_a[n1 * A.ntypes + t] = W.tcount[A.ntypes + t];
                 }
                 __syncwarp();
             } else if (lane == 0) {
