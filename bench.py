@@ -230,7 +230,7 @@ def run_nep(args, ws, local, steps, warmup, sample_clocks=True):
     the fused FP32 descriptor / network / force / virial kernel, 100,000 atoms."""
     from matpl_gb300 import _lib, nep as NP, ops
     dev = torch.device("cuda", local)
-    cfg, fr, prm = nep_workload()
+    cfg, fr, prm = nep_workload(args.nep_atoms)
     N = fr.natoms
     c = lambda a, dt: torch.tensor(np.ascontiguousarray(a), dtype=dt, device=dev)  # noqa: E731
     na, tm, bx, bo, nc = (c(fr.num_atom.reshape(-1, 1), torch.int64), c(fr.type_map, torch.int64),
@@ -329,10 +329,17 @@ def run_nep(args, ws, local, steps, warmup, sample_clocks=True):
     # type + two counts (24 B) and writes Ei, the force accumulator and force (32 B)
     ev_bytes = 40 * (n_r + n_a) + 56 * N
     launches = sum(v[1] for v in prof.values())
+    traffic = None
+    tp = os.path.join(HERE, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        tr = json.load(open(tp)).get("nep_eval:float32")
+        if tr:   # recorded for the 100,000-atom launch; DRAM bytes scale with atoms
+            traffic = {"bytes_per_launch": tr["bytes_per_launch"] * N / NEP_NATOMS,
+                       "note": tr.get("note")}
     return {
         "metric": NEP_METRIC, "value": ws * N / (ms * 1e-3), "unit": "atom-steps/s",
         "ms_per_step": ms, "steps": steps, "warmup": warmup, "dtype": "f32 (f64 lists, f64 sums)",
-        "config": {"workload": "NEP, 100,000 atoms, 4 elements (equal parts) random-packed at "
+        "config": {"workload": f"NEP, {N:,} atoms, 4 elements (equal parts) random-packed at "
                                "0.06 atoms/A^3; radial rc 6 A basis 8 n_max 4, angular rc 4 A "
                                "basis 8 n_max 4 l_max 4/2/1, 30-unit tanh layer per element; "
                                "step = calculate_neighbor + fused E/F/V",
@@ -346,6 +353,8 @@ def run_nep(args, ws, local, steps, warmup, sample_clocks=True):
         "roofline": {"kernel": "nep_eval", "bound": "simt_fp32", "achieved": fl / t_eval / 1e12,
                      "peak": simt_peak, "unit": "TFLOP/s", "frac": fl / t_eval / 1e12 / simt_peak,
                      "algorithmic_flops_per_launch": fl,
+                     "traffic": traffic["bytes_per_launch"] if traffic else None,
+                     "traffic_note": traffic["note"] if traffic else None,
                      "peak_source": "nominal FP32 SIMT at the sampled SM clock (152 SMs x 128 lanes x 2)",
                      "hbm": {"achieved": ev_bytes / t_eval / 1e9, "peak": hbm_peak,
                              "unit": "GB/s", "frac": ev_bytes / t_eval / 1e9 / hbm_peak,
@@ -619,6 +628,9 @@ def main():
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain-FP32 comparison run of a mixed form")
     ap.add_argument("--no-nep", action="store_true", help="skip the NEP workload")
+    ap.add_argument("--nep-atoms", type=int, default=NEP_NATOMS,
+                    help="atoms of the NEP box (the benchmark is 100,000; smaller boxes of the "
+                         "same density and model are for profiling captures)")
     ap.add_argument("--workload", default="dp", choices=["dp", "nep"],
                     help="dp: the headline DP line (with a nep object); nep: the NEP line alone")
     argv = sys.argv[1:]

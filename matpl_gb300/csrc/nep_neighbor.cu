@@ -36,6 +36,7 @@ struct NepFrame {
     int nc[3];            // cell bins per fractional axis (mode 0)
     int ncells;
     int rep[3];           // num_cell replicas (mode 1)
+    int ortho;            // h and h^-1 off-diagonals are all (signed) zeros
     double box[18];
     double bo[9];
     double zdelta[3];     // delta of replica (0, 0, 0), with the reference's signed zeros
@@ -64,6 +65,39 @@ __device__ __forceinline__ double exact_pair(const double *__restrict__ box, con
     x = da(da(dm(box[0], sx), dm(box[1], sy)), dm(box[2], sz));
     y = da(da(dm(box[3], sx), dm(box[4], sy)), dm(box[5], sz));
     z = da(da(dm(box[6], sx), dm(box[7], sy)), dm(box[8], sz));
+    return da(da(dm(x, x), dm(y, y)), dm(z, z));
+}
+
+// Orthorhombic cells: every off-diagonal product in exact_pair is a signed zero, which leaves a
+// nonzero sum unchanged.  A sum that is zero is +0 unless all of its terms are -0, so the
+// result is the diagonal product when it is nonzero, else a zero whose sign is the AND of the
+// terms' signs.  Same values, bit for bit, with 23 instead of 47 FP64 operations.
+__device__ __forceinline__ unsigned sgn(double v) {
+    return (unsigned)((unsigned long long)__double_as_longlong(v) >> 63);
+}
+__device__ __forceinline__ double zsum3(double diag, unsigned s1, unsigned s2) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(diag);
+    if (b << 1) return diag;                                   // nonzero (or NaN)
+    return __longlong_as_double((long long)((unsigned long long)(sgn(diag) & s1 & s2) << 63));
+}
+__device__ __forceinline__ double exact_pair_ortho(const double *__restrict__ box,
+                                                   const double *p1, const double *p2,
+                                                   const double *delta, double &x, double &y,
+                                                   double &z) {
+    x = ds(da(p2[0], delta[0]), p1[0]);
+    y = ds(da(p2[1], delta[1]), p1[1]);
+    z = ds(da(p2[2], delta[2]), p1[2]);
+    const unsigned sx_ = sgn(x), sy_ = sgn(y), sz_ = sgn(z);
+    double sx = zsum3(dm(box[9], x), sgn(box[10]) ^ sy_, sgn(box[11]) ^ sz_);
+    double sy = zsum3(dm(box[13], y), sgn(box[12]) ^ sx_, sgn(box[14]) ^ sz_);
+    double sz = zsum3(dm(box[17], z), sgn(box[15]) ^ sx_, sgn(box[16]) ^ sy_);
+    sx = ds(sx, nearbyint(sx));
+    sy = ds(sy, nearbyint(sy));
+    sz = ds(sz, nearbyint(sz));
+    const unsigned tx = sgn(sx), ty = sgn(sy), tz = sgn(sz);
+    x = zsum3(dm(box[0], sx), sgn(box[1]) ^ ty, sgn(box[2]) ^ tz);
+    y = zsum3(dm(box[4], sy), sgn(box[3]) ^ tx, sgn(box[5]) ^ tz);
+    z = zsum3(dm(box[8], sz), sgn(box[6]) ^ tx, sgn(box[7]) ^ ty);
     return da(da(dm(x, x), dm(y, y)), dm(z, z));
 }
 
@@ -112,6 +146,12 @@ __global__ void nepnb_setup(const long long *__restrict__ num_atom,
         for (int q = 0; q < 18; ++q) F.box[q] = box[18 * f + q];
         for (int q = 0; q < 9; ++q) F.bo[q] = box_orig[9 * f + q];
         replica_delta(F.bo, 0, 0, 0, F.zdelta);
+        {
+            const int off[12] = {1, 2, 3, 5, 6, 7, 10, 11, 12, 14, 15, 16};
+            bool o = true;
+            for (int q = 0; q < 12; ++q) o &= F.box[off[q]] == 0.0;
+            F.ortho = o;
+        }
         bool single = true;
         for (int k = 0; k < 3; ++k) {
             F.rep[k] = (int)num_cell[3 * f + k];
@@ -349,7 +389,8 @@ __device__ __forceinline__ void drain(const SearchArgs &A, const NepFrame &F, co
     if (lane < k) {
         n2 = F.atom0 + W.queue[lane];
         const double p2[3] = {A.pos[3 * n2], A.pos[3 * n2 + 1], A.pos[3 * n2 + 2]};
-        d2 = exact_pair(F.box, p1, p2, F.zdelta, x, y, z);
+        d2 = F.ortho ? exact_pair_ortho(F.box, p1, p2, F.zdelta, x, y, z)
+                     : exact_pair(F.box, p1, p2, F.zdelta, x, y, z);
         in_r = d2 < A.rc2_r;
         in_a = d2 < A.rc2_a;
     }

@@ -80,6 +80,32 @@ def test_neighbor_cell_list_matches_oracle(case, with_rij):
     assert_lists_equal(got, exp)
 
 
+def _lattice_frames():
+    """Perfect FCC crystals: many pair-vector components are exactly zero, which exercises the
+    signed-zero handling of the orthorhombic path.  One with mirrored (-0.0) coordinates and
+    one left-handed cell (negative first vector, so h^-1 has -0.0 off-diagonals)."""
+    st = structures.fcc(3.615, (10, 10, 10), 0.0, seed=1)
+    a = NP.frames_from_structures([st], 6.0)
+    b = NP.frames_from_structures([st], 6.0)
+    b.position = -b.position
+    lat = np.diag([-36.15, 36.15, 36.15])
+    box, bo, nc, _ = NP.expand_box(lat, 6.0)
+    c = NP.NepFrames(st.frac @ lat, np.zeros(st.natoms, np.int64),
+                     np.array([st.natoms]), box[None], bo[None], nc[None])
+    return {"fcc": a, "fcc_mirrored": b, "fcc_left_handed": c}
+
+
+@pytest.mark.parametrize("case", ["fcc", "fcc_mirrored", "fcc_left_handed"])
+def test_neighbor_signed_zeros_match_oracle(case):
+    fr = _lattice_frames()[case]
+    cfg = NP.NepConfig(atom_type=[29])
+    cr, ca = NO.maxneigh(fr, cfg.cutoff[0], cfg.cutoff[1])
+    mr, ma = int(cr.max()), int(ca.max())
+    exp = NO.neighbor(fr, cfg.cutoff[0], cfg.cutoff[1], mr, ma, True)
+    got = gpu_neighbor(fr, cfg, mr, ma, True)
+    assert_lists_equal(got, exp)
+
+
 def test_maxneigh_matches_oracle():
     cfg = NP.NepConfig(atom_type=[3, 14, 8, 72])
     fr = _frames(CELL_CASES["mixed_batch"], cfg.cutoff[0])
