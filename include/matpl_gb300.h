@@ -187,6 +187,35 @@ int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, int natoms,
                   void *workspace, size_t workspace_bytes, void *stream);
 
 /* ------------------------------------------------------------------------------------
+ * Force-loss training: the embedding-net part of the second-order parameter gradient.
+ * Replaces what the reference gets from torch autograd with create_graph=True through
+ * DP.forward / calculate_force_virial (src/model/dp_dp.py:417-530, loss.backward() in
+ * src/PWMLFF/dp_mods/dp_trainer.py:172-275).
+ * For a loss with gE = dL/dEtot, gF = dL/dF [B,N,3], gV = dL/dVirial [B,9] (or NULL), the
+ * force / virial part of dL/dtheta is the parameter gradient of the derivative of E along the
+ * input tangent Rdot_s = Ri_d_s (gF_j - gF_i + gV r_s).
+ * matpl_dp_dual_forward: per atom A = k sum_s R_s^T G_s and its tangent
+ *   A_dot = k sum_s (Rdot_s^T G_s + R_s^T Gdot_s), both [B*N, 4*25] in the compute dtype,
+ *   k = 1 / (m * npresent); occupied slots only (add the empty-slot term of A yourself;
+ *   its tangent is zero).
+ * matpl_dp_dual_backward: given A_bar = dPhi/dA and A_dot_bar = dPhi/dA_dot [B*N, 100],
+ *   writes the gradient of Phi w.r.t. the embedding parameters (the first
+ *   ntypes^2 * 1400 entries of the packed layout) into grad_embedding, recomputing the
+ *   embedding activations slot by slot instead of storing them.
+ * list_neigh [B,N,S] int32 1-based (0 = empty), image_dr [B,N,S,4], no ghost atoms;
+ * dtype MATPL_F32 or MATPL_F64; model as for matpl_dp_eval (params, davg, dstd).
+ * ---------------------------------------------------------------------------------- */
+int matpl_dp_dual_forward(int dtype, const matpl_dp_model *model, int batch, int natoms,
+                          int nslots, const int32_t *list_neigh, const void *image_dr,
+                          const int32_t *type_map, const void *grad_force,
+                          const void *grad_virial, void *A, void *A_dot, void *stream);
+int matpl_dp_dual_backward(int dtype, const matpl_dp_model *model, int batch, int natoms,
+                           int nslots, const int32_t *list_neigh, const void *image_dr,
+                           const int32_t *type_map, const void *grad_force,
+                           const void *grad_virial, const void *A_bar, const void *A_dot_bar,
+                           void *grad_embedding, void *stream);
+
+/* ------------------------------------------------------------------------------------
  * NEP neighbor lists.  Replaces CalcOps calculate_neighbor / calculate_maxneigh
  * (src/op/src/CalcOps.cpp:1025-1172, kernels src/op/kernel/calculateNepNeighbor.cu:8-380,
  * CPU twin src/op/src/cpu_calculate_nepneighbor.cpp:6-203), bit-identical to the CPU twin.

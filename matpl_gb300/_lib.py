@@ -59,6 +59,10 @@ SIGNATURES = {
     "matpl_dp_workspace_bytes": (_sz, [_i, _i, _i]),
     "matpl_dp_eval": (_i, [_i, _c.POINTER(MatplDpModel), _i, _i, _i, _i, _vp, _vp, _vp, _vp,
                            _vp, _vp, _vp, _vp, _sz, _vp]),
+    "matpl_dp_dual_forward": (_i, [_i, _c.POINTER(MatplDpModel), _i, _i, _i, _vp, _vp, _vp,
+                                   _vp, _vp, _vp, _vp, _vp]),
+    "matpl_dp_dual_backward": (_i, [_i, _c.POINTER(MatplDpModel), _i, _i, _i, _vp, _vp, _vp,
+                                    _vp, _vp, _vp, _vp, _vp, _vp]),
     "matpl_nep_neighbor_workspace_bytes": (_sz, [_i, _ll]),
     "matpl_nep_neighbor": (_i, [_i, _ll, _vp, _vp, _vp, _vp, _vp, _d, _d, _i, _i, _i, _vp, _vp,
                                 _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),

@@ -1,0 +1,531 @@
+// Force-loss training of DP se_e2_a: the embedding-net part of the second-order gradient,
+// written by hand (the reference gets it from torch autograd with create_graph=True,
+// src/PWMLFF/dp_mods/dp_trainer.py:172-275 through src/model/dp_dp.py:417-530).
+//
+// For a loss L(E, F, V) the trainer needs dL/dtheta = gE . dE/dtheta + gF . dF/dtheta (+ gV .
+// dV/dtheta) with gE = dL/dE, gF = dL/dF, gV = dL/dV.  Forces and virial are built from the
+// per-slot vectors f_s = sum_c dE/dRi_s[c] Ri_d_s[c][:] (F_i -= f_s, F_j += f_s, V += f_s r_s^T),
+// so
+//     gF . F + gV . V = sum_s f_s . u_s,   u_s = gF_j - gF_i + gV r_s,
+//                     = sum_s sum_c dE/dRi_s[c] Rdot_s[c],   Rdot_s = Ri_d_s u_s,
+// the derivative of E along the input tangent Rdot (Ri_d does not depend on the parameters).
+// Its parameter gradient is a forward-over-reverse product:
+//   dp_dual_fwd   tangent (forward-mode) pass through every embedding net: per occupied slot
+//                 G = emb(s), Gdot = emb'(s) sdot, and per atom
+//                 A = k sum_s R_s^T G_s,  Adot = k sum_s (Rdot_s^T G_s + R_s^T Gdot_s)
+//                 (k = 1 / (m T); empty slots contribute to A only, their tangent is zero);
+//   (host)        the per-atom part - descriptor D = A^T A<, fitting nets, E and its tangent
+//                 Edot = dE/dA . Adot - and its reverse give Abar = dPhi/dA, Adotbar = dPhi/dAdot
+//                 for Phi = sum gE E + sum Edot;
+//   dp_dual_bwd   reverse through the tangent pass, recomputing the embedding activations slot
+//                 by slot instead of storing them, and reducing the embedding-weight gradients
+//                 (outer products of layer inputs and pre-activation adjoints, both for the
+//                 primal and the tangent stream) per CTA in shared memory.
+#include "common.cuh"
+#include "dp_layout.cuh"
+#include "dp_env.cuh"
+
+namespace matpl {
+namespace {
+
+using namespace dp;
+constexpr int kStg = E + 1;   // staging row stride (odd: conflict-free column access)
+
+struct TrainParams {
+    int batch, natoms, nslots, ntypes, m, present_mask, has_gv;
+    double rmin, rmax, inv_mT;
+};
+
+// Occupied slots of one centre atom (ascending), image types absent from the model skipped.
+__device__ __forceinline__ int occupied_slots(const int32_t *__restrict__ ln, int S, int m,
+                                              int present_mask, int *list, int lane) {
+    int cnt = 0;
+    for (int s0 = 0; s0 < S; s0 += 32) {
+        const int s = s0 + lane;
+        const bool occ = s < S && ln[s] > 0 && ((present_mask >> (s / m)) & 1);
+        const unsigned b = __ballot_sync(0xffffffffu, occ);
+        if (occ) list[cnt + __popc(b & ((1u << lane) - 1u))] = s;
+        cnt += __popc(b);
+    }
+    __syncwarp();
+    return cnt;
+}
+
+// One slot's normalised row, its tangent and the embedding input (s, sdot).
+template <typename T>
+__device__ __forceinline__ void slot_rows(const T *__restrict__ idr, const T *__restrict__ gF,
+                                          const T *__restrict__ gV, const int32_t *__restrict__ ln,
+                                          long long t, long long cfg0, int slot, int S,
+                                          const T *avg, const T *sd, const TrainParams &P,
+                                          T rh[4], T rd[4]) {
+    const T *row = idr + (t * S + slot) * 4;
+    const T R = row[0], x = row[1], y = row[2], z = row[3];
+    env_row(R, x, y, z, (T)P.rmin, (T)P.rmax, avg, sd, rh);
+    const long long j = cfg0 + ln[t * S + slot] - 1;
+    T u[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) u[a] = gF[3 * j + a] - gF[3 * t + a];
+    if (P.has_gv) {
+        const T *g = gV + 9 * (t / P.natoms);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) u[a] += g[3 * a] * x + g[3 * a + 1] * y + g[3 * a + 2] * z;
+    }
+    rid_dir(R, x, y, z, (T)P.rmin, (T)P.rmax, sd, u, rd);
+}
+
+// Embedding layer 0 (1 -> E) and its tangent.
+template <typename T>
+__device__ __forceinline__ void layer0(const T *w, T s, T sdot, T x[E], T xd[E]) {
+#pragma unroll
+    for (int o = 0; o < E; ++o) {
+        const T t = dev_tanh(s * w[EmbOff::W0 + o] + w[EmbOff::B0 + o]);
+        x[o] = t;
+        xd[o] = (T(1) - t * t) * sdot * w[EmbOff::W0 + o];
+    }
+}
+
+// Residual layer (E -> E): x <- tanh(x W + b) dt + x with its tangent; optionally returns the
+// tanh output t and the pre-activation tangent zd.
+template <typename T, bool KEEP>
+__device__ __forceinline__ void layer_res(const T *w, int OW, int OB, int OD, T x[E], T xd[E],
+                                          T *t_out, T *zd_out) {
+    T h[E], hd[E];
+#pragma unroll
+    for (int o = 0; o < E; ++o) { h[o] = w[OB + o]; hd[o] = T(0); }
+#pragma unroll
+    for (int i = 0; i < E; ++i) {
+        const T xi = x[i], xdi = xd[i];
+#pragma unroll
+        for (int o = 0; o < E; ++o) {
+            const T wv = w[OW + i * E + o];
+            h[o] += xi * wv;
+            hd[o] += xdi * wv;
+        }
+    }
+#pragma unroll
+    for (int o = 0; o < E; ++o) {
+        const T t = dev_tanh(h[o]);
+        const T dt = w[OD + o];
+        if (KEEP) { t_out[o] = t; zd_out[o] = hd[o]; }
+        x[o] = t * dt + x[o];
+        xd[o] = (T(1) - t * t) * hd[o] * dt + xd[o];
+    }
+}
+
+// ------------------------------------------------------------------------------ dual forward
+template <typename T>
+__global__ void __launch_bounds__(128)
+dp_dual_fwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
+            const int32_t *__restrict__ type_map, const T *__restrict__ params,
+            const T *__restrict__ davg, const T *__restrict__ dstd, const T *__restrict__ gF,
+            const T *__restrict__ gV, T *__restrict__ Aout, T *__restrict__ Adout,
+            TrainParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nnet = P.ntypes * P.ntypes, S = P.nslots;
+    const int warps = blockDim.x >> 5;
+    T *wsm = reinterpret_cast<T *>(smem_raw);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T *stg = wsm + nnet * EmbOff::SIZE + warp * 32 * (2 * kStg + 8);   // G, Gdot, rh, rd
+    int *list = reinterpret_cast<int *>(wsm + nnet * EmbOff::SIZE + warps * 32 * (2 * kStg + 8)) +
+                warp * S;
+    for (int q = threadIdx.x; q < nnet * EmbOff::SIZE; q += blockDim.x) wsm[q] = params[q];
+    __syncthreads();
+    const long long total = (long long)P.batch * P.natoms;
+    for (long long t = (long long)blockIdx.x * warps + warp; t < total;
+         t += (long long)gridDim.x * warps) {
+        const int ti = type_map[t % P.natoms];
+        T *Arow = Aout + t * NA, *Adrow = Adout + t * NA;
+        if (ti < 0 || ti >= P.ntypes || !((P.present_mask >> ti) & 1)) {
+            for (int e = lane; e < NA; e += 32) Arow[e] = Adrow[e] = T(0);
+            continue;
+        }
+        const long long cfg0 = (t / P.natoms) * P.natoms;
+        const int cnt = occupied_slots(list_neigh + t * S, S, P.m, P.present_mask, list, lane);
+        const T *avg = davg + 4 * ti, *sd = dstd + 4 * ti;
+        T a[4], ad[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a[q] = ad[q] = T(0);
+        for (int c0 = 0; c0 < cnt; c0 += 32) {
+            const int k = c0 + lane;
+            T rh[4] = {T(0), T(0), T(0), T(0)}, rd[4] = {T(0), T(0), T(0), T(0)};
+            T x[E], xd[E];
+            int tj = 0;
+            if (k < cnt) {
+                const int slot = list[k];
+                tj = slot / P.m;
+                slot_rows(idr, gF, gV, list_neigh, t, cfg0, slot, S, avg, sd, P, rh, rd);
+            }
+            const T *w = wsm + (ti * P.ntypes + tj) * EmbOff::SIZE;
+            layer0(w, rh[0], rd[0], x, xd);
+            layer_res<T, false>(w, EmbOff::W1, EmbOff::B1, EmbOff::DT1, x, xd, nullptr, nullptr);
+            layer_res<T, false>(w, EmbOff::W2, EmbOff::B2, EmbOff::DT2, x, xd, nullptr, nullptr);
+            if (k >= cnt) {
+#pragma unroll
+                for (int c = 0; c < 4; ++c) rh[c] = rd[c] = T(0);
+            }
+            __syncwarp();
+            T *my = stg + lane * (2 * kStg + 8);
+#pragma unroll
+            for (int p = 0; p < E; ++p) { my[p] = x[p]; my[kStg + p] = xd[p]; }
+#pragma unroll
+            for (int c = 0; c < 4; ++c) { my[2 * kStg + c] = rh[c]; my[2 * kStg + 4 + c] = rd[c]; }
+            __syncwarp();
+            const int nv = min(32, cnt - c0);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int e = lane + 32 * q;
+                if (e < NA) {
+                    const int c = e / E, p = e - c * E;
+                    T s0 = a[q], s1 = ad[q];
+                    for (int l = 0; l < nv; ++l) {
+                        const T *r = stg + l * (2 * kStg + 8);
+                        const T g = r[p];
+                        s0 += r[2 * kStg + c] * g;
+                        s1 += r[2 * kStg + 4 + c] * g + r[2 * kStg + c] * r[kStg + p];
+                    }
+                    a[q] = s0;
+                    ad[q] = s1;
+                }
+            }
+            __syncwarp();
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int e = lane + 32 * q;
+            if (e < NA) {
+                Arow[e] = a[q] * (T)P.inv_mT;
+                Adrow[e] = ad[q] * (T)P.inv_mT;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// ----------------------------------------------------------------------------- dual backward
+// Per-warp staging of one layer for the weight-gradient reduction: layer input x and its
+// tangent xd, pre-activation adjoints zb / zdb, and the dt-gradient term q.
+struct Stage {
+    static constexpr int X = 0, XD = kStg, ZB = 2 * kStg, ZDB = 3 * kStg, Q = 4 * kStg;
+    static constexpr int ROW = 5 * kStg + 3;          // + (s, sdot, pad)
+};
+
+// Adds, for every net present among the chunk's lanes, sum over its lanes of the layer's
+// gradient terms into the CTA accumulator gacc (shared).  lay = 1 or 2 (W/b/dt of that layer),
+// lay = 0: W0 / b0 from (s, sdot).
+template <typename T>
+__device__ __forceinline__ void reduce_layer(const T *stg, int nv, int ti, int ntypes,
+                                             unsigned tmask[], int lay, T *gacc, int lane) {
+    for (int tj = 0; tj < ntypes; ++tj) {
+        const unsigned mk = tmask[tj];
+        if (!mk) continue;
+        const int lo = __ffs(mk) - 1, hi = 32 - __clz(mk);
+        T *g = gacc + (ti * ntypes + tj) * EmbOff::SIZE;
+        if (lay == 0) {
+            for (int e = lane; e < 2 * E; e += 32) {
+                const int o = e < E ? e : e - E;
+                T acc = T(0);
+                for (int l = lo; l < hi; ++l) {
+                    const T *r = stg + l * Stage::ROW;
+                    acc += e < E ? r[5 * kStg] * r[Stage::ZB + o] + r[5 * kStg + 1] * r[Stage::ZDB + o]
+                                 : r[Stage::ZB + o];
+                }
+                atomicAdd(g + (e < E ? EmbOff::W0 : EmbOff::B0) + o, acc);
+            }
+            continue;
+        }
+        const int OW = lay == 1 ? EmbOff::W1 : EmbOff::W2;
+        const int OB = lay == 1 ? EmbOff::B1 : EmbOff::B2;
+        const int OD = lay == 1 ? EmbOff::DT1 : EmbOff::DT2;
+        for (int e = lane; e < E * E + 2 * E; e += 32) {
+            T acc = T(0);
+            if (e < E * E) {
+                const int i = e / E, o = e - i * E;
+                for (int l = lo; l < hi; ++l) {
+                    const T *r = stg + l * Stage::ROW;
+                    acc += r[Stage::X + i] * r[Stage::ZB + o] + r[Stage::XD + i] * r[Stage::ZDB + o];
+                }
+                atomicAdd(g + OW + e, acc);
+            } else {
+                const int o = e - E * E;
+                const int col = o < E ? Stage::ZB + o : Stage::Q + (o - E);
+                for (int l = lo; l < hi; ++l) acc += stg[l * Stage::ROW + col];
+                atomicAdd(g + (o < E ? OB + o : OD + (o - E)), acc);
+            }
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128)
+dp_dual_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
+            const int32_t *__restrict__ type_map, const T *__restrict__ params,
+            const T *__restrict__ davg, const T *__restrict__ dstd, const T *__restrict__ gF,
+            const T *__restrict__ gV, const T *__restrict__ Abar, const T *__restrict__ Adbar,
+            T *__restrict__ grad, TrainParams P) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int nnet = P.ntypes * P.ntypes, S = P.nslots;
+    const int warps = blockDim.x >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    T *wsm = reinterpret_cast<T *>(smem_raw);                   // weights
+    T *gacc = wsm + nnet * EmbOff::SIZE;                        // gradient accumulator
+    T *stg_all = gacc + nnet * EmbOff::SIZE;                    // [warps][32][Stage::ROW]
+    T *ab_all = stg_all + warps * 32 * Stage::ROW;              // [warps][2][NA]
+    int *list_all = reinterpret_cast<int *>(ab_all + warps * 2 * NA);
+    T *stg = stg_all + warp * 32 * Stage::ROW;
+    T *ab = ab_all + warp * 2 * NA;
+    int *list = list_all + warp * S;
+    for (int q = threadIdx.x; q < nnet * EmbOff::SIZE; q += blockDim.x) {
+        wsm[q] = params[q];
+        gacc[q] = T(0);
+    }
+    __syncthreads();
+    const T k = (T)P.inv_mT;
+    const long long total = (long long)P.batch * P.natoms;
+    for (long long t = (long long)blockIdx.x * warps + warp; t < total;
+         t += (long long)gridDim.x * warps) {
+        const int ti = type_map[t % P.natoms];
+        if (ti < 0 || ti >= P.ntypes || !((P.present_mask >> ti) & 1)) continue;
+        const long long cfg0 = (t / P.natoms) * P.natoms;
+        const int cnt = occupied_slots(list_neigh + t * S, S, P.m, P.present_mask, list, lane);
+        for (int e = lane; e < NA; e += 32) {
+            ab[e] = Abar[t * NA + e] * k;
+            ab[NA + e] = Adbar[t * NA + e] * k;
+        }
+        __syncwarp();
+        const T *avg = davg + 4 * ti, *sd = dstd + 4 * ti;
+        for (int c0 = 0; c0 < cnt; c0 += 32) {
+            const int kk = c0 + lane;
+            const bool valid = kk < cnt;
+            T rh[4] = {T(0), T(0), T(0), T(0)}, rd[4] = {T(0), T(0), T(0), T(0)};
+            int tj = 0;
+            if (valid) {
+                const int slot = list[kk];
+                tj = slot / P.m;
+                slot_rows(idr, gF, gV, list_neigh, t, cfg0, slot, S, avg, sd, P, rh, rd);
+            }
+            unsigned tmask[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q)
+                tmask[q] = q < P.ntypes ? __ballot_sync(0xffffffffu, valid && tj == q) : 0u;
+            const int nv = min(32, cnt - c0);
+            const T *w = wsm + (ti * P.ntypes + tj) * EmbOff::SIZE;
+            T *my = stg + lane * Stage::ROW;
+            // seeds: Gbar = k (R Abar + Rdot Adbar), Gdotbar = k R Adbar (k folded into ab)
+            T gb[E], gdb[E];
+#pragma unroll
+            for (int p = 0; p < E; ++p) {
+                T s0 = T(0), s1 = T(0);
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    s0 += rh[c] * ab[c * E + p] + rd[c] * ab[NA + c * E + p];
+                    s1 += rh[c] * ab[NA + c * E + p];
+                }
+                gb[p] = valid ? s0 : T(0);
+                gdb[p] = valid ? s1 : T(0);
+            }
+            // ---- layer 2: forward to its input, keep t2 and its pre-activation tangent
+            {
+                T x[E], xd[E], t2[E], zd2[E];
+                layer0(w, rh[0], rd[0], x, xd);
+                layer_res<T, false>(w, EmbOff::W1, EmbOff::B1, EmbOff::DT1, x, xd, nullptr, nullptr);
+                __syncwarp();
+#pragma unroll
+                for (int p = 0; p < E; ++p) { my[Stage::X + p] = x[p]; my[Stage::XD + p] = xd[p]; }
+                layer_res<T, true>(w, EmbOff::W2, EmbOff::B2, EmbOff::DT2, x, xd, t2, zd2);
+#pragma unroll
+                for (int o = 0; o < E; ++o) {
+                    const T dt = w[EmbOff::DT2 + o], g = T(1) - t2[o] * t2[o];
+                    const T tb = gb[o] * dt, tdb = gdb[o] * dt;
+                    my[Stage::Q + o] = gb[o] * t2[o] + gdb[o] * g * zd2[o];
+                    my[Stage::ZB + o] = g * (tb - T(2) * t2[o] * zd2[o] * tdb);
+                    my[Stage::ZDB + o] = g * tdb;
+                }
+            }
+            __syncwarp();
+            // x1bar = Gbar + W2 zb2, x1dotbar = Gdotbar + W2 zdb2
+#pragma unroll
+            for (int i = 0; i < E; ++i) {
+                T s0 = gb[i], s1 = gdb[i];
+#pragma unroll
+                for (int o = 0; o < E; ++o) {
+                    const T wv = w[EmbOff::W2 + i * E + o];
+                    s0 += wv * my[Stage::ZB + o];
+                    s1 += wv * my[Stage::ZDB + o];
+                }
+                gb[i] = s0;
+                gdb[i] = s1;
+            }
+            reduce_layer(stg, nv, ti, P.ntypes, tmask, 2, gacc, lane);
+            __syncwarp();
+            // ---- layer 1: recompute layer 0, keep t1 and its pre-activation tangent
+            T x0[E], xd0[E];
+            layer0(w, rh[0], rd[0], x0, xd0);
+            {
+                T x[E], xd[E], t1[E], zd1[E];
+#pragma unroll
+                for (int p = 0; p < E; ++p) {
+                    x[p] = x0[p];
+                    xd[p] = xd0[p];
+                    my[Stage::X + p] = x0[p];
+                    my[Stage::XD + p] = xd0[p];
+                }
+                layer_res<T, true>(w, EmbOff::W1, EmbOff::B1, EmbOff::DT1, x, xd, t1, zd1);
+#pragma unroll
+                for (int o = 0; o < E; ++o) {
+                    const T dt = w[EmbOff::DT1 + o], g = T(1) - t1[o] * t1[o];
+                    const T tb = gb[o] * dt, tdb = gdb[o] * dt;
+                    my[Stage::Q + o] = gb[o] * t1[o] + gdb[o] * g * zd1[o];
+                    my[Stage::ZB + o] = g * (tb - T(2) * t1[o] * zd1[o] * tdb);
+                    my[Stage::ZDB + o] = g * tdb;
+                }
+            }
+            __syncwarp();
+#pragma unroll
+            for (int i = 0; i < E; ++i) {
+                T s0 = gb[i], s1 = gdb[i];
+#pragma unroll
+                for (int o = 0; o < E; ++o) {
+                    const T wv = w[EmbOff::W1 + i * E + o];
+                    s0 += wv * my[Stage::ZB + o];
+                    s1 += wv * my[Stage::ZDB + o];
+                }
+                gb[i] = s0;
+                gdb[i] = s1;
+            }
+            reduce_layer(stg, nv, ti, P.ntypes, tmask, 1, gacc, lane);
+            __syncwarp();
+            // ---- layer 0: x0 = tanh(s W0 + b0), x0dot = (1 - x0^2) sdot W0
+#pragma unroll
+            for (int o = 0; o < E; ++o) {
+                const T g = T(1) - x0[o] * x0[o];
+                const T zd0 = rd[0] * w[EmbOff::W0 + o];
+                my[Stage::ZB + o] = g * (gb[o] - T(2) * x0[o] * zd0 * gdb[o]);
+                my[Stage::ZDB + o] = g * gdb[o];
+            }
+            my[5 * kStg] = rh[0];
+            my[5 * kStg + 1] = rd[0];
+            __syncwarp();
+            reduce_layer(stg, nv, ti, P.ntypes, tmask, 0, gacc, lane);
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < nnet * EmbOff::SIZE; q += blockDim.x)
+        if (gacc[q] != T(0)) atomicAdd(grad + q, gacc[q]);
+}
+
+int check_args(int dtype, int batch, int natoms, int nslots, int ntypes, int m) {
+    MATPL_REQUIRE(dtype == MATPL_F32 || dtype == MATPL_F64, MATPL_ERR_DTYPE,
+                  "the training kernels support MATPL_F32 and MATPL_F64");
+    MATPL_REQUIRE(batch > 0 && natoms > 0 && ntypes >= 1 && ntypes <= 16 && m > 0 &&
+                      nslots == ntypes * m && nslots <= 4096,
+                  MATPL_ERR_INVALID, "bad batch / natoms / ntypes / m / nslots");
+    return MATPL_OK;
+}
+
+template <typename T>
+int launch(bool backward, const matpl_dp_model *md, int batch, int natoms, int nslots,
+           const int32_t *ln, const void *idr, const int32_t *tm, const void *gF, const void *gV,
+           const void *a_in, const void *ad_in, void *out0, void *out1, cudaStream_t s) {
+    TrainParams P;
+    P.batch = batch; P.natoms = natoms; P.nslots = nslots; P.ntypes = md->ntypes; P.m = md->m;
+    P.present_mask = 0;
+    for (int q = 0; q < md->npresent; ++q) P.present_mask |= 1 << md->present[q];
+    P.has_gv = gV != nullptr;
+    P.rmin = md->rmin; P.rmax = md->rmax;
+    P.inv_mT = 1.0 / ((double)md->m * (double)md->npresent);
+    const int nnet = md->ntypes * md->ntypes;
+    const size_t wbytes = (size_t)nnet * EmbOff::SIZE * sizeof(T);
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long total = (long long)batch * natoms;
+    if (!backward) {
+        const int warps = 4;
+        const size_t smem = wbytes + (size_t)warps * 32 * (2 * kStg + 8) * sizeof(T) +
+                            (size_t)warps * nslots * sizeof(int);
+        MATPL_REQUIRE(smem <= 220 * 1024, MATPL_ERR_UNSUPPORTED, "too many types for shared memory");
+        cudaFuncSetAttribute(dp_dual_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        long long grid = (total + warps - 1) / warps;
+        if (grid > (long long)sms * 8) grid = (long long)sms * 8;
+        ProfScope ps("dp_dual_fwd", s);
+        dp_dual_fwd<T><<<(int)grid, 32 * warps, smem, s>>>(
+            ln, (const T *)idr, tm, (const T *)md->params, (const T *)md->davg,
+            (const T *)md->dstd, (const T *)gF, (const T *)gV, (T *)out0, (T *)out1, P);
+        return check_launch("matpl_dp_dual_forward");
+    }
+    int warps = 4;
+    auto need = [&](int w) {
+        return 2 * wbytes + (size_t)w * 32 * Stage::ROW * sizeof(T) +
+               (size_t)w * 2 * NA * sizeof(T) + (size_t)w * nslots * sizeof(int);
+    };
+    while (warps > 1 && need(warps) > 220 * 1024) --warps;
+    const size_t smem = need(warps);
+    MATPL_REQUIRE(smem <= 220 * 1024, MATPL_ERR_UNSUPPORTED, "too many types for shared memory");
+    cudaFuncSetAttribute(dp_dual_bwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    long long grid = (total + warps - 1) / warps;
+    if (grid > (long long)sms * 4) grid = (long long)sms * 4;
+    cudaMemsetAsync(out0, 0, wbytes, s);
+    ProfScope ps("dp_dual_bwd", s);
+    dp_dual_bwd<T><<<(int)grid, 32 * warps, smem, s>>>(
+        ln, (const T *)idr, tm, (const T *)md->params, (const T *)md->davg, (const T *)md->dstd,
+        (const T *)gF, (const T *)gV, (const T *)a_in, (const T *)ad_in, (T *)out0, P);
+    return check_launch("matpl_dp_dual_backward");
+}
+
+int validate(int dtype, const matpl_dp_model *model, int batch, int natoms, int nslots,
+             const int32_t *ln, const void *idr, const int32_t *tm, const void *gF) {
+    MATPL_REQUIRE(model != nullptr, MATPL_ERR_INVALID, "null model");
+    int st = check_args(dtype, batch, natoms, nslots, model->ntypes, model->m);
+    if (st) return st;
+    MATPL_REQUIRE(model->npresent >= 1 && model->npresent <= 8, MATPL_ERR_INVALID,
+                  "npresent must be 1..8");
+    for (int q = 0; q < model->npresent; ++q)
+        MATPL_REQUIRE(model->present[q] >= 0 && model->present[q] < model->ntypes,
+                      MATPL_ERR_INVALID, "present[] entry outside [0, ntypes)");
+    MATPL_REQUIRE(model->params && model->davg && model->dstd && ln && idr && tm && gF,
+                  MATPL_ERR_INVALID, "null pointer argument");
+    return MATPL_OK;
+}
+
+}  // namespace
+}  // namespace matpl
+
+using namespace matpl;
+
+extern "C" int matpl_dp_dual_forward(int dtype, const matpl_dp_model *model, int batch,
+                                     int natoms, int nslots, const int32_t *list_neigh,
+                                     const void *image_dr, const int32_t *type_map,
+                                     const void *grad_force, const void *grad_virial, void *A,
+                                     void *A_dot, void *stream) {
+    int st = validate(dtype, model, batch, natoms, nslots, list_neigh, image_dr, type_map,
+                      grad_force);
+    if (st) return st;
+    MATPL_REQUIRE(A && A_dot, MATPL_ERR_INVALID, "null output");
+    return dtype == MATPL_F64
+               ? launch<double>(false, model, batch, natoms, nslots, list_neigh, image_dr,
+                                type_map, grad_force, grad_virial, nullptr, nullptr, A, A_dot,
+                                as_stream(stream))
+               : launch<float>(false, model, batch, natoms, nslots, list_neigh, image_dr,
+                               type_map, grad_force, grad_virial, nullptr, nullptr, A, A_dot,
+                               as_stream(stream));
+}
+
+extern "C" int matpl_dp_dual_backward(int dtype, const matpl_dp_model *model, int batch,
+                                      int natoms, int nslots, const int32_t *list_neigh,
+                                      const void *image_dr, const int32_t *type_map,
+                                      const void *grad_force, const void *grad_virial,
+                                      const void *A_bar, const void *A_dot_bar,
+                                      void *grad_embedding, void *stream) {
+    int st = validate(dtype, model, batch, natoms, nslots, list_neigh, image_dr, type_map,
+                      grad_force);
+    if (st) return st;
+    MATPL_REQUIRE(A_bar && A_dot_bar && grad_embedding, MATPL_ERR_INVALID, "null pointer");
+    return dtype == MATPL_F64
+               ? launch<double>(true, model, batch, natoms, nslots, list_neigh, image_dr,
+                                type_map, grad_force, grad_virial, A_bar, A_dot_bar,
+                                grad_embedding, nullptr, as_stream(stream))
+               : launch<float>(true, model, batch, natoms, nslots, list_neigh, image_dr,
+                               type_map, grad_force, grad_virial, A_bar, A_dot_bar,
+                               grad_embedding, nullptr, as_stream(stream));
+}

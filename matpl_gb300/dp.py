@@ -125,7 +125,8 @@ class DP(torch.nn.Module):
     device sync); the benchmark turns it off inside its timed loop."""
 
     def __init__(self, cfg: DPConfig, params: Dict[str, torch.Tensor], davg, dstd,
-                 precision: str = "float64", device="cuda", check_errors: bool = True):
+                 precision: str = "float64", device="cuda", check_errors: bool = True,
+                 packed: Optional[torch.Tensor] = None):
         super().__init__()
         check_shape(cfg)
         if precision not in PRECISIONS:
@@ -137,7 +138,9 @@ class DP(torch.nn.Module):
         dev = torch.device(device)
         self.register_buffer("err", torch.zeros(1, dtype=torch.int32, device=dev))
         self.device = dev
-        self.register_buffer("packed", pack_params(cfg, params, self.dtype).to(dev))
+        if packed is None:
+            packed = pack_params(cfg, params, self.dtype)
+        self.register_buffer("packed", packed.to(device=dev, dtype=self.dtype).clone())
         davg = torch.as_tensor(davg)
         dstd = torch.as_tensor(dstd)
         self.register_buffer("davg4", per_type_stats(davg, cfg.ntypes).to(dev, self.dtype))

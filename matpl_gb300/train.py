@@ -143,3 +143,202 @@ def train_step(model: DPTrainModel, batches: Sequence[dict], optimizer: torch.op
         optimizer.step()
         total += float(loss.detach())
     return total
+
+
+# ----------------------------------------------------------------------------------------------
+# Fused force-loss gradient: the embedding nets' second-order part runs in this library's
+# kernels (matpl_dp_dual_forward / matpl_dp_dual_backward, recomputing activations), the small
+# per-atom fitting part in torch.
+# ----------------------------------------------------------------------------------------------
+import ctypes  # noqa: E402
+
+from . import _lib, dp as _dp  # noqa: E402
+from ._lib import check as _check, ptr as _ptr  # noqa: E402
+
+
+def _emb_flat(model: DPTrainModel) -> torch.Tensor:
+    """Embedding parameters of every (t_i, t_j) net in the packed order of csrc/dp_layout.cuh,
+    built from the model's Parameters with differentiable ops (gradients flow back to them)."""
+    E = _dp.E
+    parts = []
+    for k in range(model.cfg.ntypes ** 2):
+        pre = f"embedding_net.{k}.layers."
+        for l in range(3):
+            w = model.param(pre + f"{l}.weight")
+            b = model.param(pre + f"{l}.bias")
+            parts.append(w.reshape(-1))
+            parts.append(b.reshape(-1) if b is not None else w.new_zeros(E))
+            if l > 0:
+                dt = model.param(pre + f"{l}.resnet_dt")
+                parts.append(dt.reshape(-1) if dt is not None else w.new_ones(E))
+    return torch.cat(parts)
+
+
+def _pack_device(model: DPTrainModel) -> torch.Tensor:
+    """Full packed parameter buffer (csrc/dp_layout.cuh) on the model's device, no autograd."""
+    cfg, F, DIN = model.cfg, _dp.F, _dp.DIN
+    with torch.no_grad():
+        parts = [_emb_flat(model)]
+        for t in range(cfg.ntypes):
+            pre = f"fitting_net.{t}.layers."
+
+            def g(name, n, fill):
+                v = model.param(pre + name)
+                return v.reshape(-1) if v is not None else torch.full(
+                    (n,), fill, dtype=model.dtype, device=model.davg.device)
+            W0, W1, W2 = g("0.weight", 0, 0), g("1.weight", 0, 0), g("2.weight", 0, 0)
+            parts += [W0, g("0.bias", F, 0.0), W1, g("1.bias", F, 0.0), g("1.resnet_dt", F, 1.0),
+                      W2, g("2.bias", F, 0.0), g("2.resnet_dt", F, 1.0), g("3.weight", 0, 0),
+                      g("3.bias", 1, 0.0), W0.new_zeros(3),
+                      W0.reshape(DIN, F).t().reshape(-1), W1.reshape(F, F).t().reshape(-1),
+                      W2.reshape(F, F).t().reshape(-1)]
+        return torch.cat(parts).contiguous()
+
+
+class _EmbedDual(torch.autograd.Function):
+    """(A, A_dot) = per-atom descriptor factor over occupied slots and its tangent along the
+    force / virial seed (matpl_dp_dual_forward); the backward is matpl_dp_dual_backward."""
+
+    @staticmethod
+    def forward(ctx, emb_flat, trainer, ln, idr, tm, gF, gV):
+        B, N, S = ln.shape
+        dev = idr.device
+        A = torch.empty(B * N, 4 * _dp.E, dtype=idr.dtype, device=dev)
+        Ad = torch.empty_like(A)
+        flat = emb_flat.detach().contiguous()
+        m = trainer._struct(flat)
+        _check(_lib.load().matpl_dp_dual_forward(
+            trainer.code, ctypes.byref(m), B, N, S, _ptr(ln), _ptr(idr), _ptr(tm), _ptr(gF),
+            _ptr(gV), _ptr(A), _ptr(Ad), torch.cuda.current_stream(dev).cuda_stream),
+            "matpl_dp_dual_forward")
+        ctx.trainer = trainer
+        ctx.save_for_backward(flat, ln, idr, tm, gF, gV if gV is not None else flat[:0])
+        ctx.has_gv = gV is not None
+        return A, Ad
+
+    @staticmethod
+    def backward(ctx, gA, gAd):
+        flat, ln, idr, tm, gF, gV = ctx.saved_tensors
+        B, N, S = ln.shape
+        dev = idr.device
+        gA = torch.zeros_like(flat[:0].new_empty(B * N, 4 * _dp.E)) if gA is None else gA.contiguous()
+        gAd = torch.zeros_like(gA) if gAd is None else gAd.contiguous()
+        grad = torch.empty_like(flat)
+        m = ctx.trainer._struct(flat)
+        _check(_lib.load().matpl_dp_dual_backward(
+            ctx.trainer.code, ctypes.byref(m), B, N, S, _ptr(ln), _ptr(idr), _ptr(tm), _ptr(gF),
+            _ptr(gV) if ctx.has_gv else 0, _ptr(gA), _ptr(gAd), _ptr(grad),
+            torch.cuda.current_stream(dev).cuda_stream), "matpl_dp_dual_backward")
+        return grad, None, None, None, None, None, None
+
+
+class FusedTrainer:
+    """Force-loss training step with the embedding nets' second-order gradient in this
+    library's kernels.  Per composition cluster (as ``dp_trainer.train``):
+
+    1. E, F with the current parameters through the fused evaluation (``matpl_dp_eval``);
+    2. gE = dL/dE, gF = dL/dF of the loss (dp_loss's MSE terms) on those values;
+    3. A, A_dot = per-atom descriptor factor and its tangent along the seed gF
+       (``matpl_dp_dual_forward``), plus the empty-slot term of A in torch;
+    4. Ei = fitting nets (torch) on D = A^T A<, Edot = dEi/dA . A_dot;
+    5. Phi = sum gE Etot + sum Edot; Phi.backward() gives dL/dtheta: the fitting part by torch
+       autograd on per-atom tensors, the embedding part by ``matpl_dp_dual_backward``.
+
+    ``model`` is a DPTrainModel (its Parameters are trained); ``precision`` "float64" or
+    "float32" must match the model's dtype."""
+
+    def __init__(self, model: DPTrainModel):
+        if model.dtype not in (torch.float32, torch.float64):
+            raise _lib.MatplError("FusedTrainer needs a float32 or float64 DPTrainModel")
+        self.model = model
+        cfg = model.cfg
+        self.code = _lib.MATPL_F64 if model.dtype == torch.float64 else _lib.MATPL_F32
+        prec = "float64" if model.dtype == torch.float64 else "float32"
+        dev = model.davg.device
+        self.evaluator = _dp.DP(cfg, {}, model.davg.cpu(), model.dstd.cpu(), precision=prec,
+                                device=dev, check_errors=False, packed=_pack_device(model))
+        self.davg4 = self.evaluator.davg4
+        self.dstd4 = self.evaluator.dstd4
+        self._present = None
+
+    def _struct(self, flat):
+        m = _lib.MatplDpModel()
+        cfg = self.model.cfg
+        m.ntypes, m.m = cfg.ntypes, cfg.maxNeighborNum
+        m.npresent = len(self._present)
+        for q, t in enumerate(self._present):
+            m.present[q] = t
+        m.rmin, m.rmax = float(cfg.Rmin), float(cfg.Rmax)
+        m.params, m.davg, m.dstd = _ptr(flat), _ptr(self.davg4), _ptr(self.dstd4)
+        m.err_dev = _ptr(self.evaluator.err)
+        return m
+
+    def _pad_term(self, ln, present):
+        """Empty-slot term of A (before the 1/(mT) scale is applied): per atom
+        sum over present t_j of n_empty(t_j) R_pad(t_i) (x) G_{t_i t_j}(s_pad(t_i))."""
+        model, cfg = self.model, self.model.cfg
+        B, N, S = ln.shape
+        m = cfg.maxNeighborNum
+        tmap = self._tm_long
+        out = torch.zeros(B, N, 4, _dp.E, dtype=model.dtype, device=ln.device)
+        occ = (ln > 0).reshape(B, N, cfg.ntypes, m).sum(-1)              # [B, N, ntypes]
+        for ti in present:
+            rp = (0.0 - self.davg4[ti]) / self.dstd4[ti]                 # [4]
+            sel = (tmap == ti).to(model.dtype).reshape(1, N, 1, 1)
+            for tj in present:
+                G = model._emb(ti * cfg.ntypes + tj, rp[0:1].reshape(1, 1))[0]   # [E]
+                nemp = (m - occ[:, :, tj]).to(model.dtype).reshape(B, N, 1, 1)
+                out = out + sel * nemp * (rp.reshape(4, 1) * G.reshape(1, _dp.E))
+        return out
+
+    def loss_and_backward(self, batch: dict, w_f: float = 1.0, w_e: float = 1.0):
+        model, cfg = self.model, self.model.cfg
+        ln = batch["list_neigh"]
+        B, N, S = ln.shape
+        dev = ln.device
+        ln32 = ln.to(torch.int32).contiguous()
+        idr = batch["ImageDR"].to(model.dtype).contiguous()
+        tm32 = batch["type_map"].to(device=dev, dtype=torch.int32).contiguous()
+        self._tm_long = tm32.long()
+        present = [cfg.atom_type.index(int(a)) for a in batch["atom_type"]
+                   if int(a) in cfg.atom_type]
+        self._present = present
+        # 1. E, F with the current parameters
+        self.evaluator.packed.copy_(_pack_device(model))
+        r = self.evaluator.evaluate(ln32, tm32, present, idr, 0)
+        # 2. loss gradient w.r.t. E and F
+        Et = r["Etot"].to(model.dtype).reshape(B, 1).detach().requires_grad_()
+        Fo = r["Force"].detach().requires_grad_()
+        le = torch.nn.functional.mse_loss(Et, batch["Etot"].to(model.dtype).reshape(B, 1))
+        lf = torch.nn.functional.mse_loss(Fo, batch["Force"].to(model.dtype))
+        loss = w_e * le + w_f * lf
+        gE, gF = torch.autograd.grad(loss, [Et, Fo])
+        gF = gF.contiguous()
+        # 3. descriptor factor and its tangent
+        A_occ, Ad = _EmbedDual.apply(_emb_flat(model), self, ln32, idr, tm32, gF, None)
+        A = A_occ.reshape(B, N, 4, _dp.E) + self._pad_term(ln, present) / (cfg.maxNeighborNum * len(present))
+        Ad = Ad.reshape(B, N, 4, _dp.E)
+        # 4. per-atom energies and their tangent
+        Ei = torch.zeros(B, N, dtype=model.dtype, device=dev)
+        for ti in present:
+            idx = torch.nonzero(self._tm_long == ti).flatten()
+            if idx.numel() == 0:
+                continue
+            Ab = A[:, idx]
+            D = Ab.transpose(-2, -1) @ Ab[..., :cfg.M2]
+            Ei = Ei.index_put((torch.arange(B, device=dev).unsqueeze(1), idx.unsqueeze(0)),
+                              model._fit(ti, D.reshape(B, idx.numel(), -1)).squeeze(-1))
+        gA = torch.autograd.grad(Ei.sum(), A, create_graph=True)[0]
+        phi = (gE.reshape(B) * Ei.sum(1)).sum() + (gA * Ad).sum()
+        # 5. parameter gradients
+        phi.backward()
+        return float(loss.detach()), float(le.detach()), float(lf.detach())
+
+    def step(self, batches, optimizer, w_f: float = 1.0, w_e: float = 1.0):
+        total = 0.0
+        for b in batches:
+            optimizer.zero_grad(set_to_none=True)
+            l, _, _ = self.loss_and_backward(b, w_f, w_e)
+            optimizer.step()
+            total += l
+        return total

@@ -97,3 +97,76 @@ def test_training_steps_reduce_loss():
     for _ in range(5):
         train.train_step(model, [batch], opt)
     assert train.loss_fn(model, batch)[0].item() < first
+
+
+def _fused_grads(case, dtype):
+    cfg, st, ln, idr, davg, dstd, prm, E_lab, F_lab = case
+    model = train.DPTrainModel(cfg, prm, davg, dstd, dtype=dtype, device=DEV)
+    batch = {"list_neigh": torch.tensor(ln, device=DEV), "type_map": torch.tensor(st.types, device=DEV),
+             "atom_type": cfg.atom_type, "ImageDR": torch.tensor(idr, device=DEV),
+             "Etot": E_lab.to(DEV), "Force": F_lab.to(DEV)}
+    tr = train.FusedTrainer(model)
+    loss, _, _ = tr.loss_and_backward(batch)
+    return model, loss
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-8), (torch.float32, 2e-3)])
+def test_fused_training_gradients_match_oracle(dtype, tol):
+    """Hand-written embedding double-backward (matpl_dp_dual_forward / _backward) + torch fitting
+    part against second-order autograd through the FP64 oracle, every parameter."""
+    case = make_case()
+    loss_ref, g_ref = oracle_grads(*case)
+    model, loss = _fused_grads(case, dtype)
+    assert abs(loss - loss_ref) <= (1e-10 if dtype == torch.float64 else 1e-4) * abs(loss_ref)
+    worst, where = 0.0, None
+    for k, gr in g_ref.items():
+        got = model.param(k).grad.detach().double().cpu()
+        scale = gr.abs().max().item() + 1e-30
+        err = (got - gr).abs().max().item() / scale
+        if err > worst:
+            worst, where = err, k
+    print(f"[accuracy] fused training gradients {dtype}: worst relative error {worst:.2e} ({where})")
+    assert worst < tol, (worst, where)
+
+
+def test_fused_training_two_configs_and_fd():
+    """Batch of two configurations of one composition, then a finite-difference check of the
+    fused gradient of one embedding weight."""
+    c1 = make_case(n=36, seed=7)
+    c2 = make_case(n=36, seed=8)
+    cfg, st, ln1, idr1, davg, dstd, prm, E1, F1 = c1
+    ln2, idr2, E2, F2 = c2[2], c2[3], c2[7], c2[8]
+    assert np.array_equal(c1[1].types, c2[1].types)
+    model = train.DPTrainModel(cfg, prm, davg, dstd, dtype=torch.float64, device=DEV)
+    batch = {"list_neigh": torch.tensor(np.concatenate([ln1, ln2]), device=DEV),
+             "type_map": torch.tensor(st.types, device=DEV), "atom_type": cfg.atom_type,
+             "ImageDR": torch.tensor(np.concatenate([idr1, idr2]), device=DEV),
+             "Etot": torch.cat([E1, E2]).reshape(2, 1).to(DEV),
+             "Force": torch.cat([F1, F2]).to(DEV)}
+    ref_model = train.DPTrainModel(cfg, prm, davg, dstd, dtype=torch.float64, device=DEV)
+    l_ref, _, _ = train.loss_fn(ref_model, batch)
+    l_ref.backward()
+    tr = train.FusedTrainer(model)
+    loss, _, _ = tr.loss_and_backward(batch)
+    assert abs(loss - l_ref.item()) <= 1e-10 * abs(l_ref.item())
+    for k in model.names:
+        a = model.param(k).grad
+        b = ref_model.param(k).grad
+        assert (a - b).abs().max().item() <= 1e-8 * (b.abs().max().item() + 1e-30), k
+    name = "embedding_net.2.layers.2.weight"
+    p = model.param(name)
+    flat = p.detach().view(-1)
+    q = 37
+    h = 1e-6
+    vals = []
+    for sgn in (1, -1):
+        with torch.no_grad():
+            flat[q] += sgn * h
+        vals.append(tr.loss_and_backward(batch)[0])
+        with torch.no_grad():
+            flat[q] -= sgn * h
+    fd = (vals[0] - vals[1]) / (2 * h)
+    model.zero_grad(set_to_none=True)
+    tr.loss_and_backward(batch)
+    got = model.param(name).grad.view(-1)[q].item()
+    assert abs(fd - got) <= 1e-5 * max(1.0, abs(fd)), (fd, got)
