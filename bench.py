@@ -367,6 +367,87 @@ def run_nep(args, ws, local, steps, warmup, sample_clocks=True):
     }
 
 
+TRAIN_METRIC = "DP force-loss training step atom-steps/s, fused vs plain FP32"
+
+
+def run_train(args, ws, local, steps, warmup, plain_steps):
+    """Force-loss training step (E-MSE + F-MSE, Adam) on the headline's Li/Si box: the fused
+    step (fused E/F, hand-written embedding double-backward, torch fitting part) against the
+    plain step (env matrix + torch nets + second-order autograd through this library's
+    force / virial ops, the reference's structure), both FP32.  Labels come from a teacher net of
+    the same architecture (other seed) plus N(0, 0.01) noise."""
+    from matpl_gb300 import _lib, dp, ops, params as P, train
+    dev = torch.device("cuda", local)
+    st, cfg, prm = make_workload(args.train_atoms)
+    natoms = st.natoms
+    types_d = torch.tensor(st.types, device=dev)
+    ln, idr = ops.find_neighbore(types_d, torch.tensor(st.frac, device=dev),
+                                 torch.tensor(st.lattice, device=dev), 2, M_NEIGH, RC, RC)
+    sub = slice(0, 4000)
+    davg, dstd = P.calc_stat(cfg, ln[:, sub].cpu().numpy(), idr[:, sub].cpu().numpy(), st.types[sub])
+    teacher = dp.DP(cfg, P.init_params(cfg, SEED_W + 100), davg, dstd, precision="float64", device=dev)
+    present = teacher.present_types(cfg.atom_type)
+    lab = teacher.evaluate(ln, types_d.to(torch.int32), present, idr, 0)
+    g = torch.Generator(device=dev).manual_seed(5)
+    batch = {"list_neigh": ln, "type_map": types_d, "atom_type": cfg.atom_type,
+             "ImageDR": idr.float(),
+             "Etot": (lab["Etot"] + 0.01 * torch.randn(1, generator=g, device=dev,
+                                                       dtype=torch.float64)).reshape(1, 1).float(),
+             "Force": (lab["Force"] + 0.01 * torch.randn(lab["Force"].shape, generator=g, device=dev,
+                                                          dtype=torch.float64)).float()}
+    del teacher, lab
+
+    def timed(step, n, w):
+        for _ in range(w):
+            step()
+        torch.cuda.synchronize()
+        barrier(ws)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            step()
+        e1.record()
+        torch.cuda.synchronize()
+        return max_over_ranks(e0.elapsed_time(e1) / n, ws)
+
+    fmodel = train.DPTrainModel(cfg, prm, davg, dstd, dtype=torch.float32, device=dev)
+    fopt = torch.optim.Adam(fmodel.parameters(), lr=1e-4)
+    trainer = train.FusedTrainer(fmodel)
+    _lib.profile_begin(max(4096, steps * 32))
+    fused_ms = timed(lambda: trainer.step([batch], fopt), steps, warmup)
+    prof = _lib.profile_collect()
+    pmodel = train.DPTrainModel(cfg, prm, davg, dstd, dtype=torch.float32, device=dev)
+    popt = torch.optim.Adam(pmodel.parameters(), lr=1e-4)
+    torch.cuda.reset_peak_memory_stats(dev)
+    plain_ms = timed(lambda: train.train_step(pmodel, [batch], popt), plain_steps, 1)
+    plain_peak = torch.cuda.max_memory_allocated(dev)
+    # gradient agreement of the two paths at one parameter point
+    m1 = train.DPTrainModel(cfg, prm, davg, dstd, dtype=torch.float32, device=dev)
+    m2 = train.DPTrainModel(cfg, prm, davg, dstd, dtype=torch.float32, device=dev)
+    train.FusedTrainer(m1).loss_and_backward(batch)
+    train.loss_fn(m2, batch)[0].backward()
+    worst = 0.0
+    for k in m1.names:
+        a, b = m1.param(k).grad, m2.param(k).grad
+        worst = max(worst, ((a - b).abs().max() / (b.abs().max() + 1e-30)).item())
+    per_kernel = {k: {"ms_per_launch": v[0] / v[1], "launches": v[1]} for k, v in prof.items()}
+    return {
+        "metric": TRAIN_METRIC, "value": ws * natoms / (fused_ms * 1e-3), "unit": "atom-steps/s",
+        "ms_per_step": fused_ms, "steps": steps, "warmup": warmup, "dtype": "f32",
+        "config": {"workload": f"DP se_e2_a force-loss training step (E-MSE + F-MSE, Adam), "
+                               f"{natoms:,}-atom Li/Si box of the headline's density, m=150/type, "
+                               "teacher labels",
+                   "natoms": natoms,
+                   "plain_fp32": {"form": "env matrix + torch nets + second-order autograd through "
+                                          "this library's force / virial ops",
+                                  "ms_per_step": plain_ms, "value": ws * natoms / (plain_ms * 1e-3),
+                                  "steps": plain_steps, "peak_memory_bytes": plain_peak},
+                   "speedup_vs_plain_fp32": plain_ms / fused_ms,
+                   "gradient_max_rel_diff_fused_vs_plain": worst},
+        "kernels": per_kernel,
+    }
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -562,6 +643,9 @@ def run_ours(args, ws, rank, local):
     per_scope = {"nb_cells": 4, "dp_reduce": 2}
     launches = sum(v[1] * per_scope.get(k, 1) for k, v in prof.items())
 
+    train_r = None
+    if not args.no_train:
+        train_r = run_train(args, ws, local, steps=20, warmup=3, plain_steps=3)
     nep = None
     if not args.no_nep:
         nep = run_nep(args, ws, local, steps=max(20, args.steps // 10), warmup=args.warmup,
@@ -595,7 +679,22 @@ def run_ours(args, ws, rank, local):
             "e2e": {"value": ws * NATOMS / (e2e_ms * 1e-3), "unit": "atom-steps/s",
                     "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "kernels": per_kernel, "roofline": roof,
-            "clocks": clocks, "cpu_baseline": cb, "nep": nep}
+            "clocks": clocks, "cpu_baseline": cb, "nep": nep, "train": train_r}
+    print(json.dumps(line))
+
+
+def run_train_line(args, ws, rank, local):
+    torch.cuda.set_device(local)
+    from matpl_gb300 import _lib
+    _lib.load()
+    steps = args.steps if args.steps_given else 30
+    r = run_train(args, ws, local, steps=steps, warmup=args.warmup, plain_steps=5)
+    if rank != 0:
+        return
+    line = {"metric": r.pop("metric"), "value": r.pop("value"), "unit": r.pop("unit"),
+            "n_gpus": ws, "steps": r.pop("steps"), "warmup": r.pop("warmup"),
+            "ms_per_step": r.pop("ms_per_step"), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": r.pop("dtype"), "data": "synthetic", **r}
     print(json.dumps(line))
 
 
@@ -628,10 +727,13 @@ def main():
     ap.add_argument("--no-plain", action="store_true",
                     help="skip the plain-FP32 comparison run of a mixed form")
     ap.add_argument("--no-nep", action="store_true", help="skip the NEP workload")
+    ap.add_argument("--no-train", action="store_true", help="skip the training-step workload")
+    ap.add_argument("--train-atoms", type=int, default=NATOMS,
+                    help="atoms of the training box (32,000; smaller for profiling captures)")
     ap.add_argument("--nep-atoms", type=int, default=NEP_NATOMS,
                     help="atoms of the NEP box (the benchmark is 100,000; smaller boxes of the "
                          "same density and model are for profiling captures)")
-    ap.add_argument("--workload", default="dp", choices=["dp", "nep"],
+    ap.add_argument("--workload", default="dp", choices=["dp", "nep", "train"],
                     help="dp: the headline DP line (with a nep object); nep: the NEP line alone")
     argv = sys.argv[1:]
     args = ap.parse_args()
@@ -645,6 +747,9 @@ def main():
     ws, rank, local = dist_setup()
     if args.workload == "nep":
         run_nep_line(args, ws, rank, local)
+        return
+    if args.workload == "train":
+        run_train_line(args, ws, rank, local)
         return
     run_ours(args, ws, rank, local)
 

@@ -84,37 +84,63 @@ __device__ __forceinline__ void layer0(const T *w, T s, T sdot, T x[E], T xd[E])
     }
 }
 
-// Residual layer (E -> E): x <- tanh(x W + b) dt + x with its tangent; optionally returns the
-// tanh output t and the pre-activation tangent zd.
-template <typename T, bool KEEP>
-__device__ __forceinline__ void layer_res(const T *w, int OW, int OB, int OD, T x[E], T xd[E],
-                                          T *t_out, T *zd_out) {
-    T h[E], hd[E];
+// Pre-activations of an E -> E layer for a lane's input row x (and its tangent xd) kept in
+// shared memory: h = x W + b, hd = xd W.  The input index loop stays rolled (small code, few
+// registers); the output index is unrolled into registers.
+template <typename T>
+__device__ __forceinline__ void pre_act(const T *w, int OW, int OB, const T *x, const T *xd,
+                                        T h[E], T hd[E]) {
 #pragma unroll
     for (int o = 0; o < E; ++o) { h[o] = w[OB + o]; hd[o] = T(0); }
-#pragma unroll
+#pragma unroll 1
     for (int i = 0; i < E; ++i) {
         const T xi = x[i], xdi = xd[i];
+        const T *wr = w + OW + i * E;
 #pragma unroll
         for (int o = 0; o < E; ++o) {
-            const T wv = w[OW + i * E + o];
-            h[o] += xi * wv;
-            hd[o] += xdi * wv;
+            h[o] += xi * wr[o];
+            hd[o] += xdi * wr[o];
         }
     }
+}
+
+// acc[i] += sum_o W[i][o] z[o] and accd[i] += sum_o W[i][o] zd[o] (z, zd in shared memory).
+template <typename T>
+__device__ __forceinline__ void back_act(const T *W, const T *z, const T *zd, T acc[E],
+                                         T accd[E]) {
+#pragma unroll 1
+    for (int o = 0; o < E; ++o) {
+        const T zo = z[o], zdo = zd[o];
+#pragma unroll
+        for (int i = 0; i < E; ++i) {
+            const T wv = W[i * E + o];
+            acc[i] += wv * zo;
+            accd[i] += wv * zdo;
+        }
+    }
+}
+
+// Residual layer applied in place to a lane's shared-memory rows x, xd:
+// x <- tanh(x W + b) dt + x with its tangent.
+template <typename T>
+__device__ __forceinline__ void layer_res(const T *w, int OW, int OB, int OD, T *x, T *xd) {
+    T h[E], hd[E];
+    pre_act(w, OW, OB, x, xd, h, hd);
 #pragma unroll
     for (int o = 0; o < E; ++o) {
         const T t = dev_tanh(h[o]);
         const T dt = w[OD + o];
-        if (KEEP) { t_out[o] = t; zd_out[o] = hd[o]; }
         x[o] = t * dt + x[o];
         xd[o] = (T(1) - t * t) * hd[o] * dt + xd[o];
     }
 }
 
 // ------------------------------------------------------------------------------ dual forward
+// Per-lane shared row: G (the running activation), Gdot, then rh and rd.
+constexpr int kFwdRow = 2 * kStg + 8;
+
 template <typename T>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
 dp_dual_fwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
             const int32_t *__restrict__ type_map, const T *__restrict__ params,
             const T *__restrict__ davg, const T *__restrict__ dstd, const T *__restrict__ gF,
@@ -125,12 +151,13 @@ dp_dual_fwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
     const int warps = blockDim.x >> 5;
     T *wsm = reinterpret_cast<T *>(smem_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    T *stg = wsm + nnet * EmbOff::SIZE + warp * 32 * (2 * kStg + 8);   // G, Gdot, rh, rd
-    int *list = reinterpret_cast<int *>(wsm + nnet * EmbOff::SIZE + warps * 32 * (2 * kStg + 8)) +
+    T *stg = wsm + nnet * EmbOff::SIZE + warp * 32 * kFwdRow;
+    int *list = reinterpret_cast<int *>(wsm + nnet * EmbOff::SIZE + warps * 32 * kFwdRow) +
                 warp * S;
     for (int q = threadIdx.x; q < nnet * EmbOff::SIZE; q += blockDim.x) wsm[q] = params[q];
     __syncthreads();
     const long long total = (long long)P.batch * P.natoms;
+    T *my = stg + lane * kFwdRow;
     for (long long t = (long long)blockIdx.x * warps + warp; t < total;
          t += (long long)gridDim.x * warps) {
         const int ti = type_map[t % P.natoms];
@@ -148,7 +175,6 @@ dp_dual_fwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
         for (int c0 = 0; c0 < cnt; c0 += 32) {
             const int k = c0 + lane;
             T rh[4] = {T(0), T(0), T(0), T(0)}, rd[4] = {T(0), T(0), T(0), T(0)};
-            T x[E], xd[E];
             int tj = 0;
             if (k < cnt) {
                 const int slot = list[k];
@@ -156,19 +182,21 @@ dp_dual_fwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
                 slot_rows(idr, gF, gV, list_neigh, t, cfg0, slot, S, avg, sd, P, rh, rd);
             }
             const T *w = wsm + (ti * P.ntypes + tj) * EmbOff::SIZE;
-            layer0(w, rh[0], rd[0], x, xd);
-            layer_res<T, false>(w, EmbOff::W1, EmbOff::B1, EmbOff::DT1, x, xd, nullptr, nullptr);
-            layer_res<T, false>(w, EmbOff::W2, EmbOff::B2, EmbOff::DT2, x, xd, nullptr, nullptr);
-            if (k >= cnt) {
-#pragma unroll
-                for (int c = 0; c < 4; ++c) rh[c] = rd[c] = T(0);
-            }
             __syncwarp();
-            T *my = stg + lane * (2 * kStg + 8);
+            {
+                T x[E], xd[E];
+                layer0(w, rh[0], rd[0], x, xd);
 #pragma unroll
-            for (int p = 0; p < E; ++p) { my[p] = x[p]; my[kStg + p] = xd[p]; }
+                for (int p = 0; p < E; ++p) { my[p] = x[p]; my[kStg + p] = xd[p]; }
+            }
+            layer_res(w, EmbOff::W1, EmbOff::B1, EmbOff::DT1, my, my + kStg);
+            layer_res(w, EmbOff::W2, EmbOff::B2, EmbOff::DT2, my, my + kStg);
+            const bool valid = k < cnt;
 #pragma unroll
-            for (int c = 0; c < 4; ++c) { my[2 * kStg + c] = rh[c]; my[2 * kStg + 4 + c] = rd[c]; }
+            for (int c = 0; c < 4; ++c) {
+                my[2 * kStg + c] = valid ? rh[c] : T(0);
+                my[2 * kStg + 4 + c] = valid ? rd[c] : T(0);
+            }
             __syncwarp();
             const int nv = min(32, cnt - c0);
 #pragma unroll
@@ -178,7 +206,7 @@ dp_dual_fwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
                     const int c = e / E, p = e - c * E;
                     T s0 = a[q], s1 = ad[q];
                     for (int l = 0; l < nv; ++l) {
-                        const T *r = stg + l * (2 * kStg + 8);
+                        const T *r = stg + l * kFwdRow;
                         const T g = r[p];
                         s0 += r[2 * kStg + c] * g;
                         s1 += r[2 * kStg + 4 + c] * g + r[2 * kStg + c] * r[kStg + p];
@@ -187,7 +215,6 @@ dp_dual_fwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
                     ad[q] = s1;
                 }
             }
-            __syncwarp();
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -256,7 +283,7 @@ __device__ __forceinline__ void reduce_layer(const T *stg, int nv, int ti, int n
 }
 
 template <typename T>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
 dp_dual_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
             const int32_t *__restrict__ type_map, const T *__restrict__ params,
             const T *__restrict__ davg, const T *__restrict__ dstd, const T *__restrict__ gF,
@@ -274,6 +301,7 @@ dp_dual_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
     T *stg = stg_all + warp * 32 * Stage::ROW;
     T *ab = ab_all + warp * 2 * NA;
     int *list = list_all + warp * S;
+    T *my = stg + lane * Stage::ROW;
     for (int q = threadIdx.x; q < nnet * EmbOff::SIZE; q += blockDim.x) {
         wsm[q] = params[q];
         gacc[q] = T(0);
@@ -309,7 +337,6 @@ dp_dual_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
                 tmask[q] = q < P.ntypes ? __ballot_sync(0xffffffffu, valid && tj == q) : 0u;
             const int nv = min(32, cnt - c0);
             const T *w = wsm + (ti * P.ntypes + tj) * EmbOff::SIZE;
-            T *my = stg + lane * Stage::ROW;
             // seeds: Gbar = k (R Abar + Rdot Adbar), Gdotbar = k R Adbar (k folded into ab)
             T gb[E], gdb[E];
 #pragma unroll
@@ -323,83 +350,64 @@ dp_dual_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
                 gb[p] = valid ? s0 : T(0);
                 gdb[p] = valid ? s1 : T(0);
             }
-            // ---- layer 2: forward to its input, keep t2 and its pre-activation tangent
+            __syncwarp();
+            // ---- layer 2: recompute its input x1 (staged in X / XD), reverse through it
             {
-                T x[E], xd[E], t2[E], zd2[E];
+                T x[E], xd[E];
                 layer0(w, rh[0], rd[0], x, xd);
-                layer_res<T, false>(w, EmbOff::W1, EmbOff::B1, EmbOff::DT1, x, xd, nullptr, nullptr);
-                __syncwarp();
 #pragma unroll
                 for (int p = 0; p < E; ++p) { my[Stage::X + p] = x[p]; my[Stage::XD + p] = xd[p]; }
-                layer_res<T, true>(w, EmbOff::W2, EmbOff::B2, EmbOff::DT2, x, xd, t2, zd2);
+            }
+            layer_res(w, EmbOff::W1, EmbOff::B1, EmbOff::DT1, my + Stage::X, my + Stage::XD);
+            {
+                T h[E], hd[E];
+                pre_act(w, EmbOff::W2, EmbOff::B2, my + Stage::X, my + Stage::XD, h, hd);
 #pragma unroll
                 for (int o = 0; o < E; ++o) {
-                    const T dt = w[EmbOff::DT2 + o], g = T(1) - t2[o] * t2[o];
+                    const T t2 = dev_tanh(h[o]);
+                    const T dt = w[EmbOff::DT2 + o], g = T(1) - t2 * t2;
                     const T tb = gb[o] * dt, tdb = gdb[o] * dt;
-                    my[Stage::Q + o] = gb[o] * t2[o] + gdb[o] * g * zd2[o];
-                    my[Stage::ZB + o] = g * (tb - T(2) * t2[o] * zd2[o] * tdb);
+                    my[Stage::Q + o] = gb[o] * t2 + gdb[o] * g * hd[o];
+                    my[Stage::ZB + o] = g * (tb - T(2) * t2 * hd[o] * tdb);
                     my[Stage::ZDB + o] = g * tdb;
                 }
             }
-            __syncwarp();
             // x1bar = Gbar + W2 zb2, x1dotbar = Gdotbar + W2 zdb2
-#pragma unroll
-            for (int i = 0; i < E; ++i) {
-                T s0 = gb[i], s1 = gdb[i];
-#pragma unroll
-                for (int o = 0; o < E; ++o) {
-                    const T wv = w[EmbOff::W2 + i * E + o];
-                    s0 += wv * my[Stage::ZB + o];
-                    s1 += wv * my[Stage::ZDB + o];
-                }
-                gb[i] = s0;
-                gdb[i] = s1;
-            }
+            back_act(w + EmbOff::W2, my + Stage::ZB, my + Stage::ZDB, gb, gdb);
+            __syncwarp();
             reduce_layer(stg, nv, ti, P.ntypes, tmask, 2, gacc, lane);
             __syncwarp();
-            // ---- layer 1: recompute layer 0, keep t1 and its pre-activation tangent
-            T x0[E], xd0[E];
-            layer0(w, rh[0], rd[0], x0, xd0);
+            // ---- layer 1: recompute its input x0 (staged), reverse through it
             {
-                T x[E], xd[E], t1[E], zd1[E];
+                T x[E], xd[E];
+                layer0(w, rh[0], rd[0], x, xd);
 #pragma unroll
-                for (int p = 0; p < E; ++p) {
-                    x[p] = x0[p];
-                    xd[p] = xd0[p];
-                    my[Stage::X + p] = x0[p];
-                    my[Stage::XD + p] = xd0[p];
-                }
-                layer_res<T, true>(w, EmbOff::W1, EmbOff::B1, EmbOff::DT1, x, xd, t1, zd1);
+                for (int p = 0; p < E; ++p) { my[Stage::X + p] = x[p]; my[Stage::XD + p] = xd[p]; }
+            }
+            {
+                T h[E], hd[E];
+                pre_act(w, EmbOff::W1, EmbOff::B1, my + Stage::X, my + Stage::XD, h, hd);
 #pragma unroll
                 for (int o = 0; o < E; ++o) {
-                    const T dt = w[EmbOff::DT1 + o], g = T(1) - t1[o] * t1[o];
+                    const T t1 = dev_tanh(h[o]);
+                    const T dt = w[EmbOff::DT1 + o], g = T(1) - t1 * t1;
                     const T tb = gb[o] * dt, tdb = gdb[o] * dt;
-                    my[Stage::Q + o] = gb[o] * t1[o] + gdb[o] * g * zd1[o];
-                    my[Stage::ZB + o] = g * (tb - T(2) * t1[o] * zd1[o] * tdb);
+                    my[Stage::Q + o] = gb[o] * t1 + gdb[o] * g * hd[o];
+                    my[Stage::ZB + o] = g * (tb - T(2) * t1 * hd[o] * tdb);
                     my[Stage::ZDB + o] = g * tdb;
                 }
             }
+            back_act(w + EmbOff::W1, my + Stage::ZB, my + Stage::ZDB, gb, gdb);
             __syncwarp();
-#pragma unroll
-            for (int i = 0; i < E; ++i) {
-                T s0 = gb[i], s1 = gdb[i];
-#pragma unroll
-                for (int o = 0; o < E; ++o) {
-                    const T wv = w[EmbOff::W1 + i * E + o];
-                    s0 += wv * my[Stage::ZB + o];
-                    s1 += wv * my[Stage::ZDB + o];
-                }
-                gb[i] = s0;
-                gdb[i] = s1;
-            }
             reduce_layer(stg, nv, ti, P.ntypes, tmask, 1, gacc, lane);
             __syncwarp();
-            // ---- layer 0: x0 = tanh(s W0 + b0), x0dot = (1 - x0^2) sdot W0
+            // ---- layer 0: x0 = tanh(s W0 + b0), x0dot = (1 - x0^2) sdot W0 (x0 still staged)
 #pragma unroll
             for (int o = 0; o < E; ++o) {
-                const T g = T(1) - x0[o] * x0[o];
+                const T x0 = my[Stage::X + o];
+                const T g = T(1) - x0 * x0;
                 const T zd0 = rd[0] * w[EmbOff::W0 + o];
-                my[Stage::ZB + o] = g * (gb[o] - T(2) * x0[o] * zd0 * gdb[o]);
+                my[Stage::ZB + o] = g * (gb[o] - T(2) * x0 * zd0 * gdb[o]);
                 my[Stage::ZDB + o] = g * gdb[o];
             }
             my[5 * kStg] = rh[0];
@@ -441,9 +449,12 @@ int launch(bool backward, const matpl_dp_model *md, int batch, int natoms, int n
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long total = (long long)batch * natoms;
     if (!backward) {
-        const int warps = 4;
-        const size_t smem = wbytes + (size_t)warps * 32 * (2 * kStg + 8) * sizeof(T) +
-                            (size_t)warps * nslots * sizeof(int);
+        int warps = 8;
+        auto needf = [&](int w) {
+            return wbytes + (size_t)w * 32 * kFwdRow * sizeof(T) + (size_t)w * nslots * sizeof(int);
+        };
+        while (warps > 1 && needf(warps) > 110 * 1024) --warps;
+        const size_t smem = needf(warps);
         MATPL_REQUIRE(smem <= 220 * 1024, MATPL_ERR_UNSUPPORTED, "too many types for shared memory");
         cudaFuncSetAttribute(dp_dual_fwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         long long grid = (total + warps - 1) / warps;
@@ -454,7 +465,7 @@ int launch(bool backward, const matpl_dp_model *md, int batch, int natoms, int n
             (const T *)md->dstd, (const T *)gF, (const T *)gV, (T *)out0, (T *)out1, P);
         return check_launch("matpl_dp_dual_forward");
     }
-    int warps = 4;
+    int warps = 8;
     auto need = [&](int w) {
         return 2 * wbytes + (size_t)w * 32 * Stage::ROW * sizeof(T) +
                (size_t)w * 2 * NA * sizeof(T) + (size_t)w * nslots * sizeof(int);

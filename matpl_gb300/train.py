@@ -291,6 +291,34 @@ class FusedTrainer:
                 out = out + sel * nemp * (rp.reshape(4, 1) * G.reshape(1, _dp.E))
         return out
 
+    def _fit_dual(self, t: int, x: torch.Tensor, xd: torch.Tensor):
+        """Fitting net of element t (dp_embedding.py:140-163) on rows x and its tangent xd:
+        (E, Edot) per row.  Primal and tangent share each matrix product."""
+        model, cfg = self.model, self.model.cfg
+        nl = len(cfg.fit_sizes)
+        n = x.shape[0]
+        for l in range(nl - 1):
+            pre = f"fitting_net.{t}.layers.{l}."
+            zz = torch.cat([x, xd], 0) @ model.param(pre + "weight")
+            z, zd = zz[:n], zz[n:]
+            b = model.param(pre + "bias")
+            if b is not None:
+                z = z + b
+            h = torch.tanh(z)
+            hd = (1 - h * h) * zd
+            if l == 0:
+                x, xd = h, hd
+            else:
+                dt = model.param(pre + "resnet_dt")
+                if dt is not None:
+                    h, hd = h * dt, hd * dt
+                x, xd = h + x, hd + xd
+        pre = f"fitting_net.{t}.layers.{nl - 1}."
+        ee = torch.cat([x, xd], 0) @ model.param(pre + "weight")
+        e, ed = ee[:n], ee[n:]
+        b = model.param(pre + "bias")
+        return (e + b if b is not None else e), ed
+
     def loss_and_backward(self, batch: dict, w_f: float = 1.0, w_e: float = 1.0):
         model, cfg = self.model, self.model.cfg
         ln = batch["list_neigh"]
@@ -318,19 +346,19 @@ class FusedTrainer:
         A_occ, Ad = _EmbedDual.apply(_emb_flat(model), self, ln32, idr, tm32, gF, None)
         A = A_occ.reshape(B, N, 4, _dp.E) + self._pad_term(ln, present) / (cfg.maxNeighborNum * len(present))
         Ad = Ad.reshape(B, N, 4, _dp.E)
-        # 4. per-atom energies and their tangent
-        Ei = torch.zeros(B, N, dtype=model.dtype, device=dev)
+        # 4. per-atom energies and their tangent (explicit forward-mode through D and the
+        #    fitting net), 5. one first-order backward of Phi gives every parameter gradient
+        phi = A.new_zeros(())
         for ti in present:
             idx = torch.nonzero(self._tm_long == ti).flatten()
             if idx.numel() == 0:
                 continue
-            Ab = A[:, idx]
+            n = idx.numel()
+            Ab, Adb = A[:, idx], Ad[:, idx]
             D = Ab.transpose(-2, -1) @ Ab[..., :cfg.M2]
-            Ei = Ei.index_put((torch.arange(B, device=dev).unsqueeze(1), idx.unsqueeze(0)),
-                              model._fit(ti, D.reshape(B, idx.numel(), -1)).squeeze(-1))
-        gA = torch.autograd.grad(Ei.sum(), A, create_graph=True)[0]
-        phi = (gE.reshape(B) * Ei.sum(1)).sum() + (gA * Ad).sum()
-        # 5. parameter gradients
+            Dd = Adb.transpose(-2, -1) @ Ab[..., :cfg.M2] + Ab.transpose(-2, -1) @ Adb[..., :cfg.M2]
+            e, ed = self._fit_dual(ti, D.reshape(B * n, -1), Dd.reshape(B * n, -1))
+            phi = phi + (gE.reshape(B, 1) * e.reshape(B, n)).sum() + ed.sum()
         phi.backward()
         return float(loss.detach()), float(le.detach()), float(lf.detach())
 
