@@ -319,18 +319,33 @@ class FusedTrainer:
         b = model.param(pre + "bias")
         return (e + b if b is not None else e), ed
 
-    def loss_and_backward(self, batch: dict, w_f: float = 1.0, w_e: float = 1.0):
+    def _type_index(self, tm32: torch.Tensor, present):
+        """Atom indices of each present element (cached per type map: no host sync on reuse)."""
+        key = (self._tm_src.data_ptr(), tm32.numel(), tuple(present))
+        if getattr(self, "_tidx_key", None) != key:
+            tl = tm32.long()
+            self._tidx = {ti: torch.nonzero(tl == ti).flatten() for ti in present}
+            self._tidx_key = key
+        return self._tidx
+
+    def _loss_and_backward(self, batch: dict, w_f: float, w_e: float):
+        """Steps 1-5 with device tensors only (no host synchronisation once the type index is
+        cached): returns (loss, le, lf) as 0-d tensors and leaves the gradients in .grad."""
         model, cfg = self.model, self.model.cfg
         ln = batch["list_neigh"]
         B, N, S = ln.shape
         dev = ln.device
-        ln32 = ln.to(torch.int32).contiguous()
-        idr = batch["ImageDR"].to(model.dtype).contiguous()
-        tm32 = batch["type_map"].to(device=dev, dtype=torch.int32).contiguous()
+        ln32 = ln if ln.dtype == torch.int32 and ln.is_contiguous() else ln.to(torch.int32).contiguous()
+        idr = batch["ImageDR"]
+        idr = idr if idr.dtype == model.dtype and idr.is_contiguous() else idr.to(model.dtype).contiguous()
+        tm32 = batch["type_map"]
+        self._tm_src = tm32
+        tm32 = tm32 if tm32.dtype == torch.int32 else tm32.to(device=dev, dtype=torch.int32).contiguous()
         self._tm_long = tm32.long()
         present = [cfg.atom_type.index(int(a)) for a in batch["atom_type"]
                    if int(a) in cfg.atom_type]
         self._present = present
+        tidx = self._type_index(tm32, present)
         # 1. E, F with the current parameters
         self.evaluator.packed.copy_(_pack_device(model))
         r = self.evaluator.evaluate(ln32, tm32, present, idr, 0)
@@ -350,17 +365,21 @@ class FusedTrainer:
         #    fitting net), 5. one first-order backward of Phi gives every parameter gradient
         phi = A.new_zeros(())
         for ti in present:
-            idx = torch.nonzero(self._tm_long == ti).flatten()
-            if idx.numel() == 0:
-                continue
+            idx = tidx[ti]
             n = idx.numel()
+            if n == 0:
+                continue
             Ab, Adb = A[:, idx], Ad[:, idx]
             D = Ab.transpose(-2, -1) @ Ab[..., :cfg.M2]
             Dd = Adb.transpose(-2, -1) @ Ab[..., :cfg.M2] + Ab.transpose(-2, -1) @ Adb[..., :cfg.M2]
             e, ed = self._fit_dual(ti, D.reshape(B * n, -1), Dd.reshape(B * n, -1))
             phi = phi + (gE.reshape(B, 1) * e.reshape(B, n)).sum() + ed.sum()
         phi.backward()
-        return float(loss.detach()), float(le.detach()), float(lf.detach())
+        return loss.detach(), le.detach(), lf.detach()
+
+    def loss_and_backward(self, batch: dict, w_f: float = 1.0, w_e: float = 1.0):
+        loss, le, lf = self._loss_and_backward(batch, w_f, w_e)
+        return float(loss), float(le), float(lf)
 
     def step(self, batches, optimizer, w_f: float = 1.0, w_e: float = 1.0):
         total = 0.0
@@ -370,3 +389,48 @@ class FusedTrainer:
             optimizer.step()
             total += l
         return total
+
+
+class GraphedTrainer:
+    """The fused training step (FusedTrainer) captured once per batch shape in a CUDA graph:
+    loss, both dual kernels, the fitting part, the backward and the optimizer update replay as
+    one graph launch, so the step costs no host work beyond copying the batch into the graph's
+    static buffers.  The optimizer must keep its state on the device (torch.optim.Adam /
+    AdamW with capturable=True, or SGD).  ``step`` returns the loss as a device tensor."""
+
+    KEYS = ("list_neigh", "ImageDR", "type_map", "Etot", "Force")
+
+    def __init__(self, trainer: FusedTrainer, optimizer: torch.optim.Optimizer,
+                 w_f: float = 1.0, w_e: float = 1.0, warmup: int = 3):
+        self.tr, self.opt = trainer, optimizer
+        self.w_f, self.w_e, self.warmup = w_f, w_e, warmup
+        self.graphs = {}
+
+    def _capture(self, batch):
+        static = {k: batch[k].clone() for k in self.KEYS}
+        static["atom_type"] = list(batch["atom_type"])
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            for _ in range(self.warmup):            # allocator, workspaces, type index, attrs
+                self.opt.zero_grad(set_to_none=True)
+                self.tr._loss_and_backward(static, self.w_f, self.w_e)
+                self.opt.step()
+        torch.cuda.current_stream().wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        self.opt.zero_grad(set_to_none=True)
+        with torch.cuda.graph(g):
+            loss, le, lf = self.tr._loss_and_backward(static, self.w_f, self.w_e)
+            self.opt.step()
+        return g, static, loss
+
+    def step(self, batch):
+        key = tuple(tuple(batch[k].shape) for k in self.KEYS) + (tuple(batch["atom_type"]),)
+        if key not in self.graphs:
+            self.graphs[key] = self._capture(batch)
+        g, static, loss = self.graphs[key]
+        for k in self.KEYS:
+            if batch[k].data_ptr() != static[k].data_ptr():
+                static[k].copy_(batch[k], non_blocking=True)
+        g.replay()
+        return loss
