@@ -556,6 +556,15 @@ def run_ours(args, ws, rank, local):
         return ms, prof, clocks
 
     model, step = make_step(prec)
+    tuning = None
+    if prec.startswith("mixed"):
+        from matpl_gb300 import autotune
+        l0, r0 = ops.find_neighbore(types_d, frac_d, lat_d, 2, M_NEIGH, RC, RC,
+                                    out_dtype=model.dtype)
+        tuning = autotune.tune_dp_mixed(model, l0, tm32, present, r0)
+        tuning["table"] = [(t["group_atoms"], t["ctas_per_sm"], round(t["ms"], 4))
+                           for t in tuning["table"]]
+        del l0, r0
     acc = accuracy(model, step)
     ms, prof, clocks = timed(step, args.steps, args.warmup, True)
     value = ws * NATOMS / (ms * 1e-3)
@@ -675,6 +684,7 @@ def run_ours(args, ws, rank, local):
               "parallelism": "replicas" if ws > 1 else "single GPU",
               "l2": "no flush: per-step working set ~230 MB (neighbor list + ImageDR) exceeds the "
                     "129 MB L2",
+              "tile_tuning": tuning,
               "model_only_ms_per_step": model_ms,
               "model_only_value": ws * NATOMS / (model_ms * 1e-3), **acc}
     if plain:

@@ -186,6 +186,14 @@ int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, int natoms,
                   const int32_t *type_map, void *Ei, double *Etot, void *force, double *virial,
                   void *workspace, size_t workspace_bytes, void *stream);
 
+/* Tile shape of the MATPL_MIXED* embedding kernels, process-wide (this project's tuning
+ * hook; the reference has no tensor-core path).  mixed_group_atoms = centre atoms whose pair
+ * rows one CTA walks in 128-row tcgen05 tiles (1..16, capped by shared memory), and
+ * mixed_ctas_per_sm = resident CTAs per SM (1..3); 0 = automatic.  Results do not depend on
+ * them (same per-atom arithmetic); matpl_gb300/autotune.py picks them by timing. */
+int matpl_dp_set_tuning(int mixed_group_atoms, int mixed_ctas_per_sm);
+int matpl_dp_get_tuning(int *mixed_group_atoms, int *mixed_ctas_per_sm);
+
 /* ------------------------------------------------------------------------------------
  * Force-loss training: the embedding-net part of the second-order parameter gradient.
  * Replaces what the reference gets from torch autograd with create_graph=True through

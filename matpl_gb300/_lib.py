@@ -59,6 +59,8 @@ SIGNATURES = {
     "matpl_dp_workspace_bytes": (_sz, [_i, _i, _i]),
     "matpl_dp_eval": (_i, [_i, _c.POINTER(MatplDpModel), _i, _i, _i, _i, _vp, _vp, _vp, _vp,
                            _vp, _vp, _vp, _vp, _sz, _vp]),
+    "matpl_dp_set_tuning": (_i, [_i, _i]),
+    "matpl_dp_get_tuning": (_i, [_c.POINTER(_i), _c.POINTER(_i)]),
     "matpl_dp_dual_forward": (_i, [_i, _c.POINTER(MatplDpModel), _i, _i, _i, _vp, _vp, _vp,
                                    _vp, _vp, _vp, _vp, _vp]),
     "matpl_dp_dual_backward": (_i, [_i, _c.POINTER(MatplDpModel), _i, _i, _i, _vp, _vp, _vp,

@@ -18,6 +18,7 @@
 //     per-atom virial (FP64) per atom.
 // Every mbarrier wait is bounded; a timeout sets MATPL_KERR_TIMEOUT in err_dev.
 #include <algorithm>
+#include <atomic>
 #include "common.cuh"
 #include "dp_layout.cuh"
 #include "tc.cuh"
@@ -674,8 +675,16 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
 
 }  // namespace
 
+// Tuning of the mixed embedding kernels (matpl_dp_set_tuning): centre atoms per CTA group
+// (how many pair rows feed each 128-row MMA tile) and resident CTAs per SM; 0 = automatic.
+static std::atomic<int> g_ga_override{0}, g_ctas_override{0};
+
 // Launch helpers used by dp_fused.cu's matpl_dp_eval for the MATPL_MIXED forms.
-int mixed_ga(int S) { return std::max(1, std::min(GAMAX, 9600 / std::max(1, S))); }
+int mixed_ga(int S) {
+    const int lim = std::max(1, std::min(GAMAX, 9600 / std::max(1, S)));
+    const int o = g_ga_override.load();
+    return o > 0 ? std::min(o, lim) : lim;
+}
 
 size_t mixed_smem(int ntypes, int S) { return mix_smem_bytes(ntypes * ntypes, S, mixed_ga(S)); }
 
@@ -703,6 +712,7 @@ int launch_mixed_embed(bool backward, const int32_t *list_neigh, const float *id
     const long long total = (long long)batch * natoms;
     const long long ngroups = (total + P.ga - 1) / P.ga;
     int per_sm = (int)std::max<size_t>(1, std::min<size_t>(3, (220 * 1024) / (smem + 2048)));
+    if (g_ctas_override.load() > 0) per_sm = std::min(per_sm, g_ctas_override.load());
     const int grid = (int)std::min<long long>(ngroups, 152LL * per_sm);
     if (!backward) {
         auto k = dp_embed_fwd_tc<SPLIT, FAST>;
@@ -734,3 +744,22 @@ template int launch_mixed_embed<3, true>(
     int, int, int, int, double, double, double, cudaStream_t);
 
 }  // namespace matpl
+
+extern "C" int matpl_dp_set_tuning(int mixed_group_atoms, int mixed_ctas_per_sm) {
+    using namespace matpl;
+    MATPL_REQUIRE(mixed_group_atoms >= 0 && mixed_group_atoms <= GAMAX, MATPL_ERR_INVALID,
+                  "mixed_group_atoms must be 0 (automatic) .. 16");
+    MATPL_REQUIRE(mixed_ctas_per_sm >= 0 && mixed_ctas_per_sm <= 3, MATPL_ERR_INVALID,
+                  "mixed_ctas_per_sm must be 0 (automatic) .. 3");
+    g_ga_override.store(mixed_group_atoms);
+    g_ctas_override.store(mixed_ctas_per_sm);
+    return MATPL_OK;
+}
+
+extern "C" int matpl_dp_get_tuning(int *mixed_group_atoms, int *mixed_ctas_per_sm) {
+    using namespace matpl;
+    MATPL_REQUIRE(mixed_group_atoms && mixed_ctas_per_sm, MATPL_ERR_INVALID, "null pointer");
+    *mixed_group_atoms = g_ga_override.load();
+    *mixed_ctas_per_sm = g_ctas_override.load();
+    return MATPL_OK;
+}

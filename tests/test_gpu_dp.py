@@ -215,3 +215,23 @@ def test_mixed_forms_full_size(precision):
     else:
         assert rmse <= 0.02 * F64[0].abs().max().item(), rmse
     assert F[0].double().sum(0).abs().max().item() < 1e-2
+
+
+def test_autotuner_sets_tile_shape_without_changing_results(golden_case):
+    """The mixed kernels' tile shape (centre atoms per CTA group, CTAs per SM) is timed by the
+    autotuner, which keeps the fastest; forces are the same for every candidate."""
+    from matpl_gb300 import autotune, dp
+    c = golden_case("lisi600_f64")
+    model = dp.DP(c.cfg, c.params, c.davg, c.dstd, precision="mixed", device="cuda")
+    ln = torch.tensor(c.list_neigh, device="cuda")
+    idr = torch.tensor(c.image_dr, device="cuda", dtype=torch.float32)
+    tm = torch.tensor(c.types, device="cuda", dtype=torch.int32)
+    present = model.present_types(c.cfg.atom_type)
+    try:
+        res = autotune.tune_dp_mixed(model, ln, tm, present, idr, groups=(2, 7, 16), ctas=(1, 3),
+                                     reps=2)
+        assert len(res["table"]) == 6
+        assert autotune.get_tuning() == (res["group_atoms"], res["ctas_per_sm"])
+    finally:
+        autotune.set_tuning(0, 0)
+    assert autotune.get_tuning() == (0, 0)
