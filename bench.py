@@ -459,6 +459,77 @@ def run_train(args, ws, local, steps, warmup, plain_steps):
     }
 
 
+MD_METRIC = "batched replica MD atom-steps/s (velocity Verlet, DP mixed, one graph launch per step)"
+MD_REPLICAS, MD_NMIN, MD_NMAX, MD_SEED = 256, 64, 2048, 77
+
+
+def md_replicas(n=MD_REPLICAS, seed=MD_SEED):
+    """Cu FCC replicas (a = 3.615 A, sigma = 0.05 A) with atom counts log-uniform in
+    [64, 2048]: the count picks nx = ny = round((N/4)^(1/3)) and nz = round(N / (4 nx ny))
+    conventional cells, so the counts are 4 nx ny nz (uneven)."""
+    from matpl_gb300 import structures
+    rng = np.random.default_rng(seed)
+    out = []
+    for r in range(n):
+        N = float(np.exp(rng.uniform(np.log(MD_NMIN), np.log(MD_NMAX))))
+        nc = N / 4.0
+        nx = max(2, int(round(nc ** (1.0 / 3.0))))
+        nz = max(2, int(round(nc / (nx * nx))))
+        out.append(structures.fcc(3.615, (nx, nx, nz), 0.05, seed=seed + r))
+    return out
+
+
+def run_md(args, ws, local, steps):
+    """256 Cu replicas of uneven size, DP (1 type, m = 100, Rc 6, random weights N(0, 1/fan_in)),
+    Maxwell-Boltzmann velocities at 300 K, dt = 1 fs: `steps` velocity-Verlet steps of every
+    replica, each step one CUDA-graph launch (neighbor search + E/F/V + update per group).
+    Reports the total-energy drift per atom, FP64 energy sums."""
+    from matpl_gb300 import autotune, md, params as P, structures
+    dev = torch.device("cuda", local)
+    autotune.set_tuning(0, 0)              # the headline's tuned tile shape is for its own box
+    cfg = P.DPConfig(atom_type=[29], maxNeighborNum=100, Rmax=6.0, Rmin=0.5)
+    reps = md_replicas()
+    st = structures.fcc(3.615, (4, 4, 4), 0.05, seed=1)
+    from matpl_gb300 import ops
+    l0, r0 = ops.find_neighbore(torch.tensor(st.types, device=dev), torch.tensor(st.frac, device=dev),
+                                torch.tensor(st.lattice, device=dev), 1, 100, 6.0, 6.0)
+    davg, dstd = P.calc_stat(cfg, l0.cpu().numpy(), r0.cpu().numpy(), st.types)
+    prm = P.init_params(cfg, SEED_W)
+    sim = md.ReplicaMD(cfg, prm, davg, dstd, reps, [63.546], dt_fs=1.0, precision="mixed",
+                       device=dev)
+    sim.capture()
+    e0 = sim.energies().sum(1)
+    n = sim.natoms()
+    torch.cuda.synchronize()
+    barrier(ws)
+    e_0, e_1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_0.record()
+    chunk = max(1, steps // 10)
+    worst = 0.0
+    done = 0
+    while done < steps:
+        k = min(chunk, steps - done)
+        sim.step(k)
+        done += k
+        e = sim.energies().sum(1)           # one sync per chunk
+        worst = max(worst, float(np.max(np.abs(e - e0) / n)))
+    e_1.record()
+    torch.cuda.synchronize()
+    sim.check_errors()
+    ms = max_over_ranks(e_0.elapsed_time(e_1) / steps, ws)
+    drift = (e - e0) / n
+    return {"metric": MD_METRIC, "value": ws * sim.natoms_total / (ms * 1e-3),
+            "unit": "atom-steps/s", "ms_per_step": ms, "steps": steps,
+            "config": {"workload": f"{len(reps)} Cu FCC replicas, atom counts log-uniform in "
+                                   f"[{MD_NMIN}, {MD_NMAX}] ({int(n.min())}..{int(n.max())}, "
+                                   f"{sim.natoms_total} atoms in {len(sim.groups)} size groups), "
+                                   "DP m=100 Rc 6, 300 K, dt 1 fs, neighbor lists rebuilt every step",
+                       "natoms_total": sim.natoms_total, "size_groups": len(sim.groups),
+                       "energy_drift_per_atom_eV": {"final_mean_abs": float(np.mean(np.abs(drift))),
+                                                    "max_abs_over_run": worst},
+                       "tile_tuning": "automatic"}}
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -666,6 +737,9 @@ def run_ours(args, ws, rank, local):
     train_r = None
     if not args.no_train:
         train_r = run_train(args, ws, local, steps=20, warmup=3, plain_steps=3)
+    md_r = None
+    if not args.no_md:
+        md_r = run_md(args, ws, local, steps=200)
     nep = None
     if not args.no_nep:
         nep = run_nep(args, ws, local, steps=max(20, args.steps // 10), warmup=args.warmup,
@@ -700,7 +774,22 @@ def run_ours(args, ws, rank, local):
             "e2e": {"value": ws * NATOMS / (e2e_ms * 1e-3), "unit": "atom-steps/s",
                     "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "kernels": per_kernel, "roofline": roof,
-            "clocks": clocks, "cpu_baseline": cb, "nep": nep, "train": train_r}
+            "clocks": clocks, "cpu_baseline": cb, "nep": nep, "train": train_r, "md": md_r}
+    print(json.dumps(line))
+
+
+def run_md_line(args, ws, rank, local):
+    torch.cuda.set_device(local)
+    from matpl_gb300 import _lib
+    _lib.load()
+    steps = args.steps if args.steps_given else 1000
+    r = run_md(args, ws, local, steps)
+    if rank != 0:
+        return
+    line = {"metric": r.pop("metric"), "value": r.pop("value"), "unit": r.pop("unit"),
+            "n_gpus": ws, "steps": r.pop("steps"), "warmup": 2,
+            "ms_per_step": r.pop("ms_per_step"), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16x3 tensor / f32 / f64 sums", "data": "synthetic", **r}
     print(json.dumps(line))
 
 
@@ -749,12 +838,13 @@ def main():
                     help="skip the plain-FP32 comparison run of a mixed form")
     ap.add_argument("--no-nep", action="store_true", help="skip the NEP workload")
     ap.add_argument("--no-train", action="store_true", help="skip the training-step workload")
+    ap.add_argument("--no-md", action="store_true", help="skip the batched-replica MD workload")
     ap.add_argument("--train-atoms", type=int, default=NATOMS,
                     help="atoms of the training box (32,000; smaller for profiling captures)")
     ap.add_argument("--nep-atoms", type=int, default=NEP_NATOMS,
                     help="atoms of the NEP box (the benchmark is 100,000; smaller boxes of the "
                          "same density and model are for profiling captures)")
-    ap.add_argument("--workload", default="dp", choices=["dp", "nep", "train"],
+    ap.add_argument("--workload", default="dp", choices=["dp", "nep", "train", "md"],
                     help="dp: the headline DP line (with a nep object); nep: the NEP line alone")
     argv = sys.argv[1:]
     args = ap.parse_args()
@@ -771,6 +861,9 @@ def main():
         return
     if args.workload == "train":
         run_train_line(args, ws, rank, local)
+        return
+    if args.workload == "md":
+        run_md_line(args, ws, rank, local)
         return
     run_ours(args, ws, rank, local)
 
