@@ -628,7 +628,7 @@ def run_ours(args, ws, rank, local):
 
     model, step = make_step(prec)
     tuning = None
-    if prec.startswith("mixed"):
+    if prec.startswith("mixed") and not args.no_tune:
         from matpl_gb300 import autotune
         l0, r0 = ops.find_neighbore(types_d, frac_d, lat_d, 2, M_NEIGH, RC, RC,
                                     out_dtype=model.dtype)
@@ -839,6 +839,8 @@ def main():
     ap.add_argument("--no-nep", action="store_true", help="skip the NEP workload")
     ap.add_argument("--no-train", action="store_true", help="skip the training-step workload")
     ap.add_argument("--no-md", action="store_true", help="skip the batched-replica MD workload")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="keep the automatic tile shape of the mixed kernels (no autotuning)")
     ap.add_argument("--train-atoms", type=int, default=NATOMS,
                     help="atoms of the training box (32,000; smaller for profiling captures)")
     ap.add_argument("--nep-atoms", type=int, default=NEP_NATOMS,
