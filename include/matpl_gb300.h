@@ -304,6 +304,57 @@ int matpl_nep_descriptor(int dtype, const matpl_nep_model *model, int nframes, l
                          const double *Ri_angular, void *feats, void *workspace,
                          size_t workspace_bytes, void *stream);
 
+/* ------------------------------------------------------------------------------------
+ * LAMMPS pair style (DP).  Replaces PairMATPL::generate_neighdata
+ * (src/lmps/lammps-libtorch/MATPL/pair_matpl.cpp:522-616) and the DP branch of
+ * PairMATPL::compute (pair_matpl.cpp:893-996), which copies the expanded slot arrays to the
+ * GPU and runs the TorchScript model (src/model/dp_dp_script.py:137-185) every step.
+ *
+ * matpl_lammps_dp_neighbors: per-type DP slots from a LAMMPS full list (device pointers).
+ *   ilist [inum] local atom of each list row; the list of row ii is jflat[jstart[ii] ..
+ *   jstart[ii+1]) (jstart [inum+1] int64), atom indices into x [nall, 3] f64 and
+ *   type [nall] (LAMMPS types, 1-based); type_to_model [ntypes_lmp] = model type index of each
+ *   LAMMPS type (pair_coeff * * <elements>).  For every j of the list with
+ *   rsq = dx*dx + dy*dy + dz*dz <= rcut^2 (d = x_j - x_i, no FMA), in list order: slot
+ *   i*S + t_j*m + (count of earlier kept neighbors of type t_j) gets list_neigh = j + 1 and
+ *   image_dr = (sqrt(rsq), dx, dy, dz) in out_dtype (MATPL_F32 / MATPL_F64); other slots 0.
+ *   type_map[ii] = model type of ilist[ii].  min_rsq (device f64) = smallest kept rsq (1e300 if
+ *   none; the reference aborts when it is below 0.61).  err_dev gets
+ *   MATPL_KERR_NEIGHBOR_OVERFLOW (a block longer than m; the reference writes past it),
+ *   MATPL_KERR_BAD_TYPE or MATPL_KERR_BAD_COUNT (an index outside the atoms).
+ *   As in the reference, the row of a list is its local atom i (not ii): LAMMPS' standard
+ *   full lists have ilist[ii] = ii.
+ *
+ * matpl_lammps_dp_create / compute / destroy: the pair style's per-step force call.  create
+ *   copies the model struct (params, davg, dstd stay owned by the caller and must outlive the
+ *   handle) and sets the image types to type_to_model in LAMMPS type order (the atom_type
+ *   tensor pair_matpl.cpp:913 passes).  compute takes LAMMPS' host arrays as they are (inum ==
+ *   nlocal, ilist, numneigh and firstneigh indexed by atom, x = atom->x[0] [nall, 3],
+ *   type = atom->type) and writes f [nall, 3] (local and ghost rows, replaced, like
+ *   pair_matpl.cpp:982-987), *eng = Etot, virial[6] = xx yy zz xy xz yz (pair_matpl.cpp:989-
+ *   994), eatom [inum] (or NULL; in list-row order, or grouped by LAMMPS type like the
+ *   TorchScript model's Ei when eatom_grouped) and *min_rsq.  One host-to-device copy of
+ *   x / type / the packed list and one device-to-host copy of the results per call; blocks
+ *   until they are on the host.  A kernel error returns MATPL_ERR_INVALID with its code in
+ *   matpl_last_error().  inum == 0 writes nothing (pair_matpl.cpp:906).
+ * ---------------------------------------------------------------------------------- */
+int matpl_lammps_dp_neighbors(int inum, int nall, const int *ilist, const long long *jstart,
+                              const int *jflat, const double *x, const int *type,
+                              const int *type_to_model, int ntypes_lmp, int model_ntypes, int m,
+                              double rcut, int out_dtype, int32_t *list_neigh, void *image_dr,
+                              int32_t *type_map, double *min_rsq, int32_t *err_dev,
+                              void *stream);
+
+typedef struct matpl_lammps_dp matpl_lammps_dp;
+int matpl_lammps_dp_create(int dtype, const matpl_dp_model *model, int ntypes_lmp,
+                           const int *type_to_model, int eatom_grouped,
+                           matpl_lammps_dp **handle);
+int matpl_lammps_dp_compute(matpl_lammps_dp *handle, int nlocal, int nghost, int inum,
+                            const int *ilist, const int *numneigh, const int *const *firstneigh,
+                            const double *x, const int *type, double *f, double *eng,
+                            double *virial, double *eatom, double *min_rsq);
+void matpl_lammps_dp_destroy(matpl_lammps_dp *handle);
+
 #ifdef __cplusplus
 }
 #endif

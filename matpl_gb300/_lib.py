@@ -76,6 +76,13 @@ SIGNATURES = {
                             _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "matpl_nep_descriptor": (_i, [_i, _c.POINTER(MatplNepModel), _i, _ll, _vp, _vp, _i, _vp, _vp,
                                   _vp, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "matpl_lammps_dp_neighbors": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _i,
+                                       _vp, _vp, _vp, _vp, _vp, _vp]),
+    "matpl_lammps_dp_create": (_i, [_i, _c.POINTER(MatplDpModel), _i, _vp, _i,
+                                    _c.POINTER(_vp)]),
+    "matpl_lammps_dp_compute": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                     _vp, _vp]),
+    "matpl_lammps_dp_destroy": (None, [_vp]),
 }
 
 

@@ -1,0 +1,453 @@
+// LAMMPS pair-style support for DP models, on the GPU.
+//
+// matpl_lammps_dp_neighbors replaces PairMATPL::generate_neighdata
+// (src/lmps/lammps-libtorch/MATPL/pair_matpl.cpp:522-616), which builds on the host, every
+// step, the per-type neighbor slots the TorchScript DP forward takes, from LAMMPS' full list
+// over local and ghost atoms.  For every local atom i = ilist[ii] and every j of its list, in
+// list order: d = x_j - x_i, rsq = dx dx + dy dy + dz dz (source operation order, no FMA);
+// j is kept when rsq <= rc^2, in the block of j's model type, at the next free slot of that
+// block (so slots keep the list order).  list_neigh = j + 1 (j may be a ghost atom),
+// image_dr = (sqrt(rsq), dx, dy, dz), empty slots 0; type_map[ii] = model type of i; min_rsq =
+// the smallest kept rsq (the reference stops the run when it is below 0.61).  One warp per
+// local atom walks its list 32 entries at a time; a ballot per type gives each kept neighbor
+// its slot in list order.  A block longer than m sets MATPL_KERR_NEIGHBOR_OVERFLOW (the
+// reference writes past the block).
+//
+// The matpl_lammps_dp_* handle replaces the DP branch of PairMATPL::compute
+// (pair_matpl.cpp:893-996): per step one host-to-device copy of the positions, types and the
+// packed list, the slot kernel, the fused evaluation with ghost rows (matpl_dp_eval), a pack
+// kernel and one device-to-host copy of forces, energies and the Voigt virial.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace matpl {
+namespace {
+
+__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
+
+constexpr double kNoPair = 1e300;
+
+template <typename TO>
+__global__ void __launch_bounds__(128)
+lmp_neighbors(int inum, int nall, const int *__restrict__ ilist,
+              const long long *__restrict__ jstart, const int *__restrict__ jflat,
+              const double *__restrict__ x, const int *__restrict__ type,
+              const int *__restrict__ type_to_model, int ntypes_lmp, int nt, int m, double rc2,
+              int32_t *__restrict__ list_neigh, TO *__restrict__ image_dr,
+              int32_t *__restrict__ type_map, unsigned long long *__restrict__ min_rsq,
+              int32_t *__restrict__ err) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const long long S = (long long)nt * m;
+    const long long gw = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long ii = gw; ii < inum; ii += nw) {
+        const int i = ilist[ii];
+        if (i < 0 || i >= inum) {  // rows are indexed by i (pair_matpl.cpp:589)
+            if (lane == 0) atomicOr(err, MATPL_KERR_BAD_COUNT);
+            continue;
+        }
+        const int til = type[i] - 1;
+        const int ti = (til >= 0 && til < ntypes_lmp) ? type_to_model[til] : -1;
+        if (lane == 0) {
+            type_map[ii] = ti;
+            if (ti < 0 || ti >= nt) atomicOr(err, MATPL_KERR_BAD_TYPE);
+        }
+        const double xi = x[3 * i], yi = x[3 * i + 1], zi = x[3 * i + 2];
+        int cnt[16];
+#pragma unroll
+        for (int t = 0; t < 16; ++t) cnt[t] = 0;
+        double local_min = kNoPair;
+        const long long j0 = jstart[ii], jn = jstart[ii + 1] - j0;
+        const long long row = (long long)i * S;
+        for (long long base = 0; base < jn; base += 32) {
+            const long long jj = base + lane;
+            bool keep = false;
+            int tj = -1, j = 0;
+            double dx = 0, dy = 0, dz = 0, rsq = 0;
+            if (jj < jn) {
+                j = jflat[j0 + jj];
+                if (j >= 0 && j < nall) {
+                    const int tl = type[j] - 1;
+                    tj = (tl >= 0 && tl < ntypes_lmp) ? type_to_model[tl] : -1;
+                    dx = da(x[3 * j], -xi);
+                    dy = da(x[3 * j + 1], -yi);
+                    dz = da(x[3 * j + 2], -zi);
+                    rsq = da(da(dm(dx, dx), dm(dy, dy)), dm(dz, dz));
+                    keep = rsq <= rc2;
+                    if (keep && (tj < 0 || tj >= nt)) {
+                        atomicOr(err, MATPL_KERR_BAD_TYPE);
+                        keep = false;
+                    }
+                } else {
+                    atomicOr(err, MATPL_KERR_BAD_COUNT);
+                }
+            }
+            if (keep && rsq < local_min) local_min = rsq;
+#pragma unroll
+            for (int t = 0; t < 16; ++t) {
+                if (t >= nt) break;
+                const bool mine = keep && tj == t;
+                const unsigned mk = __ballot_sync(0xffffffffu, mine);
+                if (mine) {
+                    const int slot = cnt[t] + __popc(mk & lt);
+                    if (slot < m) {
+                        const long long s = row + (long long)t * m + slot;
+                        list_neigh[s] = j + 1;
+                        TO *o = image_dr + 4 * s;
+                        o[0] = (TO)__dsqrt_rn(rsq);
+                        o[1] = (TO)dx;
+                        o[2] = (TO)dy;
+                        o[3] = (TO)dz;
+                    }
+                }
+                cnt[t] += __popc(mk);
+            }
+        }
+        bool over = false;
+#pragma unroll
+        for (int t = 0; t < 16; ++t) {
+            if (t >= nt) break;
+            over |= cnt[t] > m;
+            for (int s = cnt[t] + lane; s < m; s += 32) {
+                const long long q = row + (long long)t * m + s;
+                list_neigh[q] = 0;
+                TO *o = image_dr + 4 * q;
+                o[0] = o[1] = o[2] = o[3] = TO(0);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double v = __shfl_xor_sync(0xffffffffu, local_min, o);
+            local_min = v < local_min ? v : local_min;
+        }
+        if (lane == 0) {
+            if (over) atomicOr(err, MATPL_KERR_NEIGHBOR_OVERFLOW);
+            // rsq >= 0, so its bit pattern orders like the value
+            if (local_min < kNoPair)
+                atomicMin(min_rsq, (unsigned long long)__double_as_longlong(local_min));
+        }
+    }
+}
+
+__global__ void lmp_init_min(unsigned long long *min_rsq) {
+    *min_rsq = (unsigned long long)__double_as_longlong(kNoPair);
+}
+
+int launch_neighbors(int inum, int nall, const int *ilist, const long long *jstart,
+                     const int *jflat, const double *x, const int *type,
+                     const int *type_to_model, int ntypes_lmp, int nt, int m, double rcut,
+                     int out_dtype, int32_t *list_neigh, void *image_dr, int32_t *type_map,
+                     double *min_rsq, int32_t *err, cudaStream_t s) {
+    ProfScope ps("lmp_neighbors", s);
+    auto *mn = reinterpret_cast<unsigned long long *>(min_rsq);
+    lmp_init_min<<<1, 1, 0, s>>>(mn);
+    if (inum > 0) {
+        long long grid = ((long long)inum + 3) / 4;
+        grid = std::min(grid, 152LL * 16);
+        const double rc2 = rcut * rcut;
+        if (out_dtype == MATPL_F64)
+            lmp_neighbors<double><<<(int)grid, 128, 0, s>>>(
+                inum, nall, ilist, jstart, jflat, x, type, type_to_model, ntypes_lmp, nt, m, rc2,
+                list_neigh, (double *)image_dr, type_map, mn, err);
+        else
+            lmp_neighbors<float><<<(int)grid, 128, 0, s>>>(
+                inum, nall, ilist, jstart, jflat, x, type, type_to_model, ntypes_lmp, nt, m, rc2,
+                list_neigh, (float *)image_dr, type_map, mn, err);
+    }
+    return check_launch("matpl_lammps_dp_neighbors");
+}
+
+// out = [force (nall x 3) | Ei (inum) | Etot, virial xx yy zz xy xz yz, min_rsq, err]
+// The Voigt pairs follow the TorchScript model's upper triangle sum_pairs Rij_a f_c
+// (src/model/dp_dp_script.py:417-426) mapped by pair_matpl.cpp:989-994; matpl_dp_eval's
+// virial[a*3+c] = sum f_a Rij_c, so xy / xz / yz are its entries 3, 6, 7.
+template <typename T>
+__global__ void lmp_pack(long long nall3, int inum, const T *__restrict__ force,
+                         const T *__restrict__ Ei, const double *__restrict__ Etot,
+                         const double *__restrict__ virial, const double *__restrict__ min_rsq,
+                         const int32_t *__restrict__ err, double *__restrict__ out) {
+    const long long n = nall3 + inum;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n + 9;
+         k += (long long)gridDim.x * blockDim.x) {
+        double v;
+        if (k < nall3) v = (double)force[k];
+        else if (k < n) v = (double)Ei[k - nall3];
+        else {
+            const int q = (int)(k - n);
+            const int voigt[6] = {0, 4, 8, 3, 6, 7};
+            v = q == 0 ? Etot[0] : q <= 6 ? virial[voigt[q - 1]] : q == 7 ? *min_rsq
+                                                                          : (double)*err;
+        }
+        out[k] = v;
+    }
+}
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    bool ensure(size_t bytes) {
+        if (bytes <= cap) return true;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        const size_t want = std::max<size_t>(align_up(bytes + bytes / 4, 256), 256);
+        if (cudaMalloc(&p, want) != cudaSuccess) return false;
+        cap = want;
+        return true;
+    }
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+};
+
+struct HostBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    bool ensure(size_t bytes) {
+        if (bytes <= cap) return true;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        const size_t want = std::max<size_t>(align_up(bytes + bytes / 4, 256), 256);
+        if (cudaHostAlloc(&p, want, cudaHostAllocDefault) != cudaSuccess) return false;
+        cap = want;
+        return true;
+    }
+    ~HostBuf() {
+        if (p) cudaFreeHost(p);
+    }
+};
+
+}  // namespace
+}  // namespace matpl
+
+using namespace matpl;
+
+struct matpl_lammps_dp {
+    int dtype = MATPL_F64;
+    matpl_dp_model model{};
+    int ntypes_lmp = 0;
+    int eatom_grouped = 0;
+    std::vector<int> t2m;
+    cudaStream_t stream = nullptr;
+    int32_t *err = nullptr;
+    int *d_t2m = nullptr;
+    DevBuf din, ln, idr, tmap, Ei, Etot, force, vir, mn, out, ws;
+    HostBuf hin, hout;
+    ~matpl_lammps_dp() {
+        if (stream) cudaStreamSynchronize(stream);
+        if (err) cudaFree(err);
+        if (d_t2m) cudaFree(d_t2m);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+extern "C" int matpl_lammps_dp_neighbors(int inum, int nall, const int *ilist,
+                                         const long long *jstart, const int *jflat,
+                                         const double *x, const int *type,
+                                         const int *type_to_model, int ntypes_lmp,
+                                         int model_ntypes, int m, double rcut, int out_dtype,
+                                         int32_t *list_neigh, void *image_dr, int32_t *type_map,
+                                         double *min_rsq, int32_t *err_dev, void *stream) {
+    MATPL_REQUIRE(inum >= 0 && nall >= inum, MATPL_ERR_INVALID, "need 0 <= inum <= nall");
+    MATPL_REQUIRE(model_ntypes >= 1 && model_ntypes <= 16 && m > 0 && ntypes_lmp >= 1,
+                  MATPL_ERR_INVALID, "model_ntypes must be 1..16, m > 0, ntypes_lmp >= 1");
+    MATPL_REQUIRE(rcut > 0, MATPL_ERR_INVALID, "rcut must be positive");
+    MATPL_REQUIRE(out_dtype == MATPL_F32 || out_dtype == MATPL_F64, MATPL_ERR_DTYPE,
+                  "image_dr is f32 or f64");
+    MATPL_REQUIRE(ilist && jstart && x && type && type_to_model && list_neigh && image_dr &&
+                      type_map && min_rsq && err_dev && (jflat || inum == 0),
+                  MATPL_ERR_INVALID, "null pointer argument");
+    return launch_neighbors(inum, nall, ilist, jstart, jflat, x, type, type_to_model,
+                            ntypes_lmp, model_ntypes, m, rcut, out_dtype, list_neigh, image_dr,
+                            type_map, min_rsq, err_dev, as_stream(stream));
+}
+
+extern "C" int matpl_lammps_dp_create(int dtype, const matpl_dp_model *model, int ntypes_lmp,
+                                      const int *type_to_model, int eatom_grouped,
+                                      matpl_lammps_dp **handle) {
+    MATPL_REQUIRE(handle, MATPL_ERR_INVALID, "handle is NULL");
+    *handle = nullptr;
+    MATPL_REQUIRE(dtype >= MATPL_F32 && dtype <= MATPL_MIXED_TANHF, MATPL_ERR_DTYPE,
+                  "unknown dtype");
+    MATPL_REQUIRE(model && model->params && model->davg && model->dstd, MATPL_ERR_INVALID,
+                  "model and its parameter pointers are required");
+    MATPL_REQUIRE(model->ntypes >= 1 && model->ntypes <= 8 && model->m > 0, MATPL_ERR_INVALID,
+                  "model ntypes must be 1..8 and m > 0");
+    MATPL_REQUIRE(ntypes_lmp >= 1 && ntypes_lmp <= model->ntypes && type_to_model,
+                  MATPL_ERR_INVALID, "need 1 <= LAMMPS types <= model types (pair_coeff)");
+    std::vector<int> t2m(type_to_model, type_to_model + ntypes_lmp);
+    for (int a = 0; a < ntypes_lmp; ++a) {
+        MATPL_REQUIRE(t2m[a] >= 0 && t2m[a] < model->ntypes, MATPL_ERR_INVALID,
+                      "type_to_model entry outside the model's types");
+        for (int b = 0; b < a; ++b)
+            MATPL_REQUIRE(t2m[a] != t2m[b], MATPL_ERR_INVALID,
+                          "two LAMMPS types map to the same model type");
+    }
+    auto *h = new matpl_lammps_dp();
+    h->dtype = dtype;
+    h->model = *model;
+    // the TorchScript model gets atom_type = the pair_coeff elements in LAMMPS type order
+    // (pair_matpl.cpp:913), so its image types are type_to_model in that order
+    h->model.npresent = ntypes_lmp;
+    for (int a = 0; a < 8; ++a) h->model.present[a] = a < ntypes_lmp ? t2m[a] : 0;
+    h->ntypes_lmp = ntypes_lmp;
+    h->eatom_grouped = eatom_grouped;
+    h->t2m = t2m;
+    bool ok = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaMalloc(&h->err, sizeof(int32_t)) == cudaSuccess &&
+              cudaMalloc(&h->d_t2m, sizeof(int) * ntypes_lmp) == cudaSuccess &&
+              cudaMemcpy(h->d_t2m, t2m.data(), sizeof(int) * ntypes_lmp,
+                         cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemset(h->err, 0, sizeof(int32_t)) == cudaSuccess;
+    if (!ok) {
+        delete h;
+        set_error("matpl_lammps_dp_create: CUDA allocation failed");
+        return MATPL_ERR_CUDA;
+    }
+    h->model.err_dev = h->err;
+    *handle = h;
+    return MATPL_OK;
+}
+
+extern "C" void matpl_lammps_dp_destroy(matpl_lammps_dp *handle) { delete handle; }
+
+extern "C" int matpl_lammps_dp_compute(matpl_lammps_dp *h, int nlocal, int nghost, int inum,
+                                       const int *ilist, const int *numneigh,
+                                       const int *const *firstneigh, const double *x,
+                                       const int *type, double *f, double *eng, double *virial,
+                                       double *eatom, double *min_rsq) {
+    MATPL_REQUIRE(h, MATPL_ERR_INVALID, "handle is NULL");
+    MATPL_REQUIRE(nlocal >= 0 && nghost >= 0 && inum == nlocal, MATPL_ERR_INVALID,
+                  "a full list over the local atoms is required (inum == nlocal)");
+    if (min_rsq) *min_rsq = kNoPair;
+    if (inum == 0) return MATPL_OK;  // pair_matpl.cpp:906: nothing is written
+    MATPL_REQUIRE(ilist && numneigh && firstneigh && x && type && f, MATPL_ERR_INVALID,
+                  "null pointer argument");
+    const int nall = nlocal + nghost;
+    const int nt = h->model.ntypes, m = h->model.m;
+    const long long S = (long long)nt * m;
+    const bool f64 = h->dtype == MATPL_F64;
+    const size_t es = f64 ? 8 : 4;
+    long long tot = 0;
+    for (int ii = 0; ii < inum; ++ii) {
+        const int i = ilist[ii];
+        MATPL_REQUIRE(i >= 0 && i < inum, MATPL_ERR_INVALID, "ilist entry outside [0, inum)");
+        MATPL_REQUIRE(numneigh[i] >= 0, MATPL_ERR_INVALID, "negative numneigh");
+        tot += numneigh[i];
+    }
+    // staged input: x | type | ilist | jstart | jflat
+    const size_t o_x = 0, o_ty = align_up(o_x + 24 * (size_t)nall, 16);
+    const size_t o_il = align_up(o_ty + 4 * (size_t)nall, 16);
+    const size_t o_js = align_up(o_il + 4 * (size_t)inum, 16);
+    const size_t o_jf = align_up(o_js + 8 * ((size_t)inum + 1), 16);
+    const size_t in_bytes = align_up(o_jf + 4 * (size_t)tot, 16);
+    const size_t out_n = 3 * (size_t)nall + inum + 9;
+    const size_t ws_bytes = matpl_dp_workspace_bytes(h->dtype, 1, inum);
+    bool ok = h->hin.ensure(in_bytes) && h->din.ensure(in_bytes) &&
+              h->hout.ensure(8 * out_n) && h->out.ensure(8 * out_n) &&
+              h->ln.ensure(4 * S * inum) && h->idr.ensure(es * 4 * S * inum) &&
+              h->tmap.ensure(4 * (size_t)inum) && h->Ei.ensure(es * inum) &&
+              h->Etot.ensure(8) && h->force.ensure(es * 3 * (size_t)nall) &&
+              h->vir.ensure(72) && h->mn.ensure(8) && h->ws.ensure(std::max<size_t>(ws_bytes, 16));
+    MATPL_REQUIRE(ok, MATPL_ERR_CUDA, "matpl_lammps_dp_compute: CUDA allocation failed");
+    char *hp = (char *)h->hin.p;
+    std::memcpy(hp + o_x, x, 24 * (size_t)nall);
+    std::memcpy(hp + o_ty, type, 4 * (size_t)nall);
+    std::memcpy(hp + o_il, ilist, 4 * (size_t)inum);
+    auto *js = (long long *)(hp + o_js);
+    auto *jf = (int *)(hp + o_jf);
+    long long off = 0;
+    for (int ii = 0; ii < inum; ++ii) {
+        const int i = ilist[ii];
+        js[ii] = off;
+        if (numneigh[i]) std::memcpy(jf + off, firstneigh[i], 4 * (size_t)numneigh[i]);
+        off += numneigh[i];
+    }
+    js[inum] = off;
+    cudaStream_t s = h->stream;
+    char *dp = (char *)h->din.p;
+    if (cudaMemcpyAsync(dp, hp, in_bytes, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+        cudaMemsetAsync(h->err, 0, sizeof(int32_t), s) != cudaSuccess) {
+        set_error("matpl_lammps_dp_compute: host-to-device copy failed");
+        return MATPL_ERR_CUDA;
+    }
+    const int out_dtype = f64 ? MATPL_F64 : MATPL_F32;
+    int rc = launch_neighbors(inum, nall, (const int *)(dp + o_il), (const long long *)(dp + o_js),
+                              (const int *)(dp + o_jf), (const double *)(dp + o_x),
+                              (const int *)(dp + o_ty), h->d_t2m, h->ntypes_lmp, nt, m,
+                              h->model.rmax, out_dtype, (int32_t *)h->ln.p, h->idr.p,
+                              (int32_t *)h->tmap.p, (double *)h->mn.p, h->err, s);
+    if (rc) return rc;
+    rc = matpl_dp_eval(h->dtype, &h->model, 1, inum, (int)S, nghost, (const int32_t *)h->ln.p,
+                       h->idr.p, (const int32_t *)h->tmap.p, h->Ei.p, (double *)h->Etot.p,
+                       h->force.p, (double *)h->vir.p, h->ws.p, h->ws.cap, s);
+    if (rc) return rc;
+    {
+        ProfScope ps("lmp_pack", s);
+        const long long n = (long long)out_n;
+        const int grid = (int)std::min<long long>((n + 255) / 256, 152LL * 8);
+        if (f64)
+            lmp_pack<double><<<grid, 256, 0, s>>>(3LL * nall, inum, (const double *)h->force.p,
+                                                  (const double *)h->Ei.p,
+                                                  (const double *)h->Etot.p,
+                                                  (const double *)h->vir.p,
+                                                  (const double *)h->mn.p, h->err,
+                                                  (double *)h->out.p);
+        else
+            lmp_pack<float><<<grid, 256, 0, s>>>(3LL * nall, inum, (const float *)h->force.p,
+                                                 (const float *)h->Ei.p, (const double *)h->Etot.p,
+                                                 (const double *)h->vir.p,
+                                                 (const double *)h->mn.p, h->err,
+                                                 (double *)h->out.p);
+        if ((rc = check_launch("matpl_lammps_dp_compute"))) return rc;
+    }
+    if (cudaMemcpyAsync(h->hout.p, h->out.p, 8 * out_n, cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+        set_error(std::string("matpl_lammps_dp_compute: ") +
+                  cudaGetErrorString(cudaGetLastError()));
+        return MATPL_ERR_CUDA;
+    }
+    const double *o = (const double *)h->hout.p;
+    const double *tail = o + 3 * (size_t)nall + inum;
+    const int kerr = (int)tail[8];
+    if (kerr) {
+        set_error("matpl_lammps_dp_compute: kernel error code " + std::to_string(kerr) +
+                  (kerr == MATPL_KERR_NEIGHBOR_OVERFLOW
+                       ? " (more neighbors of one type than maxNeighborNum)"
+                       : kerr == MATPL_KERR_BAD_TYPE ? " (atom type outside the pair_coeff map)"
+                                                     : " (list index outside the atoms)"));
+        return MATPL_ERR_INVALID;
+    }
+    // pair_matpl.cpp:982-996: forces of local and ghost atoms are set (LAMMPS' reverse
+    // communication adds the ghost rows to their owners), energy and Voigt virial
+    std::memcpy(f, o, 24 * (size_t)nall);
+    if (eng) *eng = tail[0];
+    if (virial)
+        for (int q = 0; q < 6; ++q) virial[q] = tail[1 + q];
+    if (min_rsq) *min_rsq = tail[7];
+    if (eatom) {
+        const double *Ei = o + 3 * (size_t)nall;
+        if (!h->eatom_grouped) {
+            std::memcpy(eatom, Ei, 8 * (size_t)inum);
+        } else {
+            // the TorchScript model returns Ei grouped by image type (dp_dp_script.py:296-311)
+            // and pair_matpl.cpp:1000 stores it as is
+            int k = 0;
+            for (int q = 0; q < h->ntypes_lmp; ++q)
+                for (int ii = 0; ii < inum; ++ii) {
+                    const int tl = type[ilist[ii]] - 1;
+                    if (tl == q) eatom[k++] = Ei[ii];
+                }
+            for (; k < inum; ++k) eatom[k] = 0.0;
+        }
+    }
+    return MATPL_OK;
+}

@@ -1,7 +1,8 @@
 """ORACLE build recipe (test infrastructure only).
 
-Compiles ``oracle/neighconst.c`` (DP neighbor list) and ``oracle/nepneigh.c`` (NEP neighbor
-lists) into ``oracle/_build/libmatpl_oracle.so`` with gcc.  ``-ffp-contract=off`` is required:
+Compiles ``oracle/neighconst.c`` (DP neighbor list), ``oracle/nepneigh.c`` (NEP neighbor
+lists) and ``oracle/lammps_neigh.c`` (DP slots from a LAMMPS full list) into
+``oracle/_build/libmatpl_oracle.so`` with gcc.  ``-ffp-contract=off`` is required:
 the restatements' floating-point order is the reference source order with no fused
 multiply-add, on x86_64 and aarch64 alike.
 """
@@ -14,7 +15,7 @@ LIB = os.path.join(OUT_DIR, "libmatpl_oracle.so")
 
 
 def build(force: bool = False) -> str:
-    srcs = [os.path.join(HERE, f) for f in ("neighconst.c", "nepneigh.c")]
+    srcs = [os.path.join(HERE, f) for f in ("neighconst.c", "nepneigh.c", "lammps_neigh.c")]
     os.makedirs(OUT_DIR, exist_ok=True)
     if (not force and os.path.exists(LIB)
             and os.path.getmtime(LIB) >= max(os.path.getmtime(s) for s in srcs)):
