@@ -18,7 +18,10 @@ forces and virial (what an MD step needs).  Synthetic data: no dataset is involv
 A second workload, NEP (100,000 atoms, four elements, radial / angular cutoffs 6 / 4 A), is
 measured in the same run and reported in the line's "nep" object (step = calculate_neighbor with
 exact FP64 lists + the fused FP32 energy / force / virial kernel); --workload nep prints it as
-its own line.
+its own line.  Further objects: "train" (force-loss training step), "md" (batched replica MD)
+and "lammps" (the headline box as LAMMPS hands it to pair_style matpl: local + ghost atoms and a
+full list in random order, one PairMATPL.compute per step from host arrays to host forces;
+--workload lammps prints it as its own line).
 
 --impl reference runs only the CPU implementation (oracle port) and prints its line.
 For N > 1 (torchrun) every rank runs its own replica (replicas only, weak scaling).
@@ -530,6 +533,156 @@ def run_md(args, ws, local, steps):
                        "tile_tuning": "automatic"}}
 
 
+LMP_METRIC = ("LAMMPS pair_style DP step atom-steps/s (LAMMPS host positions + full list in, "
+              "host forces / energy / virial out)")
+LMP_SKIN = 1.0      # neighbor 1.0 bin (the reference's LAMMPS demo)
+
+
+def lammps_bytes(inum, nall, entries, S, es):
+    """Unique bytes the slot conversion must move: the list (4 B per entry), ilist + jstart,
+    positions and types of every atom once, and the slot arrays it writes (list_neigh 4 B +
+    ImageDR 4 * es B per slot) + type_map."""
+    return 4 * entries + inum * (4 + 8) + nall * (24 + 4) + inum * S * (4 + 4 * es) + 4 * inum
+
+
+def cpu_baseline_lammps(s, cfg, t2m, sample):
+    """The reference's host-side per-step stage, generate_neighdata (oracle restatement in C,
+    one core, like the reference's loop), on the first `sample` list rows of the same system
+    (all of them by default); median of up to 20 runs within about 10 s."""
+    from oracle import lammps as OL
+    n = min(sample, s["nlocal"])
+    js = s["jstart"][:n + 1]
+    jf = s["jflat"][:js[-1]]
+    reps = []
+    t_end = time.perf_counter() + 10.0
+    while time.perf_counter() < t_end and len(reps) < 20:
+        t0 = time.perf_counter()
+        OL.neighdata(s["ilist"][:n], js, jf, s["x"], s["type"], t2m, cfg.ntypes,
+                     cfg.maxNeighborNum, cfg.Rmax)
+        reps.append(time.perf_counter() - t0)
+    t = statistics.median(reps)
+    return {"value": n / t, "unit": "atom-steps/s", "cores": 1, "kind": "port",
+            "sample": f"generate_neighdata (pair_matpl.cpp:522-616) restated in C, {n} list rows "
+                      f"of the same system, median of {len(reps)} runs; the reference then copies "
+                      "the slot arrays to the GPU and runs its TorchScript model, not timed here"}
+
+
+def run_lammps(args, ws, local, steps, warmup):
+    """The headline system as LAMMPS hands it to a full-list pair style: 32,000 local atoms,
+    periodic images within Rc + skin (7 A) as ghost atoms, a full list per local atom in random
+    order (a neighbor-bin build), pair_coeff * * 3 14.  One step = PairMATPL.compute on the
+    host arrays: pack + one host-to-device copy, slot conversion on the GPU, fused E/F/V with
+    ghost rows, one device-to-host copy of forces (local + ghost), energy, virial."""
+    from matpl_gb300 import _lib, dp, lammps as L, ops, params as P
+    dev = torch.device("cuda", local)
+    st, cfg, prm = make_workload(args.lammps_atoms)
+    l0, r0 = ops.find_neighbore(torch.tensor(st.types), torch.tensor(st.frac, device=dev),
+                                torch.tensor(st.lattice), cfg.ntypes, cfg.maxNeighborNum, RC, RC)
+    davg, dstd = P.calc_stat(cfg, l0.cpu().numpy(), r0.cpu().numpy(), st.types)
+    del l0, r0
+    s = L.lammps_system(st.lattice, st.cart, st.types + 1, RC + LMP_SKIN, seed=SEED_STRUCT)
+    prec = args.precision
+    model = dp.DP(cfg, prm, torch.as_tensor(davg), torch.as_tensor(dstd), precision=prec,
+                  device=dev, check_errors=False)
+    pair = L.PairMATPL(model, ELEMENTS, eatom_grouped=True, host_access="auto")
+    fn = L.firstneigh_of(s)
+    nall = s["nlocal"] + s["nghost"]
+    f = np.zeros((nall, 3))
+
+    def step(p=pair):
+        return p.compute(s["x"], s["type"], s["nlocal"], s["nghost"], s["ilist"],
+                         s["numneigh"], fn, f_out=f)
+
+    def wall(p, n, w):
+        for _ in range(w):
+            step(p)
+        torch.cuda.synchronize()
+        barrier(ws)
+        t0 = time.perf_counter()
+        for _ in range(n):
+            r = step(p)
+        return max_over_ranks((time.perf_counter() - t0) * 1e3 / n, ws), r
+
+    wall_ms, r = wall(pair, steps, warmup)
+    f_direct = r["f"].copy()
+    staged = None
+    if pair.host_access == "direct":
+        sp = L.PairMATPL(model, ELEMENTS, eatom_grouped=True, host_access="staged")
+        s_ms, s_r = wall(sp, max(5, steps // 2), 3)
+        staged = {"ms_per_step": s_ms, "value": ws * s["nlocal"] / (s_ms * 1e-3),
+                  "max_abs_force_diff_vs_direct": float(np.abs(s_r["f"] - f_direct).max())}
+        sp.close()
+        step()   # leave f from the in-place form
+    # the same steps again with per-kernel CUDA events (device-time split)
+    psteps = max(3, min(steps, 20))
+    _lib.profile_begin(max(4096, psteps * 16))
+    for _ in range(psteps):
+        step()
+    prof = _lib.profile_collect()
+    S = cfg.ntypes * cfg.maxNeighborNum
+    es = 8 if prec == "float64" else 4
+    entries = int(s["jflat"].size)
+    nbytes = lammps_bytes(s["nlocal"], nall, entries, S, es)
+    peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(HERE, "MEASURED_PEAKS.json")) else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    nb_ms, nb_n = prof.get("lmp_neighbors", (0.0, 1))
+    nb_avg = nb_ms / max(nb_n, 1)
+    achieved = nbytes / (nb_avg * 1e-3) / 1e9 if nb_avg > 0 else None
+    if pair.host_access == "direct":
+        # copies: x, type, ilist, numneigh in; the lists are read in place over NVLink-C2C
+        # and the results written in place (host bytes the GPU reads / writes per step)
+        h2d = nall * 28 + s["nlocal"] * 8 + 4 * entries + 8 * s["nlocal"]
+        d2h = 8 * (3 * nall + s["nlocal"] + 9)
+    else:
+        h2d = nall * 28 + s["nlocal"] * 12 + 8 + 4 * entries
+        d2h = 8 * (3 * nall + s["nlocal"] + 9)
+    ref_h2d = s["nlocal"] * (S * (4 + 32) + 4)   # int32 list + f64 dR + imagetype_map
+    kernels = {k: {"ms_per_step": v[0] / psteps, "launches_per_step": v[1] / psteps}
+               for k, v in prof.items()}
+    return {"metric": LMP_METRIC, "value": ws * s["nlocal"] / (wall_ms * 1e-3),
+            "unit": "atom-steps/s", "ms_per_step": wall_ms, "steps": steps, "warmup": warmup,
+            "dtype": {"float32": "f32", "float64": "f64"}.get(prec, "bf16x3 tensor / f32 / f64 sums"),
+            "config": {"workload": f"{s['nlocal']} local Li/Si atoms (the headline box) + "
+                                   f"{s['nghost']} ghost atoms, full list within Rc + {LMP_SKIN} A "
+                                   f"in random order ({entries} entries), pair_coeff * * 3 14",
+                       "precision_form": prec, "nlocal": s["nlocal"], "nghost": s["nghost"],
+                       "list_entries": entries, "host_access": pair.host_access,
+                       "staged_host_access": staged,
+                       "timing": "host wall clock around PairMATPL.compute (it returns with the "
+                                 "results on the host), max over ranks",
+                       "reference_h2d_bytes_per_step": ref_h2d},
+            "e2e": {"value": ws * s["nlocal"] / (wall_ms * 1e-3), "unit": "atom-steps/s",
+                    "ms_per_step": wall_ms, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "kernels": kernels,
+            "gpu_launches": int(sum(v[1] for v in prof.values()) / psteps * steps),
+            "roofline": {"kernel": "lmp_neighbors", "bound": "hbm", "achieved": achieved,
+                         "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak if achieved else None,
+                         "algorithmic_bytes_per_launch": nbytes, "traffic": None,
+                         "ms_per_launch": nb_avg,
+                         "peak_source": "of measured (MEASURED_PEAKS.json)" if peaks
+                         else "of fallback"},
+            "energy": r["eng"]}, s, cfg
+
+
+def run_lammps_line(args, ws, rank, local):
+    torch.cuda.set_device(local)
+    from matpl_gb300 import _lib
+    _lib.load()
+    steps = args.steps if args.steps_given else 50
+    r, s, cfg = run_lammps(args, ws, local, steps=steps, warmup=args.warmup)
+    if rank == 0 and not args.no_cpu_baseline:
+        r["cpu_baseline"] = cpu_baseline_lammps(s, cfg, [0, 1], NATOMS)
+    if rank != 0:
+        return
+    line = {"metric": r.pop("metric"), "value": r.pop("value"), "unit": r.pop("unit"),
+            "n_gpus": ws, "steps": r.pop("steps"), "warmup": r.pop("warmup"),
+            "ms_per_step": r.pop("ms_per_step"), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": r.pop("dtype"), "data": "synthetic", **r}
+    print(json.dumps(line))
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return
@@ -740,6 +893,12 @@ def run_ours(args, ws, rank, local):
     md_r = None
     if not args.no_md:
         md_r = run_md(args, ws, local, steps=200)
+    lmp_r = None
+    if not args.no_lammps:
+        lmp_r, lmp_s, lmp_cfg = run_lammps(args, ws, local, steps=30, warmup=3)
+        if rank == 0 and not args.no_cpu_baseline:
+            lmp_r["cpu_baseline"] = cpu_baseline_lammps(lmp_s, lmp_cfg, [0, 1], NATOMS)
+        del lmp_s
     nep = None
     if not args.no_nep:
         nep = run_nep(args, ws, local, steps=max(20, args.steps // 10), warmup=args.warmup,
@@ -774,7 +933,8 @@ def run_ours(args, ws, rank, local):
             "e2e": {"value": ws * NATOMS / (e2e_ms * 1e-3), "unit": "atom-steps/s",
                     "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "kernels": per_kernel, "roofline": roof,
-            "clocks": clocks, "cpu_baseline": cb, "nep": nep, "train": train_r, "md": md_r}
+            "clocks": clocks, "cpu_baseline": cb, "nep": nep, "train": train_r, "md": md_r,
+            "lammps": lmp_r}
     print(json.dumps(line))
 
 
@@ -846,7 +1006,10 @@ def main():
     ap.add_argument("--nep-atoms", type=int, default=NEP_NATOMS,
                     help="atoms of the NEP box (the benchmark is 100,000; smaller boxes of the "
                          "same density and model are for profiling captures)")
-    ap.add_argument("--workload", default="dp", choices=["dp", "nep", "train", "md"],
+    ap.add_argument("--lammps-atoms", type=int, default=NATOMS,
+                    help="local atoms of the LAMMPS pair-step box (32,000; smaller for captures)")
+    ap.add_argument("--no-lammps", action="store_true", help="skip the LAMMPS pair-step workload")
+    ap.add_argument("--workload", default="dp", choices=["dp", "nep", "train", "md", "lammps"],
                     help="dp: the headline DP line (with a nep object); nep: the NEP line alone")
     argv = sys.argv[1:]
     args = ap.parse_args()
@@ -866,6 +1029,9 @@ def main():
         return
     if args.workload == "md":
         run_md_line(args, ws, rank, local)
+        return
+    if args.workload == "lammps":
+        run_lammps_line(args, ws, rank, local)
         return
     run_ours(args, ws, rank, local)
 

@@ -333,10 +333,14 @@ int matpl_nep_descriptor(int dtype, const matpl_nep_model *model, int nframes, l
  *   type = atom->type) and writes f [nall, 3] (local and ghost rows, replaced, like
  *   pair_matpl.cpp:982-987), *eng = Etot, virial[6] = xx yy zz xy xz yz (pair_matpl.cpp:989-
  *   994), eatom [inum] (or NULL; in list-row order, or grouped by LAMMPS type like the
- *   TorchScript model's Ei when eatom_grouped) and *min_rsq.  One host-to-device copy of
- *   x / type / the packed list and one device-to-host copy of the results per call; blocks
- *   until they are on the host.  A kernel error returns MATPL_ERR_INVALID with its code in
- *   matpl_last_error().  inum == 0 writes nothing (pair_matpl.cpp:906).
+ *   TorchScript model's Ei when eatom_grouped) and *min_rsq; it returns when they are on the
+ *   host.  A kernel error returns MATPL_ERR_INVALID with its code in matpl_last_error().
+ *   inum == 0 writes nothing (pair_matpl.cpp:906).
+ *   host_access: MATPL_LMP_DIRECT = kernels read the lists in place through firstneigh and
+ *   write f in place (needs a GPU that reads pageable host memory, cudaDevAttrPageableMemory-
+ *   Access, e.g. Grace; MATPL_ERR_UNSUPPORTED otherwise); MATPL_LMP_STAGED = the host packs
+ *   x / type / lists into pinned memory, one copy each way; MATPL_LMP_AUTO = direct where
+ *   possible.  matpl_lammps_dp_host_access returns the form a handle uses.
  * ---------------------------------------------------------------------------------- */
 int matpl_lammps_dp_neighbors(int inum, int nall, const int *ilist, const long long *jstart,
                               const int *jflat, const double *x, const int *type,
@@ -345,10 +349,14 @@ int matpl_lammps_dp_neighbors(int inum, int nall, const int *ilist, const long l
                               int32_t *type_map, double *min_rsq, int32_t *err_dev,
                               void *stream);
 
+#define MATPL_LMP_AUTO 0
+#define MATPL_LMP_STAGED 1
+#define MATPL_LMP_DIRECT 2
 typedef struct matpl_lammps_dp matpl_lammps_dp;
 int matpl_lammps_dp_create(int dtype, const matpl_dp_model *model, int ntypes_lmp,
-                           const int *type_to_model, int eatom_grouped,
+                           const int *type_to_model, int eatom_grouped, int host_access,
                            matpl_lammps_dp **handle);
+int matpl_lammps_dp_host_access(const matpl_lammps_dp *handle);
 int matpl_lammps_dp_compute(matpl_lammps_dp *handle, int nlocal, int nghost, int inum,
                             const int *ilist, const int *numneigh, const int *const *firstneigh,
                             const double *x, const int *type, double *f, double *eng,

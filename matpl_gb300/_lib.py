@@ -14,6 +14,7 @@ KERR_BAD_TYPE = 2
 KERR_TIMEOUT = 3
 KERR_BAD_BOX = 4
 KERR_BAD_COUNT = 5
+LMP_AUTO, LMP_STAGED, LMP_DIRECT = 0, 1, 2
 
 _c = ctypes
 _vp, _i, _d, _sz = _c.c_void_p, _c.c_int, _c.c_double, _c.c_size_t
@@ -78,8 +79,9 @@ SIGNATURES = {
                                   _vp, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "matpl_lammps_dp_neighbors": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _i,
                                        _vp, _vp, _vp, _vp, _vp, _vp]),
-    "matpl_lammps_dp_create": (_i, [_i, _c.POINTER(MatplDpModel), _i, _vp, _i,
+    "matpl_lammps_dp_create": (_i, [_i, _c.POINTER(MatplDpModel), _i, _vp, _i, _i,
                                     _c.POINTER(_vp)]),
+    "matpl_lammps_dp_host_access": (_i, [_vp]),
     "matpl_lammps_dp_compute": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                      _vp, _vp]),
     "matpl_lammps_dp_destroy": (None, [_vp]),

@@ -14,9 +14,15 @@
 // reference writes past the block).
 //
 // The matpl_lammps_dp_* handle replaces the DP branch of PairMATPL::compute
-// (pair_matpl.cpp:893-996): per step one host-to-device copy of the positions, types and the
-// packed list, the slot kernel, the fused evaluation with ghost rows (matpl_dp_eval), a pack
-// kernel and one device-to-host copy of forces, energies and the Voigt virial.
+// (pair_matpl.cpp:893-996): slot kernel, fused evaluation with ghost rows (matpl_dp_eval) and a
+// pack kernel per step.  Two ways to reach LAMMPS' host arrays:
+//   direct  (a GPU that reads pageable host memory through the host's page tables, as on
+//           Grace): positions, types, ilist and numneigh are copied in with plain
+//           cudaMemcpyAsync from LAMMPS' own arrays, the slot kernel reads every list in place
+//           through firstneigh, and the pack kernel writes the forces straight into atom->f and
+//           the energy / virial / Ei into mapped pinned memory.  No host-side packing.
+//   staged  (elsewhere): the host packs positions, types and the list into pinned memory, one
+//           host-to-device copy, one device-to-host copy of the packed results.
 #include <algorithm>
 #include <cstring>
 #include <string>
@@ -32,13 +38,58 @@ __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b
 
 constexpr double kNoPair = 1e300;
 
-template <typename TO>
+// f64 -> f32 round-to-nearest-even in integer arithmetic (keeps the conversions off the FP64
+// pipe, which runs 2 lanes per clock per SM on this part); magnitudes below the f32 normal
+// range take the hardware conversion (never met by interatomic distances in Angstrom).
+__device__ __forceinline__ float to_f32(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned ex = (hi >> 20) & 0x7ffu;
+    const int e = (int)ex - 1023 + 127;
+    if (e <= 0 || e >= 255) return __double2float_rn(v);
+    const unsigned sign = hi & 0x80000000u;
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1fffffffu;
+    unsigned r = ((unsigned)e << 23) | m;
+    r += (rest > 0x10000000u) || (rest == 0x10000000u && (m & 1u));
+    return __uint_as_float(sign | r);
+}
+template <typename TO> __device__ __forceinline__ TO conv(double v);
+template <> __device__ __forceinline__ float conv<float>(double v) { return to_f32(v); }
+template <> __device__ __forceinline__ double conv<double>(double v) { return v; }
+
+// bit pattern of a non-negative double: orders like the value (NaN above +inf)
+__device__ __forceinline__ unsigned long long ubits(double v) {
+    return (unsigned long long)__double_as_longlong(v);
+}
+
+// the list of row ii (local atom i): packed rows (jstart / jflat, device) ...
+struct CsrLists {
+    const long long *jstart;
+    const int *jflat;
+    __device__ __forceinline__ const int *row(long long ii, int, long long &n) const {
+        const long long a = jstart[ii];
+        n = jstart[ii + 1] - a;
+        return jflat + a;
+    }
+};
+// ... or LAMMPS' own numneigh[i] / firstneigh[i] (host memory read in place)
+struct LammpsLists {
+    const int *numneigh;
+    const int *const *firstneigh;
+    __device__ __forceinline__ const int *row(long long, int i, long long &n) const {
+        n = numneigh[i];
+        return firstneigh[i];
+    }
+};
+
+template <typename TO, typename Lists>
 __global__ void __launch_bounds__(128)
-lmp_neighbors(int inum, int nall, const int *__restrict__ ilist,
-              const long long *__restrict__ jstart, const int *__restrict__ jflat,
+lmp_neighbors(int inum, int nall, const int *__restrict__ ilist, Lists lists,
               const double *__restrict__ x, const int *__restrict__ type,
-              const int *__restrict__ type_to_model, int ntypes_lmp, int nt, int m, double rc2,
-              int32_t *__restrict__ list_neigh, TO *__restrict__ image_dr,
+              const int *__restrict__ type_to_model, int ntypes_lmp, int nt, int m,
+              unsigned long long rc2_bits, int32_t *__restrict__ list_neigh,
+              TO *__restrict__ image_dr,
               int32_t *__restrict__ type_map, unsigned long long *__restrict__ min_rsq,
               int32_t *__restrict__ err) {
     const int lane = threadIdx.x & 31;
@@ -62,8 +113,9 @@ lmp_neighbors(int inum, int nall, const int *__restrict__ ilist,
         int cnt[16];
 #pragma unroll
         for (int t = 0; t < 16; ++t) cnt[t] = 0;
-        double local_min = kNoPair;
-        const long long j0 = jstart[ii], jn = jstart[ii + 1] - j0;
+        unsigned long long local_min = ubits(kNoPair);
+        long long jn;
+        const int *jl = lists.row(ii, i, jn);
         const long long row = (long long)i * S;
         for (long long base = 0; base < jn; base += 32) {
             const long long jj = base + lane;
@@ -71,7 +123,7 @@ lmp_neighbors(int inum, int nall, const int *__restrict__ ilist,
             int tj = -1, j = 0;
             double dx = 0, dy = 0, dz = 0, rsq = 0;
             if (jj < jn) {
-                j = jflat[j0 + jj];
+                j = jl[jj];
                 if (j >= 0 && j < nall) {
                     const int tl = type[j] - 1;
                     tj = (tl >= 0 && tl < ntypes_lmp) ? type_to_model[tl] : -1;
@@ -79,7 +131,7 @@ lmp_neighbors(int inum, int nall, const int *__restrict__ ilist,
                     dy = da(x[3 * j + 1], -yi);
                     dz = da(x[3 * j + 2], -zi);
                     rsq = da(da(dm(dx, dx), dm(dy, dy)), dm(dz, dz));
-                    keep = rsq <= rc2;
+                    keep = ubits(rsq) <= rc2_bits;
                     if (keep && (tj < 0 || tj >= nt)) {
                         atomicOr(err, MATPL_KERR_BAD_TYPE);
                         keep = false;
@@ -88,7 +140,7 @@ lmp_neighbors(int inum, int nall, const int *__restrict__ ilist,
                     atomicOr(err, MATPL_KERR_BAD_COUNT);
                 }
             }
-            if (keep && rsq < local_min) local_min = rsq;
+            if (keep && ubits(rsq) < local_min) local_min = ubits(rsq);
 #pragma unroll
             for (int t = 0; t < 16; ++t) {
                 if (t >= nt) break;
@@ -100,10 +152,10 @@ lmp_neighbors(int inum, int nall, const int *__restrict__ ilist,
                         const long long s = row + (long long)t * m + slot;
                         list_neigh[s] = j + 1;
                         TO *o = image_dr + 4 * s;
-                        o[0] = (TO)__dsqrt_rn(rsq);
-                        o[1] = (TO)dx;
-                        o[2] = (TO)dy;
-                        o[3] = (TO)dz;
+                        o[0] = conv<TO>(__dsqrt_rn(rsq));
+                        o[1] = conv<TO>(dx);
+                        o[2] = conv<TO>(dy);
+                        o[3] = conv<TO>(dz);
                     }
                 }
                 cnt[t] += __popc(mk);
@@ -123,14 +175,12 @@ lmp_neighbors(int inum, int nall, const int *__restrict__ ilist,
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            const double v = __shfl_xor_sync(0xffffffffu, local_min, o);
+            const unsigned long long v = __shfl_xor_sync(0xffffffffu, local_min, o);
             local_min = v < local_min ? v : local_min;
         }
         if (lane == 0) {
             if (over) atomicOr(err, MATPL_KERR_NEIGHBOR_OVERFLOW);
-            // rsq >= 0, so its bit pattern orders like the value
-            if (local_min < kNoPair)
-                atomicMin(min_rsq, (unsigned long long)__double_as_longlong(local_min));
+            if (local_min < ubits(kNoPair)) atomicMin(min_rsq, local_min);
         }
     }
 }
@@ -139,31 +189,36 @@ __global__ void lmp_init_min(unsigned long long *min_rsq) {
     *min_rsq = (unsigned long long)__double_as_longlong(kNoPair);
 }
 
-int launch_neighbors(int inum, int nall, const int *ilist, const long long *jstart,
-                     const int *jflat, const double *x, const int *type,
-                     const int *type_to_model, int ntypes_lmp, int nt, int m, double rcut,
-                     int out_dtype, int32_t *list_neigh, void *image_dr, int32_t *type_map,
-                     double *min_rsq, int32_t *err, cudaStream_t s) {
+template <typename Lists>
+int launch_neighbors(int inum, int nall, const int *ilist, Lists lists, const double *x,
+                     const int *type, const int *type_to_model, int ntypes_lmp, int nt, int m,
+                     double rcut, int out_dtype, int32_t *list_neigh, void *image_dr,
+                     int32_t *type_map, double *min_rsq, int32_t *err, cudaStream_t s) {
     ProfScope ps("lmp_neighbors", s);
     auto *mn = reinterpret_cast<unsigned long long *>(min_rsq);
     lmp_init_min<<<1, 1, 0, s>>>(mn);
     if (inum > 0) {
         long long grid = ((long long)inum + 3) / 4;
         grid = std::min(grid, 152LL * 16);
-        const double rc2 = rcut * rcut;
+        const double rc2 = rcut * rcut;   // pair_matpl.cpp:536
+        const unsigned long long rc2_bits = (unsigned long long)[&] {
+            long long b;
+            std::memcpy(&b, &rc2, 8);
+            return b;
+        }();
         if (out_dtype == MATPL_F64)
-            lmp_neighbors<double><<<(int)grid, 128, 0, s>>>(
-                inum, nall, ilist, jstart, jflat, x, type, type_to_model, ntypes_lmp, nt, m, rc2,
+            lmp_neighbors<double, Lists><<<(int)grid, 128, 0, s>>>(
+                inum, nall, ilist, lists, x, type, type_to_model, ntypes_lmp, nt, m, rc2_bits,
                 list_neigh, (double *)image_dr, type_map, mn, err);
         else
-            lmp_neighbors<float><<<(int)grid, 128, 0, s>>>(
-                inum, nall, ilist, jstart, jflat, x, type, type_to_model, ntypes_lmp, nt, m, rc2,
+            lmp_neighbors<float, Lists><<<(int)grid, 128, 0, s>>>(
+                inum, nall, ilist, lists, x, type, type_to_model, ntypes_lmp, nt, m, rc2_bits,
                 list_neigh, (float *)image_dr, type_map, mn, err);
     }
     return check_launch("matpl_lammps_dp_neighbors");
 }
 
-// out = [force (nall x 3) | Ei (inum) | Etot, virial xx yy zz xy xz yz, min_rsq, err]
+// fout [nall x 3] = forces; tail = [Ei (inum) | Etot, virial xx yy zz xy xz yz, min_rsq, err].
 // The Voigt pairs follow the TorchScript model's upper triangle sum_pairs Rij_a f_c
 // (src/model/dp_dp_script.py:417-426) mapped by pair_matpl.cpp:989-994; matpl_dp_eval's
 // virial[a*3+c] = sum f_a Rij_c, so xy / xz / yz are its entries 3, 6, 7.
@@ -171,20 +226,26 @@ template <typename T>
 __global__ void lmp_pack(long long nall3, int inum, const T *__restrict__ force,
                          const T *__restrict__ Ei, const double *__restrict__ Etot,
                          const double *__restrict__ virial, const double *__restrict__ min_rsq,
-                         const int32_t *__restrict__ err, double *__restrict__ out) {
+                         const int32_t *__restrict__ err, double *__restrict__ fout,
+                         double *__restrict__ tail) {
     const long long n = nall3 + inum;
     for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n + 9;
          k += (long long)gridDim.x * blockDim.x) {
+        if (k < nall3) {
+            fout[k] = (double)force[k];
+            continue;
+        }
+        const long long q = k - nall3;
         double v;
-        if (k < nall3) v = (double)force[k];
-        else if (k < n) v = (double)Ei[k - nall3];
-        else {
-            const int q = (int)(k - n);
+        if (q < inum) {
+            v = (double)Ei[q];
+        } else {
+            const int r = (int)(q - inum);
             const int voigt[6] = {0, 4, 8, 3, 6, 7};
-            v = q == 0 ? Etot[0] : q <= 6 ? virial[voigt[q - 1]] : q == 7 ? *min_rsq
+            v = r == 0 ? Etot[0] : r <= 6 ? virial[voigt[r - 1]] : r == 7 ? *min_rsq
                                                                           : (double)*err;
         }
-        out[k] = v;
+        tail[q] = v;
     }
 }
 
@@ -206,16 +267,22 @@ struct DevBuf {
     }
 };
 
+// pinned, mapped host memory: p for the host, dev for kernels
 struct HostBuf {
-    void *p = nullptr;
+    void *p = nullptr, *dev = nullptr;
     size_t cap = 0;
     bool ensure(size_t bytes) {
         if (bytes <= cap) return true;
         if (p) cudaFreeHost(p);
-        p = nullptr;
+        p = dev = nullptr;
         cap = 0;
         const size_t want = std::max<size_t>(align_up(bytes + bytes / 4, 256), 256);
-        if (cudaHostAlloc(&p, want, cudaHostAllocDefault) != cudaSuccess) return false;
+        if (cudaHostAlloc(&p, want, cudaHostAllocMapped) != cudaSuccess) return false;
+        if (cudaHostGetDevicePointer(&dev, p, 0) != cudaSuccess) {
+            cudaFreeHost(p);
+            p = nullptr;
+            return false;
+        }
         cap = want;
         return true;
     }
@@ -234,6 +301,7 @@ struct matpl_lammps_dp {
     matpl_dp_model model{};
     int ntypes_lmp = 0;
     int eatom_grouped = 0;
+    int host_access = MATPL_LMP_STAGED;
     std::vector<int> t2m;
     cudaStream_t stream = nullptr;
     int32_t *err = nullptr;
@@ -264,14 +332,14 @@ extern "C" int matpl_lammps_dp_neighbors(int inum, int nall, const int *ilist,
     MATPL_REQUIRE(ilist && jstart && x && type && type_to_model && list_neigh && image_dr &&
                       type_map && min_rsq && err_dev && (jflat || inum == 0),
                   MATPL_ERR_INVALID, "null pointer argument");
-    return launch_neighbors(inum, nall, ilist, jstart, jflat, x, type, type_to_model,
+    return launch_neighbors(inum, nall, ilist, CsrLists{jstart, jflat}, x, type, type_to_model,
                             ntypes_lmp, model_ntypes, m, rcut, out_dtype, list_neigh, image_dr,
                             type_map, min_rsq, err_dev, as_stream(stream));
 }
 
 extern "C" int matpl_lammps_dp_create(int dtype, const matpl_dp_model *model, int ntypes_lmp,
                                       const int *type_to_model, int eatom_grouped,
-                                      matpl_lammps_dp **handle) {
+                                      int host_access, matpl_lammps_dp **handle) {
     MATPL_REQUIRE(handle, MATPL_ERR_INVALID, "handle is NULL");
     *handle = nullptr;
     MATPL_REQUIRE(dtype >= MATPL_F32 && dtype <= MATPL_MIXED_TANHF, MATPL_ERR_DTYPE,
@@ -282,6 +350,8 @@ extern "C" int matpl_lammps_dp_create(int dtype, const matpl_dp_model *model, in
                   "model ntypes must be 1..8 and m > 0");
     MATPL_REQUIRE(ntypes_lmp >= 1 && ntypes_lmp <= model->ntypes && type_to_model,
                   MATPL_ERR_INVALID, "need 1 <= LAMMPS types <= model types (pair_coeff)");
+    MATPL_REQUIRE(host_access >= MATPL_LMP_AUTO && host_access <= MATPL_LMP_DIRECT,
+                  MATPL_ERR_INVALID, "host_access is MATPL_LMP_AUTO, _STAGED or _DIRECT");
     std::vector<int> t2m(type_to_model, type_to_model + ntypes_lmp);
     for (int a = 0; a < ntypes_lmp; ++a) {
         MATPL_REQUIRE(t2m[a] >= 0 && t2m[a] < model->ntypes, MATPL_ERR_INVALID,
@@ -290,6 +360,14 @@ extern "C" int matpl_lammps_dp_create(int dtype, const matpl_dp_model *model, in
             MATPL_REQUIRE(t2m[a] != t2m[b], MATPL_ERR_INVALID,
                           "two LAMMPS types map to the same model type");
     }
+    int dev = 0, pageable = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+        set_error("matpl_lammps_dp_create: no CUDA device");
+        return MATPL_ERR_CUDA;
+    }
+    MATPL_REQUIRE(host_access != MATPL_LMP_DIRECT || pageable, MATPL_ERR_UNSUPPORTED,
+                  "this GPU cannot read pageable host memory (MATPL_LMP_DIRECT)");
     auto *h = new matpl_lammps_dp();
     h->dtype = dtype;
     h->model = *model;
@@ -299,6 +377,10 @@ extern "C" int matpl_lammps_dp_create(int dtype, const matpl_dp_model *model, in
     for (int a = 0; a < 8; ++a) h->model.present[a] = a < ntypes_lmp ? t2m[a] : 0;
     h->ntypes_lmp = ntypes_lmp;
     h->eatom_grouped = eatom_grouped;
+    h->host_access = (host_access == MATPL_LMP_DIRECT ||
+                      (host_access == MATPL_LMP_AUTO && pageable))
+                         ? MATPL_LMP_DIRECT
+                         : MATPL_LMP_STAGED;
     h->t2m = t2m;
     bool ok = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) == cudaSuccess &&
               cudaMalloc(&h->err, sizeof(int32_t)) == cudaSuccess &&
@@ -316,6 +398,10 @@ extern "C" int matpl_lammps_dp_create(int dtype, const matpl_dp_model *model, in
     return MATPL_OK;
 }
 
+extern "C" int matpl_lammps_dp_host_access(const matpl_lammps_dp *handle) {
+    return handle ? handle->host_access : -1;
+}
+
 extern "C" void matpl_lammps_dp_destroy(matpl_lammps_dp *handle) { delete handle; }
 
 extern "C" int matpl_lammps_dp_compute(matpl_lammps_dp *h, int nlocal, int nghost, int inum,
@@ -330,6 +416,7 @@ extern "C" int matpl_lammps_dp_compute(matpl_lammps_dp *h, int nlocal, int nghos
     if (inum == 0) return MATPL_OK;  // pair_matpl.cpp:906: nothing is written
     MATPL_REQUIRE(ilist && numneigh && firstneigh && x && type && f, MATPL_ERR_INVALID,
                   "null pointer argument");
+    const bool direct = h->host_access == MATPL_LMP_DIRECT;
     const int nall = nlocal + nghost;
     const int nt = h->model.ntypes, m = h->model.m;
     const long long S = (long long)nt * m;
@@ -342,53 +429,80 @@ extern "C" int matpl_lammps_dp_compute(matpl_lammps_dp *h, int nlocal, int nghos
         MATPL_REQUIRE(numneigh[i] >= 0, MATPL_ERR_INVALID, "negative numneigh");
         tot += numneigh[i];
     }
-    // staged input: x | type | ilist | jstart | jflat
+    // device input: x | type | ilist | (staged: jstart | jflat, direct: numneigh)
     const size_t o_x = 0, o_ty = align_up(o_x + 24 * (size_t)nall, 16);
     const size_t o_il = align_up(o_ty + 4 * (size_t)nall, 16);
     const size_t o_js = align_up(o_il + 4 * (size_t)inum, 16);
     const size_t o_jf = align_up(o_js + 8 * ((size_t)inum + 1), 16);
-    const size_t in_bytes = align_up(o_jf + 4 * (size_t)tot, 16);
-    const size_t out_n = 3 * (size_t)nall + inum + 9;
+    const size_t in_bytes = direct ? align_up(o_js + 4 * (size_t)inum, 16)
+                                   : align_up(o_jf + 4 * (size_t)tot, 16);
+    const size_t tail_n = (size_t)inum + 9;
+    const size_t out_n = 3 * (size_t)nall + tail_n;
     const size_t ws_bytes = matpl_dp_workspace_bytes(h->dtype, 1, inum);
-    bool ok = h->hin.ensure(in_bytes) && h->din.ensure(in_bytes) &&
-              h->hout.ensure(8 * out_n) && h->out.ensure(8 * out_n) &&
+    bool ok = h->din.ensure(in_bytes) && h->hout.ensure(8 * out_n) &&
+              (direct || (h->hin.ensure(in_bytes) && h->out.ensure(8 * out_n))) &&
               h->ln.ensure(4 * S * inum) && h->idr.ensure(es * 4 * S * inum) &&
               h->tmap.ensure(4 * (size_t)inum) && h->Ei.ensure(es * inum) &&
               h->Etot.ensure(8) && h->force.ensure(es * 3 * (size_t)nall) &&
               h->vir.ensure(72) && h->mn.ensure(8) && h->ws.ensure(std::max<size_t>(ws_bytes, 16));
     MATPL_REQUIRE(ok, MATPL_ERR_CUDA, "matpl_lammps_dp_compute: CUDA allocation failed");
-    char *hp = (char *)h->hin.p;
-    std::memcpy(hp + o_x, x, 24 * (size_t)nall);
-    std::memcpy(hp + o_ty, type, 4 * (size_t)nall);
-    std::memcpy(hp + o_il, ilist, 4 * (size_t)inum);
-    auto *js = (long long *)(hp + o_js);
-    auto *jf = (int *)(hp + o_jf);
-    long long off = 0;
-    for (int ii = 0; ii < inum; ++ii) {
-        const int i = ilist[ii];
-        js[ii] = off;
-        if (numneigh[i]) std::memcpy(jf + off, firstneigh[i], 4 * (size_t)numneigh[i]);
-        off += numneigh[i];
-    }
-    js[inum] = off;
     cudaStream_t s = h->stream;
     char *dp = (char *)h->din.p;
-    if (cudaMemcpyAsync(dp, hp, in_bytes, cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaMemsetAsync(h->err, 0, sizeof(int32_t), s) != cudaSuccess) {
-        set_error("matpl_lammps_dp_compute: host-to-device copy failed");
-        return MATPL_ERR_CUDA;
-    }
     const int out_dtype = f64 ? MATPL_F64 : MATPL_F32;
-    int rc = launch_neighbors(inum, nall, (const int *)(dp + o_il), (const long long *)(dp + o_js),
-                              (const int *)(dp + o_jf), (const double *)(dp + o_x),
-                              (const int *)(dp + o_ty), h->d_t2m, h->ntypes_lmp, nt, m,
-                              h->model.rmax, out_dtype, (int32_t *)h->ln.p, h->idr.p,
-                              (int32_t *)h->tmap.p, (double *)h->mn.p, h->err, s);
+    int rc;
+    if (direct) {
+        // LAMMPS' arrays as they are: positions / types / ilist / numneigh copied in, the lists
+        // read in place through firstneigh
+        bool c = cudaMemcpyAsync(dp + o_x, x, 24 * (size_t)nall, cudaMemcpyHostToDevice, s) ==
+                     cudaSuccess &&
+                 cudaMemcpyAsync(dp + o_ty, type, 4 * (size_t)nall, cudaMemcpyHostToDevice, s) ==
+                     cudaSuccess &&
+                 cudaMemcpyAsync(dp + o_il, ilist, 4 * (size_t)inum, cudaMemcpyHostToDevice, s) ==
+                     cudaSuccess &&
+                 cudaMemcpyAsync(dp + o_js, numneigh, 4 * (size_t)inum, cudaMemcpyHostToDevice,
+                                 s) == cudaSuccess &&
+                 cudaMemsetAsync(h->err, 0, sizeof(int32_t), s) == cudaSuccess;
+        MATPL_REQUIRE(c, MATPL_ERR_CUDA, "matpl_lammps_dp_compute: host-to-device copy failed");
+        rc = launch_neighbors(inum, nall, (const int *)(dp + o_il),
+                              LammpsLists{(const int *)(dp + o_js), firstneigh},
+                              (const double *)(dp + o_x), (const int *)(dp + o_ty), h->d_t2m,
+                              h->ntypes_lmp, nt, m, h->model.rmax, out_dtype, (int32_t *)h->ln.p,
+                              h->idr.p, (int32_t *)h->tmap.p, (double *)h->mn.p, h->err, s);
+    } else {
+        char *hp = (char *)h->hin.p;
+        std::memcpy(hp + o_x, x, 24 * (size_t)nall);
+        std::memcpy(hp + o_ty, type, 4 * (size_t)nall);
+        std::memcpy(hp + o_il, ilist, 4 * (size_t)inum);
+        auto *js = (long long *)(hp + o_js);
+        auto *jf = (int *)(hp + o_jf);
+        long long off = 0;
+        for (int ii = 0; ii < inum; ++ii) {
+            const int i = ilist[ii];
+            js[ii] = off;
+            if (numneigh[i]) std::memcpy(jf + off, firstneigh[i], 4 * (size_t)numneigh[i]);
+            off += numneigh[i];
+        }
+        js[inum] = off;
+        if (cudaMemcpyAsync(dp, hp, in_bytes, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemsetAsync(h->err, 0, sizeof(int32_t), s) != cudaSuccess) {
+            set_error("matpl_lammps_dp_compute: host-to-device copy failed");
+            return MATPL_ERR_CUDA;
+        }
+        rc = launch_neighbors(inum, nall, (const int *)(dp + o_il),
+                              CsrLists{(const long long *)(dp + o_js), (const int *)(dp + o_jf)},
+                              (const double *)(dp + o_x), (const int *)(dp + o_ty), h->d_t2m,
+                              h->ntypes_lmp, nt, m, h->model.rmax, out_dtype, (int32_t *)h->ln.p,
+                              h->idr.p, (int32_t *)h->tmap.p, (double *)h->mn.p, h->err, s);
+    }
     if (rc) return rc;
     rc = matpl_dp_eval(h->dtype, &h->model, 1, inum, (int)S, nghost, (const int32_t *)h->ln.p,
                        h->idr.p, (const int32_t *)h->tmap.p, h->Ei.p, (double *)h->Etot.p,
                        h->force.p, (double *)h->vir.p, h->ws.p, h->ws.cap, s);
     if (rc) return rc;
+    // direct: forces straight into f, the rest into mapped pinned memory; staged: all into
+    // one device buffer, copied back below
+    double *fout = direct ? f : (double *)h->out.p;
+    double *tdev = direct ? (double *)h->hout.dev : (double *)h->out.p + 3 * (size_t)nall;
     {
         ProfScope ps("lmp_pack", s);
         const long long n = (long long)out_n;
@@ -398,25 +512,24 @@ extern "C" int matpl_lammps_dp_compute(matpl_lammps_dp *h, int nlocal, int nghos
                                                   (const double *)h->Ei.p,
                                                   (const double *)h->Etot.p,
                                                   (const double *)h->vir.p,
-                                                  (const double *)h->mn.p, h->err,
-                                                  (double *)h->out.p);
+                                                  (const double *)h->mn.p, h->err, fout, tdev);
         else
             lmp_pack<float><<<grid, 256, 0, s>>>(3LL * nall, inum, (const float *)h->force.p,
                                                  (const float *)h->Ei.p, (const double *)h->Etot.p,
                                                  (const double *)h->vir.p,
-                                                 (const double *)h->mn.p, h->err,
-                                                 (double *)h->out.p);
+                                                 (const double *)h->mn.p, h->err, fout, tdev);
         if ((rc = check_launch("matpl_lammps_dp_compute"))) return rc;
     }
-    if (cudaMemcpyAsync(h->hout.p, h->out.p, 8 * out_n, cudaMemcpyDeviceToHost, s) !=
-            cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess) {
+    bool c = direct || cudaMemcpyAsync(h->hout.p, h->out.p, 8 * out_n, cudaMemcpyDeviceToHost,
+                                       s) == cudaSuccess;
+    if (!c || cudaStreamSynchronize(s) != cudaSuccess) {
         set_error(std::string("matpl_lammps_dp_compute: ") +
                   cudaGetErrorString(cudaGetLastError()));
         return MATPL_ERR_CUDA;
     }
     const double *o = (const double *)h->hout.p;
-    const double *tail = o + 3 * (size_t)nall + inum;
+    const double *t = direct ? o : o + 3 * (size_t)nall;
+    const double *tail = t + inum;
     const int kerr = (int)tail[8];
     if (kerr) {
         set_error("matpl_lammps_dp_compute: kernel error code " + std::to_string(kerr) +
@@ -428,13 +541,13 @@ extern "C" int matpl_lammps_dp_compute(matpl_lammps_dp *h, int nlocal, int nghos
     }
     // pair_matpl.cpp:982-996: forces of local and ghost atoms are set (LAMMPS' reverse
     // communication adds the ghost rows to their owners), energy and Voigt virial
-    std::memcpy(f, o, 24 * (size_t)nall);
+    if (!direct) std::memcpy(f, o, 24 * (size_t)nall);
     if (eng) *eng = tail[0];
     if (virial)
         for (int q = 0; q < 6; ++q) virial[q] = tail[1 + q];
     if (min_rsq) *min_rsq = tail[7];
     if (eatom) {
-        const double *Ei = o + 3 * (size_t)nall;
+        const double *Ei = t;
         if (!h->eatom_grouped) {
             std::memcpy(eatom, Ei, 8 * (size_t)inum);
         } else {

@@ -35,9 +35,12 @@ class PairMATPL:
     """``pair_style matpl model.pt`` + ``pair_coeff * * <Z of each LAMMPS type>`` for one DP
     model.  ``eatom_grouped`` keeps the per-atom energies in the TorchScript model's order
     (grouped by LAMMPS type, what the reference stores in ``eatom``); False gives list-row
-    order."""
+    order.  ``host_access``: "auto" | "direct" (the GPU reads the lists and writes the forces in
+    place in host memory; a GPU with pageable host memory access, e.g. on Grace) | "staged"
+    (pinned copies)."""
 
-    def __init__(self, model: DP, pair_coeff: Sequence[int], eatom_grouped: bool = True):
+    def __init__(self, model: DP, pair_coeff: Sequence[int], eatom_grouped: bool = True,
+                 host_access: str = "auto"):
         at = list(model.cfg.atom_type)
         for z in pair_coeff:
             if z not in at:   # pair_matpl.cpp:296-299
@@ -49,12 +52,18 @@ class PairMATPL:
         t2m = (ctypes.c_int * self.ntypes_lmp)(*self.type_to_model)
         present = list(range(model.cfg.ntypes))
         self._mstruct = model._model_struct(present)
+        modes = {"auto": _lib.LMP_AUTO, "staged": _lib.LMP_STAGED, "direct": _lib.LMP_DIRECT}
+        if host_access not in modes:
+            raise _lib.MatplError(f"host_access is one of {list(modes)}")
         h = ctypes.c_void_p()
-        check(_lib.load().matpl_lammps_dp_create(model.code, ctypes.byref(self._mstruct),
-                                                 self.ntypes_lmp, ctypes.cast(t2m, ctypes.c_void_p),
-                                                 int(eatom_grouped), ctypes.byref(h)),
+        lib = _lib.load()
+        check(lib.matpl_lammps_dp_create(model.code, ctypes.byref(self._mstruct), self.ntypes_lmp,
+                                         ctypes.cast(t2m, ctypes.c_void_p), int(eatom_grouped),
+                                         modes[host_access], ctypes.byref(h)),
               "matpl_lammps_dp_create")
         self._h = h
+        self.host_access = {_lib.LMP_STAGED: "staged", _lib.LMP_DIRECT: "direct"}[
+            lib.matpl_lammps_dp_host_access(h)]
         self._f = None
 
     def close(self):

@@ -2,6 +2,8 @@
 against the oracle restatement of generate_neighdata, and the pair driver
 (matpl_lammps_dp_compute) against MatPL's shipped TorchScript model on a LAMMPS-like layout,
 against the oracle pair step, and (ghost forces folded) against the periodic path."""
+import platform
+
 import numpy as np
 import pytest
 import torch
@@ -94,9 +96,12 @@ def test_slots_overflow_empty_and_bad_index():
     assert int(r["err"][0]) == _lib.KERR_BAD_COUNT
 
 
-def pair_of(cfg, params, davg, dstd, precision, pair_coeff, grouped=True):
+ACCESS = ["staged", "direct"]
+
+
+def pair_of(cfg, params, davg, dstd, precision, pair_coeff, grouped=True, access="staged"):
     model = dp.DP(cfg, params, davg, dstd, precision=precision, device=DEV)
-    return PairMATPL(model, pair_coeff, eatom_grouped=grouped)
+    return PairMATPL(model, pair_coeff, eatom_grouped=grouped, host_access=access)
 
 
 def run_pair(pair, s, eflag_atom=True):
@@ -104,12 +109,15 @@ def run_pair(pair, s, eflag_atom=True):
                         firstneigh_of(s), eflag_atom=eflag_atom)
 
 
-def test_pair_matches_torchscript_model(lmp):
+@pytest.mark.parametrize("access", ACCESS)
+def test_pair_matches_torchscript_model(lmp, access):
     """pair_coeff * * 72 8 on the demo HfO2 cell: forces on local and ghost rows, energy,
-    Voigt virial and type-grouped per-atom energies = jit_dp.pt's (FP64)."""
+    Voigt virial and type-grouped per-atom energies = jit_dp.pt's (FP64); both ways of reaching
+    LAMMPS' host arrays."""
     g, cfg, base, s = lmp
     pair = pair_of(cfg, base.params, base.davg, base.dstd, "float64",
-                   [int(z) for z in g["pair_coeff"]])
+                   [int(z) for z in g["pair_coeff"]], access=access)
+    assert pair.host_access == access
     r = run_pair(pair, s)
     fs = np.abs(g["Force"]).max()
     np.testing.assert_allclose(r["f"], g["Force"][0], rtol=0, atol=1e-10 * fs)
@@ -127,9 +135,23 @@ def test_pair_matches_torchscript_model(lmp):
     pair.close()
 
 
+def test_auto_host_access_is_direct_on_grace():
+    """On a GPU that reads pageable host memory through the host's page tables the automatic
+    choice is the in-place form."""
+    cfg = P.DPConfig(atom_type=[29], maxNeighborNum=100)
+    st = structures.fcc(3.615, (3, 3, 3), 0.05, seed=1)
+    davg, dstd = stats(cfg, st)
+    pair = pair_of(cfg, P.init_params(cfg, 1), davg, dstd, "float64", [29], access="auto")
+    assert pair.host_access in ("direct", "staged")
+    if platform.machine() == "aarch64":
+        assert pair.host_access == "direct"
+    pair.close()
+
+
 @pytest.mark.parametrize("precision,tol", [("float64", 1e-10), ("float32", 2e-5),
                                            ("mixed", 2e-5)])
-def test_pair_matches_oracle_two_types(precision, tol):
+@pytest.mark.parametrize("access", ACCESS)
+def test_pair_matches_oracle_two_types(precision, tol, access):
     st, s = mixed_system(600, seed=21)
     cfg = P.DPConfig(atom_type=[3, 14], maxNeighborNum=150)
     params = P.init_params(cfg, 201)
@@ -143,7 +165,7 @@ def test_pair_matches_oracle_two_types(precision, tol):
         ref = OL.pair_compute(cfg, params, davg, dstd, t2m, sk["nlocal"], sk["nghost"],
                               sk["ilist"], sk["jstart"], sk["jflat"], sk["x"], sk["type"])
         for grouped in (True, False):
-            pair = pair_of(cfg, params, davg, dstd, precision, pc, grouped)
+            pair = pair_of(cfg, params, davg, dstd, precision, pc, grouped, access)
             r = run_pair(pair, sk)
             fs = np.abs(ref["f"]).max()
             np.testing.assert_allclose(r["f"], ref["f"], rtol=0, atol=tol * fs * 10)
@@ -156,7 +178,8 @@ def test_pair_matches_oracle_two_types(precision, tol):
             pair.close()
 
 
-def test_pair_ghosts_fold_to_periodic_path():
+@pytest.mark.parametrize("access", ACCESS)
+def test_pair_ghosts_fold_to_periodic_path(access):
     """Cu, 4000 atoms: ghost forces folded onto their owners = the periodic matpl path."""
     st = structures.fcc(3.615, (10, 10, 10), 0.05, seed=4)
     cfg = P.DPConfig(atom_type=[29], maxNeighborNum=100)
@@ -164,7 +187,7 @@ def test_pair_ghosts_fold_to_periodic_path():
     davg, dstd = stats(cfg, st)
     s = lammps_system(st.lattice, st.cart, st.types + 1, 7.0, seed=4)
     model = dp.DP(cfg, params, davg, dstd, precision="float64", device=DEV)
-    pair = PairMATPL(model, [29])
+    pair = PairMATPL(model, [29], host_access=access)
     r = run_pair(pair, s)
     n = s["nlocal"]
     lat = torch.tensor(st.lattice[None], device=DEV)
@@ -182,13 +205,14 @@ def test_pair_ghosts_fold_to_periodic_path():
     pair.close()
 
 
-def test_pair_too_close_and_sizes_change():
+@pytest.mark.parametrize("access", ACCESS)
+def test_pair_too_close_and_sizes_change(access):
     st, s = mixed_system(600, seed=9)
     cfg = P.DPConfig(atom_type=[3, 14], maxNeighborNum=150)
     params = P.init_params(cfg, 7)
     davg, dstd = stats(cfg, st)
     s["numneigh"] = np.diff(s["jstart"]).astype(np.int32)
-    pair = pair_of(cfg, params, davg, dstd, "float64", [3, 14])
+    pair = pair_of(cfg, params, davg, dstd, "float64", [3, 14], access=access)
     r_big = run_pair(pair, s)
     st2, s2 = mixed_system(100, seed=10)
     s2["numneigh"] = np.diff(s2["jstart"]).astype(np.int32)

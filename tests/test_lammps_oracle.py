@@ -113,14 +113,14 @@ def test_capi_lammps_argument_checks():
     h = ctypes.c_void_p()
     t2m = (ctypes.c_int * 2)(1, 1)
     # no parameter pointers
-    assert lib.matpl_lammps_dp_create(1, ctypes.byref(m), 2, ctypes.cast(t2m, ctypes.c_void_p), 1,
-                                      ctypes.byref(h)) == 1
+    t2m_p = ctypes.cast(t2m, ctypes.c_void_p)
+    assert lib.matpl_lammps_dp_create(1, ctypes.byref(m), 2, t2m_p, 1, 0, ctypes.byref(h)) == 1
     m.params = m.davg = m.dstd = 16
-    st = lib.matpl_lammps_dp_create(1, ctypes.byref(m), 2, ctypes.cast(t2m, ctypes.c_void_p), 1,
-                                    ctypes.byref(h))
+    st = lib.matpl_lammps_dp_create(1, ctypes.byref(m), 2, t2m_p, 1, 0, ctypes.byref(h))
     assert st == 1 and b"same model type" in lib.matpl_last_error()
-    assert lib.matpl_lammps_dp_create(9, ctypes.byref(m), 2, ctypes.cast(t2m, ctypes.c_void_p), 1,
-                                      ctypes.byref(h)) == 2
+    assert lib.matpl_lammps_dp_create(9, ctypes.byref(m), 2, t2m_p, 1, 0, ctypes.byref(h)) == 2
+    assert lib.matpl_lammps_dp_create(1, ctypes.byref(m), 2, t2m_p, 1, 7, ctypes.byref(h)) == 1
+    assert lib.matpl_lammps_dp_host_access(None) == -1
     assert lib.matpl_lammps_dp_compute(None, 1, 0, 1, *([None] * 10)) == 1
     assert lib.matpl_lammps_dp_neighbors(1, 1, *([None] * 6), 1, 2, 100, 6.0, 1,
                                          *([None] * 6)) == 1
