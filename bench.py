@@ -579,11 +579,18 @@ def run_lammps(args, ws, local, steps, warmup):
     l0, r0 = ops.find_neighbore(torch.tensor(st.types), torch.tensor(st.frac, device=dev),
                                 torch.tensor(st.lattice), cfg.ntypes, cfg.maxNeighborNum, RC, RC)
     davg, dstd = P.calc_stat(cfg, l0.cpu().numpy(), r0.cpu().numpy(), st.types)
-    del l0, r0
     s = L.lammps_system(st.lattice, st.cart, st.types + 1, RC + LMP_SKIN, seed=SEED_STRUCT)
     prec = args.precision
     model = dp.DP(cfg, prm, torch.as_tensor(davg), torch.as_tensor(dstd), precision=prec,
                   device=dev, check_errors=False)
+    tuning = "automatic"
+    if prec.startswith("mixed") and not args.no_tune:
+        # tile shape of the mixed kernels, timed on this machine's own slot occupancy
+        from matpl_gb300 import autotune
+        tm0 = torch.tensor(st.types, dtype=torch.int32, device=dev)
+        t = autotune.tune_dp_mixed(model, l0, tm0, [0, 1], r0.to(model.dtype))
+        tuning = {"group_atoms": t["group_atoms"], "ctas_per_sm": t["ctas_per_sm"]}
+    del l0, r0
     pair = L.PairMATPL(model, ELEMENTS, eatom_grouped=True, host_access="auto")
     fn = L.firstneigh_of(s)
     nall = s["nlocal"] + s["nghost"]
@@ -648,6 +655,7 @@ def run_lammps(args, ws, local, steps, warmup):
                                    f"in random order ({entries} entries), pair_coeff * * 3 14",
                        "precision_form": prec, "nlocal": s["nlocal"], "nghost": s["nghost"],
                        "list_entries": entries, "host_access": pair.host_access,
+                       "tile_tuning": tuning,
                        "staged_host_access": staged,
                        "timing": "host wall clock around PairMATPL.compute (it returns with the "
                                  "results on the host), max over ranks",
