@@ -591,7 +591,7 @@ def run_lammps(args, ws, local, steps, warmup):
         t = autotune.tune_dp_mixed(model, l0, tm0, [0, 1], r0.to(model.dtype))
         tuning = {"group_atoms": t["group_atoms"], "ctas_per_sm": t["ctas_per_sm"]}
     del l0, r0
-    pair = L.PairMATPL(model, ELEMENTS, eatom_grouped=True, host_access="auto")
+    pair = L.PairMATPL(model, ELEMENTS, eatom_grouped=True, host_access=args.lammps_access)
     fn = L.firstneigh_of(s)
     nall = s["nlocal"] + s["nghost"]
     f = np.zeros((nall, 3))
@@ -647,6 +647,11 @@ def run_lammps(args, ws, local, steps, warmup):
     ref_h2d = s["nlocal"] * (S * (4 + 32) + 4)   # int32 list + f64 dR + imagetype_map
     kernels = {k: {"ms_per_step": v[0] / psteps, "launches_per_step": v[1] / psteps}
                for k, v in prof.items()}
+    tp = os.path.join(HERE, "profiles", "traffic.json")
+    traffic = None
+    if os.path.exists(tp):
+        tr = json.load(open(tp)).get(f"lmp_neighbors:{'float64' if prec == 'float64' else 'mixed'}")
+        traffic = tr["bytes_per_launch"] if tr else None
     return {"metric": LMP_METRIC, "value": ws * s["nlocal"] / (wall_ms * 1e-3),
             "unit": "atom-steps/s", "ms_per_step": wall_ms, "steps": steps, "warmup": warmup,
             "dtype": {"float32": "f32", "float64": "f64"}.get(prec, "bf16x3 tensor / f32 / f64 sums"),
@@ -667,7 +672,7 @@ def run_lammps(args, ws, local, steps, warmup):
             "roofline": {"kernel": "lmp_neighbors", "bound": "hbm", "achieved": achieved,
                          "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak if achieved else None,
-                         "algorithmic_bytes_per_launch": nbytes, "traffic": None,
+                         "algorithmic_bytes_per_launch": nbytes, "traffic": traffic,
                          "ms_per_launch": nb_avg,
                          "peak_source": "of measured (MEASURED_PEAKS.json)" if peaks
                          else "of fallback"},
@@ -1017,6 +1022,9 @@ def main():
     ap.add_argument("--lammps-atoms", type=int, default=NATOMS,
                     help="local atoms of the LAMMPS pair-step box (32,000; smaller for captures)")
     ap.add_argument("--no-lammps", action="store_true", help="skip the LAMMPS pair-step workload")
+    ap.add_argument("--lammps-access", default="auto", choices=["auto", "direct", "staged"],
+                    help="how the LAMMPS driver reaches host arrays (profiling captures use "
+                         "staged: ncu replays distort kernels that read host memory)")
     ap.add_argument("--workload", default="dp", choices=["dp", "nep", "train", "md", "lammps"],
                     help="dp: the headline DP line (with a nep object); nep: the NEP line alone")
     argv = sys.argv[1:]
