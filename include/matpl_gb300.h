@@ -305,6 +305,31 @@ int matpl_nep_descriptor(int dtype, const matpl_nep_model *model, int nframes, l
                          size_t workspace_bytes, void *stream);
 
 /* ------------------------------------------------------------------------------------
+ * NEP training operators.  Replace CalcOps calculateNepFeat (part 0, radial) and
+ * calculateNepMbFeat (part 1, 3-/4-/5-body) with their Grad functions
+ * (src/op/src/CalcOps.cpp:385-1023, kernels calculateNepFeat*.cu / calculateNepMbFeat*.cu).
+ * coeff [T, T, n_max, n_base] (the c_param_2 / c_param_3 tensor), d12 [N, max_nn, 4] =
+ * (r, x, y, z), NL [N, max_nn] int64 (-1 = empty), type_map [N] int64; dtype MATPL_F32/F64.
+ * mode 0 (forward):  q [N, ldQ] = the part's features (radial n_max; angular n_max per
+ *                    l = 1..l_max_3b, then the 4-body and 5-body blocks).
+ * mode 1 (backward): for G [N, ldG] = dL/dq writes grad_d12 [N, max_nn, 4] = G . dq/dd12
+ *                    (partials in the four columns; caller zero-fills) and W, zero-filled by
+ *                    the caller: radial [N, T, n_base] = sum over neighbors of type t of
+ *                    f_k(r) (dL/dc[t_i, t, n, k] = sum_i G[i, n] W[i, t, k]); angular
+ *                    [N, T, n_max, n_base] (dL/dc[t_i] = sum_i W[i]).
+ * mode 2 (second backward): for H [N, max_nn, 4] = dL/d(grad_d12) writes q = dq/dd12 . H
+ *                    [N, ldQ] (= dL/dG) and W as in mode 1 for dL/dc (radial: sum of
+ *                    H_r f_k'(r), to be contracted with G).
+ * Compiled for n_max <= 8, n_base <= 16, l_max_3b <= 4, l_max_4b in {0, 2}, l_max_5b in {0, 1}.
+ * ---------------------------------------------------------------------------------- */
+int matpl_nep_feat_op(int dtype, int part, int mode, int natoms, int max_nn, int ntypes,
+                      int n_max, int n_base, int l_max_3b, int l_max_4b, int l_max_5b,
+                      double cutoff, const void *coeff, const void *d12, const long long *NL,
+                      const long long *type_map, const void *G, long long ldG, const void *H,
+                      void *q, long long ldQ, void *grad_d12, void *W, int *err_dev,
+                      void *stream);
+
+/* ------------------------------------------------------------------------------------
  * LAMMPS pair style (DP).  Replaces PairMATPL::generate_neighdata
  * (src/lmps/lammps-libtorch/MATPL/pair_matpl.cpp:522-616) and the DP branch of
  * PairMATPL::compute (pair_matpl.cpp:893-996), which copies the expanded slot arrays to the

@@ -1,0 +1,205 @@
+"""Drop-ins for MatPL's NEP training operators: ``CalcOps.calculateNepFeat`` /
+``calculateNepMbFeat`` (descriptor with first and second backward, src/op/src/CalcOps.cpp:385-1023)
+and ``calculateNepForce`` / ``calculateNepVirial`` (CalcOps.cpp:75-330), with the reference's
+signatures and list returns, as ``nep_net.NEP.forward`` calls them (nep_net.py:352-380, 612-631).
+
+The descriptor functions run ``matpl_nep_feat_op`` (csrc/nep_train.cu).  Like the reference's
+``CalculateNepFeat``: backward gives dL/dc and dL/dRi; the Grad function's own backward gives
+dL/dG and dL/dc from the gradient reaching dL/dRi (the force-loss path of training); the
+gradient reaching dL/dc of the Grad function is not propagated further (the reference returns
+none for it either), nor is a third-order term in Ri.  dL/dRi holds the partial derivatives in
+the four columns (r, x, y, z) taken as independent, as the reference's CPU descriptor gives them
+under autograd; the reference's CUDA kernel distributes the angular part between the columns in
+GPUMD's way, and both give the same forces once contracted with Ri_d.  The force and virial
+functions reuse the DP force / virial kernels (one configuration of N atoms); the virial is
+summed per image of ``num_atom`` and its backward uses each image's own gradient (the
+reference's CUDA backward applies the first image's to all atoms).
+"""
+from typing import List
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import check, ptr
+from .ops import _CalculateForce, _dtype_code, _require_cuda, _stream
+
+PART_RADIAL, PART_ANGULAR = 0, 1
+MODE_FWD, MODE_BWD, MODE_BWD2 = 0, 1, 2
+
+
+def _nfeat(part, nmax, l3, l4, l5):
+    if part == PART_RADIAL:
+        return nmax
+    return nmax * (l3 + (1 if l4 > 0 else 0) + (1 if l5 > 0 else 0))
+
+
+def _feat_call(part, mode, coeff, d12, NL, atom_map, rc, l3=0, l4=0, l5=0, G=None, H=None):
+    """One launch of ``matpl_nep_feat_op``; returns (q or gso, grad_d12, W)."""
+    _require_cuda(coeff, d12, NL, atom_map)
+    N, NN = NL.shape
+    T, _, nmax, K = coeff.shape
+    dev, dt = d12.device, d12.dtype
+    code = _dtype_code(d12)
+    c = coeff.detach().to(dt).contiguous()
+    dd = d12.detach().contiguous()
+    nl = NL.contiguous().to(torch.int64)
+    tm = atom_map.contiguous().to(torch.int64)
+    F = _nfeat(part, nmax, l3, l4, l5)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    q = gd = W = None
+    Gc = G.detach().to(dt).contiguous() if G is not None else None
+    Hc = H.detach().to(dt).contiguous() if H is not None else None
+    if mode in (MODE_FWD, MODE_BWD2):
+        q = torch.empty(N, F, dtype=dt, device=dev) if mode == MODE_FWD else \
+            torch.zeros(N, F, dtype=dt, device=dev)
+        if N * NN == 0:
+            q.zero_()
+    if mode == MODE_BWD:
+        gd = torch.zeros(N, NN, 4, dtype=dt, device=dev)
+    if mode != MODE_FWD:
+        shape = (N, T, K) if part == PART_RADIAL else (N, T, nmax, K)
+        W = torch.zeros(shape, dtype=dt, device=dev)
+    check(_lib.load().matpl_nep_feat_op(
+        code, part, mode, N, NN, T, nmax, K, l3, l4, l5, float(rc), ptr(c), ptr(dd), ptr(nl),
+        ptr(tm), ptr(Gc), F, ptr(Hc), ptr(q), F, ptr(gd), ptr(W), ptr(err), _stream(dev)),
+        "matpl_nep_feat_op")
+    code_k = int(err.item())
+    if code_k:
+        raise _lib.MatplError(f"matpl_nep_feat_op kernel error {code_k} (2 = bad type, "
+                              "5 = list index outside the atoms)")
+    return q, gd, W
+
+
+def _c_grad(part, W, G, atom_map, T):
+    """dL/dc [T, T, n, K] from the per-atom tables: radial sum_i G[i, n] W[i, t, k]; angular
+    sum_i W[i] (G already folded in), each into row t_i."""
+    tm = atom_map.long()
+    if part == PART_RADIAL:
+        per = torch.einsum("in,itk->itnk", G.to(W.dtype), W)
+    else:
+        per = W
+    out = torch.zeros((T,) + tuple(per.shape[1:]), dtype=W.dtype, device=W.device)
+    return out.index_add_(0, tm, per)
+
+
+class _NepFeatGrad(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, G, coeff, d12, NL, atom_map, part, rc, l3, l4, l5):
+        _, gd, W = _feat_call(part, MODE_BWD, coeff, d12, NL, atom_map, rc, l3, l4, l5, G=G)
+        gc = _c_grad(part, W, G.detach(), atom_map, coeff.shape[0]).to(coeff.dtype)
+        ctx.save_for_backward(G, coeff, d12, NL, atom_map)
+        ctx.meta = (part, rc, l3, l4, l5)
+        return gc, gd
+
+    @staticmethod
+    def backward(ctx, g_gc, g_gd):
+        G, coeff, d12, NL, atom_map = ctx.saved_tensors
+        part, rc, l3, l4, l5 = ctx.meta
+        if g_gd is None:
+            return (None,) * 10
+        gso, _, W2 = _feat_call(part, MODE_BWD2, coeff, d12, NL, atom_map, rc, l3, l4, l5,
+                                G=G, H=g_gd)
+        gsc = _c_grad(part, W2, G.detach(), atom_map, coeff.shape[0]).to(coeff.dtype)
+        return gso.to(G.dtype), gsc, None, None, None, None, None, None, None, None
+
+
+class _NepFeat(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, coeff, d12, NL, atom_map, part, rc, l3, l4, l5):
+        q, _, _ = _feat_call(part, MODE_FWD, coeff, d12, NL, atom_map, rc, l3, l4, l5)
+        ctx.save_for_backward(coeff, d12, NL, atom_map)
+        ctx.meta = (part, rc, l3, l4, l5)
+        return q
+
+    @staticmethod
+    def backward(ctx, gq):
+        coeff, d12, NL, atom_map = ctx.saved_tensors
+        part, rc, l3, l4, l5 = ctx.meta
+        gc, gd = _NepFeatGrad.apply(gq, coeff, d12, NL, atom_map, part, rc, l3, l4, l5)
+        return gc, gd, None, None, None, None, None, None, None
+
+
+def calculateNepFeat(coeff2: torch.Tensor, d12_radial: torch.Tensor, NL_radial: torch.Tensor,
+                     atom_map: torch.Tensor, feats: torch.Tensor, rcut_radial: float,
+                     multi_feat_num: int) -> List[torch.Tensor]:
+    """``CalcOps.calculateNepFeat`` (CalcOps.cpp:385-680): coeff2 [T, T, n, K], d12_radial
+    [N, NN, 4] (r, x, y, z), NL_radial [N, NN] int64 (-1 empty), atom_map [N] -> [feat_2b
+    [N, n]].  ``feats`` (the reference's zero-filled output buffer) only fixes the dtype;
+    ``multi_feat_num`` is accepted for the signature."""
+    return [_NepFeat.apply(coeff2, d12_radial, NL_radial, atom_map, PART_RADIAL,
+                           float(rcut_radial), 0, 0, 0).to(feats.dtype)]
+
+
+def calculateNepMbFeat(coeff3: torch.Tensor, d12: torch.Tensor, NL: torch.Tensor,
+                       atom_map: torch.Tensor, feats: torch.Tensor, feat_2b_num: int,
+                       lmax_3: int, lmax_4: int, lmax_5: int,
+                       rcut_angular: float) -> List[torch.Tensor]:
+    """``CalcOps.calculateNepMbFeat`` (CalcOps.cpp:680-1023) -> [feat_mb [N, n*(l3 + 4b + 5b)]]
+    in the order l-major 3-body, 4-body, 5-body."""
+    return [_NepFeat.apply(coeff3, d12, NL, atom_map, PART_ANGULAR, float(rcut_angular),
+                           int(lmax_3), int(lmax_4), int(lmax_5)).to(feats.dtype)]
+
+
+def calculateNepForce(list_neigh: torch.Tensor, dE: torch.Tensor, Ri_d: torch.Tensor,
+                      F: torch.Tensor) -> List[torch.Tensor]:
+    """``CalcOps.calculateNepForce`` (CalcOps.cpp:75-168): list_neigh [N, NN] int64 (-1 empty),
+    dE [N, NN, 4], Ri_d [N, NN*4, 3] (or [N, NN, 4, 3]), F [N, 3] the centre term -> [F plus
+    the neighbors' terms]; differentiable in dE (centre and neighbor parts)."""
+    _require_cuda(list_neigh, dE, Ri_d, F)
+    N, NN = list_neigh.shape
+    out = _CalculateForce.apply(list_neigh.reshape(1, N, NN), dE.reshape(1, N, 4 * NN),
+                                Ri_d.reshape(1, N, 4 * NN, 3), F.reshape(1, N, 3), 0)
+    return [out.reshape(N, 3)]
+
+
+class _NepVirial(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, list_neigh, dE, Rij, Ri_d, num_atom):
+        N, NN = list_neigh.shape
+        nl = list_neigh.contiguous().to(torch.int32)
+        dE_c = dE.contiguous().reshape(N, 4 * NN)
+        Rj = Rij.contiguous().to(dE.dtype).reshape(N, NN, 3)
+        Rd = Ri_d.contiguous().reshape(N, 4 * NN, 3)
+        counts = [int(v) for v in np.asarray(num_atom.detach().cpu()).reshape(-1)]
+        vir1 = torch.empty(1, 9, dtype=dE.dtype, device=dE.device)
+        avir = torch.empty(N, 9, dtype=dE.dtype, device=dE.device)
+        check(_lib.load().matpl_calc_virial(_dtype_code(dE), ptr(nl), ptr(dE_c), ptr(Rj), ptr(Rd),
+                                            1, N, NN, 0, ptr(vir1), ptr(avir), _stream(dE.device)),
+              "matpl_calc_virial")
+        img = torch.repeat_interleave(torch.arange(len(counts), device=dE.device),
+                                      torch.tensor(counts, device=dE.device))
+        vir = torch.zeros(len(counts), 9, dtype=dE.dtype, device=dE.device).index_add_(0, img,
+                                                                                       avir)
+        ctx.save_for_backward(nl, Rj, Rd)
+        ctx.counts = counts
+        ctx.dshape = dE.shape
+        ctx.mark_non_differentiable(avir)
+        return vir, avir
+
+    @staticmethod
+    def backward(ctx, grad_vir, grad_avir):
+        nl, Rj, Rd = ctx.saved_tensors
+        N, NN = nl.shape
+        grad = torch.zeros(N, 4 * NN, dtype=Rd.dtype, device=Rd.device)
+        if grad_vir is not None:
+            g = grad_vir.contiguous().to(Rd.dtype)
+            lib = _lib.load()
+            off = 0
+            for b, n in enumerate(ctx.counts):
+                if n:
+                    check(lib.matpl_calc_virial_grad(
+                        _dtype_code(Rd), ptr(nl[off:off + n]), ptr(Rj[off:off + n]),
+                        ptr(Rd[off:off + n]), ptr(g[b:b + 1]), 1, n, NN, ptr(grad[off:off + n]),
+                        _stream(Rd.device)), "matpl_calc_virial_grad")
+                off += n
+        return None, grad.reshape(ctx.dshape), None, None, None
+
+
+def calculateNepVirial(list_neigh: torch.Tensor, dE: torch.Tensor, Rij: torch.Tensor,
+                       Ri_d: torch.Tensor, num_atom: torch.Tensor) -> List[torch.Tensor]:
+    """``CalcOps.calculateNepVirial`` (CalcOps.cpp:239-330) -> [virial [B, 9] per image,
+    atom_virial [N, 9]], virial[a*3+c] = sum (dE . Ri_d)_a Rij_c credited to the neighbor."""
+    _require_cuda(list_neigh, dE, Rij, Ri_d)
+    v, av = _NepVirial.apply(list_neigh, dE, Rij, Ri_d, num_atom)
+    return [v, av]

@@ -310,3 +310,16 @@ def calculate_neighbor(num_atoms: torch.Tensor, atom_type_map: torch.Tensor,
     if check_overflow:
         _nep_kernel_error(err, "calculate_neighbor")
     return [NN_r, NN_a, NL_r, NL_a, Ri_r, Ri_a]
+
+
+# NEP training operators (CalcOps.calculateNepFeat / calculateNepMbFeat / calculateNepForce /
+# calculateNepVirial) live in nep_ops (which builds on this module) and resolve here on access
+_NEP_OPS = ("calculateNepFeat", "calculateNepMbFeat", "calculateNepForce", "calculateNepVirial")
+
+
+def __getattr__(name):
+    if name in _NEP_OPS:
+        from . import nep_ops
+        return getattr(nep_ops, name)
+    raise AttributeError(f"module {__name__!r} has no attribute {name!r}")
+

@@ -148,32 +148,45 @@ def _pair_c(c: torch.Tensor, ti: torch.Tensor, NL: torch.Tensor, type_map: torch
     return cc * valid[..., None, None]
 
 
+def features_2b(cfg, c2, type_map, NL_r, Ri_r):
+    """[N, n_r] radial descriptor (cal_feat_2body, nep_net.py:717-743)."""
+    ti = type_map.long()
+    fk = _fk(Ri_r[..., 0], cfg.kr, cfg.cutoff[0])                          # [N, S, k]
+    cc = _pair_c(c2, ti, NL_r.long(), type_map.long())                     # [N, S, n, k]
+    return torch.einsum("isnk,isk->in", cc, fk)
+
+
+def features_mb(cfg, c3, type_map, NL_a, Ri_a):
+    """[N, F_mb] 3-/4-/5-body descriptor (cal_feat_multi_body, nep_net.py:745-814): l-major
+    3-body block, then the 4-body and the 5-body n blocks."""
+    ti = type_map.long()
+    fk = _fk(Ri_a[..., 0], cfg.ka, cfg.cutoff[1])
+    cc = _pair_c(c3, ti, NL_a.long(), type_map.long())
+    g = torch.einsum("isnk,isk->isn", cc, fk)                               # [N, S, n]
+    b = _blm(Ri_a[..., 0], Ri_a[..., 1:], cfg.cutoff[1])                    # [N, S, 24]
+    s = torch.einsum("isn,isl->inl", g, b)                                  # [N, n, 24]
+    sq = s * s
+    cq = sq * torch.tensor(C3B, dtype=s.dtype)
+    qnl = torch.stack([cq[..., a:b_].sum(-1) for a, b_ in L_SLICES[:cfg.l_max[0]]], 1)
+    out = [qnl.reshape(qnl.shape[0], -1)]                                   # l-major, then n
+    if cfg.l_max[1] > 0:
+        s3, s4, s5, s6, s7 = (s[..., k] for k in range(3, 8))
+        out.append(C4B[0] * s3 * sq[..., 3] + C4B[1] * s3 * (sq[..., 4] + sq[..., 5])
+                   + C4B[2] * s3 * (sq[..., 6] + sq[..., 7])
+                   + C4B[3] * s6 * (sq[..., 5] - sq[..., 4]) + C4B[4] * s4 * s5 * s7)
+    if cfg.l_max[2] > 0:
+        a0, a12 = sq[..., 0], sq[..., 1] + sq[..., 2]
+        out.append(C5B[0] * a0 * a0 + C5B[1] * a0 * a12 + C5B[2] * a12 * a12)
+    return torch.cat(out, -1)
+
+
 def features(cfg, p: Dict[str, torch.Tensor], type_map, NL_r, Ri_r, NL_a, Ri_a):
     """[N, F] descriptor q (before q_scaler)."""
-    ti = type_map.long()
     out = []
     if cfg.train_2b:
-        fk = _fk(Ri_r[..., 0], cfg.kr, cfg.cutoff[0])                      # [N, S, k]
-        c2 = _pair_c(p["c_param_2"], ti, NL_r.long(), type_map.long())     # [N, S, n, k]
-        out.append(torch.einsum("isnk,isk->in", c2, fk))
+        out.append(features_2b(cfg, p["c_param_2"], type_map, NL_r, Ri_r))
     if cfg.l_max[0] > 0:
-        fk = _fk(Ri_a[..., 0], cfg.ka, cfg.cutoff[1])
-        c3 = _pair_c(p["c_param_3"], ti, NL_a.long(), type_map.long())
-        g = torch.einsum("isnk,isk->isn", c3, fk)                           # [N, S, n]
-        b = _blm(Ri_a[..., 0], Ri_a[..., 1:], cfg.cutoff[1])                # [N, S, 24]
-        s = torch.einsum("isn,isl->inl", g, b)                              # [N, n, 24]
-        sq = s * s
-        cq = sq * torch.tensor(C3B, dtype=s.dtype)
-        qnl = torch.stack([cq[..., a:b_].sum(-1) for a, b_ in L_SLICES[:cfg.l_max[0]]], 1)
-        out.append(qnl.reshape(qnl.shape[0], -1))                           # l-major, then n
-        if cfg.l_max[1] > 0:
-            s3, s4, s5, s6, s7 = (s[..., k] for k in range(3, 8))
-            out.append(C4B[0] * s3 * sq[..., 3] + C4B[1] * s3 * (sq[..., 4] + sq[..., 5])
-                       + C4B[2] * s3 * (sq[..., 6] + sq[..., 7])
-                       + C4B[3] * s6 * (sq[..., 5] - sq[..., 4]) + C4B[4] * s4 * s5 * s7)
-        if cfg.l_max[2] > 0:
-            a0, a12 = sq[..., 0], sq[..., 1] + sq[..., 2]
-            out.append(C5B[0] * a0 * a0 + C5B[1] * a0 * a12 + C5B[2] * a12 * a12)
+        out.append(features_mb(cfg, p["c_param_3"], type_map, NL_a, Ri_a))
     return torch.cat(out, -1)
 
 
@@ -251,3 +264,45 @@ def nep_eval(cfg, p: Dict[str, torch.Tensor], num_atom, type_map, NL_r, Ri_r, NL
     if return_feats:
         out["feats"] = feats.detach()
     return out
+
+
+TRAIN_KEYS = ("c_param_2", "c_param_3")
+
+
+def train_grads(cfg, p: Dict[str, torch.Tensor], num_atom, type_map, NL_r, Ri_r, NL_a, Ri_a,
+                gE, gF, gV=None):
+    """Parameter gradient of L = sum gE Etot + sum gF Force + sum gV Virial (Force, Virial the
+    physical values NEP.forward returns) through the CPU branch of NEP.forward with second-order
+    autograd, as loss.backward() sees it in training (nep_net.py:293-648).  Returns
+    {name: grad} for the descriptor coefficients and every fitting-net tensor."""
+    num_atom = np.asarray(num_atom).reshape(-1)
+    type_map = torch.as_tensor(type_map)
+    NL_r, NL_a = torch.as_tensor(NL_r), torch.as_tensor(NL_a)
+    names = [k for k in p if k != "q_scaler"]
+    pp = {k: (p[k].detach().clone().requires_grad_() if k in names else p[k]) for k in p}
+    Rr = torch.as_tensor(Ri_r, dtype=torch.float64).clone().requires_grad_()
+    Ra = torch.as_tensor(Ri_a, dtype=torch.float64).clone().requires_grad_()
+    feats = features(cfg, pp, type_map, NL_r, Rr, NL_a, Ra)
+    Ei = fitting(cfg, pp, type_map, feats * pp["q_scaler"])
+    Etot = torch.stack([e.sum() for e in Ei.split(num_atom.tolist())]).unsqueeze(-1)
+    leaves, lists = [], []
+    if cfg.train_2b:
+        leaves.append(Rr)
+        lists.append((Rr, NL_r))
+    if cfg.l_max[0] > 0:
+        leaves.append(Ra)
+        lists.append((Ra, NL_a))
+    grads = torch.autograd.grad(Etot.sum(), leaves, create_graph=True, allow_unused=True)
+    F = torch.zeros(Ei.shape[0], 3, dtype=torch.float64)
+    V = torch.zeros(len(num_atom), 9, dtype=torch.float64)
+    for g, (R, NL) in zip(grads, lists):
+        if g is None:
+            continue
+        f, v = _force_virial(g, R.detach(), NL, num_atom)
+        F, V = F + f, V + v
+    L = (torch.as_tensor(gE) * Etot.reshape(-1)).sum() + (torch.as_tensor(gF) * -F).sum()
+    if gV is not None:
+        L = L + (torch.as_tensor(gV) * -V).sum()
+    leaves_p = [pp[k] for k in names]
+    gs = torch.autograd.grad(L, leaves_p, allow_unused=True)
+    return {k: (torch.zeros_like(pp[k]) if g is None else g.detach()) for k, g in zip(names, gs)}
