@@ -462,6 +462,165 @@ def run_train(args, ws, local, steps, warmup, plain_steps):
     }
 
 
+NEP_TRAIN_METRIC = ("NEP force-loss training step atom-steps/s (E + F + virial loss, Adam; "
+                    "hand-written descriptor second derivatives)")
+NEP_TRAIN_NATOMS = 20_000
+NEP_TRAIN_CPU_SAMPLE = 2000
+
+
+def nep_train_setup(dev, natoms, seed=NEP_SEED_STRUCT + 7):
+    """A NEP training batch: the NEP workload's model on a `natoms` box of the same density,
+    split into four frames (num_atom), exact lists from calculate_neighbor, q_scaler from the
+    box's descriptors, labels from a teacher NEP (other seed) plus N(0, 0.01) noise."""
+    from matpl_gb300 import nep as NP, ops, structures
+    cfg = NP.NepConfig(atom_type=list(NEP_ELEMENTS))
+    per = max(1, natoms // 4)
+    sts = [structures.random_packed(per, NEP_DENSITY, NEP_ELEMENTS, [0.25] * 4, seed=seed + k)
+           for k in range(4)]
+    fr = NP.frames_from_structures(sts, cfg.cutoff[0])
+    c = lambda a, dt: torch.tensor(np.ascontiguousarray(a), dtype=dt, device=dev)  # noqa: E731
+    na, tm = c(fr.num_atom.reshape(-1, 1), torch.int64), c(fr.type_map, torch.int64)
+    bx, bo, nc = c(fr.box, torch.float64), c(fr.box_orig, torch.float64), c(fr.num_cell, torch.int64)
+    pos = c(fr.position, torch.float64)
+    at = torch.arange(cfg.ntypes, device=dev)
+    cr, ca = ops.calculate_maxneigh(na, bx, bo, nc, pos, cfg.cutoff[0], cfg.cutoff[1], cfg.ntypes,
+                                    tm, False)
+    lists = ops.calculate_neighbor(na, tm, at, bx, bo, nc, pos, cfg.cutoff[0], cfg.cutoff[1],
+                                   int(cr.max()), int(ca.max()), True)
+    prm = NP.init_params(cfg, NEP_SEED_W, energy_shift=-3.0)
+    m64 = NP.NEP(cfg, prm, "float64", device=dev)
+    feats = m64.descriptor(lists[0], lists[2], lists[4], lists[1], lists[3], lists[5], na, tm)
+    qs = NP.calc_q_scaler(cfg, feats).cpu()
+    prm["q_scaler"] = qs
+    tprm = NP.init_params(cfg, NEP_SEED_W + 50, energy_shift=-3.0)
+    tprm["q_scaler"] = qs
+    lab = NP.NEP(cfg, tprm, "float64", device=dev).evaluate(lists[0], lists[2], lists[4],
+                                                            lists[1], lists[3], lists[5], na, tm)
+    g = torch.Generator(device=dev).manual_seed(3)
+    labels = {"Etot": lab["Etot"].reshape(-1) + 0.01 * torch.randn(len(sts), generator=g,
+                                                                   device=dev, dtype=torch.float64),
+              "Force": lab["Force"].double() + 0.01 * torch.randn(lab["Force"].shape, generator=g,
+                                                                  device=dev, dtype=torch.float64),
+              "Virial": lab["Virial"].double()}
+    return cfg, fr, prm, lists, na, tm, labels
+
+
+def run_nep_train(args, ws, local, steps, warmup):
+    """NEP force-loss training step on a 20,000-atom four-frame batch: NEPTrain (NEP.forward's
+    CUDA branch on calculateNepFeat / calculateNepMbFeat with hand-written first and second
+    backward, calculateNepForce / calculateNepVirial), loss = per-atom energy MSE + force MSE +
+    virial MSE, loss.backward(), Adam; FP32 (timed) and FP64 (beside it)."""
+    from matpl_gb300 import _lib, nep_ops
+    from matpl_gb300.nep_train import NEPTrain
+    dev = torch.device("cuda", local)
+    cfg, fr, prm, lists, na, tm, lab = nep_train_setup(dev, args.nep_train_atoms)
+    N = fr.natoms
+    na_h = torch.tensor(fr.num_atom.reshape(-1, 1))
+    nep_ops.set_check_errors(False)
+
+    def make(dt):
+        model = NEPTrain(cfg, prm, dtype=dt, device=dev)
+        opt = torch.optim.Adam(model.parameters(), lr=1e-4, fused=True)
+        labd = {k: v.to(dt) for k, v in lab.items()}
+        per_atom = torch.tensor(fr.num_atom, dtype=dt, device=dev)
+        Rr, Ra = lists[4].to(dt), lists[5].to(dt)
+
+        def step():
+            opt.zero_grad(set_to_none=True)
+            Etot, Ei, F, _, V = model(lists[0], lists[2], Rr, lists[1], lists[3], Ra, na_h, tm)
+            loss = ((Etot.reshape(-1) - labd["Etot"]) / per_atom).pow(2).mean() \
+                + (F - labd["Force"]).pow(2).mean() \
+                + 1e-4 * ((V - labd["Virial"]) / per_atom.unsqueeze(-1)).pow(2).mean()
+            loss.backward()
+            opt.step()
+            return loss
+        return step
+
+    def timed(step, n, w):
+        for _ in range(w):
+            step()
+        torch.cuda.synchronize()
+        barrier(ws)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            loss = step()
+        e1.record()
+        torch.cuda.synchronize()
+        return max_over_ranks(e0.elapsed_time(e1) / n, ws), float(loss.detach())
+
+    s32 = make(torch.float32)
+    for _ in range(warmup):
+        s32()
+    _lib.profile_begin(max(4096, steps * 64))
+    ms32, loss32 = timed(s32, steps, 0)
+    prof = _lib.profile_collect()
+    s64 = make(torch.float64)
+    ms64, loss64 = timed(s64, max(3, steps // 2), 2)
+    nep_ops.check_errors(dev)
+    nep_ops.set_check_errors(True)
+    per_kernel = {k: {"ms_per_step": v[0] / steps, "launches_per_step": v[1] / steps}
+                  for k, v in prof.items()}
+    return {"metric": NEP_TRAIN_METRIC, "value": ws * N / (ms32 * 1e-3), "unit": "atom-steps/s",
+            "ms_per_step": ms32, "steps": steps, "warmup": warmup, "dtype": "f32",
+            "config": {"workload": f"NEP training batch of 4 frames, {N:,} atoms, four elements, "
+                                   f"{NEP_DENSITY} atoms/A^3, rc 6 / 4 A, n_max 4 / 4, basis 8 / 8, "
+                                   "l_max 4 / 2 / 1, 30 hidden; teacher labels (E, F, V)",
+                       "natoms": N, "loss_fp32": loss32,
+                       "fp64": {"ms_per_step": ms64, "value": ws * N / (ms64 * 1e-3),
+                                "loss": loss64},
+                       "form": "autograd over this library's operators (the reference's op "
+                               "structure), eager"},
+            "kernels": per_kernel}
+
+
+def cpu_baseline_nep_train(steps=5):
+    """The reference's NEP training gradient on the host cores: the oracle port of the CPU
+    branch of NEP.forward with second-order autograd (torch FP64, all host threads) on a
+    bounded 2,000-atom sample of the same model and density."""
+    from oracle import nep_oracle as NO
+    from matpl_gb300 import nep as NP, structures
+    ncores = os.cpu_count() or 1
+    torch.set_num_threads(ncores)
+    cfg = NP.NepConfig(atom_type=list(NEP_ELEMENTS))
+    st = structures.random_packed(NEP_TRAIN_CPU_SAMPLE, NEP_DENSITY, NEP_ELEMENTS, [0.25] * 4,
+                                  seed=NEP_SEED_STRUCT + 9)
+    fr = NP.frames_from_structures([st], cfg.cutoff[0])
+    cr, ca = NO.maxneigh(fr, cfg.cutoff[0], cfg.cutoff[1])
+    L = NO.neighbor(fr, cfg.cutoff[0], cfg.cutoff[1], int(cr.max()), int(ca.max()))
+    prm = NP.init_params(cfg, NEP_SEED_W, energy_shift=-3.0)
+    rng = np.random.default_rng(1)
+    N = fr.natoms
+    gE, gF, gV = rng.standard_normal(1), rng.standard_normal((N, 3)), rng.standard_normal((1, 9))
+    ts = []
+    for _ in range(steps + 1):
+        t0 = time.perf_counter()
+        NO.train_grads(cfg, prm, fr.num_atom, fr.type_map, L[2], L[4], L[3], L[5], gE, gF, gV)
+        ts.append(time.perf_counter() - t0)
+    med = statistics.median(ts[1:])
+    return {"value": N / med, "unit": "atom-steps/s", "cores": ncores, "kind": "port",
+            "sample": f"{N}-atom four-element box, FP64, training gradient of an E + F + V loss "
+                      f"(second-order autograd through the CPU descriptor), median of {steps}",
+            "sec_per_step": med}
+
+
+def run_nep_train_line(args, ws, rank, local):
+    torch.cuda.set_device(local)
+    from matpl_gb300 import _lib
+    _lib.load()
+    steps = args.steps if args.steps_given else 20
+    r = run_nep_train(args, ws, local, steps=steps, warmup=args.warmup)
+    if rank == 0 and not args.no_cpu_baseline:
+        r["cpu_baseline"] = cpu_baseline_nep_train()
+    if rank != 0:
+        return
+    line = {"metric": r.pop("metric"), "value": r.pop("value"), "unit": r.pop("unit"),
+            "n_gpus": ws, "steps": r.pop("steps"), "warmup": r.pop("warmup"),
+            "ms_per_step": r.pop("ms_per_step"), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": r.pop("dtype"), "data": "synthetic", **r}
+    print(json.dumps(line))
+
+
 MD_METRIC = "batched replica MD atom-steps/s (velocity Verlet, DP mixed, one graph launch per step)"
 MD_REPLICAS, MD_NMIN, MD_NMAX, MD_SEED = 256, 64, 2048, 77
 
@@ -906,6 +1065,11 @@ def run_ours(args, ws, rank, local):
     md_r = None
     if not args.no_md:
         md_r = run_md(args, ws, local, steps=200)
+    nep_train_r = None
+    if not args.no_nep_train:
+        nep_train_r = run_nep_train(args, ws, local, steps=10, warmup=3)
+        if rank == 0 and not args.no_cpu_baseline:
+            nep_train_r["cpu_baseline"] = cpu_baseline_nep_train(steps=3)
     lmp_r = None
     if not args.no_lammps:
         lmp_r, lmp_s, lmp_cfg = run_lammps(args, ws, local, steps=30, warmup=3)
@@ -947,7 +1111,7 @@ def run_ours(args, ws, rank, local):
                     "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "kernels": per_kernel, "roofline": roof,
             "clocks": clocks, "cpu_baseline": cb, "nep": nep, "train": train_r, "md": md_r,
-            "lammps": lmp_r}
+            "lammps": lmp_r, "nep_train": nep_train_r}
     print(json.dumps(line))
 
 
@@ -1025,7 +1189,11 @@ def main():
     ap.add_argument("--lammps-access", default="auto", choices=["auto", "direct", "staged"],
                     help="how the LAMMPS driver reaches host arrays (profiling captures use "
                          "staged: ncu replays distort kernels that read host memory)")
-    ap.add_argument("--workload", default="dp", choices=["dp", "nep", "train", "md", "lammps"],
+    ap.add_argument("--nep-train-atoms", type=int, default=NEP_TRAIN_NATOMS,
+                    help="atoms of the NEP training batch (20,000; smaller for captures)")
+    ap.add_argument("--no-nep-train", action="store_true", help="skip the NEP training workload")
+    ap.add_argument("--workload", default="dp",
+                    choices=["dp", "nep", "train", "md", "lammps", "neptrain"],
                     help="dp: the headline DP line (with a nep object); nep: the NEP line alone")
     argv = sys.argv[1:]
     args = ap.parse_args()
@@ -1048,6 +1216,9 @@ def main():
         return
     if args.workload == "lammps":
         run_lammps_line(args, ws, rank, local)
+        return
+    if args.workload == "neptrain":
+        run_nep_train_line(args, ws, rank, local)
         return
     run_ours(args, ws, rank, local)
 

@@ -27,6 +27,36 @@ from .ops import _CalculateForce, _dtype_code, _require_cuda, _stream
 PART_RADIAL, PART_ANGULAR = 0, 1
 MODE_FWD, MODE_BWD, MODE_BWD2 = 0, 1, 2
 
+_check_each_call = True
+_err_words = {}
+
+
+def set_check_errors(each_call: bool):
+    """True (default): every descriptor call reads the kernels' error word (one device sync).
+    False: the word accumulates on the device until ``check_errors()`` (training loops)."""
+    global _check_each_call
+    _check_each_call = bool(each_call)
+
+
+def _err_word(dev):
+    w = _err_words.get(dev)
+    if w is None:
+        w = torch.zeros(1, dtype=torch.int32, device=dev)
+        _err_words[dev] = w
+    return w
+
+
+def check_errors(device=None):
+    """Raise if a descriptor kernel flagged an error since the last check (then clear it)."""
+    for dev, w in list(_err_words.items()):
+        if device is not None and dev != torch.device(device):
+            continue
+        code = int(w.item())
+        if code:
+            w.zero_()
+            raise _lib.MatplError(f"matpl_nep_feat_op kernel error {code} (2 = bad type, "
+                                  "5 = list index outside the atoms)")
+
 
 def _nfeat(part, nmax, l3, l4, l5):
     if part == PART_RADIAL:
@@ -46,7 +76,7 @@ def _feat_call(part, mode, coeff, d12, NL, atom_map, rc, l3=0, l4=0, l5=0, G=Non
     nl = NL.contiguous().to(torch.int64)
     tm = atom_map.contiguous().to(torch.int64)
     F = _nfeat(part, nmax, l3, l4, l5)
-    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    err = _err_word(dev)
     q = gd = W = None
     Gc = G.detach().to(dt).contiguous() if G is not None else None
     Hc = H.detach().to(dt).contiguous() if H is not None else None
@@ -64,10 +94,8 @@ def _feat_call(part, mode, coeff, d12, NL, atom_map, rc, l3=0, l4=0, l5=0, G=Non
         code, part, mode, N, NN, T, nmax, K, l3, l4, l5, float(rc), ptr(c), ptr(dd), ptr(nl),
         ptr(tm), ptr(Gc), F, ptr(Hc), ptr(q), F, ptr(gd), ptr(W), ptr(err), _stream(dev)),
         "matpl_nep_feat_op")
-    code_k = int(err.item())
-    if code_k:
-        raise _lib.MatplError(f"matpl_nep_feat_op kernel error {code_k} (2 = bad type, "
-                              "5 = list index outside the atoms)")
+    if _check_each_call:
+        check_errors(dev)
     return q, gd, W
 
 
@@ -153,6 +181,21 @@ def calculateNepForce(list_neigh: torch.Tensor, dE: torch.Tensor, Ri_d: torch.Te
     return [out.reshape(N, 3)]
 
 
+_img_cache = {}
+
+
+def _image_index(counts, dev):
+    """[N] image of every atom for per-image sums, cached per (counts, device)."""
+    key = (counts, dev)
+    t = _img_cache.get(key)
+    if t is None:
+        t = torch.repeat_interleave(torch.arange(len(counts)), torch.tensor(counts)).to(dev)
+        if len(_img_cache) > 64:
+            _img_cache.clear()
+        _img_cache[key] = t
+    return t
+
+
 class _NepVirial(torch.autograd.Function):
     @staticmethod
     def forward(ctx, list_neigh, dE, Rij, Ri_d, num_atom):
@@ -167,8 +210,7 @@ class _NepVirial(torch.autograd.Function):
         check(_lib.load().matpl_calc_virial(_dtype_code(dE), ptr(nl), ptr(dE_c), ptr(Rj), ptr(Rd),
                                             1, N, NN, 0, ptr(vir1), ptr(avir), _stream(dE.device)),
               "matpl_calc_virial")
-        img = torch.repeat_interleave(torch.arange(len(counts), device=dE.device),
-                                      torch.tensor(counts, device=dE.device))
+        img = _image_index(tuple(counts), dE.device)
         vir = torch.zeros(len(counts), 9, dtype=dE.dtype, device=dE.device).index_add_(0, img,
                                                                                        avir)
         ctx.save_for_backward(nl, Rj, Rd)

@@ -112,7 +112,7 @@ class NEPTrain(torch.nn.Module):
                                     create_graph=True, allow_unused=True)
         Force = torch.zeros(N, 3, dtype=dt, device=Ri.device)
         Virial = torch.zeros(len(counts), 9, dtype=dt, device=Ri.device)
-        na = num_atom.reshape(-1).to(Ri.device)
+        na = num_atom.reshape(-1)
         for dE, (R, NL) in zip(grads, leaves):        # nep_net.py:612-631
             if dE is None:
                 continue
