@@ -12,7 +12,7 @@ virial loss reaches every parameter exactly like the reference's training step
 descriptor.  The per-element FittingNet (one tanh layer, nep_fitting.py:136-160) stays in
 torch: it is a few small GEMMs per element.
 """
-from typing import Dict, Optional
+from typing import Dict, List, Optional
 
 import torch
 
@@ -67,10 +67,17 @@ class NEPTrain(torch.nn.Module):
                                                  _Layer(p[pre + "1.weight"], p[pre + "1.bias"])]))
         self.register_buffer("q_scaler", p["q_scaler"].clone())
 
-    def calculate_Ei(self, type_map: torch.Tensor, feats: torch.Tensor) -> torch.Tensor:
+    def type_index(self, type_map: torch.Tensor) -> List[torch.Tensor]:
+        """Atom indices of every element (one device sync); pass it to ``forward`` to keep the
+        step free of host synchronisation (CUDA-graph capture)."""
+        tm = type_map.reshape(-1).long()
+        return [torch.nonzero(tm == t).flatten() for t in range(self.cfg.ntypes)]
+
+    def calculate_Ei(self, type_map: torch.Tensor, feats: torch.Tensor,
+                     type_index: Optional[List[torch.Tensor]] = None) -> torch.Tensor:
         Ei = torch.zeros(type_map.shape[0], dtype=feats.dtype, device=feats.device)
-        for t, net in enumerate(self.fitting_net):       # nep_net.py:470-501
-            idx = torch.nonzero(type_map == t).flatten()
+        idxs = type_index if type_index is not None else self.type_index(type_map)
+        for idx, net in zip(idxs, self.fitting_net):     # nep_net.py:470-501
             if idx.numel() == 0:
                 continue
             Ei = Ei.index_put((idx,), net(feats[idx]).squeeze(-1))
@@ -78,7 +85,8 @@ class NEPTrain(torch.nn.Module):
 
     def forward(self, NN_radial, NL_radial, Ri_radial, NN_angular, NL_angular, Ri_angular,
                 num_atom, atom_type_map, Egroup_weight: Optional[torch.Tensor] = None,
-                divider: Optional[torch.Tensor] = None, is_calc_f: bool = True):
+                divider: Optional[torch.Tensor] = None, is_calc_f: bool = True,
+                type_index: Optional[List[torch.Tensor]] = None):
         cfg = self.cfg
         dt = self.q_scaler.dtype
         tm = atom_type_map.reshape(-1).long()
@@ -97,7 +105,7 @@ class NEPTrain(torch.nn.Module):
                                                                 device=Ri.device),
                 cfg.two_feat_num, *cfg.l_max, cfg.cutoff[1])[0])
         feats = torch.cat(feats, -1)
-        Ei = self.calculate_Ei(tm, self.q_scaler * feats)
+        Ei = self.calculate_Ei(tm, self.q_scaler * feats, type_index)
         counts = num_atom.reshape(-1).tolist()
         Etot = torch.stack([e.sum() for e in Ei.split(counts)]).unsqueeze(-1)
         Egroup = None
@@ -121,3 +129,75 @@ class NEPTrain(torch.nn.Module):
             Force = Force + nep_ops.calculateNepForce(NL, dE, Rd, f0)[0]
             Virial = Virial + nep_ops.calculateNepVirial(NL, dE, R.detach()[:, :, 1:], Rd, na)[0]
         return Etot, Ei, -Force, Egroup, -Virial
+
+
+class GraphedNepTrainer:
+    """One NEP training step - NEPTrain forward with create_graph forces, the loss
+    w_e * MSE(E / atom) + w_f * MSE(F) + w_v * MSE(V / atom), backward through the hand-written
+    descriptor derivatives, optimizer update - captured once per batch shape in a CUDA graph and
+    replayed: a step costs one graph launch plus copying the batch into the graph's static
+    buffers.  ``num_atom`` is a host tensor (frame sizes are part of the shape key); the
+    optimizer keeps its state on the device (Adam / AdamW with capturable=True, or SGD).  The
+    descriptor kernels' error word is checked by ``check_errors()``, not per step."""
+
+    KEYS = ("NN_r", "NL_r", "Ri_r", "NN_a", "NL_a", "Ri_a", "type_map", "Etot", "Force", "Virial")
+
+    def __init__(self, model: NEPTrain, optimizer: torch.optim.Optimizer, w_e: float = 1.0,
+                 w_f: float = 1.0, w_v: float = 0.0, warmup: int = 3):
+        self.model, self.opt = model, optimizer
+        self.w = (w_e, w_f, w_v)
+        self.warmup = warmup
+        self.graphs = {}
+
+    def loss(self, b, type_index=None):
+        Etot, _, F, _, V = self.model(b["NN_r"], b["NL_r"], b["Ri_r"], b["NN_a"], b["NL_a"],
+                                      b["Ri_a"], b["num_atom"], b["type_map"],
+                                      type_index=type_index)
+        per = b["per_atom"]
+        w_e, w_f, w_v = self.w
+        loss = w_e * ((Etot.reshape(-1) - b["Etot"]) / per).pow(2).mean() \
+            + w_f * (F - b["Force"]).pow(2).mean()
+        if w_v:
+            loss = loss + w_v * ((V - b["Virial"]) / per.unsqueeze(-1)).pow(2).mean()
+        return loss
+
+    def _capture(self, batch):
+        dt = self.model.q_scaler.dtype
+        static = {k: batch[k].clone() for k in self.KEYS}
+        for k in ("Ri_r", "Ri_a", "Etot", "Force", "Virial"):
+            static[k] = static[k].to(dt)
+        static["num_atom"] = batch["num_atom"].detach().cpu().reshape(-1)
+        static["per_atom"] = static["num_atom"].to(device=static["Etot"].device, dtype=dt)
+        tindex = self.model.type_index(static["type_map"])
+        nep_ops.set_check_errors(False)
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            for _ in range(self.warmup):         # allocator, image index, kernel attributes
+                self.opt.zero_grad(set_to_none=True)
+                self.loss(static, tindex).backward()
+                self.opt.step()
+        torch.cuda.current_stream().wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        self.opt.zero_grad(set_to_none=True)
+        with torch.cuda.graph(g):
+            loss = self.loss(static, tindex)
+            loss.backward()
+            self.opt.step()
+        return g, static, loss
+
+    def step(self, batch) -> torch.Tensor:
+        key = tuple(tuple(batch[k].shape) for k in self.KEYS) + \
+            (tuple(batch["num_atom"].reshape(-1).tolist()),)
+        if key not in self.graphs:
+            self.graphs[key] = self._capture(batch)
+        g, static, loss = self.graphs[key]
+        for k in self.KEYS:
+            if batch[k].data_ptr() != static[k].data_ptr():
+                static[k].copy_(batch[k], non_blocking=True)
+        g.replay()
+        return loss
+
+    def check_errors(self):
+        nep_ops.check_errors()
+
