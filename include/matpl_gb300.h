@@ -388,6 +388,20 @@ int matpl_lammps_dp_compute(matpl_lammps_dp *handle, int nlocal, int nghost, int
                             double *virial, double *eatom, double *min_rsq);
 void matpl_lammps_dp_destroy(matpl_lammps_dp *handle);
 
+/* Model deviation (pair_style matpl with several models, pair_matpl.cpp:940-975, 1287-1320):
+ * add_model appends a model (same ntypes, m and Rmax as the first: the slots are built once
+ * with them); compute_models converts the list once and evaluates the first nmodels models,
+ * writing f [nmodels][nall][3], eng [nmodels], virial [nmodels][6], eatom [nmodels][inum]
+ * (each may be NULL but f), *min_rsq; the pair style folds the ghost rows (reverse
+ * communication) and computes the deviation as before (calc_max_error, :385-483). */
+int matpl_lammps_dp_add_model(matpl_lammps_dp *handle, const matpl_dp_model *model);
+int matpl_lammps_dp_num_models(const matpl_lammps_dp *handle);
+int matpl_lammps_dp_compute_models(matpl_lammps_dp *handle, int nmodels, int nlocal, int nghost,
+                                   int inum, const int *ilist, const int *numneigh,
+                                   const int *const *firstneigh, const double *x,
+                                   const int *type, double *f, double *eng, double *virial,
+                                   double *eatom, double *min_rsq);
+
 #ifdef __cplusplus
 }
 #endif

@@ -86,6 +86,10 @@ SIGNATURES = {
     "matpl_lammps_dp_compute": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                      _vp, _vp]),
     "matpl_lammps_dp_destroy": (None, [_vp]),
+    "matpl_lammps_dp_add_model": (_i, [_vp, _c.POINTER(MatplDpModel)]),
+    "matpl_lammps_dp_num_models": (_i, [_vp]),
+    "matpl_lammps_dp_compute_models": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp,
+                                            _vp, _vp, _vp, _vp]),
 }
 
 

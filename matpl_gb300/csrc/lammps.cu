@@ -298,7 +298,8 @@ using namespace matpl;
 
 struct matpl_lammps_dp {
     int dtype = MATPL_F64;
-    matpl_dp_model model{};
+    matpl_dp_model model{};                 // the first model (also models[0])
+    std::vector<matpl_dp_model> models;
     int ntypes_lmp = 0;
     int eatom_grouped = 0;
     int host_access = MATPL_LMP_STAGED;
@@ -394,8 +395,29 @@ extern "C" int matpl_lammps_dp_create(int dtype, const matpl_dp_model *model, in
         return MATPL_ERR_CUDA;
     }
     h->model.err_dev = h->err;
+    h->models.push_back(h->model);
     *handle = h;
     return MATPL_OK;
+}
+
+extern "C" int matpl_lammps_dp_add_model(matpl_lammps_dp *h, const matpl_dp_model *model) {
+    MATPL_REQUIRE(h && model && model->params && model->davg && model->dstd, MATPL_ERR_INVALID,
+                  "handle, model and its parameter pointers are required");
+    // the slots are built once with the first model's cutoff and maxNeighborNum
+    // (pair_matpl.cpp:536, 550), so every model must share them and the type count
+    MATPL_REQUIRE(model->ntypes == h->model.ntypes && model->m == h->model.m &&
+                      model->rmax == h->model.rmax,
+                  MATPL_ERR_INVALID, "models of one pair style share ntypes, m and Rmax");
+    matpl_dp_model m = *model;
+    m.npresent = h->model.npresent;
+    for (int a = 0; a < 8; ++a) m.present[a] = h->model.present[a];
+    m.err_dev = h->err;
+    h->models.push_back(m);
+    return MATPL_OK;
+}
+
+extern "C" int matpl_lammps_dp_num_models(const matpl_lammps_dp *h) {
+    return h ? (int)h->models.size() : -1;
 }
 
 extern "C" int matpl_lammps_dp_host_access(const matpl_lammps_dp *handle) {
@@ -404,12 +426,15 @@ extern "C" int matpl_lammps_dp_host_access(const matpl_lammps_dp *handle) {
 
 extern "C" void matpl_lammps_dp_destroy(matpl_lammps_dp *handle) { delete handle; }
 
-extern "C" int matpl_lammps_dp_compute(matpl_lammps_dp *h, int nlocal, int nghost, int inum,
-                                       const int *ilist, const int *numneigh,
-                                       const int *const *firstneigh, const double *x,
-                                       const int *type, double *f, double *eng, double *virial,
-                                       double *eatom, double *min_rsq) {
+extern "C" int matpl_lammps_dp_compute_models(matpl_lammps_dp *h, int nmodels, int nlocal,
+                                              int nghost, int inum, const int *ilist,
+                                              const int *numneigh, const int *const *firstneigh,
+                                              const double *x, const int *type, double *f,
+                                              double *eng, double *virial, double *eatom,
+                                              double *min_rsq) {
     MATPL_REQUIRE(h, MATPL_ERR_INVALID, "handle is NULL");
+    MATPL_REQUIRE(nmodels >= 1 && nmodels <= (int)h->models.size(), MATPL_ERR_INVALID,
+                  "nmodels must be 1 .. the handle's model count");
     MATPL_REQUIRE(nlocal >= 0 && nghost >= 0 && inum == nlocal, MATPL_ERR_INVALID,
                   "a full list over the local atoms is required (inum == nlocal)");
     if (min_rsq) *min_rsq = kNoPair;
@@ -438,9 +463,10 @@ extern "C" int matpl_lammps_dp_compute(matpl_lammps_dp *h, int nlocal, int nghos
                                    : align_up(o_jf + 4 * (size_t)tot, 16);
     const size_t tail_n = (size_t)inum + 9;
     const size_t out_n = 3 * (size_t)nall + tail_n;
+    const size_t nm = (size_t)nmodels;
     const size_t ws_bytes = matpl_dp_workspace_bytes(h->dtype, 1, inum);
-    bool ok = h->din.ensure(in_bytes) && h->hout.ensure(8 * out_n) &&
-              (direct || (h->hin.ensure(in_bytes) && h->out.ensure(8 * out_n))) &&
+    bool ok = h->din.ensure(in_bytes) && h->hout.ensure(8 * out_n * nm) &&
+              (direct || (h->hin.ensure(in_bytes) && h->out.ensure(8 * out_n * nm))) &&
               h->ln.ensure(4 * S * inum) && h->idr.ensure(es * 4 * S * inum) &&
               h->tmap.ensure(4 * (size_t)inum) && h->Ei.ensure(es * inum) &&
               h->Etot.ensure(8) && h->force.ensure(es * 3 * (size_t)nall) &&
@@ -495,15 +521,18 @@ extern "C" int matpl_lammps_dp_compute(matpl_lammps_dp *h, int nlocal, int nghos
                               h->idr.p, (int32_t *)h->tmap.p, (double *)h->mn.p, h->err, s);
     }
     if (rc) return rc;
-    rc = matpl_dp_eval(h->dtype, &h->model, 1, inum, (int)S, nghost, (const int32_t *)h->ln.p,
-                       h->idr.p, (const int32_t *)h->tmap.p, h->Ei.p, (double *)h->Etot.p,
-                       h->force.p, (double *)h->vir.p, h->ws.p, h->ws.cap, s);
-    if (rc) return rc;
-    // direct: forces straight into f, the rest into mapped pinned memory; staged: all into
-    // one device buffer, copied back below
-    double *fout = direct ? f : (double *)h->out.p;
-    double *tdev = direct ? (double *)h->hout.dev : (double *)h->out.p + 3 * (size_t)nall;
-    {
+    // one slot conversion, then every model (pair_matpl.cpp:945-965 runs them one by one)
+    for (int k = 0; k < nmodels; ++k) {
+        rc = matpl_dp_eval(h->dtype, &h->models[k], 1, inum, (int)S, nghost,
+                           (const int32_t *)h->ln.p, h->idr.p, (const int32_t *)h->tmap.p,
+                           h->Ei.p, (double *)h->Etot.p, h->force.p, (double *)h->vir.p, h->ws.p,
+                           h->ws.cap, s);
+        if (rc) return rc;
+        // direct: forces straight into f, the rest into mapped pinned memory; staged: all into
+        // one device buffer, copied back below
+        double *fout = direct ? f + k * 3 * (size_t)nall : (double *)h->out.p + k * out_n;
+        double *tdev = direct ? (double *)h->hout.dev + k * tail_n
+                              : (double *)h->out.p + k * out_n + 3 * (size_t)nall;
         ProfScope ps("lmp_pack", s);
         const long long n = (long long)out_n;
         const int grid = (int)std::min<long long>((n + 255) / 256, 152LL * 8);
@@ -520,17 +549,18 @@ extern "C" int matpl_lammps_dp_compute(matpl_lammps_dp *h, int nlocal, int nghos
                                                  (const double *)h->mn.p, h->err, fout, tdev);
         if ((rc = check_launch("matpl_lammps_dp_compute"))) return rc;
     }
-    bool c = direct || cudaMemcpyAsync(h->hout.p, h->out.p, 8 * out_n, cudaMemcpyDeviceToHost,
-                                       s) == cudaSuccess;
+    bool c = direct || cudaMemcpyAsync(h->hout.p, h->out.p, 8 * out_n * nm,
+                                       cudaMemcpyDeviceToHost, s) == cudaSuccess;
     if (!c || cudaStreamSynchronize(s) != cudaSuccess) {
         set_error(std::string("matpl_lammps_dp_compute: ") +
                   cudaGetErrorString(cudaGetLastError()));
         return MATPL_ERR_CUDA;
     }
     const double *o = (const double *)h->hout.p;
-    const double *t = direct ? o : o + 3 * (size_t)nall;
-    const double *tail = t + inum;
-    const int kerr = (int)tail[8];
+    // the error word of the last model's pack holds every kernel's flags of this call
+    const double *last = direct ? o + (nm - 1) * tail_n
+                                : o + (nm - 1) * out_n + 3 * (size_t)nall;
+    const int kerr = (int)last[inum + 8];
     if (kerr) {
         set_error("matpl_lammps_dp_compute: kernel error code " + std::to_string(kerr) +
                   (kerr == MATPL_KERR_NEIGHBOR_OVERFLOW
@@ -539,28 +569,41 @@ extern "C" int matpl_lammps_dp_compute(matpl_lammps_dp *h, int nlocal, int nghos
                                                      : " (list index outside the atoms)"));
         return MATPL_ERR_INVALID;
     }
-    // pair_matpl.cpp:982-996: forces of local and ghost atoms are set (LAMMPS' reverse
-    // communication adds the ghost rows to their owners), energy and Voigt virial
-    if (!direct) std::memcpy(f, o, 24 * (size_t)nall);
-    if (eng) *eng = tail[0];
-    if (virial)
-        for (int q = 0; q < 6; ++q) virial[q] = tail[1 + q];
-    if (min_rsq) *min_rsq = tail[7];
-    if (eatom) {
-        const double *Ei = t;
-        if (!h->eatom_grouped) {
-            std::memcpy(eatom, Ei, 8 * (size_t)inum);
-        } else {
-            // the TorchScript model returns Ei grouped by image type (dp_dp_script.py:296-311)
-            // and pair_matpl.cpp:1000 stores it as is
-            int k = 0;
-            for (int q = 0; q < h->ntypes_lmp; ++q)
-                for (int ii = 0; ii < inum; ++ii) {
-                    const int tl = type[ilist[ii]] - 1;
-                    if (tl == q) eatom[k++] = Ei[ii];
-                }
-            for (; k < inum; ++k) eatom[k] = 0.0;
+    for (int k = 0; k < nmodels; ++k) {
+        const double *t = direct ? o + k * tail_n : o + k * out_n + 3 * (size_t)nall;
+        const double *tail = t + inum;
+        // pair_matpl.cpp:982-996: forces of local and ghost atoms are set (LAMMPS' reverse
+        // communication adds the ghost rows to their owners), energy and Voigt virial
+        if (!direct) std::memcpy(f + k * 3 * (size_t)nall, o + k * out_n, 24 * (size_t)nall);
+        if (eng) eng[k] = tail[0];
+        if (virial)
+            for (int q = 0; q < 6; ++q) virial[6 * k + q] = tail[1 + q];
+        if (min_rsq && k == 0) *min_rsq = tail[7];
+        if (eatom) {
+            double *ea = eatom + (size_t)k * inum;
+            if (!h->eatom_grouped) {
+                std::memcpy(ea, t, 8 * (size_t)inum);
+            } else {
+                // the TorchScript model returns Ei grouped by image type (dp_dp_script.py:296-311)
+                // and pair_matpl.cpp:1000 stores it as is
+                int j = 0;
+                for (int q = 0; q < h->ntypes_lmp; ++q)
+                    for (int ii = 0; ii < inum; ++ii) {
+                        const int tl = type[ilist[ii]] - 1;
+                        if (tl == q) ea[j++] = t[ii];
+                    }
+                for (; j < inum; ++j) ea[j] = 0.0;
+            }
         }
     }
     return MATPL_OK;
+}
+
+extern "C" int matpl_lammps_dp_compute(matpl_lammps_dp *h, int nlocal, int nghost, int inum,
+                                       const int *ilist, const int *numneigh,
+                                       const int *const *firstneigh, const double *x,
+                                       const int *type, double *f, double *eng, double *virial,
+                                       double *eatom, double *min_rsq) {
+    return matpl_lammps_dp_compute_models(h, 1, nlocal, nghost, inum, ilist, numneigh, firstneigh,
+                                          x, type, f, eng, virial, eatom, min_rsq);
 }

@@ -64,7 +64,20 @@ class PairMATPL:
         self._h = h
         self.host_access = {_lib.LMP_STAGED: "staged", _lib.LMP_DIRECT: "direct"}[
             lib.matpl_lammps_dp_host_access(h)]
-        self._f = None
+        self.models = [model]
+        self._structs = [self._mstruct]
+
+    def add_model(self, model: DP):
+        """Another model for the deviation (``pair_style matpl m1.pt m2.pt ...``): same type
+        count, maxNeighborNum and Rmax as the first, any weights and precision form that
+        matches the first's dtype."""
+        if model.code != self.models[0].code:
+            raise _lib.MatplError("all models of one pair style use the same precision form")
+        st = model._model_struct(list(range(model.cfg.ntypes)))
+        check(_lib.load().matpl_lammps_dp_add_model(self._h, ctypes.byref(st)),
+              "matpl_lammps_dp_add_model")
+        self.models.append(model)
+        self._structs.append(st)
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -105,6 +118,55 @@ class PairMATPL:
         if len(ilist) and mn.value < MIN_RSQ:
             raise _lib.MatplError(f"there are two atoms too close, min_dR_all = {mn.value}")
         return {"f": f, "eng": eng.value, "virial": vir, "eatom": eatom, "min_rsq": mn.value}
+
+
+def _compute_models(pair: PairMATPL, nmodels, x, type_, nlocal, nghost, ilist, numneigh,
+                    firstneigh, eflag_atom):
+    nall = nlocal + nghost
+    x = _np(x, np.float64).reshape(nall, 3)
+    type_ = _np(type_, np.int32)
+    ilist = _np(ilist, np.int32)
+    numneigh = _np(numneigh, np.int32)
+    firstneigh = _np(firstneigh, np.uint64)
+    f = np.zeros((nmodels, nall, 3), dtype=np.float64)
+    eng = np.zeros(nmodels, dtype=np.float64)
+    vir = np.zeros((nmodels, 6), dtype=np.float64)
+    eatom = np.zeros((nmodels, len(ilist)), dtype=np.float64) if eflag_atom else None
+    mn = ctypes.c_double(0.0)
+    c = ctypes.c_void_p
+    check(_lib.load().matpl_lammps_dp_compute_models(
+        pair._h, nmodels, int(nlocal), int(nghost), len(ilist), ilist.ctypes.data_as(c),
+        numneigh.ctypes.data_as(c), firstneigh.ctypes.data_as(c), x.ctypes.data_as(c),
+        type_.ctypes.data_as(c), f.ctypes.data_as(c), eng.ctypes.data_as(c),
+        vir.ctypes.data_as(c), eatom.ctypes.data_as(c) if eatom is not None else None,
+        ctypes.cast(ctypes.byref(mn), c)), "matpl_lammps_dp_compute_models")
+    if len(ilist) and mn.value < MIN_RSQ:
+        raise _lib.MatplError(f"there are two atoms too close, min_dR_all = {mn.value}")
+    return {"f": f, "eng": eng, "virial": vir, "eatom": eatom, "min_rsq": mn.value}
+
+
+def compute_models(pair: PairMATPL, x, type_, nlocal, nghost, ilist, numneigh, firstneigh,
+                   eflag_atom: bool = True) -> Dict:
+    """Every model of the pair style on one slot conversion: f [K, nall, 3], eng [K],
+    virial [K, 6], eatom [K, inum] (the f_n / e_atom_n of pair_matpl.cpp:951-963)."""
+    return _compute_models(pair, len(pair.models), x, type_, nlocal, nghost, ilist, numneigh,
+                           firstneigh, eflag_atom)
+
+
+def model_deviation(f_n: np.ndarray, e_n: np.ndarray) -> Tuple[float, ...]:
+    """PairMATPL::calc_max_error (pair_matpl.cpp:385-483) after the ghost rows are folded:
+    f_n [K, nlocal, 3], e_n [K, nlocal] -> (max over atoms of the RMS force deviation, max and
+    min per-model force deviation, the same three for Ei), the model_devi.out columns."""
+    f_n = np.asarray(f_n, dtype=np.float64)
+    e_n = np.asarray(e_n, dtype=np.float64)
+    K = f_n.shape[0]
+    ferr = f_n - f_n.mean(0)
+    fe = np.sqrt((ferr * ferr).sum(-1))                 # [K, nlocal]
+    eerr = np.abs(e_n - e_n.mean(0))
+    max_mean_f = float(np.sqrt((fe * fe).sum(0) / K).max())
+    max_mean_e = float(np.sqrt((eerr * eerr).sum(0) / K).max())
+    return (max_mean_f, float(fe.max()), float(fe.min()), max_mean_e, float(eerr.max()),
+            float(eerr.min()))
 
 
 def lammps_dp_neighbors(ilist: torch.Tensor, jstart: torch.Tensor, jflat: torch.Tensor,

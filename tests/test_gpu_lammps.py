@@ -232,3 +232,43 @@ def test_pair_too_close_and_sizes_change(access):
                  np.zeros(0, np.int32), np.zeros(0, np.uint64), f_out=f0)
     assert (f0 == 7.0).all()
     pair.close()
+
+
+@pytest.mark.parametrize("access", ACCESS)
+def test_model_deviation_shares_one_conversion(access):
+    """Three models on one slot conversion (compute_models) = each model's own pair step; the
+    deviation of identical models is zero; models must share ntypes, m and Rmax."""
+    from matpl_gb300.lammps import compute_models, model_deviation
+    st, s = mixed_system(600, seed=31)
+    cfg = P.DPConfig(atom_type=[3, 14], maxNeighborNum=150)
+    davg, dstd = stats(cfg, st)
+    s["numneigh"] = np.diff(s["jstart"]).astype(np.int32)
+    models = [dp.DP(cfg, P.init_params(cfg, 300 + k), davg, dstd, precision="float64",
+                    device=DEV) for k in range(3)]
+    pair = PairMATPL(models[0], [3, 14], host_access=access)
+    for mdl in models[1:]:
+        pair.add_model(mdl)
+    r = compute_models(pair, s["x"], s["type"], s["nlocal"], s["nghost"], s["ilist"],
+                       s["numneigh"], firstneigh_of(s))
+    assert r["f"].shape == (3, s["nlocal"] + s["nghost"], 3)
+    for k, mdl in enumerate(models):
+        one = PairMATPL(mdl, [3, 14], host_access=access)
+        o = run_pair(one, s)
+        np.testing.assert_allclose(r["f"][k], o["f"], rtol=0, atol=1e-12 * np.abs(o["f"]).max())
+        np.testing.assert_allclose(r["eng"][k], o["eng"], rtol=1e-13)
+        np.testing.assert_allclose(r["virial"][k], o["virial"], rtol=0,
+                                   atol=1e-12 * np.abs(o["virial"]).max())
+        np.testing.assert_allclose(r["eatom"][k], o["eatom"], rtol=0, atol=1e-13)
+        one.close()
+    n = s["nlocal"]
+    f_fold = np.stack([fold_ghosts(r["f"][k], s["owner"], n) for k in range(3)])
+    dev = model_deviation(f_fold, r["eatom"])
+    assert dev[1] >= dev[0] / np.sqrt(3) and dev[1] >= dev[2] >= 0 and dev[4] >= dev[5] >= 0
+    same = model_deviation(np.stack([f_fold[0]] * 3), np.stack([r["eatom"][0]] * 3))
+    assert max(same) < 1e-12
+    other = P.DPConfig(atom_type=[3, 14], maxNeighborNum=120)
+    bad = dp.DP(other, P.init_params(other, 1), davg[:, :120 * 2 * 4], dstd[:, :120 * 2 * 4],
+                precision="float64", device=DEV)
+    with pytest.raises(_lib.MatplError, match="share ntypes"):
+        pair.add_model(bad)
+    pair.close()
