@@ -639,6 +639,51 @@ def run_nep_train_line(args, ws, rank, local):
     print(json.dumps(line))
 
 
+DATA_METRIC = "dataset statistics pass (neighbor search + davg/dstd sums) images/s"
+DATA_IMAGES = 2048
+
+
+def run_data(args, ws, local):
+    """The data path's statistics pass over a dataset of 2,048 Li/Si images (108 atoms, the
+    headline density and model, m = 150): neighbor lists of every image and the per-type sums
+    behind davg / dstd (matpl_gb300.data.image_stats), images of one shape batched into one
+    launch; host wall clock.  CPU baseline: the oracle port (C NeighConst restatement + the
+    numpy restatement of calc_stat's sums) on a 64-image sample."""
+    from matpl_gb300 import data as D, params as P, structures
+    from oracle import neigh
+    cfg = P.DPConfig(atom_type=list(ELEMENTS), maxNeighborNum=M_NEIGH, Rmax=RC, Rmin=RMIN)
+    base = [structures.random_packed(108, DENSITY, ELEMENTS, [0.5, 0.5], seed=900 + k)
+            for k in range(16)]
+    ims = []
+    for k in range(DATA_IMAGES):       # 16 compositions, jittered positions
+        b = base[k % 16]
+        rng = np.random.default_rng(k)
+        ims.append(structures.Structure(b.lattice, np.mod(b.frac + 0.002 * rng.standard_normal(
+            b.frac.shape), 1.0), b.types, b.elements))
+    D.image_stats(cfg, ims[:32])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    D.image_stats(cfg, ims)
+    torch.cuda.synchronize()
+    sec = max_over_ranks(time.perf_counter() - t0, ws)
+    cb = None
+    if not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        for st in ims[:64]:
+            tm = D.model_types(st, cfg.atom_type)
+            ln, idr = neigh.find_neighbore(tm, st.frac, st.lattice, cfg.ntypes, M_NEIGH, RC,
+                                           [RC, RC])
+            neigh.env_sums(cfg, ln, idr, tm)
+        ct = time.perf_counter() - t0
+        cb = {"value": 64 / ct, "unit": "images/s", "cores": 1, "kind": "port",
+              "sample": "64 of the same images, C restatement of NeighConst + numpy sums"}
+    return {"metric": DATA_METRIC, "value": ws * DATA_IMAGES / sec, "unit": "images/s",
+            "seconds": sec, "config": {"workload": f"{DATA_IMAGES} Li/Si images of 108 atoms "
+                                                   "(16 compositions), m = 150, Rc 6",
+                                       "timing": "host wall clock, one pass"},
+            "cpu_baseline": cb}
+
+
 MD_METRIC = "batched replica MD atom-steps/s (velocity Verlet, DP mixed, one graph launch per step)"
 MD_REPLICAS, MD_NMIN, MD_NMAX, MD_SEED = 256, 64, 2048, 77
 
@@ -1083,6 +1128,7 @@ def run_ours(args, ws, rank, local):
     md_r = None
     if not args.no_md:
         md_r = run_md(args, ws, local, steps=200)
+    data_r = run_data(args, ws, local) if not args.no_data else None
     nep_train_r = None
     if not args.no_nep_train:
         nep_train_r = run_nep_train(args, ws, local, steps=10, warmup=3)
@@ -1129,7 +1175,7 @@ def run_ours(args, ws, rank, local):
                     "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "kernels": per_kernel, "roofline": roof,
             "clocks": clocks, "cpu_baseline": cb, "nep": nep, "train": train_r, "md": md_r,
-            "lammps": lmp_r, "nep_train": nep_train_r}
+            "lammps": lmp_r, "nep_train": nep_train_r, "data_path": data_r}
     print(json.dumps(line))
 
 
@@ -1210,6 +1256,7 @@ def main():
     ap.add_argument("--nep-train-atoms", type=int, default=NEP_TRAIN_NATOMS,
                     help="atoms of the NEP training batch (20,000; smaller for captures)")
     ap.add_argument("--no-nep-train", action="store_true", help="skip the NEP training workload")
+    ap.add_argument("--no-data", action="store_true", help="skip the data-path statistics pass")
     ap.add_argument("--workload", default="dp",
                     choices=["dp", "nep", "train", "md", "lammps", "neptrain"],
                     help="dp: the headline DP line (with a nep object); nep: the NEP line alone")

@@ -305,6 +305,18 @@ int matpl_nep_descriptor(int dtype, const matpl_nep_model *model, int nframes, l
                          size_t workspace_bytes, void *stream);
 
 /* ------------------------------------------------------------------------------------
+ * Data-path statistics.  Replaces the per-image calc_stat + smooth of
+ * src/pre_data/dpuni_data_loader.py:422-563 (davg / dstd of calculate_davg_dstd, :377-420).
+ * list_neigh [B,N,S] int32 (1-based, 0 empty), image_dr [B,N,S,4] f64 (r, x, y, z),
+ * type_map [N] model type.  sums [B, ntypes, 8] f64 (overwritten): over every slot of the atoms
+ * of type t, sum Ri_c and sum Ri_c^2 for c = 0..3, Ri = vv(r) (1/r, x/r^2, y/r^2, z/r^2) with
+ * the switching function of smooth (rmin, rmax); r^2 and r are formed from (x, y, z).
+ * ---------------------------------------------------------------------------------- */
+int matpl_env_stats(int batch, int natoms, int nslots, int ntypes, const int32_t *type_map,
+                    const int32_t *list_neigh, const double *image_dr, double rmin, double rmax,
+                    double *sums, int32_t *err_dev, void *stream);
+
+/* ------------------------------------------------------------------------------------
  * NEP training operators.  Replace CalcOps calculateNepFeat (part 0, radial) and
  * calculateNepMbFeat (part 1, 3-/4-/5-body) with their Grad functions
  * (src/op/src/CalcOps.cpp:385-1023, kernels calculateNepFeat*.cu / calculateNepMbFeat*.cu).

@@ -77,6 +77,7 @@ SIGNATURES = {
                             _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "matpl_nep_descriptor": (_i, [_i, _c.POINTER(MatplNepModel), _i, _ll, _vp, _vp, _i, _vp, _vp,
                                   _vp, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "matpl_env_stats": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _d, _d, _vp, _vp, _vp]),
     "matpl_nep_feat_op": (_i, [_i] * 11 + [_d] + [_vp] * 5 + [_ll, _vp, _vp, _ll] + [_vp] * 4),
     "matpl_lammps_dp_neighbors": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _i,
                                        _vp, _vp, _vp, _vp, _vp, _vp]),

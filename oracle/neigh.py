@@ -60,3 +60,32 @@ def find_neighbore(type_maps, frac_position, lattice, ntypes, m_neigh, Rc_M, Rc_
     idr = np.zeros((images, natoms, S, 4), dtype=np.float64)
     lib.matpl_oracle_image_dr(images * natoms * S, ln.ctypes.data, dr.ctypes.data, idr.ctypes.data)
     return ln, idr
+
+
+def env_sums(cfg, list_neigh, image_dr, type_map):
+    """ORACLE of matpl_env_stats: [B, ntypes, 8] sums of Ri_c and Ri_c^2 (c = 0..3) over the
+    slots of each centre type, Ri = vv(r) (1/r, x/r^2, y/r^2, z/r^2) with r, r^2 formed from the
+    pair vector like calc_stat + smooth (src/pre_data/dpuni_data_loader.py:436-534)."""
+    ln = np.asarray(list_neigh)
+    dr = np.asarray(image_dr, dtype=np.float64)
+    B, N, S = ln.shape
+    tm = np.asarray(type_map)
+    out = np.zeros((B, cfg.ntypes, 8))
+    mask = ln > 0
+    xyz = dr[..., 1:]
+    r2 = (xyz * xyz).sum(-1)
+    r2s = np.where(mask, r2, 1.0)
+    r = r2s / np.sqrt(r2s)
+    u = (r - cfg.Rmin) / (cfg.Rmax - cfg.Rmin)
+    vv = np.where(r < cfg.Rmin, 1.0, np.where(r < cfg.Rmax, u ** 3 * (-6 * u * u + 15 * u - 10) + 1,
+                                              0.0))
+    Ri = np.stack([vv / r, vv * xyz[..., 0] / r2s, vv * xyz[..., 1] / r2s, vv * xyz[..., 2] / r2s],
+                  -1)
+    Ri = np.where(mask[..., None], Ri, 0.0)
+    for b in range(B):
+        for t in range(cfg.ntypes):
+            sel = Ri[b][tm == t].reshape(-1, 4)
+            out[b, t, 0::2] = sel.sum(0)
+            out[b, t, 1::2] = (sel * sel).sum(0)
+    return out
+
