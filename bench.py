@@ -639,6 +639,59 @@ def run_nep_train_line(args, ws, rank, local):
     print(json.dumps(line))
 
 
+VARIANT_ATOMS = 8000
+
+
+def run_dp_variants(args, ws, local):
+    """The DP model variants evaluated through this library's operators in the reference's own
+    structure (environment matrix, per type-pair contraction, fitting nets, autograd dE/dRi,
+    calculateForce / calculateVirial): the compressed model (order-5 table through
+    calculateCompress) and the type-embedding model, FP32, on an 8,000-atom box of the
+    headline's density; E + F + V per step, CUDA events."""
+    from matpl_gb300 import compress as C, ops, params as P
+    from matpl_gb300.typedp import TypeDP, init_type_params
+    dev = torch.device("cuda", local)
+    st, cfg, prm = make_workload(VARIANT_ATOMS)
+    tm = torch.tensor(st.types, dtype=torch.int32, device=dev)
+    ln, idr = ops.find_neighbore(tm, torch.tensor(st.frac, device=dev),
+                                 torch.tensor(st.lattice, device=dev), 2, M_NEIGH, RC, RC)
+    davg, dstd = P.calc_stat(cfg, ln.cpu().numpy(), idr.cpu().numpy(), st.types)
+    idr32 = idr.float()
+    r = idr[..., 0][ln > 0]
+    u = (r - RMIN) / (RC - RMIN)
+    vv = torch.where(r < RMIN, torch.ones_like(r),
+                     torch.where(r < RC, u ** 3 * (-6 * u * u + 15 * u - 10) + 1, torch.zeros_like(r)))
+    sij_max = float((vv / r).max())
+    out = {}
+
+    def timed(model, n=5):
+        for _ in range(2):
+            model(ln, tm, cfg.atom_type, idr32, 0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            model(ln, tm, cfg.atom_type, idr32, 0)
+        e1.record()
+        torch.cuda.synchronize()
+        return max_over_ranks(e0.elapsed_time(e1) / n, ws)
+
+    comp = C.build_table(cfg, prm, davg, dstd, sij_max, 0.01, 5, device=dev)
+    ms = timed(C.CompressedDP(cfg, prm, davg, dstd, comp, dtype=torch.float32, device=dev))
+    out["compressed_order5"] = {"ms_per_step": ms, "value": ws * VARIANT_ATOMS / (ms * 1e-3),
+                                "table_rows": int(comp["table"].shape[1])}
+    vec = {3: [0.0185, 0.0216, 0.3], 14: [0.1204, 0.0985, 0.2]}
+    tprm = init_type_params(cfg, 3, SEED_W)
+    ms = timed(TypeDP(cfg, tprm, davg, dstd, vec, dtype=torch.float32, device=dev))
+    out["type_embedding"] = {"ms_per_step": ms, "value": ws * VARIANT_ATOMS / (ms * 1e-3)}
+    return {"metric": "DP variant E+F+virial atom-steps/s (reference structure on this "
+                      "library's operators, FP32)", "unit": "atom-steps/s",
+            "config": {"workload": f"{VARIANT_ATOMS}-atom Li/Si box, m=150/type, Rc 6",
+                       "cpu_baseline": "none on the GPU box (the reference's Python is not "
+                                       "there); parity is pinned by the golden fixtures"},
+            **out}
+
+
 DATA_METRIC = "dataset statistics pass (neighbor search + davg/dstd sums) images/s"
 DATA_IMAGES = 2048
 
@@ -1129,6 +1182,7 @@ def run_ours(args, ws, rank, local):
     if not args.no_md:
         md_r = run_md(args, ws, local, steps=200)
     data_r = run_data(args, ws, local) if not args.no_data else None
+    variants_r = run_dp_variants(args, ws, local) if not args.no_variants else None
     nep_train_r = None
     if not args.no_nep_train:
         nep_train_r = run_nep_train(args, ws, local, steps=10, warmup=3)
@@ -1175,7 +1229,8 @@ def run_ours(args, ws, rank, local):
                     "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "kernels": per_kernel, "roofline": roof,
             "clocks": clocks, "cpu_baseline": cb, "nep": nep, "train": train_r, "md": md_r,
-            "lammps": lmp_r, "nep_train": nep_train_r, "data_path": data_r}
+            "lammps": lmp_r, "nep_train": nep_train_r, "data_path": data_r,
+            "dp_variants": variants_r}
     print(json.dumps(line))
 
 
@@ -1257,6 +1312,8 @@ def main():
                     help="atoms of the NEP training batch (20,000; smaller for captures)")
     ap.add_argument("--no-nep-train", action="store_true", help="skip the NEP training workload")
     ap.add_argument("--no-data", action="store_true", help="skip the data-path statistics pass")
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip the compressed / type-embedding DP variants")
     ap.add_argument("--workload", default="dp",
                     choices=["dp", "nep", "train", "md", "lammps", "neptrain"],
                     help="dp: the headline DP line (with a nep object); nep: the NEP line alone")

@@ -1,0 +1,89 @@
+"""Type-embedding DP (``TypeDP``, src/model/dp_dp_typ_emb.py:44-549) on the GPU.
+
+One embedding net shared by all type pairs takes [s_ij, v(t_j)] - the scaled s of the slot and
+the neighbor element's normalised physical-property vector v (``type_vector``,
+utils/atom_type_emb_dict.py:143-161) - as its first-layer input (dp_embedding_typ_emb.py:
+EmbeddingNet with ``type_feat_num``); the contraction, the per-element fitting nets and the
+force / virial path are those of DP.  ``TypeDP`` is ``train.DPTrainModel`` (environment matrix,
+fitting nets, forces and virial through this library's operators, second-order differentiable
+for training) with that embedding; parameter names follow the reference
+(``embedding_net.{E}.layers.{l}``, E = index of the embedding net after an optional type
+embedding net).
+
+The property vectors are an input: ``type_vector`` maps each model element to the list the
+reference's ``get_normalized_data_list(atom_type, physical_property)`` gives for it (stored
+with a trained model; this package does not carry the element property table).  The
+reference's optional type-embedding net (``network_size`` non-empty) is not applied to the
+vectors by its own forward (calculate_xyz_scater feeds the raw vectors), so it is not used
+here either.
+"""
+import math
+from typing import Dict, Sequence
+
+import torch
+
+from .params import DPConfig
+from .train import DPTrainModel
+
+
+def init_type_params(cfg: DPConfig, nfeat: int, seed: int, emb_index: int = 0,
+                     dtype=torch.float64) -> Dict[str, torch.Tensor]:
+    """Seeded parameters with the reference's shapes and initial distributions
+    (dp_embedding_typ_emb.py:71-88 and the fitting net): embedding widths
+    [1 + nfeat] + emb_sizes, one fitting net per element on M2 * emb_sizes[-1] inputs."""
+    g = torch.Generator().manual_seed(seed)
+    p = {}
+    widths = [1 + nfeat] + list(cfg.emb_sizes)
+    for l in range(len(cfg.emb_sizes)):
+        pre = f"embedding_net.{emb_index}.layers.{l}."
+        p[pre + "weight"] = torch.randn(widths[l], widths[l + 1], generator=g,
+                                        dtype=torch.float64) / math.sqrt(widths[l] + widths[l + 1])
+        p[pre + "bias"] = torch.randn(1, widths[l + 1], generator=g, dtype=torch.float64)
+        if cfg.emb_resnet_dt:
+            p[pre + "resnet_dt"] = 1 + 0.001 * torch.randn(1, widths[l + 1], generator=g,
+                                                           dtype=torch.float64)
+    fw = [cfg.M2 * cfg.emb_sizes[-1]] + list(cfg.fit_sizes)
+    for t in range(cfg.ntypes):
+        for l in range(len(cfg.fit_sizes)):
+            pre = f"fitting_net.{t}.layers.{l}."
+            p[pre + "weight"] = torch.randn(fw[l], fw[l + 1], generator=g,
+                                            dtype=torch.float64) / math.sqrt(fw[l] + fw[l + 1])
+            p[pre + "bias"] = torch.randn(1, fw[l + 1], generator=g, dtype=torch.float64)
+            if cfg.fit_resnet_dt and 0 < l < len(cfg.fit_sizes) - 1:
+                p[pre + "resnet_dt"] = 0.1 + 0.001 * torch.randn(1, fw[l + 1], generator=g,
+                                                                 dtype=torch.float64)
+    return {k: v.to(dtype) for k, v in p.items()}
+
+
+class TypeDP(DPTrainModel):
+    def __init__(self, cfg: DPConfig, params: Dict[str, torch.Tensor], davg, dstd,
+                 type_vector: Dict[int, Sequence[float]], emb_index: int = None,
+                 dtype=torch.float64, device="cuda"):
+        super().__init__(cfg, params, davg, dstd, dtype=dtype, device=device)
+        vec = torch.tensor([list(type_vector[z]) for z in cfg.atom_type], dtype=dtype,
+                           device=device)
+        self.register_buffer("type_vec", vec)
+        if emb_index is None:
+            idx = sorted({int(k.split(".")[1]) for k in params if k.startswith("embedding_net.")})
+            emb_index = idx[-1]
+        self.emb_index = emb_index
+
+    def _emb(self, k: int, s: torch.Tensor) -> torch.Tensor:
+        # calculate_xyz_scater (dp_dp_typ_emb.py:360-375): [s, v(t_j)] -> the shared net
+        tj = k % self.cfg.ntypes
+        v = self.type_vec[tj].expand(*s.shape[:-1], self.type_vec.shape[1])
+        x = torch.cat((s, v), dim=-1)
+        widths = [x.shape[-1]] + list(self.cfg.emb_sizes)
+        for l in range(len(self.cfg.emb_sizes)):
+            pre = f"embedding_net.{self.emb_index}.layers.{l}."
+            h = x @ self.param(pre + "weight")
+            b = self.param(pre + "bias")
+            h = torch.tanh(h + b if b is not None else h)
+            dt = self.param(pre + "resnet_dt")
+            if widths[l + 1] == widths[l]:
+                x = (h * dt if dt is not None else h) + x
+            elif widths[l + 1] == 2 * widths[l]:
+                x = torch.cat((x, x), dim=-1) + (h * dt if dt is not None else h)
+            else:
+                x = h
+        return x
