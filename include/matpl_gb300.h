@@ -189,7 +189,8 @@ int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, int natoms,
 /* Tile shape of the MATPL_MIXED* embedding kernels, process-wide (this project's tuning
  * hook; the reference has no tensor-core path).  mixed_group_atoms = centre atoms whose pair
  * rows one CTA walks in 128-row tcgen05 tiles (1..16, capped by shared memory), and
- * mixed_ctas_per_sm = resident CTAs per SM (1..3); 0 = automatic.  Results do not depend on
+ * mixed_ctas_per_sm = resident CTAs per SM (1..6, as shared memory and registers allow);
+ * 0 = automatic (3).  Results do not depend on
  * them (same per-atom arithmetic); matpl_gb300/autotune.py picks them by timing. */
 int matpl_dp_set_tuning(int mixed_group_atoms, int mixed_ctas_per_sm);
 int matpl_dp_get_tuning(int *mixed_group_atoms, int *mixed_ctas_per_sm);

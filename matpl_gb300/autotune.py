@@ -19,8 +19,8 @@ import torch
 from . import _lib
 from ._lib import check
 
-DEFAULT_GROUPS = (4, 6, 8, 10, 11, 12, 14, 16)
-DEFAULT_CTAS = (2, 3)
+DEFAULT_GROUPS = (6, 8, 10, 11, 12, 14, 16)
+DEFAULT_CTAS = (2, 3, 4)
 
 
 def set_tuning(group_atoms: int = 0, ctas_per_sm: int = 0):

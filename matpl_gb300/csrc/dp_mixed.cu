@@ -354,7 +354,7 @@ __device__ void build_group_list(const MixSmem &sm, const int32_t *__restrict__ 
 
 // ------------------------------------------------------------------ forward (A descriptor)
 template <int SPLIT, bool FAST>
-__global__ void __launch_bounds__(TM, 3)
+__global__ void __launch_bounds__(TM, 4)
 dp_embed_fwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict__ idr,
                 const int32_t *__restrict__ type_map, const float *__restrict__ params,
                 const unsigned char *__restrict__ wtiles, const float *__restrict__ davg,
@@ -711,8 +711,11 @@ int launch_mixed_embed(bool backward, const int32_t *list_neigh, const float *id
     const size_t smem = mix_smem_bytes(ntypes * ntypes, nslots, P.ga);
     const long long total = (long long)batch * natoms;
     const long long ngroups = (total + P.ga - 1) / P.ga;
-    int per_sm = (int)std::max<size_t>(1, std::min<size_t>(3, (220 * 1024) / (smem + 2048)));
-    if (g_ctas_override.load() > 0) per_sm = std::min(per_sm, g_ctas_override.load());
+    // resident CTAs per SM: what shared memory allows (the automatic choice stays at 3, the
+    // tuning hook may ask for up to 6; the backward's registers cap it at 3 anyway)
+    const int fit = (int)std::max<size_t>(1, (220 * 1024) / (smem + 2048));
+    int per_sm = std::min(fit, 3);
+    if (g_ctas_override.load() > 0) per_sm = std::min(fit, g_ctas_override.load());
     const int grid = (int)std::min<long long>(ngroups, 152LL * per_sm);
     if (!backward) {
         auto k = dp_embed_fwd_tc<SPLIT, FAST>;
@@ -749,8 +752,8 @@ extern "C" int matpl_dp_set_tuning(int mixed_group_atoms, int mixed_ctas_per_sm)
     using namespace matpl;
     MATPL_REQUIRE(mixed_group_atoms >= 0 && mixed_group_atoms <= GAMAX, MATPL_ERR_INVALID,
                   "mixed_group_atoms must be 0 (automatic) .. 16");
-    MATPL_REQUIRE(mixed_ctas_per_sm >= 0 && mixed_ctas_per_sm <= 3, MATPL_ERR_INVALID,
-                  "mixed_ctas_per_sm must be 0 (automatic) .. 3");
+    MATPL_REQUIRE(mixed_ctas_per_sm >= 0 && mixed_ctas_per_sm <= 6, MATPL_ERR_INVALID,
+                  "mixed_ctas_per_sm must be 0 (automatic) .. 6");
     g_ga_override.store(mixed_group_atoms);
     g_ctas_override.store(mixed_ctas_per_sm);
     return MATPL_OK;
