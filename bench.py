@@ -556,7 +556,7 @@ def run_nep_train(args, ws, local, steps, warmup):
 
     # graphed FP32 step (the headline of this workload)
     gmodel = NEPTrain(cfg, prm, dtype=torch.float32, device=dev)
-    gopt = torch.optim.Adam(gmodel.parameters(), lr=1e-4, capturable=True)
+    gopt = torch.optim.Adam(gmodel.parameters(), lr=1e-4, capturable=True, fused=True)
     graphed = GraphedNepTrainer(gmodel, gopt, w_e=1.0, w_f=1.0, w_v=1e-4)
     b32 = batch(torch.float32)
     gms, gloss = timed(lambda: graphed.step(b32), steps, warmup)

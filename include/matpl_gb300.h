@@ -342,6 +342,41 @@ int matpl_nep_feat_op(int dtype, int part, int mode, int natoms, int max_nn, int
                       void *q, long long ldQ, void *grad_d12, void *W, int *err_dev,
                       void *stream);
 
+/* matpl_nep_cgrad: the coefficient gradient dL/dc [ntypes, ntypes, n_max, n_base] (zeroed,
+ *   then accumulated) from the per-atom table W of matpl_nep_feat_op's backward modes, summed
+ *   over the atoms of each centre type type_map[i] - the grad_coeff2 / grad_coeff3 of the
+ *   reference's backward (src/op/src/CalcOps.cpp:534-538, 802-812) and the c-terms of its second
+ *   backward (:618, :956).  part 0 (radial): W [natoms, ntypes, n_base],
+ *   dc[t_i, tt, n, k] += G[i*ldG + n] * W[i, tt, k]; part 1 (angular): W [natoms, ntypes, n_max,
+ *   n_base] already contracted with G, dc[t_i] += W[i] (G unused).  Column sums in the atoms'
+ *   list order per chunk of 256 atoms, FP atomics across chunks.  err_dev gets
+ *   MATPL_KERR_BAD_TYPE for a type outside [0, ntypes).
+ */
+int matpl_nep_cgrad(int dtype, int part, int natoms, int ntypes, int n_max, int n_base,
+                    const long long *type_map, const void *G, long long ldG, const void *W,
+                    void *dc, int *err_dev, void *stream);
+
+/* matpl_nep_force_virial: forces force [natoms, 3] and per-image virial virial [nimages, 9]
+ *   (both zeroed, then accumulated) of one NEP list from dE [natoms, max_nn, 4] = dE/d(r, x, y,
+ *   z) and the rows Ri [natoms, max_nn, 4] = (r, x, y, z): what calculateNepForce with the centre
+ *   term f0 = -sum_s dE . Ri_d and calculateNepVirial's per-image sum give
+ *   (src/op/src/CalcOps.cpp:75-168, 239-330; src/model/nep_net.py:612-631) with Ri_d =
+ *   calculate_Ri(Ri) (nep_net.py:440-468) formed in registers instead of read from a
+ *   [natoms, max_nn, 4, 3] array.  Per slot f_a = dE_0 x_a / r + dE_(1+a) (slots with
+ *   |r| <= 1e-5 give 0); force[i] -= f, force[NL] += f (NL int64, < 0 empty); virial[image_of[i]]
+ *   [3a + b] += f_a x_b.  err_dev gets MATPL_KERR_BAD_COUNT for a list index >= natoms or an
+ *   image index outside [0, nimages).
+ * matpl_nep_force_virial_grad: g_dE [natoms, max_nn, 4] (written) from g_force [natoms, 3] and
+ *   g_virial [nimages, 9] (either may be NULL = zero), the transpose of the map above.
+ */
+int matpl_nep_force_virial(int dtype, int natoms, int max_nn, int nimages, const long long *NL,
+                           const long long *image_of, const void *dE, const void *Ri, void *force,
+                           void *virial, int *err_dev, void *stream);
+int matpl_nep_force_virial_grad(int dtype, int natoms, int max_nn, int nimages,
+                                const long long *NL, const long long *image_of, const void *Ri,
+                                const void *g_force, const void *g_virial, void *g_dE,
+                                int *err_dev, void *stream);
+
 /* ------------------------------------------------------------------------------------
  * LAMMPS pair style (DP).  Replaces PairMATPL::generate_neighdata
  * (src/lmps/lammps-libtorch/MATPL/pair_matpl.cpp:522-616) and the DP branch of

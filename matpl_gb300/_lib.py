@@ -79,6 +79,9 @@ SIGNATURES = {
                                   _vp, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "matpl_env_stats": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _d, _d, _vp, _vp, _vp]),
     "matpl_nep_feat_op": (_i, [_i] * 11 + [_d] + [_vp] * 5 + [_ll, _vp, _vp, _ll] + [_vp] * 4),
+    "matpl_nep_cgrad": (_i, [_i] * 6 + [_vp, _vp, _ll, _vp, _vp, _vp, _vp]),
+    "matpl_nep_force_virial": (_i, [_i] * 4 + [_vp] * 8),
+    "matpl_nep_force_virial_grad": (_i, [_i] * 4 + [_vp] * 8),
     "matpl_lammps_dp_neighbors": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _i,
                                        _vp, _vp, _vp, _vp, _vp, _vp]),
     "matpl_lammps_dp_create": (_i, [_i, _c.POINTER(MatplDpModel), _i, _vp, _i, _i,

@@ -540,6 +540,344 @@ int dispatch(bool angular, const FeatArgs &A, cudaStream_t s) {
 
 using namespace matpl;
 
+namespace matpl {
+namespace {
+
+// dL/dc [T, T, n, K] from the per-atom tables of the backward modes.  A block takes kCgAtoms
+// consecutive atoms; for each centre type t present among them it compacts their indices
+// (warp ballots, list order kept), its 8 warps split those atoms, and each lane sums kCols
+// columns (a 256-column pass: lane + 32 c) of their rows - radial G[i, nn] * W[i, tt, k],
+// angular W[i, tt, nn, k] - with the loads of all its columns in flight together.  The warps'
+// partial sums meet in shared memory and each column leaves with one atomic into dc[t] per
+// block.  The work of a block does not depend on how the types are mixed (sorted or
+// interleaved atoms cost the same).
+constexpr int kCgWarps = 8;
+constexpr int kCgAtoms = 64;
+constexpr int kCols = 8;
+constexpr int kPass = 32 * kCols;
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kCgWarps)
+nep_cgrad_kernel(int part, int natoms, int ntypes, int nmax, int K,
+                 const long long *__restrict__ type_map, const T *__restrict__ G, long long ldG,
+                 const T *__restrict__ W, T *__restrict__ dc, int *__restrict__ err) {
+    __shared__ int tsh[kCgAtoms];
+    __shared__ int idx[kCgAtoms];
+    __shared__ int wbase[kCgAtoms / 32];
+    __shared__ int cnt;
+    __shared__ T part_sum[kCgWarps][kPass];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const long long base = (long long)blockIdx.x * kCgAtoms;
+    if (threadIdx.x < kCgAtoms) {
+        const long long a = base + threadIdx.x;
+        int ta = -1;
+        if (a < natoms) {
+            const long long v = type_map[a];
+            if (v < 0 || v >= ntypes) atomicOr(err, MATPL_KERR_BAD_TYPE);
+            else ta = (int)v;
+        }
+        tsh[threadIdx.x] = ta;
+    }
+    __syncthreads();
+    const int E = ntypes * nmax * K;
+    for (int t = 0; t < ntypes; ++t) {
+        if (threadIdx.x < kCgAtoms) {
+            const bool mine = tsh[threadIdx.x] == t;
+            const unsigned bal = __ballot_sync(0xffffffffu, mine);
+            if (lane == 0) wbase[warp] = __popc(bal);
+            __syncwarp();
+            if (mine) idx[32 * warp + __popc(bal & ((1u << lane) - 1u))] = threadIdx.x;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            // close the gap between the warps' runs (list order kept)
+            int n0 = wbase[0];
+            for (int w = 1; w < kCgAtoms / 32; ++w) {
+                for (int k = 0; k < wbase[w]; ++k) idx[n0 + k] = idx[32 * w + k];
+                n0 += wbase[w];
+            }
+            cnt = n0;
+        }
+        __syncthreads();
+        const int n = cnt;
+        if (n == 0) continue;
+        for (int e0 = 0; e0 < E; e0 += kPass) {
+            T acc[kCols];
+            long long goff[kCols], woff[kCols];
+#pragma unroll
+            for (int c = 0; c < kCols; ++c) {
+                acc[c] = 0;
+                const int e = e0 + lane + 32 * c;
+                const int tt = e / (nmax * K), nn = (e / K) % nmax, k = e % K;
+                goff[c] = nn;
+                woff[c] = part == 0 ? (long long)tt * K + k : e;
+            }
+            for (int j = warp; j < n; j += kCgWarps) {
+                const long long i = base + idx[j];
+                if (part == 0) {
+                    const T *g = G + i * ldG;
+                    const T *w = W + i * ntypes * K;
+#pragma unroll
+                    for (int c = 0; c < kCols; ++c)
+                        if (e0 + lane + 32 * c < E) acc[c] += g[goff[c]] * w[woff[c]];
+                } else {
+                    const T *w = W + i * E;
+#pragma unroll
+                    for (int c = 0; c < kCols; ++c)
+                        if (e0 + lane + 32 * c < E) acc[c] += w[woff[c]];
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < kCols; ++c) part_sum[warp][lane + 32 * c] = acc[c];
+            __syncthreads();
+            const int e = e0 + threadIdx.x;
+            if (threadIdx.x < kPass && e < E) {
+                T v = 0;
+#pragma unroll
+                for (int w = 0; w < kCgWarps; ++w) v += part_sum[w][threadIdx.x];
+                atomicAdd(dc + (long long)t * E + e, v);
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Forces and per-image virial of one NEP list from dE = dE/d(r, x, y, z) [N, NN, 4] and the
+// rows Ri = (r, x, y, z) themselves (the expanded d(r, x, y, z)/d(x, y, z) of nep_net.py:440-468
+// has x_a / r in row 0 and the identity below, so it is formed in registers): per slot
+// f_a = dE_0 x_a / r + dE_(1+a) (empty slots, |r| <= 1e-5, give 0), the centre gets -f, the
+// neighbor NL +f, and the slot adds f_a r_b to the virial of the centre's image.  A block takes
+// kFvAtoms consecutive atoms, each warp kFvAtoms / 8 of them (lanes over slots, warp sums of the
+// centre force); the virial is summed per warp and then per block in shared memory, runs of one
+// image (frames are contiguous) leaving with 9 atomics, so the atomics on the few virial
+// addresses stay at one set per block.
+constexpr int kFvWarps = 8;
+constexpr int kFvAtoms = 32;
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kFvWarps)
+nep_force_virial_kernel(int natoms, int nn, int nimages, const long long *__restrict__ NL,
+                        const long long *__restrict__ image_of, const T *__restrict__ dE,
+                        const T *__restrict__ Ri, T *__restrict__ force, T *__restrict__ virial,
+                        int *__restrict__ err) {
+    __shared__ T vsh[kFvWarps][9];
+    __shared__ long long bsh[kFvWarps];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int per_warp = kFvAtoms / kFvWarps;
+    const long long a0 = (long long)blockIdx.x * kFvAtoms + (long long)warp * per_warp;
+    T v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    long long cur = -1;
+    for (int k = 0; k < per_warp; ++k) {
+        const long long i = a0 + k;
+        if (i >= natoms) break;
+        const long long b = image_of[i];
+        if (b < 0 || b >= nimages) {
+            if (lane == 0) atomicOr(err, MATPL_KERR_BAD_COUNT);
+            continue;
+        }
+        if (b != cur) {                 // a frame boundary inside the warp's atoms
+            if (cur >= 0 && lane < 9) atomicAdd(virial + 9 * cur + lane, v[0]);
+#pragma unroll
+            for (int c = 0; c < 9; ++c) v[c] = 0;
+            cur = b;
+        }
+        T fc[3] = {0, 0, 0}, vi[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int s = lane; s < nn; s += 32) {
+            const long long q = i * nn + s;
+            const T r = Ri[4 * q];
+            if (!(fabs(r) > T(1e-5))) continue;
+            const T x[3] = {Ri[4 * q + 1], Ri[4 * q + 2], Ri[4 * q + 3]};
+            const T e0 = dE[4 * q];
+            T f[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) f[c] = e0 * (x[c] / r) + dE[4 * q + 1 + c];
+            const long long j = NL[q];
+            if (j >= natoms) {
+                atomicOr(err, MATPL_KERR_BAD_COUNT);
+            } else if (j >= 0) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) atomicAdd(force + 3 * j + c, f[c]);
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                fc[c] -= f[c];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) vi[3 * c + d] += f[c] * x[d];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) fc[c] = warp_sum(fc[c]);
+        if (lane < 3) atomicAdd(force + 3 * i + lane, lane == 0 ? fc[0] : lane == 1 ? fc[1] : fc[2]);
+        // the warp's 9 virial sums, lane c < 9 keeping term c in v[0]
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {
+            const T t = warp_sum(vi[c]);
+            if (lane == c) v[0] += t;
+        }
+    }
+    if (lane < 9) vsh[warp][lane] = v[0];
+    if (lane == 0) bsh[warp] = cur;
+    __syncthreads();
+    if (threadIdx.x < 9) {
+        long long run = -1;
+        T acc = 0;
+        for (int w = 0; w < kFvWarps; ++w) {
+            const long long b = bsh[w];
+            if (b < 0) continue;
+            if (b != run) {
+                if (run >= 0) atomicAdd(virial + 9 * run + threadIdx.x, acc);
+                run = b;
+                acc = 0;
+            }
+            acc += vsh[w][threadIdx.x];
+        }
+        if (run >= 0) atomicAdd(virial + 9 * run + threadIdx.x, acc);
+    }
+}
+
+// The gradient of the kernel above (linear in dE): per slot u_a = gF[NL]_a - gF[i]_a +
+// sum_b gV[image(i)][a][b] r_b, then gdE = (sum_a u_a x_a / r, u_0, u_1, u_2); empty slots 0.
+// One thread per slot; gF or gV may be absent (zero).
+template <typename T>
+__global__ void __launch_bounds__(256)
+nep_force_virial_grad_kernel(int natoms, int nn, int nimages, const long long *__restrict__ NL,
+                             const long long *__restrict__ image_of, const T *__restrict__ Ri,
+                             const T *__restrict__ gF, const T *__restrict__ gV,
+                             T *__restrict__ gdE, int *__restrict__ err) {
+    const long long total = (long long)natoms * nn;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+         q += (long long)gridDim.x * blockDim.x) {
+        const long long i = q / nn;
+        const T r = Ri[4 * q];
+        T g[4] = {0, 0, 0, 0};
+        if (fabs(r) > T(1e-5)) {
+            const T x[3] = {Ri[4 * q + 1], Ri[4 * q + 2], Ri[4 * q + 3]};
+            T u[3] = {0, 0, 0};
+            if (gF) {
+                const long long j = NL[q];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) u[a] = -gF[3 * i + a];
+                if (j >= natoms) {
+                    atomicOr(err, MATPL_KERR_BAD_COUNT);
+                } else if (j >= 0) {
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) u[a] += gF[3 * j + a];
+                }
+            }
+            if (gV) {
+                const long long b = image_of[i];
+                if (b < 0 || b >= nimages) {
+                    atomicOr(err, MATPL_KERR_BAD_COUNT);
+                } else {
+#pragma unroll
+                    for (int a = 0; a < 3; ++a)
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) u[a] += gV[9 * b + 3 * a + c] * x[c];
+                }
+            }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                g[0] += u[a] * (x[a] / r);
+                g[1 + a] = u[a];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) gdE[4 * q + c] = g[c];
+    }
+}
+
+}  // namespace
+}  // namespace matpl
+
+extern "C" int matpl_nep_cgrad(int dtype, int part, int natoms, int ntypes, int n_max, int n_base,
+                               const long long *type_map, const void *G, long long ldG,
+                               const void *W, void *dc, int *err_dev, void *stream) {
+    MATPL_REQUIRE(dtype == MATPL_F32 || dtype == MATPL_F64, MATPL_ERR_DTYPE,
+                  "matpl_nep_cgrad: dtype is MATPL_F32 or MATPL_F64");
+    MATPL_REQUIRE(part == 0 || part == 1, MATPL_ERR_INVALID, "part: 0 radial, 1 angular");
+    MATPL_REQUIRE(natoms >= 0 && ntypes >= 1 && n_max >= 1 && n_base >= 1, MATPL_ERR_INVALID,
+                  "bad sizes");
+    MATPL_REQUIRE(part == 1 || ldG >= n_max, MATPL_ERR_INVALID, "radial: ldG >= n_max");
+    MATPL_REQUIRE(dc && err_dev && (natoms == 0 || (type_map && W && (part == 1 || G))),
+                  MATPL_ERR_INVALID, "null pointer argument");
+    cudaStream_t s = as_stream(stream);
+    const size_t esz = dtype == MATPL_F64 ? sizeof(double) : sizeof(float);
+    const size_t nout = (size_t)ntypes * ntypes * n_max * n_base;
+    if (cudaMemsetAsync(dc, 0, esz * nout, s) != cudaSuccess) {
+        set_error("matpl_nep_cgrad: memset failed");
+        return MATPL_ERR_CUDA;
+    }
+    if (natoms == 0) return MATPL_OK;
+    ProfScope ps("nep_cgrad", s);
+    const int grid = (int)((natoms + kCgAtoms - 1) / kCgAtoms);
+    if (dtype == MATPL_F64)
+        nep_cgrad_kernel<double><<<grid, 32 * kCgWarps, 0, s>>>(
+            part, natoms, ntypes, n_max, n_base, type_map, (const double *)G, ldG,
+            (const double *)W, (double *)dc, err_dev);
+    else
+        nep_cgrad_kernel<float><<<grid, 32 * kCgWarps, 0, s>>>(
+            part, natoms, ntypes, n_max, n_base, type_map, (const float *)G, ldG,
+            (const float *)W, (float *)dc, err_dev);
+    return check_launch("matpl_nep_cgrad");
+}
+
+extern "C" int matpl_nep_force_virial(int dtype, int natoms, int max_nn, int nimages,
+                                      const long long *NL, const long long *image_of,
+                                      const void *dE, const void *Ri, void *force, void *virial,
+                                      int *err_dev, void *stream) {
+    MATPL_REQUIRE(dtype == MATPL_F32 || dtype == MATPL_F64, MATPL_ERR_DTYPE,
+                  "matpl_nep_force_virial: dtype is MATPL_F32 or MATPL_F64");
+    MATPL_REQUIRE(natoms >= 0 && max_nn >= 0 && nimages >= 1, MATPL_ERR_INVALID, "bad sizes");
+    MATPL_REQUIRE(force && virial && err_dev &&
+                      (natoms * (long long)max_nn == 0 || (NL && image_of && dE && Ri)),
+                  MATPL_ERR_INVALID, "null pointer argument");
+    cudaStream_t s = as_stream(stream);
+    const size_t esz = dtype == MATPL_F64 ? sizeof(double) : sizeof(float);
+    if (cudaMemsetAsync(force, 0, esz * 3 * (size_t)natoms, s) != cudaSuccess ||
+        cudaMemsetAsync(virial, 0, esz * 9 * (size_t)nimages, s) != cudaSuccess) {
+        set_error("matpl_nep_force_virial: memset failed");
+        return MATPL_ERR_CUDA;
+    }
+    if (natoms == 0 || max_nn == 0) return MATPL_OK;
+    ProfScope ps("nep_force_virial", s);
+    const int grid = (int)((natoms + kFvAtoms - 1) / kFvAtoms);
+    if (dtype == MATPL_F64)
+        nep_force_virial_kernel<double><<<grid, 32 * kFvWarps, 0, s>>>(
+            natoms, max_nn, nimages, NL, image_of, (const double *)dE, (const double *)Ri,
+            (double *)force, (double *)virial, err_dev);
+    else
+        nep_force_virial_kernel<float><<<grid, 32 * kFvWarps, 0, s>>>(
+            natoms, max_nn, nimages, NL, image_of, (const float *)dE, (const float *)Ri,
+            (float *)force, (float *)virial, err_dev);
+    return check_launch("matpl_nep_force_virial");
+}
+
+extern "C" int matpl_nep_force_virial_grad(int dtype, int natoms, int max_nn, int nimages,
+                                           const long long *NL, const long long *image_of,
+                                           const void *Ri, const void *g_force,
+                                           const void *g_virial, void *g_dE, int *err_dev,
+                                           void *stream) {
+    MATPL_REQUIRE(dtype == MATPL_F32 || dtype == MATPL_F64, MATPL_ERR_DTYPE,
+                  "matpl_nep_force_virial_grad: dtype is MATPL_F32 or MATPL_F64");
+    MATPL_REQUIRE(natoms >= 0 && max_nn >= 0 && nimages >= 1, MATPL_ERR_INVALID, "bad sizes");
+    MATPL_REQUIRE(err_dev && (natoms * (long long)max_nn == 0 || (NL && image_of && Ri && g_dE)),
+                  MATPL_ERR_INVALID, "null pointer argument");
+    const long long total = (long long)natoms * max_nn;
+    if (total == 0) return MATPL_OK;
+    cudaStream_t s = as_stream(stream);
+    ProfScope ps("nep_force_virial_grad", s);
+    const int grid = (int)std::min<long long>((total + 255) / 256, 152LL * 16);
+    if (dtype == MATPL_F64)
+        nep_force_virial_grad_kernel<double><<<grid, 256, 0, s>>>(
+            natoms, max_nn, nimages, NL, image_of, (const double *)Ri, (const double *)g_force,
+            (const double *)g_virial, (double *)g_dE, err_dev);
+    else
+        nep_force_virial_grad_kernel<float><<<grid, 256, 0, s>>>(
+            natoms, max_nn, nimages, NL, image_of, (const float *)Ri, (const float *)g_force,
+            (const float *)g_virial, (float *)g_dE, err_dev);
+    return check_launch("matpl_nep_force_virial_grad");
+}
+
 extern "C" int matpl_nep_feat_op(int dtype, int part, int mode, int natoms, int max_nn,
                                  int ntypes, int n_max, int n_base, int l_max_3b, int l_max_4b,
                                  int l_max_5b, double cutoff, const void *coeff, const void *d12,

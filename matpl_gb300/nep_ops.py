@@ -100,15 +100,23 @@ def _feat_call(part, mode, coeff, d12, NL, atom_map, rc, l3=0, l4=0, l5=0, G=Non
 
 
 def _c_grad(part, W, G, atom_map, T):
-    """dL/dc [T, T, n, K] from the per-atom tables: radial sum_i G[i, n] W[i, t, k]; angular
-    sum_i W[i] (G already folded in), each into row t_i."""
-    tm = atom_map.long()
+    """dL/dc [T, T, n, K] from the per-atom tables (``matpl_nep_cgrad``): radial
+    sum_i G[i, n] W[i, t, k]; angular sum_i W[i] (G already folded in), each into row t_i."""
+    dev, dt = W.device, W.dtype
+    N = W.shape[0]
     if part == PART_RADIAL:
-        per = torch.einsum("in,itk->itnk", G.to(W.dtype), W)
+        _, Tt, K = W.shape
+        Gc = G.detach().to(dt).contiguous()
+        n = Gc.shape[1]
     else:
-        per = W
-    out = torch.zeros((T,) + tuple(per.shape[1:]), dtype=W.dtype, device=W.device)
-    return out.index_add_(0, tm, per)
+        _, Tt, n, K = W.shape
+        Gc = None
+    out = torch.empty(T, Tt, n, K, dtype=dt, device=dev)
+    tm = atom_map.contiguous().to(torch.int64)
+    check(_lib.load().matpl_nep_cgrad(_dtype_code(W), part, N, T, n, K, ptr(tm), ptr(Gc),
+                                      n, ptr(W.contiguous()), ptr(out), ptr(_err_word(dev)),
+                                      _stream(dev)), "matpl_nep_cgrad")
+    return out
 
 
 class _NepFeatGrad(torch.autograd.Function):
@@ -194,6 +202,53 @@ def _image_index(counts, dev):
             _img_cache.clear()
         _img_cache[key] = t
     return t
+
+
+class _NepForceVirial(torch.autograd.Function):
+    """Forces [N, 3] and per-image virial [B, 9] of one list (``matpl_nep_force_virial``);
+    linear in dE, its backward (``matpl_nep_force_virial_grad``) is the transpose map."""
+
+    @staticmethod
+    def forward(ctx, NL, dE, Ri, image_of, nimages):
+        N, NN = NL.shape
+        dev, dt = dE.device, dE.dtype
+        nl = NL.contiguous().to(torch.int64)
+        R = Ri.detach().to(dt).contiguous()
+        F = torch.empty(N, 3, dtype=dt, device=dev)
+        V = torch.empty(nimages, 9, dtype=dt, device=dev)
+        check(_lib.load().matpl_nep_force_virial(
+            _dtype_code(dE), N, NN, nimages, ptr(nl), ptr(image_of), ptr(dE.contiguous()),
+            ptr(R), ptr(F), ptr(V), ptr(_err_word(dev)), _stream(dev)), "matpl_nep_force_virial")
+        ctx.save_for_backward(nl, R, image_of)
+        ctx.nimages = nimages
+        return F, V
+
+    @staticmethod
+    @torch.autograd.function.once_differentiable
+    def backward(ctx, gF, gV):
+        nl, R, image_of = ctx.saved_tensors
+        N, NN = nl.shape
+        gdE = torch.empty(N, NN, 4, dtype=R.dtype, device=R.device)
+        gFc = gF.contiguous().to(R.dtype) if gF is not None else None
+        gVc = gV.contiguous().to(R.dtype) if gV is not None else None
+        check(_lib.load().matpl_nep_force_virial_grad(
+            _dtype_code(R), N, NN, ctx.nimages, ptr(nl), ptr(image_of), ptr(R), ptr(gFc),
+            ptr(gVc), ptr(gdE), ptr(_err_word(R.device)), _stream(R.device)),
+            "matpl_nep_force_virial_grad")
+        return None, gdE, None, None, None
+
+
+def nep_force_virial(NL: torch.Tensor, dE: torch.Tensor, Ri: torch.Tensor, num_atom
+                     ) -> List[torch.Tensor]:
+    """[force [N, 3], virial [B, 9]] of one list: calculateNepForce with the centre term
+    -sum_s dE . Ri_d and calculateNepVirial's per-image sum, with Ri_d = calculate_Ri(Ri)
+    formed in the kernel (frames contiguous with sizes ``num_atom``); differentiable in dE."""
+    _require_cuda(NL, dE, Ri)
+    counts = tuple(int(c) for c in np.asarray(num_atom).reshape(-1)) \
+        if not torch.is_tensor(num_atom) else tuple(int(c) for c in num_atom.reshape(-1).tolist())
+    img = _image_index(counts, dE.device)
+    F, V = _NepForceVirial.apply(NL, dE, Ri, img, len(counts))
+    return [F, V]
 
 
 class _NepVirial(torch.autograd.Function):

@@ -5,14 +5,16 @@
 ``fitting_net.{t}.layers.{0,1}.weight / bias``, buffer ``q_scaler``), so reference checkpoints
 load unchanged, and its forward takes the lists of ``calculate_neighbor``.  The descriptor runs
 ``calculateNepFeat`` / ``calculateNepMbFeat`` (csrc/nep_train.cu: the forward, backward and
-second backward that the force loss needs), forces and virial ``calculateNepForce`` /
-``calculateNepVirial``; with ``create_graph`` forces, ``loss.backward()`` of an energy + force +
-virial loss reaches every parameter exactly like the reference's training step
-(nep_trainer.py), through the hand-written second derivatives instead of autograd over the
-descriptor.  The per-element FittingNet (one tanh layer, nep_fitting.py:136-160) stays in
-torch: it is a few small GEMMs per element.
+second backward that the force loss needs, and the coefficient gradient); forces and virial run
+``nep_force_virial``, the kernel form of calculate_Ri + calculateNepForce + calculateNepVirial
+that reads the rows (r, x, y, z) and forms d(r, x, y, z)/d(x, y, z) in registers.  With
+``create_graph`` forces, ``loss.backward()`` of an energy + force + virial loss reaches every
+parameter exactly like the reference's training step (nep_trainer.py), through the hand-written
+second derivatives instead of autograd over the descriptor.  The per-element FittingNet (one
+tanh layer, nep_fitting.py:136-160) stays in torch, all elements in one product
+(``calculate_Ei``).
 """
-from typing import Dict, List, Optional
+from typing import Dict, Optional
 
 import torch
 
@@ -39,14 +41,88 @@ class _FittingNet(torch.nn.Module):
 
 def calculate_Ri(Ri: torch.Tensor) -> torch.Tensor:
     """[N, NN, 4, 3] d(r, x, y, z)/d(x, y, z) of the non-empty slots (nep_net.py:440-468)."""
-    N, NN = Ri.shape[:2]
-    mask = (Ri[:, :, 0].abs() > 1e-5).to(Ri.dtype)
-    safe = torch.where(mask > 0, Ri[:, :, 0], torch.ones_like(Ri[:, :, 0]))
-    d = torch.zeros(N, NN, 4, 3, dtype=Ri.dtype, device=Ri.device)
-    for a in range(3):
-        d[:, :, 0, a] = Ri[:, :, 1 + a] / safe * mask
-        d[:, :, 1 + a, a] = mask
-    return d
+    mask = (Ri[:, :, 0:1].abs() > 1e-5).to(Ri.dtype)
+    safe = torch.where(mask > 0, Ri[:, :, 0:1], torch.ones_like(mask))
+    eye = torch.eye(3, dtype=Ri.dtype, device=Ri.device)
+    return torch.cat(((Ri[:, :, 1:] / safe * mask).unsqueeze(2), eye * mask.unsqueeze(-1)), 2)
+
+
+def _mm_impl(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+    """a [M, K] @ b [K, N].  A long contraction onto few outputs (the weight and bias gradients
+    of the fitting net, K = atoms) goes as S partial products of about 1024 atoms in one
+    batched launch plus their sum: the work spreads over the SMs instead of the handful of
+    output tiles a single GEMM of that shape gets."""
+    M, K = a.shape
+    N = b.shape[1]
+    if K < 8192 or M * N > 256 * 256:
+        return a @ b
+    S = min(64, K // 1024)
+    c = K // S
+    K0 = S * c
+    out = torch.bmm(a[:, :K0].reshape(M, S, c).transpose(0, 1), b[:K0].reshape(S, c, N)).sum(0)
+    if K0 < K:
+        out = out + a[:, K0:] @ b[K0:]
+    return out
+
+
+class _MM(torch.autograd.Function):
+    """Matrix product through ``_mm_impl`` in the forward and every order of backward."""
+
+    @staticmethod
+    def forward(ctx, a, b):
+        ctx.save_for_backward(a, b)
+        return _mm_impl(a, b)
+
+    @staticmethod
+    def backward(ctx, g):
+        a, b = ctx.saved_tensors
+        ga = _MM.apply(g, b.t()) if ctx.needs_input_grad[0] else None
+        gb = _MM.apply(a.t(), g) if ctx.needs_input_grad[1] else None
+        return ga, gb
+
+
+_ones_rows = {}
+
+
+def _ones_row(n, dev, dt):
+    key = (n, dev, dt)
+    t = _ones_rows.get(key)
+    if t is None:
+        if len(_ones_rows) > 16:
+            _ones_rows.clear()
+        t = _ones_rows[key] = torch.ones(1, n, dtype=dt, device=dev)
+    return t
+
+
+class _AddRow(torch.autograd.Function):
+    """z [N, F] + b [F]; the gradient of b, a sum over the N rows, as ones[1, N] @ g through
+    ``_MM`` (differentiable again)."""
+
+    @staticmethod
+    def forward(ctx, z, b):
+        ctx.n = z.shape[0]
+        return z + b
+
+    @staticmethod
+    def backward(ctx, g):
+        gb = None
+        if ctx.needs_input_grad[1]:
+            gb = _MM.apply(_ones_row(ctx.n, g.device, g.dtype), g).reshape(-1)
+        return g, gb
+
+
+def _image_sum(x: torch.Tensor, counts) -> torch.Tensor:
+    """Per-image sums [B, ...] of per-atom rows x [N, ...] (frames contiguous, sizes
+    ``counts``): one reduction when the frames have one size (batches of one composition),
+    else an index_add over the atoms' image index."""
+    B = len(counts)
+    if B == 1:
+        return x.sum(0, keepdim=True)
+    if all(c == counts[0] for c in counts):
+        return x.reshape((B, counts[0]) + tuple(x.shape[1:])).sum(1)
+    img = nep_ops._image_index(tuple(counts), x.device)
+    return torch.zeros((B,) + tuple(x.shape[1:]), dtype=x.dtype,
+                       device=x.device).index_add(0, img, x)
 
 
 class NEPTrain(torch.nn.Module):
@@ -66,27 +142,39 @@ class NEPTrain(torch.nn.Module):
             self.fitting_net.append(_FittingNet([_Layer(p[pre + "0.weight"], p[pre + "0.bias"]),
                                                  _Layer(p[pre + "1.weight"], p[pre + "1.bias"])]))
         self.register_buffer("q_scaler", p["q_scaler"].clone())
+        H = p["fitting_net.0.layers.0.weight"].shape[1]
+        blocks = torch.eye(cfg.ntypes, dtype=dtype, device=dev).repeat_interleave(H, 0)
+        self.register_buffer("fit_blocks", blocks, persistent=False)              # [T*H, T]
 
-    def type_index(self, type_map: torch.Tensor) -> List[torch.Tensor]:
-        """Atom indices of every element (one device sync); pass it to ``forward`` to keep the
-        step free of host synchronisation (CUDA-graph capture)."""
-        tm = type_map.reshape(-1).long()
-        return [torch.nonzero(tm == t).flatten() for t in range(self.cfg.ntypes)]
+    def type_index(self, type_map: torch.Tensor) -> torch.Tensor:
+        """[N, T] one-hot centre type of every atom (no host synchronisation); ``forward`` makes
+        it when none is passed."""
+        tm = type_map.reshape(-1, 1).long()
+        return (tm == torch.arange(self.cfg.ntypes, device=tm.device)).to(self.q_scaler.dtype)
 
     def calculate_Ei(self, type_map: torch.Tensor, feats: torch.Tensor,
-                     type_index: Optional[List[torch.Tensor]] = None) -> torch.Tensor:
-        Ei = torch.zeros(type_map.shape[0], dtype=feats.dtype, device=feats.device)
-        idxs = type_index if type_index is not None else self.type_index(type_map)
-        for idx, net in zip(idxs, self.fitting_net):     # nep_net.py:470-501
-            if idx.numel() == 0:
-                continue
-            Ei = Ei.index_put((idx,), net(feats[idx]).squeeze(-1))
-        return Ei
+                     type_index: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """Ei [N]: each atom through its element's FittingNet (nep_net.py:470-501).  All T nets
+        run on all atoms as one [N, F] x [F, T*H] product and each atom keeps its own net's
+        output through the one-hot type: a few well-shaped launches (and their backward and
+        double backward) in place of per-element gathers, small GEMMs and scatters; the other
+        elements' outputs are multiplied by zero, so every parameter's gradient is that of the
+        per-element evaluation."""
+        onehot = type_index if type_index is not None else self.type_index(type_map)
+        nets = self.fitting_net
+        W0 = torch.cat([net.layers[0].weight for net in nets], 1)                 # [F, T*H]
+        b0 = torch.cat([net.layers[0].bias.reshape(-1) for net in nets])          # [T*H]
+        # output layers as one block-diagonal [T*H, T] matrix
+        W1 = torch.cat([net.layers[1].weight for net in nets], 0) * self.fit_blocks
+        b1 = torch.cat([net.layers[1].bias.reshape(-1) for net in nets])          # [T]
+        h = torch.tanh(_AddRow.apply(_MM.apply(feats, W0), b0))
+        y = _AddRow.apply(_MM.apply(h, W1), b1)                                   # [N, T]
+        return (y * onehot).sum(-1)
 
     def forward(self, NN_radial, NL_radial, Ri_radial, NN_angular, NL_angular, Ri_angular,
                 num_atom, atom_type_map, Egroup_weight: Optional[torch.Tensor] = None,
                 divider: Optional[torch.Tensor] = None, is_calc_f: bool = True,
-                type_index: Optional[List[torch.Tensor]] = None):
+                type_index: Optional[torch.Tensor] = None):
         cfg = self.cfg
         dt = self.q_scaler.dtype
         tm = atom_type_map.reshape(-1).long()
@@ -106,8 +194,8 @@ class NEPTrain(torch.nn.Module):
                 cfg.two_feat_num, *cfg.l_max, cfg.cutoff[1])[0])
         feats = torch.cat(feats, -1)
         Ei = self.calculate_Ei(tm, self.q_scaler * feats, type_index)
-        counts = num_atom.reshape(-1).tolist()
-        Etot = torch.stack([e.sum() for e in Ei.split(counts)]).unsqueeze(-1)
+        counts = tuple(int(c) for c in num_atom.reshape(-1).tolist())
+        Etot = _image_sum(Ei, counts).unsqueeze(-1)
         Egroup = None
         if Egroup_weight is not None and divider is not None:
             Egroup = torch.divide(torch.matmul(Egroup_weight, Ei.unsqueeze(-1)).squeeze(-1), divider)
@@ -120,14 +208,14 @@ class NEPTrain(torch.nn.Module):
                                     create_graph=True, allow_unused=True)
         Force = torch.zeros(N, 3, dtype=dt, device=Ri.device)
         Virial = torch.zeros(len(counts), 9, dtype=dt, device=Ri.device)
-        na = num_atom.reshape(-1)
         for dE, (R, NL) in zip(grads, leaves):        # nep_net.py:612-631
             if dE is None:
                 continue
-            Rd = calculate_Ri(R.detach())
-            f0 = -torch.matmul(dE.reshape(N, 1, -1), Rd.reshape(N, -1, 3)).squeeze(-2)
-            Force = Force + nep_ops.calculateNepForce(NL, dE, Rd, f0)[0]
-            Virial = Virial + nep_ops.calculateNepVirial(NL, dE, R.detach()[:, :, 1:], Rd, na)[0]
+            # calculateNepForce + calculateNepVirial of the list with calculate_Ri formed in the
+            # kernel (one pass over the slots, no [N, NN, 4, 3] array)
+            F_l, V_l = nep_ops.nep_force_virial(NL, dE, R.detach(), counts)
+            Force = Force + F_l
+            Virial = Virial + V_l
         return Etot, Ei, -Force, Egroup, -Virial
 
 

@@ -165,8 +165,8 @@ def test_graphed_step_equals_eager_step(nep_case):
          "Etot": dev(rng.standard_normal(B)), "Force": dev(rng.standard_normal((N, 3))),
          "Virial": dev(rng.standard_normal((B, 9)))}
     m1, m2 = nep_train_model(c), nep_train_model(c)
-    o1 = torch.optim.Adam(m1.parameters(), lr=1e-3, capturable=True)
-    o2 = torch.optim.Adam(m2.parameters(), lr=1e-3, capturable=True)
+    o1 = torch.optim.Adam(m1.parameters(), lr=1e-3, capturable=True, fused=True)
+    o2 = torch.optim.Adam(m2.parameters(), lr=1e-3, capturable=True, fused=True)
     t1 = GraphedNepTrainer(m1, o1, w_v=0.1, warmup=1)
     t2 = GraphedNepTrainer(m2, o2, w_v=0.1, warmup=1)
     try:
@@ -183,3 +183,28 @@ def test_graphed_step_equals_eager_step(nep_case):
     for (k, a), (_, bb) in zip(m1.named_parameters(), m2.named_parameters()):
         close(a, bb.detach().cpu().numpy(), 1e-10)
     assert torch.isfinite(l1).all()
+
+
+@pytest.mark.parametrize("case", ["nep_q4_tri2", "nep_hfo_l4"])
+def test_force_virial_kernel_equals_public_ops(nep_case, case):
+    """nep_force_virial (Ri_d formed in the kernel) = calculate_Ri + calculateNepForce with the
+    centre term + calculateNepVirial, values and the gradient in dE, for both lists."""
+    from matpl_gb300.nep_train import calculate_Ri
+    c = nep_case(case)
+    na = np.asarray(c.g["num_atom"]).reshape(-1)
+    for k, (NL, R) in enumerate(((c.NL_r, c.Ri_r), (c.NL_a, c.Ri_a))):
+        N, NN = NL.shape
+        R, NLd = dev(R), dev(NL)
+        dE = dev(seeded(11 + k, (N, NN, 4))).requires_grad_()
+        F, V = nep_ops.nep_force_virial(NLd, dE, R, na)
+        Rd = calculate_Ri(R)
+        f0 = -torch.matmul(dE.reshape(N, 1, -1), Rd.reshape(N, -1, 3)).squeeze(-2)
+        F2 = nep_ops.calculateNepForce(NLd, dE, Rd, f0)[0]
+        V2 = nep_ops.calculateNepVirial(NLd, dE, R[:, :, 1:], Rd, torch.tensor(na))[0]
+        close(F, F2.detach().cpu().numpy(), 1e-13)
+        close(V, V2.detach().cpu().numpy(), 1e-13)
+        gF, gV = dev(seeded(21 + k, (N, 3))), dev(seeded(31 + k, (len(na), 9)))
+        g1 = torch.autograd.grad((F * gF).sum() + (V * gV).sum(), dE)[0]
+        g2 = torch.autograd.grad((F2 * gF).sum() + (V2 * gV).sum(), dE)[0]
+        close(g1, g2.cpu().numpy(), 1e-13)
+    nep_ops.check_errors()
