@@ -587,8 +587,10 @@ def run_nep_train(args, ws, local, steps, warmup):
                                       "loss": loss32},
                        "eager_fp64": {"ms_per_step": ms64, "value": ws * N / (ms64 * 1e-3),
                                       "loss": loss64},
-                       "form": "autograd over this library's operators (the reference's op "
-                               "structure)"},
+                       "form": "autograd over this library's operators in the reference's op "
+                               "structure; the force path takes the descriptor's d12 gradient "
+                               "alone, forces and virial in one kernel reading the (r, x, y, z) "
+                               "rows, all elements' fitting nets in one product"},
             "kernels": per_kernel}
 
 

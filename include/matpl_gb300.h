@@ -329,7 +329,9 @@ int matpl_env_stats(int batch, int natoms, int nslots, int ntypes, const int32_t
  *                    (partials in the four columns; caller zero-fills) and W, zero-filled by
  *                    the caller: radial [N, T, n_base] = sum over neighbors of type t of
  *                    f_k(r) (dL/dc[t_i, t, n, k] = sum_i G[i, n] W[i, t, k]); angular
- *                    [N, T, n_max, n_base] (dL/dc[t_i] = sum_i W[i]).
+ *                    [N, T, n_max, n_base] (dL/dc[t_i] = sum_i W[i]).  Either output may be
+ *                    NULL (not computed): the force path needs grad_d12 alone, the energy
+ *                    path's coefficient gradient W alone.
  * mode 2 (second backward): for H [N, max_nn, 4] = dL/d(grad_d12) writes q = dq/dd12 . H
  *                    [N, ldQ] (= dL/dG) and W as in mode 1 for dL/dc (radial: sum of
  *                    H_r f_k'(r), to be contracted with G).

@@ -5,8 +5,8 @@
 // For a descriptor q(c, d12) of one list (d12 [N, NN, 4] = (r, x, y, z) of every slot, c the
 // coefficients [T, T, n, K]) and the features' gradient G = dL/dq [N, F]:
 //   FWD   q [N, F]
-//   BWD   grad_d12 = G . dq/dd12 [N, NN, 4] and W, from which dL/dc follows by a sum over the
-//         atoms of each centre type (the caller's index_add):
+//   BWD   grad_d12 = G . dq/dd12 [N, NN, 4] and W (either may be skipped), from which dL/dc
+//         follows by a sum over the atoms of each centre type (matpl_nep_cgrad):
 //           radial   W [N, T, K] = sum over neighbors j of type t of f_k(r_ij),
 //                    dL/dc[ti, t, n, k] = sum_i G[i, n] W[i, t, k];
 //           angular  W [N, T, n, K] = sum_j of type t of f_k(r_ij) sum_m Sbar_nm b_m(r_ij),
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(32 * kFeatWarps) nep2b_op(FeatArgs A) {
                         acc[n] += g;
                     }
             } else if (MODE == kBwd) {
-                if (use) {
+                if (use && A.grad_d12) {
                     T gp = T(0);
 #pragma unroll
                     for (int n = 0; n < NM; ++n) {
@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(32 * kFeatWarps) nep2b_op(FeatArgs A) {
                 for (int k = 0; k < KM; ++k) s_st[wib][lane][k] = use ? h0 * df[k] : T(0);
                 s_tj[wib][lane] = use ? tj : -1;
             }
-            if (MODE != kFwd) {
+            if (MODE == kBwd2 || (MODE == kBwd && A.W)) {
                 __syncwarp();
                 T *W = static_cast<T *>(A.W) + i * (long long)T_ * K;
                 for (int e = lane; e < T_ * K; e += 32) {
@@ -407,8 +407,9 @@ __global__ void __launch_bounds__(32 * kFeatWarps) nepmb_op(FeatArgs A) {
             if (MODE == kBwd2) S.sbd[n][m] = sbar_dot<T>(m, S.s[n], S.sd[n], g3, g4, g5, four, five);
         }
         __syncwarp();
-        // ---- pass 2: grad_d12 (BWD) and the per-atom c-gradient table W
-        T *W = static_cast<T *>(A.W) + i * (long long)T_ * n_ * K;
+        // ---- pass 2: grad_d12 (BWD) and the per-atom c-gradient table W (either may be
+        // skipped in BWD: null pointer)
+        T *W = A.W ? static_cast<T *>(A.W) + i * (long long)T_ * n_ * K : nullptr;
         for (int base = 0; base < nvalid; base += 32) {
             const int slot = base + lane;
             const long long ps = i * A.nn + slot;
@@ -418,7 +419,21 @@ __global__ void __launch_bounds__(32 * kFeatWarps) nepmb_op(FeatArgs A) {
             T f[KM], df[KM], g[NM], gp[NM], ux, uy, uz, ri;
             const T *cr = c + ((long long)(ti * T_ + (ok ? tj : 0)) * n_) * K;
             mb_pair<T, NM, KM>(A, cr, ok ? ps : 0, f, df, g, gp, ux, uy, uz, ri);
-            if (MODE == kBwd) {
+            if (MODE == kBwd && !A.grad_d12) {
+                // c-gradient only: B_n = sum_m Sbar_nm b_m
+                T Bn[NM];
+#pragma unroll
+                for (int n = 0; n < NM; ++n) Bn[n] = T(0);
+#pragma unroll
+                for (int m = 0; m < 24; ++m) {
+                    T b, br, bx, by, bz;
+                    harm_d<T>(m, ux, uy, uz, ri, b, br, bx, by, bz);
+#pragma unroll
+                    for (int n = 0; n < NM; ++n) Bn[n] += (n < n_ ? S.sb[n][m] : T(0)) * b;
+                }
+#pragma unroll
+                for (int n = 0; n < NM; ++n) S.ga[lane][n] = ok ? Bn[n] : T(0);
+            } else if (MODE == kBwd) {
                 T Bn[NM], Br[NM], Bx[NM], By[NM], Bz[NM];
 #pragma unroll
                 for (int n = 0; n < NM; ++n) Bn[n] = Br[n] = Bx[n] = By[n] = Bz[n] = T(0);
@@ -482,6 +497,7 @@ __global__ void __launch_bounds__(32 * kFeatWarps) nepmb_op(FeatArgs A) {
                     S.gb[lane][n] = ok ? Q[n] : T(0);
                 }
             }
+            if (MODE == kBwd && !A.W) continue;     // grad_d12 only
 #pragma unroll
             for (int k = 0; k < KM; ++k) {
                 S.fa[lane][k] = ok ? f[k] : T(0);
@@ -898,8 +914,8 @@ extern "C" int matpl_nep_feat_op(int dtype, int part, int mode, int natoms, int 
     MATPL_REQUIRE(err_dev && coeff && type_map && (natoms == 0 || (d12 && NL)), MATPL_ERR_INVALID,
                   "null pointer argument");
     MATPL_REQUIRE(mode != 0 || q, MATPL_ERR_INVALID, "fwd needs q");
-    MATPL_REQUIRE(mode != 1 || (G && W && (grad_d12 || natoms == 0)), MATPL_ERR_INVALID,
-                  "bwd needs G, grad_d12, W");
+    MATPL_REQUIRE(mode != 1 || (G && (W || grad_d12)), MATPL_ERR_INVALID,
+                  "bwd needs G and grad_d12 or W");
     MATPL_REQUIRE(mode != 2 || (G && H && q && W), MATPL_ERR_INVALID, "bwd2 needs G, H, gso, W");
     if (natoms == 0 || max_nn == 0) return MATPL_OK;
     FeatArgs A{};

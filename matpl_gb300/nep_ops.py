@@ -64,8 +64,10 @@ def _nfeat(part, nmax, l3, l4, l5):
     return nmax * (l3 + (1 if l4 > 0 else 0) + (1 if l5 > 0 else 0))
 
 
-def _feat_call(part, mode, coeff, d12, NL, atom_map, rc, l3=0, l4=0, l5=0, G=None, H=None):
-    """One launch of ``matpl_nep_feat_op``; returns (q or gso, grad_d12, W)."""
+def _feat_call(part, mode, coeff, d12, NL, atom_map, rc, l3=0, l4=0, l5=0, G=None, H=None,
+               want_d=True, want_c=True):
+    """One launch of ``matpl_nep_feat_op``; returns (q or gso, grad_d12, W).  In the backward
+    mode ``want_d`` / ``want_c`` select grad_d12 and the c-gradient table (None if not)."""
     _require_cuda(coeff, d12, NL, atom_map)
     N, NN = NL.shape
     T, _, nmax, K = coeff.shape
@@ -85,9 +87,9 @@ def _feat_call(part, mode, coeff, d12, NL, atom_map, rc, l3=0, l4=0, l5=0, G=Non
             torch.zeros(N, F, dtype=dt, device=dev)
         if N * NN == 0:
             q.zero_()
-    if mode == MODE_BWD:
+    if mode == MODE_BWD and want_d:
         gd = torch.zeros(N, NN, 4, dtype=dt, device=dev)
-    if mode != MODE_FWD:
+    if mode == MODE_BWD2 or (mode == MODE_BWD and want_c):
         shape = (N, T, K) if part == PART_RADIAL else (N, T, nmax, K)
         W = torch.zeros(shape, dtype=dt, device=dev)
     check(_lib.load().matpl_nep_feat_op(
@@ -119,7 +121,20 @@ def _c_grad(part, W, G, atom_map, T):
     return out
 
 
+def _second_backward(ctx, g_gd):
+    """Gradients (G, coeff) of grad_d12 = G . dq/dd12 for its upstream gradient g_gd: the
+    second backward mode (gso = dq/dd12 . g_gd, and the c-terms)."""
+    G, coeff, d12, NL, atom_map = ctx.saved_tensors
+    part, rc, l3, l4, l5 = ctx.meta
+    gso, _, W2 = _feat_call(part, MODE_BWD2, coeff, d12, NL, atom_map, rc, l3, l4, l5,
+                            G=G, H=g_gd)
+    gsc = _c_grad(part, W2, G.detach(), atom_map, coeff.shape[0]).to(coeff.dtype)
+    return gso.to(G.dtype), gsc
+
+
 class _NepFeatGrad(torch.autograd.Function):
+    """(dL/dc, grad_d12) of the features for G = dL/dq; differentiable in G and c."""
+
     @staticmethod
     def forward(ctx, G, coeff, d12, NL, atom_map, part, rc, l3, l4, l5):
         _, gd, W = _feat_call(part, MODE_BWD, coeff, d12, NL, atom_map, rc, l3, l4, l5, G=G)
@@ -130,14 +145,43 @@ class _NepFeatGrad(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, g_gc, g_gd):
-        G, coeff, d12, NL, atom_map = ctx.saved_tensors
-        part, rc, l3, l4, l5 = ctx.meta
         if g_gd is None:
             return (None,) * 10
-        gso, _, W2 = _feat_call(part, MODE_BWD2, coeff, d12, NL, atom_map, rc, l3, l4, l5,
-                                G=G, H=g_gd)
-        gsc = _c_grad(part, W2, G.detach(), atom_map, coeff.shape[0]).to(coeff.dtype)
-        return gso.to(G.dtype), gsc, None, None, None, None, None, None, None, None
+        gso, gsc = _second_backward(ctx, g_gd)
+        return gso, gsc, None, None, None, None, None, None, None, None
+
+
+class _NepFeatD12(torch.autograd.Function):
+    """grad_d12 = G . dq/dd12 alone (the force path); differentiable in G and c."""
+
+    @staticmethod
+    def forward(ctx, G, coeff, d12, NL, atom_map, part, rc, l3, l4, l5):
+        _, gd, _ = _feat_call(part, MODE_BWD, coeff, d12, NL, atom_map, rc, l3, l4, l5, G=G,
+                              want_c=False)
+        ctx.save_for_backward(G, coeff, d12, NL, atom_map)
+        ctx.meta = (part, rc, l3, l4, l5)
+        return gd
+
+    @staticmethod
+    def backward(ctx, g_gd):
+        gso, gsc = _second_backward(ctx, g_gd)
+        return gso, gsc, None, None, None, None, None, None, None, None
+
+
+class _NepFeatCGrad(torch.autograd.Function):
+    """dL/dc alone for G = dL/dq (the features' backward when d12 needs no gradient)."""
+
+    @staticmethod
+    def forward(ctx, G, coeff, d12, NL, atom_map, part, rc, l3, l4, l5):
+        _, _, W = _feat_call(part, MODE_BWD, coeff, d12, NL, atom_map, rc, l3, l4, l5, G=G,
+                             want_d=False)
+        return _c_grad(part, W, G.detach(), atom_map, coeff.shape[0]).to(coeff.dtype)
+
+    @staticmethod
+    @torch.autograd.function.once_differentiable
+    def backward(ctx, g):
+        raise RuntimeError("the coefficient gradient of a descriptor whose d12 needs no "
+                           "gradient is not differentiable again")
 
 
 class _NepFeat(torch.autograd.Function):
@@ -152,8 +196,22 @@ class _NepFeat(torch.autograd.Function):
     def backward(ctx, gq):
         coeff, d12, NL, atom_map = ctx.saved_tensors
         part, rc, l3, l4, l5 = ctx.meta
+        if not ctx.needs_input_grad[1]:
+            gc = _NepFeatCGrad.apply(gq, coeff, d12, NL, atom_map, part, rc, l3, l4, l5)
+            return gc, None, None, None, None, None, None, None, None
         gc, gd = _NepFeatGrad.apply(gq, coeff, d12, NL, atom_map, part, rc, l3, l4, l5)
         return gc, gd, None, None, None, None, None, None, None
+
+
+def nep_feat_d12(coeff: torch.Tensor, G: torch.Tensor, d12: torch.Tensor, NL: torch.Tensor,
+                 atom_map: torch.Tensor, angular: bool, rc: float, lmax_3: int = 0,
+                 lmax_4: int = 0, lmax_5: int = 0) -> torch.Tensor:
+    """grad_d12 [N, NN, 4] = G . dq/dd12 of one list's features for G = dE/dq [N, F] (the
+    gradient the force path of NEP.forward takes of the descriptor, nep_net.py:603-611),
+    without the coefficient table; differentiable in G and coeff (second backward mode)."""
+    part = PART_ANGULAR if angular else PART_RADIAL
+    return _NepFeatD12.apply(G, coeff, d12, NL, atom_map, part, float(rc), int(lmax_3),
+                             int(lmax_4), int(lmax_5))
 
 
 def calculateNepFeat(coeff2: torch.Tensor, d12_radial: torch.Tensor, NL_radial: torch.Tensor,

@@ -49,14 +49,14 @@ def calculate_Ri(Ri: torch.Tensor) -> torch.Tensor:
 
 def _mm_impl(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     """a [M, K] @ b [K, N].  A long contraction onto few outputs (the weight and bias gradients
-    of the fitting net, K = atoms) goes as S partial products of about 1024 atoms in one
+    of the fitting net, K = atoms) goes as S partial products of about 256 atoms in one
     batched launch plus their sum: the work spreads over the SMs instead of the handful of
     output tiles a single GEMM of that shape gets."""
     M, K = a.shape
     N = b.shape[1]
     if K < 8192 or M * N > 256 * 256:
         return a @ b
-    S = min(64, K // 1024)
+    S = min(128, K // 256)
     c = K // S
     K0 = S * c
     out = torch.bmm(a[:, :K0].reshape(M, S, c).transpose(0, 1), b[:K0].reshape(S, c, N)).sum(0)
@@ -178,20 +178,25 @@ class NEPTrain(torch.nn.Module):
         cfg = self.cfg
         dt = self.q_scaler.dtype
         tm = atom_type_map.reshape(-1).long()
-        Ri = Ri_radial.to(dt).detach().clone().requires_grad_()
-        Ra = Ri_angular.to(dt).detach().clone().requires_grad_()
+        Ri = Ri_radial.to(dt).detach()
+        Ra = Ri_angular.to(dt).detach()
         N = tm.shape[0]
-        feats = []
+        # descriptor parts: (coefficients, rows, list, angular, cutoff, features)
+        parts = []
         if cfg.train_2b:
-            feats.append(nep_ops.calculateNepFeat(
-                self.c_param_2, Ri, NL_radial, tm, torch.zeros(N, cfg.two_feat_num, dtype=dt,
-                                                               device=Ri.device),
-                cfg.cutoff[0], cfg.multi_feat_num)[0])
+            parts.append((self.c_param_2, Ri, NL_radial, False, cfg.cutoff[0], cfg.two_feat_num))
         if cfg.l_max[0] > 0:
-            feats.append(nep_ops.calculateNepMbFeat(
-                self.c_param_3, Ra, NL_angular, tm, torch.zeros(N, cfg.multi_feat_num, dtype=dt,
-                                                                device=Ri.device),
-                cfg.two_feat_num, *cfg.l_max, cfg.cutoff[1])[0])
+            parts.append((self.c_param_3, Ra, NL_angular, True, cfg.cutoff[1],
+                          cfg.multi_feat_num))
+        feats = []
+        for c, R, NL, ang, rc, nf in parts:
+            buf = torch.zeros(N, nf, dtype=dt, device=Ri.device)
+            if ang:
+                feats.append(nep_ops.calculateNepMbFeat(c, R, NL, tm, buf, cfg.two_feat_num,
+                                                        *cfg.l_max, rc)[0])
+            else:
+                feats.append(nep_ops.calculateNepFeat(c, R, NL, tm, buf, rc,
+                                                      cfg.multi_feat_num)[0])
         feats = torch.cat(feats, -1)
         Ei = self.calculate_Ei(tm, self.q_scaler * feats, type_index)
         counts = tuple(int(c) for c in num_atom.reshape(-1).tolist())
@@ -201,19 +206,20 @@ class NEPTrain(torch.nn.Module):
             Egroup = torch.divide(torch.matmul(Egroup_weight, Ei.unsqueeze(-1)).squeeze(-1), divider)
         if not is_calc_f:
             return Etot, Ei, None, Egroup, None
-        leaves = ([(Ri, NL_radial)] if cfg.train_2b else []) + \
-                 ([(Ra, NL_angular)] if cfg.l_max[0] > 0 else [])
-        grads = torch.autograd.grad([Etot], [r for r, _ in leaves],
-                                    grad_outputs=[torch.ones_like(Etot)], retain_graph=True,
-                                    create_graph=True, allow_unused=True)
+        # dE/dd12 of each list (nep_net.py:603-611): dEtot/dq through the fitting nets, then
+        # G . dq/dd12 by the descriptor's backward mode alone (no coefficient table), kept
+        # differentiable in G and the coefficients for the force and virial loss
+        G = torch.autograd.grad(Etot.sum(), feats, create_graph=True)[0]
         Force = torch.zeros(N, 3, dtype=dt, device=Ri.device)
         Virial = torch.zeros(len(counts), 9, dtype=dt, device=Ri.device)
-        for dE, (R, NL) in zip(grads, leaves):        # nep_net.py:612-631
-            if dE is None:
-                continue
+        off = 0
+        for c, R, NL, ang, rc, nf in parts:         # nep_net.py:612-631
+            dE = nep_ops.nep_feat_d12(c, G[:, off:off + nf], R, NL, tm, ang, rc,
+                                      *(cfg.l_max if ang else (0, 0, 0)))
+            off += nf
             # calculateNepForce + calculateNepVirial of the list with calculate_Ri formed in the
             # kernel (one pass over the slots, no [N, NN, 4, 3] array)
-            F_l, V_l = nep_ops.nep_force_virial(NL, dE, R.detach(), counts)
+            F_l, V_l = nep_ops.nep_force_virial(NL, dE, R, counts)
             Force = Force + F_l
             Virial = Virial + V_l
         return Etot, Ei, -Force, Egroup, -Virial
