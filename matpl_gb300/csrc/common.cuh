@@ -63,6 +63,32 @@ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 __device__ __forceinline__ float dev_tanh(float x) { return tanhf(x); }
 __device__ __forceinline__ double dev_tanh(double x) { return tanh(x); }
 
+// f64 -> f32 round-to-nearest-even in integer arithmetic (keeps the conversions off the FP64
+// pipe, which runs 2 lanes per clock per SM on this part); magnitudes below the f32 normal
+// range take the hardware conversion (never met by interatomic distances in Angstrom).
+__device__ __forceinline__ float to_f32(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const unsigned ex = (hi >> 20) & 0x7ffu;
+    const int e = (int)ex - 1023 + 127;
+    if ((b << 1) == 0ull) return __uint_as_float(hi & 0x80000000u);     // signed zero
+    if (e <= 0 || e >= 255) return __double2float_rn(v);
+    const unsigned sign = hi & 0x80000000u;
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1fffffffu;
+    unsigned r = ((unsigned)e << 23) | m;
+    r += (rest > 0x10000000u) || (rest == 0x10000000u && (m & 1u));
+    return __uint_as_float(sign | r);
+}
+template <typename TO> __device__ __forceinline__ TO conv(double v);
+template <> __device__ __forceinline__ float conv<float>(double v) { return to_f32(v); }
+template <> __device__ __forceinline__ double conv<double>(double v) { return v; }
+
+// bit pattern of a non-negative double: orders like the value (NaN above +inf)
+__device__ __forceinline__ unsigned long long ubits(double v) {
+    return (unsigned long long)__double_as_longlong(v);
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll

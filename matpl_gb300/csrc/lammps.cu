@@ -38,31 +38,6 @@ __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b
 
 constexpr double kNoPair = 1e300;
 
-// f64 -> f32 round-to-nearest-even in integer arithmetic (keeps the conversions off the FP64
-// pipe, which runs 2 lanes per clock per SM on this part); magnitudes below the f32 normal
-// range take the hardware conversion (never met by interatomic distances in Angstrom).
-__device__ __forceinline__ float to_f32(double v) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
-    const unsigned ex = (hi >> 20) & 0x7ffu;
-    const int e = (int)ex - 1023 + 127;
-    if (e <= 0 || e >= 255) return __double2float_rn(v);
-    const unsigned sign = hi & 0x80000000u;
-    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
-    const unsigned rest = lo & 0x1fffffffu;
-    unsigned r = ((unsigned)e << 23) | m;
-    r += (rest > 0x10000000u) || (rest == 0x10000000u && (m & 1u));
-    return __uint_as_float(sign | r);
-}
-template <typename TO> __device__ __forceinline__ TO conv(double v);
-template <> __device__ __forceinline__ float conv<float>(double v) { return to_f32(v); }
-template <> __device__ __forceinline__ double conv<double>(double v) { return v; }
-
-// bit pattern of a non-negative double: orders like the value (NaN above +inf)
-__device__ __forceinline__ unsigned long long ubits(double v) {
-    return (unsigned long long)__double_as_longlong(v);
-}
-
 // the list of row ii (local atom i): packed rows (jstart / jflat, device) ...
 struct CsrLists {
     const long long *jstart;

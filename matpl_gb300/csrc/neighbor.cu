@@ -31,6 +31,7 @@ struct NbImage {
     int nper[3];     // nperiod (NeighConst.f90:42)
     int nb[3];       // cell bins per fractional axis (minimum-image branch)
     int ncells;
+    int ortho;       // off-diagonal lattice entries all (signed) zero
 };
 
 struct NbParams {
@@ -43,17 +44,55 @@ struct NbParams {
 __device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
 
-__device__ __forceinline__ void mic(double &d) {
-    if (fabs(da(d, 1.0)) < fabs(d)) d = da(d, 1.0);
-    if (fabs(da(d, -1.0)) < fabs(d)) d = da(d, -1.0);
-}
-
 __device__ __forceinline__ void cart(const double *L, double d1, double d2, double d3, double &x,
                                      double &y, double &z, double &dd) {
     x = da(da(dm(L[0], d1), dm(L[3], d2)), dm(L[6], d3));
     y = da(da(dm(L[1], d1), dm(L[4], d2)), dm(L[7], d3));
     z = da(da(dm(L[2], d1), dm(L[5], d2)), dm(L[8], d3));
     dd = da(da(dm(x, x), dm(y, y)), dm(z, z));
+}
+
+// mic with integer tests on the bit pattern: for |d| < 2 (fractional differences of wrapped
+// positions lie in (-1, 1)) d + 1 and d - 1 are exact (Sterbenz), so |d + 1| < |d| holds exactly
+// when d < -0.5 and |d - 1| < |d| when d > 0.5.  Called by all lanes of the warp: the one FP64
+// add is issued only when some lane needs it.
+__device__ __forceinline__ void mic_bits(double &d) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    const bool need = (u & 0x7FFFFFFFFFFFFFFFull) > 0x3FE0000000000000ull;
+    if (__any_sync(0xffffffffu, need)) {
+        const double dn = da(d, (u >> 63) ? 1.0 : -1.0);
+        if (need) d = dn;
+    }
+}
+
+__device__ __forceinline__ bool is_zero_bits(double v) {
+    return ((unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull) == 0ull;
+}
+
+// cart() for a lattice whose off-diagonal entries are (signed) zeros: a non-zero product plus
+// signed zeros is that product exactly, so only a zero diagonal product needs the full sum (for
+// its sign); bit-identical to cart().  Called by all lanes of the warp (the full sums are issued
+// only when some lane has a zero product).
+__device__ __forceinline__ void cart_ortho(const double *L, double d1, double d2, double d3,
+                                           double &x, double &y, double &z, double &dd) {
+    x = dm(L[0], d1);
+    y = dm(L[4], d2);
+    z = dm(L[8], d3);
+    const bool zx = is_zero_bits(x), zy = is_zero_bits(y), zz = is_zero_bits(z);
+    if (__any_sync(0xffffffffu, zx || zy || zz)) {
+        const double fx = da(da(x, dm(L[3], d2)), dm(L[6], d3));
+        const double fy = da(da(dm(L[1], d1), y), dm(L[7], d3));
+        const double fz = da(da(dm(L[2], d1), dm(L[5], d2)), z);
+        if (zx) x = fx;
+        if (zy) y = fy;
+        if (zz) z = fz;
+    }
+    dd = da(da(dm(x, x), dm(y, y)), dm(z, z));
+}
+
+// a < b for non-negative doubles (and +inf / NaN above every finite value) as integers
+__device__ __forceinline__ bool lt_bits(double a, double b) {
+    return __double_as_longlong(a) < __double_as_longlong(b);
 }
 
 __device__ __forceinline__ void store4(float *p, float a, float b, float c, float d) {
@@ -104,6 +143,8 @@ __global__ void nb_setup(const double *__restrict__ lattice, NbImage *__restrict
             im.nb[kmax] = (im.nb[kmax] + 1) / 2;
         }
         im.ncells = im.iflag ? 0 : (int)prod;
+        im.ortho = L[1] == 0.0 && L[2] == 0.0 && L[3] == 0.0 && L[5] == 0.0 && L[6] == 0.0 &&
+                   L[7] == 0.0;
         img[b] = im;
     }
 }
@@ -369,35 +410,35 @@ nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
         int n_acc = 0;
         const double rct2 = P.rct2[ti];
         for (int c0 = 0; c0 < ncand; c0 += 32) {
+            // every lane evaluates a candidate (lanes past the end repeat the last one and are
+            // masked), so the warp-wide votes in mic_bits / cart_ortho see the whole warp
             const int c = c0 + lane;
-            bool inM = false, inT = false;
-            int tj = 0, key = 0;
-            double px = 0.0, py = 0.0, pz = 0.0, pdd = 0.0;
-            if (c < ncand) {
-                key = cand[c];
-                const int j = key / nimg, idx = key - (key / nimg) * nimg;
-                double d1, d2, d3;
-                if (im.iflag) {
-                    const int i3 = idx % nimg1 - im.nper[2];
-                    const int i2 = (idx / nimg1) % nimg2 - im.nper[1];
-                    const int i1 = idx / (nimg1 * nimg2) - im.nper[0];
-                    d1 = da(da(pos[3 * j], -pi0), (double)i1);
-                    d2 = da(da(pos[3 * j + 1], -pi1), (double)i2);
-                    d3 = da(da(pos[3 * j + 2], -pi2), (double)i3);
-                } else {
-                    d1 = da(pos[3 * j], -pi0); mic(d1);
-                    d2 = da(pos[3 * j + 1], -pi1); mic(d2);
-                    d3 = da(pos[3 * j + 2], -pi2); mic(d3);
-                }
-                cart(im.L, d1, d2, d3, px, py, pz, pdd);
-                inM = pdd < P.rc2 && pdd > 1.0e-8;
-                inT = inM && pdd < rct2;
-                tj = type_map[j];
-                if (tj < 0 || tj >= P.ntypes) {
-                    atomicMax(err, MATPL_KERR_BAD_TYPE);
-                    inM = inT = false;
-                    tj = 0;
-                }
+            const bool valid = c < ncand;
+            const int key = cand[valid ? c : ncand - 1];
+            const int j = key / nimg, idx = key - (key / nimg) * nimg;
+            double d1, d2, d3, px, py, pz, pdd;
+            if (im.iflag) {
+                const int i3 = idx % nimg1 - im.nper[2];
+                const int i2 = (idx / nimg1) % nimg2 - im.nper[1];
+                const int i1 = idx / (nimg1 * nimg2) - im.nper[0];
+                d1 = da(da(pos[3 * j], -pi0), (double)i1);
+                d2 = da(da(pos[3 * j + 1], -pi1), (double)i2);
+                d3 = da(da(pos[3 * j + 2], -pi2), (double)i3);
+            } else {
+                d1 = da(pos[3 * j], -pi0); mic_bits(d1);
+                d2 = da(pos[3 * j + 1], -pi1); mic_bits(d2);
+                d3 = da(pos[3 * j + 2], -pi2); mic_bits(d3);
+            }
+            if (im.ortho) cart_ortho(im.L, d1, d2, d3, px, py, pz, pdd);
+            else cart(im.L, d1, d2, d3, px, py, pz, pdd);
+            // pdd >= +0: the comparisons as integer comparisons of the bit patterns
+            bool inM = valid && lt_bits(pdd, P.rc2) && lt_bits(1.0e-8, pdd);
+            bool inT = inM && lt_bits(pdd, rct2);
+            int tj = type_map[j];
+            if (tj < 0 || tj >= P.ntypes) {
+                if (valid) atomicMax(err, MATPL_KERR_BAD_TYPE);
+                inM = inT = false;
+                tj = 0;
             }
 #pragma unroll
             for (int q = 0; q < kMaxTypes; ++q)
@@ -441,7 +482,8 @@ nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
             const double x = xa.x, y = xa.y, z = xb.x, dd = xb.y;
             const long long slot = row + (long long)ty * P.m + rank;
             list_neigh[slot] = j + 1;
-            store4(image_dr + 4 * slot, (TO)__dsqrt_rn(dd), (TO)x, (TO)y, (TO)z);
+            store4(image_dr + 4 * slot, conv<TO>(__dsqrt_rn(dd)), conv<TO>(x), conv<TO>(y),
+                   conv<TO>(z));
         }
         // ---- phase D: clear the empty slots
         for (int s = lane; s < S; s += 32) {

@@ -106,3 +106,32 @@ def test_full_size_counts_and_symmetry():
     pairs_fwd = (i_idx[mask] * 32000 + (ln[mask] - 1)).sort().values
     pairs_rev = ((ln[mask] - 1) * 32000 + i_idx[mask]).sort().values
     assert torch.equal(pairs_fwd, pairs_rev)
+
+
+def _bits(a):
+    a = np.ascontiguousarray(a)
+    return a.view(np.int64 if a.dtype == np.float64 else np.int32)
+
+
+@pytest.mark.parametrize("variant", ["plain", "neg_zero", "neg_diag"])
+def test_orthorhombic_crystal_exact_zeros_bitwise(variant):
+    """A perfect FCC crystal (non-cubic orthorhombic cell) in the nearest-image branch: many
+    pair components are exact zeros, so the signed-zero handling of the orthorhombic form must
+    give the general formula's bits (compared as integers, so -0.0 != +0.0): off-diagonal zeros
+    +0.0 or -0.0, and a negative diagonal entry (left-handed cell) that turns products of +0
+    into -0."""
+    st = structures.fcc(3.615, (6, 5, 7), 0.0, seed=1)
+    L = st.lattice.copy()
+    if variant == "neg_zero":
+        for q in ((0, 1), (0, 2), (1, 0), (1, 2), (2, 0), (2, 1)):
+            L[q] = -0.0
+    if variant == "neg_diag":
+        L[0, 0] = -L[0, 0]
+        L[1, 0] = -0.0
+    st = structures.Structure(L, st.frac, st.types, st.elements)
+    ln_o, idr_o = neigh.find_neighbore(st.types, st.frac, st.lattice, 1, 100, 6.0, [6.0])
+    for dt, ref in ((torch.float64, idr_o), (torch.float32, idr_o.astype(np.float32))):
+        ln_g, idr_g = gpu_build(st, 1, 100, out_dtype=dt)
+        assert np.array_equal(ln_g.cpu().numpy(), ln_o)
+        assert np.array_equal(_bits(idr_g.cpu().numpy()), _bits(ref))
+    assert (idr_o[..., 1:] == 0).any()
