@@ -224,6 +224,23 @@ int matpl_dp_dual_backward(int dtype, const matpl_dp_model *model, int batch, in
                            const void *grad_virial, const void *A_bar, const void *A_dot_bar,
                            void *grad_embedding, void *stream);
 
+/* matpl_dp_desc_dual: per atom the descriptor D = A^T A< and its tangent
+ *   D_dot = A_dot^T A< + A^T A_dot< (A, A_dot [natoms, 4, 25], A< = first m2 columns; D, D_dot
+ *   [natoms, 25, m2]) - the xyz_scater_a^T xyz_scater_b product of src/model/dp_dp.py:304-330
+ *   for the training step's primal and tangent streams.  Output row r holds atom rows[r]
+ *   (rows: a permutation of [0, natoms), e.g. the atoms grouped by element so that each
+ *   element's fitting net reads one contiguous block; NULL = identity).
+ * matpl_dp_desc_dual_grad: its transpose map: grad_A, grad_A_dot [natoms, 4, 25] (written,
+ *   atom rows[r] from row r) from grad_D, grad_D_dot [natoms, 25, m2] (either may be NULL =
+ *   zero).
+ * dtype MATPL_F32 or MATPL_F64; 1 <= m2 <= 25.
+ */
+int matpl_dp_desc_dual(int dtype, long long natoms, int m2, const long long *rows, const void *A,
+                       const void *A_dot, void *D, void *D_dot, void *stream);
+int matpl_dp_desc_dual_grad(int dtype, long long natoms, int m2, const long long *rows,
+                            const void *A, const void *A_dot, const void *grad_D,
+                            const void *grad_D_dot, void *grad_A, void *grad_A_dot, void *stream);
+
 /* ------------------------------------------------------------------------------------
  * NEP neighbor lists.  Replaces CalcOps calculate_neighbor / calculate_maxneigh
  * (src/op/src/CalcOps.cpp:1025-1172, kernels src/op/kernel/calculateNepNeighbor.cu:8-380,

@@ -80,6 +80,8 @@ SIGNATURES = {
     "matpl_env_stats": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _d, _d, _vp, _vp, _vp]),
     "matpl_nep_feat_op": (_i, [_i] * 11 + [_d] + [_vp] * 5 + [_ll, _vp, _vp, _ll] + [_vp] * 4),
     "matpl_nep_cgrad": (_i, [_i] * 6 + [_vp, _vp, _ll, _vp, _vp, _vp, _vp]),
+    "matpl_dp_desc_dual": (_i, [_i, _ll, _i] + [_vp] * 6),
+    "matpl_dp_desc_dual_grad": (_i, [_i, _ll, _i] + [_vp] * 8),
     "matpl_nep_force_virial": (_i, [_i] * 4 + [_vp] * 8),
     "matpl_nep_force_virial_grad": (_i, [_i] * 4 + [_vp] * 8),
     "matpl_lammps_dp_neighbors": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _i,

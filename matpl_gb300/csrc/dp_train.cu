@@ -263,21 +263,41 @@ __device__ __forceinline__ void reduce_layer(const T *stg, int nv, int ti, int n
         const int OW = lay == 1 ? EmbOff::W1 : EmbOff::W2;
         const int OB = lay == 1 ? EmbOff::B1 : EmbOff::B2;
         const int OD = lay == 1 ? EmbOff::DT1 : EmbOff::DT2;
-        for (int e = lane; e < E * E + 2 * E; e += 32) {
-            T acc = T(0);
-            if (e < E * E) {
-                const int i = e / E, o = e - i * E;
-                for (int l = lo; l < hi; ++l) {
-                    const T *r = stg + l * Stage::ROW;
-                    acc += r[Stage::X + i] * r[Stage::ZB + o] + r[Stage::XD + i] * r[Stage::ZDB + o];
+        // weight gradient sum_l x_i zb_o + xd_i zdb_o: lane < 25 owns a 5 x 5 block (i, o), so
+        // a row costs 20 shared loads for 50 FMAs
+        static_assert(E == 25, "5 x 5 register blocks of the 25 x 25 weight gradient");
+        if (lane < 25) {
+            const int i0 = 5 * (lane / 5), o0 = 5 * (lane % 5);
+            T acc[5][5];
+#pragma unroll
+            for (int a = 0; a < 5; ++a)
+#pragma unroll
+                for (int b = 0; b < 5; ++b) acc[a][b] = T(0);
+            for (int l = lo; l < hi; ++l) {
+                const T *r = stg + l * Stage::ROW;
+                T xi[5], xdi[5], zo[5], zdo[5];
+#pragma unroll
+                for (int a = 0; a < 5; ++a) {
+                    xi[a] = r[Stage::X + i0 + a];
+                    xdi[a] = r[Stage::XD + i0 + a];
+                    zo[a] = r[Stage::ZB + o0 + a];
+                    zdo[a] = r[Stage::ZDB + o0 + a];
                 }
-                atomicAdd(g + OW + e, acc);
-            } else {
-                const int o = e - E * E;
-                const int col = o < E ? Stage::ZB + o : Stage::Q + (o - E);
-                for (int l = lo; l < hi; ++l) acc += stg[l * Stage::ROW + col];
-                atomicAdd(g + (o < E ? OB + o : OD + (o - E)), acc);
+#pragma unroll
+                for (int a = 0; a < 5; ++a)
+#pragma unroll
+                    for (int b = 0; b < 5; ++b) acc[a][b] += xi[a] * zo[b] + xdi[a] * zdo[b];
             }
+#pragma unroll
+            for (int a = 0; a < 5; ++a)
+#pragma unroll
+                for (int b = 0; b < 5; ++b) atomicAdd(g + OW + (i0 + a) * E + o0 + b, acc[a][b]);
+        }
+        for (int o = lane; o < 2 * E; o += 32) {
+            T acc = T(0);
+            const int col = o < E ? Stage::ZB + o : Stage::Q + (o - E);
+            for (int l = lo; l < hi; ++l) acc += stg[l * Stage::ROW + col];
+            atomicAdd(g + (o < E ? OB + o : OD + (o - E)), acc);
         }
     }
 }
@@ -422,6 +442,107 @@ dp_dual_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
         if (gacc[q] != T(0)) atomicAdd(grad + q, gacc[q]);
 }
 
+// ---------------------------------------------------------------- descriptor and its tangent
+// Per atom D = A^T A< and Ddot = Adot^T A< + A^T Adot< (A, Adot [4][E], A< its first m2
+// columns; D [E][m2]): the products of dp_dp.py:304-330 (xyz_scater_a^T xyz_scater_b) for the
+// training step's primal and tangent streams.  One thread per (output row, p, q); output row r
+// holds atom rows[r] (rows: a permutation, e.g. atoms grouped by element; NULL = identity).
+template <typename T>
+__global__ void __launch_bounds__(256)
+desc_dual_kernel(long long natoms, int m2, const long long *__restrict__ rows,
+                 const T *__restrict__ A, const T *__restrict__ Ad, T *__restrict__ D,
+                 T *__restrict__ Dd) {
+    const long long per = (long long)E * m2, total = natoms * per;
+    for (long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x; o < total;
+         o += (long long)gridDim.x * blockDim.x) {
+        const long long r = o / per;
+        const int pq = (int)(o - r * per), p = pq / m2, q = pq - p * m2;
+        const long long a = rows ? rows[r] : r;
+        const T *ar = A + a * NA, *dr = Ad + a * NA;
+        T d = T(0), dd = T(0);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const T ap = __ldg(ar + c * E + p), aq = __ldg(ar + c * E + q);
+            d += ap * aq;
+            dd += __ldg(dr + c * E + p) * aq + ap * __ldg(dr + c * E + q);
+        }
+        D[o] = d;
+        Dd[o] = dd;
+    }
+}
+
+// The transpose map: for gD = dPhi/dD, gDd = dPhi/dDdot (either may be absent)
+//   gA[c][x]  = sum_q gD[x][q] A[c][q] + [x < m2] sum_p gD[p][x] A[c][p]
+//             + sum_q gDd[x][q] Ad[c][q] + [x < m2] sum_p gDd[p][x] Ad[c][p],
+//   gAd[c][x] = sum_q gDd[x][q] A[c][q] + [x < m2] sum_p gDd[p][x] A[c][p].
+// One thread per (row, x) writes the 4 + 4 entries of atom rows[r] (a permutation: no two rows
+// write the same atom).
+template <typename T>
+__global__ void __launch_bounds__(256)
+desc_dual_grad_kernel(long long natoms, int m2, const long long *__restrict__ rows,
+                      const T *__restrict__ A, const T *__restrict__ Ad, const T *__restrict__ gD,
+                      const T *__restrict__ gDd, T *__restrict__ gA, T *__restrict__ gAd) {
+    const long long total = natoms * E;
+    const long long per = (long long)E * m2;
+    for (long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x; o < total;
+         o += (long long)gridDim.x * blockDim.x) {
+        const long long r = o / E;
+        const int x = (int)(o - r * E);
+        const long long a = rows ? rows[r] : r;
+        const T *ar = A + a * NA, *dr = Ad + a * NA;
+        const T *g = gD ? gD + r * per : nullptr, *gd = gDd ? gDd + r * per : nullptr;
+        T ga[4] = {T(0), T(0), T(0), T(0)}, gad[4] = {T(0), T(0), T(0), T(0)};
+        for (int q = 0; q < m2; ++q) {
+            const T u = g ? __ldg(g + x * m2 + q) : T(0);
+            const T v = gd ? __ldg(gd + x * m2 + q) : T(0);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const T aq = __ldg(ar + c * E + q), dq = __ldg(dr + c * E + q);
+                ga[c] += u * aq + v * dq;
+                gad[c] += v * aq;
+            }
+        }
+        if (x < m2) {
+            for (int p = 0; p < E; ++p) {
+                const T u = g ? __ldg(g + p * m2 + x) : T(0);
+                const T v = gd ? __ldg(gd + p * m2 + x) : T(0);
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const T ap = __ldg(ar + c * E + p), dp = __ldg(dr + c * E + p);
+                    ga[c] += u * ap + v * dp;
+                    gad[c] += v * ap;
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            gA[a * NA + c * E + x] = ga[c];
+            gAd[a * NA + c * E + x] = gad[c];
+        }
+    }
+}
+
+template <typename T>
+int launch_desc(bool grad, long long natoms, int m2, const long long *rows, const void *A,
+                const void *Ad, const void *gD, const void *gDd, void *o0, void *o1,
+                cudaStream_t s) {
+    const long long work = grad ? natoms * E : natoms * E * m2;
+    long long grid = (work + 255) / 256;
+    if (grid > 152LL * 32) grid = 152LL * 32;
+    if (grid < 1) grid = 1;
+    if (!grad) {
+        ProfScope ps("dp_desc_dual", s);
+        desc_dual_kernel<T><<<(int)grid, 256, 0, s>>>(natoms, m2, rows, (const T *)A,
+                                                       (const T *)Ad, (T *)o0, (T *)o1);
+        return check_launch("matpl_dp_desc_dual");
+    }
+    ProfScope ps("dp_desc_dual_grad", s);
+    desc_dual_grad_kernel<T><<<(int)grid, 256, 0, s>>>(natoms, m2, rows, (const T *)A,
+                                                        (const T *)Ad, (const T *)gD,
+                                                        (const T *)gDd, (T *)o0, (T *)o1);
+    return check_launch("matpl_dp_desc_dual_grad");
+}
+
 int check_args(int dtype, int batch, int natoms, int nslots, int ntypes, int m) {
     MATPL_REQUIRE(dtype == MATPL_F32 || dtype == MATPL_F64, MATPL_ERR_DTYPE,
                   "the training kernels support MATPL_F32 and MATPL_F64");
@@ -539,4 +660,39 @@ extern "C" int matpl_dp_dual_backward(int dtype, const matpl_dp_model *model, in
                : launch<float>(true, model, batch, natoms, nslots, list_neigh, image_dr,
                                type_map, grad_force, grad_virial, A_bar, A_dot_bar,
                                grad_embedding, nullptr, as_stream(stream));
+}
+
+extern "C" int matpl_dp_desc_dual(int dtype, long long natoms, int m2, const long long *rows,
+                                  const void *A, const void *A_dot, void *D, void *D_dot,
+                                  void *stream) {
+    MATPL_REQUIRE(dtype == MATPL_F32 || dtype == MATPL_F64, MATPL_ERR_DTYPE,
+                  "matpl_dp_desc_dual: dtype is MATPL_F32 or MATPL_F64");
+    MATPL_REQUIRE(natoms >= 0 && m2 >= 1 && m2 <= dp::E, MATPL_ERR_INVALID,
+                  "natoms >= 0 and 1 <= m2 <= 25");
+    MATPL_REQUIRE(natoms == 0 || (A && A_dot && D && D_dot), MATPL_ERR_INVALID,
+                  "null pointer argument");
+    if (natoms == 0) return MATPL_OK;
+    return dtype == MATPL_F64
+               ? launch_desc<double>(false, natoms, m2, rows, A, A_dot, nullptr, nullptr, D,
+                                     D_dot, as_stream(stream))
+               : launch_desc<float>(false, natoms, m2, rows, A, A_dot, nullptr, nullptr, D,
+                                    D_dot, as_stream(stream));
+}
+
+extern "C" int matpl_dp_desc_dual_grad(int dtype, long long natoms, int m2,
+                                       const long long *rows, const void *A, const void *A_dot,
+                                       const void *grad_D, const void *grad_D_dot, void *grad_A,
+                                       void *grad_A_dot, void *stream) {
+    MATPL_REQUIRE(dtype == MATPL_F32 || dtype == MATPL_F64, MATPL_ERR_DTYPE,
+                  "matpl_dp_desc_dual_grad: dtype is MATPL_F32 or MATPL_F64");
+    MATPL_REQUIRE(natoms >= 0 && m2 >= 1 && m2 <= dp::E, MATPL_ERR_INVALID,
+                  "natoms >= 0 and 1 <= m2 <= 25");
+    MATPL_REQUIRE(natoms == 0 || (A && A_dot && grad_A && grad_A_dot), MATPL_ERR_INVALID,
+                  "null pointer argument");
+    if (natoms == 0) return MATPL_OK;
+    return dtype == MATPL_F64
+               ? launch_desc<double>(true, natoms, m2, rows, A, A_dot, grad_D, grad_D_dot,
+                                     grad_A, grad_A_dot, as_stream(stream))
+               : launch_desc<float>(true, natoms, m2, rows, A, A_dot, grad_D, grad_D_dot,
+                                    grad_A, grad_A_dot, as_stream(stream));
 }

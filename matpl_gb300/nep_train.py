@@ -19,6 +19,7 @@ from typing import Dict, Optional
 import torch
 
 from . import nep_ops
+from .splitk import _AddRow, _MM
 from .nep import NepConfig
 
 
@@ -45,70 +46,6 @@ def calculate_Ri(Ri: torch.Tensor) -> torch.Tensor:
     safe = torch.where(mask > 0, Ri[:, :, 0:1], torch.ones_like(mask))
     eye = torch.eye(3, dtype=Ri.dtype, device=Ri.device)
     return torch.cat(((Ri[:, :, 1:] / safe * mask).unsqueeze(2), eye * mask.unsqueeze(-1)), 2)
-
-
-def _mm_impl(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
-    """a [M, K] @ b [K, N].  A long contraction onto few outputs (the weight and bias gradients
-    of the fitting net, K = atoms) goes as S partial products of about 256 atoms in one
-    batched launch plus their sum: the work spreads over the SMs instead of the handful of
-    output tiles a single GEMM of that shape gets."""
-    M, K = a.shape
-    N = b.shape[1]
-    if K < 8192 or M * N > 256 * 256:
-        return a @ b
-    S = min(128, K // 256)
-    c = K // S
-    K0 = S * c
-    out = torch.bmm(a[:, :K0].reshape(M, S, c).transpose(0, 1), b[:K0].reshape(S, c, N)).sum(0)
-    if K0 < K:
-        out = out + a[:, K0:] @ b[K0:]
-    return out
-
-
-class _MM(torch.autograd.Function):
-    """Matrix product through ``_mm_impl`` in the forward and every order of backward."""
-
-    @staticmethod
-    def forward(ctx, a, b):
-        ctx.save_for_backward(a, b)
-        return _mm_impl(a, b)
-
-    @staticmethod
-    def backward(ctx, g):
-        a, b = ctx.saved_tensors
-        ga = _MM.apply(g, b.t()) if ctx.needs_input_grad[0] else None
-        gb = _MM.apply(a.t(), g) if ctx.needs_input_grad[1] else None
-        return ga, gb
-
-
-_ones_rows = {}
-
-
-def _ones_row(n, dev, dt):
-    key = (n, dev, dt)
-    t = _ones_rows.get(key)
-    if t is None:
-        if len(_ones_rows) > 16:
-            _ones_rows.clear()
-        t = _ones_rows[key] = torch.ones(1, n, dtype=dt, device=dev)
-    return t
-
-
-class _AddRow(torch.autograd.Function):
-    """z [N, F] + b [F]; the gradient of b, a sum over the N rows, as ones[1, N] @ g through
-    ``_MM`` (differentiable again)."""
-
-    @staticmethod
-    def forward(ctx, z, b):
-        ctx.n = z.shape[0]
-        return z + b
-
-    @staticmethod
-    def backward(ctx, g):
-        gb = None
-        if ctx.needs_input_grad[1]:
-            gb = _MM.apply(_ones_row(ctx.n, g.device, g.dtype), g).reshape(-1)
-        return g, gb
 
 
 def _image_sum(x: torch.Tensor, counts) -> torch.Tensor:

@@ -17,7 +17,7 @@ from typing import Dict, List, Optional, Sequence
 
 import torch
 
-from . import ops
+from . import ops, splitk
 from .params import DPConfig
 
 
@@ -232,6 +232,43 @@ class _EmbedDual(torch.autograd.Function):
         return grad, None, None, None, None, None, None
 
 
+class _DescDual(torch.autograd.Function):
+    """(D, D_dot) = (A^T A<, A_dot^T A< + A^T A_dot<) for the atoms rows (matpl_dp_desc_dual,
+    output row r = atom rows[r]); the backward is the transpose map (matpl_dp_desc_dual_grad)."""
+
+    @staticmethod
+    def forward(ctx, A, Ad, m2, rows):
+        A = A.contiguous()
+        Ad = Ad.contiguous()
+        R = rows.numel()
+        D = torch.empty(R, _dp.E, m2, dtype=A.dtype, device=A.device)
+        Dd = torch.empty_like(D)
+        code = _lib.MATPL_F64 if A.dtype == torch.float64 else _lib.MATPL_F32
+        _check(_lib.load().matpl_dp_desc_dual(code, R, m2, _ptr(rows), _ptr(A), _ptr(Ad), _ptr(D),
+                                              _ptr(Dd),
+                                              torch.cuda.current_stream(A.device).cuda_stream),
+               "matpl_dp_desc_dual")
+        ctx.save_for_backward(A, Ad, rows)
+        ctx.m2 = m2
+        return D, Dd
+
+    @staticmethod
+    @torch.autograd.function.once_differentiable
+    def backward(ctx, gD, gDd):
+        A, Ad, rows = ctx.saved_tensors
+        R = rows.numel()
+        full = R == A.shape[0]               # a permutation of every atom writes every row
+        gA = torch.empty_like(A) if full else torch.zeros_like(A)
+        gAd = torch.empty_like(Ad) if full else torch.zeros_like(Ad)
+        code = _lib.MATPL_F64 if A.dtype == torch.float64 else _lib.MATPL_F32
+        gD = gD.contiguous() if gD is not None else None
+        gDd = gDd.contiguous() if gDd is not None else None
+        _check(_lib.load().matpl_dp_desc_dual_grad(
+            code, R, ctx.m2, _ptr(rows), _ptr(A), _ptr(Ad), _ptr(gD), _ptr(gDd), _ptr(gA),
+            _ptr(gAd), torch.cuda.current_stream(A.device).cuda_stream), "matpl_dp_desc_dual_grad")
+        return gA, gAd, None, None
+
+
 class FusedTrainer:
     """Force-loss training step with the embedding nets' second-order gradient in this
     library's kernels.  Per composition cluster (as ``dp_trainer.train``):
@@ -299,11 +336,11 @@ class FusedTrainer:
         n = x.shape[0]
         for l in range(nl - 1):
             pre = f"fitting_net.{t}.layers.{l}."
-            zz = torch.cat([x, xd], 0) @ model.param(pre + "weight")
+            zz = splitk.mm(torch.cat([x, xd], 0), model.param(pre + "weight"))
             z, zd = zz[:n], zz[n:]
             b = model.param(pre + "bias")
             if b is not None:
-                z = z + b
+                z = splitk.add_row(z, b)
             h = torch.tanh(z)
             hd = (1 - h * h) * zd
             if l == 0:
@@ -314,19 +351,31 @@ class FusedTrainer:
                     h, hd = h * dt, hd * dt
                 x, xd = h + x, hd + xd
         pre = f"fitting_net.{t}.layers.{nl - 1}."
-        ee = torch.cat([x, xd], 0) @ model.param(pre + "weight")
+        ee = splitk.mm(torch.cat([x, xd], 0), model.param(pre + "weight"))
         e, ed = ee[:n], ee[n:]
         b = model.param(pre + "bias")
-        return (e + b if b is not None else e), ed
+        return (splitk.add_row(e, b) if b is not None else e), ed
 
-    def _type_index(self, tm32: torch.Tensor, present):
-        """Atom indices of each present element (cached per type map: no host sync on reuse)."""
-        key = (self._tm_src.data_ptr(), tm32.numel(), tuple(present))
+    def _type_index(self, tm32: torch.Tensor, present, B: int):
+        """Atom rows of the [B*N] batch grouped by present element, b-major inside each
+        element ([B, n] blocks), and each element's (start, count) in that order (cached per
+        type map and batch size: one host sync when it changes)."""
+        key = (self._tm_src.data_ptr(), tm32.numel(), tuple(present), B)
         if getattr(self, "_tidx_key", None) != key:
             tl = tm32.long()
-            self._tidx = {ti: torch.nonzero(tl == ti).flatten() for ti in present}
+            N = tl.numel()
+            base = torch.arange(B, device=tl.device).reshape(B, 1) * N
+            rows, blocks, off = [], {}, 0
+            for ti in present:
+                idx = torch.nonzero(tl == ti).flatten()
+                n = idx.numel()
+                rows.append((base + idx.reshape(1, n)).reshape(-1))
+                blocks[ti] = (off, n)
+                off += B * n
+            self._rows = torch.cat(rows).contiguous()
+            self._blocks = blocks
             self._tidx_key = key
-        return self._tidx
+        return self._rows, self._blocks
 
     def _loss_and_backward(self, batch: dict, w_f: float, w_e: float):
         """Steps 1-5 with device tensors only (no host synchronisation once the type index is
@@ -345,7 +394,7 @@ class FusedTrainer:
         present = [cfg.atom_type.index(int(a)) for a in batch["atom_type"]
                    if int(a) in cfg.atom_type]
         self._present = present
-        tidx = self._type_index(tm32, present)
+        rows, blocks = self._type_index(tm32, present, B)
         # 1. E, F with the current parameters
         self.evaluator.packed.copy_(_pack_device(model))
         r = self.evaluator.evaluate(ln32, tm32, present, idr, 0)
@@ -363,16 +412,18 @@ class FusedTrainer:
         Ad = Ad.reshape(B, N, 4, _dp.E)
         # 4. per-atom energies and their tangent (explicit forward-mode through D and the
         #    fitting net), 5. one first-order backward of Phi gives every parameter gradient
+        # D rows grouped by element (b-major inside each element): every fitting net reads a
+        # contiguous block, no gather / scatter
+        D_all, Dd_all = _DescDual.apply(A.reshape(B * N, 4, _dp.E), Ad.reshape(B * N, 4, _dp.E),
+                                        cfg.M2, rows)
+        D_all = D_all.reshape(D_all.shape[0], -1)
+        Dd_all = Dd_all.reshape(Dd_all.shape[0], -1)
         phi = A.new_zeros(())
         for ti in present:
-            idx = tidx[ti]
-            n = idx.numel()
+            o, n = blocks[ti]
             if n == 0:
                 continue
-            Ab, Adb = A[:, idx], Ad[:, idx]
-            D = Ab.transpose(-2, -1) @ Ab[..., :cfg.M2]
-            Dd = Adb.transpose(-2, -1) @ Ab[..., :cfg.M2] + Ab.transpose(-2, -1) @ Adb[..., :cfg.M2]
-            e, ed = self._fit_dual(ti, D.reshape(B * n, -1), Dd.reshape(B * n, -1))
+            e, ed = self._fit_dual(ti, D_all[o:o + B * n], Dd_all[o:o + B * n])
             phi = phi + (gE.reshape(B, 1) * e.reshape(B, n)).sum() + ed.sum()
         phi.backward()
         return loss.detach(), le.detach(), lf.detach()

@@ -197,3 +197,35 @@ def test_graphed_training_step_matches_eager():
         assert abs(a - b) <= 1e-10 * abs(a)
     for k in m1.names:
         assert torch.allclose(m1.param(k), m2.param(k), rtol=1e-10, atol=1e-12), k
+
+
+@pytest.mark.parametrize("m2,partial", [(16, False), (25, True), (4, False)])
+def test_descriptor_product_kernel_matches_torch(m2, partial):
+    """matpl_dp_desc_dual / _grad = torch's D = A^T A<, D_dot = A_dot^T A< + A^T A_dot< on the
+    rows of a permutation (or a subset: the other atoms get zero gradient) and their autograd
+    transpose (FP64, random A, A_dot, seeds; either seed absent)."""
+    from matpl_gb300.train import _DescDual
+    g = torch.Generator(device=DEV).manual_seed(m2)
+    A = torch.randn(37, 4, 25, generator=g, device=DEV, dtype=torch.float64, requires_grad=True)
+    Ad = torch.randn(37, 4, 25, generator=g, device=DEV, dtype=torch.float64, requires_grad=True)
+    rows = torch.randperm(37, generator=g, device=DEV)
+    if partial:
+        rows = rows[:30]
+    D, Dd = _DescDual.apply(A, Ad, m2, rows)
+    Ar, Adr = A.index_select(0, rows), Ad.index_select(0, rows)
+    Dr = Ar.transpose(-2, -1) @ Ar[..., :m2]
+    Ddr = Adr.transpose(-2, -1) @ Ar[..., :m2] + Ar.transpose(-2, -1) @ Adr[..., :m2]
+    torch.testing.assert_close(D, Dr, rtol=1e-13, atol=1e-13)
+    torch.testing.assert_close(Dd, Ddr, rtol=1e-13, atol=1e-13)
+    gD = torch.randn(D.shape, generator=g, device=DEV, dtype=torch.float64)
+    gDd = torch.randn(D.shape, generator=g, device=DEV, dtype=torch.float64)
+    for seeds in ((gD, gDd), (gD, None), (None, gDd)):
+        outs = [o for o, s in zip((D, Dd), seeds) if s is not None]
+        refs = [o for o, s in zip((Dr, Ddr), seeds) if s is not None]
+        gs = [s for s in seeds if s is not None]
+        k = torch.autograd.grad(outs, [A, Ad], gs, retain_graph=True, allow_unused=True)
+        r = torch.autograd.grad(refs, [A, Ad], gs, retain_graph=True, allow_unused=True)
+        for a, b in zip(k, r):
+            a = torch.zeros_like(A) if a is None else a
+            b = torch.zeros_like(A) if b is None else b
+            torch.testing.assert_close(a, b, rtol=1e-12, atol=1e-12)
