@@ -424,7 +424,7 @@ def run_train(args, ws, local, steps, warmup, plain_steps):
     del etrainer, emodel, eopt
     # fused step captured in one CUDA graph (the headline of this workload)
     fmodel = train.DPTrainModel(cfg, prm, davg, dstd, dtype=torch.float32, device=dev)
-    fopt = torch.optim.Adam(fmodel.parameters(), lr=1e-4, capturable=True)
+    fopt = torch.optim.Adam(fmodel.parameters(), lr=1e-4, capturable=True, fused=True)
     graphed = train.GraphedTrainer(train.FusedTrainer(fmodel), fopt)
     fused_ms = timed(lambda: graphed.step(batch), steps, warmup)
     pmodel = train.DPTrainModel(cfg, prm, davg, dstd, dtype=torch.float32, device=dev)
