@@ -375,6 +375,24 @@ int matpl_nep_cgrad(int dtype, int part, int natoms, int ntypes, int n_max, int 
                     const long long *type_map, const void *G, long long ldG, const void *W,
                     void *dc, int *err_dev, void *stream);
 
+/* matpl_nep_zbl: the ZBL term of NEP (src/model/nep_net.py:399-408, calculate_zbl / cal_zbl
+ *   :916-991) added to existing outputs.  For every angular-list slot (NL [natoms, max_nn] int64,
+ *   < 0 empty; Ri [natoms, max_nn, 4] (r, x, y, z), ri_dtype MATPL_F64, or MATPL_F32 with dtype
+ *   MATPL_F32) with 0 < r <= zbl: x = r s_ij 2.134563, phi = sum_k a_k exp(-b_k x) (universal ZBL
+ *   screening), fc = 1 below zbl/2 and 0.5 + 0.5 cos(pi (r - zbl/2) / (zbl/2)) above,
+ *   e = c_ij phi fc / r; Ei[i] += e/2, Etot[image_of[i]] += e/2 (Etot may be NULL), and with
+ *   f = (1/2) de/dr (x, y, z)/r: force[i] += f, force[j] -= f, virial[image_of[i]] -= f (x) r.
+ *   pair_s, pair_c [ntypes, ntypes] f64 = Z_i^0.23 + Z_j^0.23 and 14.399645 Z_i Z_j as the
+ *   reference forms them (torch's default dtype on int64 element numbers).  Ei and force in
+ *   dtype, Etot [nimages] and virial [nimages, 9] f64.  err_dev gets MATPL_KERR_BAD_TYPE /
+ *   MATPL_KERR_BAD_COUNT.
+ */
+int matpl_nep_zbl(int dtype, int ri_dtype, long long natoms, int max_nn, int nimages,
+                  const long long *NL, const void *Ri, const long long *type_map,
+                  const long long *image_of, int ntypes, const double *pair_s,
+                  const double *pair_c, double zbl, void *Ei, double *Etot, void *force,
+                  double *virial, int *err_dev, void *stream);
+
 /* matpl_nep_force_virial: forces force [natoms, 3] and per-image virial virial [nimages, 9]
  *   (both zeroed, then accumulated) of one NEP list from dE [natoms, max_nn, 4] = dE/d(r, x, y,
  *   z) and the rows Ri [natoms, max_nn, 4] = (r, x, y, z): what calculateNepForce with the centre

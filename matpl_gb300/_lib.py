@@ -83,6 +83,7 @@ SIGNATURES = {
     "matpl_dp_desc_dual": (_i, [_i, _ll, _i] + [_vp] * 6),
     "matpl_dp_desc_dual_grad": (_i, [_i, _ll, _i] + [_vp] * 8),
     "matpl_nep_force_virial": (_i, [_i] * 4 + [_vp] * 8),
+    "matpl_nep_zbl": (_i, [_i, _i, _ll, _i, _i] + [_vp] * 4 + [_i, _vp, _vp, _d] + [_vp] * 6),
     "matpl_nep_force_virial_grad": (_i, [_i] * 4 + [_vp] * 8),
     "matpl_lammps_dp_neighbors": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _d, _i,
                                        _vp, _vp, _vp, _vp, _vp, _vp]),

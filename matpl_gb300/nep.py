@@ -3,8 +3,8 @@
 Mirrors the parts of MatPL that the NEP evaluation path reads:
 
 * ``NepConfig``: ``NepParam`` (src/user/nep_param.py:51-83) - cutoff [radial, angular], n_max,
-  basis_size, l_max [3-body, 4-body, 5-body], neuron [hidden, 1], train_2b - plus the element
-  list; ``feature_nums`` follows ``NEP.set_init_nep_param`` (src/model/nep_net.py:111-143).
+  basis_size, l_max [3-body, 4-body, 5-body], neuron [hidden, 1], train_2b, zbl - plus the
+  element list (atomic numbers); ``feature_nums`` follows ``NEP.set_init_nep_param`` (src/model/nep_net.py:111-143).
 * ``init_params``: seeded parameters of the shapes ``NEP`` holds - ``c_param_2``
   [T, T, n_max_r + 1, basis_r + 1], ``c_param_3`` [T, T, n_max_a + 1, basis_a + 1]
   (nep_net.py:160-176), one single-hidden-layer ``FittingNet`` per element
@@ -16,7 +16,7 @@ Mirrors the parts of MatPL that the NEP evaluation path reads:
 * ``pack_params``: the flat device layout of ``matpl_nep_eval``.
 """
 from dataclasses import dataclass, field
-from typing import Dict, List, Sequence
+from typing import Dict, List, Optional, Sequence
 
 import math
 
@@ -33,6 +33,7 @@ class NepConfig:
     l_max: Sequence[int] = (4, 2, 1)
     neuron: int = 30
     train_2b: bool = True
+    zbl: Optional[float] = None     # outer cutoff of the ZBL term (nep_param.zbl), None = off
 
     @property
     def ntypes(self) -> int:
@@ -236,7 +237,8 @@ NEP_PRECISIONS = {"float64": (1, torch.float64), "float32": (0, torch.float32)}
 
 
 class NEP(torch.nn.Module):
-    """Inference NEP on GB300 through ``matpl_nep_eval``.
+    """Inference NEP on GB300 through ``matpl_nep_eval`` (plus ``matpl_nep_zbl`` when the
+    model has a ZBL cutoff).
 
     ``forward`` takes what ``src/model/nep_net.py:NEP.forward`` takes (the six tensors of
     ``calculate_neighbor`` with with_rij, num_atom, atom_type_map) and returns
@@ -322,6 +324,12 @@ class NEP(torch.nn.Module):
                                      *lists, ptr(out["Ei"]), ptr(out["Etot"]), ptr(out["Force"]),
                                      ptr(out["Virial"]), ptr(ws), ws.numel(), stream),
                   "matpl_nep_eval")
+            if self.cfg.zbl is not None:                 # nep_net.py:399-408
+                from . import nep_ops
+                counts = tuple(int(c) for c in num_atom.reshape(-1).tolist())
+                nep_ops.nep_zbl(self.cfg.zbl, self.cfg.atom_type, i64(NL_angular),
+                                f64(Ri_angular), tm, counts, out["Ei"], out["Etot"], out["Force"],
+                                out["Virial"])
         if self.check_errors:
             code = int(self.err.item())
             if code:

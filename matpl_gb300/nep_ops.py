@@ -309,6 +309,58 @@ def nep_force_virial(NL: torch.Tensor, dE: torch.Tensor, Ri: torch.Tensor, num_a
     return [F, V]
 
 
+ZBL_K = 14.399645       # e^2 / (4 pi eps0) in eV A, nep_net.py:223
+_zbl_tables = {}
+
+
+def zbl_tables(atom_type, dev):
+    """(pair_s, pair_c) [T, T] f64 on dev: Z_i^0.23 + Z_j^0.23 and K Z_i Z_j in float32 as
+    cal_zbl (nep_net.py:985-989) forms them under torch's default float32 dtype: the powers
+    rounded to float32, their sum and the products rounded in float32.  Z^0.23 is taken as the
+    correctly rounded float32 value (float64 pow, then rounded): torch's own float32 pow, which
+    the reference calls, is not correctly rounded everywhere and depends on where an element
+    sits in the tensor (on x86 one call gives 2.6741543 and 2.6741545 for Z = 72, and one ulp off
+    for Z = 98, 101-103, 110, 115, 116 in an arange), so no fixed table reproduces it pair for
+    pair.  Cached per (elements, device)."""
+    key = (tuple(int(z) for z in atom_type), dev)
+    t = _zbl_tables.get(key)
+    if t is None:
+        Z = np.array(key[0], dtype=np.float64)
+        f = (Z ** np.float64(np.float32(0.23))).astype(np.float32)
+        s = f.reshape(-1, 1) + f.reshape(1, -1)                          # float32 adds
+        Zf = Z.astype(np.float32)
+        c = (np.float32(ZBL_K) * Zf.reshape(-1, 1)) * Zf.reshape(1, -1)   # float32 products
+        t = (torch.tensor(s.astype(np.float64), device=dev),
+             torch.tensor(c.astype(np.float64), device=dev))
+        _zbl_tables[key] = t
+    return t
+
+
+def nep_zbl(zbl: float, atom_type, NL_a: torch.Tensor, Ri_a: torch.Tensor,
+            type_map: torch.Tensor, counts, Ei: torch.Tensor, Etot, force: torch.Tensor,
+            virial: torch.Tensor) -> None:
+    """Adds the ZBL term (``matpl_nep_zbl``; nep_net.py:399-408, 916-991) of the angular list
+    to Ei [N], Etot [B] f64 (or None), force [N, 3] (Ei's dtype) and virial [B, 9] f64 in
+    place: per pair 0 < r <= zbl, e = K Z_i Z_j phi(r (Z_i^0.23 + Z_j^0.23) / 0.46848) fc(r) / r,
+    half of it to the centre.  Frames contiguous with sizes ``counts``."""
+    _require_cuda(NL_a, Ri_a, type_map, Ei, force, virial)
+    dev = Ei.device
+    N, NN = NL_a.shape
+    pair_s, pair_c = zbl_tables(atom_type, dev)
+    nl = NL_a.contiguous().to(torch.int64)
+    tm = type_map.reshape(-1).contiguous().to(torch.int64)
+    R = Ri_a.detach().contiguous()
+    if R.dtype != torch.float64 and Ei.dtype == torch.float64:
+        R = R.to(torch.float64)
+    img = _image_index(tuple(int(c) for c in counts), dev)
+    if virial.dtype != torch.float64 or not virial.is_contiguous():
+        raise _lib.MatplError("nep_zbl: virial must be a contiguous float64 tensor")
+    check(_lib.load().matpl_nep_zbl(
+        _dtype_code(Ei), _dtype_code(R), N, NN, len(counts), ptr(nl), ptr(R), ptr(tm), ptr(img),
+        len(atom_type), ptr(pair_s), ptr(pair_c), float(zbl), ptr(Ei), ptr(Etot), ptr(force),
+        ptr(virial), ptr(_err_word(dev)), _stream(dev)), "matpl_nep_zbl")
+
+
 class _NepVirial(torch.autograd.Function):
     @staticmethod
     def forward(ctx, list_neigh, dE, Rij, Ri_d, num_atom):

@@ -137,6 +137,16 @@ class NEPTrain(torch.nn.Module):
         feats = torch.cat(feats, -1)
         Ei = self.calculate_Ei(tm, self.q_scaler * feats, type_index)
         counts = tuple(int(c) for c in num_atom.reshape(-1).tolist())
+        zbl = None
+        if cfg.zbl is not None:
+            # ZBL term (nep_net.py:399-408, 916-991): parameter-free, so its energy, forces and
+            # virial enter as constants
+            zbl = (torch.zeros(N, dtype=dt, device=Ri.device),
+                   torch.zeros(N, 3, dtype=dt, device=Ri.device),
+                   torch.zeros(len(counts), 9, dtype=torch.float64, device=Ri.device))
+            nep_ops.nep_zbl(cfg.zbl, cfg.atom_type, NL_angular, Ra, tm, counts, zbl[0], None,
+                            zbl[1], zbl[2])
+            Ei = Ei + zbl[0]
         Etot = _image_sum(Ei, counts).unsqueeze(-1)
         Egroup = None
         if Egroup_weight is not None and divider is not None:
@@ -159,6 +169,9 @@ class NEPTrain(torch.nn.Module):
             F_l, V_l = nep_ops.nep_force_virial(NL, dE, R, counts)
             Force = Force + F_l
             Virial = Virial + V_l
+        if zbl is not None:          # physical force / virial of the ZBL term: -(op convention)
+            Force = Force - zbl[1]
+            Virial = Virial - zbl[2].to(dt)
         return Etot, Ei, -Force, Egroup, -Virial
 
 

@@ -15,8 +15,12 @@ FP64 CPU restatement of MatPL's NEP evaluation path.
   autograd with Ri = (r, x, y, z) as the leaf, forces and virial as ``calculate_force_virial``'s
   CPU branch (nep_net.py:486-560): contraction with Ri_d (Ri_d[0][a] = x_a / r, Ri_d[1+a][a] = 1),
   scatter to the neighbors, upper-triangle virial mirrored, both negated.
+* ``zbl_energy``: the ZBL term of ``NEP.calculate_zbl`` / ``cal_zbl`` (nep_net.py:916-991),
+  added to Ei when the model's ``zbl`` (outer cutoff) is set and some angular pair lies in
+  (0, zbl) (nep_net.py:399-408); its forces follow from the same autograd leaf.
 """
 import ctypes
+import math
 from typing import Dict
 
 import numpy as np
@@ -37,6 +41,10 @@ C4B = [-0.007499480826664, -0.134990654879954, 0.067495327439977, 0.404971964639
        -0.809943929279723]
 C5B = [0.026596810706114, 0.053193621412227, 0.026596810706114]
 L_SLICES = [(0, 3), (3, 8), (8, 15), (15, 24)]
+
+# ZBL universal screening function (Ziegler, Biersack, Littmark) as nep_net.py:222-224 holds it
+ZBL_K = 14.399645            # e^2 / (4 pi eps0) in eV A
+ZBL_PARA = [0.18175, 3.1998, 0.50986, 0.94229, 0.28022, 0.4029, 0.02817, 0.20162]
 
 _lib = None
 
@@ -234,10 +242,62 @@ def _force_virial(dE, Ri, NL, num_atom):
     return F[1:], V
 
 
+def zbl_energy(cfg, type_map, NL_a, Ra, factors: str = "torch"):
+    """Ei_zbl [N] (differentiable in Ra) following cal_zbl (nep_net.py:957-991) on the
+    angular list restricted to r <= zbl (calculate_zbl :916-955), or None when no pair lies in
+    (0, zbl) (the gate of nep_net.py:399-402).
+
+    factors "torch": the element factors exactly as the reference forms them - Z**0.23 and
+    K * Z_i * Z_j of int64 element numbers under torch's default float32 dtype, pair by pair in
+    the masked order.  torch's float32 pow is not correctly rounded everywhere and its result
+    depends on where an element sits in the tensor (vectorised body or scalar tail; Z = 72 gives
+    both 2.6741543 and 2.6741545 in one call on x86), so this mode pins the reference bit for
+    bit only on the reference's own layout.  factors "rounded": the correctly rounded float32
+    Z^0.23, float32 sums and products per element pair - the values the GPU kernel uses."""
+    if cfg.zbl is None:
+        return None
+    rc = float(cfg.zbl) / 2
+    r_all = Ra[:, :, 0]
+    if not bool(((r_all > 0) & (r_all < cfg.zbl)).any()):
+        return None
+    keep = (r_all <= cfg.zbl) & (torch.as_tensor(NL_a) != -1)
+    r = torch.where(keep, r_all, torch.zeros_like(r_all))
+    Z = torch.tensor(list(cfg.atom_type), dtype=torch.int64)
+    tm = torch.as_tensor(type_map).long()
+    tj = torch.where(keep, tm[torch.as_tensor(NL_a).clamp(min=0)], torch.zeros_like(tm[:1]))
+    zi = Z[tm].unsqueeze(1).expand_as(tj)[keep]
+    zj = Z[tj][keep]
+    rk = r[keep]
+    fc = torch.ones_like(rk)
+    mid = (rk.abs() >= rc) & (rk <= 2 * rc)
+    fc = torch.where(mid, 0.5 + 0.5 * torch.cos((math.pi / rc) * (rk - rc)), fc)
+    fc = torch.where(rk.abs() < rc, torch.ones_like(rk), fc)
+    if factors == "torch":
+        x = rk * (zi ** 0.23 + zj ** 0.23) * 2.134563
+        c = ZBL_K * zi * zj
+    else:
+        Zn = np.array(list(cfg.atom_type), dtype=np.float64)
+        f = (Zn ** np.float64(np.float32(0.23))).astype(np.float32)
+        Zf = Zn.astype(np.float32)
+        s_tab = torch.tensor((f.reshape(-1, 1) + f.reshape(1, -1)).astype(np.float64))
+        c_tab = torch.tensor(((np.float32(ZBL_K) * Zf.reshape(-1, 1)) * Zf.reshape(1, -1))
+                             .astype(np.float64))
+        ti_k = tm.unsqueeze(1).expand_as(tj)[keep]
+        tj_k = tj[keep]
+        x = rk * s_tab[ti_k, tj_k] * 2.134563
+        c = c_tab[ti_k, tj_k]
+    phi = ZBL_PARA[0] * torch.exp(-ZBL_PARA[1] * x) + ZBL_PARA[2] * torch.exp(-ZBL_PARA[3] * x) + \
+        ZBL_PARA[4] * torch.exp(-ZBL_PARA[5] * x) + ZBL_PARA[6] * torch.exp(-ZBL_PARA[7] * x)
+    e = c * phi * fc / rk
+    full = torch.zeros(r.shape, dtype=e.dtype)
+    full = full.masked_scatter(keep, e)
+    return 0.5 * full.sum(-1)
+
+
 def nep_eval(cfg, p: Dict[str, torch.Tensor], num_atom, type_map, NL_r, Ri_r, NL_a, Ri_a,
-             return_feats: bool = False):
+             return_feats: bool = False, zbl_factors: str = "torch"):
     """Etot [B, 1], Ei [N], Force [N, 3], Virial [B, 9] (physical force and virial, i.e. the
-    values ``NEP.forward`` returns)."""
+    values ``NEP.forward`` returns); ``zbl_factors`` as in ``zbl_energy``."""
     num_atom = np.asarray(num_atom).reshape(-1)
     type_map = torch.as_tensor(type_map)
     NL_r, NL_a = torch.as_tensor(NL_r), torch.as_tensor(NL_a)
@@ -245,13 +305,16 @@ def nep_eval(cfg, p: Dict[str, torch.Tensor], num_atom, type_map, NL_r, Ri_r, NL
     Ra = torch.as_tensor(Ri_a, dtype=torch.float64).clone().requires_grad_()
     feats = features(cfg, p, type_map, NL_r, Rr, NL_a, Ra)
     Ei = fitting(cfg, p, type_map, feats * p["q_scaler"])
+    ez = zbl_energy(cfg, type_map, NL_a, Ra, zbl_factors)
+    if ez is not None:
+        Ei = Ei + ez
     Etot = torch.stack([e.sum() for e in Ei.split(num_atom.tolist())]).unsqueeze(-1)
-    leaves = ([Rr] if cfg.train_2b else []) + ([Ra] if cfg.l_max[0] > 0 else [])
+    leaves = ([Rr] if cfg.train_2b else []) + ([Ra] if (cfg.l_max[0] > 0 or ez is not None) else [])
     grads = torch.autograd.grad(Etot.sum(), leaves, allow_unused=True)
     F = torch.zeros(Ei.shape[0], 3, dtype=torch.float64)
     V = torch.zeros(len(num_atom), 9, dtype=torch.float64)
     gi = 0
-    for R, NL, on in ((Rr, NL_r, cfg.train_2b), (Ra, NL_a, cfg.l_max[0] > 0)):
+    for R, NL, on in ((Rr, NL_r, cfg.train_2b), (Ra, NL_a, cfg.l_max[0] > 0 or ez is not None)):
         if not on:
             continue
         g = grads[gi]

@@ -86,7 +86,9 @@ class NepCase:
                                 n_max=tuple(int(x) for x in g["n_max"]),
                                 basis_size=tuple(int(x) for x in g["basis_size"]),
                                 l_max=tuple(int(x) for x in g["l_max"]),
-                                neuron=int(g["neuron"]), train_2b=bool(g["train_2b"]))
+                                neuron=int(g["neuron"]), train_2b=bool(g["train_2b"]),
+                                zbl=(float(g["zbl"]) if "zbl" in g and not np.isnan(g["zbl"])
+                                     else None))
         self.frames = NP.NepFrames(g["position"].copy(), g["type_map"], g["num_atom"], g["box"],
                                    g["box_orig"], g["num_cell"])
         self.params = NP.init_params(self.cfg, int(g["seed_w"]), energy_shift=-3.0)

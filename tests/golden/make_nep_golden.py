@@ -13,7 +13,7 @@ the committed ``nep_*.npz`` files are what the tests read.  For each case it
    evaluates ``forward`` in FP64,
 4. stores the inputs, the seeds, checksums of the neighbor lists, the descriptors and E/F/V.
 
-Usage:  python tests/golden/make_nep_golden.py
+Usage:  python tests/golden/make_nep_golden.py [case names]   (default: every case)
 """
 import hashlib
 import os
@@ -54,7 +54,7 @@ def reference_nep_class():
 
 def fake_input_param(cfg: NP.NepConfig):
     nep_param = _types.SimpleNamespace(
-        zbl=None, c2_param=None, c3_param=None, q_scaler=None, model_wb=None,
+        zbl=cfg.zbl, c2_param=None, c3_param=None, q_scaler=None, model_wb=None,
         bias_lastlayer=None, cutoff=list(cfg.cutoff), n_max=list(cfg.n_max),
         basis_size=list(cfg.basis_size), l_max=list(cfg.l_max), neuron=[cfg.neuron, 1],
         train_2b=cfg.train_2b)
@@ -118,6 +118,7 @@ def run_case(name, cfg: NP.NepConfig, structs, seed_w, NEP, ops):
         name=name, seed_w=seed_w, atom_type=np.array(cfg.atom_type), cutoff=np.array(cfg.cutoff),
         n_max=np.array(cfg.n_max), basis_size=np.array(cfg.basis_size),
         l_max=np.array(cfg.l_max), neuron=cfg.neuron, train_2b=cfg.train_2b,
+        zbl=np.nan if cfg.zbl is None else float(cfg.zbl),
         position=fr.position, type_map=fr.type_map, num_atom=fr.num_atom, box=fr.box,
         box_orig=fr.box_orig, num_cell=fr.num_cell, lattice=np.stack([s.lattice for s in structs]),
         max_r=max_r, max_a=max_a, cnt_r=cnt_r.numpy(), cnt_a=cnt_a.numpy(),
@@ -131,21 +132,34 @@ def run_case(name, cfg: NP.NepConfig, structs, seed_w, NEP, ops):
           "max_r", max_r, "max_a", max_a, "Etot", Etot.detach().numpy().ravel())
 
 
-def main():
+def main(which=None):
     NEP, ops = reference_nep_class()
+    want = (lambda n: which is None or n in which)  # noqa: E731
     cfg4 = NP.NepConfig(atom_type=[3, 14, 8, 72])
-    st = structures.random_packed(240, 0.06, [3, 14, 8, 72], [0.25] * 4, seed=41)
-    run_case("nep_q4_240", cfg4, [st], seed_w=401, NEP=NEP, ops=ops)
+    if want("nep_q4_240"):
+        st = structures.random_packed(240, 0.06, [3, 14, 8, 72], [0.25] * 4, seed=41)
+        run_case("nep_q4_240", cfg4, [st], seed_w=401, NEP=NEP, ops=ops)
     # two triclinic frames, small enough that the box is replicated (num_cell > 1)
-    a = structures.random_packed(40, 0.06, [3, 14, 8, 72], [0.25] * 4, seed=42, strain=0.04)
-    b = structures.random_packed(64, 0.06, [3, 14, 8, 72], [0.25] * 4, seed=43, strain=0.04)
-    run_case("nep_q4_tri2", cfg4, [a, b], seed_w=402, NEP=NEP, ops=ops)
+    if want("nep_q4_tri2"):
+        a = structures.random_packed(40, 0.06, [3, 14, 8, 72], [0.25] * 4, seed=42, strain=0.04)
+        b = structures.random_packed(64, 0.06, [3, 14, 8, 72], [0.25] * 4, seed=43, strain=0.04)
+        run_case("nep_q4_tri2", cfg4, [a, b], seed_w=402, NEP=NEP, ops=ops)
     # 3-body only (no 4-body / 5-body), two elements, a wider hidden layer
-    cfg_b = NP.NepConfig(atom_type=[8, 72], cutoff=(5.0, 3.5), n_max=(3, 5), basis_size=(6, 7),
-                         l_max=(4, 0, 0), neuron=40)
-    c = structures.random_packed(150, 0.07, [8, 72], [2 / 3, 1 / 3], seed=44, strain=0.02)
-    run_case("nep_hfo_l4", cfg_b, [c], seed_w=403, NEP=NEP, ops=ops)
+    if want("nep_hfo_l4"):
+        cfg_b = NP.NepConfig(atom_type=[8, 72], cutoff=(5.0, 3.5), n_max=(3, 5),
+                             basis_size=(6, 7), l_max=(4, 0, 0), neuron=40)
+        c = structures.random_packed(150, 0.07, [8, 72], [2 / 3, 1 / 3], seed=44, strain=0.02)
+        run_case("nep_hfo_l4", cfg_b, [c], seed_w=403, NEP=NEP, ops=ops)
+    # the ZBL term (outer cutoff 2.2 A, inner 1.1 A): atoms packed down to 0.9 A (first frame)
+    # and 1.3 A (second) so that pairs fall in both the inner and the switching region
+    if want("nep_zbl"):
+        cfg_z = NP.NepConfig(atom_type=[3, 14, 8, 72], zbl=2.2)
+        a = structures.random_packed(96, 0.07, [3, 14, 8, 72], [0.25] * 4, seed=45,
+                                     min_dist=0.9)
+        b = structures.random_packed(80, 0.07, [3, 14, 8, 72], [0.25] * 4, seed=46,
+                                     min_dist=1.3, strain=0.03)
+        run_case("nep_zbl", cfg_z, [a, b], seed_w=404, NEP=NEP, ops=ops)
 
 
 if __name__ == "__main__":
-    main()
+    main(set(sys.argv[1:]) or None)

@@ -324,3 +324,32 @@ def test_descriptor_matches_reference_fixture(nep_case, name):
         f = m.descriptor(NN_r, NL_r, Ri_r, NN_a, NL_a, Ri_a, t(g["num_atom"]), t(g["type_map"]))
         f = f.double().cpu().numpy()
         assert np.all(np.abs(f - g["feats"]) <= tol * scale), prec
+
+
+def test_eval_zbl_matches_oracle_and_reference(nep_case):
+    """The ZBL term (outer cutoff 2.2 A; pairs in the inner and the switching region, two
+    frames).  FP64 = the oracle with the kernel's correctly rounded float32 element factors to
+    1e-10 (E to 1e-12); = the reference's own values (golden) to 1e-7 relative: the reference's
+    float32 Z^0.23 (torch pow) is one ulp off for some pairs; FP32 within 1e-5 of the force and
+    virial scale."""
+    c = nep_case("nep_zbl")
+    g = c.g
+    lists = (c.NN_r, c.NN_a, c.NL_r, c.NL_a, c.Ri_r, c.Ri_a)
+    ref = NO.nep_eval(c.cfg, c.params, g["num_atom"], torch.tensor(g["type_map"]),
+                      torch.tensor(c.NL_r), torch.tensor(c.Ri_r), torch.tensor(c.NL_a),
+                      torch.tensor(c.Ri_a), zbl_factors="rounded")
+    rE, rF, rV = ref["Etot"].numpy().ravel(), ref["Force"].numpy(), ref["Virial"].numpy()
+    E, Ei, F, V = _eval(c.cfg, c.params, lists, g["num_atom"], g["type_map"], "float64")
+    np.testing.assert_allclose(E.ravel(), rE, rtol=1e-12)
+    np.testing.assert_allclose(Ei, ref["Ei"].numpy(), rtol=0, atol=1e-11 * np.abs(rE).max())
+    np.testing.assert_allclose(F, rF, rtol=0, atol=1e-10 * np.abs(rF).max())
+    np.testing.assert_allclose(V, rV, rtol=0, atol=1e-10 * np.abs(rV).max())
+    np.testing.assert_allclose(E.ravel(), g["Etot"].ravel(), rtol=1e-7)
+    np.testing.assert_allclose(F, g["Force"], rtol=0, atol=1e-7 * np.abs(g["Force"]).max())
+    np.testing.assert_allclose(V, g["Virial"], rtol=0, atol=1e-7 * np.abs(g["Virial"]).max())
+    E, Ei, F, V = _eval(c.cfg, c.params, lists, g["num_atom"], g["type_map"], "float32")
+    print(f"[accuracy] nep zbl f32: force max err / max |F| "
+          f"{np.abs(F - rF).max() / np.abs(rF).max():.2e}")
+    np.testing.assert_allclose(E.ravel(), rE, rtol=1e-5)
+    np.testing.assert_allclose(F, rF, rtol=0, atol=1e-5 * np.abs(rF).max())
+    np.testing.assert_allclose(V, rV, rtol=0, atol=1e-5 * np.abs(rV).max())

@@ -208,3 +208,30 @@ def test_force_virial_kernel_equals_public_ops(nep_case, case):
         g2 = torch.autograd.grad((F2 * gF).sum() + (V2 * gV).sum(), dE)[0]
         close(g1, g2.cpu().numpy(), 1e-13)
     nep_ops.check_errors()
+
+
+def test_zbl_term_in_training_forward(nep_case):
+    """NEPTrain with the ZBL term (outer cutoff 2.2 A, pairs in the inner and the switching
+    region), FP64: E, F, V = the oracle with the kernel's float32 element factors (1e-10) and the
+    reference's own values (golden, 1e-7: its float32 Z^0.23 is one ulp off for some pairs); the
+    training gradient = the oracle's (the ZBL term has no parameters: it enters as constants)."""
+    c = nep_case("nep_zbl")
+    g = c.g
+    N = c.NL_r.shape[0]
+    B = len(g["num_atom"])
+    rng = np.random.default_rng(8)
+    gE, gF, gV = rng.standard_normal(B), rng.standard_normal((N, 3)), rng.standard_normal((B, 9))
+    Etot, F, V, grads = run_step(nep_train_model(c), c, gE, gF, gV)
+    ref = NO.nep_eval(c.cfg, c.params, g["num_atom"], torch.tensor(g["type_map"]),
+                      torch.tensor(c.NL_r), torch.tensor(c.Ri_r), torch.tensor(c.NL_a),
+                      torch.tensor(c.Ri_a), zbl_factors="rounded")
+    close(Etot.reshape(-1), ref["Etot"].numpy().reshape(-1), 1e-12)
+    close(F, ref["Force"].numpy(), 1e-10)
+    close(V, ref["Virial"].numpy(), 1e-10)
+    close(Etot.reshape(-1), g["Etot"].reshape(-1), 1e-7)     # the reference's own values
+    close(F, g["Force"], 1e-7)
+    ref = NO.train_grads(c.cfg, c.params, g["num_atom"], g["type_map"], c.NL_r, c.Ri_r, c.NL_a,
+                         c.Ri_a, gE, gF, gV)
+    for k, v in ref.items():
+        close(grads[k], v.numpy(), 1e-10)
+    nep_ops.check_errors()

@@ -9,7 +9,7 @@ import torch
 from matpl_gb300 import nep as NP
 from oracle import nep_oracle as NO
 
-CASES = ["nep_q4_240", "nep_q4_tri2", "nep_hfo_l4"]
+CASES = ["nep_q4_240", "nep_q4_tri2", "nep_hfo_l4", "nep_zbl"]
 
 
 def _sha(a):
