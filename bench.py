@@ -682,12 +682,20 @@ def run_dp_variants(args, ws, local):
     ms = timed(C.CompressedDP(cfg, prm, davg, dstd, comp, dtype=torch.float32, device=dev))
     out["compressed_order5"] = {"ms_per_step": ms, "value": ws * VARIANT_ATOMS / (ms * 1e-3),
                                 "table_rows": int(comp["table"].shape[1])}
+    # the same table in the fused FP32 kernels (matpl_dp_eval with ctable)
+    fused = C.fused_model(cfg, prm, davg, dstd, comp, "float32", dev)
+    fused.check_errors = False
+    ms = timed(fused)
+    out["compressed_order5_fused"] = {"ms_per_step": ms,
+                                      "value": ws * VARIANT_ATOMS / (ms * 1e-3),
+                                      "form": "fused FP32 kernels, table polynomial in place of "
+                                              "the embedding nets"}
     vec = {3: [0.0185, 0.0216, 0.3], 14: [0.1204, 0.0985, 0.2]}
     tprm = init_type_params(cfg, 3, SEED_W)
     ms = timed(TypeDP(cfg, tprm, davg, dstd, vec, dtype=torch.float32, device=dev))
     out["type_embedding"] = {"ms_per_step": ms, "value": ws * VARIANT_ATOMS / (ms * 1e-3)}
     return {"metric": "DP variant E+F+virial atom-steps/s (reference structure on this "
-                      "library's operators, FP32)", "unit": "atom-steps/s",
+                      "library's operators, FP32; compressed also fused)", "unit": "atom-steps/s",
             "config": {"workload": f"{VARIANT_ATOMS}-atom Li/Si box, m=150/type, Rc 6",
                        "cpu_baseline": "none on the GPU box (the reference's Python is not "
                                        "there); parity is pinned by the golden fixtures"},

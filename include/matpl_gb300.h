@@ -35,6 +35,7 @@ typedef enum {
 #define MATPL_KERR_NEIGHBOR_OVERFLOW 1   /* a type block exceeds m (NeighConst.f90:75-78) */
 #define MATPL_KERR_BAD_TYPE 2            /* atom type index outside [0, ntypes) */
 #define MATPL_KERR_TIMEOUT 3             /* a bounded tensor-core completion wait gave up */
+#define MATPL_KERR_TABLE_RANGE 6         /* compressed model: s outside the table's grid */
 
 /* Compute forms.  MIXED*: FP32 data, embedding and fitting GEMMs on the tensor cores
  * (tcgen05, BF16 operands, FP32 accumulation in TMEM), FP64 energy / virial reductions.
@@ -171,6 +172,16 @@ typedef struct {
     const void *davg;       /* [ntypes,4] per centre type (device, compute dtype) */
     const void *dstd;       /* [ntypes,4] */
     int32_t *err_dev;       /* device int32 for kernel error codes (MATPL_KERR_*), or NULL */
+    /* Compressed model (src/user/ckpt_compress.py tables, evaluated like
+     * calc_compress_polynomial, src/model/dp_dp.py:572-601); ctable == NULL (zero-initialise
+     * the struct) keeps the embedding nets.  ctable: [ntypes^2 * ctab_rows, 25, ctab_order + 1]
+     * in the compute dtype (coefficients highest power first); ctab_dx, ctab_smin, ctab_smax:
+     * the grid's dx, sij_min, sij_max.  MATPL_F32 / MATPL_F64 forms only; an s outside the
+     * table sets MATPL_KERR_TABLE_RANGE. */
+    const void *ctable;
+    int ctab_rows;
+    int ctab_order;
+    double ctab_dx, ctab_smin, ctab_smax;
 } matpl_dp_model;
 
 size_t matpl_dp_param_count(int ntypes);

@@ -24,7 +24,8 @@ class MatplDpModel(ctypes.Structure):
     """Mirror of ``matpl_dp_model``."""
     _fields_ = [("ntypes", _i), ("m", _i), ("npresent", _i), ("present", _i * 8),
                 ("rmin", _d), ("rmax", _d), ("params", _vp), ("davg", _vp), ("dstd", _vp),
-                ("err_dev", _vp)]
+                ("err_dev", _vp), ("ctable", _vp), ("ctab_rows", _i), ("ctab_order", _i),
+                ("ctab_dx", _d), ("ctab_smin", _d), ("ctab_smax", _d)]
 
 
 class MatplNepModel(ctypes.Structure):

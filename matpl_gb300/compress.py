@@ -8,8 +8,10 @@ CalcOps.cpp:331-383).
   it) and per type pair and embedding output the Hermite coefficients of each grid interval
   from G, dG/ds (order 3, ``dp_model_compress_3order``, :110-150) and d2G/ds2 (order 5,
   ``dp_model_compress_5order``, :152-227), derivatives by autograd through the nets.
-* ``CompressedDP`` is ``train.DPTrainModel`` (environment matrix, contraction, fitting nets,
-  forces / virial through this library's operators) with the embedding taken from the table:
+* ``fused_model`` runs the table inside the fused FP32 / FP64 evaluation kernels (the
+  production path); ``CompressedDP`` is the reference's structure on this library's operators
+  (``train.DPTrainModel``: environment matrix, contraction, fitting nets, forces / virial) with
+  the embedding taken from the table:
   the interval index and offset of ``calc_compress_polynomial`` (including its float32 grid
   point and the coarse-region index it uses as it is) and the polynomial from
   ``ops.calculateCompress`` (csrc/compress.cu), differentiable in s for the forces.
@@ -112,6 +114,15 @@ def build_table(cfg: DPConfig, params: Dict[str, torch.Tensor], davg, dstd, sij_
     return {"table": table, "dx": dx, "order": order, "sij_min": smin, "sij_max": smax,
             "sij_out_max": out_max, "sij_len": len_sij, "sij_out_len": len_out,
             "davg": np.asarray(davg)[:, 0], "dstd": np.asarray(dstd)[:, 0]}
+
+
+def fused_model(cfg: DPConfig, params: Dict[str, torch.Tensor], davg, dstd, compress: Dict,
+                precision: str = "float64", device="cuda"):
+    """The compressed model in the fused evaluation (``matpl_dp_eval`` with the table in
+    ``matpl_dp_model.ctable``: environment row, table polynomial, descriptor, fitting nets,
+    adjoint and force / virial scatter in the FP32 / FP64 kernels, no per-slot tensors)."""
+    from .dp import DP
+    return DP(cfg, params, davg, dstd, precision=precision, device=device, compress=compress)
 
 
 class CompressedDP(DPTrainModel):

@@ -50,7 +50,47 @@ struct EvalParams {
     int present_mask;     // bit t set when model type t is an image type
     double rmin, rmax;
     double inv_mT;        // 1 / (m * npresent)   (dp_dp.py:413)
+    // compressed model (tabulated embedding), ctab == NULL: embedding nets
+    const void *ctab;     // [ntypes^2 * crows][E][cnc]
+    int crows, cnc;
+    double cdx, cdx10, csmin, csmax;
+    int *err;
 };
+
+// --------------------------------------------------------------------------- compressed model
+// G(s) and dG/ds of one type pair from the tables of calc_compress_polynomial (dp_dp.py:572-601):
+// fine grid below smax (interval dx from smin), coarse grid of 10 dx above it; the interval
+// index truncates; the grid point xk is formed in float32 (the reference multiplies the int64
+// index by the Python float step under torch's float32 default dtype) and f2 = s - xk in the
+// compute dtype; the row is idx + k * rows in both grids (the reference adds no offset for the
+// coarse grid either); polynomial coefficients highest power first (calculateCompress).
+template <typename T>
+__device__ __forceinline__ void cmp_forward(const T *__restrict__ tab, int k, T s,
+                                            const EvalParams &P, T G[E], T dG[E]) {
+    const bool fine = s < (T)P.csmax;
+    const T xr = fine ? (s - (T)P.csmin) / (T)P.cdx : (s - (T)P.csmax) / (T)P.cdx10;
+    long long idx = (long long)xr;
+    const float fi = (float)idx;
+    const float xk = fine ? __fadd_rn(__fmul_rn(fi, (float)P.cdx), (float)P.csmin)
+                          : __fadd_rn((float)P.csmax, __fmul_rn(__fmul_rn(fi, (float)P.cdx), 10.f));
+    const T f2 = s - (T)xk;
+    if (idx < 0 || idx >= P.crows) {
+        if (P.err) atomicOr(P.err, MATPL_KERR_TABLE_RANGE);
+        idx = idx < 0 ? 0 : P.crows - 1;
+    }
+    const T *c = tab + ((long long)k * P.crows + idx) * E * P.cnc;
+#pragma unroll
+    for (int o = 0; o < E; ++o) {
+        const T *co = c + o * P.cnc;
+        T g = co[0], dg = T(0);
+        for (int q = 1; q < P.cnc; ++q) {
+            dg = dg * f2 + g;
+            g = g * f2 + co[q];
+        }
+        G[o] = g;
+        if (dG) dG[o] = dg;
+    }
+}
 
 // --------------------------------------------------------------------------- embedding MLP
 // x[E] <- emb(s); optionally saves layer-1/2 tanh outputs (strided by `st`) and returns the
@@ -97,14 +137,16 @@ __device__ __forceinline__ void emb_forward(const T *__restrict__ w, T s, T x[E]
 // --------------------------------------------------------------------------- dp_pad
 template <typename T>
 __global__ void dp_pad(const T *__restrict__ params, const T *__restrict__ davg,
-                       const T *__restrict__ dstd, T *__restrict__ pad, int ntypes) {
+                       const T *__restrict__ dstd, T *__restrict__ pad, int ntypes,
+                       EvalParams P) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= ntypes * ntypes) return;
     const int ti = k / ntypes;
     T rp[4];
     for (int c = 0; c < 4; ++c) rp[c] = (T(0) - davg[4 * ti + c]) / dstd[4 * ti + c];
     T x[E], t3[E];
-    emb_forward<T, false>(params + (long long)k * EmbOff::SIZE, rp[0], x, t3, nullptr, nullptr, 0);
+    if (P.ctab) cmp_forward<T>((const T *)P.ctab, k, rp[0], P, x, nullptr);
+    else emb_forward<T, false>(params + (long long)k * EmbOff::SIZE, rp[0], x, t3, nullptr, nullptr, 0);
     for (int c = 0; c < 4; ++c)
         for (int p = 0; p < E; ++p) pad[(long long)k * NA + c * E + p] = rp[c] * x[p];
 }
@@ -141,7 +183,7 @@ __device__ __forceinline__ void stage_weights(const T *__restrict__ src, T *dst,
 }
 
 // --------------------------------------------------------------------------- dp_embed_fwd
-template <typename T, bool WS>
+template <typename T, bool WS, bool CMP>
 __global__ void __launch_bounds__(kWarps * 32)
 dp_embed_fwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
              const int32_t *__restrict__ type_map, const T *__restrict__ params,
@@ -188,7 +230,8 @@ dp_embed_fwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
             env_row(R, px, py, pz, (T)P.rmin, (T)P.rmax, avg, sd, rh);
             const T *w = WS ? wsm + (ti * P.ntypes + tj) * EmbOff::SIZE
                             : params + (long long)(ti * P.ntypes + tj) * EmbOff::SIZE;
-            emb_forward<T, false>(w, rh[0], x, t3, nullptr, nullptr, 0);
+            if (CMP) cmp_forward<T>((const T *)P.ctab, ti * P.ntypes + tj, rh[0], P, x, nullptr);
+            else emb_forward<T, false>(w, rh[0], x, t3, nullptr, nullptr, 0);
             if (k >= cnt) {
 #pragma unroll
                 for (int c = 0; c < 4; ++c) rh[c] = T(0);
@@ -468,7 +511,7 @@ dp_fit(const T *__restrict__ Ain, const int32_t *__restrict__ type_map,
 }
 
 // --------------------------------------------------------------------------- dp_embed_bwd
-template <typename T, bool WS>
+template <typename T, bool WS, bool CMP>
 __global__ void __launch_bounds__(kWarps * 32)
 dp_embed_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
              const int32_t *__restrict__ type_map, const T *__restrict__ params,
@@ -521,7 +564,8 @@ dp_embed_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
                 const T *w = WS ? wsm + (ti * P.ntypes + tj) * EmbOff::SIZE
                                 : params + (long long)(ti * P.ntypes + tj) * EmbOff::SIZE;
                 T x[E], h[E];
-                emb_forward<T, true>(w, rh[0], x, h, t1s, t2s, 32);
+                if (CMP) cmp_forward<T>((const T *)P.ctab, ti * P.ntypes + tj, rh[0], P, x, h);
+                else emb_forward<T, true>(w, rh[0], x, h, t1s, t2s, 32);
                 // dE/dR_k[c] = sum_p dA[c][p] G[p];  dE/dG[p] = sum_c dA[c][p] R_k[c]
                 T g[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
@@ -535,6 +579,12 @@ dp_embed_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
                            dAs[3 * E + p] * rh[3];
                 }
                 __syncwarp();
+                T dsv = T(0);
+                if (CMP) {
+                    // tabulated embedding: dE/ds = sum_p dE/dG[p] dG[p]/ds (dG in h)
+#pragma unroll
+                    for (int p = 0; p < E; ++p) dsv += x[p] * h[p];
+                } else {
                 // layer 2 adjoint: G = t3*dt2 + x2
 #pragma unroll
                 for (int o = 0; o < E; ++o) h[o] = x[o] * w[EmbOff::DT2 + o] * (T(1) - h[o] * h[o]);
@@ -561,11 +611,11 @@ dp_embed_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
                 }
                 __syncwarp();
                 // layer 0 adjoint: x1 = tanh(s W0 + b0)
-                T dsv = T(0);
 #pragma unroll
                 for (int o = 0; o < E; ++o) {
                     const T tv = t1s[o * 32];
                     dsv += w[EmbOff::W0 + o] * x[o] * (T(1) - tv * tv);
+                }
                 }
                 g[0] += dsv;
                 T f[3];
@@ -711,20 +761,22 @@ int launch_eval(int mode, const matpl_dp_model *M, const EvalParams &P,
     const int nnet = P.ntypes * P.ntypes;
     {
         ProfScope ps("dp_pad", s);
-        dp_pad<T><<<(nnet + 31) / 32, 32, 0, s>>>(params, davg, dstd, pad, P.ntypes);
+        dp_pad<T><<<(nnet + 31) / 32, 32, 0, s>>>(params, davg, dstd, pad, P.ntypes, P);
     }
 
     const long long nwarp_blocks = (total + kWarps - 1) / kWarps;
     const int gridw = (int)(nwarp_blocks < 152LL * 8 ? (nwarp_blocks < 1 ? 1 : nwarp_blocks) : 152LL * 8);
     const size_t wbytes = sizeof(T) * (size_t)nnet * EmbOff::SIZE;
-    const bool ws_ok = wbytes <= 128 * 1024;
+    const bool ws_ok = wbytes <= 128 * 1024 && P.ctab == nullptr;   // tables: no net weights
     const size_t wpart = ws_ok ? wbytes : 0;
     const size_t smem_f = wpart + sizeof(T) * kWarps * 32 * (E + 1 + 4) +
                           sizeof(int) * kWarps * P.nslots;
     const size_t smem_b = wpart + sizeof(T) * kWarps * (2 * E * 32 + NA) +
                           sizeof(int) * kWarps * P.nslots;
-    auto kf = ws_ok ? dp_embed_fwd<T, true> : dp_embed_fwd<T, false>;
-    auto kb = ws_ok ? dp_embed_bwd<T, true> : dp_embed_bwd<T, false>;
+    auto kf = P.ctab ? dp_embed_fwd<T, false, true>
+                     : (ws_ok ? dp_embed_fwd<T, true, false> : dp_embed_fwd<T, false, false>);
+    auto kb = P.ctab ? dp_embed_bwd<T, false, true>
+                     : (ws_ok ? dp_embed_bwd<T, true, false> : dp_embed_bwd<T, false, false>);
     int st = MATPL_OK;
     if (mode == MATPL_F32 || mode == MATPL_F64) {
         cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f);
@@ -819,6 +871,21 @@ extern "C" int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, 
     P.present_mask = mask;
     P.rmin = model->rmin; P.rmax = model->rmax;
     P.inv_mT = 1.0 / ((double)model->m * model->npresent);
+    P.ctab = model->ctable;
+    P.crows = model->ctab_rows;
+    P.cnc = model->ctab_order + 1;
+    P.cdx = model->ctab_dx;
+    P.cdx10 = 10.0 * model->ctab_dx;
+    P.csmin = model->ctab_smin;
+    P.csmax = model->ctab_smax;
+    P.err = model->err_dev;
+    if (model->ctable) {
+        MATPL_REQUIRE(dtype == MATPL_F32 || dtype == MATPL_F64, MATPL_ERR_UNSUPPORTED,
+                      "compressed models run the MATPL_F32 / MATPL_F64 forms");
+        MATPL_REQUIRE((model->ctab_order == 3 || model->ctab_order == 5) &&
+                          model->ctab_rows >= 1 && model->ctab_dx > 0,
+                      MATPL_ERR_INVALID, "compressed model: order 3 or 5, rows >= 1, dx > 0");
+    }
     cudaStream_t s = as_stream(stream);
     if (natoms == 0) {
         cudaMemsetAsync(Etot, 0, 8 * (size_t)batch, s);

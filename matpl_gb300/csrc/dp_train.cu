@@ -617,6 +617,8 @@ int validate(int dtype, const matpl_dp_model *model, int batch, int natoms, int 
                       MATPL_ERR_INVALID, "present[] entry outside [0, ntypes)");
     MATPL_REQUIRE(model->params && model->davg && model->dstd && ln && idr && tm && gF,
                   MATPL_ERR_INVALID, "null pointer argument");
+    MATPL_REQUIRE(model->ctable == nullptr, MATPL_ERR_UNSUPPORTED,
+                  "the training kernels take the embedding nets, not a compressed table");
     return MATPL_OK;
 }
 

@@ -126,11 +126,13 @@ class DP(torch.nn.Module):
 
     def __init__(self, cfg: DPConfig, params: Dict[str, torch.Tensor], davg, dstd,
                  precision: str = "float64", device="cuda", check_errors: bool = True,
-                 packed: Optional[torch.Tensor] = None):
+                 packed: Optional[torch.Tensor] = None, compress: Optional[Dict] = None):
         super().__init__()
         check_shape(cfg)
         if precision not in PRECISIONS:
             raise _lib.MatplError(f"unknown precision {precision!r}; one of {list(PRECISIONS)}")
+        if compress is not None and precision not in ("float64", "float32"):
+            raise _lib.MatplError("a compressed model runs the float64 / float32 forms")
         self.cfg = cfg
         self.precision = precision
         self.code, self.dtype = PRECISIONS[precision]
@@ -146,6 +148,17 @@ class DP(torch.nn.Module):
         self.register_buffer("davg4", per_type_stats(davg, cfg.ntypes).to(dev, self.dtype))
         self.register_buffer("dstd4", per_type_stats(dstd, cfg.ntypes).to(dev, self.dtype))
         self._perm_cache = {}
+        # compressed model: the tables of compress.build_table (ckpt_compress.py) in the fused
+        # kernels instead of the embedding nets
+        self.compress = compress
+        if compress is not None:
+            import numpy as _np
+            tab = torch.as_tensor(_np.asarray(compress["table"]))
+            if tab.dim() != 4 or tab.shape[0] != cfg.ntypes ** 2 or tab.shape[2] != E:
+                raise _lib.MatplError("compress table must be [ntypes^2, rows, 25, order + 1]")
+            self.register_buffer("ctable", tab.to(device=dev, dtype=self.dtype).contiguous())
+            self._ctab = (int(tab.shape[1]), int(compress["order"]), float(compress["dx"]),
+                          float(compress["sij_min"]), float(compress["sij_max"]))
 
     # dp_dp.py:145-165
     def present_types(self, atom_type) -> List[int]:
@@ -162,6 +175,9 @@ class DP(torch.nn.Module):
         m.rmin, m.rmax = float(self.cfg.Rmin), float(self.cfg.Rmax)
         m.params, m.davg, m.dstd = ptr(self.packed), ptr(self.davg4), ptr(self.dstd4)
         m.err_dev = ptr(self.err)
+        if self.compress is not None:
+            m.ctable = ptr(self.ctable)
+            m.ctab_rows, m.ctab_order, m.ctab_dx, m.ctab_smin, m.ctab_smax = self._ctab
         return m
 
     def _grouped_perm(self, tmap: torch.Tensor, present: List[int]) -> torch.Tensor:
