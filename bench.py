@@ -651,7 +651,7 @@ def run_dp_variants(args, ws, local):
     calculateCompress) and the type-embedding model, FP32, on an 8,000-atom box of the
     headline's density; E + F + V per step, CUDA events."""
     from matpl_gb300 import compress as C, ops, params as P
-    from matpl_gb300.typedp import TypeDP, init_type_params
+    from matpl_gb300.typedp import TypeDP, init_type_params, fused_model as typedp_fused
     dev = torch.device("cuda", local)
     st, cfg, prm = make_workload(VARIANT_ATOMS)
     tm = torch.tensor(st.types, dtype=torch.int32, device=dev)
@@ -694,8 +694,16 @@ def run_dp_variants(args, ws, local):
     tprm = init_type_params(cfg, 3, SEED_W)
     ms = timed(TypeDP(cfg, tprm, davg, dstd, vec, dtype=torch.float32, device=dev))
     out["type_embedding"] = {"ms_per_step": ms, "value": ws * VARIANT_ATOMS / (ms * 1e-3)}
+    # the same model folded into per-pair nets in the fused kernels (FP32 and BF16x3 tcgen05)
+    for prec in ("float32", "mixed"):
+        fm = typedp_fused(cfg, tprm, davg, dstd, vec, precision=prec, device=dev)
+        fm.check_errors = False
+        ms = timed(fm)
+        out[f"type_embedding_fused_{prec}"] = {"ms_per_step": ms,
+                                               "value": ws * VARIANT_ATOMS / (ms * 1e-3)}
     return {"metric": "DP variant E+F+virial atom-steps/s (reference structure on this "
-                      "library's operators, FP32; compressed also fused)", "unit": "atom-steps/s",
+                      "library's operators, FP32; both also in the fused kernels)",
+            "unit": "atom-steps/s",
             "config": {"workload": f"{VARIANT_ATOMS}-atom Li/Si box, m=150/type, Rc 6",
                        "cpu_baseline": "none on the GPU box (the reference's Python is not "
                                        "there); parity is pinned by the golden fixtures"},

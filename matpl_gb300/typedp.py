@@ -10,7 +10,9 @@ for training) with that embedding; parameter names follow the reference
 (``embedding_net.{E}.layers.{l}``, E = index of the embedding net after an optional type
 embedding net).
 
-The property vectors are an input: ``type_vector`` maps each model element to the list the
+``fused_model`` evaluates the same model in the fused kernels (every precision form) by
+folding v(t_j) into the first layer's bias (``dp_params``).  The property vectors are an
+input: ``type_vector`` maps each model element to the list the
 reference's ``get_normalized_data_list(atom_type, physical_property)`` gives for it (stored
 with a trained model; this package does not carry the element property table).  The
 reference's optional type-embedding net (``network_size`` non-empty) is not applied to the
@@ -53,6 +55,46 @@ def init_type_params(cfg: DPConfig, nfeat: int, seed: int, emb_index: int = 0,
                 p[pre + "resnet_dt"] = 0.1 + 0.001 * torch.randn(1, fw[l + 1], generator=g,
                                                                  dtype=torch.float64)
     return {k: v.to(dtype) for k, v in p.items()}
+
+
+def dp_params(cfg: DPConfig, params: Dict[str, torch.Tensor], type_vector: Dict[int, Sequence[float]],
+              emb_index: int = None) -> Dict[str, torch.Tensor]:
+    """The TypeDP model as per-type-pair embedding nets (DP's parameter names): the shared net
+    with input [s, v(t_j)] has the first-layer pre-activation s W0[0] + (b0 + v(t_j) W0[1:]),
+    so net (t_i, t_j) is DP's 1 -> 25 layer with weight W0[0] and bias b0 + v(t_j) W0[1:],
+    followed by the shared 25 -> 25 layers.  The fused evaluation (``dp.DP``, every precision
+    form including the tcgen05 ones) then runs TypeDP unchanged."""
+    if emb_index is None:
+        emb_index = sorted({int(k.split(".")[1]) for k in params if k.startswith("embedding_net.")})[-1]
+    pre = f"embedding_net.{emb_index}.layers."
+    W0 = params[pre + "0.weight"].detach().to(torch.float64).cpu()
+    b0 = params.get(pre + "0.bias")
+    b0 = torch.zeros(W0.shape[1], dtype=torch.float64) if b0 is None else \
+        b0.detach().to(torch.float64).cpu().reshape(-1)
+    out = {k: v for k, v in params.items() if k.startswith("fitting_net.")}
+    T = cfg.ntypes
+    for ti in range(T):
+        for tj in range(T):
+            k = ti * T + tj
+            v = torch.tensor(list(type_vector[cfg.atom_type[tj]]), dtype=torch.float64)
+            q = f"embedding_net.{k}.layers."
+            out[q + "0.weight"] = W0[0:1].clone()
+            out[q + "0.bias"] = (b0 + v @ W0[1:]).reshape(1, -1)
+            for l in (1, 2):
+                for name in ("weight", "bias", "resnet_dt"):
+                    src = params.get(pre + f"{l}.{name}")
+                    if src is not None:
+                        out[q + f"{l}.{name}"] = src.detach().to(torch.float64).cpu()
+    return out
+
+
+def fused_model(cfg: DPConfig, params: Dict[str, torch.Tensor], davg, dstd,
+                type_vector: Dict[int, Sequence[float]], precision: str = "float64",
+                device="cuda", emb_index: int = None):
+    """TypeDP in the fused evaluation (``dp.DP`` on ``dp_params``)."""
+    from .dp import DP
+    return DP(cfg, dp_params(cfg, params, type_vector, emb_index), davg, dstd,
+              precision=precision, device=device)
 
 
 class TypeDP(DPTrainModel):

@@ -38,3 +38,35 @@ def test_typedp_matches_reference(golden_case):
         ref = g["grad:" + name]
         got = model.param(name).grad.detach().cpu().numpy()
         np.testing.assert_allclose(got, ref, rtol=0, atol=1e-9 * max(1.0, np.abs(ref).max()))
+
+
+def test_typedp_fused_matches_reference(golden_case):
+    """TypeDP in the fused kernels (v(t_j) folded into the first layer's bias of per-pair
+    nets): FP64 = the reference's TypeDP (golden) to 1e-10; FP32 and the BF16x3 tcgen05 form
+    within 1e-5 eV/atom (energy) and 1e-5 of the force scale."""
+    from matpl_gb300.typedp import fused_model
+    from tests.conftest import load_golden
+    g = load_golden("typedp_hfo48")
+    c = golden_case("hfo48_f64")
+    cfg = c.cfg
+    vec = {z: list(v) for z, v in zip(cfg.atom_type, g["type_vector"])}
+    params = init_type_params(cfg, g["type_vector"].shape[1], int(g["seed_w"]))
+    ln = torch.tensor(c.list_neigh, device=DEV)
+    tm = torch.tensor(c.types, device=DEV)
+    idr = torch.tensor(c.image_dr, device=DEV)
+    fs, vs = np.abs(g["Force"]).max(), np.abs(g["Virial"]).max()
+    for prec, tol in (("float64", 1e-10), ("float32", 1e-5), ("mixed", 1e-5)):
+        m = fused_model(cfg, params, c.davg, c.dstd, vec, precision=prec, device=DEV)
+        Etot, Ei, F, _, V = m(ln, tm, cfg.atom_type, idr if prec == "float64" else idr.float(), 0)
+        E = Etot.detach().double().cpu().numpy().ravel()
+        Fn = F.detach().double().cpu().numpy().reshape(g["Force"].shape)
+        print(f"[accuracy] typedp fused {prec}: E/atom {np.abs(E - g['Etot'].ravel()).max() / 48:.2e}"
+              f" max|dF| {np.abs(Fn - g['Force']).max():.2e}")
+        if prec == "float64":
+            np.testing.assert_allclose(E, g["Etot"].ravel(), rtol=1e-11)
+        else:
+            assert np.abs(E - g["Etot"].ravel()).max() <= 1e-5 * 48
+        np.testing.assert_allclose(F.detach().double().cpu().numpy().reshape(g["Force"].shape),
+                                   g["Force"], rtol=0, atol=tol * fs)
+        np.testing.assert_allclose(V.detach().double().cpu().numpy().reshape(g["Virial"].shape),
+                                   g["Virial"], rtol=0, atol=10 * tol * vs)
