@@ -682,14 +682,14 @@ def run_dp_variants(args, ws, local):
     ms = timed(C.CompressedDP(cfg, prm, davg, dstd, comp, dtype=torch.float32, device=dev))
     out["compressed_order5"] = {"ms_per_step": ms, "value": ws * VARIANT_ATOMS / (ms * 1e-3),
                                 "table_rows": int(comp["table"].shape[1])}
-    # the same table in the fused FP32 kernels (matpl_dp_eval with ctable)
-    fused = C.fused_model(cfg, prm, davg, dstd, comp, "float32", dev)
-    fused.check_errors = False
-    ms = timed(fused)
-    out["compressed_order5_fused"] = {"ms_per_step": ms,
-                                      "value": ws * VARIANT_ATOMS / (ms * 1e-3),
-                                      "form": "fused FP32 kernels, table polynomial in place of "
-                                              "the embedding nets"}
+    # the same table in the fused kernels (matpl_dp_eval with ctable): FP32, and the mixed
+    # form (table on SIMT, fitting nets on the tensor cores)
+    for prec in ("float32", "mixed"):
+        fused = C.fused_model(cfg, prm, davg, dstd, comp, prec, dev)
+        fused.check_errors = False
+        ms = timed(fused)
+        out[f"compressed_order5_fused_{prec}"] = {"ms_per_step": ms,
+                                                  "value": ws * VARIANT_ATOMS / (ms * 1e-3)}
     vec = {3: [0.0185, 0.0216, 0.3], 14: [0.1204, 0.0985, 0.2]}
     tprm = init_type_params(cfg, 3, SEED_W)
     ms = timed(TypeDP(cfg, tprm, davg, dstd, vec, dtype=torch.float32, device=dev))

@@ -176,8 +176,9 @@ typedef struct {
      * calc_compress_polynomial, src/model/dp_dp.py:572-601); ctable == NULL (zero-initialise
      * the struct) keeps the embedding nets.  ctable: [ntypes^2 * ctab_rows, 25, ctab_order + 1]
      * in the compute dtype (coefficients highest power first); ctab_dx, ctab_smin, ctab_smax:
-     * the grid's dx, sij_min, sij_max.  MATPL_F32 / MATPL_F64 forms only; an s outside the
-     * table sets MATPL_KERR_TABLE_RANGE. */
+     * the grid's dx, sij_min, sij_max.  Every form: the table runs in the SIMT embedding
+     * kernels (FP32 data for the MATPL_MIXED* forms, whose fitting nets stay on the tensor
+     * cores); an s outside the table sets MATPL_KERR_TABLE_RANGE. */
     const void *ctable;
     int ctab_rows;
     int ctab_order;

@@ -778,7 +778,10 @@ int launch_eval(int mode, const matpl_dp_model *M, const EvalParams &P,
     auto kb = P.ctab ? dp_embed_bwd<T, false, true>
                      : (ws_ok ? dp_embed_bwd<T, true, false> : dp_embed_bwd<T, false, false>);
     int st = MATPL_OK;
-    if (mode == MATPL_F32 || mode == MATPL_F64) {
+    // compressed models take the SIMT embedding kernels in every form (the table polynomial is
+    // no GEMM); the mixed forms still run the fitting nets on the tensor cores
+    const bool simt_embed = mode == MATPL_F32 || mode == MATPL_F64 || P.ctab != nullptr;
+    if (simt_embed) {
         cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_f);
         cudaFuncSetAttribute(kb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b);
         ProfScope ps("dp_embed_fwd", s);
@@ -804,7 +807,7 @@ int launch_eval(int mode, const matpl_dp_model *M, const EvalParams &P,
                            M->err_dev, P.batch, P.natoms, P.ntypes, P.present_mask, s);
         if (st) return st;
     }
-    if (mode == MATPL_F32 || mode == MATPL_F64) {
+    if (simt_embed) {
         ProfScope ps("dp_embed_bwd", s);
         kb<<<gridw, kWarps * 32, smem_b, s>>>(list_neigh, idr, type_map, params, davg, dstd, dA,
                                               force, avir, P);
@@ -880,8 +883,6 @@ extern "C" int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, 
     P.csmax = model->ctab_smax;
     P.err = model->err_dev;
     if (model->ctable) {
-        MATPL_REQUIRE(dtype == MATPL_F32 || dtype == MATPL_F64, MATPL_ERR_UNSUPPORTED,
-                      "compressed models run the MATPL_F32 / MATPL_F64 forms");
         MATPL_REQUIRE((model->ctab_order == 3 || model->ctab_order == 5) &&
                           model->ctab_rows >= 1 && model->ctab_dx > 0,
                       MATPL_ERR_INVALID, "compressed model: order 3 or 5, rows >= 1, dx > 0");
@@ -896,7 +897,8 @@ extern "C" int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, 
     if (dtype >= MATPL_MIXED) {
         MATPL_REQUIRE(model->ntypes <= 15, MATPL_ERR_UNSUPPORTED,
                       "mixed-precision forms support up to 15 types");
-        MATPL_REQUIRE(mixed_smem(model->ntypes, nslots) <= 220 * 1024, MATPL_ERR_UNSUPPORTED,
+        MATPL_REQUIRE(model->ctable || mixed_smem(model->ntypes, nslots) <= 220 * 1024,
+                      MATPL_ERR_UNSUPPORTED,
                       "mixed-precision form: too many slots for the shared-memory pair list");
     }
     if (dtype == MATPL_F64)

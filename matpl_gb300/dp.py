@@ -131,8 +131,6 @@ class DP(torch.nn.Module):
         check_shape(cfg)
         if precision not in PRECISIONS:
             raise _lib.MatplError(f"unknown precision {precision!r}; one of {list(PRECISIONS)}")
-        if compress is not None and precision not in ("float64", "float32"):
-            raise _lib.MatplError("a compressed model runs the float64 / float32 forms")
         self.cfg = cfg
         self.precision = precision
         self.code, self.dtype = PRECISIONS[precision]

@@ -57,8 +57,9 @@ def test_compressed_close_to_exact_with_correct_widths(golden_case):
 @pytest.mark.parametrize("order", [5, 3])
 def test_fused_compressed_matches_reference(golden_case, order):
     """The table in the fused kernels (matpl_dp_eval with ctable): FP64 = the reference's
-    compressed model (golden) and the operator path (CompressedDP) to 1e-10; FP32 within 1e-5
-    of the force scale."""
+    compressed model (golden) and the operator path (CompressedDP) to 1e-10; FP32 within 1e-5 of
+    the force scale, the mixed form (fitting nets on the tensor cores) within 1e-5 eV/A and
+    1e-5 eV/atom."""
     g = load("compress_hfo48")
     c = golden_case("hfo48_f64")
     cfg = c.cfg
@@ -87,4 +88,11 @@ def test_fused_compressed_matches_reference(golden_case, order):
                                rtol=1e-5)
     np.testing.assert_allclose(F32.detach().cpu().numpy().reshape(rF.shape), g[f"o{order}_Force"],
                                rtol=0, atol=1e-5 * fs)
-    assert int(model.err.item()) == 0 and int(m32.err.item()) == 0
+    # the mixed forms: table in the SIMT embedding kernels, fitting nets on the tensor cores
+    mx = C.fused_model(cfg, c.params, c.davg, c.dstd, comp, "mixed", DEV)
+    Em, _, Fm, _, _ = mx(ln, tm, cfg.atom_type, idr.float(), 0)
+    natoms = c.list_neigh.shape[1]
+    assert abs(Em.item() - float(g[f"o{order}_Etot"].ravel()[0])) <= 1e-5 * natoms
+    np.testing.assert_allclose(Fm.detach().cpu().numpy().reshape(rF.shape), g[f"o{order}_Force"],
+                               rtol=0, atol=1e-5)         # eV/A (this cell's forces are < 0.1)
+    assert int(model.err.item()) == 0 and int(m32.err.item()) == 0 and int(mx.err.item()) == 0
