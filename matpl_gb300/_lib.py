@@ -14,6 +14,7 @@ KERR_BAD_TYPE = 2
 KERR_TIMEOUT = 3
 KERR_BAD_BOX = 4
 KERR_BAD_COUNT = 5
+KERR_TABLE_RANGE = 6
 LMP_AUTO, LMP_STAGED, LMP_DIRECT = 0, 1, 2
 
 _c = ctypes

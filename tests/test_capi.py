@@ -50,6 +50,34 @@ def test_host_side_validation_needs_no_gpu():
     assert st == 1
 
 
+def test_training_and_nep_entry_points_validate_on_the_host():
+    """The training / NEP entry points refuse bad dtypes and sizes before any CUDA call."""
+    lib = _lib.load()
+    err = ctypes.c_int(0)
+    st = lib.matpl_nep_zbl(9, 1, 10, 4, 1, None, None, None, None, 2, None, None, 2.0, None, None,
+                           None, None, ctypes.byref(err), None)
+    assert st == 2 and b"dtype" in lib.matpl_last_error()
+    st = lib.matpl_nep_zbl(0, 1, 10, 4, 1, None, None, None, None, 2, None, None, -1.0, None,
+                           None, None, None, ctypes.byref(err), None)
+    assert st == 1
+    st = lib.matpl_dp_desc_dual(0, 10, 0, None, None, None, None, None, None)
+    assert st == 1 and b"m2" in lib.matpl_last_error()
+    st = lib.matpl_dp_desc_dual_grad(1, 10, 26, None, None, None, None, None, None, None, None)
+    assert st == 1
+    st = lib.matpl_nep_cgrad(0, 2, 10, 2, 4, 8, None, None, 4, None, None, ctypes.byref(err), None)
+    assert st == 1 and b"part" in lib.matpl_last_error()
+    st = lib.matpl_nep_force_virial(0, 10, 4, 0, None, None, None, None, None, None,
+                                    ctypes.byref(err), None)
+    assert st == 1
+    m = _lib.MatplDpModel()
+    m.ntypes, m.m, m.npresent, m.present[0] = 1, 100, 1, 0
+    m.ctable, m.ctab_order, m.ctab_rows, m.ctab_dx = 1, 4, 10, 0.01      # order must be 3 or 5
+    ws = ctypes.create_string_buffer(1 << 20)
+    st = lib.matpl_dp_eval(1, ctypes.byref(m), 1, 1, 100, 0, None, None, None, None, None, None,
+                           None, ws, len(ws), None)
+    assert st == 1 and b"compressed" in lib.matpl_last_error()
+
+
 def test_workspace_queries():
     lib = _lib.load()
     assert lib.matpl_neighbor_workspace_bytes(1, 32000) > 32000 * 24
