@@ -67,8 +67,11 @@ def dist_setup():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if ws > 1:
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:                       # host-only ranks (the multi-process tests): gloo
+            dist.init_process_group("gloo")
     return ws, rank, local
 
 
@@ -79,12 +82,20 @@ def barrier(ws):
 
 
 def max_over_ranks(x, ws):
+    """The largest of every rank's x (the slowest replica sets the time of a step)."""
     if ws == 1:
         return x
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return t.item()
+
+
+def replica_value(units_per_rank, ms_max, ws):
+    """Whole-job throughput of ws replicas: the units all ranks processed / the step time of
+    the slowest rank (ms, already reduced by max_over_ranks)."""
+    return ws * units_per_rank / (ms_max * 1e-3)
 
 
 def make_workload(natoms=NATOMS, seed=SEED_STRUCT):
@@ -1097,7 +1108,7 @@ def run_ours(args, ws, rank, local):
         del l0, r0
     acc = accuracy(model, step)
     ms, prof, clocks = timed(step, args.steps, args.warmup, True)
-    value = ws * NATOMS / (ms * 1e-3)
+    value = replica_value(NATOMS, ms, ws)
     model_ms = sum(v[0] for k, v in prof.items() if not k.startswith("nb_")) / args.steps
 
     plain = None
