@@ -19,7 +19,7 @@ from typing import Dict, Optional
 import torch
 
 from . import nep_ops
-from .splitk import _AddRow, _MM
+from . import splitk
 from .nep import NepConfig
 
 
@@ -104,8 +104,8 @@ class NEPTrain(torch.nn.Module):
         # output layers as one block-diagonal [T*H, T] matrix
         W1 = torch.cat([net.layers[1].weight for net in nets], 0) * self.fit_blocks
         b1 = torch.cat([net.layers[1].bias.reshape(-1) for net in nets])          # [T]
-        h = torch.tanh(_AddRow.apply(_MM.apply(feats, W0), b0))
-        y = _AddRow.apply(_MM.apply(h, W1), b1)                                   # [N, T]
+        h = torch.tanh(splitk.add_row(splitk.mm(feats, W0), b0))
+        y = splitk.add_row(splitk.mm(h, W1), b1)                                  # [N, T]
         return (y * onehot).sum(-1)
 
     def forward(self, NN_radial, NL_radial, Ri_radial, NN_angular, NL_angular, Ri_angular,
