@@ -235,3 +235,36 @@ def test_zbl_term_in_training_forward(nep_case):
     for k, v in ref.items():
         close(grads[k], v.numpy(), 1e-10)
     nep_ops.check_errors()
+
+
+def test_graphed_step_with_zbl_equals_eager_step(nep_case):
+    """The CUDA-graph trainer with the ZBL term (FP64): two graphed steps = two eager steps."""
+    from matpl_gb300.nep_train import GraphedNepTrainer
+    c = nep_case("nep_zbl")
+    N = c.NL_r.shape[0]
+    B = len(c.g["num_atom"])
+    rng = np.random.default_rng(4)
+    b = {"NN_r": dev(c.NN_r), "NL_r": dev(c.NL_r), "Ri_r": dev(c.Ri_r), "NN_a": dev(c.NN_a),
+         "NL_a": dev(c.NL_a), "Ri_a": dev(c.Ri_a), "type_map": dev(c.g["type_map"]),
+         "num_atom": torch.tensor(c.g["num_atom"]),
+         "per_atom": dev(np.asarray(c.g["num_atom"], dtype=np.float64)),
+         "Etot": dev(rng.standard_normal(B)), "Force": dev(rng.standard_normal((N, 3))),
+         "Virial": dev(rng.standard_normal((B, 9)))}
+    m1, m2 = nep_train_model(c), nep_train_model(c)
+    o1 = torch.optim.Adam(m1.parameters(), lr=1e-3, capturable=True, fused=True)
+    o2 = torch.optim.Adam(m2.parameters(), lr=1e-3, capturable=True, fused=True)
+    t1 = GraphedNepTrainer(m1, o1, w_v=0.1, warmup=1)
+    t2 = GraphedNepTrainer(m2, o2, w_v=0.1, warmup=1)
+    try:
+        for _ in range(3):
+            o2.zero_grad(set_to_none=True)
+            t2.loss(b).backward()
+            o2.step()
+        l1 = [t1.step(b) for _ in range(2)][-1]
+        torch.cuda.synchronize()
+        t1.check_errors()
+    finally:
+        nep_ops.set_check_errors(True)
+    for (k, a), (_, bb) in zip(m1.named_parameters(), m2.named_parameters()):
+        close(a, bb.detach().cpu().numpy(), 1e-10)
+    assert torch.isfinite(l1).all()
