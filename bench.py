@@ -32,6 +32,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -46,7 +47,8 @@ SEED_STRUCT, SEED_W = 2024, 11
 METRIC = "E+F+virial atom-steps/s, mixed vs plain FP32 at force err ≤1e-4 eV/Å"
 CPU_SAMPLE = 4000
 
-# algorithmic FLOPs (no recompute): per occupied pair / per atom, see the design doc
+# algorithmic FLOPs (no recompute): per occupied pair of the embedding forward / backward and
+# per atom of the fitting part (25 -> 25 -> 25 embedding, M2 = 16, 400 -> 50 -> 50 -> 50 -> 1)
 FLOP_EMB_FWD_PAIR = 2 * (25 + 625 + 625) + 2 * 4 * 25          # 2750
 FLOP_EMB_BWD_PAIR = 2 * 2 * 100 + 2 * (625 + 625 + 25) + 42     # 2992
 FLOP_FIT_ATOM = 2 * 4 * 25 * 16 + 2 * 2 * (400 * 50 + 50 * 50 + 50 * 50 + 50) + 2 * 3200
@@ -114,7 +116,8 @@ class ClockSampler:
     def __init__(self, gpu_index):
         self.proc = None
         self.gpu = gpu_index
-        self.path = os.path.join(HERE, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        out_dir = os.environ.get("MATPL_BENCH_OUT", tempfile.gettempdir())
+        self.path = os.path.join(out_dir, f"clocks_{os.getpid()}.csv")
 
     def start(self):
         try:
@@ -716,8 +719,9 @@ def run_dp_variants(args, ws, local):
                       "library's operators, FP32; both also in the fused kernels)",
             "unit": "atom-steps/s",
             "config": {"workload": f"{VARIANT_ATOMS}-atom Li/Si box, m=150/type, Rc 6",
-                       "cpu_baseline": "none on the GPU box (the reference's Python is not "
-                                       "there); parity is pinned by the golden fixtures"},
+                       "cpu_baseline": "none: the reference path of these variants is its "
+                                       "Python model, which the bench does not run; parity "
+                                       "is pinned by the golden fixtures"},
             **out}
 
 

@@ -1,8 +1,8 @@
 """ORACLE — test infrastructure only.
 
 Nothing in the product package (``matpl_gb300``) imports this package.  Only the tests,
-``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use it, and only as the
-checker / CPU baseline, never as the thing measured on the GPU.
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use it, and only to check
+results and as the CPU baseline, never as the thing measured on the GPU.
 
 Contents
 --------

@@ -12,7 +12,7 @@ torch-FP64 (or FP32) CPU restatement of MatPL's DP se_e2_a evaluation, the path 
 Weights are passed as a mapping with the reference's own ``state_dict`` key names
 (``embedding_net.{k}.layers.{l}.weight`` ...), so a reference checkpoint or TorchScript
 ``jit_dp.pt`` state dict can be used directly.  Autograd builds the same derivative graph
-the reference builds; the checker is pinned against outputs of the reference itself
+the reference builds; the oracle is pinned against outputs of the reference itself
 (``tests/golden``).
 """
 from dataclasses import dataclass, field

@@ -1,7 +1,7 @@
 /*
  * ORACLE — test infrastructure only.  Never linked into, loaded by or called from
  * the product library; only tests/, __graft_entry__.smoke() and bench.py's CPU
- * baseline leg use it, as the checker.
+ * baseline leg use it, to check results and to time the CPU baseline.
  *
  * Plain-C restatement of MatPL's DP neighbor search
  *   src/pre_data/gen_feature/NeighConst.f90:14-149  (subroutine find_neighbore)
