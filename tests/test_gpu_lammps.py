@@ -272,3 +272,32 @@ def test_model_deviation_shares_one_conversion(access):
     with pytest.raises(_lib.MatplError, match="share ntypes"):
         pair.add_model(bad)
     pair.close()
+
+
+def test_pair_with_compressed_model_folds_to_periodic_path():
+    """A compressed model (order-5 table) in the pair style: ghost forces folded onto their
+    owners, energy and virial = the same compressed model on the periodic cell (FP64)."""
+    from matpl_gb300 import compress as C
+    st = structures.fcc(3.615, (8, 8, 8), 0.05, seed=5)
+    cfg = P.DPConfig(atom_type=[29], maxNeighborNum=100)
+    params = P.init_params(cfg, 103)
+    davg, dstd = stats(cfg, st)
+    comp = C.build_table(cfg, params, davg.numpy(), dstd.numpy(), 2.5, 0.01, 5, device=DEV)
+    model = C.fused_model(cfg, params, davg, dstd, comp, "float64", DEV)
+    s = lammps_system(st.lattice, st.cart, st.types + 1, 7.0, seed=5)
+    pair = PairMATPL(model, [29], host_access="staged")
+    r = run_pair(pair, s)
+    n = s["nlocal"]
+    lat = torch.tensor(st.lattice[None], device=DEV)
+    frac = torch.tensor(np.mod(s["x"][:n] @ np.linalg.inv(st.lattice), 1.0)[None], device=DEV)
+    ln, idr = ops.find_neighbore(torch.zeros(n, dtype=torch.int32), frac, lat, 1, 100, 6.0, 6.0)
+    out = model.evaluate(ln, torch.zeros(n, dtype=torch.int32, device=DEV), [0], idr, 0)
+    F = out["Force"][0].cpu().numpy()
+    np.testing.assert_allclose(fold_ghosts(r["f"], s["owner"], n), F, rtol=0,
+                               atol=1e-10 * np.abs(F).max())
+    np.testing.assert_allclose(r["eng"], out["Etot"].item(), rtol=1e-12)
+    V = out["Virial"][0].cpu().numpy()
+    np.testing.assert_allclose(r["virial"], V[[0, 4, 8, 3, 6, 7]], rtol=0,
+                               atol=1e-10 * np.abs(V).max())
+    assert int(model.err.item()) == 0
+    pair.close()
