@@ -312,21 +312,47 @@ class FusedTrainer:
 
     def _pad_term(self, ln, present):
         """Empty-slot term of A (before the 1/(mT) scale is applied): per atom
-        sum over present t_j of n_empty(t_j) R_pad(t_i) (x) G_{t_i t_j}(s_pad(t_i))."""
+        sum over present t_j of n_empty(t_j) R_pad(t_i) (x) G_{t_i t_j}(s_pad(t_i)).  Every
+        present pair's net is evaluated at its s_pad together (stacked weights, batched
+        products), and the per-atom weights onehot(t_i) n_empty(t_j) enter as one product over
+        the pairs (its gradient, a sum over the atoms, split like the fitting products)."""
         model, cfg = self.model, self.model.cfg
         B, N, S = ln.shape
-        m = cfg.maxNeighborNum
-        tmap = self._tm_long
-        out = torch.zeros(B, N, 4, _dp.E, dtype=model.dtype, device=ln.device)
-        occ = (ln > 0).reshape(B, N, cfg.ntypes, m).sum(-1)              # [B, N, ntypes]
-        for ti in present:
-            rp = (0.0 - self.davg4[ti]) / self.dstd4[ti]                 # [4]
-            sel = (tmap == ti).to(model.dtype).reshape(1, N, 1, 1)
-            for tj in present:
-                G = model._emb(ti * cfg.ntypes + tj, rp[0:1].reshape(1, 1))[0]   # [E]
-                nemp = (m - occ[:, :, tj]).to(model.dtype).reshape(B, N, 1, 1)
-                out = out + sel * nemp * (rp.reshape(4, 1) * G.reshape(1, _dp.E))
-        return out
+        T, m = cfg.ntypes, cfg.maxNeighborNum
+        dev, dt = ln.device, model.dtype
+        pairs = [(ti, tj) for ti in present for tj in present]
+        P = len(pairs)
+        key = (tuple(present), dev)
+        if getattr(self, "_pair_idx_key", None) != key:      # made outside graph capture
+            self._pair_idx = (torch.tensor([p[0] for p in pairs], device=dev),
+                              torch.tensor([p[1] for p in pairs], device=dev))
+            self._pair_idx_key = key
+        ti_idx, tj_idx = self._pair_idx
+        rpp = ((0.0 - self.davg4) / self.dstd4).index_select(0, ti_idx)      # [P, 4]
+
+        def stacked(l, name):
+            vals = [model.param(f"embedding_net.{ti * T + tj}.layers.{l}.{name}")
+                    for ti, tj in pairs]
+            if all(v is None for v in vals):
+                return None
+            return torch.stack([v if v is not None else
+                                (torch.ones_like(vals[0]) if name == "resnet_dt"
+                                 else torch.zeros_like(vals[0])) for v in vals])
+        # layer 0 (1 -> E): s W0 + b0; layers 1, 2 (E -> E, residual), as DPTrainModel._emb
+        x = rpp[:, 0].reshape(P, 1, 1) * stacked(0, "weight")                 # [P, 1, E]
+        b0 = stacked(0, "bias")
+        x = torch.tanh(x + b0 if b0 is not None else x)
+        for l in (1, 2):
+            h = torch.bmm(x, stacked(l, "weight"))
+            b = stacked(l, "bias")
+            h = torch.tanh(h + b if b is not None else h)
+            d = stacked(l, "resnet_dt")
+            x = (h * d if d is not None else h) + x
+        prow = (rpp.unsqueeze(-1) * x.reshape(P, 1, _dp.E)).reshape(P, 4 * _dp.E)
+        occ = (ln > 0).reshape(B, N, T, m).sum(-1).to(dt)                      # [B, N, T]
+        onehot = (self._tm_long.reshape(1, N, 1) == ti_idx.reshape(1, 1, P)).to(dt)
+        wts = onehot * (m - occ).index_select(2, tj_idx)                       # [B, N, P]
+        return splitk.mm(wts.reshape(B * N, P), prow).reshape(B, N, 4, _dp.E)
 
     def _fit_dual(self, t: int, x: torch.Tensor, xd: torch.Tensor):
         """Fitting net of element t (dp_embedding.py:140-163) on rows x and its tangent xd:
