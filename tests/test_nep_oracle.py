@@ -92,3 +92,22 @@ def test_oracle_forces_are_energy_gradient(nep_case):
         fd = -(es[0] - es[1]) / (2 * h)
         assert abs(fd - float(out["Force"][atom, comp])) < 1e-6 * max(1.0, abs(fd))
     fr.position = base
+
+
+def test_zbl_rounded_factors_close_to_reference(nep_case):
+    """The oracle's "rounded" ZBL element factors (the kernel's: correctly rounded float32
+    Z^0.23) against the reference's own values (torch's float32 pow): within 1e-7 relative."""
+    c = nep_case("nep_zbl")
+    g = c.g
+    out = NO.nep_eval(c.cfg, c.params, g["num_atom"], torch.tensor(g["type_map"]),
+                      torch.tensor(c.NL_r), torch.tensor(c.Ri_r), torch.tensor(c.NL_a),
+                      torch.tensor(c.Ri_a), zbl_factors="rounded")
+    np.testing.assert_allclose(out["Etot"].numpy().ravel(), g["Etot"].ravel(), rtol=1e-7)
+    np.testing.assert_allclose(out["Force"].numpy(), g["Force"], rtol=0,
+                               atol=1e-7 * np.abs(g["Force"]).max())
+    # the ZBL term is what moves these frames: without it the energies differ entirely
+    import dataclasses
+    off = NO.nep_eval(dataclasses.replace(c.cfg, zbl=None), c.params, g["num_atom"],
+                      torch.tensor(g["type_map"]), torch.tensor(c.NL_r), torch.tensor(c.Ri_r),
+                      torch.tensor(c.NL_a), torch.tensor(c.Ri_a))
+    assert np.abs(off["Etot"].numpy().ravel() - g["Etot"].ravel()).min() > 1.0
