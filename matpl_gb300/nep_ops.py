@@ -14,6 +14,12 @@ GPUMD's way, and both give the same forces once contracted with Ri_d.  The force
 functions reuse the DP force / virial kernels (one configuration of N atoms); the virial is
 summed per image of ``num_atom`` and its backward uses each image's own gradient (the
 reference's CUDA backward applies the first image's to all atoms).
+
+For ``nep_train.NEPTrain`` the module also has the training step's own forms: ``nep_feat_d12``
+(the descriptor's d12 gradient alone, the force path), the c-gradient reduction
+``matpl_nep_cgrad`` behind every backward, ``nep_force_virial`` (forces and per-image virial
+from dE and the (r, x, y, z) rows, calculate_Ri formed in the kernel) and ``nep_zbl`` (the ZBL
+term, nep_net.py:916-991).
 """
 from typing import List
 
