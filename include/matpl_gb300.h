@@ -379,8 +379,10 @@ int matpl_nep_feat_op(int dtype, int part, int mode, int natoms, int max_nn, int
  *   reference's backward (src/op/src/CalcOps.cpp:534-538, 802-812) and the c-terms of its second
  *   backward (:618, :956).  part 0 (radial): W [natoms, ntypes, n_base],
  *   dc[t_i, tt, n, k] += G[i*ldG + n] * W[i, tt, k]; part 1 (angular): W [natoms, ntypes, n_max,
- *   n_base] already contracted with G, dc[t_i] += W[i] (G unused).  Column sums in the atoms'
- *   list order per chunk of 256 atoms, FP atomics across chunks.  err_dev gets
+ *   n_base] already contracted with G, dc[t_i] += W[i] (G unused).  Each block of 64
+ *   consecutive atoms sums its atoms of one centre type in shared memory (8 warps' partial
+ *   sums), then adds each column to dc with one FP atomic per block, so the order of the
+ *   atomics across blocks (and the last bits of dc) may differ between runs.  err_dev gets
  *   MATPL_KERR_BAD_TYPE for a type outside [0, ntypes).
  */
 int matpl_nep_cgrad(int dtype, int part, int natoms, int ntypes, int n_max, int n_base,
@@ -394,8 +396,9 @@ int matpl_nep_cgrad(int dtype, int part, int natoms, int ntypes, int n_max, int 
  *   screening), fc = 1 below zbl/2 and 0.5 + 0.5 cos(pi (r - zbl/2) / (zbl/2)) above,
  *   e = c_ij phi fc / r; Ei[i] += e/2, Etot[image_of[i]] += e/2 (Etot may be NULL), and with
  *   f = (1/2) de/dr (x, y, z)/r: force[i] += f, force[j] -= f, virial[image_of[i]] -= f (x) r.
- *   pair_s, pair_c [ntypes, ntypes] f64 = Z_i^0.23 + Z_j^0.23 and 14.399645 Z_i Z_j as the
- *   reference forms them (torch's default dtype on int64 element numbers).  Ei and force in
+ *   pair_s, pair_c [ntypes, ntypes] f64 = Z_i^0.23 + Z_j^0.23 and 14.399645 Z_i Z_j, float32
+ *   values widened to f64 as the reference forms them under torch's default float32 dtype
+ *   (the Python layer passes correctly rounded float32 powers).  Ei and force in
  *   dtype, Etot [nimages] and virial [nimages, 9] f64.  err_dev gets MATPL_KERR_BAD_TYPE /
  *   MATPL_KERR_BAD_COUNT.
  */
