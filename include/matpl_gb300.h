@@ -72,6 +72,8 @@ int matpl_profile_collect(int max_names, char *names, int name_len, double *tota
  *   Ri_d       [B,N,4S,3]  dRi/dr_i
  *   Rij        [B,N,S,3]   pair vectors (ImageDR[...,1:])
  * Batch stride of force / atom_virial is N+nghost (the shape of the returned tensor).
+ * A pointer that a call with these sizes reads or writes is never NULL (MATPL_ERR_INVALID,
+ * checked on the host); a call whose outputs are all empty returns MATPL_OK without a CUDA call.
  * ---------------------------------------------------------------------------------- */
 int matpl_calc_force(int dtype, const int32_t *list_neigh, const void *dE, const void *Ri_d,
                      const void *F_center, int batch, int natoms, int nslots, int nghost,
@@ -97,6 +99,7 @@ int matpl_calc_virial_grad(int dtype, const int32_t *list_neigh, const void *Rij
  *   f2 [nsij] (the [nsij,1] tensor), coefficient [nsij, layer_node, coe_num] highest power first,
  *   coe_num 4 (order 3) or 6 (order 5) -> G [nsij, layer_node].
  * The backward returns grad_f2 [nsij] = sum_i grad_G[s][i] dG[s][i]/df2 directly.
+ * NULL for a pointer that the sizes make read or written: MATPL_ERR_INVALID.
  * ---------------------------------------------------------------------------------- */
 int matpl_calc_compress(int dtype, const void *f2, const void *coefficient, long long nsij,
                         int layer_node, int coe_num, void *G, void *stream);

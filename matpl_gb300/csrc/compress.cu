@@ -121,6 +121,8 @@ extern "C" int matpl_calc_compress(int dtype, const void *f2, const void *coeffi
     int st = check_args(dtype, nsij, layer_node, coe_num);
     if (st) return st;
     if (nsij == 0 || layer_node == 0) return MATPL_OK;
+    MATPL_REQUIRE(f2 && coefficient && G, MATPL_ERR_INVALID,
+                  "matpl_calc_compress: null pointer argument");
     return dtype == MATPL_F64
                ? launch<double>(false, f2, coefficient, nullptr, nsij, layer_node, coe_num, G,
                                 as_stream(stream))
@@ -134,6 +136,8 @@ extern "C" int matpl_calc_compress_grad(int dtype, const void *f2, const void *c
     int st = check_args(dtype, nsij, layer_node, coe_num);
     if (st) return st;
     if (nsij == 0) return MATPL_OK;
+    MATPL_REQUIRE(f2 && grad_f2 && (layer_node == 0 || (coefficient && grad_G)), MATPL_ERR_INVALID,
+                  "matpl_calc_compress_grad: null pointer argument");
     return dtype == MATPL_F64
                ? launch<double>(true, f2, coefficient, grad_G, nsij, layer_node, coe_num, grad_f2,
                                 as_stream(stream))

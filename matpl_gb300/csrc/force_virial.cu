@@ -185,6 +185,9 @@ extern "C" int matpl_calc_force(int dtype, const int32_t *list_neigh, const void
     cudaStream_t s = as_stream(stream);
     const long long nout = (long long)batch * (natoms + nghost) * 3;
     const long long nsl = (long long)batch * natoms * nslots;
+    MATPL_REQUIRE((nout == 0 || force_out) && ((long long)batch * natoms == 0 || F_center) &&
+                      (nsl == 0 || (list_neigh && dE && Ri_d)),
+                  MATPL_ERR_INVALID, "matpl_calc_force: null pointer argument");
     if (nout == 0) return MATPL_OK;
     if (dtype == MATPL_F64) {
         copy_center_force<double><<<grid_for(nout), kThreads, 0, s>>>(
@@ -210,6 +213,10 @@ extern "C" int matpl_calc_virial(int dtype, const int32_t *list_neigh, const voi
                                  void *stream) {
     int st = check_common(dtype, batch, natoms, nslots, nghost);
     if (st) return st;
+    MATPL_REQUIRE((batch == 0 || (virial_out && (natoms + nghost == 0 || atom_virial_out))) &&
+                      ((long long)batch * natoms * nslots == 0 || (list_neigh && dE && Rij && Ri_d)),
+                  MATPL_ERR_INVALID, "matpl_calc_virial: null pointer argument");
+    if (batch == 0) return MATPL_OK;
     cudaStream_t s = as_stream(stream);
     const size_t es = dtype == MATPL_F64 ? 8 : 4;
     if (cudaMemsetAsync(virial_out, 0, es * 9 * (size_t)batch, s) != cudaSuccess ||
@@ -238,6 +245,8 @@ extern "C" int matpl_calc_force_grad(int dtype, const int32_t *list_neigh, const
     if (st) return st;
     const long long nsl = (long long)batch * natoms * nslots;
     if (nsl == 0) return MATPL_OK;
+    MATPL_REQUIRE(list_neigh && Ri_d && grad_force && grad_dE, MATPL_ERR_INVALID,
+                  "matpl_calc_force_grad: null pointer argument");
     cudaStream_t s = as_stream(stream);
     if (dtype == MATPL_F64)
         force_grad_kernel<double><<<grid_for(nsl), kThreads, 0, s>>>(
@@ -257,6 +266,8 @@ extern "C" int matpl_calc_virial_grad(int dtype, const int32_t *list_neigh, cons
     if (st) return st;
     const long long nsl = (long long)batch * natoms * nslots;
     if (nsl == 0) return MATPL_OK;
+    MATPL_REQUIRE(list_neigh && Rij && Ri_d && grad_virial && grad_dE, MATPL_ERR_INVALID,
+                  "matpl_calc_virial_grad: null pointer argument");
     cudaStream_t s = as_stream(stream);
     if (dtype == MATPL_F64)
         virial_grad_kernel<double><<<grid_for(nsl), kThreads, 0, s>>>(

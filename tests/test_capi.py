@@ -78,6 +78,38 @@ def test_training_and_nep_entry_points_validate_on_the_host():
     assert st == 1 and b"compressed" in lib.matpl_last_error()
 
 
+def test_empty_sizes_and_null_pointers_are_handled_on_the_host():
+    """Empty inputs return MATPL_OK before any CUDA call; a NULL pointer that the sizes would
+    make a kernel read or write is refused (MATPL_ERR_INVALID) instead of reaching the GPU."""
+    lib = _lib.load()
+    err = ctypes.c_int(0)
+    OK, INVALID = 0, 1
+    assert lib.matpl_calc_force(0, None, None, None, None, 2, 0, 5, 0, None, None) == OK
+    assert lib.matpl_calc_force(0, None, None, None, None, 1, 3, 5, 0, None, None) == INVALID
+    assert b"null" in lib.matpl_last_error()
+    assert lib.matpl_calc_virial(1, None, None, None, None, 0, 3, 5, 0, None, None, None) == OK
+    assert lib.matpl_calc_virial(1, None, None, None, None, 1, 3, 5, 0, None, None,
+                                 None) == INVALID
+    assert lib.matpl_calc_force_grad(0, None, None, None, 1, 0, 5, 0, None, None) == OK
+    assert lib.matpl_calc_force_grad(0, None, None, None, 1, 3, 5, 0, None, None) == INVALID
+    assert lib.matpl_calc_virial_grad(0, None, None, None, None, 1, 3, 0, None, None) == OK
+    assert lib.matpl_calc_virial_grad(0, None, None, None, None, 1, 3, 5, None, None) == INVALID
+    assert lib.matpl_calc_compress(1, None, None, 0, 25, 6, None, None) == OK
+    assert lib.matpl_calc_compress(1, None, None, 10, 25, 6, None, None) == INVALID
+    assert lib.matpl_calc_compress_grad(1, None, None, None, 0, 25, 4, None, None) == OK
+    assert lib.matpl_calc_compress_grad(1, None, None, None, 10, 25, 4, None, None) == INVALID
+    assert lib.matpl_dp_desc_dual(0, 0, 16, None, None, None, None, None, None) == OK
+    assert lib.matpl_dp_desc_dual_grad(1, 0, 16, None, None, None, None, None, None, None,
+                                       None) == OK
+    assert lib.matpl_nep_zbl(1, 1, 0, 4, 1, None, None, None, None, 2, None, None, 2.0, None, None,
+                             None, None, ctypes.byref(err), None) == OK
+    assert lib.matpl_nep_zbl(1, 1, 5, 4, 1, None, None, None, None, 2, None, None, 2.0, None, None,
+                             None, None, ctypes.byref(err), None) == INVALID
+    assert lib.matpl_nep_force_virial_grad(0, 0, 4, 1, None, None, None, None, None, None,
+                                           ctypes.byref(err), None) == OK
+    assert err.value == 0
+
+
 def test_workspace_queries():
     lib = _lib.load()
     assert lib.matpl_neighbor_workspace_bytes(1, 32000) > 32000 * 24
