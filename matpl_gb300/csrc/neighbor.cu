@@ -669,6 +669,8 @@ extern "C" int matpl_env_mat(int dtype, int batch, int natoms, int nslots,
     MATPL_REQUIRE(batch >= 0 && natoms >= 0 && nslots >= 0, MATPL_ERR_INVALID, "negative size");
     const long long total = (long long)batch * natoms * nslots;
     if (total == 0) return MATPL_OK;
+    MATPL_REQUIRE(type_map && image_dr && davg && dstd && Ri && Ri_d, MATPL_ERR_INVALID,
+                  "matpl_env_mat: null pointer argument");
     cudaStream_t s = as_stream(stream);
     if (dtype == MATPL_F64)
         env_mat_kernel<double><<<grid_for(total, 256), 256, 0, s>>>(

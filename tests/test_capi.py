@@ -94,6 +94,10 @@ def test_empty_sizes_and_null_pointers_are_handled_on_the_host():
     assert lib.matpl_calc_force_grad(0, None, None, None, 1, 3, 5, 0, None, None) == INVALID
     assert lib.matpl_calc_virial_grad(0, None, None, None, None, 1, 3, 0, None, None) == OK
     assert lib.matpl_calc_virial_grad(0, None, None, None, None, 1, 3, 5, None, None) == INVALID
+    assert lib.matpl_env_mat(1, 1, 0, 200, None, None, None, None, 0.5, 6.0, None, None,
+                             None) == OK
+    assert lib.matpl_env_mat(1, 1, 4, 200, None, None, None, None, 0.5, 6.0, None, None,
+                             None) == INVALID
     assert lib.matpl_calc_compress(1, None, None, 0, 25, 6, None, None) == OK
     assert lib.matpl_calc_compress(1, None, None, 10, 25, 6, None, None) == INVALID
     assert lib.matpl_calc_compress_grad(1, None, None, None, 0, 25, 4, None, None) == OK
