@@ -62,6 +62,8 @@ extern "C" int matpl_profile_begin(int max_launches) {
 extern "C" int matpl_profile_collect(int max_names, char *names, int name_len, double *total_ms,
                                      int *launches, int *n_out) {
     std::lock_guard<std::mutex> lk(g_prof_mu);
+    MATPL_REQUIRE(n_out && (max_names <= 0 || (names && name_len > 0 && total_ms && launches)),
+                  MATPL_ERR_INVALID, "matpl_profile_collect: null output array or name_len <= 0");
     g_prof_on = false;
     std::map<std::string, std::pair<double, int>> agg;
     for (auto &r : g_recs) {

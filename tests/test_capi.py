@@ -112,6 +112,11 @@ def test_empty_sizes_and_null_pointers_are_handled_on_the_host():
     assert lib.matpl_nep_force_virial_grad(0, 0, 4, 1, None, None, None, None, None, None,
                                            ctypes.byref(err), None) == OK
     assert err.value == 0
+    n = ctypes.c_int(-1)
+    assert lib.matpl_profile_collect(4, None, 64, None, None, None) == INVALID
+    assert lib.matpl_profile_collect(4, None, 64, None, None, ctypes.byref(n)) == INVALID
+    assert lib.matpl_profile_collect(0, None, 0, None, None, ctypes.byref(n)) == OK
+    assert n.value == 0
 
 
 def test_workspace_queries():
