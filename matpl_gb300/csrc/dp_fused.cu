@@ -887,6 +887,10 @@ extern "C" int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, 
                           model->ctab_rows >= 1 && model->ctab_dx > 0,
                       MATPL_ERR_INVALID, "compressed model: order 3 or 5, rows >= 1, dx > 0");
     }
+    MATPL_REQUIRE(Etot && virial && (nghost == 0 || force) &&
+                      (natoms == 0 || (model->params && model->davg && model->dstd && list_neigh &&
+                                       image_dr && type_map && Ei && force)),
+                  MATPL_ERR_INVALID, "matpl_dp_eval: null pointer argument");
     cudaStream_t s = as_stream(stream);
     if (natoms == 0) {
         cudaMemsetAsync(Etot, 0, 8 * (size_t)batch, s);

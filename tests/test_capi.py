@@ -112,6 +112,14 @@ def test_empty_sizes_and_null_pointers_are_handled_on_the_host():
     assert lib.matpl_nep_force_virial_grad(0, 0, 4, 1, None, None, None, None, None, None,
                                            ctypes.byref(err), None) == OK
     assert err.value == 0
+    m = _lib.MatplDpModel()
+    m.ntypes, m.m, m.npresent, m.present[0] = 1, 100, 1, 0
+    ws = ctypes.create_string_buffer(1 << 20)
+    assert lib.matpl_dp_eval(1, ctypes.byref(m), 0, 4, 100, 0, None, None, None, None, None, None,
+                             None, ws, len(ws), None) == OK
+    assert lib.matpl_dp_eval(1, ctypes.byref(m), 1, 4, 100, 0, None, None, None, None, None, None,
+                             None, ws, len(ws), None) == INVALID
+    assert b"null" in lib.matpl_last_error()
     n = ctypes.c_int(-1)
     assert lib.matpl_profile_collect(4, None, 64, None, None, None) == INVALID
     assert lib.matpl_profile_collect(4, None, 64, None, None, ctypes.byref(n)) == INVALID
