@@ -1007,8 +1007,9 @@ def run_lammps_line(args, ws, rank, local):
 def run_reference(args, ws, rank):
     if rank != 0:
         return
-    steps = max(3, min(args.steps, 10))
-    warm = 1
+    # the requested K and W, bounded so that the host run stays within a few minutes
+    steps = max(3, min(args.steps, 50))
+    warm = max(3, min(args.warmup, 10))
     if args.workload == "nep":
         cb = cpu_baseline_nep(steps, warm)
         line = {"metric": NEP_METRIC, "value": cb["value"], "unit": "atom-steps/s",
@@ -1033,7 +1034,7 @@ def run_reference(args, ws, rank):
             "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "nep": None if args.no_nep else cpu_baseline_nep(3, 1)}
+            "nep": None if args.no_nep else cpu_baseline_nep(3, 3)}
     print(json.dumps(line))
 
 
