@@ -2,6 +2,7 @@
 without a GPU, the barrier, the max-over-ranks step time and the whole-job value built from it,
 and the reference arm's rank > 0 exit without work.  The path shards into independent replicas
 (no collective on the data path), so these helpers are all of it."""
+import json
 import os
 import socket
 import subprocess
@@ -60,3 +61,28 @@ def test_reference_arm_rank_above_zero_exits_without_work():
                        timeout=300)
     assert r.returncode == 0
     assert r.stdout.strip() == ""
+
+
+def test_reference_arm_line_keeps_the_bench_contract():
+    """Rank 0 of the reference arm prints one JSON line with the contract's keys, the requested
+    step counts (warm-up at least 3), a host e2e object with no copies and a cpu_baseline that
+    describes the same run."""
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--workload", "nep",
+                        "--steps", "3", "--warmup", "3"], cwd=REPO, env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
+              "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
+              "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["steps"] == 3 and d["warmup"] >= 3
+    assert d["value"] > 0 and d["higher_is_better"] is True
+    assert d["e2e"]["value"] == d["value"] and d["e2e"]["unit"] == d["unit"]
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1
+    assert "workload" in d["config"]
