@@ -1,8 +1,11 @@
 """CPU-side checks of the C ABI: the library builds for sm_103a, loads, and exports every
-function that include/matpl_gb300.h declares; host-side packing logic."""
+function that include/matpl_gb300.h declares; host-side argument checks; the ctypes mirrors
+agree with the header's struct layouts and codes; host-side packing logic."""
 import ctypes
 import os
 import re
+import shutil
+import subprocess
 
 import numpy as np
 import pytest
@@ -159,3 +162,40 @@ def test_per_type_stats_rejects_untiled():
     a[0, 4] = 1.0
     with pytest.raises(_lib.MatplError):
         dp.per_type_stats(a, 1)
+
+
+def _c_layout(tmp_path, struct, fields):
+    """sizeof and offsetof of a header struct as the C compiler lays it out."""
+    src = tmp_path / f"{struct}.c"
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "matpl_gb300.h"',
+             'int main(void) {', f'    printf("%zu\\n", sizeof({struct}));']
+    lines += [f'    printf("%zu\\n", offsetof({struct}, {f}));' for f in fields]
+    lines += ['    return 0;', '}']
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / struct
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(REPO, "include"), str(src), "-o",
+                    str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    return int(out[0]), [int(v) for v in out[1:]]
+
+
+@pytest.mark.parametrize("struct,mirror", [("matpl_dp_model", _lib.MatplDpModel),
+                                           ("matpl_nep_model", _lib.MatplNepModel)])
+def test_ctypes_structs_match_the_header_layout(tmp_path, struct, mirror):
+    """The ctypes mirrors have the C compiler's size and field offsets (an offset that drifts
+    would hand the kernels a wrong device pointer)."""
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    names = [f[0] for f in mirror._fields_]
+    size, offs = _c_layout(tmp_path, struct, names)
+    assert ctypes.sizeof(mirror) == size
+    for n, off in zip(names, offs):
+        assert getattr(mirror, n).offset == off, n
+
+
+def test_error_codes_and_dtype_codes_match_the_header():
+    txt = open(os.path.join(REPO, "include", "matpl_gb300.h")).read()
+    kerr = dict(re.findall(r"#define MATPL_KERR_([A-Z_]+) (\d+)", txt))
+    assert kerr and all(getattr(_lib, "KERR_" + k) == int(v) for k, v in kerr.items())
+    dt = dict(re.findall(r"\bMATPL_(F32|F64|MIXED|MIXED_FAST|MIXED_TANHF) = (\d+)", txt))
+    assert dt == {"F32": "0", "F64": "1", "MIXED": "2", "MIXED_FAST": "3", "MIXED_TANHF": "4"}
