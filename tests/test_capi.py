@@ -199,3 +199,45 @@ def test_error_codes_and_dtype_codes_match_the_header():
     assert kerr and all(getattr(_lib, "KERR_" + k) == int(v) for k, v in kerr.items())
     dt = dict(re.findall(r"\bMATPL_(F32|F64|MIXED|MIXED_FAST|MIXED_TANHF) = (\d+)", txt))
     assert dt == {"F32": "0", "F64": "1", "MIXED": "2", "MIXED_FAST": "3", "MIXED_TANHF": "4"}
+
+
+def _header_prototypes():
+    txt = open(os.path.join(REPO, "include", "matpl_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    protos = {}
+    for ret, name, params in re.findall(r"([A-Za-z_][\w \*]*?)\b(matpl_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;",
+                                        txt):
+        ps = [p.strip() for p in params.split(",") if p.strip()]
+        protos[name] = [] if ps == ["void"] else ps
+    return protos
+
+
+def _c_class(decl):
+    if "*" in decl:
+        return "ptr"
+    if "double" in decl:
+        return "f64"
+    if "long long" in decl:
+        return "i64"
+    if "size_t" in decl:
+        return "size"
+    return "i32"
+
+
+def _ctypes_class(t):
+    if t in (ctypes.c_void_p, ctypes.c_char_p) or hasattr(t, "contents"):
+        return "ptr"
+    return {ctypes.c_double: "f64", ctypes.c_longlong: "i64", ctypes.c_size_t: "size",
+            ctypes.c_int: "i32"}.get(t, repr(t))
+
+
+def test_ctypes_signatures_match_the_header_prototypes():
+    """Every ctypes signature has the header's parameter count and, per parameter, the same
+    class (pointer, int, long long, size_t, double)."""
+    protos = _header_prototypes()
+    assert set(protos) == set(header_functions())
+    for name, params in protos.items():
+        _, argtypes = _lib.SIGNATURES[name]
+        assert len(argtypes) == len(params), name
+        for i, (p, t) in enumerate(zip(params, argtypes)):
+            assert _c_class(p) == _ctypes_class(t), f"{name} parameter {i}: {p!r} vs {t!r}"
