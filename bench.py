@@ -100,6 +100,11 @@ def replica_value(units_per_rank, ms_max, ws):
     return ws * units_per_rank / (ms_max * 1e-3)
 
 
+def sm_count() -> int:
+    """Streaming multiprocessors of the current GPU (the SIMT peak is quoted per SM)."""
+    return torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+
+
 def make_workload(natoms=NATOMS, seed=SEED_STRUCT):
     from matpl_gb300 import params as P, structures
     st = structures.random_packed(natoms, DENSITY, ELEMENTS, [0.5, 0.5], seed=seed)
@@ -332,7 +337,7 @@ def run_nep(args, ws, local, steps, warmup, sample_clocks=True):
     for k, v in prof.items():
         per_kernel[k]["share"] = v[0] / tot if tot else None
     sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
-    simt_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    simt_peak = sm_count() * 128 * 2 * sm_mhz * 1e6 / 1e12
     fl = nep_flops(cfg, n_r, n_a, N)
     t_eval = per_kernel["nep_eval"]["ms_per_launch"] * 1e-3
     # neighbor operator: reads positions (24 B / atom), writes NN (16 B / atom) and the padded
@@ -372,7 +377,7 @@ def run_nep(args, ws, local, steps, warmup, sample_clocks=True):
                      "algorithmic_flops_per_launch": fl,
                      "traffic": traffic["bytes_per_launch"] if traffic else None,
                      "traffic_note": traffic["note"] if traffic else None,
-                     "peak_source": "nominal FP32 SIMT at the sampled SM clock (152 SMs x 128 lanes x 2)",
+                     "peak_source": f"nominal FP32 SIMT at the sampled SM clock ({sm_count()} SMs x 128 lanes x 2)",
                      "hbm": {"achieved": ev_bytes / t_eval / 1e9, "peak": hbm_peak,
                              "unit": "GB/s", "frac": ev_bytes / t_eval / 1e9 / hbm_peak,
                              "algorithmic_bytes_per_launch": ev_bytes}},
@@ -1127,6 +1132,18 @@ def run_ours(args, ws, rank, local):
                  "ms_per_step": pms, "model_only_ms_per_step": pmodel_ms,
                  "model_only_value": ws * NATOMS / (pmodel_ms * 1e-3), **pacc}
         del pmodel
+    plain64 = None
+    if prec != "float64" and not args.no_plain:
+        # the FP64 form: the arithmetic of the CPU arm, so the two compare like for like
+        dmodel, dstep = make_step("float64")
+        dsteps = 5
+        dms, dprof, _ = timed(dstep, dsteps, 3, False)
+        dmodel_ms = sum(v[0] for k, v in dprof.items() if not k.startswith("nb_")) / dsteps
+        plain64 = {"form": "float64 (plain SIMT, the precision of the CPU baseline)",
+                   "value": ws * NATOMS / (dms * 1e-3), "ms_per_step": dms,
+                   "model_only_ms_per_step": dmodel_ms,
+                   "model_only_value": ws * NATOMS / (dmodel_ms * 1e-3)}
+        del dmodel
 
     # ---- end to end through host buffers
     out_dt = model.dtype
@@ -1194,7 +1211,7 @@ def run_ours(args, ws, rank, local):
         else:
             ach = flops[dom] / t_launch / 1e12
             sm_mhz = (clocks or {}).get("sm_mhz") or 2070.0
-            simt_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+            simt_peak = sm_count() * 128 * 2 * sm_mhz * 1e6 / 1e12
             roof = {"kernel": dom, "bound": "tensor", "achieved": ach, "peak": bf16_peak,
                     "unit": "TFLOP/s", "frac": ach / bf16_peak, "traffic": None,
                     "algorithmic_flops_per_launch": flops[dom], "peak_source": src + " bf16 burst",
@@ -1249,6 +1266,10 @@ def run_ours(args, ws, rank, local):
               "tile_tuning": tuning,
               "model_only_ms_per_step": model_ms,
               "model_only_value": ws * NATOMS / (model_ms * 1e-3), **acc}
+    if plain64:
+        config["plain_fp64"] = plain64
+        if cb and cb.get("value"):
+            config["plain_fp64"]["ratio_vs_cpu_baseline"] = plain64["value"] / cb["value"]
     if plain:
         config["plain_fp32"] = plain
         config["speedup_vs_plain_fp32"] = plain["ms_per_step"] / ms

@@ -120,6 +120,9 @@ int matpl_calc_compress_grad(int dtype, const void *f2, const void *coefficient,
  *   image_dr   [B,N,ntypes*m,4] (r, dx, dy, dz), f64 or f32 per out_dtype
  *   num_neigh  [B,N,ntypes] int32 or NULL
  * Index sets and f64 dR are bit-identical to the restatement of the Fortran source.
+ * err_dev: MATPL_KERR_NEIGHBOR_OVERFLOW (a type block needs more than m slots),
+ * MATPL_KERR_BAD_TYPE, MATPL_KERR_BAD_BOX (a cell so small that natoms x periodic images
+ * exceeds 2^31; its lists are left empty).  The arrays must live on the current device.
  * ---------------------------------------------------------------------------------- */
 size_t matpl_neighbor_workspace_bytes(int batch, int natoms);
 int matpl_neighbor_build(int batch, int natoms, int ntypes, int m_neigh, double Rc_M,
@@ -137,8 +140,11 @@ int matpl_neighbor_build(int batch, int natoms, int ntypes, int m_neigh, double 
  * MATPL_ERR_WORKSPACE without launching.  The first call on a device looks up that array's
  * device address (set-up), so make the first call before any stream capture.  All calls share
  * the array and it keeps the previous call's contents (the call clears what must start at
- * zero itself); calls that overlap on the GPU race on it, so serialise them.  Allocates no
- * memory.  Arguments and outputs as matpl_neighbor_build. */
+ * zero itself); calls that overlap on the GPU race on it, so serialise them.  The address
+ * looked up at set-up is kept per device ordinal for the life of the process: do not call
+ * cudaDeviceReset, and do not switch the device to a context other than its primary one,
+ * while this entry point is in use.  Allocates no memory.  Arguments and outputs as
+ * matpl_neighbor_build. */
 int matpl_neighbor_build_noalloc(int batch, int natoms, int ntypes, int m_neigh, double Rc_M,
                                  const double *Rc_type, const int32_t *type_map,
                                  const double *lattice, const double *frac_pos, int out_dtype,
@@ -270,7 +276,8 @@ int matpl_dp_desc_dual_grad(int dtype, long long natoms, int m2, const long long
  * matpl_nep_maxneigh writes only the counts: NN_* [N], or [N, ntypes] per neighbor element
  * when with_type (type_map [N] int64 element index).
  * ---------------------------------------------------------------------------------- */
-#define MATPL_KERR_BAD_BOX 4             /* num_cell entry < 1 */
+#define MATPL_KERR_BAD_BOX 4             /* num_cell entry < 1; DP search: natoms x periodic
+                                            images of one cell above 2^31 (lists left empty) */
 #define MATPL_KERR_BAD_COUNT 5           /* num_atom does not sum to natoms, or a list index
                                             outside [0, natoms) */
 size_t matpl_nep_neighbor_workspace_bytes(int nframes, long long natoms);

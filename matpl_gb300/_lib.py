@@ -4,7 +4,10 @@ The library is built in-tree by ``matpl_gb300.build``.  There is no fallback: wh
 is missing or a call fails, a ``MatplError`` is raised.
 """
 import ctypes
+import functools
 import os
+
+import torch
 
 from . import build as _build
 
@@ -161,3 +164,34 @@ def profile_collect():
 def ptr(t) -> int:
     """Device pointer of a torch tensor (None -> NULL)."""
     return 0 if t is None else t.data_ptr()
+
+
+def _cuda_devices(objs, found):
+    for o in objs:
+        if isinstance(o, torch.Tensor):
+            if o.is_cuda:
+                found.add(o.device.index)
+        elif isinstance(o, (list, tuple)):
+            _cuda_devices(o, found)
+
+
+def on_device(fn):
+    """Run ``fn`` with the device of its CUDA tensor arguments current.
+
+    The C library launches on the current device (and torch's current stream of the tensors'
+    device is passed to it), so every wrapper that calls into it goes through this: tensors
+    spread over several GPUs are refused, and the GPU that holds them is made current for the
+    duration of the call (a no-op when it already is)."""
+    @functools.wraps(fn)
+    def wrapper(*args, **kwargs):
+        found = set()
+        _cuda_devices(args, found)
+        _cuda_devices(kwargs.values(), found)
+        if not found:
+            return fn(*args, **kwargs)
+        if len(found) > 1:
+            raise MatplError(f"{fn.__qualname__}: CUDA tensors on several devices "
+                             f"{sorted(found)}; put every argument on one GPU")
+        with torch.cuda.device(found.pop()):
+            return fn(*args, **kwargs)
+    return wrapper

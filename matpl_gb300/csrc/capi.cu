@@ -1,4 +1,5 @@
 // Library-wide C ABI pieces: error reporting, version, per-kernel timing.
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <string>
@@ -20,6 +21,45 @@ std::vector<Rec> g_recs;
 }  // namespace
 
 void set_error(const std::string &msg) { g_last_error = msg; }
+
+int device_sms() {
+    static std::atomic<int> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        dev = 0;
+    }
+    int n = cache[dev].load(std::memory_order_relaxed);
+    if (n > 0) return n;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        return 148;                    // a Blackwell-class part; only sizes grids
+    }
+    cache[dev].store(n, std::memory_order_relaxed);
+    return n;
+}
+
+int require_current_device(const void *p, const char *what) {
+    if (p == nullptr) return MATPL_OK;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();            // not a pointer the runtime knows: nothing to compare
+        return MATPL_OK;
+    }
+    if (a.type != cudaMemoryTypeDevice) return MATPL_OK;
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess) {
+        set_error(std::string(what) + ": no current CUDA device");
+        return MATPL_ERR_CUDA;
+    }
+    if (a.device != cur) {
+        set_error(std::string(what) + ": arrays live on GPU " + std::to_string(a.device) +
+                  " but GPU " + std::to_string(cur) +
+                  " is current; make the arrays' device current before the call");
+        return MATPL_ERR_INVALID;
+    }
+    return MATPL_OK;
+}
 
 bool profiling_enabled() { return g_prof_on; }
 

@@ -32,6 +32,19 @@ inline int check_launch(const char *what) {
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// The kernels of an entry point launch on the current device.  A device pointer that lives on
+// another GPU would be read through peer mappings at best (an illegal address without peer
+// access), so every entry point checks one of its device arrays here: MATPL_ERR_INVALID when
+// it belongs to a device other than the current one.  Host, managed and unregistered memory
+// pass (the LAMMPS path reads host arrays in place where the GPU can).
+int require_current_device(const void *p, const char *what);
+
+#define MATPL_REQUIRE_ON_DEVICE(p, what)                                        \
+    do {                                                                        \
+        const int matpl_dev_rc_ = ::matpl::require_current_device((p), (what)); \
+        if (matpl_dev_rc_ != MATPL_OK) return matpl_dev_rc_;                    \
+    } while (0)
+
 // Optional per-kernel timing (matpl_profile_begin / matpl_profile_collect): when enabled,
 // every launch site records a CUDA event pair on its own stream.
 bool profiling_enabled();
@@ -58,6 +71,10 @@ struct ProfScope {
 };
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Streaming multiprocessors of the current device (queried once per device; grids are sized
+// in multiples of it).
+int device_sms();
 
 // Device math wrappers: the plain forms call CUDA's tanhf / tanh.
 __device__ __forceinline__ float dev_tanh(float x) { return tanhf(x); }

@@ -74,7 +74,7 @@ __global__ void compress_bwd(const T *__restrict__ f2, const T *__restrict__ coe
 
 inline int grid_for_rows(long long nsij) {
     long long g = (nsij * 32 + kThreads - 1) / kThreads;
-    if (g > 152LL * 16) g = 152LL * 16;
+    if (g > (long long)device_sms() * 16) g = (long long)device_sms() * 16;
     return (int)(g < 1 ? 1 : g);
 }
 
@@ -123,6 +123,7 @@ extern "C" int matpl_calc_compress(int dtype, const void *f2, const void *coeffi
     if (nsij == 0 || layer_node == 0) return MATPL_OK;
     MATPL_REQUIRE(f2 && coefficient && G, MATPL_ERR_INVALID,
                   "matpl_calc_compress: null pointer argument");
+    MATPL_REQUIRE_ON_DEVICE(G, "matpl_calc_compress");
     return dtype == MATPL_F64
                ? launch<double>(false, f2, coefficient, nullptr, nsij, layer_node, coe_num, G,
                                 as_stream(stream))
@@ -138,6 +139,7 @@ extern "C" int matpl_calc_compress_grad(int dtype, const void *f2, const void *c
     if (nsij == 0) return MATPL_OK;
     MATPL_REQUIRE(f2 && grad_f2 && (layer_node == 0 || (coefficient && grad_G)), MATPL_ERR_INVALID,
                   "matpl_calc_compress_grad: null pointer argument");
+    MATPL_REQUIRE_ON_DEVICE(grad_f2, "matpl_calc_compress_grad");
     return dtype == MATPL_F64
                ? launch<double>(true, f2, coefficient, grad_G, nsij, layer_node, coe_num, grad_f2,
                                 as_stream(stream))

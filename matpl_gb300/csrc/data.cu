@@ -79,6 +79,7 @@ extern "C" int matpl_env_stats(int batch, int natoms, int nslots, int ntypes,
                                       (type_map && list_neigh && image_dr)),
                   MATPL_ERR_INVALID, "null pointer argument");
     cudaStream_t s = as_stream(stream);
+    MATPL_REQUIRE_ON_DEVICE(sums, "matpl_env_stats");
     if (cudaMemsetAsync(sums, 0, sizeof(double) * 8 * (size_t)batch * ntypes, s) != cudaSuccess) {
         set_error("matpl_env_stats: memset failed");
         return MATPL_ERR_CUDA;
@@ -86,7 +87,7 @@ extern "C" int matpl_env_stats(int batch, int natoms, int nslots, int ntypes,
     const long long total = (long long)batch * natoms;
     if (total == 0 || nslots == 0) return MATPL_OK;
     ProfScope ps("env_stats", s);
-    const long long grid = std::min<long long>((total + 3) / 4, 152LL * 16);
+    const long long grid = std::min<long long>((total + 3) / 4, (long long)device_sms() * 16);
     env_stats_kernel<<<(int)grid, 128, 0, s>>>(batch, natoms, nslots, ntypes, type_map,
                                                list_neigh, image_dr, rmin, rmax, sums, err_dev);
     return check_launch("matpl_env_stats");

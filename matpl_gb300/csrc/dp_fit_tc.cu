@@ -391,7 +391,7 @@ int launch_fit_tc(bool fast, const float *A, const int32_t *type_map, const floa
     }
     const long long total = (long long)batch * natoms;
     const long long ntiles = (total + FM - 1) / FM;
-    const int grid = (int)(ntiles < 152 ? ntiles : 152);
+    const int grid = (int)(ntiles < device_sms() ? ntiles : device_sms());
     auto k = fast ? dp_fit_tc<true> : dp_fit_tc<false>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FIT_SMEM);
     ProfScope ps("dp_fit_tc", s);

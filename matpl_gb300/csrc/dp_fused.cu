@@ -765,7 +765,7 @@ int launch_eval(int mode, const matpl_dp_model *M, const EvalParams &P,
     }
 
     const long long nwarp_blocks = (total + kWarps - 1) / kWarps;
-    const int gridw = (int)(nwarp_blocks < 152LL * 8 ? (nwarp_blocks < 1 ? 1 : nwarp_blocks) : 152LL * 8);
+    const int gridw = (int)(nwarp_blocks < (long long)device_sms() * 8 ? (nwarp_blocks < 1 ? 1 : nwarp_blocks) : (long long)device_sms() * 8);
     const size_t wbytes = sizeof(T) * (size_t)nnet * EmbOff::SIZE;
     const bool ws_ok = wbytes <= 128 * 1024 && P.ctab == nullptr;   // tables: no net weights
     const size_t wpart = ws_ok ? wbytes : 0;
@@ -797,7 +797,7 @@ int launch_eval(int mode, const matpl_dp_model *M, const EvalParams &P,
     const size_t smem_fit = sizeof(T) * (size_t)TILE * (NA + DIN + 4 * F);
     cudaFuncSetAttribute(dp_fit<T, TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_fit);
     const long long ntiles = (total + TILE - 1) / TILE;
-    const int gridf = (int)(ntiles < 152LL * 4 ? ntiles : 152LL * 4);
+    const int gridf = (int)(ntiles < (long long)device_sms() * 4 ? ntiles : (long long)device_sms() * 4);
     if (mode == MATPL_F32 || mode == MATPL_F64) {
         ProfScope ps("dp_fit", s);
         dp_fit<T, TILE><<<gridf, 256, smem_fit, s>>>(A, type_map, params, Ei, dA, P);
@@ -868,6 +868,7 @@ extern "C" int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, 
     MATPL_REQUIRE(workspace != nullptr && workspace_bytes >= lay.total, MATPL_ERR_WORKSPACE,
                   "dp workspace too small");
     if (batch == 0) return MATPL_OK;
+    MATPL_REQUIRE_ON_DEVICE(workspace, "matpl_dp_eval");
     EvalParams P;
     P.batch = batch; P.natoms = natoms; P.nslots = nslots; P.nghost = nghost;
     P.ntypes = model->ntypes; P.m = model->m; P.npresent = model->npresent;

@@ -716,7 +716,7 @@ int launch_mixed_embed(bool backward, const int32_t *list_neigh, const float *id
     const int fit = (int)std::max<size_t>(1, (220 * 1024) / (smem + 2048));
     int per_sm = std::min(fit, 3);
     if (g_ctas_override.load() > 0) per_sm = std::min(fit, g_ctas_override.load());
-    const int grid = (int)std::min<long long>(ngroups, 152LL * per_sm);
+    const int grid = (int)std::min<long long>(ngroups, (long long)device_sms() * per_sm);
     if (!backward) {
         auto k = dp_embed_fwd_tc<SPLIT, FAST>;
         cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -528,7 +528,7 @@ int launch_desc(bool grad, long long natoms, int m2, const long long *rows, cons
                 cudaStream_t s) {
     const long long work = grad ? natoms * E : natoms * E * m2;
     long long grid = (work + 255) / 256;
-    if (grid > 152LL * 32) grid = 152LL * 32;
+    if (grid > (long long)device_sms() * 32) grid = (long long)device_sms() * 32;
     if (grid < 1) grid = 1;
     if (!grad) {
         ProfScope ps("dp_desc_dual", s);
@@ -565,9 +565,8 @@ int launch(bool backward, const matpl_dp_model *md, int batch, int natoms, int n
     P.inv_mT = 1.0 / ((double)md->m * (double)md->npresent);
     const int nnet = md->ntypes * md->ntypes;
     const size_t wbytes = (size_t)nnet * EmbOff::SIZE * sizeof(T);
-    int dev = 0, sms = 152;
+    int dev = 0, sms = device_sms();
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long total = (long long)batch * natoms;
     if (!backward) {
         int warps = 8;
@@ -636,6 +635,7 @@ extern "C" int matpl_dp_dual_forward(int dtype, const matpl_dp_model *model, int
                       grad_force);
     if (st) return st;
     MATPL_REQUIRE(A && A_dot, MATPL_ERR_INVALID, "null output");
+    MATPL_REQUIRE_ON_DEVICE(A, "matpl_dp_dual_forward");
     return dtype == MATPL_F64
                ? launch<double>(false, model, batch, natoms, nslots, list_neigh, image_dr,
                                 type_map, grad_force, grad_virial, nullptr, nullptr, A, A_dot,
@@ -655,6 +655,7 @@ extern "C" int matpl_dp_dual_backward(int dtype, const matpl_dp_model *model, in
                       grad_force);
     if (st) return st;
     MATPL_REQUIRE(A_bar && A_dot_bar && grad_embedding, MATPL_ERR_INVALID, "null pointer");
+    MATPL_REQUIRE_ON_DEVICE(grad_embedding, "matpl_dp_dual_backward");
     return dtype == MATPL_F64
                ? launch<double>(true, model, batch, natoms, nslots, list_neigh, image_dr,
                                 type_map, grad_force, grad_virial, A_bar, A_dot_bar,
@@ -674,6 +675,7 @@ extern "C" int matpl_dp_desc_dual(int dtype, long long natoms, int m2, const lon
     MATPL_REQUIRE(natoms == 0 || (A && A_dot && D && D_dot), MATPL_ERR_INVALID,
                   "null pointer argument");
     if (natoms == 0) return MATPL_OK;
+    MATPL_REQUIRE_ON_DEVICE(D, "matpl_dp_desc_dual");
     return dtype == MATPL_F64
                ? launch_desc<double>(false, natoms, m2, rows, A, A_dot, nullptr, nullptr, D,
                                      D_dot, as_stream(stream))
@@ -692,6 +694,7 @@ extern "C" int matpl_dp_desc_dual_grad(int dtype, long long natoms, int m2,
     MATPL_REQUIRE(natoms == 0 || (A && A_dot && grad_A && grad_A_dot), MATPL_ERR_INVALID,
                   "null pointer argument");
     if (natoms == 0) return MATPL_OK;
+    MATPL_REQUIRE_ON_DEVICE(grad_A, "matpl_dp_desc_dual_grad");
     return dtype == MATPL_F64
                ? launch_desc<double>(true, natoms, m2, rows, A, A_dot, grad_D, grad_D_dot,
                                      grad_A, grad_A_dot, as_stream(stream))

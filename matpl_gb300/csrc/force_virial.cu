@@ -1,7 +1,7 @@
 // Force / virial custom ops and their backward, the drop-in for MatPL's CalcOps_cuda
 // calculateForce / calculateVirial (src/op/src/CalcOps.cpp:6-72, 170-236).
 //
-// One thread per neighbor slot, grid sized in multiples of the 152 SMs.  Each slot reads its
+// One thread per neighbor slot, grid sized in multiples of the SM count.  Each slot reads its
 // 4 dE values and 12 Ri_d values (contiguous, so a warp reads a contiguous 1.5 KB (f32) /
 // 3 KB (f64) span), forms f = dE . Ri_d (3 values) and scatters it with red.global.add.
 // The virial op also reduces the per-slot outer product f (x) Rij in FP64 per block before a
@@ -15,7 +15,7 @@ constexpr int kThreads = 256;
 
 inline int grid_for(long long work) {
     long long g = (work + kThreads - 1) / kThreads;
-    const long long cap = 152LL * 16;
+    const long long cap = (long long)device_sms() * 16;
     if (g > cap) g = cap;
     if (g < 1) g = 1;
     return (int)g;
@@ -189,6 +189,7 @@ extern "C" int matpl_calc_force(int dtype, const int32_t *list_neigh, const void
                       (nsl == 0 || (list_neigh && dE && Ri_d)),
                   MATPL_ERR_INVALID, "matpl_calc_force: null pointer argument");
     if (nout == 0) return MATPL_OK;
+    MATPL_REQUIRE_ON_DEVICE(force_out, "matpl_calc_force");
     if (dtype == MATPL_F64) {
         copy_center_force<double><<<grid_for(nout), kThreads, 0, s>>>(
             (const double *)F_center, (double *)force_out, batch, natoms, nghost);
@@ -217,6 +218,7 @@ extern "C" int matpl_calc_virial(int dtype, const int32_t *list_neigh, const voi
                       ((long long)batch * natoms * nslots == 0 || (list_neigh && dE && Rij && Ri_d)),
                   MATPL_ERR_INVALID, "matpl_calc_virial: null pointer argument");
     if (batch == 0) return MATPL_OK;
+    MATPL_REQUIRE_ON_DEVICE(virial_out, "matpl_calc_virial");
     cudaStream_t s = as_stream(stream);
     const size_t es = dtype == MATPL_F64 ? 8 : 4;
     if (cudaMemsetAsync(virial_out, 0, es * 9 * (size_t)batch, s) != cudaSuccess ||
@@ -247,6 +249,7 @@ extern "C" int matpl_calc_force_grad(int dtype, const int32_t *list_neigh, const
     if (nsl == 0) return MATPL_OK;
     MATPL_REQUIRE(list_neigh && Ri_d && grad_force && grad_dE, MATPL_ERR_INVALID,
                   "matpl_calc_force_grad: null pointer argument");
+    MATPL_REQUIRE_ON_DEVICE(grad_dE, "matpl_calc_force_grad");
     cudaStream_t s = as_stream(stream);
     if (dtype == MATPL_F64)
         force_grad_kernel<double><<<grid_for(nsl), kThreads, 0, s>>>(
@@ -268,6 +271,7 @@ extern "C" int matpl_calc_virial_grad(int dtype, const int32_t *list_neigh, cons
     if (nsl == 0) return MATPL_OK;
     MATPL_REQUIRE(list_neigh && Rij && Ri_d && grad_virial && grad_dE, MATPL_ERR_INVALID,
                   "matpl_calc_virial_grad: null pointer argument");
+    MATPL_REQUIRE_ON_DEVICE(grad_dE, "matpl_calc_virial_grad");
     cudaStream_t s = as_stream(stream);
     if (dtype == MATPL_F64)
         virial_grad_kernel<double><<<grid_for(nsl), kThreads, 0, s>>>(

@@ -174,7 +174,7 @@ int launch_neighbors(int inum, int nall, const int *ilist, Lists lists, const do
     lmp_init_min<<<1, 1, 0, s>>>(mn);
     if (inum > 0) {
         long long grid = ((long long)inum + 3) / 4;
-        grid = std::min(grid, 152LL * 16);
+        grid = std::min(grid, (long long)device_sms() * 16);
         const double rc2 = rcut * rcut;   // pair_matpl.cpp:536
         const unsigned long long rc2_bits = (unsigned long long)[&] {
             long long b;
@@ -308,6 +308,7 @@ extern "C" int matpl_lammps_dp_neighbors(int inum, int nall, const int *ilist,
     MATPL_REQUIRE(ilist && jstart && x && type && type_to_model && list_neigh && image_dr &&
                       type_map && min_rsq && err_dev && (jflat || inum == 0),
                   MATPL_ERR_INVALID, "null pointer argument");
+    MATPL_REQUIRE_ON_DEVICE(list_neigh, "matpl_lammps_dp_neighbors");
     return launch_neighbors(inum, nall, ilist, CsrLists{jstart, jflat}, x, type, type_to_model,
                             ntypes_lmp, model_ntypes, m, rcut, out_dtype, list_neigh, image_dr,
                             type_map, min_rsq, err_dev, as_stream(stream));
@@ -510,7 +511,7 @@ extern "C" int matpl_lammps_dp_compute_models(matpl_lammps_dp *h, int nmodels, i
                               : (double *)h->out.p + k * out_n + 3 * (size_t)nall;
         ProfScope ps("lmp_pack", s);
         const long long n = (long long)out_n;
-        const int grid = (int)std::min<long long>((n + 255) / 256, 152LL * 8);
+        const int grid = (int)std::min<long long>((n + 255) / 256, (long long)device_sms() * 8);
         if (f64)
             lmp_pack<double><<<grid, 256, 0, s>>>(3LL * nall, inum, (const double *)h->force.p,
                                                   (const double *)h->Ei.p,

@@ -298,7 +298,11 @@ nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
         int ncand = 0;
         bool cap_hit = false;
         if (im.iflag) {
-            const long long T = (long long)P.natoms * nimg;
+            long long T = (long long)P.natoms * nimg;
+            if (T > 0x7fffffffLL) {           // keys would overflow int32: no candidates
+                if (lane == 0) atomicMax(err, MATPL_KERR_BAD_BOX);
+                T = 0;
+            }
             for (long long c0 = 0; c0 < T; c0 += 32) {
                 const long long c = c0 + lane;
                 bool keep = false;
@@ -578,7 +582,7 @@ NbLayout nb_layout(int batch, int natoms) {
 
 inline int grid_for(long long work, int per_block) {
     long long g = (work + per_block - 1) / per_block;
-    if (g > 152LL * 32) g = 152LL * 32;
+    if (g > (long long)device_sms() * 32) g = (long long)device_sms() * 32;
     return (int)(g < 1 ? 1 : g);
 }
 
@@ -612,7 +616,11 @@ extern "C" int matpl_neighbor_build(int batch, int natoms, int ntypes, int m_nei
     MATPL_REQUIRE(workspace != nullptr && workspace_bytes >= lay.total, MATPL_ERR_WORKSPACE,
                   "neighbor workspace too small");
     if (batch == 0 || natoms == 0) return MATPL_OK;
-    // key = j * nimages + image must fit in int32; nimages <= (2*(int(Rc/|a|)+1)+1)^3
+    // candidate keys j * nimages + image are int32: nb_search refuses (MATPL_KERR_BAD_BOX,
+    // empty lists) an image whose natoms * nimages would not fit
+    MATPL_REQUIRE(type_map && lattice && frac_pos && list_neigh && image_dr, MATPL_ERR_INVALID,
+                  "matpl_neighbor_build: null pointer argument");
+    MATPL_REQUIRE_ON_DEVICE(list_neigh, "matpl_neighbor_build");
     cudaStream_t s = as_stream(stream);
     NbParams P;
     P.batch = batch; P.natoms = natoms; P.ntypes = ntypes; P.m = m_neigh;
@@ -671,6 +679,7 @@ extern "C" int matpl_env_mat(int dtype, int batch, int natoms, int nslots,
     if (total == 0) return MATPL_OK;
     MATPL_REQUIRE(type_map && image_dr && davg && dstd && Ri && Ri_d, MATPL_ERR_INVALID,
                   "matpl_env_mat: null pointer argument");
+    MATPL_REQUIRE_ON_DEVICE(Ri, "matpl_env_mat");
     cudaStream_t s = as_stream(stream);
     if (dtype == MATPL_F64)
         env_mat_kernel<double><<<grid_for(total, 256), 256, 0, s>>>(

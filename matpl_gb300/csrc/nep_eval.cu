@@ -672,9 +672,8 @@ int launch_eval(const EvalArgs &A0, cudaStream_t s) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
         return check_launch("cudaFuncSetAttribute(nep_eval)");
-    int dev = 0, sms = 152, per_sm = 1;
+    int dev = 0, sms = device_sms(), per_sm = 1;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * wpb, smem);
     if (per_sm < 1) per_sm = 1;
     const long long warps = (long long)sms * per_sm * wpb;
@@ -775,7 +774,7 @@ int nep_run(int dtype, const matpl_nep_model *model, int nframes, long long nato
     if (st) return st;
     if (dtype == MATPL_F32 && !feats) {
         const long long g = (natoms + 255) / 256;
-        nep_force_out<<<(int)(g > 152 * 8 ? 152 * 8 : g), 256, 0, s>>>(
+        nep_force_out<<<(int)(g > device_sms() * 8 ? device_sms() * 8 : g), 256, 0, s>>>(
             (const float4 *)facc, (float *)force, natoms);
     }
     return check_launch("matpl_nep_eval");
@@ -794,6 +793,7 @@ extern "C" int matpl_nep_eval(int dtype, const matpl_nep_model *model, int nfram
                               double *virial, void *workspace, size_t workspace_bytes,
                               void *stream) {
     MATPL_REQUIRE(Ei && Etot && force && virial, MATPL_ERR_INVALID, "null output pointer");
+    MATPL_REQUIRE_ON_DEVICE(force, "matpl_nep_eval");
     return nep_run(dtype, model, nframes, natoms, num_atom, type_map, max_nn_radial, NN_radial,
                    NL_radial, Ri_radial, max_nn_angular, NN_angular, NL_angular, Ri_angular, Ei,
                    Etot, force, virial, nullptr, workspace, workspace_bytes, stream);
@@ -808,6 +808,7 @@ extern "C" int matpl_nep_descriptor(int dtype, const matpl_nep_model *model, int
                                     const double *Ri_angular, void *feats, void *workspace,
                                     size_t workspace_bytes, void *stream) {
     MATPL_REQUIRE(feats, MATPL_ERR_INVALID, "null feats");
+    MATPL_REQUIRE_ON_DEVICE(feats, "matpl_nep_descriptor");
     return nep_run(dtype, model, nframes, natoms, num_atom, type_map, max_nn_radial, NN_radial,
                    NL_radial, Ri_radial, max_nn_angular, NN_angular, NL_angular, Ri_angular,
                    nullptr, nullptr, nullptr, nullptr, feats, workspace, workspace_bytes, stream);

@@ -655,7 +655,7 @@ int run(int nframes, long long natoms, const long long *num_atom, const long lon
     nepnb_setup<<<1, kSetupThreads, 0, s>>>(num_atom, box, box_orig, num_cell, w.fr, nframes,
                                             natoms, rc_max, err);
     if (natoms == 0) return check_launch("nep_neighbor");
-    const int g1 = blocks_for(natoms, 256, 152 * 16);
+    const int g1 = blocks_for(natoms, 256, device_sms() * 16);
     nepnb_bin<<<g1, 256, 0, s>>>(pos, w.fr, nframes, natoms, w.spos, w.cell_of, w.cell_count);
     nepnb_scan<<<nframes, 1024, 0, s>>>(w.fr, w.cell_count, w.cell_start);
     nepnb_fill<<<g1, 256, 0, s>>>(w.fr, nframes, natoms, w.cell_of, w.cell_start, w.cell_fill,
@@ -673,7 +673,7 @@ int run(int nframes, long long natoms, const long long *num_atom, const long lon
     int wpb = 4;
     while (wpb > 1 && per_warp * wpb > 96 * 1024) wpb >>= 1;
     const size_t smem = align_up(per_warp * wpb, 16);
-    const int grid = blocks_for(natoms, wpb, 152 * 64);
+    const int grid = blocks_for(natoms, wpb, device_sms() * 64);
     if (count_only) {
         if (typed) {
             cudaFuncSetAttribute(nepnb_search<true, true>,
@@ -709,6 +709,7 @@ extern "C" int matpl_nep_neighbor(int nframes, long long natoms, const long long
                                   long long *NL_angular, double *Ri_radial, double *Ri_angular,
                                   int *err_dev, void *workspace, size_t workspace_bytes,
                                   void *stream) {
+    MATPL_REQUIRE_ON_DEVICE(position, "matpl_nep_neighbor");
     return run(nframes, natoms, num_atom, nullptr, 0, box, box_orig, num_cell, position,
                cutoff_radial, cutoff_angular, max_nn_radial, max_nn_angular, with_rij, false,
                false, NN_radial, NN_angular, NL_radial, NL_angular, Ri_radial, Ri_angular,
@@ -722,6 +723,7 @@ extern "C" int matpl_nep_maxneigh(int nframes, long long natoms, const long long
                                   const long long *type_map, int with_type, long long *NN_radial,
                                   long long *NN_angular, int *err_dev, void *workspace,
                                   size_t workspace_bytes, void *stream) {
+    MATPL_REQUIRE_ON_DEVICE(position, "matpl_nep_maxneigh");
     return run(nframes, natoms, num_atom, type_map, ntypes, box, box_orig, num_cell, position,
                cutoff_radial, cutoff_angular, 0, 0, 1, true, with_type != 0, NN_radial,
                NN_angular, nullptr, nullptr, nullptr, nullptr, err_dev, workspace,

@@ -529,14 +529,14 @@ int launch_mb(const FeatArgs &A, cudaStream_t s) {
         set_error("matpl_nep_feat: shared-memory attribute rejected");
         return MATPL_ERR_CUDA;
     }
-    const long long blocks = std::min<long long>((A.natoms + kFeatWarps - 1) / kFeatWarps, 152LL * 32);
+    const long long blocks = std::min<long long>((A.natoms + kFeatWarps - 1) / kFeatWarps, (long long)device_sms() * 32);
     k<<<(int)std::max<long long>(blocks, 1), 32 * kFeatWarps, smem, s>>>(A);
     return check_launch("matpl_nep_feat");
 }
 
 template <typename T, int MODE, int NM, int KM>
 int launch_2b(const FeatArgs &A, cudaStream_t s) {
-    const long long blocks = std::min<long long>((A.natoms + kFeatWarps - 1) / kFeatWarps, 152LL * 32);
+    const long long blocks = std::min<long long>((A.natoms + kFeatWarps - 1) / kFeatWarps, (long long)device_sms() * 32);
     nep2b_op<T, MODE, NM, KM><<<(int)std::max<long long>(blocks, 1), 32 * kFeatWarps, 0, s>>>(A);
     return check_launch("matpl_nep_feat");
 }
@@ -816,6 +816,7 @@ extern "C" int matpl_nep_cgrad(int dtype, int part, int natoms, int ntypes, int 
     MATPL_REQUIRE(part == 1 || ldG >= n_max, MATPL_ERR_INVALID, "radial: ldG >= n_max");
     MATPL_REQUIRE(dc && err_dev && (natoms == 0 || (type_map && W && (part == 1 || G))),
                   MATPL_ERR_INVALID, "null pointer argument");
+    MATPL_REQUIRE_ON_DEVICE(dc, "matpl_nep_cgrad");
     cudaStream_t s = as_stream(stream);
     const size_t esz = dtype == MATPL_F64 ? sizeof(double) : sizeof(float);
     const size_t nout = (size_t)ntypes * ntypes * n_max * n_base;
@@ -847,6 +848,7 @@ extern "C" int matpl_nep_force_virial(int dtype, int natoms, int max_nn, int nim
     MATPL_REQUIRE(force && virial && err_dev &&
                       (natoms * (long long)max_nn == 0 || (NL && image_of && dE && Ri)),
                   MATPL_ERR_INVALID, "null pointer argument");
+    MATPL_REQUIRE_ON_DEVICE(force, "matpl_nep_force_virial");
     cudaStream_t s = as_stream(stream);
     const size_t esz = dtype == MATPL_F64 ? sizeof(double) : sizeof(float);
     if (cudaMemsetAsync(force, 0, esz * 3 * (size_t)natoms, s) != cudaSuccess ||
@@ -880,9 +882,10 @@ extern "C" int matpl_nep_force_virial_grad(int dtype, int natoms, int max_nn, in
                   MATPL_ERR_INVALID, "null pointer argument");
     const long long total = (long long)natoms * max_nn;
     if (total == 0) return MATPL_OK;
+    MATPL_REQUIRE_ON_DEVICE(g_dE, "matpl_nep_force_virial_grad");
     cudaStream_t s = as_stream(stream);
     ProfScope ps("nep_force_virial_grad", s);
-    const int grid = (int)std::min<long long>((total + 255) / 256, 152LL * 16);
+    const int grid = (int)std::min<long long>((total + 255) / 256, (long long)device_sms() * 16);
     if (dtype == MATPL_F64)
         nep_force_virial_grad_kernel<double><<<grid, 256, 0, s>>>(
             natoms, max_nn, nimages, NL, image_of, (const double *)Ri, (const double *)g_force,
@@ -918,6 +921,7 @@ extern "C" int matpl_nep_feat_op(int dtype, int part, int mode, int natoms, int 
                   "bwd needs G and grad_d12 or W");
     MATPL_REQUIRE(mode != 2 || (G && H && q && W), MATPL_ERR_INVALID, "bwd2 needs G, H, gso, W");
     if (natoms == 0 || max_nn == 0) return MATPL_OK;
+    MATPL_REQUIRE_ON_DEVICE(d12, "matpl_nep_feat_op");
     FeatArgs A{};
     A.natoms = natoms;
     A.nn = max_nn;

@@ -147,10 +147,11 @@ extern "C" int matpl_nep_zbl(int dtype, int ri_dtype, long long natoms, int max_
                               (NL && Ri && type_map && image_of && pair_s && pair_c && Ei &&
                                force && virial)),
                   MATPL_ERR_INVALID, "null pointer argument");
+    MATPL_REQUIRE_ON_DEVICE(force, "matpl_nep_zbl");
     if (natoms == 0 || max_nn == 0) return MATPL_OK;
     cudaStream_t s = as_stream(stream);
     ProfScope ps("nep_zbl", s);
-    const int grid = (int)std::min<long long>((natoms + 7) / 8, 152LL * 16);
+    const int grid = (int)std::min<long long>((natoms + 7) / 8, (long long)device_sms() * 16);
     if (dtype == MATPL_F64)
         nep_zbl_kernel<double, double><<<grid, 256, 0, s>>>(
             natoms, max_nn, nimages, NL, (const double *)Ri, type_map, image_of, ntypes, pair_s,

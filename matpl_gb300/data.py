@@ -40,6 +40,7 @@ def model_types(st, atom_type: Sequence[int]) -> np.ndarray:
     return np.array([at.index(int(v)) for v in z], dtype=np.int32)
 
 
+@_lib.on_device
 def image_stats(cfg: DPConfig, images: Sequence, device="cuda") -> List[Dict]:
     """Per image: {types: model types present (first-appearance order), counts, sums [T, 8]}
     with sums[t] = (sum Ri_0, sum Ri_0^2, sum Ri_x, sum Ri_x^2, ... Ri_z) over every slot of the

@@ -187,6 +187,7 @@ class DP(torch.nn.Module):
             self._perm_cache = {key: p}
         return p
 
+    @_lib.on_device
     def evaluate(self, list_neigh: torch.Tensor, Imagetype_map: torch.Tensor, present: List[int],
                  ImageDR: torch.Tensor, nghost: int = 0, out: Optional[dict] = None):
         """Raw fused evaluation: returns dict(Ei_atom [B,N], Etot [B] f64, Force, Virial [B,9] f64)."""

@@ -120,6 +120,7 @@ class PairMATPL:
         return {"f": f, "eng": eng.value, "virial": vir, "eatom": eatom, "min_rsq": mn.value}
 
 
+@_lib.on_device
 def _compute_models(pair: PairMATPL, nmodels, x, type_, nlocal, nghost, ilist, numneigh,
                     firstneigh, eflag_atom):
     nall = nlocal + nghost
@@ -169,6 +170,7 @@ def model_deviation(f_n: np.ndarray, e_n: np.ndarray) -> Tuple[float, ...]:
             float(eerr.min()))
 
 
+@_lib.on_device
 def lammps_dp_neighbors(ilist: torch.Tensor, jstart: torch.Tensor, jflat: torch.Tensor,
                         x: torch.Tensor, type_: torch.Tensor, type_to_model: torch.Tensor,
                         ntypes: int, m: int, rcut: float, dtype=torch.float64,

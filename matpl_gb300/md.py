@@ -72,9 +72,10 @@ class ReplicaMD:
             nb_ws = max(nb_ws, lib.matpl_neighbor_workspace_bytes(B, N))
             dp_ws = max(dp_ws, lib.matpl_dp_workspace_bytes(self.model.code, B, N))
             self.groups.append(g)
-        # size the shared workspaces once: nothing is reallocated after the graph is captured
+        # the neighbor workspace is sized once for the largest group and owned here; the
+        # evaluation's workspace is sized on the capture stream before the capture
         self.nb_ws = ops.workspace(self.dev, nb_ws, "neighbor")
-        ops.workspace(self.dev, dp_ws, "dp")
+        self._dp_ws_bytes = dp_ws
         self.natoms_total = sum(g["B"] * g["N"] for g in self.groups)
         self.nreplicas = len(replicas)
         self.graph = None
@@ -88,11 +89,13 @@ class ReplicaMD:
         cfg = self.cfg
         B, N = g["B"], g["N"]
         torch.matmul(g["x"], g["inv_lat"], out=g["frac"])
-        check(_lib.load().matpl_neighbor_build(
-            B, N, cfg.ntypes, cfg.maxNeighborNum, float(cfg.Rmax), self.rct, ptr(g["types"]),
-            ptr(g["lat"]), ptr(g["frac"]), self.model.code if self.model.code in (0, 1) else 0,
-            ptr(g["ln"]), ptr(g["idr"]), 0, ptr(self.err), ptr(self.nb_ws), self.nb_ws.numel(),
-            torch.cuda.current_stream(self.dev).cuda_stream), "matpl_neighbor_build")
+        with torch.cuda.device(self.dev):
+            check(_lib.load().matpl_neighbor_build(
+                B, N, cfg.ntypes, cfg.maxNeighborNum, float(cfg.Rmax), self.rct, ptr(g["types"]),
+                ptr(g["lat"]), ptr(g["frac"]), self.model.code if self.model.code in (0, 1) else 0,
+                ptr(g["ln"]), ptr(g["idr"]), 0, ptr(self.err), ptr(self.nb_ws),
+                self.nb_ws.numel(), torch.cuda.current_stream(self.dev).cuda_stream),
+                "matpl_neighbor_build")
         self.model.evaluate(g["ln"], g["types"], self.present, g["idr"], 0, out=g["out"])
 
     def _accel(self, g):
@@ -121,11 +124,12 @@ class ReplicaMD:
         side = torch.cuda.Stream(self.dev)
         side.wait_stream(torch.cuda.current_stream(self.dev))
         with torch.cuda.stream(side):
+            ops.workspace(self.dev, self._dp_ws_bytes, "dp")   # nothing grows in the capture
             for _ in range(warmup):
                 self._step()
         torch.cuda.current_stream(self.dev).wait_stream(side)
         self.graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(self.graph):
+        with torch.cuda.graph(self.graph, stream=side):
             self._step()
         for g, kp, ko in zip(self.groups, keep, keep_out):
             for k, t in kp.items():

@@ -23,6 +23,8 @@ import math
 import numpy as np
 import torch
 
+from . import _lib
+
 
 @dataclass
 class NepConfig:
@@ -280,6 +282,7 @@ class NEP(torch.nn.Module):
         m.err_dev = ptr(self.err)
         return m
 
+    @_lib.on_device
     def evaluate(self, NN_radial, NL_radial, Ri_radial, NN_angular, NL_angular, Ri_angular,
                  num_atom, atom_type_map, out=None, descriptor_only: bool = False):
         """Raw evaluation: dict(Ei [N], Etot [B] f64, Force [N, 3], Virial [B, 9] f64)."""

@@ -70,6 +70,7 @@ def _nfeat(part, nmax, l3, l4, l5):
     return nmax * (l3 + (1 if l4 > 0 else 0) + (1 if l5 > 0 else 0))
 
 
+@_lib.on_device
 def _feat_call(part, mode, coeff, d12, NL, atom_map, rc, l3=0, l4=0, l5=0, G=None, H=None,
                want_d=True, want_c=True):
     """One launch of ``matpl_nep_feat_op``; returns (q or gso, grad_d12, W).  In the backward
@@ -107,6 +108,7 @@ def _feat_call(part, mode, coeff, d12, NL, atom_map, rc, l3=0, l4=0, l5=0, G=Non
     return q, gd, W
 
 
+@_lib.on_device
 def _c_grad(part, W, G, atom_map, T):
     """dL/dc [T, T, n, K] from the per-atom tables (``matpl_nep_cgrad``): radial
     sum_i G[i, n] W[i, t, k]; angular sum_i W[i] (G already folded in), each into row t_i."""
@@ -273,6 +275,7 @@ class _NepForceVirial(torch.autograd.Function):
     linear in dE, its backward (``matpl_nep_force_virial_grad``) is the transpose map."""
 
     @staticmethod
+    @_lib.on_device
     def forward(ctx, NL, dE, Ri, image_of, nimages):
         N, NN = NL.shape
         dev, dt = dE.device, dE.dtype
@@ -289,6 +292,7 @@ class _NepForceVirial(torch.autograd.Function):
 
     @staticmethod
     @torch.autograd.function.once_differentiable
+    @_lib.on_device
     def backward(ctx, gF, gV):
         nl, R, image_of = ctx.saved_tensors
         N, NN = nl.shape
@@ -342,6 +346,7 @@ def zbl_tables(atom_type, dev):
     return t
 
 
+@_lib.on_device
 def nep_zbl(zbl: float, atom_type, NL_a: torch.Tensor, Ri_a: torch.Tensor,
             type_map: torch.Tensor, counts, Ei: torch.Tensor, Etot, force: torch.Tensor,
             virial: torch.Tensor) -> None:
@@ -369,6 +374,7 @@ def nep_zbl(zbl: float, atom_type, NL_a: torch.Tensor, Ri_a: torch.Tensor,
 
 class _NepVirial(torch.autograd.Function):
     @staticmethod
+    @_lib.on_device
     def forward(ctx, list_neigh, dE, Rij, Ri_d, num_atom):
         N, NN = list_neigh.shape
         nl = list_neigh.contiguous().to(torch.int32)
@@ -391,6 +397,7 @@ class _NepVirial(torch.autograd.Function):
         return vir, avir
 
     @staticmethod
+    @_lib.on_device
     def backward(ctx, grad_vir, grad_avir):
         nl, Rj, Rd = ctx.saved_tensors
         N, NN = nl.shape

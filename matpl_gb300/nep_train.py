@@ -224,7 +224,7 @@ class GraphedNepTrainer:
         torch.cuda.current_stream().wait_stream(side)
         g = torch.cuda.CUDAGraph()
         self.opt.zero_grad(set_to_none=True)
-        with torch.cuda.graph(g):
+        with torch.cuda.graph(g, stream=side):   # the warm-up's workspaces are reused
             loss = self.loss(static, tindex)
             loss.backward()
             self.opt.step()

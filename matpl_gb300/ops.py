@@ -41,6 +41,7 @@ def _nghost(n) -> int:
 
 class _CalculateForce(torch.autograd.Function):
     @staticmethod
+    @_lib.on_device
     def forward(ctx, list_neigh, dE, Ri_d, F, nghost: int):
         B, N = list_neigh.shape[0], list_neigh.shape[1]
         S = list_neigh[0, 0].numel() if N > 0 else 0
@@ -56,6 +57,7 @@ class _CalculateForce(torch.autograd.Function):
         return out
 
     @staticmethod
+    @_lib.on_device
     def backward(ctx, grad_force):
         nl, Rd = ctx.saved_tensors
         B, N, S, nghost, dshape = ctx.meta
@@ -70,6 +72,7 @@ class _CalculateForce(torch.autograd.Function):
 
 class _CalculateVirial(torch.autograd.Function):
     @staticmethod
+    @_lib.on_device
     def forward(ctx, list_neigh, dE, Rij, Ri_d, nghost: int):
         B, N = list_neigh.shape[0], list_neigh.shape[1]
         S = list_neigh[0, 0].numel() if N > 0 else 0
@@ -87,6 +90,7 @@ class _CalculateVirial(torch.autograd.Function):
         return vir, avir
 
     @staticmethod
+    @_lib.on_device
     def backward(ctx, grad_vir, grad_avir):
         nl, Rj, Rd = ctx.saved_tensors
         B, N, S, dshape = ctx.meta
@@ -121,6 +125,7 @@ def calculateVirial(list_neigh: torch.Tensor, dE: torch.Tensor, Rij: torch.Tenso
 
 class _CalculateCompress(torch.autograd.Function):
     @staticmethod
+    @_lib.on_device
     def forward(ctx, f2, coefficient):
         ns, nodes, nc = coefficient.shape
         f = f2.contiguous().reshape(-1).to(coefficient.dtype)
@@ -133,6 +138,7 @@ class _CalculateCompress(torch.autograd.Function):
         return G
 
     @staticmethod
+    @_lib.on_device
     def backward(ctx, grad_G):
         f, c = ctx.saved_tensors
         ns, nodes, nc = c.shape
@@ -152,6 +158,7 @@ def calculateCompress(f2: torch.Tensor, coefficient: torch.Tensor) -> List[torch
     return [_CalculateCompress.apply(f2, coefficient)]
 
 
+@_lib.on_device
 def env_mat(ImageDR: torch.Tensor, Imagetype_map: torch.Tensor, davg: torch.Tensor,
             dstd: torch.Tensor, Rmin: float, Rmax: float) -> Tuple[torch.Tensor, torch.Tensor]:
     """``DP.calculate_Ri`` (dp_dp.py:217-302): normalised Ri [B,N,S,4] and Ri_d [B,N,S,4,3]."""
@@ -179,8 +186,13 @@ _ws_cache = {}
 
 
 def workspace(device: torch.device, nbytes: int, tag: str) -> torch.Tensor:
-    """Grow-only per-device scratch buffer (the C ABI itself never allocates)."""
-    key = (str(device), tag)
+    """Grow-only scratch buffer per (device, current stream, tag); the C ABI itself never
+    allocates.  Keying by the stream keeps calls on different streams from sharing one buffer
+    (they could overlap on the GPU), and a buffer that is replaced by a larger one was only
+    ever used on that stream, so the allocator may hand it out again in stream order."""
+    device = torch.device(device)
+    stream = torch.cuda.current_stream(device).cuda_stream
+    key = (str(device), stream, tag)
     buf = _ws_cache.get(key)
     if buf is None or buf.numel() < nbytes:
         buf = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=device)
@@ -188,6 +200,7 @@ def workspace(device: torch.device, nbytes: int, tag: str) -> torch.Tensor:
     return buf
 
 
+@_lib.on_device
 def find_neighbore(type_maps: torch.Tensor, frac_position: torch.Tensor, lattice: torch.Tensor,
                    ntypes: int, m_neigh: int, Rc_M: float, Rc_type: Union[float, Sequence[float]],
                    out_dtype: torch.dtype = torch.float64, with_counts: bool = False,
@@ -227,6 +240,9 @@ def find_neighbore(type_maps: torch.Tensor, frac_position: torch.Tensor, lattice
         code = int(err.item())
         if code == _lib.KERR_NEIGHBOR_OVERFLOW:
             raise NeighborOverflow(f"Error! maxNeighborNum too small {m_neigh}")
+        if code == _lib.KERR_BAD_BOX:
+            raise _lib.MatplError("matpl_neighbor_build: the cell is so small that natoms x "
+                                  "periodic images exceeds 2^31")
         if code != 0:
             raise _lib.MatplError(f"matpl_neighbor_build kernel error {code} (bad atom type)")
     if with_counts:
@@ -257,6 +273,7 @@ def _nep_kernel_error(err: torch.Tensor, what: str):
         raise _lib.MatplError(f"{what} kernel error code {code}")
 
 
+@_lib.on_device
 def calculate_maxneigh(num_atoms: torch.Tensor, box: torch.Tensor, box_orig: torch.Tensor,
                        num_cell: torch.Tensor, position: torch.Tensor, cutoff_2b: float,
                        cutoff_3b: float, atom_type_num: int, atom_type_map: torch.Tensor,
@@ -280,6 +297,7 @@ def calculate_maxneigh(num_atoms: torch.Tensor, box: torch.Tensor, box_orig: tor
     return [NN_r, NN_a]
 
 
+@_lib.on_device
 def calculate_neighbor(num_atoms: torch.Tensor, atom_type_map: torch.Tensor,
                        atom_types: torch.Tensor, box: torch.Tensor, box_orig: torch.Tensor,
                        num_cell: torch.Tensor, position: torch.Tensor, cutoff_2b: float,

@@ -200,6 +200,7 @@ class _EmbedDual(torch.autograd.Function):
     force / virial seed (matpl_dp_dual_forward); the backward is matpl_dp_dual_backward."""
 
     @staticmethod
+    @_lib.on_device
     def forward(ctx, emb_flat, trainer, ln, idr, tm, gF, gV):
         B, N, S = ln.shape
         dev = idr.device
@@ -217,6 +218,7 @@ class _EmbedDual(torch.autograd.Function):
         return A, Ad
 
     @staticmethod
+    @_lib.on_device
     def backward(ctx, gA, gAd):
         flat, ln, idr, tm, gF, gV = ctx.saved_tensors
         B, N, S = ln.shape
@@ -237,6 +239,7 @@ class _DescDual(torch.autograd.Function):
     output row r = atom rows[r]); the backward is the transpose map (matpl_dp_desc_dual_grad)."""
 
     @staticmethod
+    @_lib.on_device
     def forward(ctx, A, Ad, m2, rows):
         A = A.contiguous()
         Ad = Ad.contiguous()
@@ -254,6 +257,7 @@ class _DescDual(torch.autograd.Function):
 
     @staticmethod
     @torch.autograd.function.once_differentiable
+    @_lib.on_device
     def backward(ctx, gD, gDd):
         A, Ad, rows = ctx.saved_tensors
         R = rows.numel()
@@ -496,7 +500,7 @@ class GraphedTrainer:
         torch.cuda.current_stream().wait_stream(side)
         g = torch.cuda.CUDAGraph()
         self.opt.zero_grad(set_to_none=True)
-        with torch.cuda.graph(g):
+        with torch.cuda.graph(g, stream=side):   # the warm-up's workspaces are reused
             loss, le, lf = self.tr._loss_and_backward(static, self.w_f, self.w_e)
             self.opt.step()
         return g, static, loss

@@ -2,7 +2,8 @@
 
 Compiles ``oracle/neighconst.c`` (DP neighbor list), ``oracle/nepneigh.c`` (NEP neighbor
 lists) and ``oracle/lammps_neigh.c`` (DP slots from a LAMMPS full list) into
-``oracle/_build/libmatpl_oracle.so`` with gcc.  ``-ffp-contract=off`` is required:
+``oracle/_build/libmatpl_oracle.so`` with gcc (``-fopenmp`` where available).
+``-ffp-contract=off`` is required:
 the restatements' floating-point order is the reference source order with no fused
 multiply-add, on x86_64 and aarch64 alike.
 """
@@ -22,7 +23,10 @@ def build(force: bool = False) -> str:
         return LIB
     cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-shared", "-fPIC",
            "-o", LIB, *srcs, "-lm"]
-    subprocess.check_call(cmd)
+    # the centre-atom loops run in parallel with OpenMP where the compiler has it (results do
+    # not depend on it: every atom's rows are computed in the serial order)
+    if subprocess.call(cmd[:1] + ["-fopenmp"] + cmd[1:], stderr=subprocess.DEVNULL) != 0:
+        subprocess.check_call(cmd)
     return LIB
 
 

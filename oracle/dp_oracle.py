@@ -198,6 +198,39 @@ def dp_eval(cfg: DPConfig, params: Dict[str, torch.Tensor], davg, dstd,
             "Virial": V, "dE": dE, "Ri": Ri, "Ri_d": Ri_d}
 
 
+def dp_eval_chunked(cfg: DPConfig, params: Dict[str, torch.Tensor], davg, dstd,
+                    list_neigh, Imagetype_map, atom_type, ImageDR, chunk: int = 2000):
+    """``dp_eval`` for one large image, in chunks of centre atoms (the same arithmetic: the
+    energy is a sum of per-atom terms, each depending on its own row of Ri only, and every
+    row's dE/dRi contracts with Ri_d into the centre and neighbor forces,
+    ``dp_dp.py:417-459``).  Bounds the autograd graph to ``chunk`` centre atoms.  Returns
+    Etot [1], Ei_atom [1,N], Force [1,N,3] and Virial [1,9] (all nine f_a*Rij_b, the GPU
+    operator's convention, ``calculateVirial.cu:80``)."""
+    dtype = ImageDR.dtype
+    B, N, S, _ = ImageDR.shape
+    assert B == 1
+    present = _present_types(cfg, atom_type)
+    tmap = Imagetype_map.reshape(-1)
+    Force = torch.zeros(N + 1, 3, dtype=dtype)
+    V = torch.zeros(3, 3, dtype=dtype)
+    Ei_atom = torch.zeros(N, dtype=dtype)
+    for c0 in range(0, N, chunk):
+        c1 = min(N, c0 + chunk)
+        idr = ImageDR[:, c0:c1].detach()
+        Ri, Ri_d = env_matrix(cfg, idr, tmap[c0:c1], davg, dstd)
+        Ri = Ri.detach().requires_grad_()
+        _, ea = energy_from_Ri(cfg, params, Ri, tmap[c0:c1], present)
+        e = ea.sum()
+        dE = torch.autograd.grad([e], [Ri])[0]
+        f = (dE.unsqueeze(-1) * Ri_d).sum(-2)[0]                  # [n, S, 3]
+        Ei_atom[c0:c1] = ea.detach().reshape(-1)
+        Force[1 + c0:1 + c1] -= f.sum(-2)
+        Force.index_add_(0, list_neigh[0, c0:c1].reshape(-1).long(), f.reshape(-1, 3))
+        V += torch.einsum("nsa,nsc->ac", f, idr[0, ..., 1:])
+    return {"Etot": Ei_atom.sum().reshape(1), "Ei_atom": Ei_atom.reshape(1, N),
+            "Force": Force[1:].reshape(1, N, 3), "Virial": V.reshape(1, 9)}
+
+
 def force_virial_ops(list_neigh0, dE, Ri_d, Rij, F_center, nghost: int):
     """Oracle for the ``calculateForce`` / ``calculateVirial`` custom ops
     (``src/op/src/CalcOps.cpp:6-22, 170-185``; kernels ``calculateForce.cu:49-93``,

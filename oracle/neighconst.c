@@ -43,7 +43,7 @@ int matpl_oracle_find_neighbore(int images, const double *lattice, double *posit
     memset(list_neigh, 0, sizeof(int32_t) * (size_t)images * natoms * slots_per_atom);
     memset(dR_neigh, 0, sizeof(double) * 3 * (size_t)images * natoms * slots_per_atom);
     int iflag = 0; /* NeighConst.f90:35 — set once, never reset between images */
-    int num_type[64], num_type_M[64];
+    int overflow = 0;
     if (ntypes > 64) return 2;
 
     for (int n = 0; n < images; ++n) {
@@ -60,21 +60,26 @@ int matpl_oracle_find_neighbore(int images, const double *lattice, double *posit
             for (int k = 0; k < 3; ++k) P[3 * i + k] = fortran_mod1(P[3 * i + k] + 10.0);
 
         const double Rc2 = Rc_M * Rc_M;
+        /* centre atoms are independent: with OpenMP they run in parallel (each writes only its
+         * own rows); the Fortran "stop" becomes a flag that ends that atom's search */
+#pragma omp parallel for schedule(dynamic, 16) reduction(|| : overflow)
         for (int i = 0; i < natoms; ++i) {
+            int num_type[64], num_type_M[64];
             const double rct = Rc_type[type_maps[i] - 1];
             const double rct2 = rct * rct;
             int32_t *LN = list_neigh + ((size_t)n * natoms + i) * slots_per_atom;
             double *DR = dR_neigh + 3 * ((size_t)n * natoms + i) * slots_per_atom;
+            int stop = 0;
             for (int t = 0; t < ntypes; ++t) { num_type[t] = 0; num_type_M[t] = 0; }
-            for (int j = 0; j < natoms; ++j) {
+            for (int j = 0; j < natoms && !stop; ++j) {
                 int ilo[3], ihi[3];
                 for (int v = 0; v < 3; ++v) {
                     ilo[v] = iflag ? -nperiod[v] : 0;
                     ihi[v] = iflag ? nperiod[v] : 0;
                 }
-                for (int i1 = ilo[0]; i1 <= ihi[0]; ++i1)
-                for (int i2 = ilo[1]; i2 <= ihi[1]; ++i2)
-                for (int i3 = ilo[2]; i3 <= ihi[2]; ++i3) {
+                for (int i1 = ilo[0]; i1 <= ihi[0] && !stop; ++i1)
+                for (int i2 = ilo[1]; i2 <= ihi[1] && !stop; ++i2)
+                for (int i3 = ilo[2]; i3 <= ihi[2] && !stop; ++i3) {
                     double dx1, dx2, dx3;
                     if (iflag) { /* NeighConst.f90:62-64 */
                         dx1 = P[3 * j + 0] - P[3 * i + 0] + i1;
@@ -92,7 +97,7 @@ int matpl_oracle_find_neighbore(int images, const double *lattice, double *posit
                     if (dd < Rc2 && dd > 1.0e-8) {
                         const int it = type_maps[j] - 1;
                         num_type_M[it] += 1;
-                        if (num_type_M[it] > m_neigh) return 1;
+                        if (num_type_M[it] > m_neigh) { stop = 1; overflow = 1; break; }
                         if (dd < rct2 && dd > 1.0e-8) {
                             const int slot = it * m_neigh + num_type[it];
                             num_type[it] += 1;
@@ -105,7 +110,9 @@ int matpl_oracle_find_neighbore(int images, const double *lattice, double *posit
                 }
             }
         }
+        if (overflow) return 1;
         /* NeighConst.f90:136-147 — clear slots whose |dR|_1 <= 1e-8 */
+#pragma omp parallel for schedule(static)
         for (int i = 0; i < natoms; ++i) {
             int32_t *LN = list_neigh + ((size_t)n * natoms + i) * slots_per_atom;
             double *DR = dR_neigh + 3 * ((size_t)n * natoms + i) * slots_per_atom;

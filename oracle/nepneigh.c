@@ -56,6 +56,9 @@ int oracle_nep_neighbor(int64_t nframes, const int64_t *num_atom, const double *
         const int64_t N2 = N1 + num_atom[f];
         const double *bx = box + 18 * f, *bo = box_orig + 9 * f;
         const int64_t *nc = num_cell + 3 * f;
+        /* centre atoms are independent: with OpenMP they run in parallel (each writes only its
+         * own rows, in the serial order) */
+#pragma omp parallel for schedule(dynamic, 16) reduction(|| : overflow)
         for (int64_t n1 = N1; n1 < N2; ++n1) {
             for (int64_t s = 0; s < max_r; ++s) NL_r[n1 * max_r + s] = -1;
             for (int64_t s = 0; s < max_a; ++s) NL_a[n1 * max_a + s] = -1;
@@ -110,6 +113,7 @@ void oracle_nep_maxneigh(int64_t nframes, const int64_t *num_atom, const double 
         const int64_t N2 = N1 + num_atom[f];
         const double *bx = box + 18 * f, *bo = box_orig + 9 * f;
         const int64_t *nc = num_cell + 3 * f;
+#pragma omp parallel for schedule(dynamic, 16)
         for (int64_t n1 = N1; n1 < N2; ++n1) {
             const int64_t nt = with_type ? ntypes : 1;
             for (int64_t t = 0; t < nt; ++t) NN_r[n1 * nt + t] = NN_a[n1 * nt + t] = 0;

@@ -23,7 +23,10 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT_DIR, "libCalcOps_bind_cpu.so")
-REF_OP = os.environ.get("MATPL_REFERENCE_OP_DIR", "/root/reference/src/op")
+sys.path.insert(0, os.path.dirname(HERE))
+from oracle.refpath import reference_root  # noqa: E402
+
+REF_OP = os.environ.get("MATPL_REFERENCE_OP_DIR") or os.path.join(reference_root(), "src", "op")
 SOURCES = ["CalcOps_cpu.cpp", "cpu_calculate_nepneighbor.cpp", "nep_cpu.cpp",
            "CalcOps_bind_cpu.cpp"]
 

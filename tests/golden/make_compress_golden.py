@@ -1,6 +1,7 @@
 """Generate the golden fixture of the compressed DP model from MatPL's own code.
 
-Runs only where the MatPL source tree is mounted (path in MATPL_REF, default /root/reference);
+Runs only where the MatPL source tree is mounted (path in MATPL_REF, default: a
+``reference`` directory beside the repository root);
 the committed ``compress_*.npz`` files are what the tests read.  For a seeded two-element DP
 (the ``hfo48_f64`` case: its structure, weights, davg / dstd) it builds the compression table
 with the reference's own ``set_sij_range`` and ``dp_model_compress_5order`` /
@@ -28,7 +29,9 @@ from matpl_gb300 import params as P  # noqa: E402
 from make_golden import ref_config  # noqa: E402
 from oracle import neigh  # noqa: E402
 
-REF = os.environ.get("MATPL_REF", "/root/reference")
+from oracle.refpath import reference_root  # noqa: E402
+
+REF = reference_root()
 DX = 0.02
 SIJ_MAX_PAD = 1.0   # raw s maximum of the "training data": the case's own maximum times this
 

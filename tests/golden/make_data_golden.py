@@ -1,6 +1,7 @@
 """Generate the golden fixture of the data-path statistics from MatPL's own loader code.
 
-Runs only where the MatPL source tree is mounted (path in MATPL_REF, default /root/reference);
+Runs only where the MatPL source tree is mounted (path in MATPL_REF, default: a
+``reference`` directory beside the repository root);
 the committed ``data_stats.npz`` is what the tests read.  It imports
 ``src/pre_data/dpuni_data_loader.py`` (with stand-ins for the modules it imports but does not
 use here: pwdata, yaml, the input-parameter class and the Fortran NeighConst module, which
@@ -29,7 +30,9 @@ sys.path.insert(0, REPO)
 from matpl_gb300 import params as P, structures  # noqa: E402
 from oracle import neigh  # noqa: E402
 
-REF = os.environ.get("MATPL_REF", "/root/reference")
+from oracle.refpath import reference_root  # noqa: E402
+
+REF = reference_root()
 ATOM_TYPE = [3, 14]
 M, RC, RMIN = 60, 5.0, 0.5
 SEED_SHUFFLE = 1234

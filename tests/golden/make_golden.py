@@ -1,7 +1,7 @@
 """Generate the golden E/F/V fixtures by running MatPL's own DP implementation.
 
-Runs only in a container where the MatPL source tree is mounted (path in MATPL_REF, default
-/root/reference); the committed ``*.npz`` files are what the tests read.  For each case it
+Runs only in a container where the MatPL source tree is mounted (path in MATPL_REF, default: a
+``reference`` directory beside the repository root); the committed ``*.npz`` files are what the tests read.  For each case it
 
 1. builds a seeded synthetic structure (``matpl_gb300.structures``),
 2. builds the neighbor list with the oracle restatement of NeighConst.f90 (the Fortran module
@@ -28,7 +28,9 @@ sys.path.insert(0, REPO)
 from matpl_gb300 import structures, params as P  # noqa: E402
 from oracle import neigh  # noqa: E402
 
-REF = os.environ.get("MATPL_REF", "/root/reference")
+from oracle.refpath import reference_root  # noqa: E402
+
+REF = reference_root()
 
 
 def sha(a: np.ndarray) -> str:

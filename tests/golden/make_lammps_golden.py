@@ -1,6 +1,7 @@
 """Generate the golden fixture of the LAMMPS DP pair step from MatPL's shipped TorchScript model.
 
-Runs only where the MatPL source tree is mounted (path in MATPL_REF, default /root/reference);
+Runs only where the MatPL source tree is mounted (path in MATPL_REF, default: a
+``reference`` directory beside the repository root);
 the committed ``lmp_hfo2_jit.npz`` is what the tests read.  It
 
 1. reads the demo structure ``src/lmps/lammps-libtorch/dp_lmps_demo/lmp.config`` (96 atoms of
@@ -31,7 +32,9 @@ sys.path.insert(0, REPO)
 from matpl_gb300.lammps import lammps_system  # noqa: E402
 from oracle import lammps as OL  # noqa: E402
 
-REF = os.environ.get("MATPL_REF", "/root/reference")
+from oracle.refpath import reference_root  # noqa: E402
+
+REF = reference_root()
 SKIN = 1.0
 PAIR_COEFF = [72, 8]
 

@@ -1,6 +1,7 @@
 """Generate the NEP golden fixtures by running MatPL's own NEP implementation.
 
-Runs only where the MatPL source tree is mounted (path in MATPL_REF, default /root/reference);
+Runs only where the MatPL source tree is mounted (path in MATPL_REF, default: a
+``reference`` directory beside the repository root);
 the committed ``nep_*.npz`` files are what the tests read.  For each case it
 
 1. builds seeded synthetic frames (``matpl_gb300.structures``) and expands their boxes with
@@ -30,7 +31,9 @@ sys.path.insert(0, REPO)
 from matpl_gb300 import nep as NP, structures  # noqa: E402
 from oracle import ref_build  # noqa: E402
 
-REF = os.environ.get("MATPL_REF", "/root/reference")
+from oracle.refpath import reference_root  # noqa: E402
+
+REF = reference_root()
 
 
 def sha(a: np.ndarray) -> str:

@@ -1,6 +1,7 @@
 """Generate the golden fixtures of the NEP training derivatives from MatPL's own NEP code.
 
-Runs only where the MatPL source tree is mounted (path in MATPL_REF, default /root/reference);
+Runs only where the MatPL source tree is mounted (path in MATPL_REF, default: a
+``reference`` directory beside the repository root);
 the committed ``nep_train_*.npz`` files are what the tests read.  For two of the NEP cases
 (``nep_q4_tri2``: four elements, two triclinic frames, l_max 4/2/1; ``nep_hfo_l4``: two
 elements, 3-body only) it rebuilds the inputs exactly as ``make_nep_golden.py`` does (the

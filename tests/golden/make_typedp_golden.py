@@ -1,6 +1,7 @@
 """Generate the golden fixture of the type-embedding DP model from MatPL's own code.
 
-Runs only where the MatPL source tree is mounted (path in MATPL_REF, default /root/reference);
+Runs only where the MatPL source tree is mounted (path in MATPL_REF, default: a
+``reference`` directory beside the repository root);
 the committed ``typedp_hfo48.npz`` is what the tests read.  On the ``hfo48_f64`` structure
 (HfO2, 48 atoms; its davg / dstd) it builds the reference ``src.model.dp_dp_typ_emb.TypeDP``
 (CPU branch) with seeded parameters (``matpl_gb300.typedp.init_type_params``) and three physical
@@ -26,7 +27,9 @@ from matpl_gb300.typedp import init_type_params  # noqa: E402
 from make_golden import ref_config  # noqa: E402
 from oracle import neigh  # noqa: E402
 
-REF = os.environ.get("MATPL_REF", "/root/reference")
+from oracle.refpath import reference_root  # noqa: E402
+
+REF = reference_root()
 PROPS = ["atomic_number", "atom_mass", "atom_radius"]
 SEED_W = 611
 

@@ -130,6 +130,17 @@ def test_empty_sizes_and_null_pointers_are_handled_on_the_host():
     assert n.value == 0
 
 
+def test_noalloc_neighbor_search_refuses_oversize_requests_on_the_host():
+    """The allocation-free search has a fixed scratch array; a request that needs more is
+    refused before any CUDA call (200,000 atoms need far more than its 4 MiB)."""
+    lib = _lib.load()
+    rct = (ctypes.c_double * 1)(6.0)
+    st = lib.matpl_neighbor_build_noalloc(1, 200000, 1, 100, 6.0, rct, None, None, None,
+                                          _lib.MATPL_F64, None, None, None, None, None)
+    assert st == 3   # MATPL_ERR_WORKSPACE
+    assert b"4 MiB" in lib.matpl_last_error()
+
+
 def test_workspace_queries():
     lib = _lib.load()
     assert lib.matpl_neighbor_workspace_bytes(1, 32000) > 32000 * 24

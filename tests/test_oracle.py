@@ -107,3 +107,18 @@ def test_compress_oracle_matches_reference_cpu_formula():
     Gp, _ = dp_oracle.compress_oracle(f2 + h, c)
     Gm, _ = dp_oracle.compress_oracle(f2 - h, c)
     assert torch.allclose((Gp - Gm) / (2 * h), dG, rtol=1e-6, atol=1e-6)
+
+
+def test_chunked_oracle_equals_the_whole_evaluation(golden_case):
+    """dp_eval_chunked (the oracle the 32k-atom parity test uses) = dp_eval on the pinned
+    600-atom Li/Si case, with chunks that split both element groups."""
+    c = golden_case("lisi600_f64")
+    args = (c.cfg, c.params, c.davg, c.dstd, torch.tensor(c.list_neigh), torch.tensor(c.types),
+            torch.tensor(c.cfg.atom_type), torch.tensor(c.image_dr))
+    whole = dp_oracle.dp_eval(*args, 0, virial_convention="gpu")
+    part = dp_oracle.dp_eval_chunked(*args, chunk=97)
+    assert abs(part["Etot"].item() - whole["Etot"].item()) <= 1e-12 * abs(whole["Etot"].item())
+    for k in ("Ei_atom", "Force", "Virial"):
+        scale = whole[k].abs().max().item()
+        assert (part[k] - whole[k].detach()).abs().max().item() <= 1e-12 * scale, k
+    np.testing.assert_allclose(part["Etot"].numpy().ravel(), c.g["Etot"].ravel(), rtol=1e-10)
