@@ -1068,9 +1068,11 @@ def run_ours(args, ws, rank, local):
         out_dt = model.dtype
 
         def step(frac, lat):
-            l, r = ops.find_neighbore(types_d, frac, lat, 2, M_NEIGH, RC, RC, out_dtype=out_dt,
-                                      check_overflow=False)
-            return model.evaluate(l, tm32, present, r, 0)
+            # the fused step's lists: occupied slots + block lengths (no zero fill)
+            l, r, c = ops.find_neighbore(types_d, frac, lat, 2, M_NEIGH, RC, RC,
+                                         out_dtype=out_dt, check_overflow=False,
+                                         occupied_only=True)
+            return model.evaluate(l, tm32, present, r, 0, num_neigh=c)
         return model, step
 
     def accuracy(model, step):
@@ -1110,12 +1112,12 @@ def run_ours(args, ws, rank, local):
     tuning = None
     if prec.startswith("mixed") and not args.no_tune:
         from matpl_gb300 import autotune
-        l0, r0 = ops.find_neighbore(types_d, frac_d, lat_d, 2, M_NEIGH, RC, RC,
-                                    out_dtype=model.dtype)
-        tuning = autotune.tune_dp_mixed(model, l0, tm32, present, r0)
+        l0, r0, c0 = ops.find_neighbore(types_d, frac_d, lat_d, 2, M_NEIGH, RC, RC,
+                                        out_dtype=model.dtype, occupied_only=True)
+        tuning = autotune.tune_dp_mixed(model, l0, tm32, present, r0, num_neigh=c0)
         tuning["table"] = [(t["group_atoms"], t["ctas_per_sm"], round(t["ms"], 4))
                            for t in tuning["table"]]
-        del l0, r0
+        del l0, r0, c0
     acc = accuracy(model, step)
     ms, prof, clocks = timed(step, args.steps, args.warmup, True)
     value = replica_value(NATOMS, ms, ws)
@@ -1191,8 +1193,8 @@ def run_ours(args, ws, rank, local):
         flops["dp_embed_fwd" + suf] = FLOP_EMB_FWD_PAIR * n_pairs
         flops["dp_fit" + suf] = FLOP_FIT_ATOM * NATOMS
     # HBM-bound kernels: algorithmic bytes per launch (reads positions + types, writes the
-    # reference-layout list_neigh [N,S] int32 and ImageDR [N,S,4])
-    hbm_bytes = {"nb_search": NATOMS * (24 + 4 + S * (4 + 4 * es))}
+    # block lengths and the occupied slots of list_neigh (int32) and ImageDR (4 values))
+    hbm_bytes = {"nb_search": NATOMS * (24 + 4 + 4 * 2) + n_pairs * (4 + 4 * es)}
     peaks = {}
     pk_path = os.path.join(HERE, "MEASURED_PEAKS.json")
     if os.path.exists(pk_path):

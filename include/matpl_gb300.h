@@ -131,6 +131,18 @@ int matpl_neighbor_build(int batch, int natoms, int ntypes, int m_neigh, double 
                          void *image_dr, int32_t *num_neigh, int32_t *err_dev,
                          void *workspace, size_t workspace_bytes, void *stream);
 
+/* Occupied-slot form of matpl_neighbor_build (no counterpart in the reference, which always
+ * zero-fills): the same slots, but only the occupied ones (t*m + k for k < num_neigh[t]) are
+ * written and the empty ones are left as they were, which saves most of the list's write
+ * traffic.  num_neigh is required; readers take the block lengths from it
+ * (matpl_dp_eval_occupied). */
+int matpl_neighbor_build_occupied(int batch, int natoms, int ntypes, int m_neigh, double Rc_M,
+                                  const double *Rc_type, const int32_t *type_map,
+                                  const double *lattice, const double *frac_pos, int out_dtype,
+                                  int32_t *list_neigh, void *image_dr, int32_t *num_neigh,
+                                  int32_t *err_dev, void *workspace, size_t workspace_bytes,
+                                  void *stream);
+
 /* Allocation-free variant of matpl_neighbor_build.  It has no counterpart in the reference.
  * For hosts that cannot give this library device memory (an MD engine's per-step force
  * callback that owns all device memory through its own pool, or a C / Fortran host without a
@@ -215,6 +227,25 @@ int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, int natoms,
  * them (same per-atom arithmetic); matpl_gb300/autotune.py picks them by timing. */
 int matpl_dp_set_tuning(int mixed_group_atoms, int mixed_ctas_per_sm);
 int matpl_dp_get_tuning(int *mixed_group_atoms, int *mixed_ctas_per_sm);
+
+/* Occupied-slot form of matpl_dp_eval for lists from matpl_neighbor_build_occupied (this
+ * project's fused path; the reference always hands the padded list).  num_neigh [B,N,ntypes]
+ * int32 gives each type block's length: slots t*m + k with k < num_neigh[t] are read, the
+ * rest of list_neigh / image_dr is never touched (it may hold anything).  Same outputs and
+ * arithmetic as matpl_dp_eval on the zero-filled list. */
+int matpl_dp_eval_occupied(int dtype, const matpl_dp_model *model, int batch, int natoms,
+                           int nslots, int nghost, const int32_t *list_neigh,
+                           const int32_t *num_neigh, const void *image_dr,
+                           const int32_t *type_map, void *Ei, double *Etot, void *force,
+                           double *virial, void *workspace, size_t workspace_bytes,
+                           void *stream);
+
+/* Bound of every completion wait of the MATPL_MIXED* embedding kernels (this project's own
+ * hook; 0 restores the default of 2^24 polls).  A bound below 64 makes each wait a handful of
+ * non-suspending checks, which is how the tests make a wait give up on purpose: the kernel
+ * then records MATPL_KERR_TIMEOUT in the model's err_dev, stops issuing tensor-core work,
+ * drains what it issued, frees its tensor memory and returns (the outputs are invalid). */
+int matpl_dp_set_wait_limit(int polls);
 
 /* ------------------------------------------------------------------------------------
  * Force-loss training: the embedding-net part of the second-order parameter gradient.

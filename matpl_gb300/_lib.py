@@ -60,11 +60,16 @@ SIGNATURES = {
                                   _vp, _vp, _sz, _vp]),
     "matpl_neighbor_build_noalloc": (_i, [_i, _i, _i, _i, _d, _vp, _vp, _vp, _vp, _i, _vp, _vp,
                                           _vp, _vp, _vp]),
+    "matpl_neighbor_build_occupied": (_i, [_i, _i, _i, _i, _d, _vp, _vp, _vp, _vp, _i, _vp, _vp,
+                                           _vp, _vp, _vp, _sz, _vp]),
     "matpl_env_mat": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _d, _d, _vp, _vp, _vp]),
     "matpl_dp_param_count": (_sz, [_i]),
     "matpl_dp_workspace_bytes": (_sz, [_i, _i, _i]),
     "matpl_dp_eval": (_i, [_i, _c.POINTER(MatplDpModel), _i, _i, _i, _i, _vp, _vp, _vp, _vp,
                            _vp, _vp, _vp, _vp, _sz, _vp]),
+    "matpl_dp_eval_occupied": (_i, [_i, _c.POINTER(MatplDpModel), _i, _i, _i, _i, _vp, _vp,
+                                    _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "matpl_dp_set_wait_limit": (_i, [_i]),
     "matpl_dp_set_tuning": (_i, [_i, _i]),
     "matpl_dp_get_tuning": (_i, [_c.POINTER(_i), _c.POINTER(_i)]),
     "matpl_dp_dual_forward": (_i, [_i, _c.POINTER(MatplDpModel), _i, _i, _i, _vp, _vp, _vp,

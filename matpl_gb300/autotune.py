@@ -42,11 +42,13 @@ def _key(model, list_neigh, present) -> str:
 def tune_dp_mixed(model, list_neigh: torch.Tensor, type_map: torch.Tensor, present: Sequence[int],
                   image_dr: torch.Tensor, groups: Iterable[int] = DEFAULT_GROUPS,
                   ctas: Iterable[int] = DEFAULT_CTAS, reps: int = 5,
-                  cache_path: Optional[str] = None) -> Dict:
+                  cache_path: Optional[str] = None,
+                  num_neigh: Optional[torch.Tensor] = None) -> Dict:
     """Time ``model.evaluate`` (a ``matpl_gb300.dp.DP`` in a mixed form) for every
     (group_atoms, ctas_per_sm) candidate, keep the fastest set and return the table.
     ``cache_path``: optional JSON file of earlier results keyed by precision, batch shape and
-    types; a hit sets the stored choice without timing."""
+    types; a hit sets the stored choice without timing.  ``num_neigh``: block lengths of an
+    occupied-slot list (``find_neighbore(..., occupied_only=True)``)."""
     if not model.precision.startswith("mixed"):
         raise _lib.MatplError("only the mixed forms have tunable tiles")
     key = _key(model, list_neigh, present)
@@ -64,11 +66,11 @@ def tune_dp_mixed(model, list_neigh: torch.Tensor, type_map: torch.Tensor, prese
         for c in ctas:
             set_tuning(g, c)
             for _ in range(2):
-                r = model.evaluate(list_neigh, type_map, present, image_dr, 0)
+                r = model.evaluate(list_neigh, type_map, present, image_dr, 0, num_neigh=num_neigh)
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             for _ in range(reps):
-                r = model.evaluate(list_neigh, type_map, present, image_dr, 0)
+                r = model.evaluate(list_neigh, type_map, present, image_dr, 0, num_neigh=num_neigh)
             e1.record()
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1) / reps

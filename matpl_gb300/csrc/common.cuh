@@ -70,7 +70,7 @@ struct ProfScope {
     }
 };
 
-inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+__host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 // Streaming multiprocessors of the current device (queried once per device; grids are sized
 // in multiples of it).

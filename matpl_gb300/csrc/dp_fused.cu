@@ -32,12 +32,13 @@ int launch_fit_tc(bool fast, const float *A, const int32_t *type_map, const floa
                   unsigned char *tiles, float *Ei, float *dA, int32_t *err, int batch, int natoms,
                   int ntypes, int present_mask, cudaStream_t s);
 template <int SPLIT, bool FAST>
-int launch_mixed_embed(bool backward, const int32_t *list_neigh, const float *idr,
-                       const int32_t *type_map, const float *params, const unsigned char *wtiles,
-                       const float *davg, const float *dstd, const float *pad_or_dA,
-                       float *A_or_force, double *atom_vir, int32_t *err, int batch, int natoms,
-                       int nslots, int nghost, int ntypes, int m, int present_mask, double rmin,
-                       double rmax, double inv_mT, cudaStream_t s);
+int launch_mixed_embed(bool backward, const int32_t *list_neigh, const int32_t *num_neigh,
+                       const float *idr, const int32_t *type_map, const float *params,
+                       const unsigned char *wtiles, const float *davg, const float *dstd,
+                       const float *pad_or_dA, float *A_or_force, double *atom_vir, int32_t *err,
+                       int batch, int natoms, int nslots, int nghost, int ntypes, int m,
+                       int present_mask, double rmin, double rmax, double inv_mT,
+                       cudaStream_t s);
 
 namespace {
 
@@ -55,6 +56,7 @@ struct EvalParams {
     int crows, cnc;
     double cdx, cdx10, csmin, csmax;
     int *err;
+    const int32_t *num_neigh;   // [B*N][ntypes] block lengths (occupied-slot lists), or NULL
 };
 
 // --------------------------------------------------------------------------- compressed model
@@ -153,9 +155,21 @@ __global__ void dp_pad(const T *__restrict__ params, const T *__restrict__ davg,
 
 // Build the warp's list of occupied slots of one centre atom (ascending slot order) and
 // return its length.  Slots of image types that are absent are skipped.
-__device__ __forceinline__ int scan_slots(const int32_t *__restrict__ ln, int S, int m,
-                                          int present_mask, int *list, int lane) {
+__device__ __forceinline__ int scan_slots(const int32_t *__restrict__ ln,
+                                          const int32_t *__restrict__ counts, int nt, int S,
+                                          int m, int present_mask, int *list, int lane) {
     int cnt = 0;
+    if (counts) {            // block lengths given: the occupied slots are each block's prefix
+        for (int tj = 0; tj < nt; ++tj) {
+            if (!((present_mask >> tj) & 1)) continue;
+            int c = counts[tj];
+            c = c < 0 ? 0 : (c > m ? m : c);
+            for (int k = lane; k < c; k += 32) list[cnt + k] = tj * m + k;
+            cnt += c;
+        }
+        __syncwarp();
+        return cnt;
+    }
     for (int s0 = 0; s0 < S; s0 += 32) {
         const int s = s0 + lane;
         const int v = s < S ? ln[s] : 0;
@@ -212,7 +226,8 @@ dp_embed_fwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
             for (int e = lane; e < NA; e += 32) Arow[e] = T(0);
             continue;
         }
-        const int cnt = scan_slots(list_neigh + t * S, S, P.m, P.present_mask, list, lane);
+        const int cnt = scan_slots(list_neigh + t * S, P.num_neigh ? P.num_neigh + t * P.ntypes : nullptr,
+                                       P.ntypes, S, P.m, P.present_mask, list, lane);
         T acc[4] = {T(0), T(0), T(0), T(0)};
         const T *avg = davg + 4 * ti;
         const T *sd = dstd + 4 * ti;
@@ -542,7 +557,8 @@ dp_embed_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
 #pragma unroll
         for (int q = 0; q < 9; ++q) vir[q] = 0.0;
         if (ti >= 0 && ti < P.ntypes && ((P.present_mask >> ti) & 1)) {
-            const int cnt = scan_slots(list_neigh + t * S, S, P.m, P.present_mask, list, lane);
+            const int cnt = scan_slots(list_neigh + t * S, P.num_neigh ? P.num_neigh + t * P.ntypes : nullptr,
+                                       P.ntypes, S, P.m, P.present_mask, list, lane);
             for (int e = lane; e < NA; e += 32) dAs[e] = dAin[t * NA + e] * (T)P.inv_mT;
             __syncwarp();
             const T *avg = davg + 4 * ti;
@@ -727,15 +743,15 @@ int run_mixed(int mode, bool backward, const EvalParams &P, const int32_t *ln, c
     float *fo = (float *)out;
     switch (mode) {
         case MATPL_MIXED:
-            return launch_mixed_embed<3, true>(backward, ln, fi, tm, fp, wt, fa, fs, fin, fo, avir, err,
+            return launch_mixed_embed<3, true>(backward, ln, P.num_neigh, fi, tm, fp, wt, fa, fs, fin, fo, avir, err,
                                                P.batch, P.natoms, P.nslots, P.nghost, P.ntypes,
                                                P.m, P.present_mask, P.rmin, P.rmax, P.inv_mT, s);
         case MATPL_MIXED_FAST:
-            return launch_mixed_embed<1, true>(backward, ln, fi, tm, fp, wt, fa, fs, fin, fo, avir, err,
+            return launch_mixed_embed<1, true>(backward, ln, P.num_neigh, fi, tm, fp, wt, fa, fs, fin, fo, avir, err,
                                                P.batch, P.natoms, P.nslots, P.nghost, P.ntypes,
                                                P.m, P.present_mask, P.rmin, P.rmax, P.inv_mT, s);
         default:
-            return launch_mixed_embed<3, false>(backward, ln, fi, tm, fp, wt, fa, fs, fin, fo, avir,
+            return launch_mixed_embed<3, false>(backward, ln, P.num_neigh, fi, tm, fp, wt, fa, fs, fin, fo, avir,
                                                 err, P.batch, P.natoms, P.nslots, P.nghost,
                                                 P.ntypes, P.m, P.present_mask, P.rmin, P.rmax,
                                                 P.inv_mT, s);
@@ -840,11 +856,11 @@ extern "C" size_t matpl_dp_workspace_bytes(int dtype, int batch, int natoms) {
     return dp_layout(es, batch < 0 ? 0 : batch, natoms < 0 ? 0 : natoms, 16).total;
 }
 
-extern "C" int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, int natoms,
-                             int nslots, int nghost, const int32_t *list_neigh,
-                             const void *image_dr, const int32_t *type_map, void *Ei,
-                             double *Etot, void *force, double *virial, void *workspace,
-                             size_t workspace_bytes, void *stream) {
+static int dp_eval(int dtype, const matpl_dp_model *model, int batch, int natoms, int nslots,
+                   int nghost, const int32_t *list_neigh, const int32_t *num_neigh,
+                   const void *image_dr, const int32_t *type_map, void *Ei, double *Etot,
+                   void *force, double *virial, void *workspace, size_t workspace_bytes,
+                   void *stream) {
     MATPL_REQUIRE(model != nullptr, MATPL_ERR_INVALID, "model is NULL");
     MATPL_REQUIRE(dtype >= MATPL_F32 && dtype <= MATPL_MIXED_TANHF, MATPL_ERR_DTYPE,
                   "matpl_dp_eval: unknown dtype / compute form");
@@ -883,6 +899,7 @@ extern "C" int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, 
     P.csmin = model->ctab_smin;
     P.csmax = model->ctab_smax;
     P.err = model->err_dev;
+    P.num_neigh = num_neigh;
     if (model->ctable) {
         MATPL_REQUIRE((model->ctab_order == 3 || model->ctab_order == 5) &&
                           model->ctab_rows >= 1 && model->ctab_dx > 0,
@@ -913,4 +930,25 @@ extern "C" int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, 
     return launch_eval<float>(dtype, model, P, list_neigh, (const float *)image_dr, type_map,
                               (float *)Ei, Etot, (float *)force, virial, (char *)workspace, lay,
                               s);
+}
+
+extern "C" int matpl_dp_eval(int dtype, const matpl_dp_model *model, int batch, int natoms,
+                             int nslots, int nghost, const int32_t *list_neigh,
+                             const void *image_dr, const int32_t *type_map, void *Ei,
+                             double *Etot, void *force, double *virial, void *workspace,
+                             size_t workspace_bytes, void *stream) {
+    return dp_eval(dtype, model, batch, natoms, nslots, nghost, list_neigh, nullptr, image_dr,
+                   type_map, Ei, Etot, force, virial, workspace, workspace_bytes, stream);
+}
+
+extern "C" int matpl_dp_eval_occupied(int dtype, const matpl_dp_model *model, int batch,
+                                      int natoms, int nslots, int nghost,
+                                      const int32_t *list_neigh, const int32_t *num_neigh,
+                                      const void *image_dr, const int32_t *type_map, void *Ei,
+                                      double *Etot, void *force, double *virial,
+                                      void *workspace, size_t workspace_bytes, void *stream) {
+    MATPL_REQUIRE(num_neigh != nullptr || (long long)batch * natoms == 0, MATPL_ERR_INVALID,
+                  "matpl_dp_eval_occupied: num_neigh is required (it gives the block lengths)");
+    return dp_eval(dtype, model, batch, natoms, nslots, nghost, list_neigh, num_neigh, image_dr,
+                   type_map, Ei, Etot, force, virial, workspace, workspace_bytes, stream);
 }

@@ -1,22 +1,30 @@
 // Mixed-precision DP se_e2_a embedding stage on the 5th-generation tensor cores.
 //
 // Same math as dp_fused.cu's dp_embed_fwd / dp_embed_bwd (src/model/dp_dp.py:217-415 and the
-// autograd adjoint of it), reorganised for tcgen05:
+// autograd adjoint of it), organised around tcgen05 MMAs:
 //
 //   * A CTA (128 threads) takes a group of up to 16 centre atoms, builds their occupied-slot
 //     list in shared memory ordered by embedding net (t_i, t_j), then walks it in tiles of
-//     128 pair rows: thread r owns row r.
+//     128 pair rows: thread r owns row r (the M row of every MMA of the tile).
 //   * Layer 1 (1 -> 25, rank one) and every tanh / residual stay on the SIMT cores in FP32.
 //   * Layers 2 and 3 (25 x 25, padded to 32 x 32) run as tcgen05.mma kind::f16 with BF16
-//     operands staged in shared memory (K-major, no swizzle) and FP32 accumulators in TMEM
-//     (32 columns); thread r reads row r back with tcgen05.ld.32x32b.  SPLIT = 3 keeps FP32-
-//     level accuracy with hi/lo BF16 halves (x_h W_h + x_h W_l + x_l W_h).
-//   * Forward: A[4][25] per atom = sum over its rows of R^T G (rows of one atom are
-//     contiguous in a tile; one task per (atom segment, A entry)), + empty-slot term, / (m T).
-//   * Backward: recomputes layers 1-3, back-propagates dE/dA through the two transposed
-//     GEMMs (again tcgen05), contracts with Ri_d, scatters F_j, and reduces F_i and the
-//     per-atom virial (FP64) per atom.
-// Every mbarrier wait is bounded; a timeout sets MATPL_KERR_TIMEOUT in err_dev.
+//     operands in shared memory (K-major, no swizzle) and FP32 accumulators in TMEM; the layer
+//     biases ride in the MMA (activation column 25 holds 1, weight row 25 holds the bias).
+//     SPLIT = 3 keeps FP32-level accuracy with hi / lo BF16 halves (x_h W_h + x_h W_l + x_l W_h).
+//   * Forward descriptor contraction A[a][c][p] = sum over the atom's rows of R[c] G[p]
+//     (dp_dp.py:344-415) runs on the tensor cores too: the G tile the threads write row by row
+//     is read as an MN-major B operand whose K index is the pair row, against an A operand
+//     that holds, in column r, row r's environment row at M = 8 a + 2 c + h (h = BF16 hi / lo
+//     half), so one accumulator D[128 x 32] in TMEM collects every atom of the group over all
+//     its tiles and nets.
+//   * Backward: recomputes layers 1-3, forms dE/dR and dE/dG from dE/dA on the SIMT cores,
+//     back-propagates through the two transposed layer GEMMs (tcgen05), contracts with Ri_d,
+//     scatters F_j, and reduces each atom's F_i and virial with one more MMA: a one-hot A
+//     operand (column r = atom of row r) against the per-row (f, f x r) values, accumulated in
+//     TMEM over the group.
+// Every mbarrier wait is bounded.  A wait that gives up sets MATPL_KERR_TIMEOUT; the CTA then
+// issues no further MMA and no further TMEM load, drains what it already issued (bounded
+// again), frees its TMEM and returns.
 #include <algorithm>
 #include <atomic>
 #include "common.cuh"
@@ -30,75 +38,74 @@ using namespace dp;
 constexpr int TM = 128;                 // pair rows per tile = threads per CTA
 constexpr int GAMAX = 16;               // centre atoms per group
 constexpr int KP = 32;                  // padded embedding width
+constexpr int ONE = E;                  // activation column that carries the bias (value 1)
 constexpr int XKS = TM / 8 * 128;       // K-chunk stride of an activation tile (2048 B)
 constexpr int WKS = KP / 8 * 128;       // K-chunk stride of a weight tile (512 B)
 constexpr int XT = TM * KP * 2;         // activation tile bytes (8 KB)
 constexpr int WT = KP * KP * 2;         // weight tile bytes (2 KB)
-constexpr int STG = 29;                 // staging row stride (floats, odd: conflict-free)
-constexpr int kWaitLimit = 1 << 24;
+constexpr int RT = 128 * TM * 2;        // contraction A operand: 128 (M) x 128 (K) bf16 (32 KB)
+constexpr int OLBO = 128;               // MN-major operands: K-group stride
+constexpr int OSBO = TM / 8 * 128;      //                    MN-group stride (2048 B)
+constexpr int QN = 16;                  // per-row reduction values (f: 3, f x r: 9, 4 zero)
+constexpr int QT = QN * TM * 2;         // reduction B operand bytes (4 KB)
+constexpr int VW = 28;                  // per-net vector stride in floats (25 padded to 7 float4)
 constexpr int kMaxTypes = 16;
-constexpr int VEC = 6 * E;              // per-net FP32 vectors: W0 b0 b1 dt1 b2 dt2
+constexpr int kDrainPolls = 1 << 24;    // bound of the waits that drain MMAs before exit
+
+// TMEM columns: [0, 32) layer accumulator; forward: [32, 64) descriptor accumulator;
+// backward: [32, 64) layer-2 tanh stash, [64, 80) F_i / virial accumulator.
+constexpr uint32_t TCOL_A = 32, TCOL_STASH = 32, TCOL_RED = 64;
 
 struct MixParams {
     int batch, natoms, nslots, nghost, ntypes, m, present_mask, ga;
     float rmin, rmax, inv_mT;
+    int wait_polls;                      // bound of every completion wait
+    const int32_t *num_neigh;            // [B*N][ntypes] block lengths, or NULL (scan the list)
 };
 
 struct MixSmem {
-    unsigned char *wt;     // 8 weight tiles of the current net: fw1 h/l, fw2 h/l, bw2 h/l, bw1 h/l
+    unsigned char *wt;     // weight tiles of the current net: fw1 h/l, fw2 h/l (, bw2 h/l, bw1 h/l)
     unsigned char *xh, *xl;
-    float *stage;          // [TM][STG], aliases xh/xl (free once a tile's last MMA completed)
-    int *seg;              // [GAMAX + 1] segment starts of the current tile, seg_atom follows
-    int *seg_atom;         // [GAMAX]
-    float *vec;            // [nnet][VEC]
-    int *list;             // [ga * S]
+    unsigned char *rop;    // fwd: contraction A operand; bwd: one-hot A operand
+    unsigned char *qh, *ql;   // bwd: per-row reduction values (MN-major B operand)
+    float *vec;            // [4][VW] of the current net: W0, b0, dt1, dt2
+    float *dA;             // bwd: [GAMAX][E] float4 (c fastest) of dE/dA * k
+    uint16_t *list;        // [ga * S] rows: atom << 12 | slot
     int *cnt;              // [GAMAX][kMaxTypes]
     int *off;              // [GAMAX][kMaxTypes]
     int *net_start;        // [kMaxTypes*kMaxTypes + 1]
     int *tia;              // [GAMAX] model type of each group atom (-1: skipped)
-    float *acc;            // fwd: A [GAMAX][NA]; bwd: dA [GAMAX][NA]
-    float *fi;             // bwd: [GAMAX][3]
-    double *vir;           // bwd: [GAMAX][9]
 };
 
-__host__ __device__ inline size_t mix_smem_bytes(int nnet, int S, int ga) {
+__host__ __device__ inline size_t mix_smem_bytes(bool bwd, int S, int ga) {
     size_t o = 0;
-    o += 8 * WT;                                  // weight tiles
-    o += 2 * XT;                                  // activation tiles (stage aliases them)
-    o += sizeof(int) * (2 * GAMAX + 1);
-    o = (o + 15) / 16 * 16;
-    o += sizeof(float) * nnet * VEC;
-    o += sizeof(int) * (size_t)ga * S;
-    o += sizeof(int) * 2 * GAMAX * kMaxTypes + sizeof(int) * (kMaxTypes * kMaxTypes + 1);
-    o += sizeof(int) * GAMAX;
-    o = (o + 15) / 16 * 16;
-    o += sizeof(float) * GAMAX * NA + sizeof(float) * GAMAX * 4;
-    o = (o + 15) / 16 * 16;
-    o += sizeof(double) * GAMAX * 9;
-    return o + 64;
+    o += (bwd ? 8 : 4) * WT;
+    o += 2 * XT + RT;
+    if (bwd) o += 2 * QT;
+    o += sizeof(float) * 4 * VW;
+    if (bwd) o += sizeof(float) * GAMAX * E * 4;
+    o += align_up(sizeof(uint16_t) * (size_t)ga * S, 16);
+    o += sizeof(int) * (2 * GAMAX * kMaxTypes + kMaxTypes * kMaxTypes + 1 + GAMAX);
+    return o + 128;
 }
 
-__device__ MixSmem carve(unsigned char *base, int nnet, int S, int ga) {
+__device__ MixSmem carve(unsigned char *base, bool bwd, int S, int ga) {
     MixSmem m;
     size_t o = 0;
-    m.wt = base + o; o += 8 * WT;
+    m.wt = base + o; o += (bwd ? 8 : 4) * WT;
     m.xh = base + o; o += XT;
     m.xl = base + o; o += XT;
-    m.stage = reinterpret_cast<float *>(m.xh);
-    m.seg = reinterpret_cast<int *>(base + o); o += sizeof(int) * (GAMAX + 1);
-    m.seg_atom = reinterpret_cast<int *>(base + o); o += sizeof(int) * GAMAX;
-    o = (o + 15) / 16 * 16;
-    m.vec = reinterpret_cast<float *>(base + o); o += sizeof(float) * nnet * VEC;
-    m.list = reinterpret_cast<int *>(base + o); o += sizeof(int) * (size_t)ga * S;
+    m.rop = base + o; o += RT;
+    m.qh = m.ql = nullptr;
+    if (bwd) { m.qh = base + o; o += QT; m.ql = base + o; o += QT; }
+    m.vec = reinterpret_cast<float *>(base + o); o += sizeof(float) * 4 * VW;
+    m.dA = nullptr;
+    if (bwd) { m.dA = reinterpret_cast<float *>(base + o); o += sizeof(float) * GAMAX * E * 4; }
+    m.list = reinterpret_cast<uint16_t *>(base + o); o += align_up(sizeof(uint16_t) * (size_t)ga * S, 16);
     m.cnt = reinterpret_cast<int *>(base + o); o += sizeof(int) * GAMAX * kMaxTypes;
     m.off = reinterpret_cast<int *>(base + o); o += sizeof(int) * GAMAX * kMaxTypes;
     m.net_start = reinterpret_cast<int *>(base + o); o += sizeof(int) * (kMaxTypes * kMaxTypes + 1);
-    m.tia = reinterpret_cast<int *>(base + o); o += sizeof(int) * GAMAX;
-    o = (o + 15) / 16 * 16;
-    m.acc = reinterpret_cast<float *>(base + o); o += sizeof(float) * GAMAX * NA;
-    m.fi = reinterpret_cast<float *>(base + o); o += sizeof(float) * GAMAX * 4;
-    o = (o + 15) / 16 * 16;
-    m.vir = reinterpret_cast<double *>(base + o);
+    m.tia = reinterpret_cast<int *>(base + o);
     return m;
 }
 
@@ -108,7 +115,7 @@ __device__ __forceinline__ float act(float x) {
     return tanhf(x);
 }
 
-// FP32 environment row (dp_dp.py:241-297) and the Ri_d contraction, single precision.
+// FP32 switching function of dp_dp.py:241-266 and its r-derivative.
 __device__ __forceinline__ void switch_f(float R, float rmin, float rmax, float &s, float &ds) {
     s = 0.f;
     ds = 0.f;
@@ -125,40 +132,10 @@ __device__ __forceinline__ void switch_f(float R, float rmin, float rmax, float 
     }
 }
 
-__device__ __forceinline__ void rid_contract_f(float R, float x, float y, float z, float rmin,
-                                               float rmax, const float *sd, const float g[4],
-                                               float f[3]) {
-    float s, ds;
-    switch_f(R, rmin, rmax, s, ds);
-    f[0] = f[1] = f[2] = 0.f;
-    if (!(fabsf(R) > 1e-5f)) return;
-    const float inv = 1.f / R;
-    const float common = (ds - s * inv) * inv * inv;
-    const float xyz[3] = {x, y, z};
-    const float g0 = g[0] / sd[0], g1 = g[1] / sd[1], g2 = g[2] / sd[2], g3 = g[3] / sd[3];
-    const float cg = common * (g1 * x + g2 * y + g3 * z);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const float gd = (a == 0 ? g1 : (a == 1 ? g2 : g3)) * s * inv;
-        f[a] = -(g0 * ds * xyz[a] * inv + cg * xyz[a] + gd);
-    }
-}
-
-// Stage the per-net FP32 vectors of every net (W0, b0, b1, dt1, b2, dt2).  Entries of dt are
-// used as multipliers, so nothing is divided in the per-row code.
-__device__ void stage_vectors(const float *__restrict__ params, float *vec, int nnet) {
-    for (int q = threadIdx.x; q < nnet * VEC; q += blockDim.x) {
-        const int k = q / VEC, r = q - k * VEC;
-        const int part = r / E, o = r - part * E;
-        const float *w = params + (long long)k * EmbOff::SIZE;
-        const int src[6] = {EmbOff::W0, EmbOff::B0, EmbOff::B1, EmbOff::DT1, EmbOff::B2, EmbOff::DT2};
-        vec[q] = w[src[part] + o];
-    }
-}
-
 // The 8 BF16 weight tiles (hi / lo) of every net, prepared once per call in global memory:
-// fw1[n=o][k=i] = W1[i][o], fw2 likewise, bw2[n=i][k=o] = W2[i][o], bw1[n=i][k=o] = W1[i][o];
-// zero outside 25 x 25.  Layout [net][8][WT bytes].
+// fw1[n=o][k=i] = W1[i][o] with row k = 25 the bias b1[o], fw2 likewise with b2,
+// bw2[n=i][k=o] = W2[i][o], bw1[n=i][k=o] = W1[i][o] (row 25 zero); zero elsewhere.
+// Layout [net][8][WT bytes]: fw1 h, fw1 l, fw2 h, fw2 l, bw2 h, bw2 l, bw1 h, bw1 l.
 __global__ void prep_weight_tiles(const float *__restrict__ params, unsigned char *__restrict__ out,
                                   int nnet) {
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nnet * 4 * KP * KP;
@@ -175,6 +152,8 @@ __global__ void prep_weight_tiles(const float *__restrict__ params, unsigned cha
                 case 2: v = w[EmbOff::W2 + n * E + kk]; break;   // bw2: W2[i=n][o=kk]
                 default: v = w[EmbOff::W1 + n * E + kk]; break;  // bw1
             }
+        } else if (n < E && kk == ONE && mat < 2) {
+            v = w[(mat == 0 ? EmbOff::B1 : EmbOff::B2) + n];
         }
         const __nv_bfloat16 hi = __float2bfloat16_rn(v);
         const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
@@ -184,62 +163,48 @@ __global__ void prep_weight_tiles(const float *__restrict__ params, unsigned cha
     }
 }
 
-__device__ __forceinline__ void load_weight_tiles(const unsigned char *__restrict__ src, int k,
-                                                  unsigned char *wt) {
-    const uint4 *s4 = reinterpret_cast<const uint4 *>(src + (size_t)k * 8 * WT);
-    uint4 *d4 = reinterpret_cast<uint4 *>(wt);
-    for (int q = threadIdx.x; q < 8 * WT / 16; q += blockDim.x) d4[q] = __ldg(s4 + q);
+// Weight tiles (the first `ntiles` of the net's 8) and the per-net vectors of net k.
+__device__ __forceinline__ void load_net(const unsigned char *__restrict__ wsrc,
+                                         const float *__restrict__ params, int k, int ntiles,
+                                         const MixSmem &sm) {
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(wsrc + (size_t)k * 8 * WT);
+    uint4 *d4 = reinterpret_cast<uint4 *>(sm.wt);
+    for (int q = threadIdx.x; q < ntiles * WT / 16; q += blockDim.x) d4[q] = __ldg(s4 + q);
+    const float *w = params + (long long)k * EmbOff::SIZE;
+    for (int q = threadIdx.x; q < 4 * VW; q += blockDim.x) {
+        const int part = q / VW, o = q - part * VW;
+        const int src[4] = {EmbOff::W0, EmbOff::B0, EmbOff::DT1, EmbOff::DT2};
+        sm.vec[q] = o < E ? __ldg(w + src[part] + o) : 0.f;
+    }
 }
 
-// Segments of the current tile: maximal runs of one atom (rows are sorted by atom).  Every
-// thread flags whether its row starts a segment; a ballot per warp and a prefix over the four
-// warps place the segment starts.  Returns the segment count (includes __syncthreads).
-__device__ __forceinline__ int tile_segments(const MixSmem &sm, int r0, int nrows) {
-    __shared__ unsigned ballots[TM / 32];
-    const int r = threadIdx.x, lane = r & 31, warp = r >> 5;
-    int at = -1;
-    bool start = false;
-    if (r < nrows) {
-        at = sm.list[r0 + r] >> 16;
-        start = r == 0 || (sm.list[r0 + r - 1] >> 16) != at;
-    }
-    const unsigned bal = __ballot_sync(0xffffffffu, start);
-    if (lane == 0) ballots[warp] = bal;
-    __syncthreads();
-    int before = 0, total = 0;
-#pragma unroll
-    for (int w = 0; w < TM / 32; ++w) {
-        const int c = __popc(ballots[w]);
-        before += w < warp ? c : 0;
-        total += c;
-    }
-    if (start) {
-        const int idx = before + __popc(bal & ((1u << lane) - 1u));
-        sm.seg[idx] = r;
-        sm.seg_atom[idx] = at;
-    }
-    if (r == 0) sm.seg[total] = nrows;
-    __syncthreads();
-    return total;
-}
-
-// Write this thread's 32-wide row (hi and, for SPLIT 3, lo halves) into the activation tiles.
+// Write this thread's 32-wide row into the activation tiles (hi, and lo for SPLIT 3).
+// Column ONE gets `one` (1 for forward layers: the bias; 0 for the backward ones).
 template <int SPLIT>
-__device__ __forceinline__ void store_act_row(const MixSmem &sm, int r, const float v[KP]) {
+__device__ __forceinline__ void store_row(const MixSmem &sm, int r, const float v[E], float one) {
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-        float h[8], l[8];
+        float w[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            h[q] = v[8 * c + q];
-            if (SPLIT == 3) l[q] = v[8 * c + q] - __bfloat162float(__float2bfloat16_rn(v[8 * c + q]));
+            const int o = 8 * c + q;
+            w[q] = o < E ? v[o] : (o == ONE ? one : 0.f);
         }
-        tc::store_row8(sm.xh, r, c, XKS, h);
-        if (SPLIT == 3) tc::store_row8(sm.xl, r, c, XKS, l);
+        uint4 h, l;
+        tc::split8(w, h, SPLIT == 3 ? &l : nullptr);
+        const uint32_t off = tc::tile_off(r, 8 * c, XKS);
+        *reinterpret_cast<uint4 *>(sm.xh + off) = h;
+        if (SPLIT == 3) *reinterpret_cast<uint4 *>(sm.xl + off) = l;
     }
 }
 
-// D[128 x 32] = X W (weight tile pair `mat`), FP32 in TMEM; one thread issues.
+// Column-r chunk of an MN-major operand with K = pair row r: byte offset of the 16-byte chunk
+// holding M / N elements 8 g .. 8 g + 7.
+__device__ __forceinline__ uint32_t mn_chunk(int r, int g) {
+    return (uint32_t)((r & 7) * 16 + (r >> 3) * OLBO + g * OSBO);
+}
+
+// D[128 x 32] (+)= X W for the weight tile pair `mat`; one thread issues, then commits.
 template <int SPLIT>
 __device__ __forceinline__ void issue_layer(const MixSmem &sm, uint32_t tmem, int mat,
                                             uint64_t *mbar) {
@@ -262,26 +227,68 @@ __device__ __forceinline__ void issue_layer(const MixSmem &sm, uint32_t tmem, in
     tc::commit(mbar);
 }
 
-// Run one MMA layer: all rows staged -> issue -> wait -> every thread loads its row.
-template <int SPLIT>
-__device__ __forceinline__ void run_layer(const MixSmem &sm, uint32_t tmem, int mat,
-                                          uint64_t *mbar, uint32_t &phase, bool &ok,
-                                          float out[KP]) {
+// D[128 x N] (+)= Aop B over K = 128 pair rows, both operands MN-major; B is given as its hi
+// and (SPLIT 3) lo tiles.  `first`: the first product of the group starts the accumulator.
+template <int SPLIT, int N>
+__device__ __forceinline__ void issue_rows(uint32_t tmem, const unsigned char *aop,
+                                           const unsigned char *bh, const unsigned char *bl,
+                                           bool first, uint64_t *mbar) {
+    const uint32_t id = tc::idesc_bf16_mn(128, N, true, true);
+    const uint32_t a0 = tc::smem_u32(aop), h0 = tc::smem_u32(bh), l0 = tc::smem_u32(bl);
+#pragma unroll
+    for (int s = 0; s < TM / 16; ++s) {
+        const uint64_t ad = tc::desc_kmajor(a0 + s * 2 * OLBO, OLBO, OSBO);
+        tc::mma_bf16(tmem, ad, tc::desc_kmajor(h0 + s * 2 * OLBO, OLBO, OSBO), id,
+                     (first && s == 0) ? 0u : 1u);
+        if (SPLIT == 3)
+            tc::mma_bf16(tmem, ad, tc::desc_kmajor(l0 + s * 2 * OLBO, OLBO, OSBO), id, 1u);
+    }
+    tc::commit(mbar);
+}
+
+// Completion wait shared by all threads; `polls` below 64 selects plain polling (a test hook
+// that makes waits give up), otherwise the suspending try_wait.
+__device__ __forceinline__ bool wait_done(uint64_t *mbar, uint32_t parity, int polls) {
+    return polls < 64 ? tc::mbar_poll(mbar, parity, polls) : tc::mbar_wait(mbar, parity, polls);
+}
+
+// Barrier before an MMA issue: makes the generic-proxy shared stores visible to the tensor
+// cores and returns true (on every thread) when some thread has seen a wait give up.
+__device__ __forceinline__ bool pre_issue(bool ok) {
     tc::fence_proxy_async();
     tc::fence_before_sync();
-    __syncthreads();
+    const int bad = __syncthreads_or(!ok);
     tc::fence_after_sync();
-    if (threadIdx.x == 0) issue_layer<SPLIT>(sm, tmem, mat, mbar);
-    ok &= tc::mbar_wait(mbar, phase, kWaitLimit);
-    phase ^= 1u;
+    return bad != 0;
+}
+
+// Wait for one commit of `mbar`; on success flips the phase.  The result is made uniform
+// across the warp (tcgen05.ld that may follow is a warp-wide instruction).
+__device__ __forceinline__ bool wait_commit(uint64_t *mbar, uint32_t &phase, bool &pending,
+                                            int polls) {
+    const bool got = __all_sync(0xffffffffu, wait_done(mbar, phase, polls));
+    if (got) {
+        phase ^= 1u;
+        pending = false;
+    }
     tc::fence_after_sync();
-    const int warp = threadIdx.x >> 5;
-    tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), out);
+    return got;
+}
+
+// TMEM row load that is skipped (zeros) once this warp has seen a wait give up: the CTA then
+// leaves at its next barrier without touching the tensor cores again.
+__device__ __forceinline__ void ld32_if(bool ok, uint32_t taddr, float v[32]) {
+    if (ok) {
+        tc::tmem_ld32(taddr, v);
+    } else {
+#pragma unroll
+        for (int q = 0; q < 32; ++q) v[q] = 0.f;
+    }
 }
 
 // Build the group's occupied-slot list ordered by (net, atom, slot); fills cnt / off /
-// net_start / tia.  A 32-slot chunk spans at most a few type blocks (usually one): one ballot
-// per spanned block counts / places its occupied slots.  All threads participate.
+// net_start / tia.  With block lengths (num_neigh) the occupied slots of each type block are
+// its first num_neigh slots; otherwise every slot of the list is tested (ballot per 32 slots).
 __device__ void build_group_list(const MixSmem &sm, const int32_t *__restrict__ list_neigh,
                                  const int32_t *__restrict__ type_map, long long g0, int ga,
                                  const MixParams &P) {
@@ -289,10 +296,10 @@ __device__ void build_group_list(const MixSmem &sm, const int32_t *__restrict__ 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const long long total = (long long)P.batch * P.natoms;
     const unsigned lt = (1u << lane) - 1u;
-    for (int a = warp; a < ga; a += TM / 32) {
+    for (int a = warp; a < GAMAX; a += TM / 32) {
         const long long t = g0 + a;
         int ti = -1;
-        if (t < total) {
+        if (a < ga && t < total) {
             ti = type_map[(int)(t % P.natoms)];
             if (ti < 0 || ti >= nt || !((P.present_mask >> ti) & 1)) ti = -1;
         }
@@ -300,6 +307,13 @@ __device__ void build_group_list(const MixSmem &sm, const int32_t *__restrict__ 
         if (lane == 0) sm.tia[a] = ti;
         __syncwarp();
         if (ti < 0) continue;
+        if (P.num_neigh) {
+            if (lane < nt && ((P.present_mask >> lane) & 1)) {
+                const int c = P.num_neigh[t * nt + lane];
+                sm.cnt[a * kMaxTypes + lane] = c < 0 ? 0 : (c > P.m ? P.m : c);
+            }
+            continue;
+        }
         const int32_t *ln = list_neigh + t * S;
         for (int s0 = 0; s0 < S; s0 += 32) {
             const int s = s0 + lane;
@@ -331,6 +345,14 @@ __device__ void build_group_list(const MixSmem &sm, const int32_t *__restrict__ 
     for (int a = warp; a < ga; a += TM / 32) {
         const long long t = g0 + a;
         if (sm.tia[a] < 0) continue;
+        if (P.num_neigh) {
+            for (int tj = 0; tj < nt; ++tj) {
+                const int c = sm.cnt[a * kMaxTypes + tj], base = sm.off[a * kMaxTypes + tj];
+                for (int k = lane; k < c; k += 32)
+                    sm.list[base + k] = (uint16_t)((a << 12) | (tj * P.m + k));
+            }
+            continue;
+        }
         const int32_t *ln = list_neigh + t * S;
         for (int s0 = 0; s0 < S; s0 += 32) {
             const int s = s0 + lane;
@@ -342,7 +364,7 @@ __device__ void build_group_list(const MixSmem &sm, const int32_t *__restrict__ 
                 const unsigned mq = __ballot_sync(0xffffffffu, active && blk == q);
                 if (!mq) continue;
                 const int base = sm.off[a * kMaxTypes + q];
-                if (active && blk == q) sm.list[base + __popc(mq & lt)] = (a << 16) | s;
+                if (active && blk == q) sm.list[base + __popc(mq & lt)] = (uint16_t)((a << 12) | s);
                 __syncwarp();
                 if (lane == 0) sm.off[a * kMaxTypes + q] = base + __popc(mq);
                 __syncwarp();
@@ -352,131 +374,201 @@ __device__ void build_group_list(const MixSmem &sm, const int32_t *__restrict__ 
     __syncthreads();
 }
 
+// Environment row of one pair (dp_dp.py:241-297) for centre type ti.
+struct EnvRow {
+    float R, x, y, z, s, ds, inv, rh[4];
+};
+
+__device__ __forceinline__ void env_of(EnvRow &e, const float4 q4, float rmin, float rmax,
+                                       const float *av, const float *isd) {
+    e.R = q4.x; e.x = q4.y; e.y = q4.z; e.z = q4.w;
+    switch_f(e.R, rmin, rmax, e.s, e.ds);
+    e.inv = fabsf(e.R) > 1e-5f ? __frcp_rn(e.R) : 0.f;
+    e.rh[0] = (e.s - av[0]) * isd[0];
+    e.rh[1] = (e.s * e.x * e.inv - av[1]) * isd[1];
+    e.rh[2] = (e.s * e.y * e.inv - av[2]) * isd[2];
+    e.rh[3] = (e.s * e.z * e.inv - av[3]) * isd[3];
+}
+
 // ------------------------------------------------------------------ forward (A descriptor)
 template <int SPLIT, bool FAST>
-__global__ void __launch_bounds__(TM, 4)
+__global__ void __launch_bounds__(TM, 3)
 dp_embed_fwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict__ idr,
                 const int32_t *__restrict__ type_map, const float *__restrict__ params,
                 const unsigned char *__restrict__ wtiles, const float *__restrict__ davg,
                 const float *__restrict__ dstd, const float *__restrict__ pad,
                 float *__restrict__ Aout, int32_t *__restrict__ err, MixParams P) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar_l, mbar_c;
     __shared__ uint32_t tmem_base;
     const int nt = P.ntypes, nnet = nt * nt, S = P.nslots;
-    const MixSmem sm = carve(smem_raw, nnet, S, P.ga);
+    const MixSmem sm = carve(smem_raw, false, S, P.ga);
     const int tid = threadIdx.x, warp = tid >> 5;
-    stage_vectors(params, sm.vec, nnet);
-    for (int q = tid; q < 2 * XT / 16; q += TM)
-        reinterpret_cast<uint4 *>(sm.xh)[q] = make_uint4(0, 0, 0, 0);   // xh, xl contiguous
-    if (tid == 0) tc::mbar_init(&mbar, 1);
-    if (warp == 0) tc::tmem_alloc(&tmem_base, 32);
+    for (int q = tid; q < (2 * XT + RT) / 16; q += TM)       // xh, xl, rop are contiguous
+        reinterpret_cast<uint4 *>(sm.xh)[q] = make_uint4(0, 0, 0, 0);
+    if (tid == 0) {
+        tc::mbar_init(&mbar_l, 1);
+        tc::mbar_init(&mbar_c, 1);
+    }
+    if (warp == 0) tc::tmem_alloc(&tmem_base, 64);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = tmem_base;
-    uint32_t phase = 0;
-    bool ok = true;
+    const uint32_t lane_q = (uint32_t)(warp * 32) << 16;
+    uint32_t ph_l = 0, ph_c = 0;
+    bool pend_l = false, pend_c = false, ok = true;
     int cur_net = -1;
+    int my_chunk = -1;                  // this thread's nonzero chunk of the contraction operand
     const long long total = (long long)P.batch * P.natoms;
     const long long ngroups = (total + P.ga - 1) / P.ga;
     for (long long grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
         const long long g0 = grp * P.ga;
         const int ga = (int)(total - g0 < P.ga ? total - g0 : P.ga);
         build_group_list(sm, list_neigh, type_map, g0, ga, P);
-        for (int q = tid; q < GAMAX * NA; q += TM) sm.acc[q] = 0.f;
-        __syncthreads();
+        bool first = true;
         for (int k = 0; k < nnet; ++k) {
             const int ns = sm.net_start[k], ne = sm.net_start[k + 1];
             if (ns == ne) continue;
-            if (k != cur_net) {
+            if (k != cur_net) {            // no MMA in flight reads the weight tiles here
                 __syncthreads();
-                load_weight_tiles(wtiles, k, sm.wt);
+                load_net(wtiles, params, k, 4, sm);
                 cur_net = k;
                 __syncthreads();
             }
             const int ti = k / nt;
-            const float *v = sm.vec + k * VEC;
-            const float av0 = davg[4 * ti], av1 = davg[4 * ti + 1], av2 = davg[4 * ti + 2],
-                        av3 = davg[4 * ti + 3];
-            const float is0 = 1.f / dstd[4 * ti], is1 = 1.f / dstd[4 * ti + 1],
-                        is2 = 1.f / dstd[4 * ti + 2], is3 = 1.f / dstd[4 * ti + 3];
+            const float av[4] = {davg[4 * ti], davg[4 * ti + 1], davg[4 * ti + 2], davg[4 * ti + 3]};
+            const float isd[4] = {1.f / dstd[4 * ti], 1.f / dstd[4 * ti + 1],
+                                  1.f / dstd[4 * ti + 2], 1.f / dstd[4 * ti + 3]};
+            const float4 *v4 = reinterpret_cast<const float4 *>(sm.vec);
             for (int r0 = ns; r0 < ne; r0 += TM) {
                 const int nrows = ne - r0 < TM ? ne - r0 : TM;
                 const bool valid = tid < nrows;
-                float R = 0.f, px = 0.f, py = 0.f, pz = 0.f;
+                int a = 0;
+                float4 q4 = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (valid) {
                     const int e = sm.list[r0 + tid];
-                    const long long t = g0 + (e >> 16);
-                    const float4 q4 = __ldg(reinterpret_cast<const float4 *>(idr) + t * S + (e & 0xFFFF));
-                    R = q4.x; px = q4.y; py = q4.z; pz = q4.w;
+                    a = e >> 12;
+                    q4 = __ldg(reinterpret_cast<const float4 *>(idr) + (g0 + a) * S + (e & 0xFFF));
                 }
-                float s, dsw;
-                switch_f(R, P.rmin, P.rmax, s, dsw);
-                const float inv = fabsf(R) > 1e-5f ? __frcp_rn(R) : 0.f;
-                float rh[4];
-                rh[0] = (s - av0) * is0;
-                rh[1] = (s * px * inv - av1) * is1;
-                rh[2] = (s * py * inv - av2) * is2;
-                rh[3] = (s * pz * inv - av3) * is3;
-                float x[KP], h[KP];
+                EnvRow en;
+                env_of(en, q4, P.rmin, P.rmax, av, isd);
+                float x[E];
 #pragma unroll
-                for (int o = 0; o < KP; ++o) x[o] = o < E ? act<FAST>(rh[0] * v[o] + v[E + o]) : 0.f;
-                store_act_row<SPLIT>(sm, tid, x);
-                run_layer<SPLIT>(sm, tmem, 0, &mbar, phase, ok, h);
+                for (int o4 = 0; o4 < 7; ++o4) {
+                    const float4 w = v4[o4], b = v4[VW / 4 + o4];
+                    const float wv[4] = {w.x, w.y, w.z, w.w}, bv[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
-                for (int o = 0; o < E; ++o) x[o] += act<FAST>(h[o] + v[2 * E + o]) * v[3 * E + o];
-                store_act_row<SPLIT>(sm, tid, x);
-                run_layer<SPLIT>(sm, tmem, 1, &mbar, phase, ok, h);
-                // the layer-3 MMA has completed: the activation tiles are free for staging
-                float *st = sm.stage + tid * STG;
+                    for (int q = 0; q < 4; ++q)
+                        if (4 * o4 + q < E) x[4 * o4 + q] = act<FAST>(en.rh[0] * wv[q] + bv[q]);
+                }
+                // the previous tile's contraction still reads the tiles written below
+                if (pend_c && !wait_commit(&mbar_c, ph_c, pend_c, P.wait_polls)) ok = false;
+                store_row<SPLIT>(sm, tid, x, 1.f);
+                {   // contraction operand: column tid holds this row's (R_h, R_l) at M = 8 a + 2 c + h
+                    if (my_chunk >= 0)
+                        *reinterpret_cast<uint4 *>(sm.rop + my_chunk) = make_uint4(0, 0, 0, 0);
+                    my_chunk = -1;
+                    if (valid) {
+                        float rv[8];
 #pragma unroll
-                for (int o = 0; o < E; ++o)
-                    st[o] = valid ? act<FAST>(h[o] + v[4 * E + o]) * v[5 * E + o] + x[o] : 0.f;
-#pragma unroll
-                for (int c = 0; c < 4; ++c) st[E + c] = valid ? rh[c] : 0.f;
-                const int nseg = tile_segments(sm, r0, nrows);   // includes __syncthreads
-                // A[atom][c][p] += sum over the atom's rows of R[c] G[p]: (segment, entry) tasks
-                for (int task = tid; task < nseg * NA; task += TM) {
-                    const int sg = task / NA, e = task - sg * NA;
-                    const int c = e / E, p = e - (e / E) * E;
-                    const int ra = sm.seg[sg], rb = sm.seg[sg + 1];
-                    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-                    int r = ra;
-                    for (; r + 4 <= rb; r += 4) {
-                        a0 += sm.stage[r * STG + E + c] * sm.stage[r * STG + p];
-                        a1 += sm.stage[(r + 1) * STG + E + c] * sm.stage[(r + 1) * STG + p];
-                        a2 += sm.stage[(r + 2) * STG + E + c] * sm.stage[(r + 2) * STG + p];
-                        a3 += sm.stage[(r + 3) * STG + E + c] * sm.stage[(r + 3) * STG + p];
+                        for (int c = 0; c < 4; ++c) {
+                            const float h = __bfloat162float(__float2bfloat16_rn(en.rh[c]));
+                            rv[2 * c] = h;
+                            rv[2 * c + 1] = SPLIT == 3 ? en.rh[c] - h : 0.f;
+                        }
+                        uint4 pk;
+                        tc::split8(rv, pk, nullptr);
+                        my_chunk = (int)mn_chunk(tid, a);
+                        *reinterpret_cast<uint4 *>(sm.rop + my_chunk) = pk;
                     }
-                    for (; r < rb; ++r) a0 += sm.stage[r * STG + E + c] * sm.stage[r * STG + p];
-                    sm.acc[sm.seg_atom[sg] * NA + e] += (a0 + a1) + (a2 + a3);
                 }
-                __syncthreads();
+                if (pre_issue(ok)) goto done;
+                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 0, &mbar_l);
+                pend_l = true;
+                if (!wait_commit(&mbar_l, ph_l, pend_l, P.wait_polls)) ok = false;
+                {
+                    float h[KP];
+                    ld32_if(ok, tmem + lane_q, h);
+#pragma unroll
+                    for (int o4 = 0; o4 < 7; ++o4) {
+                        const float4 d = v4[2 * VW / 4 + o4];
+                        const float dv[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            if (4 * o4 + q < E) x[4 * o4 + q] += act<FAST>(h[4 * o4 + q]) * dv[q];
+                    }
+                }
+                store_row<SPLIT>(sm, tid, x, 1.f);
+                if (pre_issue(ok)) goto done;
+                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 1, &mbar_l);
+                pend_l = true;
+                if (!wait_commit(&mbar_l, ph_l, pend_l, P.wait_polls)) ok = false;
+                {
+                    float h[KP];
+                    ld32_if(ok, tmem + lane_q, h);
+#pragma unroll
+                    for (int o4 = 0; o4 < 7; ++o4) {
+                        const float4 d = v4[3 * VW / 4 + o4];
+                        const float dv[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            if (4 * o4 + q < E) x[4 * o4 + q] += act<FAST>(h[4 * o4 + q]) * dv[q];
+                    }
+                }
+                store_row<SPLIT>(sm, tid, x, 0.f);       // G, the B operand of the contraction
+                if (pre_issue(ok)) goto done;
+                if (tid == 0)
+                    issue_rows<SPLIT, KP>(tmem + TCOL_A, sm.rop, sm.xh, sm.xl, first, &mbar_c);
+                pend_c = true;
+                first = false;
             }
         }
-        // empty-slot term, scale, write A
-        for (int q = tid; q < ga * NA; q += TM) {
-            const int a = q / NA, e = q - a * NA;
-            const int ti = sm.tia[a];
-            float val = 0.f;
-            if (ti >= 0) {
-                val = sm.acc[q];
-                for (int tj = 0; tj < nt; ++tj) {
-                    if (!((P.present_mask >> tj) & 1)) continue;
-                    const float nemp = (float)(P.m - sm.cnt[a * kMaxTypes + tj]);
-                    val += nemp * pad[(ti * nt + tj) * NA + e];
-                }
-                val *= P.inv_mT;
+        // A of the group: D[8 a + 2 c + h][p] summed over h, + empty-slot term, / (m T)
+        if (pend_c && !wait_commit(&mbar_c, ph_c, pend_c, P.wait_polls)) ok = false;
+        if (__syncthreads_or(!ok)) goto done;
+        {
+            float d[KP];
+            if (!first) {
+                tc::tmem_ld32(tmem + TCOL_A + lane_q, d);
+            } else {
+#pragma unroll
+                for (int p = 0; p < KP; ++p) d[p] = 0.f;
             }
-            Aout[(g0 + a) * NA + e] = val;
+#pragma unroll
+            for (int p = 0; p < E; ++p) d[p] += __shfl_xor_sync(0xffffffffu, d[p], 1);
+            const int a = tid >> 3, c = (tid >> 1) & 3;
+            if ((tid & 1) == 0 && a < ga) {
+                const int ti = sm.tia[a];
+                float *dst = Aout + (g0 + a) * NA + c * E;
+                if (ti < 0) {
+#pragma unroll
+                    for (int p = 0; p < E; ++p) dst[p] = 0.f;
+                } else {
+                    for (int tj = 0; tj < nt; ++tj) {
+                        if (!((P.present_mask >> tj) & 1)) continue;
+                        const float nemp = (float)(P.m - sm.cnt[a * kMaxTypes + tj]);
+                        const float *pp = pad + (ti * nt + tj) * NA + c * E;
+#pragma unroll
+                        for (int p = 0; p < E; ++p) d[p] += nemp * pp[p];
+                    }
+#pragma unroll
+                    for (int p = 0; p < E; ++p) dst[p] = d[p] * P.inv_mT;
+                }
+            }
         }
+        tc::fence_before_sync();
         __syncthreads();
+        tc::fence_after_sync();
     }
-    if (!ok) atomicMax(err, MATPL_KERR_TIMEOUT);
+done:
+    // drain: nothing this CTA issued may still run when its TMEM is freed
+    if (pend_l) tc::mbar_wait(&mbar_l, ph_l, kDrainPolls);
+    if (pend_c) tc::mbar_wait(&mbar_c, ph_c, kDrainPolls);
+    if (!ok && (tid & 31) == 0) atomicMax(err, MATPL_KERR_TIMEOUT);
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, 32);
+    if (warp == 0) tc::tmem_dealloc(tmem, 64);
 }
 
 // ------------------------------------------------------------------ backward (forces)
@@ -489,188 +581,277 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
                 float *__restrict__ force, double *__restrict__ atom_vir,
                 int32_t *__restrict__ err, MixParams P) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t mbar;
+    __shared__ __align__(8) uint64_t mbar_l, mbar_c;
     __shared__ uint32_t tmem_base;
     const int nt = P.ntypes, nnet = nt * nt, S = P.nslots;
-    const MixSmem sm = carve(smem_raw, nnet, S, P.ga);
+    const MixSmem sm = carve(smem_raw, true, S, P.ga);
     const int tid = threadIdx.x, warp = tid >> 5;
-    stage_vectors(params, sm.vec, nnet);
-    for (int q = tid; q < 2 * XT / 16; q += TM)
+    for (int q = tid; q < (2 * XT + RT + 2 * QT) / 16; q += TM)   // xh, xl, rop, qh, ql
         reinterpret_cast<uint4 *>(sm.xh)[q] = make_uint4(0, 0, 0, 0);
-    if (tid == 0) tc::mbar_init(&mbar, 1);
-    if (warp == 0) tc::tmem_alloc(&tmem_base, 32);
+    if (tid == 0) {
+        tc::mbar_init(&mbar_l, 1);
+        tc::mbar_init(&mbar_c, 1);
+    }
+    if (warp == 0) tc::tmem_alloc(&tmem_base, 128);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = tmem_base;
-    uint32_t phase = 0;
-    bool ok = true;
+    const uint32_t lane_q = (uint32_t)(warp * 32) << 16;
+    uint32_t ph_l = 0, ph_c = 0;
+    bool pend_l = false, pend_c = false, ok = true;
     int cur_net = -1;
+    int my_chunk = -1;                  // this thread's nonzero chunk of the one-hot operand
     const int nall = P.natoms + P.nghost;
     const long long total = (long long)P.batch * P.natoms;
     const long long ngroups = (total + P.ga - 1) / P.ga;
+    const float4 *dA4 = reinterpret_cast<const float4 *>(sm.dA);
     for (long long grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
         const long long g0 = grp * P.ga;
         const int ga = (int)(total - g0 < P.ga ? total - g0 : P.ga);
         build_group_list(sm, list_neigh, type_map, g0, ga, P);
-        for (int q = tid; q < GAMAX * NA; q += TM) {
-            const int a = q / NA;
-            sm.acc[q] = a < ga ? dAin[g0 * NA + q] * P.inv_mT : 0.f;
+        for (int q = tid; q < GAMAX * E; q += TM) {          // dA[a][p][c] = dE/dA[c][p] k
+            const int a = q / E, p = q - a * E;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (a < ga) {
+                const float *s = dAin + (g0 + a) * NA + p;
+                v = make_float4(s[0] * P.inv_mT, s[E] * P.inv_mT, s[2 * E] * P.inv_mT,
+                                s[3 * E] * P.inv_mT);
+            }
+            reinterpret_cast<float4 *>(sm.dA)[q] = v;
         }
-        for (int q = tid; q < GAMAX * 4; q += TM) sm.fi[q] = 0.f;
-        for (int q = tid; q < GAMAX * 9; q += TM) sm.vir[q] = 0.0;
         __syncthreads();
+        bool first = true;
         for (int k = 0; k < nnet; ++k) {
             const int ns = sm.net_start[k], ne = sm.net_start[k + 1];
             if (ns == ne) continue;
             if (k != cur_net) {
                 __syncthreads();
-                load_weight_tiles(wtiles, k, sm.wt);
+                load_net(wtiles, params, k, 8, sm);
                 cur_net = k;
                 __syncthreads();
             }
             const int ti = k / nt;
-            const float *v = sm.vec + k * VEC;
-            const float av0 = davg[4 * ti], av1 = davg[4 * ti + 1], av2 = davg[4 * ti + 2],
-                        av3 = davg[4 * ti + 3];
+            const float av[4] = {davg[4 * ti], davg[4 * ti + 1], davg[4 * ti + 2], davg[4 * ti + 3]};
             const float isd[4] = {1.f / dstd[4 * ti], 1.f / dstd[4 * ti + 1],
                                   1.f / dstd[4 * ti + 2], 1.f / dstd[4 * ti + 3]};
+            const float4 *v4 = reinterpret_cast<const float4 *>(sm.vec);
             for (int r0 = ns; r0 < ne; r0 += TM) {
                 const int nrows = ne - r0 < TM ? ne - r0 : TM;
                 const bool valid = tid < nrows;
-                float R = 0.f, px = 0.f, py = 0.f, pz = 0.f;
-                int a_loc = 0, j = -1;
+                int a = 0, j = -1;
                 long long t = g0;
+                float4 q4 = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (valid) {
                     const int e = sm.list[r0 + tid];
-                    a_loc = e >> 16;
-                    t = g0 + a_loc;
-                    const int slot = e & 0xFFFF;
-                    const float4 q4 = __ldg(reinterpret_cast<const float4 *>(idr) + t * S + slot);
-                    R = q4.x; px = q4.y; py = q4.z; pz = q4.w;
-                    j = __ldg(list_neigh + t * S + slot) - 1;
+                    a = e >> 12;
+                    t = g0 + a;
+                    q4 = __ldg(reinterpret_cast<const float4 *>(idr) + t * S + (e & 0xFFF));
+                    j = __ldg(list_neigh + t * S + (e & 0xFFF)) - 1;
                 }
-                float s, dsw;
-                switch_f(R, P.rmin, P.rmax, s, dsw);
-                const bool mask = fabsf(R) > 1e-5f;
-                const float inv = mask ? __frcp_rn(R) : 0.f;
-                float rh[4];
-                rh[0] = (s - av0) * isd[0];
-                rh[1] = (s * px * inv - av1) * isd[1];
-                rh[2] = (s * py * inv - av2) * isd[2];
-                rh[3] = (s * pz * inv - av3) * isd[3];
-                // recompute forward, keeping t1 (= x1), t2, t3
-                float x[KP], h[KP], t1[E], t2[E];
+                EnvRow en;
+                env_of(en, q4, P.rmin, P.rmax, av, isd);
+                float x[E];
 #pragma unroll
-                for (int o = 0; o < KP; ++o) {
-                    x[o] = o < E ? act<FAST>(rh[0] * v[o] + v[E + o]) : 0.f;
-                    if (o < E) t1[o] = x[o];
-                }
-                store_act_row<SPLIT>(sm, tid, x);
-                run_layer<SPLIT>(sm, tmem, 0, &mbar, phase, ok, h);
+                for (int o4 = 0; o4 < 7; ++o4) {
+                    const float4 w = v4[o4], b = v4[VW / 4 + o4];
+                    const float wv[4] = {w.x, w.y, w.z, w.w}, bv[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
-                for (int o = 0; o < E; ++o) {
-                    t2[o] = act<FAST>(h[o] + v[2 * E + o]);
-                    x[o] += t2[o] * v[3 * E + o];
+                    for (int q = 0; q < 4; ++q)
+                        if (4 * o4 + q < E) x[4 * o4 + q] = act<FAST>(en.rh[0] * wv[q] + bv[q]);
                 }
-                store_act_row<SPLIT>(sm, tid, x);
-                run_layer<SPLIT>(sm, tmem, 1, &mbar, phase, ok, h);
+                store_row<SPLIT>(sm, tid, x, 1.f);
+                if (pre_issue(ok)) goto done;
+                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 0, &mbar_l);
+                pend_l = true;
+                if (!wait_commit(&mbar_l, ph_l, pend_l, P.wait_polls)) ok = false;
+                {
+                    float h[KP];
+                    ld32_if(ok, tmem + lane_q, h);
 #pragma unroll
-                for (int o = 0; o < E; ++o) {
-                    h[o] = act<FAST>(h[o] + v[4 * E + o]);       // t3
-                    x[o] += h[o] * v[5 * E + o];                 // G
+                    for (int o4 = 0; o4 < 7; ++o4) {
+                        const float4 d = v4[2 * VW / 4 + o4];
+                        const float dv[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const int o = 4 * o4 + q;
+                            if (o < E) {
+                                h[o] = act<FAST>(h[o]);           // t2, stashed in TMEM
+                                x[o] += h[o] * dv[q];
+                            }
+                        }
+                    }
+                    if (ok) tc::tmem_st32(tmem + TCOL_STASH + lane_q, h);
                 }
-                // dE/dR[c] = sum_p dA[c][p] G[p];  dG[p] = sum_c dA[c][p] R[c]
-                const float *dA = sm.acc + a_loc * NA;
+                store_row<SPLIT>(sm, tid, x, 1.f);
+                if (pre_issue(ok)) goto done;
+                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 1, &mbar_l);
+                pend_l = true;
+                if (!wait_commit(&mbar_l, ph_l, pend_l, P.wait_polls)) ok = false;
                 float g[4] = {0.f, 0.f, 0.f, 0.f};
+                {
+                    // G = x + dt2 t3;  dE/dR[c] = sum_p dA[c][p] G[p];  dG[p] = sum_c dA[c][p] R[c];
+                    // y = dG dt2 (1 - t3^2) feeds the transposed layer-3 GEMM
+                    float h[KP];
+                    ld32_if(ok, tmem + lane_q, h);
+                    const float4 *da = dA4 + a * E;
 #pragma unroll
-                for (int p = 0; p < E; ++p) {
-                    const float d0 = dA[p], d1 = dA[E + p], d2 = dA[2 * E + p], d3 = dA[3 * E + p];
-                    g[0] += d0 * x[p];
-                    g[1] += d1 * x[p];
-                    g[2] += d2 * x[p];
-                    g[3] += d3 * x[p];
-                    x[p] = d0 * rh[0] + d1 * rh[1] + d2 * rh[2] + d3 * rh[3];
+                    for (int o4 = 0; o4 < 7; ++o4) {
+                        const float4 d = v4[3 * VW / 4 + o4];
+                        const float dv[4] = {d.x, d.y, d.z, d.w};
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const int o = 4 * o4 + q;
+                            if (o < E) {
+                                const float t3 = act<FAST>(h[o]);
+                                const float G = x[o] + dv[q] * t3;
+                                const float4 w = da[o];
+                                g[0] += w.x * G; g[1] += w.y * G; g[2] += w.z * G; g[3] += w.w * G;
+                                const float dG = w.x * en.rh[0] + w.y * en.rh[1] + w.z * en.rh[2] +
+                                                 w.w * en.rh[3];
+                                x[o] = dG;                               // x now holds dG
+                                h[o] = dG * dv[q] * (1.f - t3 * t3);     // h now holds y
+                            }
+                        }
+                    }
+                    store_row<SPLIT>(sm, tid, h, 0.f);
                 }
-                float y[KP];
+                if (pre_issue(ok)) goto done;
+                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 2, &mbar_l);
+                pend_l = true;
+                if (!wait_commit(&mbar_l, ph_l, pend_l, P.wait_polls)) ok = false;
+                {
+                    float h[KP], t2[KP];
+                    ld32_if(ok, tmem + lane_q, h);
+                    ld32_if(ok, tmem + TCOL_STASH + lane_q, t2);
 #pragma unroll
-                for (int o = 0; o < KP; ++o) y[o] = o < E ? x[o] * v[5 * E + o] * (1.f - h[o] * h[o]) : 0.f;
-                store_act_row<SPLIT>(sm, tid, y);
-                run_layer<SPLIT>(sm, tmem, 2, &mbar, phase, ok, h);
+                    for (int o4 = 0; o4 < 7; ++o4) {
+                        const float4 d = v4[2 * VW / 4 + o4];
+                        const float dv[4] = {d.x, d.y, d.z, d.w};
 #pragma unroll
-                for (int o = 0; o < E; ++o) x[o] += h[o];
-#pragma unroll
-                for (int o = 0; o < KP; ++o) y[o] = o < E ? x[o] * v[3 * E + o] * (1.f - t2[o] * t2[o]) : 0.f;
-                store_act_row<SPLIT>(sm, tid, y);
-                run_layer<SPLIT>(sm, tmem, 3, &mbar, phase, ok, h);
-                float dsv = 0.f;
-#pragma unroll
-                for (int o = 0; o < E; ++o) dsv += v[o] * (x[o] + h[o]) * (1.f - t1[o] * t1[o]);
-                g[0] += dsv;
-                float f[3] = {0.f, 0.f, 0.f};
-                if (mask) {   // f_a = sum_c g[c] Ri_d[c][a], Ri_d = -dfeat / dstd
-                    const float common = (dsw - s * inv) * inv * inv;
-                    const float g0 = g[0] * isd[0], g1 = g[1] * isd[1], g2 = g[2] * isd[2],
-                                g3 = g[3] * isd[3];
-                    const float cg = common * (g1 * px + g2 * py + g3 * pz);
-                    const float sv = s * inv;
-                    f[0] = -(g0 * dsw * px * inv + cg * px + g1 * sv);
-                    f[1] = -(g0 * dsw * py * inv + cg * py + g2 * sv);
-                    f[2] = -(g0 * dsw * pz * inv + cg * pz + g3 * sv);
+                        for (int q = 0; q < 4; ++q) {
+                            const int o = 4 * o4 + q;
+                            if (o < E) {
+                                x[o] += h[o];                              // dx2
+                                h[o] = x[o] * dv[q] * (1.f - t2[o] * t2[o]);
+                            }
+                        }
+                    }
+                    store_row<SPLIT>(sm, tid, h, 0.f);
                 }
-                float *st = sm.stage + tid * STG;     // activation tiles are free again
-                if (valid) {
-                    const long long b = t / P.natoms;
-                    if (j >= 0 && j < nall) {
+                if (pre_issue(ok)) goto done;
+                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 3, &mbar_l);
+                pend_l = true;
+                if (!wait_commit(&mbar_l, ph_l, pend_l, P.wait_polls)) ok = false;
+                {
+                    // dE/ds = sum_o W0[o] (dx2 + h)[o] (1 - t1^2), t1 recomputed
+                    float h[KP];
+                    ld32_if(ok, tmem + lane_q, h);
+                    float dsv = 0.f;
+#pragma unroll
+                    for (int o4 = 0; o4 < 7; ++o4) {
+                        const float4 w = v4[o4], b = v4[VW / 4 + o4];
+                        const float wv[4] = {w.x, w.y, w.z, w.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const int o = 4 * o4 + q;
+                            if (o < E) {
+                                const float t1 = act<FAST>(en.rh[0] * wv[q] + bv[q]);
+                                dsv += wv[q] * (x[o] + h[o]) * (1.f - t1 * t1);
+                            }
+                        }
+                    }
+                    g[0] += dsv;
+                }
+                {
+                    // f_a = sum_c g[c] Ri_d[c][a], Ri_d = -dfeat / dstd (dp_dp.py:266-299)
+                    float f[3] = {0.f, 0.f, 0.f};
+                    if (valid && fabsf(en.R) > 1e-5f) {
+                        const float common = (en.ds - en.s * en.inv) * en.inv * en.inv;
+                        const float g0 = g[0] * isd[0], g1 = g[1] * isd[1], g2 = g[2] * isd[2],
+                                    g3 = g[3] * isd[3];
+                        const float cg = common * (g1 * en.x + g2 * en.y + g3 * en.z);
+                        const float sv = en.s * en.inv;
+                        f[0] = -(g0 * en.ds * en.x * en.inv + cg * en.x + g1 * sv);
+                        f[1] = -(g0 * en.ds * en.y * en.inv + cg * en.y + g2 * sv);
+                        f[2] = -(g0 * en.ds * en.z * en.inv + cg * en.z + g3 * sv);
+                    }
+                    if (valid && j >= 0 && j < nall) {
+                        const long long b = t / P.natoms;
                         float *dst = force + (b * nall + j) * 3;
                         atomicAdd(dst + 0, f[0]);
                         atomicAdd(dst + 1, f[1]);
                         atomicAdd(dst + 2, f[2]);
                     }
-                    st[0] = f[0]; st[1] = f[1]; st[2] = f[2];
-                    st[3] = px; st[4] = py; st[5] = pz;
-                } else {
+                    // the previous tile's reduction still reads the operands written below
+                    if (pend_c && !wait_commit(&mbar_c, ph_c, pend_c, P.wait_polls)) ok = false;
+                    const float qv[QN] = {f[0], f[1], f[2],
+                                          f[0] * en.x, f[0] * en.y, f[0] * en.z,
+                                          f[1] * en.x, f[1] * en.y, f[1] * en.z,
+                                          f[2] * en.x, f[2] * en.y, f[2] * en.z, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-                    for (int q = 0; q < 6; ++q) st[q] = 0.f;
-                }
-                const int nseg = tile_segments(sm, r0, nrows);   // includes __syncthreads
-                // per-atom F_i (3) and virial (9): (segment, quantity) tasks
-                for (int task = tid; task < nseg * 12; task += TM) {
-                    const int sg = task / 12, q = task - sg * 12;
-                    const int ra = sm.seg[sg], rb = sm.seg[sg + 1];
-                    const int qa = q < 3 ? q : (q - 3) / 3, qc = q < 3 ? 0 : (q - 3) % 3;
-                    double a0 = 0.0, a1 = 0.0;
-                    int r = ra;
-                    for (; r + 2 <= rb; r += 2) {
-                        const float *s0 = sm.stage + r * STG, *s1 = s0 + STG;
-                        a0 += q < 3 ? (double)s0[qa] : (double)s0[qa] * (double)s0[3 + qc];
-                        a1 += q < 3 ? (double)s1[qa] : (double)s1[qa] * (double)s1[3 + qc];
+                    for (int gq = 0; gq < 2; ++gq) {
+                        uint4 hq, lq;
+                        tc::split8(qv + 8 * gq, hq, SPLIT == 3 ? &lq : nullptr);
+                        *reinterpret_cast<uint4 *>(sm.qh + mn_chunk(tid, gq)) = hq;
+                        if (SPLIT == 3) *reinterpret_cast<uint4 *>(sm.ql + mn_chunk(tid, gq)) = lq;
                     }
-                    if (r < rb) {
-                        const float *s0 = sm.stage + r * STG;
-                        a0 += q < 3 ? (double)s0[qa] : (double)s0[qa] * (double)s0[3 + qc];
+                    // one-hot operand: column tid holds 1 at M = a
+                    if (my_chunk >= 0)
+                        *reinterpret_cast<uint4 *>(sm.rop + my_chunk) = make_uint4(0, 0, 0, 0);
+                    my_chunk = -1;
+                    if (valid) {
+                        uint32_t w[4] = {0u, 0u, 0u, 0u};
+                        w[(a & 7) >> 1] = 0x3F80u << (16 * (a & 1));   // bf16 1.0
+                        my_chunk = (int)mn_chunk(tid, a >> 3);
+                        *reinterpret_cast<uint4 *>(sm.rop + my_chunk) = make_uint4(w[0], w[1], w[2], w[3]);
                     }
-                    const int at = sm.seg_atom[sg];
-                    if (q < 3) sm.fi[at * 4 + q] -= (float)(a0 + a1);
-                    else sm.vir[at * 9 + q - 3] += a0 + a1;
                 }
-                __syncthreads();
+                if (pre_issue(ok)) goto done;
+                if (tid == 0)
+                    issue_rows<SPLIT, QN>(tmem + TCOL_RED, sm.rop, sm.qh, sm.ql, first, &mbar_c);
+                pend_c = true;
+                first = false;
             }
         }
-        for (int q = tid; q < ga * 9; q += TM) atom_vir[(g0 + q / 9) * 9 + q % 9] = sm.vir[q];
-        for (int q = tid; q < ga * 3; q += TM) {
-            const int a = q / 3, c = q - a * 3;
-            const long long t = g0 + a;
-            const long long b = t / P.natoms;
-            const int i = (int)(t - b * P.natoms);
-            atomicAdd(force + (b * nall + i) * 3 + c, sm.fi[a * 4 + c]);
+        // F_i = -sum f and the per-atom virial of the group's atoms (TMEM rows 0..15)
+        if (pend_c && !wait_commit(&mbar_c, ph_c, pend_c, P.wait_polls)) ok = false;
+        if (__syncthreads_or(!ok)) goto done;
+        if (warp == 0) {
+            float d[QN];
+            if (!first) {
+                tc::tmem_ld16(tmem + TCOL_RED, d);
+            } else {
+#pragma unroll
+                for (int q = 0; q < QN; ++q) d[q] = 0.f;
+            }
+            const int a = tid;
+            if (a < ga) {
+                const long long t = g0 + a;
+                double *av9 = atom_vir + t * 9;
+#pragma unroll
+                for (int q = 0; q < 9; ++q) av9[q] = (double)d[3 + q];
+                if (sm.tia[a] >= 0) {
+                    const long long b = t / P.natoms;
+                    const int i = (int)(t - b * P.natoms);
+                    float *dst = force + (b * nall + i) * 3;
+                    atomicAdd(dst + 0, -d[0]);
+                    atomicAdd(dst + 1, -d[1]);
+                    atomicAdd(dst + 2, -d[2]);
+                }
+            }
         }
+        tc::fence_before_sync();
         __syncthreads();
+        tc::fence_after_sync();
     }
-    if (!ok) atomicMax(err, MATPL_KERR_TIMEOUT);
+done:
+    if (pend_l) tc::mbar_wait(&mbar_l, ph_l, kDrainPolls);
+    if (pend_c) tc::mbar_wait(&mbar_c, ph_c, kDrainPolls);
+    if (!ok && (tid & 31) == 0) atomicMax(err, MATPL_KERR_TIMEOUT);
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, 32);
+    if (warp == 0) tc::tmem_dealloc(tmem, 128);
 }
 
 }  // namespace
@@ -678,15 +859,20 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
 // Tuning of the mixed embedding kernels (matpl_dp_set_tuning): centre atoms per CTA group
 // (how many pair rows feed each 128-row MMA tile) and resident CTAs per SM; 0 = automatic.
 static std::atomic<int> g_ga_override{0}, g_ctas_override{0};
+// Bound of every completion wait of the mixed embedding kernels (matpl_dp_set_wait_limit).
+static std::atomic<int> g_wait_polls{1 << 24};
 
 // Launch helpers used by dp_fused.cu's matpl_dp_eval for the MATPL_MIXED forms.
 int mixed_ga(int S) {
-    const int lim = std::max(1, std::min(GAMAX, 9600 / std::max(1, S)));
+    const int lim = std::max(1, std::min(GAMAX, 8192 / std::max(1, S)));
     const int o = g_ga_override.load();
     return o > 0 ? std::min(o, lim) : lim;
 }
 
-size_t mixed_smem(int ntypes, int S) { return mix_smem_bytes(ntypes * ntypes, S, mixed_ga(S)); }
+size_t mixed_smem(int ntypes, int S) {
+    (void)ntypes;
+    return std::max(mix_smem_bytes(false, S, mixed_ga(S)), mix_smem_bytes(true, S, mixed_ga(S)));
+}
 
 size_t mixed_tile_bytes(int ntypes) { return (size_t)ntypes * ntypes * 8 * WT; }
 
@@ -698,24 +884,27 @@ int prep_mixed_tiles(const float *params, unsigned char *out, int ntypes, cudaSt
 }
 
 template <int SPLIT, bool FAST>
-int launch_mixed_embed(bool backward, const int32_t *list_neigh, const float *idr,
-                       const int32_t *type_map, const float *params, const unsigned char *wtiles,
-                       const float *davg, const float *dstd, const float *pad_or_dA,
-                       float *A_or_force, double *atom_vir, int32_t *err, int batch, int natoms,
-                       int nslots, int nghost, int ntypes, int m, int present_mask, double rmin,
-                       double rmax, double inv_mT, cudaStream_t s) {
+int launch_mixed_embed(bool backward, const int32_t *list_neigh, const int32_t *num_neigh,
+                       const float *idr, const int32_t *type_map, const float *params,
+                       const unsigned char *wtiles, const float *davg, const float *dstd,
+                       const float *pad_or_dA, float *A_or_force, double *atom_vir, int32_t *err,
+                       int batch, int natoms, int nslots, int nghost, int ntypes, int m,
+                       int present_mask, double rmin, double rmax, double inv_mT,
+                       cudaStream_t s) {
     MixParams P;
     P.batch = batch; P.natoms = natoms; P.nslots = nslots; P.nghost = nghost;
     P.ntypes = ntypes; P.m = m; P.present_mask = present_mask; P.ga = mixed_ga(nslots);
     P.rmin = (float)rmin; P.rmax = (float)rmax; P.inv_mT = (float)inv_mT;
-    const size_t smem = mix_smem_bytes(ntypes * ntypes, nslots, P.ga);
+    P.wait_polls = g_wait_polls.load();
+    P.num_neigh = num_neigh;
+    const size_t smem = mix_smem_bytes(backward, nslots, P.ga);
     const long long total = (long long)batch * natoms;
     const long long ngroups = (total + P.ga - 1) / P.ga;
-    // resident CTAs per SM: what shared memory allows (the automatic choice stays at 3, the
-    // tuning hook may ask for up to 6; the backward's registers cap it at 3 anyway)
-    const int fit = (int)std::max<size_t>(1, (220 * 1024) / (smem + 2048));
-    int per_sm = std::min(fit, 3);
-    if (g_ctas_override.load() > 0) per_sm = std::min(fit, g_ctas_override.load());
+    // resident CTAs per SM: what shared memory and TMEM allow (64 / 128 columns per CTA);
+    // the tuning hook may ask for fewer
+    const int fit = (int)std::max<size_t>(1, (227 * 1024) / (smem + 1024));
+    int per_sm = std::min(fit, backward ? 3 : 4);
+    if (g_ctas_override.load() > 0) per_sm = std::min(per_sm, g_ctas_override.load());
     const int grid = (int)std::min<long long>(ngroups, (long long)device_sms() * per_sm);
     if (!backward) {
         auto k = dp_embed_fwd_tc<SPLIT, FAST>;
@@ -733,18 +922,15 @@ int launch_mixed_embed(bool backward, const int32_t *list_neigh, const float *id
     return check_launch(backward ? "dp_embed_bwd_tc" : "dp_embed_fwd_tc");
 }
 
-template int launch_mixed_embed<1, true>(
-    bool, const int32_t *, const float *, const int32_t *, const float *, const unsigned char *,
-    const float *, const float *, const float *, float *, double *, int32_t *, int, int, int,
-    int, int, int, int, double, double, double, cudaStream_t);
-template int launch_mixed_embed<3, false>(
-    bool, const int32_t *, const float *, const int32_t *, const float *, const unsigned char *,
-    const float *, const float *, const float *, float *, double *, int32_t *, int, int, int,
-    int, int, int, int, double, double, double, cudaStream_t);
-template int launch_mixed_embed<3, true>(
-    bool, const int32_t *, const float *, const int32_t *, const float *, const unsigned char *,
-    const float *, const float *, const float *, float *, double *, int32_t *, int, int, int,
-    int, int, int, int, double, double, double, cudaStream_t);
+#define MATPL_INSTANTIATE_MIXED(SPLIT, FAST)                                                   \
+    template int launch_mixed_embed<SPLIT, FAST>(                                              \
+        bool, const int32_t *, const int32_t *, const float *, const int32_t *, const float *, \
+        const unsigned char *, const float *, const float *, const float *, float *, double *,  \
+        int32_t *, int, int, int, int, int, int, int, double, double, double, cudaStream_t);
+MATPL_INSTANTIATE_MIXED(1, true)
+MATPL_INSTANTIATE_MIXED(3, false)
+MATPL_INSTANTIATE_MIXED(3, true)
+#undef MATPL_INSTANTIATE_MIXED
 
 }  // namespace matpl
 
@@ -764,5 +950,12 @@ extern "C" int matpl_dp_get_tuning(int *mixed_group_atoms, int *mixed_ctas_per_s
     MATPL_REQUIRE(mixed_group_atoms && mixed_ctas_per_sm, MATPL_ERR_INVALID, "null pointer");
     *mixed_group_atoms = g_ga_override.load();
     *mixed_ctas_per_sm = g_ctas_override.load();
+    return MATPL_OK;
+}
+
+extern "C" int matpl_dp_set_wait_limit(int polls) {
+    using namespace matpl;
+    MATPL_REQUIRE(polls >= 0, MATPL_ERR_INVALID, "polls must be >= 0 (0: default)");
+    g_wait_polls.store(polls == 0 ? (1 << 24) : polls);
     return MATPL_OK;
 }

@@ -39,6 +39,7 @@ struct NbParams {
     double rc2;                    // Rc_M**2
     double rct2[kMaxTypes];        // Rc_type(t)**2
     int cell_cap;                  // cell capacity per image
+    int occupied_only;             // 1: write the occupied slots only (counts in num_neigh)
 };
 
 __device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
@@ -489,8 +490,9 @@ nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
             store4(image_dr + 4 * slot, conv<TO>(__dsqrt_rn(dd)), conv<TO>(x), conv<TO>(y),
                    conv<TO>(z));
         }
-        // ---- phase D: clear the empty slots
-        for (int s = lane; s < S; s += 32) {
+        // ---- phase D: clear the empty slots (the occupied-slot form leaves them untouched:
+        // its readers take the block lengths from num_neigh)
+        for (int s = lane; s < S && !P.occupied_only; s += 32) {
             const int ty = s / P.m;
             int nt = 0;
 #pragma unroll
@@ -596,12 +598,11 @@ extern "C" size_t matpl_neighbor_workspace_bytes(int batch, int natoms) {
     return nb_layout(batch, natoms).total;
 }
 
-extern "C" int matpl_neighbor_build(int batch, int natoms, int ntypes, int m_neigh, double Rc_M,
-                                    const double *Rc_type, const int32_t *type_map,
-                                    const double *lattice, const double *frac_pos, int out_dtype,
-                                    int32_t *list_neigh, void *image_dr, int32_t *num_neigh,
-                                    int32_t *err_dev, void *workspace, size_t workspace_bytes,
-                                    void *stream) {
+static int neighbor_build(int batch, int natoms, int ntypes, int m_neigh, double Rc_M,
+                          const double *Rc_type, const int32_t *type_map, const double *lattice,
+                          const double *frac_pos, int out_dtype, int32_t *list_neigh,
+                          void *image_dr, int32_t *num_neigh, int32_t *err_dev, void *workspace,
+                          size_t workspace_bytes, void *stream, bool occupied_only) {
     MATPL_REQUIRE(batch >= 0 && natoms >= 0, MATPL_ERR_INVALID, "negative size");
     MATPL_REQUIRE(ntypes >= 1 && ntypes <= kMaxTypes, MATPL_ERR_UNSUPPORTED,
                   "ntypes must be in [1, 16]");
@@ -627,6 +628,7 @@ extern "C" int matpl_neighbor_build(int batch, int natoms, int ntypes, int m_nei
     P.rc2 = Rc_M * Rc_M;
     for (int q = 0; q < kMaxTypes; ++q) P.rct2[q] = q < ntypes ? Rc_type[q] * Rc_type[q] : 0.0;
     P.cell_cap = natoms + 27;
+    P.occupied_only = occupied_only ? 1 : 0;
     char *ws = static_cast<char *>(workspace);
     NbImage *img = reinterpret_cast<NbImage *>(ws + lay.img);
     double *wpos = reinterpret_cast<double *>(ws + lay.wpos);
@@ -666,6 +668,33 @@ extern "C" int matpl_neighbor_build(int batch, int natoms, int ntypes, int m_nei
             num_neigh, err_dev, P);
     }
     return check_launch("matpl_neighbor_build");
+}
+
+extern "C" int matpl_neighbor_build(int batch, int natoms, int ntypes, int m_neigh, double Rc_M,
+                                    const double *Rc_type, const int32_t *type_map,
+                                    const double *lattice, const double *frac_pos, int out_dtype,
+                                    int32_t *list_neigh, void *image_dr, int32_t *num_neigh,
+                                    int32_t *err_dev, void *workspace, size_t workspace_bytes,
+                                    void *stream) {
+    return neighbor_build(batch, natoms, ntypes, m_neigh, Rc_M, Rc_type, type_map, lattice,
+                          frac_pos, out_dtype, list_neigh, image_dr, num_neigh, err_dev,
+                          workspace, workspace_bytes, stream, false);
+}
+
+extern "C" int matpl_neighbor_build_occupied(int batch, int natoms, int ntypes, int m_neigh,
+                                             double Rc_M, const double *Rc_type,
+                                             const int32_t *type_map, const double *lattice,
+                                             const double *frac_pos, int out_dtype,
+                                             int32_t *list_neigh, void *image_dr,
+                                             int32_t *num_neigh, int32_t *err_dev,
+                                             void *workspace, size_t workspace_bytes,
+                                             void *stream) {
+    MATPL_REQUIRE(num_neigh != nullptr, MATPL_ERR_INVALID,
+                  "matpl_neighbor_build_occupied: num_neigh is required (it gives the block "
+                  "lengths)");
+    return neighbor_build(batch, natoms, ntypes, m_neigh, Rc_M, Rc_type, type_map, lattice,
+                          frac_pos, out_dtype, list_neigh, image_dr, num_neigh, err_dev,
+                          workspace, workspace_bytes, stream, true);
 }
 
 extern "C" int matpl_env_mat(int dtype, int batch, int natoms, int nslots,

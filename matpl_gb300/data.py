@@ -196,3 +196,54 @@ def uniform_batches(images: Sequence, atom_type: Sequence[int],
         for a in range(0, len(idx), max_batch):
             out.append(idx[a:a + max_batch])
     return out
+
+
+@_lib.on_device
+def ragged_batch(cfg: DPConfig, images: Sequence, device="cuda", energies=None, forces=None,
+                 out_dtype: torch.dtype = torch.float64) -> Dict:
+    """Ragged collate: configurations of uneven atom count and composition concatenated into
+    one image of sum(N_c) atoms, the training batch of ``FusedTrainer`` / ``GraphedTrainer``
+    without ``_classify_batchs``' per-composition clusters (dp_trainer.py:536-547).
+
+    Each configuration's neighbor list comes from ``matpl_neighbor_build`` on its own cell
+    (``find_neighbore``, dpuni_data_loader.py:595-650) and its neighbor indices are shifted by
+    the configuration's first atom, so no pair crosses configurations; the per-atom quantities
+    of the fused kernels then need no padding, and energies are per-configuration sums of the
+    atoms' energies (``config_of_atom``).  Returns a batch dict: list_neigh [1, sum N, S] int32
+    (1-based, 0 = empty), ImageDR [1, sum N, S, 4], type_map [sum N], atom_type,
+    config_of_atom [sum N] int64, natoms [C] int64, and, when given, Etot [C] and Force
+    [1, sum N, 3] labels."""
+    dev = torch.device(device)
+    S = cfg.ntypes * cfg.maxNeighborNum
+    lns, idrs, tms, cfg_of = [], [], [], []
+    start = 0
+    for c, st in enumerate(images):
+        tm = torch.tensor(model_types(st, cfg.atom_type), device=dev)
+        ln, idr = ops.find_neighbore(tm, torch.tensor(st.frac, device=dev),
+                                     torch.tensor(st.lattice, device=dev), cfg.ntypes,
+                                     cfg.maxNeighborNum, float(cfg.Rmax), float(cfg.Rmax),
+                                     out_dtype=out_dtype)
+        lns.append(torch.where(ln > 0, ln + start, ln))
+        idrs.append(idr)
+        tms.append(tm)
+        cfg_of.append(torch.full((st.natoms,), c, dtype=torch.int64, device=dev))
+        start += st.natoms
+    batch = {"list_neigh": torch.cat(lns, 1).contiguous(),
+             "ImageDR": torch.cat(idrs, 1).contiguous(),
+             "type_map": torch.cat(tms).to(torch.int32).contiguous(),
+             "atom_type": list(cfg.atom_type),
+             "config_of_atom": torch.cat(cfg_of).contiguous(),
+             "natoms": torch.tensor([st.natoms for st in images], dtype=torch.int64, device=dev)}
+    assert batch["list_neigh"].shape == (1, start, S)
+    if energies is not None:
+        batch["Etot"] = torch.as_tensor(energies, dtype=torch.float64).to(dev).reshape(-1)
+    if forces is not None:
+        batch["Force"] = torch.cat([torch.as_tensor(f, dtype=torch.float64).to(dev).reshape(-1, 3)
+                                    for f in forces]).reshape(1, start, 3)
+    return batch
+
+
+def config_energies(Ei_atom: torch.Tensor, config_of_atom: torch.Tensor, nconfig: int) -> torch.Tensor:
+    """Per-configuration energy of a ragged batch: the sum of its atoms' energies."""
+    out = torch.zeros(nconfig, dtype=Ei_atom.dtype, device=Ei_atom.device)
+    return out.index_add(0, config_of_atom, Ei_atom.reshape(-1))

@@ -189,8 +189,12 @@ class DP(torch.nn.Module):
 
     @_lib.on_device
     def evaluate(self, list_neigh: torch.Tensor, Imagetype_map: torch.Tensor, present: List[int],
-                 ImageDR: torch.Tensor, nghost: int = 0, out: Optional[dict] = None):
-        """Raw fused evaluation: returns dict(Ei_atom [B,N], Etot [B] f64, Force, Virial [B,9] f64)."""
+                 ImageDR: torch.Tensor, nghost: int = 0, out: Optional[dict] = None,
+                 num_neigh: Optional[torch.Tensor] = None):
+        """Raw fused evaluation: returns dict(Ei_atom [B,N], Etot [B] f64, Force, Virial [B,9] f64).
+
+        ``num_neigh`` [B,N,ntypes] int32 (from ``find_neighbore(..., occupied_only=True)``)
+        gives the type blocks' lengths; the list's slots past them are then never read."""
         if not (list_neigh.is_cuda and ImageDR.is_cuda):
             raise _lib.MatplError("DP.evaluate takes CUDA tensors (no CPU fallback)")
         B, N, S = list_neigh.shape
@@ -211,14 +215,29 @@ class DP(torch.nn.Module):
         nbytes = lib.matpl_dp_workspace_bytes(self.code, B, N)
         ws = workspace(dev, nbytes, "dp")
         model = self._model_struct(present)
-        check(lib.matpl_dp_eval(self.code, ctypes.byref(model), B, N, S, nghost, ptr(ln), ptr(idr),
-                                ptr(tm), ptr(out["Ei_atom"]), ptr(out["Etot"]), ptr(out["Force"]),
-                                ptr(out["Virial"]), ptr(ws), ws.numel(),
-                                torch.cuda.current_stream(dev).cuda_stream), "matpl_dp_eval")
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        if num_neigh is None:
+            check(lib.matpl_dp_eval(self.code, ctypes.byref(model), B, N, S, nghost, ptr(ln),
+                                    ptr(idr), ptr(tm), ptr(out["Ei_atom"]), ptr(out["Etot"]),
+                                    ptr(out["Force"]), ptr(out["Virial"]), ptr(ws), ws.numel(),
+                                    stream), "matpl_dp_eval")
+        else:
+            nn = num_neigh if num_neigh.dtype == torch.int32 and num_neigh.is_contiguous() \
+                else num_neigh.to(torch.int32).contiguous()
+            if nn.numel() != B * N * self.cfg.ntypes:
+                raise _lib.MatplError("num_neigh must be [B, N, ntypes]")
+            check(lib.matpl_dp_eval_occupied(self.code, ctypes.byref(model), B, N, S, nghost,
+                                             ptr(ln), ptr(nn), ptr(idr), ptr(tm),
+                                             ptr(out["Ei_atom"]), ptr(out["Etot"]),
+                                             ptr(out["Force"]), ptr(out["Virial"]), ptr(ws),
+                                             ws.numel(), stream), "matpl_dp_eval_occupied")
         if self.check_errors:
             code = int(self.err.item())
             if code:
                 self.err.zero_()
+                if code == _lib.KERR_TIMEOUT:
+                    raise _lib.MatplError("matpl_dp_eval: a tensor-core completion wait gave up "
+                                          "(MATPL_KERR_TIMEOUT); the outputs are invalid")
                 raise _lib.MatplError(f"matpl_dp_eval kernel error code {code}")
         return out
 

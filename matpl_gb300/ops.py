@@ -204,14 +204,16 @@ def workspace(device: torch.device, nbytes: int, tag: str) -> torch.Tensor:
 def find_neighbore(type_maps: torch.Tensor, frac_position: torch.Tensor, lattice: torch.Tensor,
                    ntypes: int, m_neigh: int, Rc_M: float, Rc_type: Union[float, Sequence[float]],
                    out_dtype: torch.dtype = torch.float64, with_counts: bool = False,
-                   check_overflow: bool = True):
+                   check_overflow: bool = True, occupied_only: bool = False):
     """GPU DP neighbor search (dpuni_data_loader.py:595-650 + compute_Ri's r column).
 
     type_maps [N] 0-based types; frac_position [B,N,3] (or [N,3]) f64 fractional; lattice
     [B,3,3] (or [3,3]) f64 row vectors.  Returns list_neigh [B,N,ntypes*m] int32 (1-based,
     0 = empty) and ImageDR [B,N,ntypes*m,4] = (r, dx, dy, dz) (plus num_neigh [B,N,ntypes]
     when ``with_counts``).  Raises NeighborOverflow like the Fortran "stop" when
-    ``check_overflow`` (that reads one device flag and synchronises the stream)."""
+    ``check_overflow`` (that reads one device flag and synchronises the stream).
+    ``occupied_only`` writes only the occupied slots (the empty ones hold whatever the
+    fresh tensors held) and always returns the counts; pass them to ``DP.evaluate``."""
     _require_cuda(frac_position)
     dev = frac_position.device
     pos = frac_position.to(torch.float64)
@@ -228,14 +230,16 @@ def find_neighbore(type_maps: torch.Tensor, frac_position: torch.Tensor, lattice
     S = ntypes * m_neigh
     ln = torch.empty(B, N, S, dtype=torch.int32, device=dev)
     idr = torch.empty(B, N, S, 4, dtype=out_dtype, device=dev)
+    with_counts = with_counts or occupied_only
     cnt = torch.empty(B, N, ntypes, dtype=torch.int32, device=dev) if with_counts else None
     err = torch.zeros(1, dtype=torch.int32, device=dev)
     lib = _lib.load()
     nbytes = lib.matpl_neighbor_workspace_bytes(B, N)
     ws = workspace(dev, nbytes, "neighbor")
-    check(lib.matpl_neighbor_build(B, N, ntypes, m_neigh, float(Rc_M), rct_c, ptr(tm), ptr(lat),
-                                   ptr(pos), _DT[out_dtype], ptr(ln), ptr(idr), ptr(cnt), ptr(err),
-                                   ptr(ws), ws.numel(), _stream(dev)), "matpl_neighbor_build")
+    build = lib.matpl_neighbor_build_occupied if occupied_only else lib.matpl_neighbor_build
+    check(build(B, N, ntypes, m_neigh, float(Rc_M), rct_c, ptr(tm), ptr(lat), ptr(pos),
+                _DT[out_dtype], ptr(ln), ptr(idr), ptr(cnt), ptr(err), ptr(ws), ws.numel(),
+                _stream(dev)), "matpl_neighbor_build")
     if check_overflow:
         code = int(err.item())
         if code == _lib.KERR_NEIGHBOR_OVERFLOW:

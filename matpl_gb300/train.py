@@ -117,14 +117,29 @@ def dp_loss_prefactors(real_lr: float, start_lr: float = 0.001, pre_f=(1000.0, 1
     return f, e
 
 
+def _atom_order_energies(model: DPTrainModel, Ei: torch.Tensor, type_map: torch.Tensor,
+                         atom_type) -> torch.Tensor:
+    """Ei of DPTrainModel.forward (type-grouped, dp_dp.py:339) back in atom order."""
+    cfg = model.cfg
+    present = [cfg.atom_type.index(int(a)) for a in atom_type if int(a) in cfg.atom_type]
+    tl = type_map.long().reshape(-1)
+    order = torch.cat([torch.nonzero(tl == ti).flatten() for ti in present])
+    return Ei.new_zeros(tl.numel()).index_copy(0, order, Ei.reshape(-1))
+
+
 def loss_fn(model: DPTrainModel, batch: dict, w_f: float = 1.0, w_e: float = 1.0,
             per_atom_energy: bool = False):
     """Force-loss objective of one composition cluster: w_e * MSE(Etot) [/ natoms when
-    ``per_atom_energy``, as dp_loss does] + w_f * MSE(F)."""
+    ``per_atom_energy``, as dp_loss does] + w_f * MSE(F).  A ragged batch
+    (``data.ragged_batch``) takes the MSE over its configurations' energies."""
     Etot, Ei, F, V = model(batch["list_neigh"], batch["type_map"], batch["atom_type"],
                            batch["ImageDR"], 0)
     n = batch["list_neigh"].shape[1]
-    le = torch.nn.functional.mse_loss(Etot, batch["Etot"].to(Etot.dtype))
+    if "config_of_atom" in batch:
+        from .data import config_energies
+        Ei_atom = _atom_order_energies(model, Ei, batch["type_map"], batch["atom_type"])
+        Etot = config_energies(Ei_atom, batch["config_of_atom"], batch["Etot"].numel())
+    le = torch.nn.functional.mse_loss(Etot, batch["Etot"].to(Etot.dtype).reshape(Etot.shape))
     lf = torch.nn.functional.mse_loss(F[:, :n], batch["Force"].to(F.dtype))
     if per_atom_energy:
         le = le / n
@@ -428,10 +443,19 @@ class FusedTrainer:
         # 1. E, F with the current parameters
         self.evaluator.packed.copy_(_pack_device(model))
         r = self.evaluator.evaluate(ln32, tm32, present, idr, 0)
-        # 2. loss gradient w.r.t. E and F
-        Et = r["Etot"].to(model.dtype).reshape(B, 1).detach().requires_grad_()
+        # 2. loss gradient w.r.t. E and F (a ragged batch: E per configuration)
+        ragged = "config_of_atom" in batch
+        if ragged:
+            from .data import config_energies
+            cfg_of = batch["config_of_atom"]
+            C = batch["Etot"].numel()
+            Et = config_energies(r["Ei_atom"].to(model.dtype), cfg_of, C).detach().requires_grad_()
+            E_lab = batch["Etot"].to(model.dtype).reshape(C)
+        else:
+            Et = r["Etot"].to(model.dtype).reshape(B, 1).detach().requires_grad_()
+            E_lab = batch["Etot"].to(model.dtype).reshape(B, 1)
         Fo = r["Force"].detach().requires_grad_()
-        le = torch.nn.functional.mse_loss(Et, batch["Etot"].to(model.dtype).reshape(B, 1))
+        le = torch.nn.functional.mse_loss(Et, E_lab)
         lf = torch.nn.functional.mse_loss(Fo, batch["Force"].to(model.dtype))
         loss = w_e * le + w_f * lf
         gE, gF = torch.autograd.grad(loss, [Et, Fo])
@@ -454,7 +478,11 @@ class FusedTrainer:
             if n == 0:
                 continue
             e, ed = self._fit_dual(ti, D_all[o:o + B * n], Dd_all[o:o + B * n])
-            phi = phi + (gE.reshape(B, 1) * e.reshape(B, n)).sum() + ed.sum()
+            if ragged:          # dL/dE of each row's configuration
+                gr = gE.index_select(0, cfg_of.index_select(0, rows[o:o + n]))
+                phi = phi + (gr * e.reshape(-1)).sum() + ed.sum()
+            else:
+                phi = phi + (gE.reshape(B, 1) * e.reshape(B, n)).sum() + ed.sum()
         phi.backward()
         return loss.detach(), le.detach(), lf.detach()
 
@@ -487,8 +515,11 @@ class GraphedTrainer:
         self.w_f, self.w_e, self.warmup = w_f, w_e, warmup
         self.graphs = {}
 
+    def _keys(self, batch):
+        return self.KEYS + (("config_of_atom",) if "config_of_atom" in batch else ())
+
     def _capture(self, batch):
-        static = {k: batch[k].clone() for k in self.KEYS}
+        static = {k: batch[k].clone() for k in self._keys(batch)}
         static["atom_type"] = list(batch["atom_type"])
         side = torch.cuda.Stream()
         side.wait_stream(torch.cuda.current_stream())
@@ -506,11 +537,12 @@ class GraphedTrainer:
         return g, static, loss
 
     def step(self, batch):
-        key = tuple(tuple(batch[k].shape) for k in self.KEYS) + (tuple(batch["atom_type"]),)
+        keys = self._keys(batch)
+        key = tuple(tuple(batch[k].shape) for k in keys) + (tuple(batch["atom_type"]),)
         if key not in self.graphs:
             self.graphs[key] = self._capture(batch)
         g, static, loss = self.graphs[key]
-        for k in self.KEYS:
+        for k in keys:
             if batch[k].data_ptr() != static[k].data_ptr():
                 static[k].copy_(batch[k], non_blocking=True)
         g.replay()
