@@ -390,34 +390,51 @@ def run_nep(args, ws, local, steps, warmup, sample_clocks=True):
 
 
 TRAIN_METRIC = "DP force-loss training step atom-steps/s, fused vs plain FP32"
+# force-loss training batch: 64 Hf:O (1:2) configurations with atom counts drawn uniformly in
+# [32, 512], random-packed at 0.07 atoms/A^3 with a 3 % symmetric cell strain, the headline's
+# nets (m = 100 per type), labels from a teacher net (other seed) + N(0, 0.01) noise
+TRAIN_CONFIGS, TRAIN_NMIN, TRAIN_NMAX, TRAIN_DENSITY, TRAIN_STRAIN = 64, 32, 512, 0.07, 0.03
+TRAIN_SEED = 303
+
+
+def train_workload(dev, nconf=TRAIN_CONFIGS, seed=TRAIN_SEED):
+    """The ragged training batch and its labels (teacher net of the same architecture)."""
+    from matpl_gb300 import data, dp, params as P, structures
+    rng = np.random.default_rng(seed)
+    counts = rng.integers(TRAIN_NMIN, TRAIN_NMAX + 1, nconf)
+    sts = [structures.random_packed(int(n), TRAIN_DENSITY, [72, 8], [1 / 3, 2 / 3],
+                                    seed=seed + 1 + k, strain=TRAIN_STRAIN)
+           for k, n in enumerate(counts)]
+    cfg = P.DPConfig(atom_type=[72, 8], maxNeighborNum=100, Rmax=RC, Rmin=RMIN)
+    batch = data.ragged_batch(cfg, sts, device=dev)
+    ln, idr = batch["list_neigh"], batch["ImageDR"]
+    davg, dstd = P.calc_stat(cfg, ln.cpu().numpy(), idr.cpu().numpy(),
+                             batch["type_map"].cpu().numpy())
+    teacher = dp.DP(cfg, P.init_params(cfg, SEED_W + 100), davg, dstd, precision="float64",
+                    device=dev)
+    present = teacher.present_types(cfg.atom_type)
+    lab = teacher.evaluate(ln, batch["type_map"], present, idr, 0)
+    g = torch.Generator(device=dev).manual_seed(5)
+    E = data.config_energies(lab["Ei_atom"], batch["config_of_atom"], nconf)
+    batch["Etot"] = (E + 0.01 * torch.randn(E.shape, generator=g, device=dev,
+                                            dtype=torch.float64)).float()
+    batch["Force"] = (lab["Force"] + 0.01 * torch.randn(lab["Force"].shape, generator=g,
+                                                         device=dev, dtype=torch.float64)).float()
+    batch["ImageDR"] = idr.float()
+    return cfg, batch, davg, dstd, counts
 
 
 def run_train(args, ws, local, steps, warmup, plain_steps):
-    """Force-loss training step (E-MSE + F-MSE, Adam) on the headline's Li/Si box: the fused
-    step (fused E/F, hand-written embedding double-backward, torch fitting part) against the
-    plain step (env matrix + torch nets + second-order autograd through this library's
-    force / virial ops, the reference's structure), both FP32.  Labels come from a teacher net of
-    the same architecture (other seed) plus N(0, 0.01) noise."""
-    from matpl_gb300 import _lib, dp, ops, params as P, train
+    """Force-loss training step (E-MSE over the configurations + F-MSE, Adam) on the ragged
+    batch of 64 uneven Hf:O configurations (one concatenated image, no per-composition
+    clusters): the fused step (fused E/F, hand-written embedding double-backward, torch fitting
+    part) against the plain step (env matrix + torch nets + second-order autograd through this
+    library's force / virial ops, the reference's structure), both FP32."""
+    from matpl_gb300 import _lib, params as P, train
     dev = torch.device("cuda", local)
-    st, cfg, prm = make_workload(args.train_atoms)
-    natoms = st.natoms
-    types_d = torch.tensor(st.types, device=dev)
-    ln, idr = ops.find_neighbore(types_d, torch.tensor(st.frac, device=dev),
-                                 torch.tensor(st.lattice, device=dev), 2, M_NEIGH, RC, RC)
-    sub = slice(0, 4000)
-    davg, dstd = P.calc_stat(cfg, ln[:, sub].cpu().numpy(), idr[:, sub].cpu().numpy(), st.types[sub])
-    teacher = dp.DP(cfg, P.init_params(cfg, SEED_W + 100), davg, dstd, precision="float64", device=dev)
-    present = teacher.present_types(cfg.atom_type)
-    lab = teacher.evaluate(ln, types_d.to(torch.int32), present, idr, 0)
-    g = torch.Generator(device=dev).manual_seed(5)
-    batch = {"list_neigh": ln, "type_map": types_d, "atom_type": cfg.atom_type,
-             "ImageDR": idr.float(),
-             "Etot": (lab["Etot"] + 0.01 * torch.randn(1, generator=g, device=dev,
-                                                       dtype=torch.float64)).reshape(1, 1).float(),
-             "Force": (lab["Force"] + 0.01 * torch.randn(lab["Force"].shape, generator=g, device=dev,
-                                                          dtype=torch.float64)).float()}
-    del teacher, lab
+    cfg, batch, davg, dstd, counts = train_workload(dev, args.train_configs)
+    natoms = int(counts.sum())
+    prm = P.init_params(cfg, SEED_W)
 
     def timed(step, n, w):
         for _ in range(w):
@@ -461,13 +478,29 @@ def run_train(args, ws, local, steps, warmup, plain_steps):
         a, b = m1.param(k).grad, m2.param(k).grad
         worst = max(worst, ((a - b).abs().max() / (b.abs().max() + 1e-30)).item())
     per_kernel = {k: {"ms_per_launch": v[0] / v[1], "launches": v[1]} for k, v in prof.items()}
+    pairs = int((batch["list_neigh"] > 0).sum())
+    # roofline of the dominant library kernel: the embedding double-backward recomputes the
+    # forward and runs the reverse of the tangent pass, ~6.6 kflop per occupied pair
+    roof = None
+    if "dp_dual_bwd" in per_kernel:
+        t = per_kernel["dp_dual_bwd"]["ms_per_launch"] * 1e-3
+        ach = 6600.0 * pairs / t / 1e12
+        simt_peak = sm_count() * 128 * 2 * 2070.0 * 1e6 / 1e12
+        roof = {"kernel": "dp_dual_bwd", "bound": "simt fp32", "achieved": ach,
+                "peak": simt_peak, "unit": "TFLOP/s", "frac": ach / simt_peak,
+                "peak_source": "nominal FP32 SIMT at 2070 MHz",
+                "algorithmic_flops_per_launch": 6600.0 * pairs}
     return {
         "metric": TRAIN_METRIC, "value": ws * natoms / (fused_ms * 1e-3), "unit": "atom-steps/s",
         "ms_per_step": fused_ms, "steps": steps, "warmup": warmup, "dtype": "f32",
-        "config": {"workload": f"DP se_e2_a force-loss training step (E-MSE + F-MSE, Adam), "
-                               f"{natoms:,}-atom Li/Si box of the headline's density, m=150/type, "
-                               "teacher labels",
-                   "natoms": natoms,
+        "config": {"workload": f"DP se_e2_a force-loss training step (E-MSE + F-MSE, Adam) on a "
+                               f"ragged batch of {TRAIN_CONFIGS} Hf:O configurations, atom counts "
+                               f"U[{TRAIN_NMIN}, {TRAIN_NMAX}] ({natoms:,} atoms), "
+                               f"{TRAIN_DENSITY} atoms/A^3, {TRAIN_STRAIN:.0%} cell strain, m=100/type, "
+                               "teacher labels + N(0, 0.01)",
+                   "natoms": natoms, "pairs": pairs, "configurations": TRAIN_CONFIGS,
+                   "batching": "one concatenated image (data.ragged_batch), energies per "
+                               "configuration",
                    "plain_fp32": {"form": "env matrix + torch nets + second-order autograd through "
                                           "this library's force / virial ops",
                                   "ms_per_step": plain_ms, "value": ws * natoms / (plain_ms * 1e-3),
@@ -477,7 +510,7 @@ def run_train(args, ws, local, steps, warmup, plain_steps):
                               "Adam) in one CUDA graph, replayed per step",
                    "speedup_vs_plain_fp32": plain_ms / fused_ms,
                    "gradient_max_rel_diff_fused_vs_plain": worst},
-        "kernels": per_kernel,
+        "kernels": per_kernel, "roofline": roof,
     }
 
 
@@ -1354,8 +1387,8 @@ def main():
     ap.add_argument("--no-md", action="store_true", help="skip the batched-replica MD workload")
     ap.add_argument("--no-tune", action="store_true",
                     help="keep the automatic tile shape of the mixed kernels (no autotuning)")
-    ap.add_argument("--train-atoms", type=int, default=NATOMS,
-                    help="atoms of the training box (32,000; smaller for profiling captures)")
+    ap.add_argument("--train-configs", type=int, default=TRAIN_CONFIGS,
+                    help="configurations of the ragged training batch (64; fewer for captures)")
     ap.add_argument("--nep-atoms", type=int, default=NEP_NATOMS,
                     help="atoms of the NEP box (the benchmark is 100,000; smaller boxes of the "
                          "same density and model are for profiling captures)")

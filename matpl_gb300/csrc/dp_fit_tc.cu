@@ -2,14 +2,16 @@
 //
 // Same math as dp_fused.cu's dp_fit (src/model/dp_embedding.py:140-163 and dp_dp.py:304-342 plus
 // the autograd adjoint down to dE/dA): per atom D = A^T A[:, :16] (400), Ei = fit(D), dE/dA.
-// A CTA of 128 threads owns a tile of 128 atoms (thread r = atom r, MMA M = 128):
+// Atoms are first sorted by element (fit_order, a stable counting sort), so that a CTA of 128
+// threads owns a tile of 128 atoms of one element (thread r = atom r, MMA M = 128) and runs
+// that element's net only:
 //
 //   layer 1  h1 = D W0: 13 K-chunks of 32; each chunk of D is built on the SIMT cores from the
 //            atom's A (kept in shared memory) and double-buffered into the MMA (N = 64, the 50
 //            outputs padded), FP32 accumulator in 64 TMEM columns.
 //   layers 2, 3 (50 x 50 padded to 64 x 64) and the two transposed GEMMs of the adjoint run as
-//            single MMAs (K = 64); tanh / residual / bias on SIMT; tanh outputs kept in shared
-//            memory for the adjoint.
+//            single MMAs (K = 64); tanh / residual / bias on SIMT; the three layers' tanh
+//            outputs are stashed in TMEM (tcgen05.st) for the adjoint.
 //   dE/dD = g1 W0^T (N = 400) in 7 chunks of 64 columns, each consumed straight from TMEM into
 //            dE/dA = sum_q dD[p][q] A[c][q] + sum_p' dD[p'][p] A[c][p'].
 // BF16x3 (hi/lo split) operands keep FP32-level accuracy; weight tiles are prepared once per
@@ -162,61 +164,128 @@ __device__ __forceinline__ float fit_act(float x) {
     return tanhf(x);
 }
 
-constexpr size_t FIT_SMEM = sizeof(float) * (FM * ASTR + 3 * F * FM) + 2 * X64 + 2 * W64;
+constexpr size_t FIT_SMEM = sizeof(float) * (FM * ASTR) + 2 * X64 + 2 * W64;
+constexpr int FIT_TCOLS = 256;   // TMEM: [0, 64) accumulator, [64 + 64 l, 128 + 64 l) tanh of layer l
+
+// Stable counting sort of the atoms of one image by model type into order[natoms], with
+// type_start[0..ntypes+1] (bucket ntypes: atoms whose type is not evaluated).  One block.
+__global__ void fit_order(const int32_t *__restrict__ type_map, int natoms, int ntypes,
+                          int present_mask, int *__restrict__ order, int *__restrict__ type_start) {
+    __shared__ int wsum[32];
+    __shared__ int base[18];
+    __shared__ int tot;
+    const int T = ntypes + 1;
+    const int per = (natoms + blockDim.x - 1) / blockDim.x;
+    const int a0 = threadIdx.x * per, a1 = min(natoms, a0 + per);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    auto bucket = [&](int i) {
+        const int t = type_map[i];
+        return (t >= 0 && t < ntypes && ((present_mask >> t) & 1)) ? t : ntypes;
+    };
+    int off[17];
+    if (threadIdx.x == 0) base[0] = 0;
+    for (int q = 0; q < T; ++q) {
+        int c = 0;
+        for (int i = a0; i < a1; ++i) c += bucket(i) == q;
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) wsum[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            int w = lane < nw ? wsum[lane] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            if (lane < nw) wsum[lane] = w - (lane < nw ? wsum[lane] : 0);   // exclusive
+            if (lane == nw - 1) tot = w;
+        }
+        __syncthreads();
+        off[q] = wsum[warp] + incl - c;
+        if (threadIdx.x == 0) base[q + 1] = base[q] + tot;
+        __syncthreads();
+    }
+    for (int i = a0; i < a1; ++i) {
+        const int q = bucket(i);
+        int o = 0;
+#pragma unroll
+        for (int k = 0; k < 17; ++k)
+            if (k == q) o = off[k]++;
+        order[base[q] + o] = i;
+    }
+    if (threadIdx.x <= T) type_start[threadIdx.x] = base[threadIdx.x];
+}
+
+__device__ __forceinline__ void st64(uint32_t taddr, const float v[64]) {
+    tc::tmem_st32(taddr, v);
+    tc::tmem_st32(taddr + 32, v + 32);
+}
 
 template <bool FAST>
-__global__ void __launch_bounds__(FM, 1)
-dp_fit_tc(const float *__restrict__ Ain, const int32_t *__restrict__ type_map,
-          const float *__restrict__ params, const unsigned char *__restrict__ ftiles,
-          float *__restrict__ Ei, float *__restrict__ dAout, int32_t *__restrict__ err,
-          int batch, int natoms, int ntypes, int present_mask) {
+__global__ void __launch_bounds__(FM, 2)
+dp_fit_tc(const float *__restrict__ Ain, const int *__restrict__ order,
+          const int *__restrict__ type_start, const float *__restrict__ params,
+          const unsigned char *__restrict__ ftiles, float *__restrict__ Ei,
+          float *__restrict__ dAout, int32_t *__restrict__ err, int batch, int natoms,
+          int ntypes) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t mbar[2];
     __shared__ uint32_t tmem_base;
-    __shared__ int rtype[FM];
-    __shared__ int tflag[16];
+    __shared__ long long ratom[FM];
     __shared__ float vec[6 * FN + 4];
     float *As = reinterpret_cast<float *>(smem_raw);
-    float *Tsm = As + FM * ASTR;                                   // [3][F][FM]
-    unsigned char *XB = reinterpret_cast<unsigned char *>(Tsm + 3 * F * FM);
+    unsigned char *XB = reinterpret_cast<unsigned char *>(As + FM * ASTR);
     unsigned char *WB = XB + 2 * X64;
     const int r = threadIdx.x, warp = r >> 5;
     if (r == 0) {
         tc::mbar_init(&mbar[0], 1);
         tc::mbar_init(&mbar[1], 1);
     }
-    if (warp == 0) tc::tmem_alloc(&tmem_base, 64);
+    if (warp == 0) tc::tmem_alloc(&tmem_base, FIT_TCOLS);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = tmem_base;
+    const uint32_t lane_q = (uint32_t)(warp * 32) << 16;
     uint32_t ph[2] = {0u, 0u};
     bool ok = true;
-    const long long total = (long long)batch * natoms;
-    const long long ntiles = (total + FM - 1) / FM;
     const long long woff = (long long)ntypes * ntypes * EmbOff::SIZE;
     const int vsrc[6] = {FitOff::B0, FitOff::B1, FitOff::DT1, FitOff::B2, FitOff::DT2, FitOff::W3};
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const long long t0 = tile * FM, t = t0 + r;
-        const bool valid = t < total;
-        __syncthreads();
-        if (r < 16) tflag[r] = 0;
-        __syncthreads();
-        int ty = -1;
-        if (valid) {
-            ty = type_map[(int)(t % natoms)];
-            if (ty < 0 || ty >= ntypes || !((present_mask >> ty) & 1)) ty = -1;
+    // tiles: per image, ceil(n_t / 128) tiles of each element t (an upper bound of their number
+    // per image is ceil(natoms / 128) + ntypes; the surplus indices have no work)
+    const long long tiles_b = (natoms + FM - 1) / FM + ntypes;
+    for (long long v = blockIdx.x; v < (long long)batch * tiles_b; v += gridDim.x) {
+        const long long b = v / tiles_b;
+        int rem = (int)(v - b * tiles_b), tt = -1, chunk = 0;
+        for (int q = 0; q < ntypes; ++q) {
+            const int nq = (type_start[q + 1] - type_start[q] + FM - 1) / FM;
+            if (rem < nq) {
+                tt = q;
+                chunk = rem;
+                break;
+            }
+            rem -= nq;
         }
-        rtype[r] = ty;
-        if (ty >= 0) tflag[ty] = 1;
+        if (tt < 0) continue;                      // the same for every thread of the CTA
+        const int idx = type_start[tt] + chunk * FM + r;
+        const bool valid = idx < type_start[tt + 1];
+        const long long t = valid ? b * natoms + order[idx] : -1;
+        __syncthreads();
+        ratom[r] = t;
+        __syncthreads();
         for (int q = r; q < FM * NA; q += FM) {
             const int row = q / NA, e = q - row * NA;
-            As[row * ASTR + e] = (t0 + row < total) ? Ain[(t0 + row) * NA + e] : 0.f;
+            const long long tr = ratom[row];
+            As[row * ASTR + e] = tr >= 0 ? Ain[tr * NA + e] : 0.f;
         }
         __syncthreads();
         const float *a = As + r * ASTR;
-        for (int tt = 0; tt < ntypes; ++tt) {
-            if (!tflag[tt]) continue;
+        {
             const float *fw = params + woff + (long long)tt * FitOff::SIZE;
             const unsigned char *tw = ftiles + (size_t)tt * FIT_TILE_BYTES;
             __syncthreads();
@@ -226,7 +295,7 @@ dp_fit_tc(const float *__restrict__ Ain, const int32_t *__restrict__ type_map,
             }
             if (r == 0) vec[6 * FN] = fw[FitOff::B3];
             __syncthreads();
-            const bool mine = valid && rtype[r] == tt;
+            const bool mine = valid;
             // ---- layer 1: 13 double-buffered K chunks of D W0
             for (int c = 0; c < K1C; ++c) {
                 const int b = c & 1;
@@ -259,10 +328,8 @@ dp_fit_tc(const float *__restrict__ Ain, const int32_t *__restrict__ type_map,
             float h[64], x[64];
             ld64(tmem, h);
 #pragma unroll
-            for (int o = 0; o < 64; ++o) {
-                x[o] = o < F ? fit_act<FAST>(h[o] + vec[o]) : 0.f;
-                if (o < F) Tsm[o * FM + r] = x[o];
-            }
+            for (int o = 0; o < 64; ++o) x[o] = o < F ? fit_act<FAST>(h[o] + vec[o]) : 0.f;
+            st64(tmem + 64 + lane_q, x);
             // ---- layers 2, 3
 #pragma unroll 1
             for (int l = 1; l <= 2; ++l) {
@@ -279,13 +346,12 @@ dp_fit_tc(const float *__restrict__ Ain, const int32_t *__restrict__ type_map,
                 ld64(tmem, h);
                 const float *bias = vec + (l == 1 ? FN : 3 * FN);
                 const float *dt = vec + (l == 1 ? 2 * FN : 4 * FN);
-                float *T = Tsm + l * F * FM;
 #pragma unroll
-                for (int o = 0; o < F; ++o) {
-                    const float tv = fit_act<FAST>(h[o] + bias[o]);
-                    T[o * FM + r] = tv;
-                    x[o] = tv * dt[o] + x[o];
+                for (int o = 0; o < 64; ++o) {
+                    h[o] = o < F ? fit_act<FAST>(h[o] + bias[o]) : 0.f;
+                    if (o < F) x[o] = h[o] * dt[o] + x[o];
                 }
+                st64(tmem + 64 + 64 * l + lane_q, h);
             }
             float e = vec[6 * FN];
 #pragma unroll
@@ -296,13 +362,10 @@ dp_fit_tc(const float *__restrict__ Ain, const int32_t *__restrict__ type_map,
             for (int o = 0; o < F; ++o) x[o] = vec[5 * FN + o];
 #pragma unroll 1
             for (int l = 2; l >= 1; --l) {
-                const float *T = Tsm + l * F * FM;
                 const float *dt = vec + (l == 2 ? 4 * FN : 2 * FN);
+                ld64(tmem + 64 + 64 * l, h);          // tanh outputs of layer l
 #pragma unroll
-                for (int o = 0; o < 64; ++o) {
-                    const float tv = o < F ? T[o * FM + r] : 0.f;
-                    h[o] = o < F ? x[o] * dt[o] * (1.f - tv * tv) : 0.f;
-                }
+                for (int o = 0; o < 64; ++o) h[o] = o < F ? x[o] * dt[o] * (1.f - h[o] * h[o]) : 0.f;
                 store_row_hilo<64>(XB, XB + X64, r, h);
                 copy_tiles(tw + (l == 2 ? OFF_B2 : OFF_B1), WB, 2 * W64);
                 mma_sync_point();
@@ -317,11 +380,9 @@ dp_fit_tc(const float *__restrict__ Ain, const int32_t *__restrict__ type_map,
 #pragma unroll
                 for (int o = 0; o < F; ++o) x[o] += h[o];
             }
+            ld64(tmem + 64, h);                       // tanh outputs of layer 1
 #pragma unroll
-            for (int o = 0; o < 64; ++o) {
-                const float tv = o < F ? Tsm[o * FM + r] : 0.f;
-                h[o] = o < F ? x[o] * (1.f - tv * tv) : 0.f;
-            }
+            for (int o = 0; o < 64; ++o) h[o] = o < F ? x[o] * (1.f - h[o] * h[o]) : 0.f;
             store_row_hilo<64>(XB, XB + X64, r, h);
             // ---- dE/dD = g1 W0^T in 7 chunks of 64 D entries, folded into dE/dA
             float acc2[4][16];
@@ -365,20 +426,30 @@ dp_fit_tc(const float *__restrict__ Ain, const int32_t *__restrict__ type_map,
                     for (int q = 0; q < M2; ++q) dAout[t * NA + c4 * E + q] += acc2[c4][q];
             }
         }
-        if (valid && rtype[r] < 0) {
-            Ei[t] = 0.f;
-            for (int q = 0; q < NA; ++q) dAout[t * NA + q] = 0.f;
-        }
+    }
+    // atoms whose element is not evaluated: Ei = 0, dE/dA = 0
+    const int nskip = type_start[ntypes + 1] - type_start[ntypes];
+    for (long long q = (long long)blockIdx.x * FM + r; q < (long long)batch * nskip;
+         q += (long long)gridDim.x * FM) {
+        const long long b = q / nskip;
+        const long long t = b * natoms + order[type_start[ntypes] + (int)(q - b * nskip)];
+        Ei[t] = 0.f;
+        for (int e = 0; e < NA; ++e) dAout[t * NA + e] = 0.f;
     }
     if (!ok) atomicMax(err, MATPL_KERR_TIMEOUT);
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, 64);
+    if (warp == 0) tc::tmem_dealloc(tmem, FIT_TCOLS);
 }
 
 }  // namespace
 
-size_t fit_tile_bytes(int ntypes) { return (size_t)ntypes * FIT_TILE_BYTES; }
+// Prepared tiles of every element, then the element order of the atoms (order [natoms],
+// type_start [ntypes + 2]).
+size_t fit_tile_bytes(int ntypes, int natoms) {
+    return align_up((size_t)ntypes * FIT_TILE_BYTES, 256) + align_up(sizeof(int) * natoms, 256) +
+           sizeof(int) * 32;
+}
 
 // Prepares the BF16 fitting tiles of every type into `tiles`, then runs the fitting kernel.
 int launch_fit_tc(bool fast, const float *A, const int32_t *type_map, const float *params,
@@ -389,14 +460,21 @@ int launch_fit_tc(bool fast, const float *A, const int32_t *type_map, const floa
         const long long n = (long long)ntypes * (K1C * 32 + NDC * 64 + 4 * 64) * FN;
         prep_fit_tiles<<<(int)((n + 255) / 256), 256, 0, s>>>(params, tiles, ntypes);
     }
-    const long long total = (long long)batch * natoms;
-    const long long ntiles = (total + FM - 1) / FM;
-    const int grid = (int)(ntiles < device_sms() ? ntiles : device_sms());
+    int *order = reinterpret_cast<int *>(tiles + align_up((size_t)ntypes * FIT_TILE_BYTES, 256));
+    int *type_start = order + align_up(sizeof(int) * natoms, 256) / sizeof(int);
+    {
+        ProfScope ps("fit_order", s);
+        fit_order<<<1, 1024, 0, s>>>(type_map, natoms, ntypes, present_mask, order, type_start);
+    }
+    const long long tiles_b = (natoms + FM - 1) / FM + ntypes;
+    const long long ntiles = (long long)batch * tiles_b;
+    const long long cap = 2LL * device_sms();            // two resident CTAs per SM
+    const int grid = (int)(ntiles < cap ? ntiles : cap);
     auto k = fast ? dp_fit_tc<true> : dp_fit_tc<false>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FIT_SMEM);
     ProfScope ps("dp_fit_tc", s);
-    k<<<grid, FM, FIT_SMEM, s>>>(A, type_map, params, tiles, Ei, dA, err, batch, natoms, ntypes,
-                                 present_mask);
+    k<<<grid, FM, FIT_SMEM, s>>>(A, order, type_start, params, tiles, Ei, dA, err, batch, natoms,
+                                 ntypes);
     return check_launch("dp_fit_tc");
 }
 

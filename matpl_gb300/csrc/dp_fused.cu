@@ -27,7 +27,7 @@ int mixed_ga(int S);
 size_t mixed_smem(int ntypes, int S);
 size_t mixed_tile_bytes(int ntypes);
 int prep_mixed_tiles(const float *params, unsigned char *out, int ntypes, cudaStream_t s);
-size_t fit_tile_bytes(int ntypes);
+size_t fit_tile_bytes(int ntypes, int natoms);
 int launch_fit_tc(bool fast, const float *A, const int32_t *type_map, const float *params,
                   unsigned char *tiles, float *Ei, float *dA, int32_t *err, int batch, int natoms,
                   int ntypes, int present_mask, cudaStream_t s);
@@ -727,7 +727,7 @@ DpLayout dp_layout(size_t es, int batch, int natoms, int ntypes) {
     l.vir = o; o = align_up(o + 8 * na * 9, 256);
     l.red = o; o = align_up(o + 8 * (size_t)batch * kReduceBlocks * 10, 256);
     l.tiles = o; o = align_up(o + mixed_tile_bytes(ntypes), 256);
-    l.ftiles = o; o = align_up(o + fit_tile_bytes(ntypes), 256);
+    l.ftiles = o; o = align_up(o + fit_tile_bytes(ntypes, natoms), 256);
     l.total = o;
     return l;
 }

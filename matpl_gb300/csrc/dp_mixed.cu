@@ -44,6 +44,7 @@ constexpr int WKS = KP / 8 * 128;       // K-chunk stride of a weight tile (512 
 constexpr int XT = TM * KP * 2;         // activation tile bytes (8 KB)
 constexpr int WT = KP * KP * 2;         // weight tile bytes (2 KB)
 constexpr int RT = 128 * TM * 2;        // contraction A operand: 128 (M) x 128 (K) bf16 (32 KB)
+constexpr int ET = 64 * TM * 2;         // one-hot A operand of the backward: 64 (M) x 128 (K)
 constexpr int OLBO = 128;               // MN-major operands: K-group stride
 constexpr int OSBO = TM / 8 * 128;      //                    MN-group stride (2048 B)
 constexpr int QN = 16;                  // per-row reduction values (f: 3, f x r: 9, 4 zero)
@@ -64,9 +65,9 @@ struct MixParams {
 };
 
 struct MixSmem {
-    unsigned char *wt;     // weight tiles of the current net: fw1 h/l, fw2 h/l (, bw2 h/l, bw1 h/l)
+    unsigned char *wt;     // weight tiles of the current net: fw1 h/l, fw2 h/l
     unsigned char *xh, *xl;
-    unsigned char *rop;    // fwd: contraction A operand; bwd: one-hot A operand
+    unsigned char *rop;    // fwd: contraction A operand (M = 128); bwd: one-hot A operand (M = 64)
     unsigned char *qh, *ql;   // bwd: per-row reduction values (MN-major B operand)
     float *vec;            // [4][VW] of the current net: W0, b0, dt1, dt2
     float *dA;             // bwd: [GAMAX][E] float4 (c fastest) of dE/dA * k
@@ -79,8 +80,8 @@ struct MixSmem {
 
 __host__ __device__ inline size_t mix_smem_bytes(bool bwd, int S, int ga) {
     size_t o = 0;
-    o += (bwd ? 8 : 4) * WT;
-    o += 2 * XT + RT;
+    o += 4 * WT;
+    o += 2 * XT + (bwd ? ET : RT);
     if (bwd) o += 2 * QT;
     o += sizeof(float) * 4 * VW;
     if (bwd) o += sizeof(float) * GAMAX * E * 4;
@@ -92,10 +93,10 @@ __host__ __device__ inline size_t mix_smem_bytes(bool bwd, int S, int ga) {
 __device__ MixSmem carve(unsigned char *base, bool bwd, int S, int ga) {
     MixSmem m;
     size_t o = 0;
-    m.wt = base + o; o += (bwd ? 8 : 4) * WT;
+    m.wt = base + o; o += 4 * WT;
     m.xh = base + o; o += XT;
     m.xl = base + o; o += XT;
-    m.rop = base + o; o += RT;
+    m.rop = base + o; o += bwd ? ET : RT;
     m.qh = m.ql = nullptr;
     if (bwd) { m.qh = base + o; o += QT; m.ql = base + o; o += QT; }
     m.vec = reinterpret_cast<float *>(base + o); o += sizeof(float) * 4 * VW;
@@ -132,44 +133,39 @@ __device__ __forceinline__ void switch_f(float R, float rmin, float rmax, float 
     }
 }
 
-// The 8 BF16 weight tiles (hi / lo) of every net, prepared once per call in global memory:
-// fw1[n=o][k=i] = W1[i][o] with row k = 25 the bias b1[o], fw2 likewise with b2,
-// bw2[n=i][k=o] = W2[i][o], bw1[n=i][k=o] = W1[i][o] (row 25 zero); zero elsewhere.
-// Layout [net][8][WT bytes]: fw1 h, fw1 l, fw2 h, fw2 l, bw2 h, bw2 l, bw1 h, bw1 l.
+// The 4 BF16 weight tiles (hi / lo) of every net, prepared once per call in global memory:
+// fw1[n=o][k=i] = W1[i][o] with row k = 25 the bias b1[o], fw2 likewise with W2 and b2; zero
+// elsewhere.  Layout [net][4][WT bytes]: fw1 h, fw1 l, fw2 h, fw2 l.  The backward's
+// transposed products read the same tiles as MN-major B operands (n = i, k = o): the bias
+// row then lands in output column 25, which nothing reads.
 __global__ void prep_weight_tiles(const float *__restrict__ params, unsigned char *__restrict__ out,
                                   int nnet) {
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nnet * 4 * KP * KP;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nnet * 2 * KP * KP;
          q += gridDim.x * blockDim.x) {
-        const int k = q / (4 * KP * KP), rr = q - k * 4 * KP * KP;
+        const int k = q / (2 * KP * KP), rr = q - k * 2 * KP * KP;
         const int mat = rr / (KP * KP), rem = rr - mat * KP * KP;
         const int n = rem / KP, kk = rem - (rem / KP) * KP;
         const float *w = params + (long long)k * EmbOff::SIZE;
         float v = 0.f;
-        if (n < E && kk < E) {
-            switch (mat) {
-                case 0: v = w[EmbOff::W1 + kk * E + n]; break;   // fw1: W1[i=kk][o=n]
-                case 1: v = w[EmbOff::W2 + kk * E + n]; break;   // fw2
-                case 2: v = w[EmbOff::W2 + n * E + kk]; break;   // bw2: W2[i=n][o=kk]
-                default: v = w[EmbOff::W1 + n * E + kk]; break;  // bw1
-            }
-        } else if (n < E && kk == ONE && mat < 2) {
+        if (n < E && kk < E)
+            v = w[(mat == 0 ? EmbOff::W1 : EmbOff::W2) + kk * E + n];   // W[i=kk][o=n]
+        else if (n < E && kk == ONE)
             v = w[(mat == 0 ? EmbOff::B1 : EmbOff::B2) + n];
-        }
         const __nv_bfloat16 hi = __float2bfloat16_rn(v);
         const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
-        unsigned char *base = out + (size_t)k * 8 * WT;
+        unsigned char *base = out + (size_t)k * 4 * WT;
         *reinterpret_cast<__nv_bfloat16 *>(base + (2 * mat) * WT + tc::tile_off(n, kk, WKS)) = hi;
         *reinterpret_cast<__nv_bfloat16 *>(base + (2 * mat + 1) * WT + tc::tile_off(n, kk, WKS)) = lo;
     }
 }
 
-// Weight tiles (the first `ntiles` of the net's 8) and the per-net vectors of net k.
+// The 4 weight tiles and the per-net vectors of net k.
 __device__ __forceinline__ void load_net(const unsigned char *__restrict__ wsrc,
-                                         const float *__restrict__ params, int k, int ntiles,
+                                         const float *__restrict__ params, int k,
                                          const MixSmem &sm) {
-    const uint4 *s4 = reinterpret_cast<const uint4 *>(wsrc + (size_t)k * 8 * WT);
+    const uint4 *s4 = reinterpret_cast<const uint4 *>(wsrc + (size_t)k * 4 * WT);
     uint4 *d4 = reinterpret_cast<uint4 *>(sm.wt);
-    for (int q = threadIdx.x; q < ntiles * WT / 16; q += blockDim.x) d4[q] = __ldg(s4 + q);
+    for (int q = threadIdx.x; q < 4 * WT / 16; q += blockDim.x) d4[q] = __ldg(s4 + q);
     const float *w = params + (long long)k * EmbOff::SIZE;
     for (int q = threadIdx.x; q < 4 * VW; q += blockDim.x) {
         const int part = q / VW, o = q - part * VW;
@@ -204,14 +200,18 @@ __device__ __forceinline__ uint32_t mn_chunk(int r, int g) {
     return (uint32_t)((r & 7) * 16 + (r >> 3) * OLBO + g * OSBO);
 }
 
-// D[128 x 32] (+)= X W for the weight tile pair `mat`; one thread issues, then commits.
+// D[128 x 32] (+)= X W for weight tile pair `mat` (0: layer 2, 1: layer 3), or X W^T with
+// `transposed` (the same tiles read MN-major); one thread issues, then commits.
 template <int SPLIT>
 __device__ __forceinline__ void issue_layer(const MixSmem &sm, uint32_t tmem, int mat,
-                                            uint64_t *mbar) {
-    const uint32_t id = tc::idesc_bf16(TM, KP);
+                                            bool transposed, uint64_t *mbar) {
+    const uint32_t id = tc::idesc_bf16_mn(TM, KP, false, transposed);
     const uint32_t xh = tc::smem_u32(sm.xh), xl = tc::smem_u32(sm.xl);
     const uint32_t wh = tc::smem_u32(sm.wt + (2 * mat) * WT);
     const uint32_t wl = tc::smem_u32(sm.wt + (2 * mat + 1) * WT);
+    // K-major: K-chunk stride WKS, row-group stride 128; transposed (n = i, k = o): K-group
+    // stride 128, N-group stride WKS
+    const uint32_t lbo = transposed ? 128u : (uint32_t)WKS, sbo = transposed ? (uint32_t)WKS : 128u;
     uint32_t acc = 0;
 #pragma unroll
     for (int p = 0; p < SPLIT; ++p) {
@@ -220,20 +220,21 @@ __device__ __forceinline__ void issue_layer(const MixSmem &sm, uint32_t tmem, in
 #pragma unroll
         for (int kk = 0; kk < 2; ++kk) {
             tc::mma_bf16(tmem, tc::desc_kmajor(xa + kk * 2 * XKS, XKS, 128),
-                         tc::desc_kmajor(wb + kk * 2 * WKS, WKS, 128), id, acc);
+                         tc::desc_kmajor(wb + kk * 2 * lbo, lbo, sbo), id, acc);
             acc = 1;
         }
     }
     tc::commit(mbar);
 }
 
-// D[128 x N] (+)= Aop B over K = 128 pair rows, both operands MN-major; B is given as its hi
+// D[M x N] (+)= Aop B over K = 128 pair rows, both operands MN-major; B is given as its hi
 // and (SPLIT 3) lo tiles.  `first`: the first product of the group starts the accumulator.
-template <int SPLIT, int N>
+// (With M = 64, rows 0..15 of D sit in TMEM lanes 0..15.)
+template <int SPLIT, int M, int N>
 __device__ __forceinline__ void issue_rows(uint32_t tmem, const unsigned char *aop,
                                            const unsigned char *bh, const unsigned char *bl,
                                            bool first, uint64_t *mbar) {
-    const uint32_t id = tc::idesc_bf16_mn(128, N, true, true);
+    const uint32_t id = tc::idesc_bf16_mn(M, N, true, true);
     const uint32_t a0 = tc::smem_u32(aop), h0 = tc::smem_u32(bh), l0 = tc::smem_u32(bl);
 #pragma unroll
     for (int s = 0; s < TM / 16; ++s) {
@@ -432,7 +433,7 @@ dp_embed_fwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
             if (ns == ne) continue;
             if (k != cur_net) {            // no MMA in flight reads the weight tiles here
                 __syncthreads();
-                load_net(wtiles, params, k, 4, sm);
+                load_net(wtiles, params, k, sm);
                 cur_net = k;
                 __syncthreads();
             }
@@ -484,7 +485,7 @@ dp_embed_fwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
                     }
                 }
                 if (pre_issue(ok)) goto done;
-                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 0, &mbar_l);
+                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 0, false, &mbar_l);
                 pend_l = true;
                 if (!wait_commit(&mbar_l, ph_l, pend_l, P.wait_polls)) ok = false;
                 {
@@ -501,7 +502,7 @@ dp_embed_fwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
                 }
                 store_row<SPLIT>(sm, tid, x, 1.f);
                 if (pre_issue(ok)) goto done;
-                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 1, &mbar_l);
+                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 1, false, &mbar_l);
                 pend_l = true;
                 if (!wait_commit(&mbar_l, ph_l, pend_l, P.wait_polls)) ok = false;
                 {
@@ -519,7 +520,7 @@ dp_embed_fwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
                 store_row<SPLIT>(sm, tid, x, 0.f);       // G, the B operand of the contraction
                 if (pre_issue(ok)) goto done;
                 if (tid == 0)
-                    issue_rows<SPLIT, KP>(tmem + TCOL_A, sm.rop, sm.xh, sm.xl, first, &mbar_c);
+                    issue_rows<SPLIT, 128, KP>(tmem + TCOL_A, sm.rop, sm.xh, sm.xl, first, &mbar_c);
                 pend_c = true;
                 first = false;
             }
@@ -586,7 +587,7 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
     const int nt = P.ntypes, nnet = nt * nt, S = P.nslots;
     const MixSmem sm = carve(smem_raw, true, S, P.ga);
     const int tid = threadIdx.x, warp = tid >> 5;
-    for (int q = tid; q < (2 * XT + RT + 2 * QT) / 16; q += TM)   // xh, xl, rop, qh, ql
+    for (int q = tid; q < (2 * XT + ET + 2 * QT) / 16; q += TM)   // xh, xl, rop, qh, ql
         reinterpret_cast<uint4 *>(sm.xh)[q] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
         tc::mbar_init(&mbar_l, 1);
@@ -627,7 +628,7 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
             if (ns == ne) continue;
             if (k != cur_net) {
                 __syncthreads();
-                load_net(wtiles, params, k, 8, sm);
+                load_net(wtiles, params, k, sm);
                 cur_net = k;
                 __syncthreads();
             }
@@ -662,7 +663,7 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
                 }
                 store_row<SPLIT>(sm, tid, x, 1.f);
                 if (pre_issue(ok)) goto done;
-                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 0, &mbar_l);
+                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 0, false, &mbar_l);
                 pend_l = true;
                 if (!wait_commit(&mbar_l, ph_l, pend_l, P.wait_polls)) ok = false;
                 {
@@ -685,7 +686,7 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
                 }
                 store_row<SPLIT>(sm, tid, x, 1.f);
                 if (pre_issue(ok)) goto done;
-                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 1, &mbar_l);
+                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 1, false, &mbar_l);
                 pend_l = true;
                 if (!wait_commit(&mbar_l, ph_l, pend_l, P.wait_polls)) ok = false;
                 float g[4] = {0.f, 0.f, 0.f, 0.f};
@@ -717,7 +718,7 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
                     store_row<SPLIT>(sm, tid, h, 0.f);
                 }
                 if (pre_issue(ok)) goto done;
-                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 2, &mbar_l);
+                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 1, true, &mbar_l);
                 pend_l = true;
                 if (!wait_commit(&mbar_l, ph_l, pend_l, P.wait_polls)) ok = false;
                 {
@@ -740,7 +741,7 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
                     store_row<SPLIT>(sm, tid, h, 0.f);
                 }
                 if (pre_issue(ok)) goto done;
-                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 3, &mbar_l);
+                if (tid == 0) issue_layer<SPLIT>(sm, tmem, 0, true, &mbar_l);
                 pend_l = true;
                 if (!wait_commit(&mbar_l, ph_l, pend_l, P.wait_polls)) ok = false;
                 {
@@ -809,7 +810,7 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
                 }
                 if (pre_issue(ok)) goto done;
                 if (tid == 0)
-                    issue_rows<SPLIT, QN>(tmem + TCOL_RED, sm.rop, sm.qh, sm.ql, first, &mbar_c);
+                    issue_rows<SPLIT, 64, QN>(tmem + TCOL_RED, sm.rop, sm.qh, sm.ql, first, &mbar_c);
                 pend_c = true;
                 first = false;
             }
@@ -874,10 +875,10 @@ size_t mixed_smem(int ntypes, int S) {
     return std::max(mix_smem_bytes(false, S, mixed_ga(S)), mix_smem_bytes(true, S, mixed_ga(S)));
 }
 
-size_t mixed_tile_bytes(int ntypes) { return (size_t)ntypes * ntypes * 8 * WT; }
+size_t mixed_tile_bytes(int ntypes) { return (size_t)ntypes * ntypes * 4 * WT; }
 
 int prep_mixed_tiles(const float *params, unsigned char *out, int ntypes, cudaStream_t s) {
-    const int n = ntypes * ntypes * 4 * KP * KP;
+    const int n = ntypes * ntypes * 2 * KP * KP;
     ProfScope ps("prep_weight_tiles", s);
     prep_weight_tiles<<<(n + 255) / 256, 256, 0, s>>>(params, out, ntypes * ntypes);
     return check_launch("prep_weight_tiles");

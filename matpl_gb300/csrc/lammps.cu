@@ -127,7 +127,7 @@ lmp_neighbors(int inum, int nall, const int *__restrict__ ilist, Lists lists,
                         const long long s = row + (long long)t * m + slot;
                         list_neigh[s] = j + 1;
                         TO *o = image_dr + 4 * s;
-                        o[0] = conv<TO>(__dsqrt_rn(rsq));
+                        o[0] = pair_r<TO>(rsq);
                         o[1] = conv<TO>(dx);
                         o[2] = conv<TO>(dy);
                         o[3] = conv<TO>(dz);

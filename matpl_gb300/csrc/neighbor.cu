@@ -487,7 +487,7 @@ nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
             const double x = xa.x, y = xa.y, z = xb.x, dd = xb.y;
             const long long slot = row + (long long)ty * P.m + rank;
             list_neigh[slot] = j + 1;
-            store4(image_dr + 4 * slot, conv<TO>(__dsqrt_rn(dd)), conv<TO>(x), conv<TO>(y),
+            store4(image_dr + 4 * slot, pair_r<TO>(dd), conv<TO>(x), conv<TO>(y),
                    conv<TO>(z));
         }
         // ---- phase D: clear the empty slots (the occupied-slot form leaves them untouched:
