@@ -14,12 +14,6 @@ namespace matpl {
 
 void set_error(const std::string &msg);
 
-__host__ __device__ inline float __uint_as_float_hd(uint32_t b) {
-    float f;
-    memcpy(&f, &b, 4);
-    return f;
-}
-
 #define MATPL_REQUIRE(cond, code, msg)                 \
     do {                                               \
         if (!(cond)) {                                 \
@@ -104,94 +98,60 @@ __device__ __forceinline__ float to_f32(double v) {
     r += (rest > 0x10000000u) || (rest == 0x10000000u && (m & 1u));
     return __uint_as_float(sign | r);
 }
-// 64 x 64 -> 128-bit product.
-__host__ __device__ inline void mul_u128(uint64_t a, uint64_t b, uint64_t &hi, uint64_t &lo) {
-#ifdef __CUDA_ARCH__
-    lo = a * b;
-    hi = __umul64hi(a, b);
-#else
-    const unsigned __int128 p = (unsigned __int128)a * b;
-    lo = (uint64_t)p;
-    hi = (uint64_t)(p >> 64);
-#endif
+// Order-preserving integer key of a double (for exact comparisons outside the FP64 pipe).
+__host__ __device__ inline long long dkey(double x) {
+    long long b;
+    memcpy(&b, &x, 8);
+    return b >= 0 ? b : (long long)((unsigned long long)b ^ 0x7FFFFFFFFFFFFFFFull);
 }
 
-// Exact comparison of (K 2^ek)^2 with a positive normal double v (K < 2^58): -1, 0, +1 as
-// the square is <, ==, > v.  Integer arithmetic only.
-__host__ __device__ inline int cmp_square(uint64_t K, int ek, uint64_t v_bits) {
-    const uint64_t D = (v_bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int dv = (int)((v_bits >> 52) & 0x7FF) - 1023 - 52;
-    uint64_t ahi, alo;
-    mul_u128(K, K, ahi, alo);                   // K^2 2^(2 ek)  vs  D 2^dv
-    const int sh = dv - 2 * ek;                  // compare K^2 with D 2^sh
-    uint64_t bhi = 0, blo = D;
-    if (sh <= -64) {
-        blo = 0;
-    } else if (sh < 0) {
-        blo = D >> (-sh);
-        if ((blo << (-sh)) != D) {               // D 2^sh is not an integer: compare K^2 2^-sh
-            const uint64_t chi = (ahi << (-sh)) | (-sh ? alo >> (64 + sh) : 0);
-            const uint64_t clo = alo << (-sh);
-            if (ahi >> (64 + sh)) return 1;      // K^2 2^-sh overflows 128 bits: larger
-            return chi != 0 || clo > D ? 1 : (clo < D ? -1 : 0);
-        }
-    } else if (sh >= 75) {
-        return -1;                               // D 2^sh >= 2^127 > K^2 (K < 2^58... 2^116)
-    } else if (sh >= 64) {
-        bhi = D << (sh - 64);
-        blo = 0;
-    } else if (sh > 0) {
-        bhi = D >> (64 - sh);
-        blo = D << sh;
-    }
-    if (ahi != bhi) return ahi < bhi ? -1 : 1;
-    return alo < blo ? -1 : (alo > blo ? 1 : 0);
+__host__ __device__ inline double dfrom(unsigned long long b) {
+    double x;
+    memcpy(&x, &b, 8);
+    return x;
 }
 
-// The float of the correctly rounded double sqrt of a positive normal double v, i.e.
-// (float)sqrt_rn(v) bit for bit, without the FP64 pipe.  From a single-precision estimate:
-// (1) the float nearest to sqrt(v), by exact comparisons of v with the squares of the float
-// midpoints on either side of it; (2) the double rounding of the reference (sqrt rounded to
-// double, then to float): when sqrt_rn(v) falls exactly on a float midpoint m, that is when v
-// lies within the squares of m -+ half a double ulp, the result is the even neighbour of m.
-__host__ __device__ inline float sqrt_to_f32_bits(float estimate, uint64_t v_bits) {
-    uint32_t yb;
-    memcpy(&yb, &estimate, 4);
-    for (int it = 0; it < 3; ++it) {
-        const uint64_t Y = (yb & 0x7FFFFFu) | 0x800000u;
-        const int ey = (int)((yb >> 23) & 0xFF) - 127 - 23;
-        const int up = cmp_square(2 * Y + 1, ey - 1, v_bits);            // midpoint above y
-        if (up < 0) { ++yb; continue; }
-        if (up == 0) { if (Y & 1) ++yb; return __uint_as_float_hd(yb); }   // exact tie
-        const bool pow2 = Y == 0x800000u;                                  // ulp below is half
-        const int dn = pow2 ? cmp_square(4 * Y - 1, ey - 2, v_bits)
-                            : cmp_square(2 * Y - 1, ey - 1, v_bits);      // midpoint below y
-        if (dn > 0) { --yb; continue; }
-        if (dn == 0) { if (Y & 1) --yb; return __uint_as_float_hd(yb); }
-        break;
-    }
-    // (2) midpoints written with 54-bit odd numerators: m -+ u/2 = (M 2^(s+1) -+ 1) 2^(e-s-1),
-    // M 2^e the midpoint (M odd, < 2^26) and u = 2^(e-s) its double ulp
-    const uint64_t Y = (yb & 0x7FFFFFu) | 0x800000u;
-    const int ey = (int)((yb >> 23) & 0xFF) - 127 - 23;
-    {   // midpoint above y, M = 2Y + 1 (25 bits): s = 28
-        const uint64_t K = ((2 * Y + 1) << 29) - 1;
-        if (cmp_square(K, ey - 1 - 29, v_bits) <= 0) {          // sqrt_rn(v) = m
-            if (Y & 1) ++yb;
-            return __uint_as_float_hd(yb);
+__host__ __device__ inline float dfrom_f(uint32_t b) {
+    float x;
+    memcpy(&x, &b, 4);
+    return x;
+}
+
+// The float of the correctly rounded double square root of a positive normal double v, i.e.
+// (float)sqrt_rn(v) bit for bit, with four FP64 operations instead of a double square root.
+// y = sqrtf((float)v) is within one float ulp of sqrt(v), so the answer is y or a neighbour,
+// decided by where s = sqrt_rn(v) lies relative to the float midpoints m = y -+ ulp/2 (exact
+// doubles; in the bit pattern of double(y) they are -+ 2^28, across a power of two too).  With
+// r = v - m*m (both operations exact: m*m has 50 bits and v, m*m are within a factor 2) and
+// T = m * ulp64(m): s > m iff r > T, and s = m iff -T < r <= T (the doubles between the
+// square roots of v's neighbours do not resolve the u64^2/4 term), the round-half-even cases
+// of the double rounding included.
+__host__ __device__ inline float sqrt_to_f32(float y, double v) {
+    uint32_t fb;
+    memcpy(&fb, &y, 4);
+    // bit pattern of double(y) (y positive and normal), built without a conversion instruction
+    const unsigned long long yb = ((unsigned long long)(((fb >> 23) & 0xFFu) + (1023u - 127u)) << 52) |
+                                  ((unsigned long long)(fb & 0x7FFFFFu) << 29);
+    const unsigned long long half = 1ull << 28;        // half a float ulp, in double units
+    for (int side = 0; side < 2; ++side) {
+        const unsigned long long mb = side == 0 ? yb + half : yb - half;
+        const double m = dfrom(mb);
+        const double r = v - m * m;                     // exact
+        const long long em = (long long)((mb >> 52) & 0x7FF) - 1023;
+        const double T = dfrom(mb + ((unsigned long long)(em - 52) << 52));   // m * ulp64(m)
+        unsigned long long tb;
+        memcpy(&tb, &T, 8);
+        const long long kr = dkey(r), kT = (long long)tb;
+        const long long kmT = (long long)((tb | (1ull << 63)) ^ 0x7FFFFFFFFFFFFFFFull);   // key of -T
+        if (side == 0) {
+            if (kr > kT) return dfrom_f(fb + 1);                   // s above m: round up
+            if (kr > kmT) return dfrom_f((fb & 1u) ? fb + 1 : fb);  // s = m: to even
+        } else {
+            if (kr <= kmT) return dfrom_f(fb - 1);                 // s below m: round down
+            if (kr <= kT) return dfrom_f((fb & 1u) ? fb - 1 : fb);  // s = m: to even
         }
     }
-    {   // midpoint below y
-        const bool pow2 = Y == 0x800000u;
-        const uint64_t M = pow2 ? 4 * Y - 1 : 2 * Y - 1;        // 25 bits (26 for pow2... 25)
-        const int e = pow2 ? ey - 2 : ey - 1;
-        const uint64_t K = (M << 29) + 1;
-        if (cmp_square(K, e - 29, v_bits) >= 0) {
-            if (Y & 1) --yb;
-            return __uint_as_float_hd(yb);
-        }
-    }
-    return __uint_as_float_hd(yb);
+    return y;
 }
 
 template <typename TO> __device__ __forceinline__ TO conv(double v);
@@ -199,11 +159,11 @@ template <> __device__ __forceinline__ float conv<float>(double v) { return to_f
 template <> __device__ __forceinline__ double conv<double>(double v) { return v; }
 
 // r = sqrt(dd) of a pair, in the output dtype: f64 correctly rounded; f32 the float nearest to
-// that f64 value, formed without the FP64 pipe (sqrt_to_f32_bits).
+// that f64 value, formed with four FP64 operations (sqrt_to_f32).
 template <typename TO> __device__ __forceinline__ TO pair_r(double dd);
 template <> __device__ __forceinline__ double pair_r<double>(double dd) { return __dsqrt_rn(dd); }
 template <> __device__ __forceinline__ float pair_r<float>(double dd) {
-    return sqrt_to_f32_bits(sqrtf(to_f32(dd)), (unsigned long long)__double_as_longlong(dd));
+    return sqrt_to_f32(sqrtf(to_f32(dd)), dd);
 }
 
 // bit pattern of a non-negative double: orders like the value (NaN above +inf)

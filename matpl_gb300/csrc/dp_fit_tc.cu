@@ -168,57 +168,59 @@ constexpr size_t FIT_SMEM = sizeof(float) * (FM * ASTR) + 2 * X64 + 2 * W64;
 constexpr int FIT_TCOLS = 256;   // TMEM: [0, 64) accumulator, [64 + 64 l, 128 + 64 l) tanh of layer l
 
 // Stable counting sort of the atoms of one image by model type into order[natoms], with
-// type_start[0..ntypes+1] (bucket ntypes: atoms whose type is not evaluated).  One block.
-__global__ void fit_order(const int32_t *__restrict__ type_map, int natoms, int ntypes,
-                          int present_mask, int *__restrict__ order, int *__restrict__ type_start) {
-    __shared__ int wsum[32];
-    __shared__ int base[18];
-    __shared__ int tot;
-    const int T = ntypes + 1;
-    const int per = (natoms + blockDim.x - 1) / blockDim.x;
-    const int a0 = threadIdx.x * per, a1 = min(natoms, a0 + per);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    auto bucket = [&](int i) {
-        const int t = type_map[i];
-        return (t >= 0 && t < ntypes && ((present_mask >> t) & 1)) ? t : ntypes;
-    };
-    int off[17];
-    if (threadIdx.x == 0) base[0] = 0;
-    for (int q = 0; q < T; ++q) {
-        int c = 0;
-        for (int i = a0; i < a1; ++i) c += bucket(i) == q;
-        int incl = c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
+// type_start[0..ntypes+1] (bucket ntypes: atoms whose type is not evaluated), in two launches
+// over 1024-atom blocks: per-block bucket counts, then per-block offsets (previous blocks'
+// counts) and the ranks inside the block (warp match + a prefix over the block's warps).
+constexpr int kOrderBlock = 1024;
+
+__device__ __forceinline__ int fit_bucket(const int32_t *__restrict__ type_map, int i, int ntypes,
+                                          int present_mask) {
+    const int t = type_map[i];
+    return (t >= 0 && t < ntypes && ((present_mask >> t) & 1)) ? t : ntypes;
+}
+
+__global__ void fit_order_count(const int32_t *__restrict__ type_map, int natoms, int ntypes,
+                                int present_mask, int *__restrict__ blk_count) {
+    __shared__ int cnt[17];
+    if (threadIdx.x < 17) cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const int i = blockIdx.x * kOrderBlock + threadIdx.x;
+    if (i < natoms) atomicAdd(&cnt[fit_bucket(type_map, i, ntypes, present_mask)], 1);
+    __syncthreads();
+    if (threadIdx.x <= ntypes) blk_count[blockIdx.x * 17 + threadIdx.x] = cnt[threadIdx.x];
+}
+
+__global__ void fit_order_scatter(const int32_t *__restrict__ type_map, int natoms, int ntypes,
+                                  int present_mask, const int *__restrict__ blk_count,
+                                  int *__restrict__ order, int *__restrict__ type_start) {
+    __shared__ int base[17];                   // global start of this block's atoms per bucket
+    __shared__ int wcnt[kOrderBlock / 32][17];
+    const int T = ntypes + 1, nblk = gridDim.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x < T) {
+        const int q = threadIdx.x;
+        int before = 0, total_lower = 0;
+        for (int b = 0; b < nblk; ++b) {
+            if (b < (int)blockIdx.x) before += blk_count[b * 17 + q];
+            for (int p = 0; p < q; ++p) total_lower += blk_count[b * 17 + p];
         }
-        if (lane == 31) wsum[warp] = incl;
-        __syncthreads();
-        if (warp == 0) {
-            int w = lane < nw ? wsum[lane] : 0;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int y = __shfl_up_sync(0xffffffffu, w, o);
-                if (lane >= o) w += y;
-            }
-            if (lane < nw) wsum[lane] = w - (lane < nw ? wsum[lane] : 0);   // exclusive
-            if (lane == nw - 1) tot = w;
-        }
-        __syncthreads();
-        off[q] = wsum[warp] + incl - c;
-        if (threadIdx.x == 0) base[q + 1] = base[q] + tot;
-        __syncthreads();
+        base[q] = total_lower + before;
+        if (blockIdx.x == 0) type_start[q] = total_lower;
+        if (blockIdx.x == 0 && q == T - 1) type_start[T] = natoms;
     }
-    for (int i = a0; i < a1; ++i) {
-        const int q = bucket(i);
-        int o = 0;
-#pragma unroll
-        for (int k = 0; k < 17; ++k)
-            if (k == q) o = off[k]++;
-        order[base[q] + o] = i;
+    const int i = blockIdx.x * kOrderBlock + threadIdx.x;
+    const int q = i < natoms ? fit_bucket(type_map, i, ntypes, present_mask) : 17;
+    const unsigned peers = __match_any_sync(0xffffffffu, q);
+    const int rank = __popc(peers & ((1u << lane) - 1u));
+    if (lane < 17) wcnt[warp][lane] = 0;
+    __syncwarp();
+    if (q < 17 && rank == 0) wcnt[warp][q] = __popc(peers);
+    __syncthreads();
+    if (q < 17) {
+        int off = base[q] + rank;
+        for (int w = 0; w < warp; ++w) off += wcnt[w][q];
+        order[off] = i;
     }
-    if (threadIdx.x <= T) type_start[threadIdx.x] = base[threadIdx.x];
 }
 
 __device__ __forceinline__ void st64(uint32_t taddr, const float v[64]) {
@@ -445,10 +447,11 @@ dp_fit_tc(const float *__restrict__ Ain, const int *__restrict__ order,
 }  // namespace
 
 // Prepared tiles of every element, then the element order of the atoms (order [natoms],
-// type_start [ntypes + 2]).
+// type_start [ntypes + 2], per-block bucket counts of the sort).
 size_t fit_tile_bytes(int ntypes, int natoms) {
+    const size_t nblk = ((size_t)natoms + kOrderBlock - 1) / kOrderBlock;
     return align_up((size_t)ntypes * FIT_TILE_BYTES, 256) + align_up(sizeof(int) * natoms, 256) +
-           sizeof(int) * 32;
+           sizeof(int) * (32 + 17 * nblk);
 }
 
 // Prepares the BF16 fitting tiles of every type into `tiles`, then runs the fitting kernel.
@@ -462,9 +465,14 @@ int launch_fit_tc(bool fast, const float *A, const int32_t *type_map, const floa
     }
     int *order = reinterpret_cast<int *>(tiles + align_up((size_t)ntypes * FIT_TILE_BYTES, 256));
     int *type_start = order + align_up(sizeof(int) * natoms, 256) / sizeof(int);
-    {
+    int *blk_count = type_start + 32;
+    const int nblk = (natoms + kOrderBlock - 1) / kOrderBlock;
+    if (nblk > 0) {
         ProfScope ps("fit_order", s);
-        fit_order<<<1, 1024, 0, s>>>(type_map, natoms, ntypes, present_mask, order, type_start);
+        fit_order_count<<<nblk, kOrderBlock, 0, s>>>(type_map, natoms, ntypes, present_mask,
+                                                    blk_count);
+        fit_order_scatter<<<nblk, kOrderBlock, 0, s>>>(type_map, natoms, ntypes, present_mask,
+                                                      blk_count, order, type_start);
     }
     const long long tiles_b = (natoms + FM - 1) / FM + ntypes;
     const long long ntiles = (long long)batch * tiles_b;

@@ -137,20 +137,41 @@ __device__ __forceinline__ void emb_forward(const T *__restrict__ w, T s, T x[E]
 }
 
 // --------------------------------------------------------------------------- dp_pad
+// One warp per (t_i, t_j) net, lane o holding output o of every layer (the layer inputs are
+// broadcast by shuffles): the same arithmetic, term order and tanh as emb_forward.
 template <typename T>
 __global__ void dp_pad(const T *__restrict__ params, const T *__restrict__ davg,
                        const T *__restrict__ dstd, T *__restrict__ pad, int ntypes,
                        EvalParams P) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (k >= ntypes * ntypes) return;
     const int ti = k / ntypes;
     T rp[4];
     for (int c = 0; c < 4; ++c) rp[c] = (T(0) - davg[4 * ti + c]) / dstd[4 * ti + c];
-    T x[E], t3[E];
-    if (P.ctab) cmp_forward<T>((const T *)P.ctab, k, rp[0], P, x, nullptr);
-    else emb_forward<T, false>(params + (long long)k * EmbOff::SIZE, rp[0], x, t3, nullptr, nullptr, 0);
-    for (int c = 0; c < 4; ++c)
-        for (int p = 0; p < E; ++p) pad[(long long)k * NA + c * E + p] = rp[c] * x[p];
+    T xo = T(0);
+    if (P.ctab) {
+        T x[E];
+        if (lane == 0) cmp_forward<T>((const T *)P.ctab, k, rp[0], P, x, nullptr);
+#pragma unroll
+        for (int p = 0; p < E; ++p) {
+            const T v = __shfl_sync(0xffffffffu, x[p], 0);
+            if (lane == p) xo = v;
+        }
+    } else {
+        const T *w = params + (long long)k * EmbOff::SIZE;
+        const int o = lane < E ? lane : 0;
+        xo = dev_tanh(rp[0] * w[EmbOff::W0 + o] + w[EmbOff::B0 + o]);
+        for (int l = 0; l < 2; ++l) {
+            const T *W = w + (l == 0 ? EmbOff::W1 : EmbOff::W2);
+            T h = w[(l == 0 ? EmbOff::B1 : EmbOff::B2) + o];
+#pragma unroll
+            for (int i = 0; i < E; ++i) h += __shfl_sync(0xffffffffu, xo, i) * W[i * E + o];
+            xo = dev_tanh(h) * w[(l == 0 ? EmbOff::DT1 : EmbOff::DT2) + o] + xo;
+        }
+    }
+    if (lane < E)
+        for (int c = 0; c < 4; ++c) pad[(long long)k * NA + c * E + lane] = rp[c] * xo;
 }
 
 // Build the warp's list of occupied slots of one centre atom (ascending slot order) and
@@ -777,7 +798,7 @@ int launch_eval(int mode, const matpl_dp_model *M, const EvalParams &P,
     const int nnet = P.ntypes * P.ntypes;
     {
         ProfScope ps("dp_pad", s);
-        dp_pad<T><<<(nnet + 31) / 32, 32, 0, s>>>(params, davg, dstd, pad, P.ntypes, P);
+        dp_pad<T><<<(nnet + 3) / 4, 128, 0, s>>>(params, davg, dstd, pad, P.ntypes, P);
     }
 
     const long long nwarp_blocks = (total + kWarps - 1) / kWarps;

@@ -68,7 +68,7 @@ struct MixSmem {
     unsigned char *wt;     // weight tiles of the current net: fw1 h/l, fw2 h/l
     unsigned char *xh, *xl;
     unsigned char *rop;    // fwd: contraction A operand (M = 128); bwd: one-hot A operand (M = 64)
-    unsigned char *qh, *ql;   // bwd: per-row reduction values (MN-major B operand)
+    unsigned char *qh, *qm, *ql;   // bwd: per-row reduction values, three BF16 parts (MN-major B)
     float *vec;            // [4][VW] of the current net: W0, b0, dt1, dt2
     float *dA;             // bwd: [GAMAX][E] float4 (c fastest) of dE/dA * k
     uint16_t *list;        // [ga * S] rows: atom << 12 | slot
@@ -76,17 +76,23 @@ struct MixSmem {
     int *off;              // [GAMAX][kMaxTypes]
     int *net_start;        // [kMaxTypes*kMaxTypes + 1]
     int *tia;              // [GAMAX] model type of each group atom (-1: skipped)
+    int *tiles;            // [tile_cap] the group's tiles in order: net << 16 | first row
+    int *ntiles;           // [1]
 };
+
+// Upper bound of a group's tiles (each net's rows rounded up to whole tiles).
+__host__ __device__ inline int tile_cap(int S, int ga) { return ga * S / TM + kMaxTypes * kMaxTypes + 1; }
 
 __host__ __device__ inline size_t mix_smem_bytes(bool bwd, int S, int ga) {
     size_t o = 0;
     o += 4 * WT;
     o += 2 * XT + (bwd ? ET : RT);
-    if (bwd) o += 2 * QT;
+    if (bwd) o += 3 * QT;
     o += sizeof(float) * 4 * VW;
     if (bwd) o += sizeof(float) * GAMAX * E * 4;
     o += align_up(sizeof(uint16_t) * (size_t)ga * S, 16);
     o += sizeof(int) * (2 * GAMAX * kMaxTypes + kMaxTypes * kMaxTypes + 1 + GAMAX);
+    o += sizeof(int) * (tile_cap(S, ga) + 1);
     return o + 128;
 }
 
@@ -97,8 +103,8 @@ __device__ MixSmem carve(unsigned char *base, bool bwd, int S, int ga) {
     m.xh = base + o; o += XT;
     m.xl = base + o; o += XT;
     m.rop = base + o; o += bwd ? ET : RT;
-    m.qh = m.ql = nullptr;
-    if (bwd) { m.qh = base + o; o += QT; m.ql = base + o; o += QT; }
+    m.qh = m.qm = m.ql = nullptr;
+    if (bwd) { m.qh = base + o; o += QT; m.qm = base + o; o += QT; m.ql = base + o; o += QT; }
     m.vec = reinterpret_cast<float *>(base + o); o += sizeof(float) * 4 * VW;
     m.dA = nullptr;
     if (bwd) { m.dA = reinterpret_cast<float *>(base + o); o += sizeof(float) * GAMAX * E * 4; }
@@ -106,7 +112,9 @@ __device__ MixSmem carve(unsigned char *base, bool bwd, int S, int ga) {
     m.cnt = reinterpret_cast<int *>(base + o); o += sizeof(int) * GAMAX * kMaxTypes;
     m.off = reinterpret_cast<int *>(base + o); o += sizeof(int) * GAMAX * kMaxTypes;
     m.net_start = reinterpret_cast<int *>(base + o); o += sizeof(int) * (kMaxTypes * kMaxTypes + 1);
-    m.tia = reinterpret_cast<int *>(base + o);
+    m.tia = reinterpret_cast<int *>(base + o); o += sizeof(int) * GAMAX;
+    m.tiles = reinterpret_cast<int *>(base + o); o += sizeof(int) * tile_cap(S, ga);
+    m.ntiles = reinterpret_cast<int *>(base + o);
     return m;
 }
 
@@ -227,22 +235,25 @@ __device__ __forceinline__ void issue_layer(const MixSmem &sm, uint32_t tmem, in
     tc::commit(mbar);
 }
 
-// D[M x N] (+)= Aop B over K = 128 pair rows, both operands MN-major; B is given as its hi
-// and (SPLIT 3) lo tiles.  `first`: the first product of the group starts the accumulator.
+// D[M x N] (+)= Aop B over K = 128 pair rows, both operands MN-major; B is given as NB tiles
+// whose sum it is (BF16 hi / lo parts).  `first`: the first product of the group starts the
+// accumulator.
 // (With M = 64, rows 0..15 of D sit in TMEM lanes 0..15.)
-template <int SPLIT, int M, int N>
+template <int NB, int M, int N>
 __device__ __forceinline__ void issue_rows(uint32_t tmem, const unsigned char *aop,
-                                           const unsigned char *bh, const unsigned char *bl,
-                                           bool first, uint64_t *mbar) {
+                                           const unsigned char *b0, const unsigned char *b1,
+                                           const unsigned char *b2, bool first, uint64_t *mbar) {
     const uint32_t id = tc::idesc_bf16_mn(M, N, true, true);
-    const uint32_t a0 = tc::smem_u32(aop), h0 = tc::smem_u32(bh), l0 = tc::smem_u32(bl);
+    const uint32_t a0 = tc::smem_u32(aop);
+    const uint32_t bb[3] = {tc::smem_u32(b0), NB > 1 ? tc::smem_u32(b1) : 0u,
+                            NB > 2 ? tc::smem_u32(b2) : 0u};
 #pragma unroll
     for (int s = 0; s < TM / 16; ++s) {
         const uint64_t ad = tc::desc_kmajor(a0 + s * 2 * OLBO, OLBO, OSBO);
-        tc::mma_bf16(tmem, ad, tc::desc_kmajor(h0 + s * 2 * OLBO, OLBO, OSBO), id,
-                     (first && s == 0) ? 0u : 1u);
-        if (SPLIT == 3)
-            tc::mma_bf16(tmem, ad, tc::desc_kmajor(l0 + s * 2 * OLBO, OLBO, OSBO), id, 1u);
+#pragma unroll
+        for (int q = 0; q < NB; ++q)
+            tc::mma_bf16(tmem, ad, tc::desc_kmajor(bb[q] + s * 2 * OLBO, OLBO, OSBO), id,
+                         (first && s == 0 && q == 0) ? 0u : 1u);
     }
     tc::commit(mbar);
 }
@@ -341,6 +352,11 @@ __device__ void build_group_list(const MixSmem &sm, const int32_t *__restrict__ 
             }
         }
         sm.net_start[nnet] = pos;
+        int nt_ = 0;                       // tile schedule: tiles never span two nets
+        for (int k = 0; k < nnet; ++k)
+            for (int r0 = sm.net_start[k]; r0 < sm.net_start[k + 1]; r0 += TM)
+                sm.tiles[nt_++] = (k << 16) | r0;
+        *sm.ntiles = nt_;
     }
     __syncthreads();
     for (int a = warp; a < ga; a += TM / 32) {
@@ -428,9 +444,24 @@ dp_embed_fwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
         const int ga = (int)(total - g0 < P.ga ? total - g0 : P.ga);
         build_group_list(sm, list_neigh, type_map, g0, ga, P);
         bool first = true;
-        for (int k = 0; k < nnet; ++k) {
-            const int ns = sm.net_start[k], ne = sm.net_start[k + 1];
-            if (ns == ne) continue;
+        const int ntl = *sm.ntiles;
+        // this thread's pair row of tile `it`, fetched one tile ahead of its use
+        int a_n = 0;
+        float4 q4_n = make_float4(0.f, 0.f, 0.f, 0.f);
+        auto fetch = [&](int it) {
+            const int tw = sm.tiles[it], k2 = tw >> 16, r = (tw & 0xFFFF) + tid;
+            a_n = 0;
+            q4_n = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r < sm.net_start[k2 + 1]) {
+                const int e = sm.list[r];
+                a_n = e >> 12;
+                q4_n = __ldg(reinterpret_cast<const float4 *>(idr) + (g0 + a_n) * S + (e & 0xFFF));
+            }
+        };
+        if (ntl > 0) fetch(0);
+        for (int it = 0; it < ntl; ++it) {
+            const int k = sm.tiles[it] >> 16, r0 = sm.tiles[it] & 0xFFFF;
+            const int ne = sm.net_start[k + 1];
             if (k != cur_net) {            // no MMA in flight reads the weight tiles here
                 __syncthreads();
                 load_net(wtiles, params, k, sm);
@@ -442,16 +473,12 @@ dp_embed_fwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
             const float isd[4] = {1.f / dstd[4 * ti], 1.f / dstd[4 * ti + 1],
                                   1.f / dstd[4 * ti + 2], 1.f / dstd[4 * ti + 3]};
             const float4 *v4 = reinterpret_cast<const float4 *>(sm.vec);
-            for (int r0 = ns; r0 < ne; r0 += TM) {
+            {
                 const int nrows = ne - r0 < TM ? ne - r0 : TM;
                 const bool valid = tid < nrows;
-                int a = 0;
-                float4 q4 = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (valid) {
-                    const int e = sm.list[r0 + tid];
-                    a = e >> 12;
-                    q4 = __ldg(reinterpret_cast<const float4 *>(idr) + (g0 + a) * S + (e & 0xFFF));
-                }
+                const int a = a_n;
+                const float4 q4 = q4_n;
+                if (it + 1 < ntl) fetch(it + 1);
                 EnvRow en;
                 env_of(en, q4, P.rmin, P.rmax, av, isd);
                 float x[E];
@@ -520,7 +547,8 @@ dp_embed_fwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
                 store_row<SPLIT>(sm, tid, x, 0.f);       // G, the B operand of the contraction
                 if (pre_issue(ok)) goto done;
                 if (tid == 0)
-                    issue_rows<SPLIT, 128, KP>(tmem + TCOL_A, sm.rop, sm.xh, sm.xl, first, &mbar_c);
+                    issue_rows<SPLIT == 3 ? 2 : 1, 128, KP>(tmem + TCOL_A, sm.rop, sm.xh, sm.xl,
+                                                          nullptr, first, &mbar_c);
                 pend_c = true;
                 first = false;
             }
@@ -587,7 +615,7 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
     const int nt = P.ntypes, nnet = nt * nt, S = P.nslots;
     const MixSmem sm = carve(smem_raw, true, S, P.ga);
     const int tid = threadIdx.x, warp = tid >> 5;
-    for (int q = tid; q < (2 * XT + ET + 2 * QT) / 16; q += TM)   // xh, xl, rop, qh, ql
+    for (int q = tid; q < (2 * XT + ET + 3 * QT) / 16; q += TM)   // xh, xl, rop, qh, qm, ql
         reinterpret_cast<uint4 *>(sm.xh)[q] = make_uint4(0, 0, 0, 0);
     if (tid == 0) {
         tc::mbar_init(&mbar_l, 1);
@@ -623,9 +651,27 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
         }
         __syncthreads();
         bool first = true;
-        for (int k = 0; k < nnet; ++k) {
-            const int ns = sm.net_start[k], ne = sm.net_start[k + 1];
-            if (ns == ne) continue;
+        const int ntl = *sm.ntiles;
+        // this thread's pair row of tile `it` (and its neighbor index), fetched one tile ahead
+        int a_n = 0, j_n = -1;
+        float4 q4_n = make_float4(0.f, 0.f, 0.f, 0.f);
+        auto fetch = [&](int it) {
+            const int tw = sm.tiles[it], k2 = tw >> 16, r = (tw & 0xFFFF) + tid;
+            a_n = 0;
+            j_n = -1;
+            q4_n = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (r < sm.net_start[k2 + 1]) {
+                const int e = sm.list[r];
+                a_n = e >> 12;
+                const long long row = (g0 + a_n) * S + (e & 0xFFF);
+                q4_n = __ldg(reinterpret_cast<const float4 *>(idr) + row);
+                j_n = __ldg(list_neigh + row) - 1;
+            }
+        };
+        if (ntl > 0) fetch(0);
+        for (int it = 0; it < ntl; ++it) {
+            const int k = sm.tiles[it] >> 16, r0 = sm.tiles[it] & 0xFFFF;
+            const int ne = sm.net_start[k + 1];
             if (k != cur_net) {
                 __syncthreads();
                 load_net(wtiles, params, k, sm);
@@ -637,19 +683,13 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
             const float isd[4] = {1.f / dstd[4 * ti], 1.f / dstd[4 * ti + 1],
                                   1.f / dstd[4 * ti + 2], 1.f / dstd[4 * ti + 3]};
             const float4 *v4 = reinterpret_cast<const float4 *>(sm.vec);
-            for (int r0 = ns; r0 < ne; r0 += TM) {
+            {
                 const int nrows = ne - r0 < TM ? ne - r0 : TM;
                 const bool valid = tid < nrows;
-                int a = 0, j = -1;
-                long long t = g0;
-                float4 q4 = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (valid) {
-                    const int e = sm.list[r0 + tid];
-                    a = e >> 12;
-                    t = g0 + a;
-                    q4 = __ldg(reinterpret_cast<const float4 *>(idr) + t * S + (e & 0xFFF));
-                    j = __ldg(list_neigh + t * S + (e & 0xFFF)) - 1;
-                }
+                const int a = a_n, j = j_n;
+                const long long t = g0 + a;
+                const float4 q4 = q4_n;
+                if (it + 1 < ntl) fetch(it + 1);
                 EnvRow en;
                 env_of(en, q4, P.rmin, P.rmax, av, isd);
                 float x[E];
@@ -790,12 +830,29 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
                                           f[0] * en.x, f[0] * en.y, f[0] * en.z,
                                           f[1] * en.x, f[1] * en.y, f[1] * en.z,
                                           f[2] * en.x, f[2] * en.y, f[2] * en.z, 0.f, 0.f, 0.f, 0.f};
+                    // three BF16 parts (hi, mid, lo: 24 significant bits) so the per-atom sums
+                    // keep FP32 accuracy
 #pragma unroll
                     for (int gq = 0; gq < 2; ++gq) {
-                        uint4 hq, lq;
-                        tc::split8(qv + 8 * gq, hq, SPLIT == 3 ? &lq : nullptr);
+                        uint4 hq, mq;
+                        float rem[8];
+                        tc::split8(qv + 8 * gq, hq, SPLIT == 3 ? &mq : nullptr);
                         *reinterpret_cast<uint4 *>(sm.qh + mn_chunk(tid, gq)) = hq;
-                        if (SPLIT == 3) *reinterpret_cast<uint4 *>(sm.ql + mn_chunk(tid, gq)) = lq;
+                        if (SPLIT == 3) {
+                            const uint32_t hw[4] = {hq.x, hq.y, hq.z, hq.w};
+                            const uint32_t mw[4] = {mq.x, mq.y, mq.z, mq.w};
+#pragma unroll
+                            for (int e = 0; e < 8; ++e) {
+                                const uint32_t hb = (hw[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
+                                const uint32_t mb = (mw[e >> 1] >> (16 * (e & 1))) & 0xFFFFu;
+                                rem[e] = qv[8 * gq + e] - __uint_as_float(hb << 16) -
+                                         __uint_as_float(mb << 16);
+                            }
+                            uint4 lq;
+                            tc::split8(rem, lq, nullptr);
+                            *reinterpret_cast<uint4 *>(sm.qm + mn_chunk(tid, gq)) = mq;
+                            *reinterpret_cast<uint4 *>(sm.ql + mn_chunk(tid, gq)) = lq;
+                        }
                     }
                     // one-hot operand: column tid holds 1 at M = a
                     if (my_chunk >= 0)
@@ -810,7 +867,8 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
                 }
                 if (pre_issue(ok)) goto done;
                 if (tid == 0)
-                    issue_rows<SPLIT, 64, QN>(tmem + TCOL_RED, sm.rop, sm.qh, sm.ql, first, &mbar_c);
+                    issue_rows<SPLIT == 3 ? 3 : 1, 64, QN>(tmem + TCOL_RED, sm.rop, sm.qh, sm.qm,
+                                                          sm.ql, first, &mbar_c);
                 pend_c = true;
                 first = false;
             }

@@ -262,13 +262,15 @@ nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
     const int S = P.ntypes * P.m;
     const int CAP = 2 * S;                         // pre-filtered candidates per atom
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double2 *kvec = reinterpret_cast<double2 *>(smem_raw) + 2 * warp * S;   // exact (x, y), (z, dd)
-    int *cand = reinterpret_cast<int *>(reinterpret_cast<double2 *>(smem_raw) + 2 * kWarps * S) +
-                warp * (CAP + S);
+    // accepted pairs: the output row (r, x, y, z) in the output dtype (the f64 values are the
+    // exact ones; the f32 ones their rounding, formed here once)
+    constexpr int KV = sizeof(TO) * 4;              // bytes per accepted pair
+    TO *kvec = reinterpret_cast<TO *>(smem_raw) + 4 * warp * S;
+    int *cand = reinterpret_cast<int *>(smem_raw + (size_t)KV * kWarps * S) + warp * (CAP + S);
     int *keys = cand + CAP;
     unsigned char *ktype = reinterpret_cast<unsigned char *>(
-                               reinterpret_cast<int *>(reinterpret_cast<double2 *>(smem_raw) +
-                                                       2 * kWarps * S) + kWarps * (CAP + S)) + warp * S;
+                               reinterpret_cast<int *>(smem_raw + (size_t)KV * kWarps * S) +
+                               kWarps * (CAP + S)) + warp * S;
     const long long total = (long long)P.batch * P.natoms;
     for (long long t = (long long)blockIdx.x * kWarps + warp; t < total;
          t += (long long)gridDim.x * kWarps) {
@@ -453,8 +455,7 @@ nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
             if (inT && at < S) {
                 keys[at] = key;
                 ktype[at] = (unsigned char)tj;
-                kvec[2 * at] = make_double2(px, py);
-                kvec[2 * at + 1] = make_double2(pz, pdd);
+                store4(kvec + 4 * at, pair_r<TO>(pdd), conv<TO>(px), conv<TO>(py), conv<TO>(pz));
             }
             n_acc += __popc(ma);
         }
@@ -483,12 +484,10 @@ nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
             for (int f = 0; f < nst; ++f) rank += (ktype[f] == ty) & (keys[f] < key);
             if (rank >= P.m) continue;
             const int j = key / nimg;
-            const double2 xa = kvec[2 * e], xb = kvec[2 * e + 1];
-            const double x = xa.x, y = xa.y, z = xb.x, dd = xb.y;
+            const TO *kv = kvec + 4 * e;
             const long long slot = row + (long long)ty * P.m + rank;
             list_neigh[slot] = j + 1;
-            store4(image_dr + 4 * slot, pair_r<TO>(dd), conv<TO>(x), conv<TO>(y),
-                   conv<TO>(z));
+            store4(image_dr + 4 * slot, kv[0], kv[1], kv[2], kv[3]);
         }
         // ---- phase D: clear the empty slots (the occupied-slot form leaves them untouched:
         // its readers take the block lengths from num_neigh)
@@ -653,7 +652,7 @@ static int neighbor_build(int batch, int natoms, int ntypes, int m_neigh, double
     }
     ProfScope ps("nb_search", s);
     const int S = ntypes * m_neigh;
-    const size_t smem = (size_t)kWarps * (S * 32 + 3 * S * 4 + S);
+    const size_t smem = (size_t)kWarps * (S * 4 * (out_dtype == MATPL_F64 ? 8 : 4) + 3 * S * 4 + S);
     if (out_dtype == MATPL_F64) {
         cudaFuncSetAttribute(nb_search<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
