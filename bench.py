@@ -213,7 +213,7 @@ def nep_workload(natoms=NEP_NATOMS, seed=NEP_SEED_STRUCT):
     st = structures.random_packed(natoms, NEP_DENSITY, NEP_ELEMENTS, [0.25] * 4, seed=seed)
     fr = NP.frames_from_structures([st], cfg.cutoff[0])
     prm = NP.init_params(cfg, NEP_SEED_W, energy_shift=-3.0)
-    return cfg, fr, prm
+    return cfg, fr, prm, st
 
 
 def cpu_baseline_nep(steps, warmup):
@@ -222,7 +222,7 @@ def cpu_baseline_nep(steps, warmup):
     from oracle import nep_oracle as NO
     ncores = os.cpu_count() or 1
     torch.set_num_threads(ncores)
-    cfg, fr, prm = nep_workload(NEP_CPU_SAMPLE, seed=NEP_SEED_STRUCT + 1)
+    cfg, fr, prm, _ = nep_workload(NEP_CPU_SAMPLE, seed=NEP_SEED_STRUCT + 1)
     cr, ca = NO.maxneigh(fr, cfg.cutoff[0], cfg.cutoff[1])
     mr, ma = int(cr.max()), int(ca.max())
     tm = torch.tensor(fr.type_map)
@@ -247,12 +247,103 @@ def cpu_baseline_nep(steps, warmup):
             "sec_per_step": med, "steps": steps}
 
 
+def cuda_kernel_ms(fn, calls):
+    """Device time per call of every CUDA kernel ``fn`` launches, from the CUPTI activity
+    records torch.profiler collects: ({kernel: ms per call}, total ms per call).  Copies and
+    memsets are left out.  (None, None) when the profiler records no kernel."""
+    from torch.autograd import DeviceType
+    from torch.profiler import ProfilerActivity, profile
+    torch.cuda.synchronize()
+    with profile(activities=[ProfilerActivity.CUDA]) as p:
+        for _ in range(calls):
+            fn()
+        torch.cuda.synchronize()
+    per = {}
+    for e in p.events():
+        if e.device_type != DeviceType.CUDA or e.name.startswith(("Memcpy", "Memset")):
+            continue
+        per[e.name] = per.get(e.name, 0.0) + e.time_range.elapsed_us() * 1e-3 / calls
+    if not per:
+        return None, None
+    return per, sum(per.values())
+
+
+def nep_reference_gpu(cfg, prm, st, r32, r64, ours_ms, ours_e2e_ms, ours_eval_ms, mr, ma,
+                      calls=10):
+    """The reference's own GPU NEP evaluator on the same structure and model: the LAMMPS
+    NEP3::compute_large_box_optim (nep3.cu:551-810), built unmodified for sm_103a from a staged
+    copy of its sources (baseline/ref_gpu.py), reading a nep5 file written from the same
+    parameters, on the LAMMPS view of the box (local atoms, ghost images within the largest
+    cutoff + 1 A skin, full lists), driven as PairMATPL::compute drives it
+    (pair_matpl.cpp:1093-1190).  Its call is synchronous: host positions in (plus type and list
+    arrays on a rebuild step), host energies / forces / virial out."""
+    try:
+        from baseline import ref_gpu
+    except ImportError as e:
+        return {"unavailable": f"comparator module not importable: {e}"}
+    from matpl_gb300 import lammps as L, nep as NP
+    if ref_gpu.load() is None:
+        return {"unavailable": "comparator library not built (reference GPU sources not staged)"}
+    s = L.lammps_system(st.lattice, st.frac @ st.lattice, st.types + 1,
+                        max(cfg.cutoff) + LMP_SKIN, seed=NEP_SEED_STRUCT)
+    ref = ref_gpu.RefNEP(NP.gpumd_text(cfg, prm, (mr, ma)), s, s["type"] - 1,
+                         device=torch.cuda.current_device())
+    try:
+        ei, f, v = ref.compute(True)
+        n = s["nlocal"]
+        F = L.fold_ghosts(f, s["owner"], n)
+        F64 = r64["Force"].reshape(-1, 3).double().cpu().numpy()
+        F32 = r32["Force"].reshape(-1, 3).double().cpu().numpy()
+        V64 = r64["Virial"].reshape(-1)[[0, 4, 8, 1, 2, 5]].double().cpu().numpy()
+        E64 = float(r64["Etot"].sum())
+        parity = {"force_max_abs_err_vs_f64_eV_per_A": float(np.abs(F - F64).max()),
+                  "force_rmse_vs_f64_eV_per_A": float(np.sqrt(((F - F64) ** 2).mean())),
+                  "ours_f32_force_max_abs_err_vs_f64_eV_per_A": float(np.abs(F32 - F64).max()),
+                  "energy_err_per_atom_eV": abs(float(ei.sum()) - E64) / n,
+                  "virial_max_abs_err_eV": float(np.abs(v - V64).max())}
+
+        def per_call(build, k):
+            ref.compute(build)
+            t0 = time.perf_counter()
+            for _ in range(k):
+                ref.compute(build)
+            return (time.perf_counter() - t0) * 1e3 / k
+
+        call_ms = per_call(False, calls)
+        call_build_ms = per_call(True, max(3, calls // 2))
+        try:
+            kern, kern_ms = cuda_kernel_ms(lambda: ref.compute(False), 3)
+        except Exception as e:  # noqa: BLE001 - profiler support differs between builds
+            kern, kern_ms = None, None
+            parity["kernel_timing_error"] = str(e)[:200]
+    finally:
+        ref.close()
+    out = {"source": "src/lmps/lammps-libtorch/MATPL/NEP_GPU (nep3.cu, nep3_large_box.cuh), "
+                     "unmodified, nvcc -O3 sm_103a",
+           "system": {"nlocal": n, "nghost": s["nghost"], "max_listed": int(s["numneigh"].max()),
+                      "list_capacity": ref.capacity, "max_pairs_in_cutoffs": ref.max_pairs},
+           "call_ms": call_ms, "call_rebuild_ms": call_build_ms,
+           "kernels_ms_per_call": kern_ms, "kernels": kern,
+           "ours_step_ms": ours_ms, "ours_nep_eval_ms": ours_eval_ms, "ours_e2e_ms": ours_e2e_ms,
+           "e2e_speedup": call_ms / ours_e2e_ms,
+           "e2e_note": "reference call (host positions in, lists already on the GPU, E/F/V out) "
+                       "vs our end-to-end step, which also rebuilds the exact lists every step",
+           **parity}
+    if kern_ms:
+        out["device_speedup"] = kern_ms / ours_ms
+        out["eval_speedup"] = kern_ms / ours_eval_ms
+        out["device_note"] = ("device_speedup: its kernels per call (list filter + sort, "
+                              "descriptor, forces, virial) vs our whole device step (exact list "
+                              "build + fused E/F/V); eval_speedup: vs nep_eval alone")
+    return out
+
+
 def run_nep(args, ws, local, steps, warmup, sample_clocks=True):
     """The NEP step on this GPU: calculate_neighbor (exact FP64 lists, the reference's layout) +
     the fused FP32 descriptor / network / force / virial kernel, 100,000 atoms."""
     from matpl_gb300 import _lib, nep as NP, ops
     dev = torch.device("cuda", local)
-    cfg, fr, prm = nep_workload(args.nep_atoms)
+    cfg, fr, prm, st = nep_workload(args.nep_atoms)
     N = fr.natoms
     c = lambda a, dt: torch.tensor(np.ascontiguousarray(a), dtype=dt, device=dev)  # noqa: E731
     na, tm, bx, bo, nc = (c(fr.num_atom.reshape(-1, 1), torch.int64), c(fr.type_map, torch.int64),
@@ -358,6 +449,8 @@ def run_nep(args, ws, local, steps, warmup, sample_clocks=True):
         if tr:   # recorded for the 100,000-atom launch; DRAM bytes scale with atoms
             traffic = {"bytes_per_launch": tr["bytes_per_launch"] * N / NEP_NATOMS,
                        "note": tr.get("note")}
+    ref_gpu = nep_reference_gpu(cfg, prm, st, r32, r64, ms, e2e_ms,
+                                per_kernel["nep_eval"]["ms_per_launch"], mr, ma)
     return {
         "metric": NEP_METRIC, "value": ws * N / (ms * 1e-3), "unit": "atom-steps/s",
         "ms_per_step": ms, "steps": steps, "warmup": warmup, "dtype": "f32 (f64 lists, f64 sums)",
@@ -381,6 +474,7 @@ def run_nep(args, ws, local, steps, warmup, sample_clocks=True):
                      "hbm": {"achieved": ev_bytes / t_eval / 1e9, "peak": hbm_peak,
                              "unit": "GB/s", "frac": ev_bytes / t_eval / 1e9 / hbm_peak,
                              "algorithmic_bytes_per_launch": ev_bytes}},
+        "reference_gpu": ref_gpu,
         "neighbor_roofline": {"kernel": "nep_neighbor", "bound": "fp64 (exact reference arithmetic)",
                               "hbm_achieved": nb_bytes / t_nb / 1e9, "hbm_peak": hbm_peak,
                               "unit": "GB/s", "frac": nb_bytes / t_nb / 1e9 / hbm_peak,
@@ -694,6 +788,82 @@ def run_nep_train_line(args, ws, rank, local):
 
 
 VARIANT_ATOMS = 8000
+
+
+def calcops_reference_gpu(ln, dev, reps=10):
+    """CalcOps_cuda calculateForce / calculateVirial: the reference's own kernels
+    (src/op/kernel/calculateForce.cu, calculateVirial.cu, built unmodified for sm_103a from a
+    staged copy, baseline/ref_gpu.py) against this library's operators on the headline list
+    (32,000 atoms, S = 300 slots), FP64, the same seeded dE / Ri_d / Rij / centre term.  Each op
+    is timed as the torch op runs it: the reference's output set-up (CalcOps.cpp:17-20,
+    :181-184: zero-fill, centre-term copy) + its launcher, against the C-ABI call."""
+    try:
+        from baseline import ref_gpu
+    except ImportError as e:
+        return {"unavailable": f"comparator module not importable: {e}"}
+    from matpl_gb300 import _lib
+    from matpl_gb300._lib import check, ptr
+    rl = ref_gpu.load()
+    if rl is None:
+        return {"unavailable": "comparator library not built (reference GPU sources not staged)"}
+    lib = _lib.load()
+    B, N, S = ln.shape
+    nb = (ln.to(torch.int32) - 1).contiguous()          # 0-based, -1 = empty slot
+    g = torch.Generator(device=dev).manual_seed(5)
+    f64 = dict(dtype=torch.float64, device=dev)
+    dE = torch.randn(B, N, 4 * S, generator=g, **f64)
+    Ri_d = torch.randn(B, N, 4 * S, 3, generator=g, **f64)
+    Rij = torch.randn(B, N, S, 3, generator=g, **f64)
+    Fc = torch.randn(B, N, 3, generator=g, **f64)
+    fo, fr = torch.empty(B, N, 3, **f64), torch.empty(B, N, 3, **f64)
+    vo, vr = torch.empty(B, 9, **f64), torch.empty(B, 9, **f64)
+    avo, avr = torch.empty(B, N, 9, **f64), torch.empty(B, N, 9, **f64)
+    st = torch.cuda.current_stream(dev).cuda_stream
+    di = dev.index if dev.index is not None else torch.cuda.current_device()
+
+    def ours_f():
+        check(lib.matpl_calc_force(_lib.MATPL_F64, ptr(nb), ptr(dE), ptr(Ri_d), ptr(Fc), B, N,
+                                   S, 0, ptr(fo), st), "matpl_calc_force")
+
+    def ref_f():
+        fr.zero_()
+        fr.copy_(Fc)
+        rl.refcalc_force(0, ptr(nb), ptr(dE), ptr(Ri_d), B, N, S, ptr(fr), 0, di)
+
+    def ours_v():
+        check(lib.matpl_calc_virial(_lib.MATPL_F64, ptr(nb), ptr(dE), ptr(Rij), ptr(Ri_d), B, N,
+                                    S, 0, ptr(vo), ptr(avo), st), "matpl_calc_virial")
+
+    def ref_v():
+        vr.zero_()
+        avr.zero_()
+        rl.refcalc_virial(0, ptr(nb), ptr(dE), ptr(Rij), ptr(Ri_d), B, N, S, ptr(vr), ptr(avr),
+                          0, di)
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    rel = lambda a, b: float((a - b).abs().max() / b.abs().max().clamp_min(1e-300))  # noqa: E731
+    out = {"config": f"FP64, batch {B}, {N} atoms, {S} slots, "
+                     f"{int((nb >= 0).sum())} occupied; inputs {(dE.numel() + Ri_d.numel() + Rij.numel()) * 8 / 1e9:.2f} GB"}
+    for name, o, r, res in (("calculateForce", ours_f, ref_f, lambda: [(fo, fr)]),
+                            ("calculateVirial", ours_v, ref_v, lambda: [(vo, vr), (avo, avr)])):
+        o(); r()
+        torch.cuda.synchronize()
+        err = max(rel(a, b) for a, b in res())
+        t_o, t_r = timed(o), timed(r)
+        out[name] = {"ours_ms": t_o, "reference_ms": t_r, "speedup": t_r / t_o,
+                     "max_rel_diff": err}
+    return out
 
 
 def run_dp_variants(args, ws, local):
@@ -1269,6 +1439,7 @@ def run_ours(args, ws, rank, local):
         md_r = run_md(args, ws, local, steps=200)
     data_r = run_data(args, ws, local) if not args.no_data else None
     variants_r = run_dp_variants(args, ws, local) if not args.no_variants else None
+    refops_r = calcops_reference_gpu(ln, dev) if not args.no_variants else None
     nep_train_r = None
     if not args.no_nep_train:
         nep_train_r = run_nep_train(args, ws, local, steps=10, warmup=3)
@@ -1320,7 +1491,7 @@ def run_ours(args, ws, rank, local):
             "gpu_launches": launches, "kernels": per_kernel, "roofline": roof,
             "clocks": clocks, "cpu_baseline": cb, "nep": nep, "train": train_r, "md": md_r,
             "lammps": lmp_r, "nep_train": nep_train_r, "data_path": data_r,
-            "dp_variants": variants_r}
+            "dp_variants": variants_r, "reference_gpu_ops": refops_r}
     print(json.dumps(line))
 
 

@@ -232,6 +232,50 @@ def pack_params(cfg: NepConfig, p: Dict[str, torch.Tensor]) -> torch.Tensor:
     return flat
 
 
+_SYMBOLS = ("H He Li Be B C N O F Ne Na Mg Al Si P S Cl Ar K Ca Sc Ti V Cr Mn Fe Co Ni Cu Zn Ga "
+            "Ge As Se Br Kr Rb Sr Y Zr Nb Mo Tc Ru Rh Pd Ag Cd In Sn Sb Te I Xe Cs Ba La Ce Pr "
+            "Nd Pm Sm Eu Gd Tb Dy Ho Er Tm Yb Lu Hf Ta W Re Os Ir Pt Au Hg Tl Pb Bi Po At Rn Fr "
+            "Ra Ac Th Pa U Np Pu Am Cm Bk Cf Es Fm Md No Lr").split()
+
+
+def gpumd_text(cfg: NepConfig, p: Dict[str, torch.Tensor],
+               max_neighbors: Sequence[int] = (500, 300)) -> str:
+    """The model as a ``nep5`` potential file for LAMMPS / GPUMD (``extract_model``,
+    utils/nep_to_gpumd.py:61-150): header lines (``nep5`` or ``nep5_zbl`` + ``zbl rc/2 rc``,
+    cutoff with the list capacities, n_max, basis_size, l_max, ``ANN H 0``), then per element
+    W0^T, -b0, W1 and -b1, a common bias 0, ``c_param_2`` and ``c_param_3`` as [n, k, t1, t2],
+    and q_scaler.  Values are written with 9 significant digits, which round-trips every FP32
+    value the reader parses them into."""
+    T, F, H = cfg.ntypes, cfg.feature_nums, cfg.neuron
+    names = [_SYMBOLS[z - 1] for z in cfg.atom_type]
+    head = f"nep5{'_zbl' if cfg.zbl is not None else ''}   {T} {' '.join(names)}\n"
+    if cfg.zbl is not None:
+        head += f"zbl   {cfg.zbl / 2} {cfg.zbl}\n"
+    head += (f"cutoff {cfg.cutoff[0]} {cfg.cutoff[1]} {int(max_neighbors[0])} "
+             f"{int(max_neighbors[1])}\n")
+    head += f"n_max  {' '.join(map(str, cfg.n_max))}\n"
+    head += f"basis_size {' '.join(map(str, cfg.basis_size))}\n"
+    head += f"l_max  {' '.join(map(str, cfg.l_max))}\n"
+    head += f"ANN    {H} 0\n"
+    f64 = lambda k: p[k].detach().to(torch.float64).cpu()  # noqa: E731
+    vals = []
+    for t in range(T):
+        pre = f"fitting_net.{t}.layers."
+        vals.append(f64(pre + "0.weight").t().reshape(-1))
+        vals.append(-f64(pre + "0.bias").reshape(-1))
+        vals.append(f64(pre + "1.weight").reshape(-1))
+        vals.append(-f64(pre + "1.bias").reshape(-1))
+    vals.append(torch.zeros(1, dtype=torch.float64))
+    vals.append(f64("c_param_2").permute(2, 3, 0, 1).reshape(-1))
+    if cfg.l_max[0] > 0:
+        vals.append(f64("c_param_3").permute(2, 3, 0, 1).reshape(-1))
+    vals.append(f64("q_scaler").reshape(-1))
+    flat = torch.cat(vals).numpy().astype(np.float32)
+    assert flat.size == T * (F * H + 2 * H + 1) + 1 + T * T * (
+        cfg.nr * cfg.kr + (cfg.na * cfg.ka if cfg.l_max[0] > 0 else 0)) + F
+    return head + "\n".join("%.9g" % float(v) for v in flat) + "\n"
+
+
 # ----------------------------------------------------------------------------------------------
 # GPU evaluator (the NEP.forward drop-in)
 # ----------------------------------------------------------------------------------------------

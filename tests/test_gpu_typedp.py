@@ -43,7 +43,8 @@ def test_typedp_matches_reference(golden_case):
 def test_typedp_fused_matches_reference(golden_case):
     """TypeDP in the fused kernels (v(t_j) folded into the first layer's bias of per-pair
     nets): FP64 = the reference's TypeDP (golden) to 1e-10; FP32 and the BF16x3 tcgen05 form
-    within 1e-5 eV/atom (energy) and 1e-5 of the force scale."""
+    within 1e-5 eV/atom (energy) and 1e-5 of the force scale (the BF16x3 form: or 1e-6 eV/A,
+    whichever is larger)."""
     from matpl_gb300.typedp import fused_model
     from tests.conftest import load_golden
     g = load_golden("typedp_hfo48")
@@ -66,7 +67,10 @@ def test_typedp_fused_matches_reference(golden_case):
             np.testing.assert_allclose(E, g["Etot"].ravel(), rtol=1e-11)
         else:
             assert np.abs(E - g["Etot"].ravel()).max() <= 1e-5 * 48
+        # the BF16x3 form keeps per-pair terms to 2^-16 relative (two-part split), an absolute
+        # floor of ~1e-6 eV/A once they cancel; this weakly forced cell has max|F| ~ 0.04 eV/A
+        f_atol = max(tol * fs, 1e-6) if prec == "mixed" else tol * fs
         np.testing.assert_allclose(F.detach().double().cpu().numpy().reshape(g["Force"].shape),
-                                   g["Force"], rtol=0, atol=tol * fs)
+                                   g["Force"], rtol=0, atol=f_atol)
         np.testing.assert_allclose(V.detach().double().cpu().numpy().reshape(g["Virial"].shape),
                                    g["Virial"], rtol=0, atol=10 * tol * vs)
