@@ -249,20 +249,28 @@ def cpu_baseline_nep(steps, warmup):
 
 def cuda_kernel_ms(fn, calls):
     """Device time per call of every CUDA kernel ``fn`` launches, from the CUPTI activity
-    records torch.profiler collects: ({kernel: ms per call}, total ms per call).  Copies and
-    memsets are left out.  (None, None) when the profiler records no kernel."""
-    from torch.autograd import DeviceType
+    records torch.profiler collects (read from its trace, where kernels launched by a library
+    outside torch appear too): ({kernel: ms per call}, total ms per call).  Copies and memsets
+    are left out.  (None, None) when the trace holds no kernel."""
+    import tempfile
     from torch.profiler import ProfilerActivity, profile
     torch.cuda.synchronize()
-    with profile(activities=[ProfilerActivity.CUDA]) as p:
+    with profile(activities=[ProfilerActivity.CPU, ProfilerActivity.CUDA]) as p:
         for _ in range(calls):
             fn()
         torch.cuda.synchronize()
+    fd, path = tempfile.mkstemp(suffix=".json")
+    os.close(fd)
+    try:
+        p.export_chrome_trace(path)
+        with open(path) as f:
+            trace = json.load(f)
+    finally:
+        os.remove(path)
     per = {}
-    for e in p.events():
-        if e.device_type != DeviceType.CUDA or e.name.startswith(("Memcpy", "Memset")):
-            continue
-        per[e.name] = per.get(e.name, 0.0) + e.time_range.elapsed_us() * 1e-3 / calls
+    for e in trace.get("traceEvents", []):
+        if e.get("cat") == "kernel" and e.get("ph") == "X":
+            per[e["name"]] = per.get(e["name"], 0.0) + float(e.get("dur", 0.0)) * 1e-3 / calls
     if not per:
         return None, None
     return per, sum(per.values())
@@ -449,8 +457,8 @@ def run_nep(args, ws, local, steps, warmup, sample_clocks=True):
         if tr:   # recorded for the 100,000-atom launch; DRAM bytes scale with atoms
             traffic = {"bytes_per_launch": tr["bytes_per_launch"] * N / NEP_NATOMS,
                        "note": tr.get("note")}
-    ref_gpu = nep_reference_gpu(cfg, prm, st, r32, r64, ms, e2e_ms,
-                                per_kernel["nep_eval"]["ms_per_launch"], mr, ma)
+    ref_gpu = None if args.no_ref_gpu else nep_reference_gpu(
+        cfg, prm, st, r32, r64, ms, e2e_ms, per_kernel["nep_eval"]["ms_per_launch"], mr, ma)
     return {
         "metric": NEP_METRIC, "value": ws * N / (ms * 1e-3), "unit": "atom-steps/s",
         "ms_per_step": ms, "steps": steps, "warmup": warmup, "dtype": "f32 (f64 lists, f64 sums)",
@@ -978,8 +986,10 @@ def run_data(args, ws, local):
             "cpu_baseline": cb}
 
 
-MD_METRIC = "batched replica MD atom-steps/s (velocity Verlet, DP mixed, one graph launch per step)"
+MD_METRIC = ("batched replica MD atom-steps/s (velocity Verlet, DP mixed, all replicas in one "
+             "ragged step, 10 steps per CUDA-graph launch, Verlet skin 1.0 A)")
 MD_REPLICAS, MD_NMIN, MD_NMAX, MD_SEED = 256, 64, 2048, 77
+MD_STEPS_PER_GRAPH = 10
 
 
 def md_replicas(n=MD_REPLICAS, seed=MD_SEED):
@@ -1001,8 +1011,11 @@ def md_replicas(n=MD_REPLICAS, seed=MD_SEED):
 def run_md(args, ws, local, steps):
     """256 Cu replicas of uneven size, DP (1 type, m = 100, Rc 6, random weights N(0, 1/fan_in)),
     Maxwell-Boltzmann velocities at 300 K, dt = 1 fs: `steps` velocity-Verlet steps of every
-    replica, each step one CUDA-graph launch (neighbor search + E/F/V + update per group).
-    Reports the total-energy drift per atom, FP64 energy sums."""
+    replica.  All replicas form one ragged atom array: per step one drift (+ rebuild flag), the
+    gated skin-list build (Rc + 1 A, run only after some atom moved > 0.5 A), one cutoff filter,
+    one mixed-form evaluation, one kick; 10 steps per CUDA-graph launch.  The evaluation's tile
+    shape is autotuned on the replicas' own list.  Reports the total-energy drift per atom (FP64
+    energy sums) and the number of list builds."""
     from matpl_gb300 import autotune, md, params as P, structures
     dev = torch.device("cuda", local)
     autotune.set_tuning(0, 0)              # the headline's tuned tile shape is for its own box
@@ -1015,15 +1028,21 @@ def run_md(args, ws, local, steps):
     davg, dstd = P.calc_stat(cfg, l0.cpu().numpy(), r0.cpu().numpy(), st.types)
     prm = P.init_params(cfg, SEED_W)
     sim = md.ReplicaMD(cfg, prm, davg, dstd, reps, [63.546], dt_fs=1.0, precision="mixed",
-                       device=dev)
+                       device=dev, skin=1.0, steps_per_graph=MD_STEPS_PER_GRAPH)
+    tuning = "automatic"
+    if not args.no_tune:
+        t = autotune.tune_dp_mixed(sim.model, sim.ln, sim.types, sim.present, sim.idr,
+                                   num_neigh=sim.nn)
+        tuning = {"group_atoms": t["group_atoms"], "ctas_per_sm": t["ctas_per_sm"]}
     sim.capture()
     e0 = sim.energies().sum(1)
     n = sim.natoms()
+    b0 = sim.rebuilds()
     torch.cuda.synchronize()
     barrier(ws)
     e_0, e_1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e_0.record()
-    chunk = max(1, steps // 10)
+    chunk = max(MD_STEPS_PER_GRAPH, (steps // 10) // MD_STEPS_PER_GRAPH * MD_STEPS_PER_GRAPH)
     worst = 0.0
     done = 0
     while done < steps:
@@ -1035,18 +1054,23 @@ def run_md(args, ws, local, steps):
     e_1.record()
     torch.cuda.synchronize()
     sim.check_errors()
+    autotune.set_tuning(0, 0)
     ms = max_over_ranks(e_0.elapsed_time(e_1) / steps, ws)
     drift = (e - e0) / n
+    pairs = int(sim.nn.sum())
     return {"metric": MD_METRIC, "value": ws * sim.natoms_total / (ms * 1e-3),
             "unit": "atom-steps/s", "ms_per_step": ms, "steps": steps,
             "config": {"workload": f"{len(reps)} Cu FCC replicas, atom counts log-uniform in "
                                    f"[{MD_NMIN}, {MD_NMAX}] ({int(n.min())}..{int(n.max())}, "
-                                   f"{sim.natoms_total} atoms in {len(sim.groups)} size groups), "
-                                   "DP m=100 Rc 6, 300 K, dt 1 fs, neighbor lists rebuilt every step",
-                       "natoms_total": sim.natoms_total, "size_groups": len(sim.groups),
+                                   f"{sim.natoms_total} atoms), DP m=100 Rc 6, 300 K, dt 1 fs, "
+                                   "Verlet skin 1.0 A (rebuild when an atom moved > 0.5 A)",
+                       "natoms_total": sim.natoms_total, "pairs_within_rc": pairs,
+                       "steps_per_graph_launch": MD_STEPS_PER_GRAPH,
+                       "list_builds_in_timed_steps": sim.rebuilds() - b0,
+                       "skin_list_capacity_per_type": sim.cap,
                        "energy_drift_per_atom_eV": {"final_mean_abs": float(np.mean(np.abs(drift))),
                                                     "max_abs_over_run": worst},
-                       "tile_tuning": "automatic"}}
+                       "tile_tuning": tuning}}
 
 
 LMP_METRIC = ("LAMMPS pair_style DP step atom-steps/s (LAMMPS host positions + full list in, "
@@ -1439,7 +1463,8 @@ def run_ours(args, ws, rank, local):
         md_r = run_md(args, ws, local, steps=200)
     data_r = run_data(args, ws, local) if not args.no_data else None
     variants_r = run_dp_variants(args, ws, local) if not args.no_variants else None
-    refops_r = calcops_reference_gpu(ln, dev) if not args.no_variants else None
+    refops_r = calcops_reference_gpu(ln, dev) if not (args.no_variants or args.no_ref_gpu) \
+        else None
     nep_train_r = None
     if not args.no_nep_train:
         nep_train_r = run_nep_train(args, ws, local, steps=10, warmup=3)
@@ -1572,6 +1597,9 @@ def main():
     ap.add_argument("--nep-train-atoms", type=int, default=NEP_TRAIN_NATOMS,
                     help="atoms of the NEP training batch (20,000; smaller for captures)")
     ap.add_argument("--no-nep-train", action="store_true", help="skip the NEP training workload")
+    ap.add_argument("--no-ref-gpu", action="store_true",
+                    help="skip the reference's own GPU code (comparator) beside the NEP step and "
+                         "the CalcOps force / virial ops")
     ap.add_argument("--no-data", action="store_true", help="skip the data-path statistics pass")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the compressed / type-embedding DP variants")

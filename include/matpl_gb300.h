@@ -543,6 +543,55 @@ int matpl_lammps_dp_compute_models(matpl_lammps_dp *handle, int nmodels, int nlo
                                    const int *type, double *f, double *eng, double *virial,
                                    double *eatom, double *min_rsq);
 
+/* ------------------------------------------------------------------------------------
+ * Batched replica MD (one DP model, many independent periodic replicas of uneven size in one
+ * ragged atom array: replica r owns atoms [rep_start[r], rep_start[r+1]); atom_rep[i] = its
+ * replica; lattice / inv_lattice [nrep, 3, 3] with the cell vectors as rows).  No counterpart
+ * in the reference's GPU code: it is the in-GPU form of the LAMMPS loop around the pair style
+ * (velocity Verlet, and the neighbor list kept at Rc + skin and rebuilt when an atom has
+ * moved more than skin / 2, the rule pair_matpl.cpp:1096-1110 defers to).  Positions x
+ * [ntot, 3] FP64 Angstrom stay unwrapped.
+ *
+ * matpl_md_drift: x += v dt + a dt^2 / 2; sets *gate = 1 when some |x - x_ref| > skin / 2.
+ *
+ * matpl_md_skin_build: only when *gate != 0 (read on the device), every pair within r_list of
+ * every atom, all periodic images, into nbr / img [ntot, ntypes * cap] (per type block: global
+ * neighbor index, image (n_a, n_b, n_c) as three signed bytes, d = x_j - x_i + n L) and cnt
+ * [ntot, ntypes]; x_ref = x; then *gate = 0 and ++*nbuild (nbuild may be NULL).  work [nwork]
+ * int32 pairs (replica, first local atom) cover every replica in blocks of 128 atoms.  err_dev:
+ * MATPL_KERR_NEIGHBOR_OVERFLOW (a block needs more than cap), MATPL_KERR_BAD_TYPE,
+ * MATPL_KERR_BAD_BOX (a cell needing more than 63 images, or an image index past +-127).
+ *
+ * matpl_md_skin_filter: the pairs of the skin list with 1e-8 < r^2 < rc^2 at the current
+ * positions, in list order, as the occupied-slot list matpl_dp_eval_occupied reads (B = 1,
+ * N = ntot, S = ntypes * m): list_neigh 1-based global indices, image_dr (r, x_j - x_i) rows in
+ * dtype (MATPL_F64 / MATPL_F32), num_neigh [ntot, ntypes]; more than m in a block sets
+ * MATPL_KERR_NEIGHBOR_OVERFLOW.  Slots past the block lengths are not written.
+ *
+ * matpl_md_kick: mode 0 a = F inv_mass; mode 1 also v += (a_old + a) dt / 2.  Per replica,
+ * ke[r] = sum conv_ke m v^2 / 2 and pe[r] = sum ei, FP64, in a fixed order (force [ntot, 3] and
+ * ei [ntot] in dtype). */
+int matpl_md_drift(int ntot, double dt, double skin, double *x, const double *v,
+                   const double *a, const double *x_ref, int32_t *gate, void *stream);
+
+int matpl_md_skin_build(int nrep, int ntot, int ntypes, int cap, double r_list,
+                        const int32_t *rep_start, const int32_t *work, int nwork,
+                        const double *lattice, const double *inv_lattice,
+                        const int32_t *type_map, const double *x, int32_t *nbr, int32_t *img,
+                        int32_t *cnt, double *x_ref, int32_t *gate, int32_t *nbuild,
+                        int32_t *err_dev, void *stream);
+
+int matpl_md_skin_filter(int dtype, int ntot, int ntypes, int cap, int m, double rc,
+                         const int32_t *atom_rep, const double *lattice, const int32_t *nbr,
+                         const int32_t *img, const int32_t *cnt, const double *x,
+                         int32_t *list_neigh, void *image_dr, int32_t *num_neigh,
+                         int32_t *err_dev, void *stream);
+
+int matpl_md_kick(int dtype, int mode, int nrep, double dt, double conv_ke,
+                  const int32_t *rep_start, const double *inv_mass, const double *mass,
+                  const void *force, const void *ei, double *v, double *a, double *ke,
+                  double *pe, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

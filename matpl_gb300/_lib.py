@@ -107,6 +107,10 @@ SIGNATURES = {
     "matpl_lammps_dp_num_models": (_i, [_vp]),
     "matpl_lammps_dp_compute_models": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp,
                                             _vp, _vp, _vp, _vp]),
+    "matpl_md_drift": (_i, [_i, _d, _d, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "matpl_md_skin_build": (_i, [_i, _i, _i, _i, _d, _vp, _vp, _i] + [_vp] * 12),
+    "matpl_md_skin_filter": (_i, [_i, _i, _i, _i, _i, _d] + [_vp] * 11),
+    "matpl_md_kick": (_i, [_i, _i, _i, _d, _d] + [_vp] * 10),
 }
 
 
