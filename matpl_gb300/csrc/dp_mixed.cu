@@ -53,9 +53,12 @@ constexpr int VW = 28;                  // per-net vector stride in floats (25 p
 constexpr int kMaxTypes = 16;
 constexpr int kDrainPolls = 1 << 24;    // bound of the waits that drain MMAs before exit
 
-// TMEM columns: [0, 32) layer accumulator; forward: [32, 64) descriptor accumulator;
-// backward: [32, 64) layer-2 tanh stash, [64, 80) F_i / virial accumulator.
-constexpr uint32_t TCOL_A = 32, TCOL_STASH = 32, TCOL_RED = 64;
+// TMEM columns: [0, 32) layer accumulator; forward: [64, 128) descriptor accumulator (the G hi
+// and lo halves side by side); backward: [32, 64) layer-2 tanh stash, [64, 112) F_i / virial
+// accumulator (the three BF16 parts side by side).  Each small MMA costs the tensor core about
+// as much as its issue, so the split parts of an operand are laid side by side along N (one
+// MMA per K step) rather than issued as separate products.
+constexpr uint32_t TCOL_A = 64, TCOL_STASH = 32, TCOL_RED = 64;
 
 struct MixParams {
     int batch, natoms, nslots, nghost, ntypes, m, present_mask, ga;
@@ -427,7 +430,7 @@ dp_embed_fwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
         tc::mbar_init(&mbar_l, 1);
         tc::mbar_init(&mbar_c, 1);
     }
-    if (warp == 0) tc::tmem_alloc(&tmem_base, 64);
+    if (warp == 0) tc::tmem_alloc(&tmem_base, 128);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -547,8 +550,10 @@ dp_embed_fwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
                 store_row<SPLIT>(sm, tid, x, 0.f);       // G, the B operand of the contraction
                 if (pre_issue(ok)) goto done;
                 if (tid == 0)
-                    issue_rows<SPLIT == 3 ? 2 : 1, 128, KP>(tmem + TCOL_A, sm.rop, sm.xh, sm.xl,
-                                                          nullptr, first, &mbar_c);
+                    // N = 64: columns [0, 32) against the G hi tile, [32, 64) against the lo
+                    // tile that follows it in shared memory
+                    issue_rows<1, 128, SPLIT == 3 ? 2 * KP : KP>(tmem + TCOL_A, sm.rop, sm.xh,
+                                                                nullptr, nullptr, first, &mbar_c);
                 pend_c = true;
                 first = false;
             }
@@ -560,6 +565,12 @@ dp_embed_fwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
             float d[KP];
             if (!first) {
                 tc::tmem_ld32(tmem + TCOL_A + lane_q, d);
+                if (SPLIT == 3) {
+                    float dl[KP];
+                    tc::tmem_ld32(tmem + TCOL_A + KP + lane_q, dl);
+#pragma unroll
+                    for (int p = 0; p < KP; ++p) d[p] += dl[p];
+                }
             } else {
 #pragma unroll
                 for (int p = 0; p < KP; ++p) d[p] = 0.f;
@@ -597,7 +608,7 @@ done:
     if (!ok && (tid & 31) == 0) atomicMax(err, MATPL_KERR_TIMEOUT);
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, 64);
+    if (warp == 0) tc::tmem_dealloc(tmem, 128);
 }
 
 // ------------------------------------------------------------------ backward (forces)
@@ -867,8 +878,9 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
                 }
                 if (pre_issue(ok)) goto done;
                 if (tid == 0)
-                    issue_rows<SPLIT == 3 ? 3 : 1, 64, QN>(tmem + TCOL_RED, sm.rop, sm.qh, sm.qm,
-                                                          sm.ql, first, &mbar_c);
+                    // N = 48: the hi, mid and lo tiles follow one another in shared memory
+                    issue_rows<1, 64, SPLIT == 3 ? 3 * QN : QN>(tmem + TCOL_RED, sm.rop, sm.qh,
+                                                               nullptr, nullptr, first, &mbar_c);
                 pend_c = true;
                 first = false;
             }
@@ -880,6 +892,13 @@ dp_embed_bwd_tc(const int32_t *__restrict__ list_neigh, const float *__restrict_
             float d[QN];
             if (!first) {
                 tc::tmem_ld16(tmem + TCOL_RED, d);
+                if (SPLIT == 3) {
+                    float dm[QN], dl[QN];
+                    tc::tmem_ld16(tmem + TCOL_RED + QN, dm);
+                    tc::tmem_ld16(tmem + TCOL_RED + 2 * QN, dl);
+#pragma unroll
+                    for (int q = 0; q < QN; ++q) d[q] += dm[q] + dl[q];
+                }
             } else {
 #pragma unroll
                 for (int q = 0; q < QN; ++q) d[q] = 0.f;
@@ -959,7 +978,7 @@ int launch_mixed_embed(bool backward, const int32_t *list_neigh, const int32_t *
     const size_t smem = mix_smem_bytes(backward, nslots, P.ga);
     const long long total = (long long)batch * natoms;
     const long long ngroups = (total + P.ga - 1) / P.ga;
-    // resident CTAs per SM: what shared memory and TMEM allow (64 / 128 columns per CTA);
+    // resident CTAs per SM: what shared memory and TMEM allow (128 columns per CTA, four);
     // the tuning hook may ask for fewer
     const int fit = (int)std::max<size_t>(1, (227 * 1024) / (smem + 1024));
     int per_sm = std::min(fit, backward ? 3 : 4);
