@@ -459,10 +459,14 @@ __global__ void __launch_bounds__(128) nepnb_search(SearchArgs A, int warps_per_
             float H[9];
 #pragma unroll
             for (int q = 0; q < 9; ++q) H[q] = F.H[q];
-            int qn = 0;
-            for (int q = 0; q < 27; ++q) {
+            // the 27 neighbor cells, one per lane: start, count and periodic shift, read in
+            // parallel; the candidates of all cells are then walked as one flat range, 32 at a
+            // time (the kept pairs are rank-sorted by n2 afterwards, so the order of the walk
+            // does not matter)
+            int cbeg = 0, ccnt = 0, csh = 0;
+            if (lane < 27) {
+                const int d[3] = {lane / 9 - 1, (lane / 3) % 3 - 1, lane % 3 - 1};
                 int c[3], sh[3];
-                const int d[3] = {q / 9 - 1, (q / 3) % 3 - 1, q % 3 - 1};
                 for (int k = 0; k < 3; ++k) {
                     c[k] = c1[k] + d[k];
                     sh[k] = 0;
@@ -470,36 +474,61 @@ __global__ void __launch_bounds__(128) nepnb_search(SearchArgs A, int warps_per_
                     if (c[k] >= F.nc[k]) { c[k] -= F.nc[k]; sh[k] = 1; }
                 }
                 const long long cell = F.cell0 + (c[0] * F.nc[1] + c[1]) * F.nc[2] + c[2];
-                const int beg = A.cell_start[cell], cnt = A.cell_count[cell];
-                for (int base = 0; base < cnt; base += 32) {
-                    const int e = base + lane;
-                    bool pass = false;
-                    int loc = -1;
-                    if (e < cnt) {
-                        loc = A.cell_atoms[F.atom0 + beg + e];
-                        if (F.atom0 + loc != n1) {
-                            const float4 s2 = A.spos[F.atom0 + loc];
-                            const float f0 = s2.x + sh[0] - s1.x, f1 = s2.y + sh[1] - s1.y,
-                                        f2 = s2.z + sh[2] - s1.z;
-                            const float xf = H[0] * f0 + H[1] * f1 + H[2] * f2;
-                            const float yf = H[3] * f0 + H[4] * f1 + H[5] * f2;
-                            const float zf = H[6] * f0 + H[7] * f1 + H[8] * f2;
-                            pass = xf * xf + yf * yf + zf * zf < A.pre2;
-                        }
+                cbeg = A.cell_start[cell];
+                ccnt = A.cell_count[cell];
+                csh = (sh[0] + 1) | ((sh[1] + 1) << 2) | ((sh[2] + 1) << 4);
+            }
+            int incl = ccnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const int excl = incl - ccnt;
+            const int total = __shfl_sync(0xffffffffu, incl, 31);
+            int qn = 0;
+            for (int base = 0; base < total; base += 32) {
+                const int e = base + lane;
+                // the last cell q with excl_q <= e (it holds e: cells with no atoms share
+                // their start with the next one)
+                int lo = 0, hi = 26;
+#pragma unroll
+                for (int it = 0; it < 5; ++it) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    const int em = __shfl_sync(0xffffffffu, excl, mid);
+                    if (em <= e) lo = mid; else hi = mid - 1;
+                }
+                const int q = lo;
+                const int qbeg = __shfl_sync(0xffffffffu, cbeg, q);
+                const int qex = __shfl_sync(0xffffffffu, excl, q);
+                const int qsh = __shfl_sync(0xffffffffu, csh, q);
+                bool pass = false;
+                int loc = -1;
+                if (e < total) {
+                    loc = A.cell_atoms[F.atom0 + qbeg + (e - qex)];
+                    if (F.atom0 + loc != n1) {
+                        const float4 s2 = A.spos[F.atom0 + loc];
+                        const float f0 = s2.x + (float)((qsh & 3) - 1) - s1.x,
+                                    f1 = s2.y + (float)(((qsh >> 2) & 3) - 1) - s1.y,
+                                    f2 = s2.z + (float)(((qsh >> 4) & 3) - 1) - s1.z;
+                        const float xf = H[0] * f0 + H[1] * f1 + H[2] * f2;
+                        const float yf = H[3] * f0 + H[4] * f1 + H[5] * f2;
+                        const float zf = H[6] * f0 + H[7] * f1 + H[8] * f2;
+                        pass = xf * xf + yf * yf + zf * zf < A.pre2;
                     }
-                    const unsigned b = __ballot_sync(0xffffffffu, pass);
-                    if (pass) W.queue[qn + __popc(b & lt)] = loc;
-                    qn += __popc(b);
-                    if (qn >= 32) {
-                        __syncwarp();
-                        drain<COUNT, TYPED>(A, F, p1, 32, lane, W, cr, ca);
-                        const int left = qn - 32;
-                        const int v = lane < left ? W.queue[32 + lane] : 0;
-                        __syncwarp();
-                        if (lane < left) W.queue[lane] = v;
-                        __syncwarp();
-                        qn = left;
-                    }
+                }
+                const unsigned b = __ballot_sync(0xffffffffu, pass);
+                if (pass) W.queue[qn + __popc(b & lt)] = loc;
+                qn += __popc(b);
+                if (qn >= 32) {
+                    __syncwarp();
+                    drain<COUNT, TYPED>(A, F, p1, 32, lane, W, cr, ca);
+                    const int left = qn - 32;
+                    const int v = lane < left ? W.queue[32 + lane] : 0;
+                    __syncwarp();
+                    if (lane < left) W.queue[lane] = v;
+                    __syncwarp();
+                    qn = left;
                 }
             }
             if (qn > 0) {
