@@ -381,13 +381,14 @@ nb_search(const NbImage *__restrict__ img, const double *__restrict__ wpos,
             const int excl = incl - rl;
             for (int c0 = 0; c0 < T; c0 += 32) {
                 const int c = c0 + lane;
-                // find the range holding flat index c: last q with excl_q <= c and rl_q > 0
-                int q = 0;
+                // find the range holding flat index c: the last q < 18 with excl_q <= c (an
+                // empty range shares its start with the next one, so that q is not empty)
+                int q = 0, qhi = 17;
 #pragma unroll
-                for (int r = 0; r < 18; ++r) {
-                    const int e_r = __shfl_sync(0xffffffffu, excl, r);
-                    const int l_r = __shfl_sync(0xffffffffu, rl, r);
-                    if (l_r > 0 && e_r <= c) q = r;
+                for (int it = 0; it < 5; ++it) {
+                    const int mid = (q + qhi + 1) >> 1;
+                    const int e_m = __shfl_sync(0xffffffffu, excl, mid);
+                    if (e_m <= c) q = mid; else qhi = mid - 1;
                 }
                 const int s_q = __shfl_sync(0xffffffffu, rs, q);
                 const int e_q = __shfl_sync(0xffffffffu, excl, q);
