@@ -528,17 +528,24 @@ def run_train(args, ws, local, steps, warmup, plain_steps):
     # fused step, eager (per-kernel times from the library's events)
     emodel = train.DPTrainModel(cfg, prm, davg, dstd, dtype=torch.float32, device=dev)
     eopt = torch.optim.Adam(emodel.parameters(), lr=1e-4, fused=True)
-    etrainer = train.FusedTrainer(emodel)
+    etrainer = train.FusedTrainer(emodel, "mixed")
     etrainer.step([batch], eopt)
     _lib.profile_begin(max(4096, steps * 32))
     eager_ms = timed(lambda: etrainer.step([batch], eopt), max(3, steps // 3), 1)
     prof = _lib.profile_collect()
     del etrainer, emodel, eopt
-    # fused step captured in one CUDA graph (the headline of this workload)
+    # fused step captured in one CUDA graph (the headline of this workload): its E / F
+    # evaluation on the tcgen05 tensor cores (BF16x3), the FP32-evaluation form beside it
     fmodel = train.DPTrainModel(cfg, prm, davg, dstd, dtype=torch.float32, device=dev)
     fopt = torch.optim.Adam(fmodel.parameters(), lr=1e-4, capturable=True, fused=True)
-    graphed = train.GraphedTrainer(train.FusedTrainer(fmodel), fopt)
+    graphed = train.GraphedTrainer(train.FusedTrainer(fmodel, "mixed"), fopt)
     fused_ms = timed(lambda: graphed.step(batch), steps, warmup)
+    del graphed, fopt, fmodel
+    smodel = train.DPTrainModel(cfg, prm, davg, dstd, dtype=torch.float32, device=dev)
+    sopt = torch.optim.Adam(smodel.parameters(), lr=1e-4, capturable=True, fused=True)
+    sgraphed = train.GraphedTrainer(train.FusedTrainer(smodel), sopt)
+    simt_ms = timed(lambda: sgraphed.step(batch), steps, warmup)
+    del sgraphed, sopt, smodel
     pmodel = train.DPTrainModel(cfg, prm, davg, dstd, dtype=torch.float32, device=dev)
     popt = torch.optim.Adam(pmodel.parameters(), lr=1e-4, fused=True)
     torch.cuda.reset_peak_memory_stats(dev)
@@ -547,7 +554,7 @@ def run_train(args, ws, local, steps, warmup, plain_steps):
     # gradient agreement of the two paths at one parameter point
     m1 = train.DPTrainModel(cfg, prm, davg, dstd, dtype=torch.float32, device=dev)
     m2 = train.DPTrainModel(cfg, prm, davg, dstd, dtype=torch.float32, device=dev)
-    train.FusedTrainer(m1).loss_and_backward(batch)
+    train.FusedTrainer(m1, "mixed").loss_and_backward(batch)
     train.loss_fn(m2, batch)[0].backward()
     worst = 0.0
     for k in m1.names:
@@ -568,7 +575,8 @@ def run_train(args, ws, local, steps, warmup, plain_steps):
                 "algorithmic_flops_per_launch": 6600.0 * pairs}
     return {
         "metric": TRAIN_METRIC, "value": ws * natoms / (fused_ms * 1e-3), "unit": "atom-steps/s",
-        "ms_per_step": fused_ms, "steps": steps, "warmup": warmup, "dtype": "f32",
+        "ms_per_step": fused_ms, "steps": steps, "warmup": warmup,
+        "dtype": "f32 (E / F evaluation bf16x3 tensor, f32 accumulation)",
         "config": {"workload": f"DP se_e2_a force-loss training step (E-MSE + F-MSE, Adam) on a "
                                f"ragged batch of {TRAIN_CONFIGS} Hf:O configurations, atom counts "
                                f"U[{TRAIN_NMIN}, {TRAIN_NMAX}] ({natoms:,} atoms), "
@@ -582,6 +590,7 @@ def run_train(args, ws, local, steps, warmup, plain_steps):
                                   "ms_per_step": plain_ms, "value": ws * natoms / (plain_ms * 1e-3),
                                   "steps": plain_steps, "peak_memory_bytes": plain_peak},
                    "fused_eager_ms_per_step": eager_ms,
+                   "fused_fp32_evaluation_ms_per_step": simt_ms,
                    "capture": "whole fused step (evaluation, dual kernels, fitting part, backward, "
                               "Adam) in one CUDA graph, replayed per step",
                    "speedup_vs_plain_fp32": plain_ms / fused_ms,

@@ -300,16 +300,25 @@ class FusedTrainer:
     5. Phi = sum gE Etot + sum Edot; Phi.backward() gives dL/dtheta: the fitting part by torch
        autograd on per-atom tensors, the embedding part by ``matpl_dp_dual_backward``.
 
-    ``model`` is a DPTrainModel (its Parameters are trained); ``precision`` "float64" or
-    "float32" must match the model's dtype."""
+    ``model`` is a DPTrainModel (its Parameters are trained), float32 or float64.
+    ``eval_precision``: the form of step 1's evaluation, which only seeds gE and gF; None = the
+    model's dtype; "mixed" (float32 models) runs it on the tcgen05 tensor cores (BF16x3
+    operands, FP32 accumulation; E / F within ~1e-5 relative of FP32, so the gradient moves by
+    that much relative to the loss residuals)."""
 
-    def __init__(self, model: DPTrainModel):
+    def __init__(self, model: DPTrainModel, eval_precision: Optional[str] = None):
         if model.dtype not in (torch.float32, torch.float64):
             raise _lib.MatplError("FusedTrainer needs a float32 or float64 DPTrainModel")
         self.model = model
         cfg = model.cfg
         self.code = _lib.MATPL_F64 if model.dtype == torch.float64 else _lib.MATPL_F32
         prec = "float64" if model.dtype == torch.float64 else "float32"
+        if eval_precision is not None and eval_precision != prec:
+            if model.dtype != torch.float32 or not eval_precision.startswith("mixed"):
+                raise _lib.MatplError("eval_precision: a mixed form for a float32 model, or the "
+                                      "model's own dtype")
+            prec = eval_precision
+        self.eval_precision = prec
         dev = model.davg.device
         self.evaluator = _dp.DP(cfg, {}, model.davg.cpu(), model.dstd.cpu(), precision=prec,
                                 device=dev, check_errors=False, packed=_pack_device(model))

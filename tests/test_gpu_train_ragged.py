@@ -79,13 +79,15 @@ def test_ragged_collate_equals_the_oracle_lists(case):
     assert b["config_of_atom"].shape[0] == sum(COUNTS)
 
 
-@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-8), (torch.float32, 2e-3)])
-def test_ragged_fused_gradients_match_oracle(case, dtype, tol):
+@pytest.mark.parametrize("dtype,eval_precision,tol", [(torch.float64, None, 1e-8),
+                                                      (torch.float32, None, 2e-3),
+                                                      (torch.float32, "mixed", 2e-3)])
+def test_ragged_fused_gradients_match_oracle(case, dtype, eval_precision, tol):
     model = train.DPTrainModel(case["cfg"], case["prm"], case["davg"], case["dstd"], dtype=dtype,
                                device=DEV)
     b = dict(case["batch"])
     b["ImageDR"] = b["ImageDR"].to(dtype)
-    loss, _, _ = train.FusedTrainer(model).loss_and_backward(b)
+    loss, _, _ = train.FusedTrainer(model, eval_precision).loss_and_backward(b)
     assert abs(loss - case["loss"]) <= (1e-10 if dtype == torch.float64 else 1e-4) * case["loss"]
     worst, where = 0.0, None
     for k, gr in case["grads"].items():
@@ -93,8 +95,8 @@ def test_ragged_fused_gradients_match_oracle(case, dtype, tol):
         err = (got - gr).abs().max().item() / (gr.abs().max().item() + 1e-30)
         if err > worst:
             worst, where = err, k
-    print(f"[accuracy] ragged fused training gradients {dtype}: worst relative error "
-          f"{worst:.2e} ({where})")
+    print(f"[accuracy] ragged fused training gradients {dtype} (evaluation "
+          f"{eval_precision or 'same'}): worst relative error {worst:.2e} ({where})")
     assert worst < tol, (worst, where)
 
 
@@ -150,3 +152,33 @@ def test_ragged_graphed_step_matches_eager(case):
         assert abs(l1 - l2) <= 1e-10 * abs(l1)
     for k in m1.names:
         assert torch.allclose(m1.param(k), m2.param(k), rtol=1e-10, atol=1e-12), k
+
+
+def test_ragged_graphed_step_with_tensor_core_evaluation(case):
+    """The FP32 step whose evaluation runs on the tensor cores: graphed = eager, and its
+    gradients within 1e-4 (relative to each parameter's largest) of the FP32-evaluation step."""
+    cfg, b = case["cfg"], dict(case["batch"])
+    b["ImageDR"] = b["ImageDR"].float()
+    m0 = train.DPTrainModel(cfg, case["prm"], case["davg"], case["dstd"], dtype=torch.float32,
+                            device=DEV)
+    mx = train.DPTrainModel(cfg, case["prm"], case["davg"], case["dstd"], dtype=torch.float32,
+                            device=DEV)
+    train.FusedTrainer(m0).loss_and_backward(b)
+    train.FusedTrainer(mx, "mixed").loss_and_backward(b)
+    for k in m0.names:
+        g0, gx = m0.param(k).grad, mx.param(k).grad
+        assert float((gx - g0).abs().max()) <= 1e-4 * float(g0.abs().max()) + 1e-12, k
+    m1 = train.DPTrainModel(cfg, case["prm"], case["davg"], case["dstd"], dtype=torch.float32,
+                            device=DEV)
+    m2 = train.DPTrainModel(cfg, case["prm"], case["davg"], case["dstd"], dtype=torch.float32,
+                            device=DEV)
+    o1 = torch.optim.SGD(m1.parameters(), lr=1e-5)
+    o2 = torch.optim.SGD(m2.parameters(), lr=1e-5)
+    t1 = train.FusedTrainer(m1, "mixed")
+    g2 = train.GraphedTrainer(train.FusedTrainer(m2, "mixed"), o2, warmup=2)
+    for _ in range(2):                 # the graphed trainer's two warm-up steps
+        t1.step([b], o1)
+    for _ in range(3):
+        l1 = t1.step([b], o1)
+        l2 = float(g2.step(b))
+        assert abs(l1 - l2) <= 1e-6 * abs(l1)
