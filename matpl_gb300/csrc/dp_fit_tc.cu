@@ -98,6 +98,19 @@ __global__ void prep_fit_tiles(const float *__restrict__ params, unsigned char *
     }
 }
 
+// Asynchronous 16-byte global -> shared copies (cp.async), waited for with cp_async_wait_all.
+__device__ __forceinline__ void copy_tiles_async(const unsigned char *__restrict__ src,
+                                                 unsigned char *dst, int bytes) {
+    for (int q = threadIdx.x; q < bytes / 16; q += blockDim.x)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_u32(dst + 16 * q)),
+                     "l"(src + 16 * q)
+                     : "memory");
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
 __device__ __forceinline__ void copy_tiles(const unsigned char *__restrict__ src, unsigned char *dst,
                                            int bytes) {
     const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
@@ -298,28 +311,47 @@ dp_fit_tc(const float *__restrict__ Ain, const int *__restrict__ order,
             if (r == 0) vec[6 * FN] = fw[FitOff::B3];
             __syncthreads();
             const bool mine = valid;
-            // ---- layer 1: 13 double-buffered K chunks of D W0
+            // ---- layer 1: 13 double-buffered K chunks of D W0.  The weights of chunk c + 1
+            // are copied asynchronously while chunk c is formed and multiplied; buffer b of
+            // chunk c is free once the MMA of chunk c - 2 is done (waited at the end of the
+            // previous chunk, before that chunk's prefetch).
+            float aq[4][M2];                      // A[c][q], q < M2: every chunk's right factor
+#pragma unroll
+            for (int c4 = 0; c4 < 4; ++c4)
+#pragma unroll
+                for (int q = 0; q < M2; ++q) aq[c4][q] = a[c4 * E + q];
+            copy_tiles_async(tw + OFF_F0, WB, 2 * W32);
             for (int c = 0; c < K1C; ++c) {
                 const int b = c & 1;
-                if (c >= 2) {
-                    ok &= tc::mbar_wait(&mbar[b], ph[b], kWait);
-                    ph[b] ^= 1u;
-                }
-                copy_tiles(tw + OFF_F0 + (size_t)c * 2 * W32, WB + b * 2 * W32, 2 * W32);
                 float d[32];
 #pragma unroll
-                for (int kk = 0; kk < 32; ++kk) {
-                    const int k = 32 * c + kk, p = k >> 4, q = k & 15;
-                    d[kk] = k < DIN ? a[p] * a[q] + a[E + p] * a[E + q] + a[2 * E + p] * a[2 * E + q] +
-                                          a[3 * E + p] * a[3 * E + q]
-                                    : 0.f;
+                for (int h2 = 0; h2 < 2; ++h2) {
+                    const int p = 2 * c + h2;
+                    const float ap0 = p < E ? a[p] : 0.f, ap1 = p < E ? a[E + p] : 0.f,
+                                ap2 = p < E ? a[2 * E + p] : 0.f, ap3 = p < E ? a[3 * E + p] : 0.f;
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
+                        const int k = 32 * c + 16 * h2 + q;
+                        d[16 * h2 + q] = k < DIN ? ap0 * aq[0][q] + ap1 * aq[1][q] +
+                                                       ap2 * aq[2][q] + ap3 * aq[3][q]
+                                                 : 0.f;
+                    }
                 }
                 unsigned char *xh = XB + b * 2 * X32;
                 store_row_hilo<32>(xh, xh + X32, r, d);
+                cp_async_wait_all();
                 mma_sync_point();
                 if (r == 0) {
                     issue_split3<2>(tmem, xh, xh + X32, WB + b * 2 * W32, WB + b * 2 * W32 + W32, c > 0);
                     tc::commit(&mbar[b]);
+                }
+                if (c + 1 < K1C) {
+                    if (c >= 1) {                     // the MMA of chunk c - 1 read buffer b ^ 1
+                        ok &= tc::mbar_wait(&mbar[b ^ 1], ph[b ^ 1], kWait);
+                        ph[b ^ 1] ^= 1u;
+                    }
+                    copy_tiles_async(tw + OFF_F0 + (size_t)(c + 1) * 2 * W32,
+                                     WB + (b ^ 1) * 2 * W32, 2 * W32);
                 }
             }
             ok &= tc::mbar_wait(&mbar[1], ph[1], kWait);
@@ -405,20 +437,25 @@ dp_fit_tc(const float *__restrict__ Ain, const int *__restrict__ order,
                 tc::fence_after_sync();
                 ld64(tmem, h);                        // h[n] = dE/dD[64c + n]
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int p = 4 * c + j;
-                    if (p >= E) break;
+                for (int c4 = 0; c4 < 4; ++c4) {
+                    float ap[4], sj[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-                    for (int c4 = 0; c4 < 4; ++c4) {
-                        float s = 0.f;
-                        const float ap = a[c4 * E + p];
+                    for (int j = 0; j < 4; ++j) ap[j] = 4 * c + j < E ? a[c4 * E + 4 * c + j] : 0.f;
 #pragma unroll
-                        for (int q = 0; q < M2; ++q) {
-                            s += h[16 * j + q] * a[c4 * E + q];
-                            acc2[c4][q] += h[16 * j + q] * ap;
+                    for (int q = 0; q < M2; ++q) {
+                        const float aqv = a[c4 * E + q];
+                        float acc = acc2[c4][q];
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            if (4 * c + j >= E) break;
+                            sj[j] += h[16 * j + q] * aqv;
+                            acc += h[16 * j + q] * ap[j];
                         }
-                        if (mine) dAout[t * NA + c4 * E + p] = s;
+                        acc2[c4][q] = acc;
                     }
+#pragma unroll
+                    for (int j = 0; j < 4; ++j)
+                        if (mine && 4 * c + j < E) dAout[t * NA + c4 * E + 4 * c + j] = sj[j];
                 }
             }
             if (mine) {
@@ -439,6 +476,15 @@ dp_fit_tc(const float *__restrict__ Ain, const int *__restrict__ order,
         for (int e = 0; e < NA; ++e) dAout[t * NA + e] = 0.f;
     }
     if (!ok) atomicMax(err, MATPL_KERR_TIMEOUT);
+    // nothing issued may still run when the TMEM is freed: one more commit after all of this
+    // thread's MMAs, waited for (bounded) by every thread
+    __shared__ __align__(8) uint64_t mbar_drain;
+    if (r == 0) {
+        tc::mbar_init(&mbar_drain, 1);
+        tc::commit(&mbar_drain);
+    }
+    __syncthreads();
+    tc::mbar_wait(&mbar_drain, 0u, kWait);
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, FIT_TCOLS);
