@@ -181,4 +181,5 @@ def test_ragged_graphed_step_with_tensor_core_evaluation(case):
     for _ in range(3):
         l1 = t1.step([b], o1)
         l2 = float(g2.step(b))
-        assert abs(l1 - l2) <= 1e-6 * abs(l1)
+        # FP32 force sums by atomics: the two runs differ in summation order only
+        assert abs(l1 - l2) <= 1e-5 * abs(l1)
