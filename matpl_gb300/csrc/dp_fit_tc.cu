@@ -208,16 +208,34 @@ __global__ void fit_order_scatter(const int32_t *__restrict__ type_map, int nato
                                   int *__restrict__ order, int *__restrict__ type_start) {
     __shared__ int base[17];                   // global start of this block's atoms per bucket
     __shared__ int wcnt[kOrderBlock / 32][17];
+    __shared__ int before_s[17], total_s[17];  // per bucket: earlier blocks' atoms, all atoms
     const int T = ntypes + 1, nblk = gridDim.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // every block's bucket counts, summed by one warp per bucket (lanes over blocks, then a
+    // shuffle tree), instead of one thread walking them serially
+    for (int q = warp; q < T; q += kOrderBlock / 32) {
+        int bef = 0, tot = 0;
+        for (int b = lane; b < nblk; b += 32) {
+            const int v = blk_count[b * 17 + q];
+            tot += v;
+            if (b < (int)blockIdx.x) bef += v;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            bef += __shfl_xor_sync(0xffffffffu, bef, o);
+            tot += __shfl_xor_sync(0xffffffffu, tot, o);
+        }
+        if (lane == 0) {
+            before_s[q] = bef;
+            total_s[q] = tot;
+        }
+    }
+    __syncthreads();
     if (threadIdx.x < T) {
         const int q = threadIdx.x;
-        int before = 0, total_lower = 0;
-        for (int b = 0; b < nblk; ++b) {
-            if (b < (int)blockIdx.x) before += blk_count[b * 17 + q];
-            for (int p = 0; p < q; ++p) total_lower += blk_count[b * 17 + p];
-        }
-        base[q] = total_lower + before;
+        int total_lower = 0;
+        for (int p = 0; p < q; ++p) total_lower += total_s[p];
+        base[q] = total_lower + before_s[q];
         if (blockIdx.x == 0) type_start[q] = total_lower;
         if (blockIdx.x == 0 && q == T - 1) type_start[T] = natoms;
     }

@@ -723,14 +723,19 @@ __global__ void dp_reduce_partial(const T *__restrict__ Ei, const double *__rest
     }
 }
 
+// One warp per output (E, then the nine virial components): lanes over the partial sums, then
+// a fixed shuffle tree, so the order of the additions never changes.
 __global__ void dp_reduce_final(const double *__restrict__ part, double *__restrict__ Etot,
                                 double *__restrict__ virial, int nblk) {
     const int b = blockIdx.x;
-    if (threadIdx.x < 10) {
-        double v = 0.0;
-        for (int k = 0; k < nblk; ++k) v += part[((long long)b * nblk + k) * 10 + threadIdx.x];
-        if (threadIdx.x == 0) Etot[b] = v;
-        else virial[b * 9 + threadIdx.x - 1] = v;
+    const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (q >= 10) return;
+    double v = 0.0;
+    for (int k = lane; k < nblk; k += 32) v += part[((long long)b * nblk + k) * 10 + q];
+    v = warp_sum(v);
+    if (lane == 0) {
+        if (q == 0) Etot[b] = v;
+        else virial[b * 9 + q - 1] = v;
     }
 }
 
@@ -858,7 +863,7 @@ int launch_eval(int mode, const matpl_dp_model *M, const EvalParams &P,
         const int nblk = (int)std::min<long long>(kReduceBlocks, (P.natoms + 255) / 256);
         double *red = (double *)(ws + lay.red);
         dp_reduce_partial<T><<<dim3(nblk, P.batch), 256, 0, s>>>(Ei, avir, red, P.natoms);
-        dp_reduce_final<<<P.batch, 32, 0, s>>>(red, Etot, virial, nblk);
+        dp_reduce_final<<<P.batch, 320, 0, s>>>(red, Etot, virial, nblk);
     }
     return check_launch("matpl_dp_eval");
 }
