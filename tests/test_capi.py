@@ -130,6 +130,28 @@ def test_empty_sizes_and_null_pointers_are_handled_on_the_host():
     assert n.value == 0
 
 
+def test_md_entry_points_validate_on_the_host():
+    """The batched-MD kernels refuse bad sizes, dtype codes and NULL pointers before any CUDA
+    call, and an empty system is a no-op."""
+    lib = _lib.load()
+    OK, INVALID, DTYPE = 0, 1, 2
+    assert lib.matpl_md_drift(0, 1.0, 1.0, None, None, None, None, None, None) == OK
+    assert lib.matpl_md_drift(10, 1.0, 1.0, None, None, None, None, None, None) == INVALID
+    assert lib.matpl_md_drift(10, 0.0, 1.0, None, None, None, None, None, None) == INVALID
+    assert lib.matpl_md_skin_build(1, 0, 1, 100, 7.0, None, None, 0, *([None] * 12)) == OK
+    assert lib.matpl_md_skin_build(1, 10, 1, 100, 7.0, None, None, 1, *([None] * 12)) == INVALID
+    assert lib.matpl_md_skin_build(1, 10, 9, 100, 7.0, None, None, 1, *([None] * 12)) == INVALID
+    assert lib.matpl_md_skin_filter(_lib.MATPL_F32, 0, 1, 100, 100, 6.0, *([None] * 11)) == OK
+    assert lib.matpl_md_skin_filter(_lib.MATPL_F32, 10, 1, 100, 100, 6.0,
+                                    *([None] * 11)) == INVALID
+    assert lib.matpl_md_skin_filter(_lib.MATPL_MIXED, 10, 1, 100, 100, 6.0,
+                                    *([None] * 11)) == DTYPE
+    assert lib.matpl_md_kick(_lib.MATPL_F64, 1, 0, 1.0, 103.6, *([None] * 10)) == OK
+    assert lib.matpl_md_kick(_lib.MATPL_F64, 1, 2, 1.0, 103.6, *([None] * 10)) == INVALID
+    assert lib.matpl_md_kick(_lib.MATPL_F64, 2, 2, 1.0, 103.6, *([None] * 10)) == INVALID
+    assert lib.matpl_md_kick(7, 1, 2, 1.0, 103.6, *([None] * 10)) == DTYPE
+
+
 def test_noalloc_neighbor_search_refuses_oversize_requests_on_the_host():
     """The allocation-free search has a fixed scratch array; a request that needs more is
     refused before any CUDA call (200,000 atoms need far more than its 4 MiB)."""

@@ -105,3 +105,42 @@ def test_energy_is_conserved(precision, tol):
     print(f"[accuracy] MD {precision}: max |E(t)-E(0)| per atom over 200 steps {worst:.2e} eV, "
           f"{sim.rebuilds()} list builds")
     assert worst < tol
+
+
+def test_two_element_replicas_match_exact_search():
+    """Li / Si replicas of different sizes (two type blocks per atom): after a few steps the
+    skin-filtered list gives the forces of a fresh exact search, replica by replica (FP64)."""
+    cfg = P.DPConfig(atom_type=[3, 14], maxNeighborNum=150, Rmax=6.0, Rmin=0.5)
+    reps = [structures.random_packed(n, 0.05, [3, 14], [0.5, 0.5], seed=40 + k)
+            for k, n in enumerate((90, 140, 64))]
+    st = reps[1]
+    ln, idr = neigh.find_neighbore(st.types, st.frac, st.lattice, 2, 150, 6.0, [6.0, 6.0])
+    davg, dstd = P.calc_stat(cfg, ln, idr, st.types)
+    prm = P.init_params(cfg, 7)
+    sim = md.ReplicaMD(cfg, prm, davg, dstd, reps, [6.94, 28.086], dt_fs=1.0,
+                       precision="float64", skin=0.3)
+    sim.step(6)
+    torch.cuda.synchronize()
+    sim.check_errors()
+    F = sim.out["Force"][0]
+    for r in range(sim.nreplicas):
+        sl = sim.replica_slice(r)
+        x = sim.x[sl]
+        frac = torch.remainder(x @ sim.inv_lat[r], 1.0)
+        frac = torch.where(frac >= 1.0, torch.zeros_like(frac), frac)
+        m = dp.DP(cfg, prm, davg, dstd, precision="float64", device=sim.dev)
+        l2, i2 = ops.find_neighbore(sim.types[sl], frac.contiguous(), sim.lat[r], 2, 150, 6.0, 6.0)
+        Fx = m.evaluate(l2, sim.types[sl], m.present_types(cfg.atom_type), i2, 0)["Force"][0]
+        scale = max(1.0, float(Fx.abs().max()))
+        assert float((F[sl] - Fx).abs().max()) <= 1e-10 * scale, r
+
+
+def test_skin_list_overflow_is_reported():
+    """A skin-list capacity below what the cells need: the build flags a neighbor overflow
+    (no write past the list) and check_errors raises."""
+    cfg, prm, davg, dstd, reps = _setup()
+    sim = md.ReplicaMD(cfg, prm, davg, dstd, reps, [63.546], precision="float64",
+                       skin_capacity=40)
+    torch.cuda.synchronize()
+    with pytest.raises(Exception, match="error code 1"):
+        sim.check_errors()
