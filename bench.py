@@ -320,6 +320,98 @@ def nep_reference_gpu(cfg, prm, st, r32, r64, ours_ms, ours_e2e_ms, ours_eval_ms
     return out
 
 
+NEP_MD_MASSES = {3: 6.94, 14: 28.085, 8: 15.999, 72: 178.49}   # amu, by atomic number
+NEP_MD_STEPS = 60
+
+
+def nep_skin_md(cfg, model, st, na, tm, bx, bo, nc, pos0, mr, ma, compact, steps=NEP_MD_STEPS):
+    """The NEP step as an MD caller runs it: positions advance by v dt every step (Maxwell-
+    Boltzmann velocities at 300 K, dt 1 fs; the forces are not fed back, so the atoms follow the
+    motion of the first femtoseconds of an MD run without its integrator), the lists come from
+    ops.SkinNeighbor (skin 1 A, rebuilt on the device when an atom has moved more than 0.5 A) and
+    the fused FP32 evaluation; the whole step is one CUDA-graph replay.  ``compact``: the MD list
+    form (FP32 pair vectors from the build plus displacements, int32 / f32 lists read by
+    matpl_nep_eval_compact); otherwise lists bit-identical to calculate_neighbor's.  Timed over
+    ``steps`` consecutive steps, so rebuild steps count at the rate the motion causes them."""
+    from matpl_gb300 import _lib, ops, structures
+    dev = pos0.device
+    masses = np.array([NEP_MD_MASSES[NEP_ELEMENTS[t]] for t in st.types])
+    vel = torch.tensor(structures.maxwell_boltzmann(masses, 300.0, seed=NEP_SEED_STRUCT),
+                       dtype=torch.float64, device=dev)
+    pos = pos0.clone()
+    sk = ops.SkinNeighbor(na, bx, bo, nc, pos, cfg.cutoff[0], cfg.cutoff[1], mr + 8, ma + 6,
+                          skin=1.0, compact=compact)
+
+    def step():
+        pos.add_(vel)                      # dt = 1 fs, v in A / fs
+        L = sk.lists(pos)
+        return model.evaluate(L[0], L[2], L[4], L[1], L[3], L[5], na, tm)
+
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(side):
+        for _ in range(3):
+            step()
+    torch.cuda.current_stream(dev).wait_stream(side)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        out = step()
+    torch.cuda.synchronize()
+    sk.check_errors()
+    b0 = sk.rebuilds()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        g.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    nbuild = sk.rebuilds() - b0
+    sk.check_errors()
+    # per-kernel split from an eager, event-bracketed run of the same motion
+    _lib.profile_begin(4096)
+    b1 = sk.rebuilds()
+    for _ in range(steps):
+        step()
+    torch.cuda.synchronize()
+    prof = _lib.profile_collect()
+    nb_prof = sk.rebuilds() - b1
+    split = {k: {"ms_per_launch": v[0] / v[1], "launches": v[1]} for k, v in prof.items()}
+    # the lists of the last step against the exact search at the same positions
+    at = torch.arange(cfg.ntypes, device=dev)
+    L = sk.lists(pos)
+    E = ops.calculate_neighbor(na, tm, at, bx, bo, nc, pos, cfg.cutoff[0], cfg.cutoff[1],
+                               mr + 8, ma + 6, True)
+    if compact:
+        nn_same = bool(torch.equal(L[0].long(), E[0]) and torch.equal(L[1].long(), E[1]))
+        slots = torch.arange(mr + 8, device=dev)[None, :] < E[0][:, None]
+        vec_err = float((L[4].double() - E[4])[slots].abs().max())
+        check = {"counts_equal_exact_search": nn_same,
+                 "max_abs_pair_vector_err_A": vec_err}
+        r = model.evaluate(L[0], L[2], L[4], L[1], L[3], L[5], na, tm)
+        rx = model.evaluate(E[0], E[2], E[4], E[1], E[3], E[5], na, tm)
+        check["max_abs_force_diff_vs_exact_lists_eV_per_A"] = float(
+            (r["Force"] - rx["Force"]).abs().max())
+    else:
+        check = {"lists_equal_exact_search_bitwise": all(
+            torch.equal(x.view(torch.int64) if x.dtype == torch.float64 else x,
+                        y.view(torch.int64) if y.dtype == torch.float64 else y)
+            for x, y in zip(L, E))}
+    vmax = float(vel.norm(dim=1).max())
+    del g, out
+    return {"ms_per_step": ms, "value": pos0.shape[0] / (ms * 1e-3), "unit": "atom-steps/s",
+            "steps_timed": steps, "rebuilds_in_timed_steps": nbuild,
+            "rebuilds_in_profiled_steps": nb_prof, "skin_A": 1.0,
+            "skin_capacity": sk.cap, "max_speed_A_per_fs": vmax, **check, "kernels": split,
+            "list_form": "compact (int32 / f32, FP32 pair vectors)" if compact else
+                         "calculate_neighbor's, bit-identical",
+            "note": "MD-style caller: Verlet-skin lists (ops.SkinNeighbor) + fused FP32 E/F/V, "
+                    "one CUDA-graph replay per step, positions advanced by v dt each step (300 K "
+                    "Maxwell-Boltzmann, 1 fs); the drop-in step above rebuilds the exact lists "
+                    "every step"}
+
+
 def run_nep(args, ws, local, steps, warmup, sample_clocks=True):
     """The NEP step on this GPU: calculate_neighbor (exact FP64 lists, the reference's layout) +
     the fused FP32 descriptor / network / force / virial kernel, 100,000 atoms."""
@@ -431,6 +523,9 @@ def run_nep(args, ws, local, steps, warmup, sample_clocks=True):
         if tr:   # recorded for the 100,000-atom launch; DRAM bytes scale with atoms
             traffic = {"bytes_per_launch": tr["bytes_per_launch"] * N / NEP_NATOMS,
                        "note": tr.get("note")}
+    md_skin = nep_skin_md(cfg, m32, st, na, tm, bx, bo, nc, pos_d, mr, ma, compact=True)
+    md_skin["exact_lists"] = nep_skin_md(cfg, m32, st, na, tm, bx, bo, nc, pos_d, mr, ma,
+                                         compact=False)
     ref_gpu = None if args.no_ref_gpu else nep_reference_gpu(
         cfg, prm, st, r32, r64, ms, e2e_ms, per_kernel["nep_eval"]["ms_per_launch"], mr, ma)
     return {
@@ -457,6 +552,7 @@ def run_nep(args, ws, local, steps, warmup, sample_clocks=True):
                              "unit": "GB/s", "frac": ev_bytes / t_eval / 1e9 / hbm_peak,
                              "algorithmic_bytes_per_launch": ev_bytes}},
         "reference_gpu": ref_gpu,
+        "md_skin": md_skin,
         "neighbor_roofline": {"kernel": "nep_neighbor", "bound": "fp64 (exact reference arithmetic)",
                               "hbm_achieved": nb_bytes / t_nb / 1e9, "hbm_peak": hbm_peak,
                               "unit": "GB/s", "frac": nb_bytes / t_nb / 1e9 / hbm_peak,

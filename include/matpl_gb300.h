@@ -326,6 +326,52 @@ int matpl_nep_maxneigh(int nframes, long long natoms, const long long *num_atom,
                        long long *NN_radial, long long *NN_angular, int *err_dev,
                        void *workspace, size_t workspace_bytes, void *stream);
 
+/* Verlet-skin reuse of the NEP lists for MD-style callers (the displacement rule of
+ * src/lmps/lammps-libtorch/MATPL/pair_matpl.cpp:1096-1110 applied to calculate_neighbor).
+ * The drop-in calculate_neighbor above stays the exact rebuild; these two replace it for a
+ * caller that steps one fixed box and passes positions that move a little per call.
+ * matpl_nep_skin_update: sets *gate when some |position - x_ref| > skin / 2 (or NaN); then,
+ *   only when *gate != 0 (read on the device: the sequence can be captured in a CUDA graph),
+ *   rebuilds skin_nbr [natoms, cap] int32 (global n2 ascending, every pair within r_list of
+ *   the frame's cell search, r_list >= max cutoff + skin), skin_cnt [natoms] and
+ *   x_ref [natoms, 3] = position, clears *gate and increments *nbuild (may be NULL).  Start
+ *   with *gate = 1.  A list longer than cap sets MATPL_KERR_NEIGHBOR_OVERFLOW; a frame that is
+ *   not a single cell at least three r_list-wide cells thick sets MATPL_KERR_BAD_BOX (use the
+ *   exact rebuild for it).  The workspace (matpl_nep_neighbor_workspace_bytes) holds the frame
+ *   table of the last build and must be kept, with box / box_orig, until the next rebuild.
+ *   skin_vec [natoms, cap, 4] f32 and delta [natoms, 4] f32 (both NULL, or both 16-byte
+ *   aligned device arrays) add what the compact filter reads: the FP32 pair vector of every
+ *   listed pair at the build, and every call's displacement position - x_ref.
+ * matpl_nep_skin_filter: NN / NL / Ri exactly as matpl_nep_neighbor returns them at these
+ *   positions (same pairs, same order, same bits), from the skin list and the frame table in
+ *   the workspace of the last update (it also writes its per-atom FP32 scratch there).
+ * matpl_nep_skin_filter_compact: the MD form, all FP32 (no FP64 pair arithmetic): pair vector
+ *   = skin_vec + delta[n2] - delta[n1], kept when r^2 < rc^2; writes NN_* [natoms] int32,
+ *   NL_* [natoms, max_nn] int32 (global 0-based n2, ascending) and Ri_* [natoms, max_nn, 4]
+ *   f32 (r, x, y, z); slots past NN are left unwritten.  The pair vectors agree with the exact
+ *   ones to a few FP32 ulps; a pair within ~1e-6 A of a cutoff may be classified the other
+ *   way (its terms vanish there).  matpl_nep_eval_compact evaluates these lists. */
+int matpl_nep_skin_update(int nframes, long long natoms, const long long *num_atom,
+                          const double *box, const double *box_orig, const long long *num_cell,
+                          const double *position, double r_list, double skin, int cap,
+                          int *skin_nbr, int *skin_cnt, double *x_ref, float *skin_vec,
+                          float *delta, int *gate, int *nbuild, int *err_dev, void *workspace,
+                          size_t workspace_bytes, void *stream);
+int matpl_nep_skin_filter(int nframes, long long natoms, const double *position,
+                          double cutoff_radial, double cutoff_angular, int max_nn_radial,
+                          int max_nn_angular, int with_rij, int cap, const int *skin_nbr,
+                          const int *skin_cnt, long long *NN_radial, long long *NN_angular,
+                          long long *NL_radial, long long *NL_angular, double *Ri_radial,
+                          double *Ri_angular, int *err_dev, void *workspace,
+                          size_t workspace_bytes, void *stream);
+int matpl_nep_skin_filter_compact(long long natoms, double cutoff_radial, double cutoff_angular,
+                                  int max_nn_radial, int max_nn_angular, int cap,
+                                  const int *skin_nbr, const int *skin_cnt,
+                                  const float *skin_vec, const float *delta, int *NN_radial,
+                                  int *NN_angular, int *NL_radial, int *NL_angular,
+                                  float *Ri_radial, float *Ri_angular, int *err_dev,
+                                  void *stream);
+
 /* ------------------------------------------------------------------------------------
  * Fused NEP energy + force + virial.  Replaces NEP.forward + calculate_force_virial
  * (src/model/nep_net.py:293-438, 486-648): descriptor (calculateNepFeat / calculateNepMbFeat,
@@ -374,6 +420,16 @@ int matpl_nep_descriptor(int dtype, const matpl_nep_model *model, int nframes, l
                          const long long *NN_angular, const long long *NL_angular,
                          const double *Ri_angular, void *feats, void *workspace,
                          size_t workspace_bytes, void *stream);
+/* matpl_nep_eval on the compact MD lists of matpl_nep_skin_filter_compact (int32 NN / NL,
+ * 16-byte aligned f32 Ri rows of (r, x, y, z)); dtype MATPL_F32 only.  Same outputs and
+ * workspace as matpl_nep_eval. */
+int matpl_nep_eval_compact(int dtype, const matpl_nep_model *model, int nframes, long long natoms,
+                           const long long *num_atom, const long long *type_map,
+                           int max_nn_radial, const int *NN_radial, const int *NL_radial,
+                           const float *Ri_radial, int max_nn_angular, const int *NN_angular,
+                           const int *NL_angular, const float *Ri_angular, void *Ei,
+                           double *Etot, void *force, double *virial, void *workspace,
+                           size_t workspace_bytes, void *stream);
 
 /* ------------------------------------------------------------------------------------
  * Data-path statistics.  Replaces the per-image calc_stat + smooth of

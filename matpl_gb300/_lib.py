@@ -81,10 +81,18 @@ SIGNATURES = {
                                 _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "matpl_nep_maxneigh": (_i, [_i, _ll, _vp, _vp, _vp, _vp, _vp, _d, _d, _i, _vp, _i, _vp, _vp,
                                 _vp, _vp, _sz, _vp]),
+    "matpl_nep_skin_update": (_i, [_i, _ll, _vp, _vp, _vp, _vp, _vp, _d, _d, _i] + [_vp] * 9 +
+                              [_sz, _vp]),
+    "matpl_nep_skin_filter_compact": (_i, [_ll, _d, _d, _i, _i, _i] + [_vp] * 12),
+    "matpl_nep_skin_filter": (_i, [_i, _ll, _vp, _d, _d, _i, _i, _i, _i] + [_vp] * 10 +
+                              [_sz, _vp]),
     "matpl_nep_param_count": (_sz, [_c.POINTER(MatplNepModel)]),
     "matpl_nep_workspace_bytes": (_sz, [_i, _i, _ll]),
     "matpl_nep_eval": (_i, [_i, _c.POINTER(MatplNepModel), _i, _ll, _vp, _vp, _i, _vp, _vp, _vp,
                             _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "matpl_nep_eval_compact": (_i, [_i, _c.POINTER(MatplNepModel), _i, _ll, _vp, _vp, _i, _vp,
+                                    _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz,
+                                    _vp]),
     "matpl_nep_descriptor": (_i, [_i, _c.POINTER(MatplNepModel), _i, _ll, _vp, _vp, _i, _vp, _vp,
                                   _vp, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "matpl_env_stats": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _d, _d, _vp, _vp, _vp]),

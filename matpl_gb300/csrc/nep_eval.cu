@@ -50,6 +50,9 @@ struct EvalArgs {
     int max_r, max_a;
     const long long *NN_r, *NL_r, *NN_a, *NL_a;
     const double *Ri_r, *Ri_a;
+    // compact lists (MD skin form): int32 NN / NL, float4 (r, x, y, z); used when CL
+    const int *cNN_r, *cNL_r, *cNN_a, *cNL_a;
+    const float4 *cRi_r, *cRi_a;
     void *Ei;
     double *Etot, *virial;
     void *facc;                     // float4 [N] (f32) or double [N, 3] (f64)
@@ -120,6 +123,35 @@ __device__ __forceinline__ void add_force<double>(void *facc, long long j, doubl
     atomicAdd(p + 2, fz);
 }
 
+// List access for the reference layout (int64 NN / NL, f64 (r, x, y, z)) and the compact one.
+template <bool CL>
+__device__ __forceinline__ long long list_count(const EvalArgs &A, bool radial, long long i) {
+    if (CL) return radial ? A.cNN_r[i] : A.cNN_a[i];
+    return radial ? A.NN_r[i] : A.NN_a[i];
+}
+template <bool CL>
+__device__ __forceinline__ long long list_index(const EvalArgs &A, bool radial, long long e) {
+    if (CL) return radial ? A.cNL_r[e] : A.cNL_a[e];
+    return radial ? A.NL_r[e] : A.NL_a[e];
+}
+// (r, x, y, z) of list entry e, or r = 0 when !valid
+template <typename T, bool CL>
+__device__ __forceinline__ void list_pair(const EvalArgs &A, bool radial, long long e, bool valid,
+                                          T &r, T &x, T &y, T &z) {
+    r = x = y = z = T(0);
+    if (!valid) return;
+    if (CL) {
+        const float4 v = __ldg((radial ? A.cRi_r : A.cRi_a) + e);
+        r = (T)v.x; x = (T)v.y; y = (T)v.z; z = (T)v.w;
+    } else {
+        const double *rr = (radial ? A.Ri_r : A.Ri_a) + e * 4;
+        r = ld_conv<T>(rr);
+        x = ld_conv<T>(rr + 1);
+        y = ld_conv<T>(rr + 2);
+        z = ld_conv<T>(rr + 3);
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ void flush_frame(const EvalArgs &A, int frame, double e, T *vir,
                                             int lane) {
@@ -132,7 +164,7 @@ __device__ __forceinline__ void flush_frame(const EvalArgs &A, int frame, double
     if (lane == 0 && e != 0.0) atomicAdd(A.Etot + frame, e);
 }
 
-template <typename T, int NRM, int KRM, int NAM, int KAM>
+template <typename T, int NRM, int KRM, int NAM, int KAM, bool CL>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -227,8 +259,8 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
             }
             continue;
         }
-        const int nnr = L.two ? (int)min(A.NN_r[i], (long long)A.max_r) : 0;
-        const int nna = L.l3 ? (int)min(A.NN_a[i], (long long)A.max_a) : 0;
+        const int nnr = L.two ? (int)min(list_count<CL>(A, true, i), (long long)A.max_r) : 0;
+        const int nna = L.l3 ? (int)min(list_count<CL>(A, false, i), (long long)A.max_a) : 0;
         const long long row_r = i * A.max_r, row_a = i * A.max_a;
 
         // ---------------- radial descriptor; pair vector and g_n' kept for the force pass
@@ -236,7 +268,7 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
 #pragma unroll
         for (int n = 0; n < NRM; ++n) qr[n] = T(0);
         for (int sl = lane; sl < nnr; sl += 32) {
-            const long long j = A.NL_r[row_r + sl];
+            const long long j = list_index<CL>(A, true, row_r + sl);
             int tj = -1;
             if (j >= 0 && j < A.natoms) {
                 tj = (int)A.type_map[j];
@@ -244,11 +276,11 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
             } else if (j >= A.natoms) {
                 atomicOr(A.err, MATPL_KERR_BAD_COUNT);
             }
-            const double *rr = A.Ri_r + (row_r + sl) * 4;
-            const T r = tj >= 0 ? ld_conv<T>(rr) : T(0);
+            T r, px, py, pz;
+            list_pair<T, CL>(A, true, row_r + sl, tj >= 0, r, px, py, pz);
             if (!(r > T(0))) { rj[sl] = -1; continue; }
             const T rinv = T(1) / r;
-            sts4(rv + 4 * sl, ld_conv<T>(rr + 1), ld_conv<T>(rr + 2), ld_conv<T>(rr + 3), rinv);
+            sts4(rv + 4 * sl, px, py, pz, rinv);
             rj[sl] = (int)j;
             T f[KRP], df[KRP];
             basis<T, KRM>(r, rc_r, rcinv_r, L.kr, f, df);
@@ -284,7 +316,7 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
         for (int base = 0; base < nna; base += 32) {
             const int sl = base + lane;
             if (sl < nna) {
-                const long long j = A.NL_a[row_a + sl];
+                const long long j = list_index<CL>(A, false, row_a + sl);
                 int tj = -1;
                 if (j >= 0 && j < A.natoms) {
                     tj = (int)A.type_map[j];
@@ -292,8 +324,8 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
                 } else if (j >= A.natoms) {
                     atomicOr(A.err, MATPL_KERR_BAD_COUNT);
                 }
-                const double *rr = A.Ri_a + (row_a + sl) * 4;
-                const T r = tj >= 0 ? ld_conv<T>(rr) : T(0);
+                T r, px, py, pz;
+                list_pair<T, CL>(A, false, row_a + sl, tj >= 0, r, px, py, pz);
                 const bool ok = r > T(0);
                 T f[KAP], df[KAP];
                 basis<T, KAM>(ok ? r : rc_a, rc_a, rcinv_a, L.ka, f, df);
@@ -320,8 +352,7 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
                     agp[sl * NAM + n] = gp;
                 }
                 const T rinv = ok ? T(1) / r : T(0);
-                const T x = ok ? ld_conv<T>(rr + 1) : T(0), y = ok ? ld_conv<T>(rr + 2) : T(0),
-                        z = ok ? ld_conv<T>(rr + 3) : T(0);
+                const T x = ok ? px : T(0), y = ok ? py : T(0), z = ok ? pz : T(0);
                 aj[sl] = ok ? (int)j : -1;
                 sts4(av + 4 * sl, x, y, z, rinv);
                 const T ux = x * rinv, uy = y * rinv, uz = z * rinv;
@@ -633,11 +664,11 @@ size_t ws_layout(int dtype, int nframes, long long natoms, unsigned char *base,
     return off;
 }
 
-template <typename T, int NRM, int KRM, int NAM, int KAM>
+template <typename T, int NRM, int KRM, int NAM, int KAM, bool CL>
 int launch_eval(const EvalArgs &A0, cudaStream_t s) {
     EvalArgs A = A0;
     const NepLayout &L = A.L;
-    auto kern = nep_eval_kernel<T, NRM, KRM, NAM, KAM>;
+    auto kern = nep_eval_kernel<T, NRM, KRM, NAM, KAM, CL>;
     // per-warp scratch, 16-byte aligned pieces
     int off = 0;
     auto take = [&](size_t bytes) {
@@ -687,15 +718,21 @@ int launch_eval(const EvalArgs &A0, cudaStream_t s) {
     return check_launch("matpl_nep_eval");
 }
 
-template <typename T>
+template <typename T, bool CL>
 int dispatch(const EvalArgs &A, cudaStream_t s) {
     const NepLayout &L = A.L;
     if (L.nr <= 5 && L.kr <= 9 && L.na <= 5 && L.ka <= 9)
-        return launch_eval<T, 5, 9, 5, 9>(A, s);
+        return launch_eval<T, 5, 9, 5, 9, CL>(A, s);
     MATPL_REQUIRE(L.nr <= 8 && L.kr <= 16 && L.na <= 8 && L.ka <= 16, MATPL_ERR_UNSUPPORTED,
                   "n_max <= 7 and basis_size <= 15 are compiled");
-    return launch_eval<T, 8, 16, 8, 16>(A, s);
+    return launch_eval<T, 8, 16, 8, 16, CL>(A, s);
 }
+
+// the compact list form: float4 entries only in FP32
+struct CompactLists {
+    const int *NN_r, *NL_r, *NN_a, *NL_a;
+    const float *Ri_r, *Ri_a;
+};
 
 }  // namespace
 }  // namespace matpl
@@ -721,9 +758,12 @@ int nep_run(int dtype, const matpl_nep_model *model, int nframes, long long nato
             const long long *NN_radial, const long long *NL_radial, const double *Ri_radial,
             int max_nn_angular, const long long *NN_angular, const long long *NL_angular,
             const double *Ri_angular, void *Ei, double *Etot, void *force, double *virial,
-            void *feats, void *workspace, size_t workspace_bytes, void *stream) {
+            void *feats, void *workspace, size_t workspace_bytes, void *stream,
+            const CompactLists *cl = nullptr) {
     MATPL_REQUIRE(dtype == MATPL_F32 || dtype == MATPL_F64, MATPL_ERR_DTYPE,
                   "NEP entry points support MATPL_F32 and MATPL_F64");
+    MATPL_REQUIRE(!cl || dtype == MATPL_F32, MATPL_ERR_DTYPE,
+                  "the compact (float4) list form is evaluated in MATPL_F32 only");
     NepLayout L;
     int st = make_layout(model, &L);
     if (st) return st;
@@ -732,10 +772,19 @@ int nep_run(int dtype, const matpl_nep_model *model, int nframes, long long nato
                   "null pointer argument");
     MATPL_REQUIRE(feats || (Ei && Etot && force && virial), MATPL_ERR_INVALID,
                   "null output pointer");
-    MATPL_REQUIRE(!L.two || (max_nn_radial >= 0 && NN_radial && NL_radial && Ri_radial),
-                  MATPL_ERR_INVALID, "radial list required");
-    MATPL_REQUIRE(!L.l3 || (max_nn_angular >= 0 && NN_angular && NL_angular && Ri_angular),
-                  MATPL_ERR_INVALID, "angular list required");
+    if (cl) {
+        MATPL_REQUIRE(!L.two || (max_nn_radial >= 0 && cl->NN_r && cl->NL_r && cl->Ri_r),
+                      MATPL_ERR_INVALID, "radial list required");
+        MATPL_REQUIRE(!L.l3 || (max_nn_angular >= 0 && cl->NN_a && cl->NL_a && cl->Ri_a),
+                      MATPL_ERR_INVALID, "angular list required");
+        MATPL_REQUIRE(((uintptr_t)cl->Ri_r & 15u) == 0 && ((uintptr_t)cl->Ri_a & 15u) == 0,
+                      MATPL_ERR_INVALID, "Ri_radial / Ri_angular must be 16-byte aligned");
+    } else {
+        MATPL_REQUIRE(!L.two || (max_nn_radial >= 0 && NN_radial && NL_radial && Ri_radial),
+                      MATPL_ERR_INVALID, "radial list required");
+        MATPL_REQUIRE(!L.l3 || (max_nn_angular >= 0 && NN_angular && NL_angular && Ri_angular),
+                      MATPL_ERR_INVALID, "angular list required");
+    }
     const size_t need = ws_layout(dtype, nframes, natoms, nullptr, nullptr, nullptr);
     MATPL_REQUIRE(workspace && workspace_bytes >= need, MATPL_ERR_WORKSPACE,
                   "workspace smaller than matpl_nep_workspace_bytes()");
@@ -754,6 +803,10 @@ int nep_run(int dtype, const matpl_nep_model *model, int nframes, long long nato
     A.max_a = max_nn_angular;
     A.NN_r = NN_radial; A.NL_r = NL_radial; A.Ri_r = Ri_radial;
     A.NN_a = NN_angular; A.NL_a = NL_angular; A.Ri_a = Ri_angular;
+    A.cNN_r = cl ? cl->NN_r : nullptr; A.cNL_r = cl ? cl->NL_r : nullptr;
+    A.cNN_a = cl ? cl->NN_a : nullptr; A.cNL_a = cl ? cl->NL_a : nullptr;
+    A.cRi_r = cl ? (const float4 *)cl->Ri_r : nullptr;
+    A.cRi_a = cl ? (const float4 *)cl->Ri_a : nullptr;
     A.Ei = Ei;
     A.Etot = Etot;
     A.virial = virial;
@@ -770,7 +823,8 @@ int nep_run(int dtype, const matpl_nep_model *model, int nframes, long long nato
     }
     nep_frame_start<<<1, 32, 0, s>>>(num_atom, nframes, natoms, fs, model->err_dev);
     if (natoms == 0) return check_launch("matpl_nep_eval");
-    st = dtype == MATPL_F32 ? dispatch<float>(A, s) : dispatch<double>(A, s);
+    st = cl ? dispatch<float, true>(A, s)
+            : (dtype == MATPL_F32 ? dispatch<float, false>(A, s) : dispatch<double, false>(A, s));
     if (st) return st;
     if (dtype == MATPL_F32 && !feats) {
         const long long g = (natoms + 255) / 256;
@@ -812,4 +866,21 @@ extern "C" int matpl_nep_descriptor(int dtype, const matpl_nep_model *model, int
     return nep_run(dtype, model, nframes, natoms, num_atom, type_map, max_nn_radial, NN_radial,
                    NL_radial, Ri_radial, max_nn_angular, NN_angular, NL_angular, Ri_angular,
                    nullptr, nullptr, nullptr, nullptr, feats, workspace, workspace_bytes, stream);
+}
+
+extern "C" int matpl_nep_eval_compact(int dtype, const matpl_nep_model *model, int nframes,
+                                      long long natoms, const long long *num_atom,
+                                      const long long *type_map, int max_nn_radial,
+                                      const int *NN_radial, const int *NL_radial,
+                                      const float *Ri_radial, int max_nn_angular,
+                                      const int *NN_angular, const int *NL_angular,
+                                      const float *Ri_angular, void *Ei, double *Etot,
+                                      void *force, double *virial, void *workspace,
+                                      size_t workspace_bytes, void *stream) {
+    MATPL_REQUIRE(Ei && Etot && force && virial, MATPL_ERR_INVALID, "null output pointer");
+    MATPL_REQUIRE_ON_DEVICE(force, "matpl_nep_eval_compact");
+    CompactLists cl{NN_radial, NL_radial, NN_angular, NL_angular, Ri_radial, Ri_angular};
+    return nep_run(dtype, model, nframes, natoms, num_atom, type_map, max_nn_radial, nullptr,
+                   nullptr, nullptr, max_nn_angular, nullptr, nullptr, nullptr, Ei, Etot, force,
+                   virial, nullptr, workspace, workspace_bytes, stream, &cl);
 }

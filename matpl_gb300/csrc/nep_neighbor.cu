@@ -26,6 +26,8 @@ namespace matpl {
 namespace {
 
 constexpr int kSetupThreads = 256;
+
+inline bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
 constexpr float kPrefilterMargin = 0.02f;   // Angstrom, on top of a relative 1e-5
 
 struct NepFrame {
@@ -122,7 +124,9 @@ __device__ __forceinline__ int frame_of(const NepFrame *__restrict__ fr, int nfr
 __global__ void nepnb_setup(const long long *__restrict__ num_atom,
                             const double *__restrict__ box, const double *__restrict__ box_orig,
                             const long long *__restrict__ num_cell, NepFrame *__restrict__ fr,
-                            int nframes, long long natoms, double rc_max, int *__restrict__ err) {
+                            int nframes, long long natoms, double rc_max, int *__restrict__ err,
+                            const int *gate) {
+    if (gate && *gate == 0) return;
     // frame offsets first; counts that overrun natoms are clipped and reported
     if (threadIdx.x == 0) {
         long long a0 = 0;
@@ -218,9 +222,15 @@ __global__ void nepnb_setup(const long long *__restrict__ num_atom,
 
 __global__ void nepnb_bin(const double *__restrict__ pos, const NepFrame *__restrict__ fr,
                           int nframes, long long natoms, float4 *__restrict__ spos,
-                          int *__restrict__ cell_of, int *__restrict__ cell_count) {
+                          int *__restrict__ cell_of, int *__restrict__ cell_count,
+                          const int *gate, double *__restrict__ x_ref,
+                          float4 *__restrict__ delta) {
+    if (gate && *gate == 0) return;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < natoms;
          t += (long long)gridDim.x * blockDim.x) {
+        if (x_ref)
+            for (int k = 0; k < 3; ++k) x_ref[3 * t + k] = pos[3 * t + k];
+        if (delta) delta[t] = make_float4(0.f, 0.f, 0.f, 0.f);
         const NepFrame &F = fr[frame_of(fr, nframes, t)];
         if (F.mode != 0) {
             cell_of[t] = -1;
@@ -245,7 +255,8 @@ __global__ void nepnb_bin(const double *__restrict__ pos, const NepFrame *__rest
 
 // exclusive scan of one frame's cell counts, one block per frame
 __global__ void nepnb_scan(const NepFrame *__restrict__ fr, const int *__restrict__ cell_count,
-                           int *__restrict__ cell_start) {
+                           int *__restrict__ cell_start, const int *gate) {
+    if (gate && *gate == 0) return;
     const NepFrame &F = fr[blockIdx.x];
     const int n = F.ncells;
     const int *cnt = cell_count + F.cell0;
@@ -284,7 +295,9 @@ __global__ void nepnb_scan(const NepFrame *__restrict__ fr, const int *__restric
 
 __global__ void nepnb_fill(const NepFrame *__restrict__ fr, int nframes, long long natoms,
                            const int *__restrict__ cell_of, const int *__restrict__ cell_start,
-                           int *__restrict__ cell_fill, int *__restrict__ cell_atoms) {
+                           int *__restrict__ cell_fill, int *__restrict__ cell_atoms,
+                           const int *gate) {
+    if (gate && *gate == 0) return;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < natoms;
          t += (long long)gridDim.x * blockDim.x) {
         const int cell = cell_of[t];
@@ -325,6 +338,12 @@ struct SearchArgs {
     long long *NN_r, *NN_a, *NL_r, *NL_a;
     double *Ri_r, *Ri_a;
     int *err;
+    // skin-list build (Verlet reuse): the kept pairs within rc_r go to skin [natoms, max_r]
+    // int32 (global n2, ascending) and their number to skin_cnt; no NL / Ri.  Runs only when
+    // *gate != 0.
+    int *skin, *skin_cnt;
+    float4 *skin_vec;        // optional: the pair vector (x, y, z, 0) at the build, FP32
+    const int *gate;
 };
 
 struct WarpLists {
@@ -337,6 +356,14 @@ struct WarpLists {
 __device__ __forceinline__ void write_entry(const SearchArgs &A, bool radial, long long n1,
                                             int slot, long long n2, double x, double y, double z,
                                             double r) {
+    if (A.skin) {
+        if (radial) {
+            A.skin[n1 * A.max_r + slot] = (int)n2;
+            if (A.skin_vec)
+                A.skin_vec[n1 * A.max_r + slot] = make_float4((float)x, (float)y, (float)z, 0.f);
+        }
+        return;
+    }
     const int mx = radial ? A.max_r : A.max_a;
     long long *NL = radial ? A.NL_r : A.NL_a;
     double *Ri = radial ? A.Ri_r : A.Ri_a;
@@ -424,6 +451,7 @@ __device__ __forceinline__ void drain(const SearchArgs &A, const NepFrame &F, co
 // COUNT: only count neighbors (calculate_maxneigh); TYPED: counts per neighbor element.
 template <bool COUNT, bool TYPED>
 __global__ void __launch_bounds__(128) nepnb_search(SearchArgs A, int warps_per_block) {
+    if (A.gate && *A.gate == 0) return;
     extern __shared__ __align__(16) unsigned char smem[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
@@ -447,6 +475,13 @@ __global__ void __launch_bounds__(128) nepnb_search(SearchArgs A, int warps_per_
         if (TYPED) {
             for (int t = lane; t < 2 * A.ntypes; t += 32) W.tcount[t] = 0;
             __syncwarp();
+        }
+        if (A.skin && F.mode != 0) {   // the skin list is built for cell-list frames only
+            if (lane == 0) {
+                A.skin_cnt[n1] = 0;
+                atomicOr(A.err, MATPL_KERR_BAD_BOX);
+            }
+            continue;
         }
         if (F.mode == 0) {
             const float4 s1 = A.spos[n1];
@@ -612,11 +647,272 @@ __global__ void __launch_bounds__(128) nepnb_search(SearchArgs A, int warps_per_
             }
             continue;
         }
+        if (A.skin) {
+            if (lane == 0) {
+                A.skin_cnt[n1] = min(cr, A.max_r);
+                if (cr > A.max_r) atomicOr(A.err, MATPL_KERR_NEIGHBOR_OVERFLOW);
+            }
+            continue;
+        }
         pad_rows(A, n1, min(cr, A.max_r), min(ca, A.max_a), lane);
         if (lane == 0) {
             A.NN_r[n1] = cr;
             A.NN_a[n1] = ca;
             if (cr > A.max_r || ca > A.max_a) atomicOr(A.err, MATPL_KERR_NEIGHBOR_OVERFLOW);
+        }
+    }
+}
+
+// ---- Verlet-skin reuse (MD-style callers) ----------------------------------------------
+// The skin list holds, per atom, every n2 within r_list = max(rc) + skin at the positions of
+// the last build (ascending, from the cell search above).  While no atom has moved more than
+// skin / 2 since that build, every pair inside max(rc) now is in the list, and the filter
+// below recomputes each listed pair with the search's own FP64 arithmetic, so its NL / Ri /
+// NN equal calculate_neighbor's at the same positions bit for bit (same pairs, same n2 order,
+// same values).  The rebuild decision is a device flag that every build kernel reads (the
+// displacement rule of pair_matpl.cpp:1096-1110), so a captured step needs no host decision.
+
+__global__ void nepnb_skin_check(long long natoms, double half_skin2,
+                                 const double *__restrict__ pos,
+                                 const double *__restrict__ x_ref, int *gate,
+                                 float4 *__restrict__ delta) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    bool far = false;
+    if (t < natoms) {
+        double d[3], d2 = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            d[k] = pos[3 * t + k] - x_ref[3 * t + k];
+            d2 += d[k] * d[k];
+        }
+        far = !(d2 <= half_skin2);   // NaN positions rebuild too
+        if (delta) delta[t] = make_float4((float)d[0], (float)d[1], (float)d[2], 0.f);
+    }
+    if (__any_sync(0xffffffffu, far) && (threadIdx.x & 31) == 0) atomicOr(gate, 1);
+}
+
+__global__ void nepnb_zero_gated(int *__restrict__ a, int *__restrict__ b, long long n,
+                                 const int *gate) {
+    if (*gate == 0) return;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        a[t] = 0;
+        b[t] = 0;
+    }
+}
+
+__global__ void nepnb_gate_clear(int *gate, int *nbuild) {
+    if (*gate != 0) {
+        if (nbuild) *nbuild += 1;
+        *gate = 0;
+    }
+}
+
+// Wrapped fractional coordinates (FP32) of every atom at the current positions, for the
+// filter's pre-test; the frame table is the last build's.
+__global__ void nepnb_skin_frac(const double *__restrict__ pos, const NepFrame *__restrict__ fr,
+                                int nframes, long long natoms, float4 *__restrict__ spos) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < natoms;
+         t += (long long)gridDim.x * blockDim.x) {
+        const NepFrame &F = fr[frame_of(fr, nframes, t)];
+        const float p[3] = {(float)pos[3 * t], (float)pos[3 * t + 1], (float)pos[3 * t + 2]};
+        float s[3];
+        for (int k = 0; k < 3; ++k) {
+            const float v = F.Hinv[3 * k] * p[0] + F.Hinv[3 * k + 1] * p[1] + F.Hinv[3 * k + 2] * p[2];
+            s[k] = v - floorf(v);
+        }
+        spos[t] = make_float4(s[0], s[1], s[2], 0.f);
+    }
+}
+
+constexpr int kFilterWarps = 8;
+
+// Exact FP64 test of the first k (<= 32) queued skin entries, written in queue order.
+__device__ __forceinline__ void skin_drain(const NepFrame &F, const double *__restrict__ pos,
+                                           const double *p1, const int *queue, int k, int lane,
+                                           long long n1, double rc2_r, double rc2_a, int max_r,
+                                           int max_a, int width, long long *__restrict__ NL_r,
+                                           long long *__restrict__ NL_a,
+                                           double *__restrict__ Ri_r, double *__restrict__ Ri_a,
+                                           int &cr, int &ca) {
+    const unsigned lt = (1u << lane) - 1u;
+    bool in_r = false, in_a = false;
+    long long n2 = -1;
+    double x = 0, y = 0, z = 0, d2 = 0;
+    if (lane < k) {
+        n2 = queue[lane];
+        const double p2[3] = {pos[3 * n2], pos[3 * n2 + 1], pos[3 * n2 + 2]};
+        d2 = F.ortho ? exact_pair_ortho(F.box, p1, p2, F.zdelta, x, y, z)
+                     : exact_pair(F.box, p1, p2, F.zdelta, x, y, z);
+        in_r = d2 < rc2_r;
+        in_a = d2 < rc2_a;
+    }
+    const unsigned br = __ballot_sync(0xffffffffu, in_r);
+    const unsigned ba = __ballot_sync(0xffffffffu, in_a);
+    const double r = (width == 4 && (in_r || in_a)) ? sqrt(d2) : 0.0;
+    for (int pass = 0; pass < 2; ++pass) {
+        const bool radial = pass == 0;
+        if (!(radial ? in_r : in_a)) continue;
+        const int slot = (radial ? cr : ca) + __popc((radial ? br : ba) & lt);
+        const int mx = radial ? max_r : max_a;
+        if (slot >= mx) continue;
+        (radial ? NL_r : NL_a)[n1 * mx + slot] = n2;
+        double *o = (radial ? Ri_r : Ri_a) + (n1 * mx + slot) * width;
+        if (width == 4) {
+            reinterpret_cast<double2 *>(o)[0] = make_double2(r, x);
+            reinterpret_cast<double2 *>(o)[1] = make_double2(y, z);
+        } else {
+            o[0] = x; o[1] = y; o[2] = z;
+        }
+    }
+    cr += __popc(br);
+    ca += __popc(ba);
+}
+
+// One warp per atom: the listed pairs inside the cutoffs at the current positions, in list
+// order (ascending n2), in calculate_neighbor's layout.  An FP32 pre-test on the fractional
+// coordinates (margin far above its error) drops the entries clearly outside the larger cutoff;
+// the survivors are queued so that the exact FP64 recomputation runs on full warps.
+__global__ void __launch_bounds__(kFilterWarps * 32)
+nepnb_skin_filter(const NepFrame *__restrict__ fr, int nframes, long long natoms,
+                  const double *__restrict__ pos, const float4 *__restrict__ spos,
+                  const int *__restrict__ skin, const int *__restrict__ skin_cnt, int cap,
+                  double rc2_r, double rc2_a, float pre2, int max_r, int max_a, int width,
+                  long long *__restrict__ NN_r, long long *__restrict__ NN_a,
+                  long long *__restrict__ NL_r, long long *__restrict__ NL_a,
+                  double *__restrict__ Ri_r, double *__restrict__ Ri_a, int *err) {
+    __shared__ int queue_s[kFilterWarps][64];
+    const int lane = threadIdx.x & 31;
+    int *queue = queue_s[threadIdx.x >> 5];
+    const unsigned lt = (1u << lane) - 1u;
+    const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long n1 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; n1 < natoms;
+         n1 += nw) {
+        const NepFrame &F = fr[frame_of(fr, nframes, n1)];
+        const double p1[3] = {pos[3 * n1], pos[3 * n1 + 1], pos[3 * n1 + 2]};
+        const float4 s1 = spos[n1];
+        float H[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) H[q] = F.H[q];
+        const int n = min(skin_cnt[n1], cap);
+        int cr = 0, ca = 0, qn = 0;
+        for (int k0 = 0; k0 < n; k0 += 32) {
+            const int k = k0 + lane;
+            bool pass = false;
+            int n2 = -1;
+            if (k < n) {
+                n2 = skin[n1 * cap + k];
+                if (n2 >= 0 && n2 < natoms) {
+                    const float4 s2 = spos[n2];
+                    float f0 = s2.x - s1.x, f1 = s2.y - s1.y, f2 = s2.z - s1.z;
+                    f0 -= rintf(f0);
+                    f1 -= rintf(f1);
+                    f2 -= rintf(f2);
+                    const float xf = H[0] * f0 + H[1] * f1 + H[2] * f2;
+                    const float yf = H[3] * f0 + H[4] * f1 + H[5] * f2;
+                    const float zf = H[6] * f0 + H[7] * f1 + H[8] * f2;
+                    pass = xf * xf + yf * yf + zf * zf < pre2;
+                } else {
+                    atomicOr(err, MATPL_KERR_BAD_COUNT);
+                }
+            }
+            const unsigned b = __ballot_sync(0xffffffffu, pass);
+            if (pass) queue[qn + __popc(b & lt)] = n2;
+            qn += __popc(b);
+            if (qn >= 32) {
+                __syncwarp();
+                skin_drain(F, pos, p1, queue, 32, lane, n1, rc2_r, rc2_a, max_r, max_a, width,
+                           NL_r, NL_a, Ri_r, Ri_a, cr, ca);
+                const int left = qn - 32;
+                const int v = lane < left ? queue[32 + lane] : 0;
+                __syncwarp();
+                if (lane < left) queue[lane] = v;
+                __syncwarp();
+                qn = left;
+            }
+        }
+        if (qn > 0) {
+            __syncwarp();
+            skin_drain(F, pos, p1, queue, qn, lane, n1, rc2_r, rc2_a, max_r, max_a, width, NL_r,
+                       NL_a, Ri_r, Ri_a, cr, ca);
+        }
+        __syncwarp();
+        for (int s = min(cr, max_r) + lane; s < max_r; s += 32) {
+            NL_r[n1 * max_r + s] = -1;
+            for (int q = 0; q < width; ++q) Ri_r[(n1 * max_r + s) * width + q] = 0.0;
+        }
+        for (int s = min(ca, max_a) + lane; s < max_a; s += 32) {
+            NL_a[n1 * max_a + s] = -1;
+            for (int q = 0; q < width; ++q) Ri_a[(n1 * max_a + s) * width + q] = 0.0;
+        }
+        if (lane == 0) {
+            NN_r[n1] = cr;
+            NN_a[n1] = ca;
+            if (cr > max_r || ca > max_a) atomicOr(err, MATPL_KERR_NEIGHBOR_OVERFLOW);
+        }
+    }
+}
+
+// The compact MD form: the pair vector now = its FP32 vector at the build plus the two atoms'
+// displacements since then (all FP32; no minimum-image fold is needed while every atom stays
+// within skin / 2 of its build position), kept when r^2 < rc^2 in FP32; written as int32 NL
+// and float4 (r, x, y, z) in list order, count in NN (int32).  Slots past NN are not written.
+__global__ void __launch_bounds__(256)
+nepnb_skin_filter_compact(long long natoms, const int *__restrict__ skin,
+                          const int *__restrict__ skin_cnt, const float4 *__restrict__ skin_vec,
+                          const float4 *__restrict__ delta, int cap, float rc2_r, float rc2_a,
+                          int max_r, int max_a, int *__restrict__ NN_r, int *__restrict__ NN_a,
+                          int *__restrict__ NL_r, int *__restrict__ NL_a,
+                          float4 *__restrict__ Ri_r, float4 *__restrict__ Ri_a, int *err) {
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long n1 = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; n1 < natoms;
+         n1 += nw) {
+        const float4 d1 = delta[n1];
+        const int n = min(skin_cnt[n1], cap);
+        int cr = 0, ca = 0;
+        for (int k0 = 0; k0 < n; k0 += 32) {
+            const int k = k0 + lane;
+            bool in_r = false, in_a = false;
+            int n2 = -1;
+            float x = 0.f, y = 0.f, z = 0.f, r2 = 0.f;
+            if (k < n) {
+                n2 = skin[n1 * cap + k];
+                if (n2 >= 0 && n2 < natoms) {
+                    const float4 v = skin_vec[n1 * cap + k];
+                    const float4 d2 = delta[n2];
+                    x = v.x + (d2.x - d1.x);
+                    y = v.y + (d2.y - d1.y);
+                    z = v.z + (d2.z - d1.z);
+                    r2 = x * x + y * y + z * z;
+                    in_r = r2 < rc2_r;
+                    in_a = r2 < rc2_a;
+                } else {
+                    atomicOr(err, MATPL_KERR_BAD_COUNT);
+                }
+            }
+            const unsigned br = __ballot_sync(0xffffffffu, in_r);
+            const unsigned ba = __ballot_sync(0xffffffffu, in_a);
+            if (in_r || in_a) {
+                const float4 o = make_float4(sqrtf(r2), x, y, z);
+                const int sr = cr + __popc(br & lt), sa = ca + __popc(ba & lt);
+                if (in_r && sr < max_r) {
+                    NL_r[n1 * max_r + sr] = n2;
+                    Ri_r[n1 * max_r + sr] = o;
+                }
+                if (in_a && sa < max_a) {
+                    NL_a[n1 * max_a + sa] = n2;
+                    Ri_a[n1 * max_a + sa] = o;
+                }
+            }
+            cr += __popc(br);
+            ca += __popc(ba);
+        }
+        if (lane == 0) {
+            NN_r[n1] = cr;
+            NN_a[n1] = ca;
+            if (cr > max_r || ca > max_a) atomicOr(err, MATPL_KERR_NEIGHBOR_OVERFLOW);
         }
     }
 }
@@ -682,13 +978,14 @@ int run(int nframes, long long natoms, const long long *num_atom, const long lon
     cudaMemsetAsync(w.cell_fill, 0, sizeof(int) * (size_t)cells, s);
     const double rc_max = rc_r > rc_a ? rc_r : rc_a;
     nepnb_setup<<<1, kSetupThreads, 0, s>>>(num_atom, box, box_orig, num_cell, w.fr, nframes,
-                                            natoms, rc_max, err);
+                                            natoms, rc_max, err, nullptr);
     if (natoms == 0) return check_launch("nep_neighbor");
     const int g1 = blocks_for(natoms, 256, device_sms() * 16);
-    nepnb_bin<<<g1, 256, 0, s>>>(pos, w.fr, nframes, natoms, w.spos, w.cell_of, w.cell_count);
-    nepnb_scan<<<nframes, 1024, 0, s>>>(w.fr, w.cell_count, w.cell_start);
+    nepnb_bin<<<g1, 256, 0, s>>>(pos, w.fr, nframes, natoms, w.spos, w.cell_of, w.cell_count,
+                                 nullptr, nullptr, nullptr);
+    nepnb_scan<<<nframes, 1024, 0, s>>>(w.fr, w.cell_count, w.cell_start, nullptr);
     nepnb_fill<<<g1, 256, 0, s>>>(w.fr, nframes, natoms, w.cell_of, w.cell_start, w.cell_fill,
-                                  w.cell_atoms);
+                                  w.cell_atoms, nullptr);
     SearchArgs A;
     A.fr = w.fr; A.nframes = nframes; A.natoms = natoms; A.pos = pos; A.spos = w.spos;
     A.cell_start = w.cell_start; A.cell_count = w.cell_count; A.cell_atoms = w.cell_atoms;
@@ -698,6 +995,7 @@ int run(int nframes, long long natoms, const long long *num_atom, const long lon
     A.max_r = max_r; A.max_a = max_a; A.width = with_rij ? 4 : 3; A.ntypes = typed ? ntypes : 1;
     A.NN_r = NN_r; A.NN_a = NN_a; A.NL_r = NL_r; A.NL_a = NL_a; A.Ri_r = Ri_r; A.Ri_a = Ri_a;
     A.err = err;
+    A.skin = nullptr; A.skin_cnt = nullptr; A.skin_vec = nullptr; A.gate = nullptr;
     const size_t per_warp = warp_scratch(count_only, typed, max_r, max_a, ntypes);
     int wpb = 4;
     while (wpb > 1 && per_warp * wpb > 96 * 1024) wpb >>= 1;
@@ -717,6 +1015,118 @@ int run(int nframes, long long natoms, const long long *num_atom, const long lon
         nepnb_search<false, false><<<grid, 32 * wpb, smem, s>>>(A, wpb);
     }
     return check_launch(count_only ? "matpl_nep_maxneigh" : "matpl_nep_neighbor");
+}
+
+int run_skin_update(int nframes, long long natoms, const long long *num_atom, const double *box,
+                    const double *box_orig, const long long *num_cell, const double *pos,
+                    double r_list, double skin, int cap, int *skin_nbr, int *skin_cnt,
+                    double *x_ref, float4 *skin_vec, float4 *delta, int *gate, int *nbuild,
+                    int *err, void *ws, size_t ws_bytes, cudaStream_t s) {
+    MATPL_REQUIRE(nframes > 0 && natoms >= 0, MATPL_ERR_INVALID, "nframes must be > 0");
+    MATPL_REQUIRE(natoms < (1LL << 31), MATPL_ERR_INVALID, "at most 2^31 - 1 atoms");
+    MATPL_REQUIRE(r_list > 0 && skin >= 0 && cap >= 1, MATPL_ERR_INVALID,
+                  "r_list > 0, skin >= 0 and cap >= 1 required");
+    MATPL_REQUIRE((size_t)cap * 36 <= 200 * 1024, MATPL_ERR_UNSUPPORTED,
+                  "skin capacity must be <= 5688");
+    MATPL_REQUIRE((skin_vec == nullptr) == (delta == nullptr), MATPL_ERR_INVALID,
+                  "skin_vec and delta go together");
+    MATPL_REQUIRE(aligned16(skin_vec) && aligned16(delta), MATPL_ERR_INVALID,
+                  "skin_vec and delta must be 16-byte aligned");
+    if (natoms == 0) return MATPL_OK;
+    MATPL_REQUIRE(num_atom && box && box_orig && num_cell && pos && skin_nbr && skin_cnt &&
+                      x_ref && gate && err,
+                  MATPL_ERR_INVALID, "null pointer argument");
+    const size_t need = workspace_layout(nframes, natoms, nullptr, nullptr);
+    MATPL_REQUIRE(ws && ws_bytes >= need, MATPL_ERR_INVALID, "workspace too small");
+    Workspace w;
+    workspace_layout(nframes, natoms, (unsigned char *)ws, &w);
+    const long long cells = natoms + 27LL * nframes;
+    ProfScope ps("nep_skin_update", s);
+    const double h = 0.5 * skin;
+    nepnb_skin_check<<<(unsigned)((natoms + 255) / 256), 256, 0, s>>>(natoms, h * h, pos, x_ref,
+                                                                      gate, delta);
+    const int g1 = blocks_for(natoms, 256, device_sms() * 16);
+    nepnb_zero_gated<<<blocks_for(cells, 256, device_sms() * 16), 256, 0, s>>>(
+        w.cell_count, w.cell_fill, cells, gate);
+    nepnb_setup<<<1, kSetupThreads, 0, s>>>(num_atom, box, box_orig, num_cell, w.fr, nframes,
+                                            natoms, r_list, err, gate);
+    nepnb_bin<<<g1, 256, 0, s>>>(pos, w.fr, nframes, natoms, w.spos, w.cell_of, w.cell_count,
+                                 gate, x_ref, delta);
+    nepnb_scan<<<nframes, 1024, 0, s>>>(w.fr, w.cell_count, w.cell_start, gate);
+    nepnb_fill<<<g1, 256, 0, s>>>(w.fr, nframes, natoms, w.cell_of, w.cell_start, w.cell_fill,
+                                  w.cell_atoms, gate);
+    SearchArgs A;
+    A.fr = w.fr; A.nframes = nframes; A.natoms = natoms; A.pos = pos; A.spos = w.spos;
+    A.cell_start = w.cell_start; A.cell_count = w.cell_count; A.cell_atoms = w.cell_atoms;
+    A.type_map = nullptr; A.rc2_r = r_list * r_list; A.rc2_a = 0.0;
+    const float pre = (float)(r_list * 1.00001) + kPrefilterMargin;
+    A.pre2 = pre * pre;
+    A.max_r = cap; A.max_a = 0; A.width = 4; A.ntypes = 1;
+    A.NN_r = nullptr; A.NN_a = nullptr; A.NL_r = nullptr; A.NL_a = nullptr;
+    A.Ri_r = nullptr; A.Ri_a = nullptr; A.err = err;
+    A.skin = skin_nbr; A.skin_cnt = skin_cnt; A.skin_vec = skin_vec; A.gate = gate;
+    const size_t per_warp = warp_scratch(false, false, cap, 0, 1);
+    int wpb = 4;
+    while (wpb > 1 && per_warp * wpb > 96 * 1024) wpb >>= 1;
+    const size_t smem = align_up(per_warp * wpb, 16);
+    const int grid = blocks_for(natoms, wpb, device_sms() * 64);
+    cudaFuncSetAttribute(nepnb_search<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)smem);
+    nepnb_search<false, false><<<grid, 32 * wpb, smem, s>>>(A, wpb);
+    nepnb_gate_clear<<<1, 1, 0, s>>>(gate, nbuild);
+    return check_launch("matpl_nep_skin_update");
+}
+
+int run_skin_filter(int nframes, long long natoms, const double *pos, double rc_r, double rc_a,
+                    int max_r, int max_a, int with_rij, int cap, const int *skin_nbr,
+                    const int *skin_cnt, long long *NN_r, long long *NN_a, long long *NL_r,
+                    long long *NL_a, double *Ri_r, double *Ri_a, int *err, void *ws,
+                    size_t ws_bytes, cudaStream_t s) {
+    MATPL_REQUIRE(nframes > 0 && natoms >= 0, MATPL_ERR_INVALID, "nframes must be > 0");
+    MATPL_REQUIRE(natoms < (1LL << 31), MATPL_ERR_INVALID, "at most 2^31 - 1 atoms");
+    MATPL_REQUIRE(rc_r > 0 && rc_a > 0 && cap >= 1 && max_r >= 0 && max_a >= 0,
+                  MATPL_ERR_INVALID, "positive cutoffs, cap >= 1 and max_nn >= 0 required");
+    if (natoms == 0) return MATPL_OK;
+    MATPL_REQUIRE(pos && skin_nbr && skin_cnt && NN_r && NN_a && NL_r && NL_a && Ri_r && Ri_a &&
+                      err,
+                  MATPL_ERR_INVALID, "null pointer argument");
+    const size_t need = workspace_layout(nframes, natoms, nullptr, nullptr);
+    MATPL_REQUIRE(ws && ws_bytes >= need, MATPL_ERR_INVALID, "workspace too small");
+    Workspace w;
+    workspace_layout(nframes, natoms, (unsigned char *)ws, &w);
+    ProfScope ps("nep_skin_filter", s);
+    nepnb_skin_frac<<<blocks_for(natoms, 256, device_sms() * 16), 256, 0, s>>>(pos, w.fr, nframes,
+                                                                             natoms, w.spos);
+    const double rc_max = rc_r > rc_a ? rc_r : rc_a;
+    const float pre = (float)(rc_max * 1.00001) + kPrefilterMargin;
+    const int grid = blocks_for(natoms, kFilterWarps, device_sms() * 32);
+    nepnb_skin_filter<<<grid, kFilterWarps * 32, 0, s>>>(
+        w.fr, nframes, natoms, pos, w.spos, skin_nbr, skin_cnt, cap, rc_r * rc_r, rc_a * rc_a,
+        pre * pre, max_r, max_a, with_rij ? 4 : 3, NN_r, NN_a, NL_r, NL_a, Ri_r, Ri_a, err);
+    return check_launch("matpl_nep_skin_filter");
+}
+
+int run_skin_filter_compact(long long natoms, double rc_r, double rc_a, int max_r, int max_a,
+                            int cap, const int *skin_nbr, const int *skin_cnt,
+                            const float4 *skin_vec, const float4 *delta, int *NN_r, int *NN_a,
+                            int *NL_r, int *NL_a, float4 *Ri_r, float4 *Ri_a, int *err,
+                            cudaStream_t s) {
+    MATPL_REQUIRE(natoms >= 0 && natoms < (1LL << 31), MATPL_ERR_INVALID,
+                  "natoms must be in [0, 2^31)");
+    MATPL_REQUIRE(rc_r > 0 && rc_a > 0 && cap >= 1 && max_r >= 0 && max_a >= 0,
+                  MATPL_ERR_INVALID, "positive cutoffs, cap >= 1 and max_nn >= 0 required");
+    if (natoms == 0) return MATPL_OK;
+    MATPL_REQUIRE(skin_nbr && skin_cnt && skin_vec && delta && NN_r && NN_a && NL_r && NL_a &&
+                      Ri_r && Ri_a && err,
+                  MATPL_ERR_INVALID, "null pointer argument");
+    MATPL_REQUIRE(aligned16(skin_vec) && aligned16(delta) && aligned16(Ri_r) && aligned16(Ri_a),
+                  MATPL_ERR_INVALID, "skin_vec, delta and Ri_* must be 16-byte aligned");
+    ProfScope ps("nep_skin_filter_compact", s);
+    const int grid = blocks_for(natoms, 8, device_sms() * 32);
+    nepnb_skin_filter_compact<<<grid, 256, 0, s>>>(
+        natoms, skin_nbr, skin_cnt, skin_vec, delta, cap, (float)(rc_r * rc_r),
+        (float)(rc_a * rc_a), max_r, max_a, NN_r, NN_a, NL_r, NL_a, Ri_r, Ri_a, err);
+    return check_launch("matpl_nep_skin_filter_compact");
 }
 
 }  // namespace
@@ -757,4 +1167,49 @@ extern "C" int matpl_nep_maxneigh(int nframes, long long natoms, const long long
                cutoff_radial, cutoff_angular, 0, 0, 1, true, with_type != 0, NN_radial,
                NN_angular, nullptr, nullptr, nullptr, nullptr, err_dev, workspace,
                workspace_bytes, as_stream(stream));
+}
+
+extern "C" int matpl_nep_skin_update(int nframes, long long natoms, const long long *num_atom,
+                                     const double *box, const double *box_orig,
+                                     const long long *num_cell, const double *position,
+                                     double r_list, double skin, int cap, int *skin_nbr,
+                                     int *skin_cnt, double *x_ref, float *skin_vec,
+                                     float *delta, int *gate, int *nbuild, int *err_dev,
+                                     void *workspace, size_t workspace_bytes, void *stream) {
+    MATPL_REQUIRE_ON_DEVICE(position, "matpl_nep_skin_update");
+    return run_skin_update(nframes, natoms, num_atom, box, box_orig, num_cell, position, r_list,
+                           skin, cap, skin_nbr, skin_cnt, x_ref, (float4 *)skin_vec,
+                           (float4 *)delta, gate, nbuild, err_dev, workspace, workspace_bytes,
+                           as_stream(stream));
+}
+
+extern "C" int matpl_nep_skin_filter(int nframes, long long natoms, const double *position,
+                                     double cutoff_radial, double cutoff_angular,
+                                     int max_nn_radial, int max_nn_angular, int with_rij,
+                                     int cap, const int *skin_nbr, const int *skin_cnt,
+                                     long long *NN_radial, long long *NN_angular,
+                                     long long *NL_radial, long long *NL_angular,
+                                     double *Ri_radial, double *Ri_angular, int *err_dev,
+                                     void *workspace, size_t workspace_bytes, void *stream) {
+    MATPL_REQUIRE_ON_DEVICE(position, "matpl_nep_skin_filter");
+    return run_skin_filter(nframes, natoms, position, cutoff_radial, cutoff_angular,
+                           max_nn_radial, max_nn_angular, with_rij, cap, skin_nbr, skin_cnt,
+                           NN_radial, NN_angular, NL_radial, NL_angular, Ri_radial, Ri_angular,
+                           err_dev, workspace, workspace_bytes, as_stream(stream));
+}
+
+extern "C" int matpl_nep_skin_filter_compact(long long natoms, double cutoff_radial,
+                                             double cutoff_angular, int max_nn_radial,
+                                             int max_nn_angular, int cap, const int *skin_nbr,
+                                             const int *skin_cnt, const float *skin_vec,
+                                             const float *delta, int *NN_radial,
+                                             int *NN_angular, int *NL_radial, int *NL_angular,
+                                             float *Ri_radial, float *Ri_angular, int *err_dev,
+                                             void *stream) {
+    MATPL_REQUIRE_ON_DEVICE(skin_nbr, "matpl_nep_skin_filter_compact");
+    return run_skin_filter_compact(natoms, cutoff_radial, cutoff_angular, max_nn_radial,
+                                   max_nn_angular, cap, skin_nbr, skin_cnt,
+                                   (const float4 *)skin_vec, (const float4 *)delta, NN_radial,
+                                   NN_angular, NL_radial, NL_angular, (float4 *)Ri_radial,
+                                   (float4 *)Ri_angular, err_dev, as_stream(stream));
 }

@@ -329,7 +329,10 @@ class NEP(torch.nn.Module):
     @_lib.on_device
     def evaluate(self, NN_radial, NL_radial, Ri_radial, NN_angular, NL_angular, Ri_angular,
                  num_atom, atom_type_map, out=None, descriptor_only: bool = False):
-        """Raw evaluation: dict(Ei [N], Etot [B] f64, Force [N, 3], Virial [B, 9] f64)."""
+        """Raw evaluation: dict(Ei [N], Etot [B] f64, Force [N, 3], Virial [B, 9] f64).
+
+        Takes calculate_neighbor's lists (int64 NN / NL, f64 Ri), or the compact MD lists of
+        ``ops.SkinNeighbor(compact=True)`` (int32 NN / NL, f32 Ri; float32 models only)."""
         import ctypes
         from . import _lib
         from ._lib import check, ptr
@@ -351,10 +354,13 @@ class NEP(torch.nn.Module):
             raise _lib.MatplError("Ri_radial / Ri_angular must be (r, x, y, z) (with_rij = True)")
         lib = _lib.load()
         ws = workspace(dev, lib.matpl_nep_workspace_bytes(self.code, B, N), "nep")
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        if Ri_radial.dtype == torch.float32 and NL_radial.dtype == torch.int32:
+            return self._evaluate_compact(NN_radial, NL_radial, Ri_radial, NN_angular, NL_angular,
+                                          Ri_angular, na, tm, ws, stream, out, descriptor_only)
         lists = (NL_radial.shape[1], ptr(i64(NN_radial)), ptr(i64(NL_radial)), ptr(f64(Ri_radial)),
                  NL_angular.shape[1], ptr(i64(NN_angular)), ptr(i64(NL_angular)),
                  ptr(f64(Ri_angular)))
-        stream = torch.cuda.current_stream(dev).cuda_stream
         if descriptor_only:
             feats = torch.empty(N, self.cfg.feature_nums, dtype=self.dtype, device=dev)
             check(lib.matpl_nep_descriptor(self.code, ctypes.byref(self._model), B, N, ptr(na),
@@ -377,6 +383,40 @@ class NEP(torch.nn.Module):
                 nep_ops.nep_zbl(self.cfg.zbl, self.cfg.atom_type, i64(NL_angular),
                                 f64(Ri_angular), tm, counts, out["Ei"], out["Etot"], out["Force"],
                                 out["Virial"])
+        if self.check_errors:
+            code = int(self.err.item())
+            if code:
+                self.err.zero_()
+                raise _lib.MatplError(f"matpl_nep_eval kernel error code {code}")
+        return out
+
+    def _evaluate_compact(self, NN_r, NL_r, Ri_r, NN_a, NL_a, Ri_a, na, tm, ws, stream, out,
+                          descriptor_only):
+        import ctypes
+        from . import _lib
+        from ._lib import check, ptr
+        if self.precision != "float32" or descriptor_only or self.cfg.zbl is not None:
+            raise _lib.MatplError("the compact (int32 / f32) lists are evaluated by float32 "
+                                  "models without ZBL, energy / force / virial only")
+        ts = (NN_r, NL_r, Ri_r, NN_a, NL_a, Ri_a)
+        if any(not t.is_contiguous() for t in ts) or NN_r.dtype != torch.int32 or \
+                NN_a.dtype != torch.int32 or NL_a.dtype != torch.int32 or \
+                Ri_a.dtype != torch.float32:
+            raise _lib.MatplError("compact lists: contiguous int32 NN / NL and float32 Ri")
+        N, B = NL_r.shape[0], na.shape[0]
+        dev = Ri_r.device
+        if out is None:
+            out = {"Ei": torch.empty(N, dtype=torch.float32, device=dev),
+                   "Etot": torch.empty(B, dtype=torch.float64, device=dev),
+                   "Force": torch.empty(N, 3, dtype=torch.float32, device=dev),
+                   "Virial": torch.empty(B, 9, dtype=torch.float64, device=dev)}
+        lib = _lib.load()
+        check(lib.matpl_nep_eval_compact(self.code, ctypes.byref(self._model), B, N, ptr(na),
+                                         ptr(tm), NL_r.shape[1], ptr(NN_r), ptr(NL_r), ptr(Ri_r),
+                                         NL_a.shape[1], ptr(NN_a), ptr(NL_a), ptr(Ri_a),
+                                         ptr(out["Ei"]), ptr(out["Etot"]), ptr(out["Force"]),
+                                         ptr(out["Virial"]), ptr(ws), ws.numel(), stream),
+              "matpl_nep_eval_compact")
         if self.check_errors:
             code = int(self.err.item())
             if code:

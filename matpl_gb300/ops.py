@@ -334,6 +334,149 @@ def calculate_neighbor(num_atoms: torch.Tensor, atom_type_map: torch.Tensor,
     return [NN_r, NN_a, NL_r, NL_a, Ri_r, Ri_a]
 
 
+class SkinNeighbor:
+    """Verlet-skin reuse of ``calculate_neighbor``'s lists for a caller that steps one fixed box
+    (molecular dynamics).  ``lists(position)`` returns what ``calculate_neighbor`` returns at
+    that position, bit for bit (same pairs, same order, same values), but rebuilds its skin list
+    (all pairs within max cutoff + ``skin``) only when some atom has moved more than skin / 2
+    since the last build, the rule of ``pair_matpl.cpp:1096-1110``; otherwise it filters the
+    skin list with the search's own FP64 arithmetic.  The rebuild decision is taken on the
+    device, so the call (and an evaluation after it) can be captured in a CUDA graph.
+
+    ``compact=True`` is the MD form: the lists are int32 NN / NL and f32 Ri [N, max_NN, 4]
+    = (r, x, y, z), made in FP32 from each pair's vector at the build plus the two atoms'
+    displacements since then (a few FP32 ulps from the exact vectors; entries past NN are not
+    written); ``nep.NEP.evaluate`` takes them in float32.
+
+    The returned tensors are owned by this object and overwritten by the next call.  The box is
+    fixed: ``set_box`` replaces it and forces a rebuild.  Every frame must be a single cell at
+    least three (max cutoff + skin)-wide cells thick; other boxes raise ValueError (use
+    ``calculate_neighbor``).  ``capacity`` (skin-list slots per atom) defaults to 1.25 x the
+    largest count within max cutoff + skin at the first positions, plus 16."""
+
+    def __init__(self, num_atoms: torch.Tensor, box: torch.Tensor, box_orig: torch.Tensor,
+                 num_cell: torch.Tensor, position: torch.Tensor, cutoff_2b: float,
+                 cutoff_3b: float, max_NN_radial: int, max_NN_angular: int,
+                 with_rij: bool = True, skin: float = 1.0, capacity: Optional[int] = None,
+                 compact: bool = False):
+        dev, na, bx, bo, nc, pos = _nep_frames(num_atoms, box, box_orig, num_cell, position)
+        if skin < 0:
+            raise ValueError("skin must be >= 0")
+        if compact and not with_rij:
+            raise ValueError("the compact lists always carry r (with_rij)")
+        self.compact = bool(compact)
+        self.device = dev
+        self.na, self.bx, self.bo, self.nc = na, bx, bo, nc
+        self.N = pos.shape[0]
+        self.rc = (float(cutoff_2b), float(cutoff_3b))
+        self.skin = float(skin)
+        # a hair above max(rc) + skin: a pair just inside rc after moves just under skin / 2
+        # each stays inside r_list whatever the last-bit rounding of the two distances
+        self.r_list = max(self.rc) + self.skin + 1e-6
+        self.mr, self.ma = int(max_NN_radial), int(max_NN_angular)
+        self.width = 4 if with_rij else 3
+        if capacity is None:
+            zeros = torch.zeros(self.N, dtype=torch.int64, device=dev)
+            cnt, _ = calculate_maxneigh(na, bx, bo, nc, pos, self.r_list, min(self.rc), 1,
+                                        zeros, False)
+            capacity = int(int(cnt.max()) * 1.25) + 16 if self.N else 16
+        self.cap = int(capacity)
+        i32 = dict(dtype=torch.int32, device=dev)
+        self.skin_nbr = torch.empty(self.N, self.cap, **i32)
+        self.skin_cnt = torch.zeros(self.N, **i32)
+        self.x_ref = torch.zeros(self.N, 3, dtype=torch.float64, device=dev)
+        self.skin_vec = (torch.zeros(self.N, self.cap, 4, dtype=torch.float32, device=dev)
+                         if compact else None)
+        self.delta = torch.zeros(self.N, 4, dtype=torch.float32, device=dev) if compact else None
+        self.gate = torch.ones(1, **i32)
+        self.nbuild = torch.zeros(1, **i32)
+        self.err = torch.zeros(1, **i32)
+        lib = _lib.load()
+        self.ws = torch.empty(max(256, lib.matpl_nep_neighbor_workspace_bytes(na.shape[0],
+                                                                              self.N)),
+                              dtype=torch.uint8, device=dev)
+        N, w = self.N, self.width
+        it, ft = (torch.int32, torch.float32) if compact else (torch.int64, torch.float64)
+        self.out = [torch.empty(N, dtype=it, device=dev),
+                    torch.empty(N, dtype=it, device=dev),
+                    torch.empty(N, self.mr, dtype=it, device=dev),
+                    torch.empty(N, self.ma, dtype=it, device=dev),
+                    torch.empty(N, self.mr, w, dtype=ft, device=dev),
+                    torch.empty(N, self.ma, w, dtype=ft, device=dev)]
+        if compact:      # entries past NN are never written: keep them defined
+            for t, v in zip(self.out[2:], (-1, -1, 0, 0)):
+                t.fill_(v)
+        self.lists(pos)
+        code = int(self.err.item())
+        if code == _lib.KERR_BAD_BOX:
+            raise ValueError("SkinNeighbor: a frame is not one cell at least three "
+                             f"{self.r_list:.3f} A cells thick; use calculate_neighbor")
+        self.check_errors()
+
+    @_lib.on_device
+    def lists(self, position: torch.Tensor) -> List[torch.Tensor]:
+        """[NN_radial, NN_angular, NL_radial, NL_angular, Ri_radial, Ri_angular] at
+        ``position`` ([N, 3] f64 cartesian, on this object's device)."""
+        pos = position
+        if not (pos.dtype == torch.float64 and pos.is_contiguous()):
+            pos = pos.to(torch.float64).contiguous()
+        if pos.device != self.device or pos.numel() != 3 * self.N:
+            raise _lib.MatplError(f"SkinNeighbor: position must be [{self.N}, 3] on {self.device}")
+        lib = _lib.load()
+        s = _stream(self.device)
+        B = self.na.shape[0]
+        check(lib.matpl_nep_skin_update(B, self.N, ptr(self.na), ptr(self.bx), ptr(self.bo),
+                                        ptr(self.nc), ptr(pos), self.r_list, self.skin, self.cap,
+                                        ptr(self.skin_nbr), ptr(self.skin_cnt), ptr(self.x_ref),
+                                        ptr(self.skin_vec), ptr(self.delta), ptr(self.gate),
+                                        ptr(self.nbuild), ptr(self.err), ptr(self.ws),
+                                        self.ws.numel(), s),
+              "matpl_nep_skin_update")
+        o = self.out
+        if self.compact:
+            check(lib.matpl_nep_skin_filter_compact(
+                self.N, self.rc[0], self.rc[1], self.mr, self.ma, self.cap, ptr(self.skin_nbr),
+                ptr(self.skin_cnt), ptr(self.skin_vec), ptr(self.delta), ptr(o[0]), ptr(o[1]),
+                ptr(o[2]), ptr(o[3]), ptr(o[4]), ptr(o[5]), ptr(self.err), s),
+                "matpl_nep_skin_filter_compact")
+            return o
+        check(lib.matpl_nep_skin_filter(B, self.N, ptr(pos), self.rc[0], self.rc[1], self.mr,
+                                        self.ma, int(self.width == 4), self.cap,
+                                        ptr(self.skin_nbr), ptr(self.skin_cnt), ptr(o[0]),
+                                        ptr(o[1]), ptr(o[2]), ptr(o[3]), ptr(o[4]), ptr(o[5]),
+                                        ptr(self.err), ptr(self.ws), self.ws.numel(), s),
+              "matpl_nep_skin_filter")
+        return o
+
+    __call__ = lists
+
+    def set_box(self, box: torch.Tensor, box_orig: torch.Tensor, num_cell: torch.Tensor):
+        """Replace the box (same frames and atoms); the next call rebuilds."""
+        B = self.na.shape[0]
+        self.bx.copy_(box.reshape(B, 18))
+        self.bo.copy_(box_orig.reshape(B, 9))
+        self.nc.copy_(num_cell.reshape(B, 3))
+        self.force_rebuild()
+
+    def force_rebuild(self):
+        self.gate.fill_(1)
+
+    def rebuilds(self) -> int:
+        """Skin-list builds so far (one device read)."""
+        return int(self.nbuild.item())
+
+    def check_errors(self):
+        """Raise on a kernel error recorded since the last check (one device read): a list
+        longer than max_NN or a skin list longer than its capacity raises NeighborOverflow."""
+        code = int(self.err.item())
+        if code:
+            self.err.zero_()
+            if code == _lib.KERR_NEIGHBOR_OVERFLOW:
+                raise NeighborOverflow("SkinNeighbor: a list is longer than max_NN or the skin "
+                                       f"capacity {self.cap}")
+            raise _lib.MatplError(f"SkinNeighbor kernel error code {code}")
+
+
 # NEP training operators (CalcOps.calculateNepFeat / calculateNepMbFeat / calculateNepForce /
 # calculateNepVirial) live in nep_ops (which builds on this module) and resolve here on access
 _NEP_OPS = ("calculateNepFeat", "calculateNepMbFeat", "calculateNepForce", "calculateNepVirial")

@@ -152,6 +152,34 @@ def test_md_entry_points_validate_on_the_host():
     assert lib.matpl_md_kick(7, 1, 2, 1.0, 103.6, *([None] * 10)) == DTYPE
 
 
+def test_nep_skin_entry_points_validate_on_the_host():
+    """The NEP skin-list update and filter refuse bad sizes, NULL pointers and a short workspace
+    before any CUDA call; an empty system is a no-op."""
+    lib = _lib.load()
+    OK, INVALID, UNSUPPORTED = 0, 1, 5
+    upd = lambda nf, n, r, skin, cap, ws=None, nb=0: lib.matpl_nep_skin_update(  # noqa: E731
+        nf, n, *([None] * 5), r, skin, cap, *([None] * 8), ws, nb, None)
+    assert upd(1, 0, 7.0, 1.0, 100) == OK
+    assert upd(0, 10, 7.0, 1.0, 100) == INVALID
+    assert upd(1, 10, 0.0, 1.0, 100) == INVALID
+    assert upd(1, 10, 7.0, -1.0, 100) == INVALID
+    assert upd(1, 10, 7.0, 1.0, 0) == INVALID
+    assert upd(1, 10, 7.0, 1.0, 6000) == UNSUPPORTED
+    assert upd(1, 10, 7.0, 1.0, 100) == INVALID            # NULL arrays
+    filt = lambda n, rr, ra, cap: lib.matpl_nep_skin_filter(  # noqa: E731
+        1, n, None, rr, ra, 80, 30, 1, cap, *([None] * 10), 0, None)
+    assert filt(0, 6.0, 4.0, 100) == OK
+    assert filt(10, 6.0, 0.0, 100) == INVALID
+    assert filt(10, 6.0, 4.0, 0) == INVALID
+    assert filt(10, 6.0, 4.0, 100) == INVALID               # NULL arrays
+    comp = lambda n, rr, cap: lib.matpl_nep_skin_filter_compact(  # noqa: E731
+        n, rr, 4.0, 80, 30, cap, *([None] * 12))
+    assert comp(0, 6.0, 100) == OK
+    assert comp(10, 0.0, 100) == INVALID
+    assert comp(10, 6.0, 0) == INVALID
+    assert comp(10, 6.0, 100) == INVALID                   # NULL arrays
+
+
 def test_noalloc_neighbor_search_refuses_oversize_requests_on_the_host():
     """The allocation-free search has a fixed scratch array; a request that needs more is
     refused before any CUDA call (200,000 atoms need far more than its 4 MiB)."""
