@@ -171,6 +171,10 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
     const NepLayout &L = A.L;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     T *P = reinterpret_cast<T *>(smem_raw);
+    // the 3-body constants in shared memory: lanes index them by their own lm, and lane-varying
+    // indices into __constant__ memory are served one address at a time
+    __shared__ T c3s[24];
+    if (threadIdx.x < 24) c3s[threadIdx.x] = C3<T>(threadIdx.x);
     // parameters: c2, c3, q_scaler as packed; per element W0 rows padded to Hp, b0, W1, b1
     {
         const T *gp = reinterpret_cast<const T *>(A.params);
@@ -201,10 +205,11 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
         }
     }
     unsigned char *Wb = smem_raw + A.smem_params + (size_t)A.warp_bytes * wib;
-    T *stash_g = reinterpret_cast<T *>(Wb + A.o_stash_g);    // [32][NAM]
+    constexpr int NAMP = (NAM + 3) / 4 * 4;                   // rows padded for 16-byte loads
+    T *stash_g = reinterpret_cast<T *>(Wb + A.o_stash_g);    // [32][NAMP]
     T *stash_b = reinterpret_cast<T *>(Wb + A.o_stash_b);    // [32][25]
     T *s_sm = reinterpret_cast<T *>(Wb + A.o_s);             // [NAM][24]
-    T *dEds = reinterpret_cast<T *>(Wb + A.o_dEds);          // [NAM][24]
+    T *dEds = reinterpret_cast<T *>(Wb + A.o_dEds);          // [24][NAMP]
     T *fin = reinterpret_cast<T *>(Wb + A.o_fin);            // [FMp] scaled features
     T *dq = reinterpret_cast<T *>(Wb + A.o_dq);              // [FMp] dE/dq
     T *dpre = reinterpret_cast<T *>(Wb + A.o_dpre);          // [Hp]
@@ -267,8 +272,8 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
         T qr[NRM];
 #pragma unroll
         for (int n = 0; n < NRM; ++n) qr[n] = T(0);
-        for (int sl = lane; sl < nnr; sl += 32) {
-            const long long j = list_index<CL>(A, true, row_r + sl);
+        // element of neighbor j, -1 (and the error recorded) when j or its type is out of range
+        auto type_of = [&](long long j) -> int {
             int tj = -1;
             if (j >= 0 && j < A.natoms) {
                 tj = (int)A.type_map[j];
@@ -276,9 +281,10 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
             } else if (j >= A.natoms) {
                 atomicOr(A.err, MATPL_KERR_BAD_COUNT);
             }
-            T r, px, py, pz;
-            list_pair<T, CL>(A, true, row_r + sl, tj >= 0, r, px, py, pz);
-            if (!(r > T(0))) { rj[sl] = -1; continue; }
+            return tj;
+        };
+        auto radial_one = [&](int sl, long long j, int tj, T r, T px, T py, T pz) {
+            if (tj < 0 || !(r > T(0))) { rj[sl] = -1; return; }
             const T rinv = T(1) / r;
             sts4(rv + 4 * sl, px, py, pz, rinv);
             rj[sl] = (int)j;
@@ -305,6 +311,21 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
                 qr[n] += g;
                 rgp[sl * NRM + n] = gp;
             }
+        };
+        // two slots per lane and pass: both slots' list loads are in flight before either's
+        // neighbor-type gather, and both gathers before the arithmetic
+        for (int sl0 = lane; sl0 < nnr; sl0 += 64) {
+            const int sl1 = sl0 + 32;
+            const bool two = sl1 < nnr;
+            const long long j0 = list_index<CL>(A, true, row_r + sl0);
+            const long long j1 = two ? list_index<CL>(A, true, row_r + sl1) : -1;
+            T r0, x0, y0, z0, r1, x1, y1, z1;
+            list_pair<T, CL>(A, true, row_r + sl0, true, r0, x0, y0, z0);
+            list_pair<T, CL>(A, true, row_r + sl1, two, r1, x1, y1, z1);
+            const int tj0 = type_of(j0);
+            const int tj1 = two ? type_of(j1) : -1;
+            radial_one(sl0, j0, tj0, r0, x0, y0, z0);
+            if (two) radial_one(sl1, j1, tj1, r1, x1, y1, z1);
         }
 #pragma unroll
         for (int n = 0; n < NRM; ++n) qr[n] = warp_sum(qr[n]);
@@ -317,16 +338,10 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
             const int sl = base + lane;
             if (sl < nna) {
                 const long long j = list_index<CL>(A, false, row_a + sl);
-                int tj = -1;
-                if (j >= 0 && j < A.natoms) {
-                    tj = (int)A.type_map[j];
-                    if (tj < 0 || tj >= L.ntypes) { atomicOr(A.err, MATPL_KERR_BAD_TYPE); tj = -1; }
-                } else if (j >= A.natoms) {
-                    atomicOr(A.err, MATPL_KERR_BAD_COUNT);
-                }
                 T r, px, py, pz;
-                list_pair<T, CL>(A, false, row_a + sl, tj >= 0, r, px, py, pz);
-                const bool ok = r > T(0);
+                list_pair<T, CL>(A, false, row_a + sl, true, r, px, py, pz);
+                const int tj = type_of(j);
+                const bool ok = tj >= 0 && r > T(0);
                 T f[KAP], df[KAP];
                 basis<T, KAM>(ok ? r : rc_a, rc_a, rcinv_a, L.ka, f, df);
 #pragma unroll
@@ -347,7 +362,7 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
                             }
                         }
                     }
-                    stash_g[lane * NAM + n] = g;
+                    stash_g[lane * NAMP + n] = g;
                     ag[sl * NAM + n] = g;
                     agp[sl * NAM + n] = gp;
                 }
@@ -369,7 +384,11 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
                 for (int jj = 0; jj < cnt; ++jj) {
                     const T b = stash_b[jj * 25 + lane];
 #pragma unroll
-                    for (int n = 0; n < NAM; ++n) sacc[n] += stash_g[jj * NAM + n] * b;
+                    T gv[NAMP];
+#pragma unroll
+                    for (int q = 0; q < NAMP; q += 4) lds4(stash_g + jj * NAMP + q, gv + q);
+#pragma unroll
+                    for (int n = 0; n < NAM; ++n) sacc[n] += gv[n] * b;
                 }
             }
             __syncwarp();
@@ -399,7 +418,7 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
                 q = T(0);
                 for (int lm = lo; lm < hi; ++lm) {
                     const T sv = s_sm[n * 24 + lm];
-                    q += C3<T>(lm) * sv * sv;
+                    q += c3s[lm] * sv * sv;
                 }
             } else if (L.four && fa < n3 + L.na) {
                 const T *s = s_sm + (fa - n3) * 24;
@@ -458,11 +477,11 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
 #pragma unroll
             for (int n = 0; n < NAM; ++n) {
                 if (n >= L.na) {              // rows past n_max are read (times zero) below
-                    dEds[n * 24 + lm] = T(0);
+                    dEds[lm * NAMP + n] = T(0);
                     continue;
                 }
                 const T *s = s_sm + n * 24;
-                T d = dq[L.two + l * L.na + n] * T(2) * C3<T>(lm) * s[lm];
+                T d = dq[L.two + l * L.na + n] * T(2) * c3s[lm] * s[lm];
                 if (L.four && lm >= 3 && lm <= 7) {
                     const T g4 = dq[L.two + n3 + n];
                     T dd;
@@ -489,7 +508,7 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
                                      : T(2) * C5<T>(1) * a0 * s[lm] + T(4) * C5<T>(2) * a12 * s[lm];
                     d += g5 * dd;
                 }
-                dEds[n * 24 + lm] = d;
+                dEds[lm * NAMP + n] = d;
             }
         }
         __syncwarp();
@@ -536,10 +555,12 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
             for (int lm = 0; lm < 24; ++lm) {
                 T b, gx, gy, gz;
                 harmonic<T>(lm, ux, uy, uz, b, gx, gy, gz);
-                T Bl = T(0);
+                T Bl = T(0), dv[NAMP];
+#pragma unroll
+                for (int q = 0; q < NAMP; q += 4) lds4(dEds + lm * NAMP + q, dv + q);
 #pragma unroll
                 for (int n = 0; n < NAM; ++n) {
-                    const T d = dEds[n * 24 + lm];
+                    const T d = dv[n];
                     Bl += d * g[n];
                     An[n] += d * b;
                 }
@@ -678,10 +699,11 @@ int launch_eval(const EvalArgs &A0, cudaStream_t s) {
     };
     const size_t t = sizeof(T);
     const int mr = A.max_r > 0 ? A.max_r : 1, ma = A.max_a > 0 ? A.max_a : 1;
-    A.o_stash_g = take(32 * NAM * t);
+    constexpr int NAMP = (NAM + 3) / 4 * 4;
+    A.o_stash_g = take(32 * NAMP * t);
     A.o_stash_b = take(32 * 25 * t);
     A.o_s = take(NAM * 24 * t);
-    A.o_dEds = take(NAM * 24 * t);
+    A.o_dEds = take(NAMP * 24 * t);
     A.o_fin = take(L.fmp * t);
     A.o_dq = take(L.fmp * t);
     A.o_dpre = take(L.hp * t);

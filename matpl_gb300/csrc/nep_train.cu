@@ -166,10 +166,12 @@ __global__ void __launch_bounds__(32 * kFeatWarps) nep2b_op(FeatArgs A) {
 __device__ __forceinline__ int f3(int l, int n, int nmax) { return l * nmax + n; }
 
 // dq_f / ds_m for the features of one n (3-body of l(m), 4-body, 5-body) contracted with G:
-// returns sum_f G_f dq_f/ds_m.  sv = s_n[0..23] of this atom.
+// returns sum_f G_f dq_f/ds_m.  sv = s_n[0..23] of this atom; c3 = the 3-body constants in
+// shared memory (lanes index them by their own m).
 template <typename T>
-__device__ __forceinline__ T sbar_of(int m, const T *sv, T g3, T g4, T g5, bool four, bool five) {
-    T v = g3 * T(2) * C3<T>(m) * sv[m];
+__device__ __forceinline__ T sbar_of(const T *c3, int m, const T *sv, T g3, T g4, T g5, bool four,
+                                     bool five) {
+    T v = g3 * T(2) * c3[m] * sv[m];
     if (four && m >= 3 && m <= 7) {
         const T s3 = sv[3], s4 = sv[4], s5 = sv[5], s6 = sv[6], s7 = sv[7];
         T d;
@@ -191,9 +193,9 @@ __device__ __forceinline__ T sbar_of(int m, const T *sv, T g3, T g4, T g5, bool 
 
 // the derivative of sbar_of along sd (Hessian of q in s times sd, contracted with G)
 template <typename T>
-__device__ __forceinline__ T sbar_dot(int m, const T *sv, const T *sd, T g3, T g4, T g5, bool four,
-                                      bool five) {
-    T v = g3 * T(2) * C3<T>(m) * sd[m];
+__device__ __forceinline__ T sbar_dot(const T *c3, int m, const T *sv, const T *sd, T g3, T g4,
+                                      T g5, bool four, bool five) {
+    T v = g3 * T(2) * c3[m] * sd[m];
     if (four && m >= 3 && m <= 7) {
         const T s3 = sv[3], s4 = sv[4], s5 = sv[5], s6 = sv[6], s7 = sv[7];
         const T d3 = sd[3], d4 = sd[4], d5 = sd[5], d6 = sd[6], d7 = sd[7];
@@ -287,6 +289,11 @@ __global__ void __launch_bounds__(32 * kFeatWarps) nepmb_op(FeatArgs A) {
     const long long gw = (long long)blockIdx.x * kFeatWarps + wib;
     const long long nw = (long long)gridDim.x * kFeatWarps;
     const int nlm = n_ * 24;
+    // the 3-body constants in shared memory: lane-varying indices into __constant__ memory are
+    // served one address at a time
+    __shared__ T c3s[24];
+    if (threadIdx.x < 24) c3s[threadIdx.x] = C3<T>(threadIdx.x);
+    __syncthreads();
     for (long long i = gw; i < A.natoms; i += nw) {
         const int ti = (int)A.type[i];
         if (ti < 0 || ti >= T_) {
@@ -372,7 +379,7 @@ __global__ void __launch_bounds__(32 * kFeatWarps) nepmb_op(FeatArgs A) {
                     const int m0 = blk == 0 ? 0 : blk == 1 ? 3 : blk == 2 ? 8 : 15;
                     const int m1 = blk == 0 ? 3 : blk == 1 ? 8 : blk == 2 ? 15 : 24;
                     for (int m = m0; m < m1; ++m)
-                        v += MODE == kFwd ? C3<T>(m) * sv[m] * sv[m] : T(2) * C3<T>(m) * sv[m] * sd[m];
+                        v += MODE == kFwd ? c3s[m] * sv[m] * sv[m] : T(2) * c3s[m] * sv[m] * sd[m];
                 } else if (four && blk == A.l3) {
                     if (MODE == kFwd) {
                         const T s3 = sv[3], s4 = sv[4], s5 = sv[5], s6 = sv[6], s7 = sv[7];
@@ -381,7 +388,7 @@ __global__ void __launch_bounds__(32 * kFeatWarps) nepmb_op(FeatArgs A) {
                             C4<T>(4) * s4 * s5 * s7;
                     } else {
                         for (int m = 3; m <= 7; ++m)
-                            v += sbar_of<T>(m, sv, T(0), T(1), T(0), true, false) * sd[m];
+                            v += sbar_of<T>(c3s, m, sv, T(0), T(1), T(0), true, false) * sd[m];
                     }
                 } else {
                     if (MODE == kFwd) {
@@ -389,7 +396,7 @@ __global__ void __launch_bounds__(32 * kFeatWarps) nepmb_op(FeatArgs A) {
                         v = C5<T>(0) * a0 * a0 + C5<T>(1) * a0 * a12 + C5<T>(2) * a12 * a12;
                     } else {
                         for (int m = 0; m <= 2; ++m)
-                            v += sbar_of<T>(m, sv, T(0), T(0), T(1), false, true) * sd[m];
+                            v += sbar_of<T>(c3s, m, sv, T(0), T(0), T(1), false, true) * sd[m];
                     }
                 }
                 out[blk * n_ + n] = v;
@@ -403,8 +410,9 @@ __global__ void __launch_bounds__(32 * kFeatWarps) nepmb_op(FeatArgs A) {
             const T g3 = l < A.l3 ? Gr[f3(l, n, n_)] : T(0);
             const T g4 = four ? Gr[A.l3 * n_ + n] : T(0);
             const T g5 = five ? Gr[(A.l3 + four) * n_ + n] : T(0);
-            S.sb[n][m] = sbar_of<T>(m, S.s[n], g3, g4, g5, four, five);
-            if (MODE == kBwd2) S.sbd[n][m] = sbar_dot<T>(m, S.s[n], S.sd[n], g3, g4, g5, four, five);
+            S.sb[n][m] = sbar_of<T>(c3s, m, S.s[n], g3, g4, g5, four, five);
+            if (MODE == kBwd2)
+                S.sbd[n][m] = sbar_dot<T>(c3s, m, S.s[n], S.sd[n], g3, g4, g5, four, five);
         }
         __syncwarp();
         // ---- pass 2: grad_d12 (BWD) and the per-atom c-gradient table W (either may be
