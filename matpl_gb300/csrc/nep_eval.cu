@@ -164,7 +164,9 @@ __device__ __forceinline__ void flush_frame(const EvalArgs &A, int frame, double
     if (lane == 0 && e != 0.0) atomicAdd(A.Etot + frame, e);
 }
 
-template <typename T, int NRM, int KRM, int NAM, int KAM, bool CL>
+// NRM / KRM / NAM / KAM: compiled maxima of n_max + 1 and basis_size + 1; EX: the model has
+// exactly these sizes (the size guards inside the unrolled loops then fold away).
+template <typename T, int NRM, int KRM, int NAM, int KAM, bool CL, bool EX>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -206,6 +208,9 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
     }
     unsigned char *Wb = smem_raw + A.smem_params + (size_t)A.warp_bytes * wib;
     constexpr int NAMP = (NAM + 3) / 4 * 4;                   // rows padded for 16-byte loads
+    const int nr_ = EX ? NRM : L.nr, kr_ = EX ? KRM : L.kr, na_ = EX ? NAM : L.na,
+              ka_ = EX ? KAM : L.ka;
+    const int kpr_ = EX ? (KRM + 3) / 4 * 4 : L.kpr, kpa_ = EX ? (KAM + 3) / 4 * 4 : L.kpa;
     T *stash_g = reinterpret_cast<T *>(Wb + A.o_stash_g);    // [32][NAMP]
     T *stash_b = reinterpret_cast<T *>(Wb + A.o_stash_b);    // [32][25]
     T *s_sm = reinterpret_cast<T *>(Wb + A.o_s);             // [NAM][24]
@@ -289,18 +294,18 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
             sts4(rv + 4 * sl, px, py, pz, rinv);
             rj[sl] = (int)j;
             T f[KRP], df[KRP];
-            basis<T, KRM>(r, rc_r, rcinv_r, L.kr, f, df);
+            basis<T, KRM>(r, rc_r, rcinv_r, kr_, f, df);
 #pragma unroll
             for (int k = KRM; k < KRP; ++k) f[k] = df[k] = T(0);
-            const T *c = c2 + (ti * L.ntypes + tj) * L.nr * L.kpr;
+            const T *c = c2 + (ti * L.ntypes + tj) * nr_ * kpr_;
 #pragma unroll
             for (int n = 0; n < NRM; ++n) {
                 T g = T(0), gp = T(0);
-                if (n < L.nr) {
+                if (n < nr_) {
 #pragma unroll
                     for (int k4 = 0; k4 < KRP; k4 += 4) {
                         T c4[4];
-                        lds4(c + n * L.kpr + k4, c4);
+                        lds4(c + n * kpr_ + k4, c4);
 #pragma unroll
                         for (int u = 0; u < 4; ++u) {
                             g += c4[u] * f[k4 + u];
@@ -343,18 +348,18 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
                 const int tj = type_of(j);
                 const bool ok = tj >= 0 && r > T(0);
                 T f[KAP], df[KAP];
-                basis<T, KAM>(ok ? r : rc_a, rc_a, rcinv_a, L.ka, f, df);
+                basis<T, KAM>(ok ? r : rc_a, rc_a, rcinv_a, ka_, f, df);
 #pragma unroll
                 for (int k = KAM; k < KAP; ++k) f[k] = df[k] = T(0);
-                const T *c = c3 + (ok ? (ti * L.ntypes + tj) : 0) * L.na * L.kpa;
+                const T *c = c3 + (ok ? (ti * L.ntypes + tj) : 0) * na_ * kpa_;
 #pragma unroll
                 for (int n = 0; n < NAM; ++n) {
                     T g = T(0), gp = T(0);
-                    if (n < L.na && ok) {
+                    if (n < na_ && ok) {
 #pragma unroll
                         for (int k4 = 0; k4 < KAP; k4 += 4) {
                             T c4[4];
-                            lds4(c + n * L.kpa + k4, c4);
+                            lds4(c + n * kpa_ + k4, c4);
 #pragma unroll
                             for (int u = 0; u < 4; ++u) {
                                 g += c4[u] * f[k4 + u];
@@ -410,9 +415,9 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
         // ---------------- angular features, scaled
         for (int fa = lane; fa < L.nfeat - L.two; fa += 32) {
             T q;
-            const int n3 = L.l3 * L.na;
+            const int n3 = L.l3 * na_;
             if (fa < n3) {
-                const int l = fa / L.na, n = fa - l * L.na;
+                const int l = fa / na_, n = fa - l * na_;
                 const int lo = l == 0 ? 0 : (l == 1 ? 3 : (l == 2 ? 8 : 15));
                 const int hi = l == 0 ? 3 : (l == 1 ? 8 : (l == 2 ? 15 : 24));
                 q = T(0);
@@ -420,13 +425,13 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
                     const T sv = s_sm[n * 24 + lm];
                     q += c3s[lm] * sv * sv;
                 }
-            } else if (L.four && fa < n3 + L.na) {
+            } else if (L.four && fa < n3 + na_) {
                 const T *s = s_sm + (fa - n3) * 24;
                 q = C4<T>(0) * s[3] * s[3] * s[3] + C4<T>(1) * s[3] * (s[4] * s[4] + s[5] * s[5]) +
                     C4<T>(2) * s[3] * (s[6] * s[6] + s[7] * s[7]) +
                     C4<T>(3) * s[6] * (s[5] * s[5] - s[4] * s[4]) + C4<T>(4) * s[4] * s[5] * s[7];
             } else {
-                const T *s = s_sm + (fa - n3 - (L.four ? L.na : 0)) * 24;
+                const T *s = s_sm + (fa - n3 - (L.four ? na_ : 0)) * 24;
                 const T a0 = s[0] * s[0], a12 = s[1] * s[1] + s[2] * s[2];
                 q = C5<T>(0) * a0 * a0 + C5<T>(1) * a0 * a12 + C5<T>(2) * a12 * a12;
             }
@@ -473,15 +478,15 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
         // ---------------- dE/ds_nlm (lanes over lm)
         if (lane < 24 && L.l3) {
             const int lm = lane, l = l_of(lm);
-            const int n3 = L.l3 * L.na;
+            const int n3 = L.l3 * na_;
 #pragma unroll
             for (int n = 0; n < NAM; ++n) {
-                if (n >= L.na) {              // rows past n_max are read (times zero) below
+                if (n >= na_) {              // rows past n_max are read (times zero) below
                     dEds[lm * NAMP + n] = T(0);
                     continue;
                 }
                 const T *s = s_sm + n * 24;
-                T d = dq[L.two + l * L.na + n] * T(2) * c3s[lm] * s[lm];
+                T d = dq[L.two + l * na_ + n] * T(2) * c3s[lm] * s[lm];
                 if (L.four && lm >= 3 && lm <= 7) {
                     const T g4 = dq[L.two + n3 + n];
                     T dd;
@@ -501,7 +506,7 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
                     d += g4 * dd;
                 }
                 if (L.five && lm <= 2) {
-                    const T g5 = dq[L.two + n3 + (L.four ? L.na : 0) + n];
+                    const T g5 = dq[L.two + n3 + (L.four ? na_ : 0) + n];
                     const T a0 = s[0] * s[0], a12 = s[1] * s[1] + s[2] * s[2];
                     const T dd = lm == 0
                                      ? T(4) * C5<T>(0) * a0 * s[0] + T(2) * C5<T>(1) * s[0] * a12
@@ -685,11 +690,11 @@ size_t ws_layout(int dtype, int nframes, long long natoms, unsigned char *base,
     return off;
 }
 
-template <typename T, int NRM, int KRM, int NAM, int KAM, bool CL>
+template <typename T, int NRM, int KRM, int NAM, int KAM, bool CL, bool EX>
 int launch_eval(const EvalArgs &A0, cudaStream_t s) {
     EvalArgs A = A0;
     const NepLayout &L = A.L;
-    auto kern = nep_eval_kernel<T, NRM, KRM, NAM, KAM, CL>;
+    auto kern = nep_eval_kernel<T, NRM, KRM, NAM, KAM, CL, EX>;
     // per-warp scratch, 16-byte aligned pieces
     int off = 0;
     auto take = [&](size_t bytes) {
@@ -743,11 +748,13 @@ int launch_eval(const EvalArgs &A0, cudaStream_t s) {
 template <typename T, bool CL>
 int dispatch(const EvalArgs &A, cudaStream_t s) {
     const NepLayout &L = A.L;
+    if (L.nr == 5 && L.kr == 9 && L.na == 5 && L.ka == 9)      // n_max 4, basis_size 8
+        return launch_eval<T, 5, 9, 5, 9, CL, true>(A, s);
     if (L.nr <= 5 && L.kr <= 9 && L.na <= 5 && L.ka <= 9)
-        return launch_eval<T, 5, 9, 5, 9, CL>(A, s);
+        return launch_eval<T, 5, 9, 5, 9, CL, false>(A, s);
     MATPL_REQUIRE(L.nr <= 8 && L.kr <= 16 && L.na <= 8 && L.ka <= 16, MATPL_ERR_UNSUPPORTED,
                   "n_max <= 7 and basis_size <= 15 are compiled");
-    return launch_eval<T, 8, 16, 8, 16, CL>(A, s);
+    return launch_eval<T, 8, 16, 8, 16, CL, false>(A, s);
 }
 
 // the compact list form: float4 entries only in FP32
