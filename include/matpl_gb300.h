@@ -293,6 +293,21 @@ int matpl_dp_desc_dual_grad(int dtype, long long natoms, int m2, const long long
                             const void *A, const void *A_dot, const void *grad_D,
                             const void *grad_D_dot, void *grad_A, void *grad_A_dot, void *stream);
 
+/* matpl_dp_fit_dual: the fitting part of the same step for the rows of one element
+ * (src/model/dp_embedding.py:140-163, net 400 -> 50 -> 50 -> 50 -> 1 with resnet_dt): with
+ * D, D_dot [nrows, 400] (matpl_dp_desc_dual's rows) and a [nrows] = dL/dE of each row, the
+ * net runs on both streams (E, E_dot) and phi = sum_r (a_r E_r + E_dot_r) is differentiated
+ * once: grad_D, grad_D_dot [nrows, 400] are written; grad_params (the first B3 + 1 entries of
+ * the element's packed fitting block: W0 [400][50], b0, W1 [50][50], b1, dt1, W2, b2, dt2,
+ * W3 [50], b3) and *phi (f64) are accumulated (+=, zero them first).  fit_params = the
+ * element's packed fitting block (with the transposed matrices).  Scratch:
+ * matpl_dp_fit_dual_workspace_bytes(dtype, nrows).  dtype MATPL_F32 or MATPL_F64. */
+size_t matpl_dp_fit_dual_workspace_bytes(int dtype, long long nrows);
+int matpl_dp_fit_dual(int dtype, long long nrows, const void *fit_params, const void *D,
+                      const void *D_dot, const void *a, void *grad_D, void *grad_D_dot,
+                      void *grad_params, double *phi, void *workspace, size_t workspace_bytes,
+                      void *stream);
+
 /* ------------------------------------------------------------------------------------
  * NEP neighbor lists.  Replaces CalcOps calculate_neighbor / calculate_maxneigh
  * (src/op/src/CalcOps.cpp:1025-1172, kernels src/op/kernel/calculateNepNeighbor.cu:8-380,

@@ -81,6 +81,8 @@ SIGNATURES = {
                                 _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "matpl_nep_maxneigh": (_i, [_i, _ll, _vp, _vp, _vp, _vp, _vp, _d, _d, _i, _vp, _i, _vp, _vp,
                                 _vp, _vp, _sz, _vp]),
+    "matpl_dp_fit_dual_workspace_bytes": (_sz, [_i, _ll]),
+    "matpl_dp_fit_dual": (_i, [_i, _ll] + [_vp] * 8 + [_vp, _sz, _vp]),
     "matpl_nep_skin_update": (_i, [_i, _ll, _vp, _vp, _vp, _vp, _vp, _d, _d, _i] + [_vp] * 9 +
                               [_sz, _vp]),
     "matpl_nep_skin_filter_compact": (_i, [_ll, _d, _d, _i, _i, _i] + [_vp] * 12),

@@ -288,6 +288,54 @@ class _DescDual(torch.autograd.Function):
         return gA, gAd, None, None
 
 
+# fitting parameters in the order of the packed fitting block (dp_layout.cuh FitOff) with their
+# (offset, size) there
+_FIT_PARAMS = (("0.weight", _dp.FIT_W0, _dp.DIN * _dp.F), ("0.bias", _dp.FIT_B0, _dp.F),
+               ("1.weight", _dp.FIT_W1, _dp.F * _dp.F), ("1.bias", _dp.FIT_B1, _dp.F),
+               ("1.resnet_dt", _dp.FIT_DT1, _dp.F), ("2.weight", _dp.FIT_W2, _dp.F * _dp.F),
+               ("2.bias", _dp.FIT_B2, _dp.F), ("2.resnet_dt", _dp.FIT_DT2, _dp.F),
+               ("3.weight", _dp.FIT_W3, _dp.F), ("3.bias", _dp.FIT_B3, 1))
+
+
+class _FitDualPhi(torch.autograd.Function):
+    """phi = sum_r (a_r E_r + E_dot_r) for one element's fitting net on the rows (D, D_dot)
+    (dp_embedding.py:140-163 on both streams) together with its first-order gradient in D, D_dot
+    and the fitting parameters, all from matpl_dp_fit_dual; ``fit_block`` is the element's packed
+    fitting block (current weights, with the transposed matrices).  The backward scales the
+    stored gradients by the incoming one."""
+
+    @staticmethod
+    @_lib.on_device
+    def forward(ctx, D, Dd, a, fit_block, *params):
+        from .ops import workspace
+        n = D.shape[0]
+        dev = D.device
+        D, Dd, a = D.contiguous(), Dd.contiguous(), a.contiguous()
+        gD = torch.empty_like(D)
+        gDd = torch.empty_like(Dd)
+        gP = torch.zeros(_dp.FIT_B3 + 1, dtype=D.dtype, device=dev)
+        phi = torch.zeros(1, dtype=torch.float64, device=dev)
+        code = _lib.MATPL_F64 if D.dtype == torch.float64 else _lib.MATPL_F32
+        lib = _lib.load()
+        ws = workspace(dev, lib.matpl_dp_fit_dual_workspace_bytes(code, n), "fit_dual")
+        _check(lib.matpl_dp_fit_dual(code, n, _ptr(fit_block), _ptr(D), _ptr(Dd), _ptr(a),
+                                     _ptr(gD), _ptr(gDd), _ptr(gP), _ptr(phi), _ptr(ws),
+                                     ws.numel(), torch.cuda.current_stream(dev).cuda_stream),
+               "matpl_dp_fit_dual")
+        ctx.save_for_backward(gD, gDd, gP)
+        ctx.shapes = [p.shape if p is not None else None for p in params]
+        return phi.to(D.dtype).reshape(())
+
+    @staticmethod
+    @torch.autograd.function.once_differentiable
+    def backward(ctx, gphi):
+        gD, gDd, gP = ctx.saved_tensors
+        grads = []
+        for (name, off, size), shape in zip(_FIT_PARAMS, ctx.shapes):
+            grads.append(None if shape is None else (gP[off:off + size] * gphi).reshape(shape))
+        return (gD.mul_(gphi), gDd.mul_(gphi), None, None, *grads)
+
+
 class FusedTrainer:
     """Force-loss training step with the embedding nets' second-order gradient in this
     library's kernels.  Per composition cluster (as ``dp_trainer.train``):
@@ -296,17 +344,23 @@ class FusedTrainer:
     2. gE = dL/dE, gF = dL/dF of the loss (dp_loss's MSE terms) on those values;
     3. A, A_dot = per-atom descriptor factor and its tangent along the seed gF
        (``matpl_dp_dual_forward``), plus the empty-slot term of A in torch;
-    4. Ei = fitting nets (torch) on D = A^T A<, Edot = dEi/dA . A_dot;
-    5. Phi = sum gE Etot + sum Edot; Phi.backward() gives dL/dtheta: the fitting part by torch
-       autograd on per-atom tensors, the embedding part by ``matpl_dp_dual_backward``.
+    4. Ei = fitting nets on D = A^T A<, Edot = dEi/dA . A_dot;
+    5. Phi = sum gE Etot + sum Edot; Phi.backward() gives dL/dtheta: the fitting part by
+       ``matpl_dp_fit_dual`` (both streams and the closed-form reverse pass in one kernel, the
+       weight gradients as row sums in a second), the embedding part by
+       ``matpl_dp_dual_backward``.
 
     ``model`` is a DPTrainModel (its Parameters are trained), float32 or float64.
     ``eval_precision``: the form of step 1's evaluation, which only seeds gE and gF; None = the
     model's dtype; "mixed" (float32 models) runs it on the tcgen05 tensor cores (BF16x3
     operands, FP32 accumulation; E / F within ~1e-5 relative of FP32, so the gradient moves by
-    that much relative to the loss residuals)."""
+    that much relative to the loss residuals).
+    ``fit_kernel``: False runs steps 4-5 of the fitting part as torch operations and autograd
+    (the same mathematics; kept for comparison and for fitting shapes other than the compiled
+    400-50-50-50-1)."""
 
-    def __init__(self, model: DPTrainModel, eval_precision: Optional[str] = None):
+    def __init__(self, model: DPTrainModel, eval_precision: Optional[str] = None,
+                 fit_kernel: bool = True):
         if model.dtype not in (torch.float32, torch.float64):
             raise _lib.MatplError("FusedTrainer needs a float32 or float64 DPTrainModel")
         self.model = model
@@ -325,6 +379,9 @@ class FusedTrainer:
         self.davg4 = self.evaluator.davg4
         self.dstd4 = self.evaluator.dstd4
         self._present = None
+        compiled = (list(cfg.fit_sizes) == [_dp.F] * 3 + [1] and cfg.M2 == _dp.M2 and
+                    list(cfg.emb_sizes) == [_dp.E] * 3)
+        self.fit_kernel = bool(fit_kernel) and compiled
 
     def _struct(self, flat):
         m = _lib.MatplDpModel()
@@ -482,9 +539,21 @@ class FusedTrainer:
         D_all = D_all.reshape(D_all.shape[0], -1)
         Dd_all = Dd_all.reshape(Dd_all.shape[0], -1)
         phi = A.new_zeros(())
+        woff = cfg.ntypes * cfg.ntypes * _dp.EMB_SIZE
         for ti in present:
             o, n = blocks[ti]
             if n == 0:
+                continue
+            if self.fit_kernel:
+                if ragged:      # dL/dE of each row's configuration
+                    a = gE.index_select(0, cfg_of.index_select(0, rows[o:o + n]))
+                else:
+                    a = gE.reshape(B, 1).expand(B, n)
+                blk = self.evaluator.packed[woff + ti * _dp.FIT_SIZE:
+                                            woff + (ti + 1) * _dp.FIT_SIZE]
+                params = [model.param(f"fitting_net.{ti}.layers.{nm}") for nm, _, _ in _FIT_PARAMS]
+                phi = phi + _FitDualPhi.apply(D_all[o:o + B * n], Dd_all[o:o + B * n],
+                                              a.reshape(-1).to(model.dtype).detach(), blk, *params)
                 continue
             e, ed = self._fit_dual(ti, D_all[o:o + B * n], Dd_all[o:o + B * n])
             if ragged:          # dL/dE of each row's configuration

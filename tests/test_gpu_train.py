@@ -129,6 +129,33 @@ def test_fused_training_gradients_match_oracle(dtype, tol):
     assert worst < tol, (worst, where)
 
 
+@pytest.mark.parametrize("dtype,tol", [(torch.float64, 1e-11), (torch.float32, 2e-5)])
+def test_fitting_kernel_matches_the_torch_fitting_part(dtype, tol):
+    """matpl_dp_fit_dual (both streams and the reverse pass of the fitting nets in one kernel,
+    the weight gradients as row sums) against the same mathematics as torch operations and
+    autograd, every parameter; 600 atoms so that tiles and row chunks end part-way."""
+    cfg, st, ln, idr, davg, dstd, prm, E_lab, F_lab = make_case(n=600, seed=13)
+    batch = {"list_neigh": torch.tensor(ln, device=DEV), "type_map": torch.tensor(st.types, device=DEV),
+             "atom_type": cfg.atom_type, "ImageDR": torch.tensor(idr, device=DEV),
+             "Etot": E_lab.to(DEV), "Force": F_lab.to(DEV)}
+    grads, losses = [], []
+    for fk in (True, False):
+        model = train.DPTrainModel(cfg, prm, davg, dstd, dtype=dtype, device=DEV)
+        tr = train.FusedTrainer(model, fit_kernel=fk)
+        assert tr.fit_kernel == fk
+        loss, _, _ = tr.loss_and_backward(batch)
+        losses.append(loss)
+        grads.append({k: model.param(k).grad.detach().double().clone() for k in model.names})
+    assert abs(losses[0] - losses[1]) <= (1e-12 if dtype == torch.float64 else 1e-6) * abs(losses[1])
+    worst, where = 0.0, None
+    for k, ref in grads[1].items():
+        err = (grads[0][k] - ref).abs().max().item() / (ref.abs().max().item() + 1e-30)
+        if err > worst:
+            worst, where = err, k
+    print(f"[accuracy] fitting kernel vs torch fitting part {dtype}: worst relative {worst:.2e} ({where})")
+    assert worst < tol, (worst, where)
+
+
 def test_fused_training_two_configs_and_fd():
     """Batch of two configurations of one composition, then a finite-difference check of the
     fused gradient of one embedding weight."""
