@@ -152,6 +152,21 @@ def test_md_entry_points_validate_on_the_host():
     assert lib.matpl_md_kick(7, 1, 2, 1.0, 103.6, *([None] * 10)) == DTYPE
 
 
+def test_fit_dual_validates_on_the_host():
+    """The training fitting kernel refuses bad dtypes, NULL pointers and a short workspace before
+    any CUDA call; no rows is a no-op."""
+    lib = _lib.load()
+    OK, INVALID, DTYPE, WORKSPACE = 0, 1, 2, 3
+    call = lambda dt, n, ws, nb: lib.matpl_dp_fit_dual(dt, n, *([None] * 8), ws, nb, None)  # noqa: E731
+    assert call(_lib.MATPL_F32, 0, None, 0) == OK
+    assert call(_lib.MATPL_MIXED, 10, None, 0) == DTYPE
+    assert call(_lib.MATPL_F32, -1, None, 0) == INVALID
+    assert call(_lib.MATPL_F32, 10, None, 0) == INVALID            # NULL arrays
+    assert lib.matpl_dp_fit_dual_workspace_bytes(_lib.MATPL_F32, 1000) >= 13 * 1000 * 50 * 4
+    assert lib.matpl_dp_fit_dual_workspace_bytes(_lib.MATPL_F64, 1000) >= 13 * 1000 * 50 * 8
+    assert lib.matpl_dp_fit_dual_workspace_bytes(_lib.MATPL_MIXED, 1000) == 0
+
+
 def test_nep_skin_entry_points_validate_on_the_host():
     """The NEP skin-list update and filter refuse bad sizes, NULL pointers and a short workspace
     before any CUDA call; an empty system is a no-op."""
