@@ -31,6 +31,61 @@ namespace {
 using namespace dp;
 constexpr int kStg = E + 1;   // staging row stride (odd: conflict-free column access)
 
+// Shared-memory copy of one embedding net: the vectors, then the two E x E matrices with rows
+// padded to kRp (16-byte aligned rows: a row is 7 vector loads instead of 25 scalar ones) and,
+// for the backward kernel, their transposes (columns as rows).
+constexpr int kRp = 28;
+struct NetS {
+    static constexpr int W0 = 0, B0 = E, B1 = 2 * E, DT1 = 3 * E, B2 = 4 * E, DT2 = 5 * E;
+    static constexpr int M1 = 152, M2 = M1 + E * kRp;          // W1, W2 [in][out]
+    static constexpr int M1T = M2 + E * kRp, M2T = M1T + E * kRp;   // W1^T, W2^T [out][in]
+    static constexpr int FWD = M1T;                            // per-net size without transposes
+    static constexpr int BWD = M2T + E * kRp;
+};
+static_assert(NetS::M1 % 4 == 0 && NetS::M1 >= 6 * E, "aligned matrix block after the vectors");
+
+// params (EmbOff layout, nnet nets) -> shared NetS layout (stride = NetS::FWD or NetS::BWD)
+template <typename T>
+__device__ __forceinline__ void load_nets(T *dst, const T *__restrict__ params, int nnet,
+                                          int stride) {
+    const bool tr = stride == NetS::BWD;
+    for (int q = threadIdx.x; q < nnet * stride; q += blockDim.x) {
+        const int n = q / stride, e = q - n * stride;
+        const T *src = params + (long long)n * EmbOff::SIZE;
+        T v = T(0);
+        if (e < 6 * E) {
+            const int which = e / E, o = e - which * E;
+            const int off[6] = {EmbOff::W0, EmbOff::B0, EmbOff::B1, EmbOff::DT1, EmbOff::B2,
+                                EmbOff::DT2};
+            v = src[off[which] + o];
+        } else if (e >= NetS::M1 && (e < NetS::M1T || tr)) {
+            const int blk = (e - NetS::M1) / (E * kRp), r = (e - NetS::M1) % (E * kRp);
+            const int row = r / kRp, col = r - row * kRp;
+            if (col < E) {
+                const int W = (blk & 1) ? EmbOff::W2 : EmbOff::W1;
+                v = blk < 2 ? src[W + row * E + col] : src[W + col * E + row];
+            }
+        }
+        dst[q] = v;
+    }
+}
+
+// 28 consecutive values of a 16-byte aligned shared row
+__device__ __forceinline__ void ld_row(const float *p, float v[kRp]) {
+#pragma unroll
+    for (int q = 0; q < kRp / 4; ++q) {
+        const float4 f = reinterpret_cast<const float4 *>(p)[q];
+        v[4 * q] = f.x; v[4 * q + 1] = f.y; v[4 * q + 2] = f.z; v[4 * q + 3] = f.w;
+    }
+}
+__device__ __forceinline__ void ld_row(const double *p, double v[kRp]) {
+#pragma unroll
+    for (int q = 0; q < kRp / 2; ++q) {
+        const double2 f = reinterpret_cast<const double2 *>(p)[q];
+        v[2 * q] = f.x; v[2 * q + 1] = f.y;
+    }
+}
+
 struct TrainParams {
     int batch, natoms, nslots, ntypes, m, present_mask, has_gv;
     double rmin, rmax, inv_mT;
@@ -78,15 +133,16 @@ template <typename T>
 __device__ __forceinline__ void layer0(const T *w, T s, T sdot, T x[E], T xd[E]) {
 #pragma unroll
     for (int o = 0; o < E; ++o) {
-        const T t = dev_tanh(s * w[EmbOff::W0 + o] + w[EmbOff::B0 + o]);
+        const T t = dev_tanh(s * w[NetS::W0 + o] + w[NetS::B0 + o]);
         x[o] = t;
-        xd[o] = (T(1) - t * t) * sdot * w[EmbOff::W0 + o];
+        xd[o] = (T(1) - t * t) * sdot * w[NetS::W0 + o];
     }
 }
 
 // Pre-activations of an E -> E layer for a lane's input row x (and its tangent xd) kept in
-// shared memory: h = x W + b, hd = xd W.  The input index loop stays rolled (small code, few
-// registers); the output index is unrolled into registers.
+// shared memory: h = x W + b, hd = xd W (OW: the padded matrix W[in][out] in the NetS copy).
+// The input index loop stays rolled (small code, few registers); the output index is unrolled
+// into registers.
 template <typename T>
 __device__ __forceinline__ void pre_act(const T *w, int OW, int OB, const T *x, const T *xd,
                                         T h[E], T hd[E]) {
@@ -95,7 +151,8 @@ __device__ __forceinline__ void pre_act(const T *w, int OW, int OB, const T *x, 
 #pragma unroll 1
     for (int i = 0; i < E; ++i) {
         const T xi = x[i], xdi = xd[i];
-        const T *wr = w + OW + i * E;
+        T wr[kRp];
+        ld_row(w + OW + i * kRp, wr);
 #pragma unroll
         for (int o = 0; o < E; ++o) {
             h[o] += xi * wr[o];
@@ -104,18 +161,20 @@ __device__ __forceinline__ void pre_act(const T *w, int OW, int OB, const T *x, 
     }
 }
 
-// acc[i] += sum_o W[i][o] z[o] and accd[i] += sum_o W[i][o] zd[o] (z, zd in shared memory).
+// acc[i] += sum_o W[i][o] z[o] and accd[i] += sum_o W[i][o] zd[o] (z, zd in shared memory;
+// WT: the padded transpose W^T[out][in] in the NetS copy).
 template <typename T>
-__device__ __forceinline__ void back_act(const T *W, const T *z, const T *zd, T acc[E],
+__device__ __forceinline__ void back_act(const T *WT, const T *z, const T *zd, T acc[E],
                                          T accd[E]) {
 #pragma unroll 1
     for (int o = 0; o < E; ++o) {
         const T zo = z[o], zdo = zd[o];
+        T wc[kRp];
+        ld_row(WT + o * kRp, wc);
 #pragma unroll
         for (int i = 0; i < E; ++i) {
-            const T wv = W[i * E + o];
-            acc[i] += wv * zo;
-            accd[i] += wv * zdo;
+            acc[i] += wc[i] * zo;
+            accd[i] += wc[i] * zdo;
         }
     }
 }
@@ -151,10 +210,10 @@ dp_dual_fwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
     const int warps = blockDim.x >> 5;
     T *wsm = reinterpret_cast<T *>(smem_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    T *stg = wsm + nnet * EmbOff::SIZE + warp * 32 * kFwdRow;
-    int *list = reinterpret_cast<int *>(wsm + nnet * EmbOff::SIZE + warps * 32 * kFwdRow) +
+    T *stg = wsm + nnet * NetS::FWD + warp * 32 * kFwdRow;
+    int *list = reinterpret_cast<int *>(wsm + nnet * NetS::FWD + warps * 32 * kFwdRow) +
                 warp * S;
-    for (int q = threadIdx.x; q < nnet * EmbOff::SIZE; q += blockDim.x) wsm[q] = params[q];
+    load_nets(wsm, params, nnet, NetS::FWD);
     __syncthreads();
     const long long total = (long long)P.batch * P.natoms;
     T *my = stg + lane * kFwdRow;
@@ -181,7 +240,7 @@ dp_dual_fwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
                 tj = slot / P.m;
                 slot_rows(idr, gF, gV, list_neigh, t, cfg0, slot, S, avg, sd, P, rh, rd);
             }
-            const T *w = wsm + (ti * P.ntypes + tj) * EmbOff::SIZE;
+            const T *w = wsm + (ti * P.ntypes + tj) * NetS::FWD;
             __syncwarp();
             {
                 T x[E], xd[E];
@@ -189,8 +248,8 @@ dp_dual_fwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
 #pragma unroll
                 for (int p = 0; p < E; ++p) { my[p] = x[p]; my[kStg + p] = xd[p]; }
             }
-            layer_res(w, EmbOff::W1, EmbOff::B1, EmbOff::DT1, my, my + kStg);
-            layer_res(w, EmbOff::W2, EmbOff::B2, EmbOff::DT2, my, my + kStg);
+            layer_res(w, NetS::M1, NetS::B1, NetS::DT1, my, my + kStg);
+            layer_res(w, NetS::M2, NetS::B2, NetS::DT2, my, my + kStg);
             const bool valid = k < cnt;
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
@@ -313,8 +372,8 @@ dp_dual_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
     const int nnet = P.ntypes * P.ntypes, S = P.nslots;
     const int warps = blockDim.x >> 5;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    T *wsm = reinterpret_cast<T *>(smem_raw);                   // weights
-    T *gacc = wsm + nnet * EmbOff::SIZE;                        // gradient accumulator
+    T *wsm = reinterpret_cast<T *>(smem_raw);                   // weights (NetS layout)
+    T *gacc = wsm + nnet * NetS::BWD;                           // gradient accumulator
     T *stg_all = gacc + nnet * EmbOff::SIZE;                    // [warps][32][Stage::ROW]
     T *ab_all = stg_all + warps * 32 * Stage::ROW;              // [warps][2][NA]
     int *list_all = reinterpret_cast<int *>(ab_all + warps * 2 * NA);
@@ -322,10 +381,8 @@ dp_dual_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
     T *ab = ab_all + warp * 2 * NA;
     int *list = list_all + warp * S;
     T *my = stg + lane * Stage::ROW;
-    for (int q = threadIdx.x; q < nnet * EmbOff::SIZE; q += blockDim.x) {
-        wsm[q] = params[q];
-        gacc[q] = T(0);
-    }
+    load_nets(wsm, params, nnet, NetS::BWD);
+    for (int q = threadIdx.x; q < nnet * EmbOff::SIZE; q += blockDim.x) gacc[q] = T(0);
     __syncthreads();
     const T k = (T)P.inv_mT;
     const long long total = (long long)P.batch * P.natoms;
@@ -356,7 +413,7 @@ dp_dual_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
             for (int q = 0; q < 16; ++q)
                 tmask[q] = q < P.ntypes ? __ballot_sync(0xffffffffu, valid && tj == q) : 0u;
             const int nv = min(32, cnt - c0);
-            const T *w = wsm + (ti * P.ntypes + tj) * EmbOff::SIZE;
+            const T *w = wsm + (ti * P.ntypes + tj) * NetS::BWD;
             // seeds: Gbar = k (R Abar + Rdot Adbar), Gdotbar = k R Adbar (k folded into ab)
             T gb[E], gdb[E];
 #pragma unroll
@@ -378,14 +435,14 @@ dp_dual_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
 #pragma unroll
                 for (int p = 0; p < E; ++p) { my[Stage::X + p] = x[p]; my[Stage::XD + p] = xd[p]; }
             }
-            layer_res(w, EmbOff::W1, EmbOff::B1, EmbOff::DT1, my + Stage::X, my + Stage::XD);
+            layer_res(w, NetS::M1, NetS::B1, NetS::DT1, my + Stage::X, my + Stage::XD);
             {
                 T h[E], hd[E];
-                pre_act(w, EmbOff::W2, EmbOff::B2, my + Stage::X, my + Stage::XD, h, hd);
+                pre_act(w, NetS::M2, NetS::B2, my + Stage::X, my + Stage::XD, h, hd);
 #pragma unroll
                 for (int o = 0; o < E; ++o) {
                     const T t2 = dev_tanh(h[o]);
-                    const T dt = w[EmbOff::DT2 + o], g = T(1) - t2 * t2;
+                    const T dt = w[NetS::DT2 + o], g = T(1) - t2 * t2;
                     const T tb = gb[o] * dt, tdb = gdb[o] * dt;
                     my[Stage::Q + o] = gb[o] * t2 + gdb[o] * g * hd[o];
                     my[Stage::ZB + o] = g * (tb - T(2) * t2 * hd[o] * tdb);
@@ -393,7 +450,7 @@ dp_dual_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
                 }
             }
             // x1bar = Gbar + W2 zb2, x1dotbar = Gdotbar + W2 zdb2
-            back_act(w + EmbOff::W2, my + Stage::ZB, my + Stage::ZDB, gb, gdb);
+            back_act(w + NetS::M2T, my + Stage::ZB, my + Stage::ZDB, gb, gdb);
             __syncwarp();
             reduce_layer(stg, nv, ti, P.ntypes, tmask, 2, gacc, lane);
             __syncwarp();
@@ -406,18 +463,18 @@ dp_dual_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
             }
             {
                 T h[E], hd[E];
-                pre_act(w, EmbOff::W1, EmbOff::B1, my + Stage::X, my + Stage::XD, h, hd);
+                pre_act(w, NetS::M1, NetS::B1, my + Stage::X, my + Stage::XD, h, hd);
 #pragma unroll
                 for (int o = 0; o < E; ++o) {
                     const T t1 = dev_tanh(h[o]);
-                    const T dt = w[EmbOff::DT1 + o], g = T(1) - t1 * t1;
+                    const T dt = w[NetS::DT1 + o], g = T(1) - t1 * t1;
                     const T tb = gb[o] * dt, tdb = gdb[o] * dt;
                     my[Stage::Q + o] = gb[o] * t1 + gdb[o] * g * hd[o];
                     my[Stage::ZB + o] = g * (tb - T(2) * t1 * hd[o] * tdb);
                     my[Stage::ZDB + o] = g * tdb;
                 }
             }
-            back_act(w + EmbOff::W1, my + Stage::ZB, my + Stage::ZDB, gb, gdb);
+            back_act(w + NetS::M1T, my + Stage::ZB, my + Stage::ZDB, gb, gdb);
             __syncwarp();
             reduce_layer(stg, nv, ti, P.ntypes, tmask, 1, gacc, lane);
             __syncwarp();
@@ -426,7 +483,7 @@ dp_dual_bwd(const int32_t *__restrict__ list_neigh, const T *__restrict__ idr,
             for (int o = 0; o < E; ++o) {
                 const T x0 = my[Stage::X + o];
                 const T g = T(1) - x0 * x0;
-                const T zd0 = rd[0] * w[EmbOff::W0 + o];
+                const T zd0 = rd[0] * w[NetS::W0 + o];
                 my[Stage::ZB + o] = g * (gb[o] - T(2) * x0 * zd0 * gdb[o]);
                 my[Stage::ZDB + o] = g * gdb[o];
             }
@@ -564,14 +621,15 @@ int launch(bool backward, const matpl_dp_model *md, int batch, int natoms, int n
     P.rmin = md->rmin; P.rmax = md->rmax;
     P.inv_mT = 1.0 / ((double)md->m * (double)md->npresent);
     const int nnet = md->ntypes * md->ntypes;
-    const size_t wbytes = (size_t)nnet * EmbOff::SIZE * sizeof(T);
+    const size_t wbytes = (size_t)nnet * EmbOff::SIZE * sizeof(T);          // gradient block
+    const size_t wf = (size_t)nnet * NetS::FWD * sizeof(T), wb = (size_t)nnet * NetS::BWD * sizeof(T);
     int dev = 0, sms = device_sms();
     cudaGetDevice(&dev);
     const long long total = (long long)batch * natoms;
     if (!backward) {
         int warps = 8;
         auto needf = [&](int w) {
-            return wbytes + (size_t)w * 32 * kFwdRow * sizeof(T) + (size_t)w * nslots * sizeof(int);
+            return wf + (size_t)w * 32 * kFwdRow * sizeof(T) + (size_t)w * nslots * sizeof(int);
         };
         while (warps > 1 && needf(warps) > 110 * 1024) --warps;
         const size_t smem = needf(warps);
@@ -587,7 +645,7 @@ int launch(bool backward, const matpl_dp_model *md, int batch, int natoms, int n
     }
     int warps = 8;
     auto need = [&](int w) {
-        return 2 * wbytes + (size_t)w * 32 * Stage::ROW * sizeof(T) +
+        return wb + wbytes + (size_t)w * 32 * Stage::ROW * sizeof(T) +
                (size_t)w * 2 * NA * sizeof(T) + (size_t)w * nslots * sizeof(int);
     };
     while (warps > 1 && need(warps) > 220 * 1024) --warps;
