@@ -254,14 +254,24 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
 #pragma unroll
     for (int q = 0; q < 9; ++q) vir[q] = T(0);
 
+    // the next atom's element and list lengths are loaded while the current atom is processed
+    long long ti_next = A.type_map[a_begin];
+    long long nr_next = L.two ? list_count<CL>(A, true, a_begin) : 0;
+    long long na_next = L.l3 ? list_count<CL>(A, false, a_begin) : 0;
     for (long long i = a_begin; i < a_end; ++i) {
+        const int ti = (int)ti_next;
+        const long long nr_i = nr_next, na_i = na_next;
+        if (i + 1 < a_end) {
+            ti_next = A.type_map[i + 1];
+            if (L.two) nr_next = list_count<CL>(A, true, i + 1);
+            if (L.l3) na_next = list_count<CL>(A, false, i + 1);
+        }
         while (i >= frame_end && frame + 1 < A.nframes) {
             if (!A.feats) flush_frame<T>(A, frame, e_frame, vir, lane);
             e_frame = 0.0;
             ++frame;
             frame_end = A.frame_start[frame + 1];
         }
-        const int ti = (int)A.type_map[i];
         if (ti < 0 || ti >= L.ntypes) {
             if (lane == 0) {
                 atomicOr(A.err, MATPL_KERR_BAD_TYPE);
@@ -269,8 +279,8 @@ nep_eval_kernel(EvalArgs A, long long atoms_per_warp) {
             }
             continue;
         }
-        const int nnr = L.two ? (int)min(list_count<CL>(A, true, i), (long long)A.max_r) : 0;
-        const int nna = L.l3 ? (int)min(list_count<CL>(A, false, i), (long long)A.max_a) : 0;
+        const int nnr = L.two ? (int)min(nr_i, (long long)A.max_r) : 0;
+        const int nna = L.l3 ? (int)min(na_i, (long long)A.max_a) : 0;
         const long long row_r = i * A.max_r, row_a = i * A.max_a;
 
         // ---------------- radial descriptor; pair vector and g_n' kept for the force pass
