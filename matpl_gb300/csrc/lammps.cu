@@ -66,7 +66,7 @@ lmp_neighbors(int inum, int nall, const int *__restrict__ ilist, Lists lists,
               unsigned long long rc2_bits, int32_t *__restrict__ list_neigh,
               TO *__restrict__ image_dr,
               int32_t *__restrict__ type_map, unsigned long long *__restrict__ min_rsq,
-              int32_t *__restrict__ err) {
+              int32_t *__restrict__ err, int32_t *__restrict__ num_neigh) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const long long S = (long long)nt * m;
@@ -141,6 +141,10 @@ lmp_neighbors(int inum, int nall, const int *__restrict__ ilist, Lists lists,
         for (int t = 0; t < 16; ++t) {
             if (t >= nt) break;
             over |= cnt[t] > m;
+            if (num_neigh) {       // occupied-slot form: block lengths instead of zero padding
+                if (lane == 0) num_neigh[(long long)i * nt + t] = min(cnt[t], m);
+                continue;
+            }
             for (int s = cnt[t] + lane; s < m; s += 32) {
                 const long long q = row + (long long)t * m + s;
                 list_neigh[q] = 0;
@@ -168,7 +172,8 @@ template <typename Lists>
 int launch_neighbors(int inum, int nall, const int *ilist, Lists lists, const double *x,
                      const int *type, const int *type_to_model, int ntypes_lmp, int nt, int m,
                      double rcut, int out_dtype, int32_t *list_neigh, void *image_dr,
-                     int32_t *type_map, double *min_rsq, int32_t *err, cudaStream_t s) {
+                     int32_t *type_map, double *min_rsq, int32_t *err, cudaStream_t s,
+                     int32_t *num_neigh = nullptr) {
     ProfScope ps("lmp_neighbors", s);
     auto *mn = reinterpret_cast<unsigned long long *>(min_rsq);
     lmp_init_min<<<1, 1, 0, s>>>(mn);
@@ -184,11 +189,11 @@ int launch_neighbors(int inum, int nall, const int *ilist, Lists lists, const do
         if (out_dtype == MATPL_F64)
             lmp_neighbors<double, Lists><<<(int)grid, 128, 0, s>>>(
                 inum, nall, ilist, lists, x, type, type_to_model, ntypes_lmp, nt, m, rc2_bits,
-                list_neigh, (double *)image_dr, type_map, mn, err);
+                list_neigh, (double *)image_dr, type_map, mn, err, num_neigh);
         else
             lmp_neighbors<float, Lists><<<(int)grid, 128, 0, s>>>(
                 inum, nall, ilist, lists, x, type, type_to_model, ntypes_lmp, nt, m, rc2_bits,
-                list_neigh, (float *)image_dr, type_map, mn, err);
+                list_neigh, (float *)image_dr, type_map, mn, err, num_neigh);
     }
     return check_launch("matpl_lammps_dp_neighbors");
 }
@@ -282,7 +287,7 @@ struct matpl_lammps_dp {
     cudaStream_t stream = nullptr;
     int32_t *err = nullptr;
     int *d_t2m = nullptr;
-    DevBuf din, ln, idr, tmap, Ei, Etot, force, vir, mn, out, ws;
+    DevBuf din, ln, idr, tmap, nn, Ei, Etot, force, vir, mn, out, ws;
     HostBuf hin, hout;
     ~matpl_lammps_dp() {
         if (stream) cudaStreamSynchronize(stream);
@@ -444,7 +449,8 @@ extern "C" int matpl_lammps_dp_compute_models(matpl_lammps_dp *h, int nmodels, i
     bool ok = h->din.ensure(in_bytes) && h->hout.ensure(8 * out_n * nm) &&
               (direct || (h->hin.ensure(in_bytes) && h->out.ensure(8 * out_n * nm))) &&
               h->ln.ensure(4 * S * inum) && h->idr.ensure(es * 4 * S * inum) &&
-              h->tmap.ensure(4 * (size_t)inum) && h->Ei.ensure(es * inum) &&
+              h->tmap.ensure(4 * (size_t)inum) && h->nn.ensure(4 * (size_t)nt * inum) &&
+              h->Ei.ensure(es * inum) &&
               h->Etot.ensure(8) && h->force.ensure(es * 3 * (size_t)nall) &&
               h->vir.ensure(72) && h->mn.ensure(8) && h->ws.ensure(std::max<size_t>(ws_bytes, 16));
     MATPL_REQUIRE(ok, MATPL_ERR_CUDA, "matpl_lammps_dp_compute: CUDA allocation failed");
@@ -452,6 +458,9 @@ extern "C" int matpl_lammps_dp_compute_models(matpl_lammps_dp *h, int nmodels, i
     char *dp = (char *)h->din.p;
     const int out_dtype = f64 ? MATPL_F64 : MATPL_F32;
     int rc;
+    // block lengths of rows that ilist does not name stay 0
+    MATPL_REQUIRE(cudaMemsetAsync(h->nn.p, 0, 4 * (size_t)nt * inum, s) == cudaSuccess,
+                  MATPL_ERR_CUDA, "matpl_lammps_dp_compute: memset failed");
     if (direct) {
         // LAMMPS' arrays as they are: positions / types / ilist / numneigh copied in, the lists
         // read in place through firstneigh
@@ -469,7 +478,8 @@ extern "C" int matpl_lammps_dp_compute_models(matpl_lammps_dp *h, int nmodels, i
                               LammpsLists{(const int *)(dp + o_js), firstneigh},
                               (const double *)(dp + o_x), (const int *)(dp + o_ty), h->d_t2m,
                               h->ntypes_lmp, nt, m, h->model.rmax, out_dtype, (int32_t *)h->ln.p,
-                              h->idr.p, (int32_t *)h->tmap.p, (double *)h->mn.p, h->err, s);
+                              h->idr.p, (int32_t *)h->tmap.p, (double *)h->mn.p, h->err, s,
+                              (int32_t *)h->nn.p);
     } else {
         char *hp = (char *)h->hin.p;
         std::memcpy(hp + o_x, x, 24 * (size_t)nall);
@@ -494,15 +504,18 @@ extern "C" int matpl_lammps_dp_compute_models(matpl_lammps_dp *h, int nmodels, i
                               CsrLists{(const long long *)(dp + o_js), (const int *)(dp + o_jf)},
                               (const double *)(dp + o_x), (const int *)(dp + o_ty), h->d_t2m,
                               h->ntypes_lmp, nt, m, h->model.rmax, out_dtype, (int32_t *)h->ln.p,
-                              h->idr.p, (int32_t *)h->tmap.p, (double *)h->mn.p, h->err, s);
+                              h->idr.p, (int32_t *)h->tmap.p, (double *)h->mn.p, h->err, s,
+                              (int32_t *)h->nn.p);
     }
     if (rc) return rc;
-    // one slot conversion, then every model (pair_matpl.cpp:945-965 runs them one by one)
+    // one slot conversion, then every model (pair_matpl.cpp:945-965 runs them one by one).  The
+    // slots are kept in their occupied form (per-type block lengths, no zero padding written):
+    // the same pairs and arithmetic as the padded list the reference builds
     for (int k = 0; k < nmodels; ++k) {
-        rc = matpl_dp_eval(h->dtype, &h->models[k], 1, inum, (int)S, nghost,
-                           (const int32_t *)h->ln.p, h->idr.p, (const int32_t *)h->tmap.p,
-                           h->Ei.p, (double *)h->Etot.p, h->force.p, (double *)h->vir.p, h->ws.p,
-                           h->ws.cap, s);
+        rc = matpl_dp_eval_occupied(h->dtype, &h->models[k], 1, inum, (int)S, nghost,
+                                    (const int32_t *)h->ln.p, (const int32_t *)h->nn.p, h->idr.p,
+                                    (const int32_t *)h->tmap.p, h->Ei.p, (double *)h->Etot.p,
+                                    h->force.p, (double *)h->vir.p, h->ws.p, h->ws.cap, s);
         if (rc) return rc;
         // direct: forces straight into f, the rest into mapped pinned memory; staged: all into
         // one device buffer, copied back below
