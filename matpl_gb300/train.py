@@ -298,30 +298,40 @@ _FIT_PARAMS = (("0.weight", _dp.FIT_W0, _dp.DIN * _dp.F), ("0.bias", _dp.FIT_B0,
 
 
 class _FitDualPhi(torch.autograd.Function):
-    """phi = sum_r (a_r E_r + E_dot_r) for one element's fitting net on the rows (D, D_dot)
-    (dp_embedding.py:140-163 on both streams) together with its first-order gradient in D, D_dot
-    and the fitting parameters, all from matpl_dp_fit_dual; ``fit_block`` is the element's packed
-    fitting block (current weights, with the transposed matrices).  The backward scales the
+    """phi = sum_r (a_r E_r + E_dot_r) over the element blocks of the rows (D, D_dot) (each
+    element's fitting net, dp_embedding.py:140-163, on both streams) together with its
+    first-order gradient in D, D_dot and the fitting parameters, all from matpl_dp_fit_dual, one
+    launch pair per element into one gradient buffer (the blocks are disjoint row ranges, so no
+    zero fill, no accumulation).  ``blocks`` = ((row offset, rows, element), ...); ``packed`` =
+    the evaluator's packed parameters (current weights, with the transposed matrices) of which
+    element t's fitting block starts at woff + t FIT_SIZE; ``params`` = the fitting parameter
+    tensors of every block's element, ``len(_FIT_PARAMS)`` per block.  The backward scales the
     stored gradients by the incoming one."""
 
     @staticmethod
     @_lib.on_device
-    def forward(ctx, D, Dd, a, fit_block, *params):
+    def forward(ctx, D, Dd, a, packed, blocks, woff, *params):
         from .ops import workspace
-        n = D.shape[0]
         dev = D.device
         D, Dd, a = D.contiguous(), Dd.contiguous(), a.contiguous()
         gD = torch.empty_like(D)
         gDd = torch.empty_like(Dd)
-        gP = torch.zeros(_dp.FIT_B3 + 1, dtype=D.dtype, device=dev)
+        npar = _dp.FIT_B3 + 1
+        gP = torch.zeros(len(blocks), npar, dtype=D.dtype, device=dev)
         phi = torch.zeros(1, dtype=torch.float64, device=dev)
         code = _lib.MATPL_F64 if D.dtype == torch.float64 else _lib.MATPL_F32
         lib = _lib.load()
-        ws = workspace(dev, lib.matpl_dp_fit_dual_workspace_bytes(code, n), "fit_dual")
-        _check(lib.matpl_dp_fit_dual(code, n, _ptr(fit_block), _ptr(D), _ptr(Dd), _ptr(a),
-                                     _ptr(gD), _ptr(gDd), _ptr(gP), _ptr(phi), _ptr(ws),
-                                     ws.numel(), torch.cuda.current_stream(dev).cuda_stream),
-               "matpl_dp_fit_dual")
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        nmax = max(n for _, n, _ in blocks)
+        ws = workspace(dev, lib.matpl_dp_fit_dual_workspace_bytes(code, nmax), "fit_dual")
+        es = D.element_size()
+        for b, (o, n, t) in enumerate(blocks):
+            blk = packed[woff + t * _dp.FIT_SIZE:woff + (t + 1) * _dp.FIT_SIZE]
+            row = o * D.shape[1] * es
+            _check(lib.matpl_dp_fit_dual(code, n, _ptr(blk), _ptr(D) + row, _ptr(Dd) + row,
+                                         _ptr(a) + o * es, _ptr(gD) + row, _ptr(gDd) + row,
+                                         _ptr(gP[b]), _ptr(phi), _ptr(ws), ws.numel(), stream),
+                   "matpl_dp_fit_dual")
         ctx.save_for_backward(gD, gDd, gP)
         ctx.shapes = [p.shape if p is not None else None for p in params]
         return phi.to(D.dtype).reshape(())
@@ -331,9 +341,12 @@ class _FitDualPhi(torch.autograd.Function):
     def backward(ctx, gphi):
         gD, gDd, gP = ctx.saved_tensors
         grads = []
-        for (name, off, size), shape in zip(_FIT_PARAMS, ctx.shapes):
-            grads.append(None if shape is None else (gP[off:off + size] * gphi).reshape(shape))
-        return (gD.mul_(gphi), gDd.mul_(gphi), None, None, *grads)
+        k = len(_FIT_PARAMS)
+        for q, shape in enumerate(ctx.shapes):
+            _, off, size = _FIT_PARAMS[q % k]
+            grads.append(None if shape is None else
+                         (gP[q // k, off:off + size] * gphi).reshape(shape))
+        return (gD.mul_(gphi), gDd.mul_(gphi), None, None, None, None, *grads)
 
 
 class FusedTrainer:
@@ -539,21 +552,25 @@ class FusedTrainer:
         D_all = D_all.reshape(D_all.shape[0], -1)
         Dd_all = Dd_all.reshape(Dd_all.shape[0], -1)
         phi = A.new_zeros(())
-        woff = cfg.ntypes * cfg.ntypes * _dp.EMB_SIZE
-        for ti in present:
+        if self.fit_kernel:
+            # every element block in one autograd node (disjoint row ranges of D_all)
+            if ragged:          # dL/dE of each row's configuration
+                a_all = gE.index_select(0, cfg_of.index_select(0, rows.remainder(N)))
+            else:               # rows are b * N + i
+                a_all = gE.reshape(B).index_select(0, torch.div(rows, N, rounding_mode="floor"))
+            fb, params = [], []
+            for ti in present:
+                o, n = blocks[ti]
+                if n == 0:
+                    continue
+                fb.append((o, B * n, ti))
+                params += [model.param(f"fitting_net.{ti}.layers.{nm}") for nm, _, _ in _FIT_PARAMS]
+            woff = cfg.ntypes * cfg.ntypes * _dp.EMB_SIZE
+            phi = _FitDualPhi.apply(D_all, Dd_all, a_all.to(model.dtype).detach(),
+                                    self.evaluator.packed, tuple(fb), woff, *params)
+        for ti in present if not self.fit_kernel else ():
             o, n = blocks[ti]
             if n == 0:
-                continue
-            if self.fit_kernel:
-                if ragged:      # dL/dE of each row's configuration
-                    a = gE.index_select(0, cfg_of.index_select(0, rows[o:o + n]))
-                else:
-                    a = gE.reshape(B, 1).expand(B, n)
-                blk = self.evaluator.packed[woff + ti * _dp.FIT_SIZE:
-                                            woff + (ti + 1) * _dp.FIT_SIZE]
-                params = [model.param(f"fitting_net.{ti}.layers.{nm}") for nm, _, _ in _FIT_PARAMS]
-                phi = phi + _FitDualPhi.apply(D_all[o:o + B * n], Dd_all[o:o + B * n],
-                                              a.reshape(-1).to(model.dtype).detach(), blk, *params)
                 continue
             e, ed = self._fit_dual(ti, D_all[o:o + B * n], Dd_all[o:o + B * n])
             if ragged:          # dL/dE of each row's configuration
