@@ -1061,7 +1061,8 @@ int run_skin_update(int nframes, long long natoms, const long long *num_atom, co
     A.type_map = nullptr; A.rc2_r = r_list * r_list; A.rc2_a = 0.0;
     const float pre = (float)(r_list * 1.00001) + kPrefilterMargin;
     A.pre2 = pre * pre;
-    A.max_r = cap; A.max_a = 0; A.width = 4; A.ntypes = 1;
+    // width 3: the skin list keeps n2 and the vector, so no pair needs its FP64 root
+    A.max_r = cap; A.max_a = 0; A.width = 3; A.ntypes = 1;
     A.NN_r = nullptr; A.NN_a = nullptr; A.NL_r = nullptr; A.NL_a = nullptr;
     A.Ri_r = nullptr; A.Ri_a = nullptr; A.err = err;
     A.skin = skin_nbr; A.skin_cnt = skin_cnt; A.skin_vec = skin_vec; A.gate = gate;
