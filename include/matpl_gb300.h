@@ -276,6 +276,31 @@ int matpl_dp_dual_backward(int dtype, const matpl_dp_model *model, int batch, in
                            const void *grad_virial, const void *A_bar, const void *A_dot_bar,
                            void *grad_embedding, void *stream);
 
+/* The empty-slot term of A that matpl_dp_dual_forward leaves out (this project's kernels; the
+ * reference gets it from the same autograd graph, its empty slots holding the normalised zero
+ * row of src/model/dp_dp.py:304-342).  For centre type t_i and each present t_j,
+ *   A_pad = k sum_{t_j} n_empty(t_j) R_pad(t_i)^T G_{t_i t_j}(s_pad(t_i)),
+ *   R_pad(t_i) = (0 - davg[t_i]) / dstd[t_i], s_pad = its first entry, k = 1 / (m npresent),
+ * n_empty(t_j) = m - (occupied slots of type block t_j).
+ * matpl_dp_pad_forward: A = A_occ + A_pad [B*N, 100] (A may alias A_occ; atoms whose type is
+ *   not in present[] copy A_occ) and n_empty [B*N, npresent] int32 for the reverse.
+ * matpl_dp_pad_backward: the gradient of Phi w.r.t. the embedding parameters through A_pad for
+ *   A_bar = dPhi/dA: grad_embedding (the first ntypes^2 * 1400 entries of the packed layout) is
+ *   written (nets of absent pairs zero).
+ * workspace: matpl_dp_pad_workspace_bytes(npresent) bytes (0 for npresent outside 1..8;
+ *   a shorter one is MATPL_ERR_WORKSPACE): the backward's FP64 sums over the atoms, kept in
+ *   16 copies that different CTAs add into.
+ * dtype MATPL_F32 or MATPL_F64; model as for matpl_dp_dual_forward. */
+size_t matpl_dp_pad_workspace_bytes(int npresent);
+int matpl_dp_pad_forward(int dtype, const matpl_dp_model *model, int batch, int natoms,
+                         int nslots, const int32_t *list_neigh, const int32_t *type_map,
+                         const void *A_occ, void *A, int32_t *n_empty, void *workspace,
+                         size_t workspace_bytes, void *stream);
+int matpl_dp_pad_backward(int dtype, const matpl_dp_model *model, int batch, int natoms,
+                          int nslots, const int32_t *type_map, const int32_t *n_empty,
+                          const void *A_bar, void *grad_embedding, void *workspace,
+                          size_t workspace_bytes, void *stream);
+
 /* matpl_dp_desc_dual: per atom the descriptor D = A^T A< and its tangent
  *   D_dot = A_dot^T A< + A^T A_dot< (A, A_dot [natoms, 4, 25], A< = first m2 columns; D, D_dot
  *   [natoms, 25, m2]) - the xyz_scater_a^T xyz_scater_b product of src/model/dp_dp.py:304-330

@@ -81,6 +81,11 @@ SIGNATURES = {
                                 _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "matpl_nep_maxneigh": (_i, [_i, _ll, _vp, _vp, _vp, _vp, _vp, _d, _d, _i, _vp, _i, _vp, _vp,
                                 _vp, _vp, _sz, _vp]),
+    "matpl_dp_pad_workspace_bytes": (_sz, [_i]),
+    "matpl_dp_pad_forward": (_i, [_i, _c.POINTER(MatplDpModel), _i, _i, _i] + [_vp] * 6 +
+                             [_sz, _vp]),
+    "matpl_dp_pad_backward": (_i, [_i, _c.POINTER(MatplDpModel), _i, _i, _i] + [_vp] * 5 +
+                              [_sz, _vp]),
     "matpl_dp_fit_dual_workspace_bytes": (_sz, [_i, _ll]),
     "matpl_dp_fit_dual": (_i, [_i, _ll] + [_vp] * 8 + [_vp, _sz, _vp]),
     "matpl_nep_skin_update": (_i, [_i, _ll, _vp, _vp, _vp, _vp, _vp, _d, _d, _i] + [_vp] * 9 +

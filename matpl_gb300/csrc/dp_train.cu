@@ -600,6 +600,313 @@ int launch_desc(bool grad, long long natoms, int m2, const long long *rows, cons
     return check_launch("matpl_dp_desc_dual_grad");
 }
 
+// ---- empty-slot term of A ------------------------------------------------------------------
+// Every empty slot of type block t_j holds the row R_pad(t_i) = (0 - davg[t_i]) / dstd[t_i]
+// (dp_dp.py's normalised zero row), so the slots the dual kernels skip add
+//     A_pad = k sum_{t_j present} n_empty(t_j) R_pad(t_i)^T G_{t_i t_j}(s_pad(t_i)),
+// one row per (t_i, t_j) pair, k = 1 / (m T).  prow[pair] = k R_pad (x) G is computed once per
+// pair (dp_pad_rows), then added per atom with the atom's empty counts (dp_pad_add).  The
+// reverse reduces dPhi/dprow over the atoms (dp_pad_reduce, FP64 sums) and runs each pair's
+// three-layer net backward (dp_pad_net_bwd).
+constexpr int kMaxPresent = 8;
+
+struct PadParams {
+    int rows, natoms, nslots, ntypes, m, npresent;
+    int present[kMaxPresent];
+    double inv_mT;
+};
+
+// The pair's net at s_pad with its activations: x0 = tanh(s W0 + b0), h_l = tanh(x W_l + b_l),
+// x_l = h_l dt_l + x_{l-1}.  One warp, lane e < E owns column e; sx holds the layer input.
+template <typename T>
+__device__ __forceinline__ void pad_net_fwd(const T *__restrict__ w, T s, T *sx, int lane,
+                                            T &x0, T &h1, T &x1, T &h2, T &x2) {
+    x0 = h1 = x1 = h2 = x2 = T(0);
+    if (lane < E) x0 = dev_tanh(s * w[EmbOff::W0 + lane] + w[EmbOff::B0 + lane]);
+    if (lane < E) sx[lane] = x0;
+    __syncwarp();
+    if (lane < E) {
+        T z = w[EmbOff::B1 + lane];
+        for (int i = 0; i < E; ++i) z += sx[i] * w[EmbOff::W1 + i * E + lane];
+        h1 = dev_tanh(z);
+        x1 = h1 * w[EmbOff::DT1 + lane] + x0;
+    }
+    __syncwarp();
+    if (lane < E) sx[lane] = x1;
+    __syncwarp();
+    if (lane < E) {
+        T z = w[EmbOff::B2 + lane];
+        for (int i = 0; i < E; ++i) z += sx[i] * w[EmbOff::W2 + i * E + lane];
+        h2 = dev_tanh(z);
+        x2 = h2 * w[EmbOff::DT2 + lane] + x1;
+    }
+    __syncwarp();
+}
+
+template <typename T>
+__device__ __forceinline__ T pad_row_value(const T *davg, const T *dstd, int ti, int c) {
+    return (T(0) - davg[ti * 4 + c]) / dstd[ti * 4 + c];
+}
+
+// One warp per present (t_i, t_j) pair: prow[qi * np + qj][c * E + e] = k R_pad[c] G[e].
+template <typename T>
+__global__ void __launch_bounds__(32) dp_pad_rows(const T *__restrict__ params,
+                                                  const T *__restrict__ davg,
+                                                  const T *__restrict__ dstd, PadParams P,
+                                                  T *__restrict__ prow) {
+    __shared__ T sx[32];
+    const int pair = blockIdx.x, lane = threadIdx.x;
+    const int ti = P.present[pair / P.npresent], tj = P.present[pair % P.npresent];
+    const T *w = params + (long long)(ti * P.ntypes + tj) * EmbOff::SIZE;
+    T x0, h1, x1, h2, x2;
+    pad_net_fwd(w, pad_row_value(davg, dstd, ti, 0), sx, lane, x0, h1, x1, h2, x2);
+    if (lane < E) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+            prow[(long long)pair * NA + c * E + lane] =
+                T(P.inv_mT) * pad_row_value(davg, dstd, ti, c) * x2;
+    }
+}
+
+// One warp per atom row (b, i): empty counts of the present types (written to n_empty for the
+// reverse) and A = A_occ + sum_j n_empty(t_j) prow[(t_i, t_j)] (A_occ copied through for atoms
+// whose type is absent from present[]).  A may alias A_occ.
+template <typename T>
+__global__ void __launch_bounds__(256) dp_pad_add(const int32_t *__restrict__ ln,
+                                                  const int32_t *__restrict__ tm,
+                                                  const T *__restrict__ prow, PadParams P,
+                                                  const T *A_occ, T *A,
+                                                  int32_t *__restrict__ n_empty) {
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+    for (long long row = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+         row < P.rows; row += warps) {
+        const int32_t *l = ln + row * P.nslots;
+        const int ti = tm[row % P.natoms];
+        // per-lane counts of occupied slots by present type (independent loads, then one
+        // warp reduction per type)
+        int ne[kMaxPresent];
+#pragma unroll
+        for (int q = 0; q < kMaxPresent; ++q) ne[q] = 0;
+#pragma unroll 4
+        for (int s = lane; s < P.nslots; s += 32) {
+            if (l[s] > 0) {
+                const int t = s / P.m;
+#pragma unroll
+                for (int q = 0; q < kMaxPresent; ++q) ne[q] += q < P.npresent && P.present[q] == t;
+            }
+        }
+        int qi = -1;
+#pragma unroll
+        for (int q = 0; q < kMaxPresent; ++q) {
+            if (q < P.npresent) {
+                ne[q] = P.m - (int)__reduce_add_sync(0xffffffffu, (unsigned)ne[q]);
+                if (P.present[q] == ti) qi = q;
+                if (lane == 0) n_empty[row * P.npresent + q] = ne[q];
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < (NA + 31) / 32; ++k) {
+            const int idx = lane + 32 * k;
+            if (idx >= NA) break;
+            T acc = A_occ[row * NA + idx];
+            if (qi >= 0) {
+#pragma unroll
+                for (int q = 0; q < kMaxPresent; ++q)
+                    if (q < P.npresent)
+                        acc += T(ne[q]) * prow[(long long)(qi * P.npresent + q) * NA + idx];
+            }
+            A[row * NA + idx] = acc;
+        }
+    }
+}
+
+// gsum[rep][qi * np + qj][idx] += sum over rows of type t_i of n_empty(t_j) Abar[row][idx].
+// A CTA of G groups of 128 threads: thread idx < NA of a group owns one column and keeps the
+// group's sums in shared memory (np^2 x NA values of the compute type: a group sums a few
+// dozen rows); the groups are then added together in FP64 and the CTA adds its sums into
+// replica rep = blockIdx.x % kPadReps (only for the centre types it met), so that the atomics
+// of different CTAs spread over kPadReps copies.
+constexpr int kPadReps = 16;
+
+template <typename T>
+__global__ void __launch_bounds__(512, 2) dp_pad_reduce(const int32_t *__restrict__ tm,
+                                                        const int32_t *__restrict__ n_empty,
+                                                        const T *__restrict__ A_bar,
+                                                        PadParams P, int chunk,
+                                                        double *__restrict__ gsum) {
+    extern __shared__ __align__(16) unsigned char pad_smem[];
+    T *sacc = reinterpret_cast<T *>(pad_smem);
+    __shared__ int seen[kMaxPresent];
+    __shared__ int qof[16];
+    const int np = P.npresent, G = blockDim.x >> 7, grp = threadIdx.x >> 7;
+    const int idx = threadIdx.x & 127;
+    const int per = np * np * NA;
+    for (int q = threadIdx.x; q < G * per; q += blockDim.x) sacc[q] = T(0);
+    if (threadIdx.x < kMaxPresent) seen[threadIdx.x] = 0;
+    if (threadIdx.x < 16) {
+        int v = -1;
+        for (int q = 0; q < np; ++q)
+            if (P.present[q] == (int)threadIdx.x) v = q;
+        qof[threadIdx.x] = v;
+    }
+    __syncthreads();
+    const int r0 = blockIdx.x * chunk;
+    const int r1 = r0 + chunk < P.rows ? r0 + chunk : P.rows;
+    T *acc = sacc + grp * per;
+    constexpr int U = 8;       // rows in flight per thread: their loads issue together
+    for (int row0 = r0 + grp; row0 < r1; row0 += U * G) {
+        int qv[U];
+        T gv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int row = row0 + u * G;
+            int t = -1;
+            if (row < r1) t = tm[row < P.natoms ? row : row % P.natoms];
+            qv[u] = t >= 0 && t < 16 ? qof[t] : -1;
+            gv[u] = qv[u] >= 0 && idx < NA ? A_bar[(long long)row * NA + idx] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            if (qv[u] >= 0 && idx == 0) seen[qv[u]] = 1;
+        if (idx < NA) {
+            for (int q = 0; q < np; ++q) {       // the U rows' counts of t_j load together
+                T nv[U];
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    nv[u] = qv[u] >= 0 ? T(n_empty[(row0 + u * G) * np + q]) : T(0);
+#pragma unroll
+                for (int u = 0; u < U; ++u)
+                    if (qv[u] >= 0) acc[(qv[u] * np + q) * NA + idx] += nv[u] * gv[u];
+            }
+        }
+    }
+    __syncthreads();
+    double *out = gsum + (long long)(blockIdx.x % kPadReps) * per;
+    for (int q = threadIdx.x; q < per; q += blockDim.x) {
+        if (!seen[q / (np * NA)]) continue;
+        double v = 0.0;
+        for (int g = 0; g < G; ++g) v += (double)sacc[g * per + q];
+        atomicAdd(out + q, v);
+    }
+}
+
+// One warp per present pair: the net's reverse from dPhi/dG = k sum_c R_pad[c] gsum[c][:],
+// writing the pair's gradient block of grad (EmbOff layout; other nets stay as zeroed).
+template <typename T>
+__global__ void __launch_bounds__(32) dp_pad_net_bwd(const T *__restrict__ params,
+                                                     const T *__restrict__ davg,
+                                                     const T *__restrict__ dstd, PadParams P,
+                                                     const double *__restrict__ gsum,
+                                                     T *__restrict__ grad) {
+    __shared__ T sx[32], sg[32];
+    const int pair = blockIdx.x, lane = threadIdx.x;
+    const int ti = P.present[pair / P.npresent], tj = P.present[pair % P.npresent];
+    const long long net = (long long)(ti * P.ntypes + tj) * EmbOff::SIZE;
+    const T *w = params + net;
+    T *g = grad + net;
+    const T s = pad_row_value(davg, dstd, ti, 0);
+    T x0, h1, x1, h2, x2;
+    pad_net_fwd(w, s, sx, lane, x0, h1, x1, h2, x2);
+    T gx = T(0);
+    if (lane < E) {
+        double a = 0.0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            double v = 0.0;
+            for (int r = 0; r < kPadReps; ++r)
+                v += gsum[((long long)r * P.npresent * P.npresent + pair) * NA + c * E + lane];
+            a += (double)pad_row_value(davg, dstd, ti, c) * v;
+        }
+        gx = T(P.inv_mT * a);
+    }
+    // layers 2 and 1: x_l = tanh(z_l) dt_l + x_{l-1}, z_l = x_{l-1} W_l + b_l
+    const int offW[2] = {EmbOff::W2, EmbOff::W1}, offB[2] = {EmbOff::B2, EmbOff::B1},
+              offD[2] = {EmbOff::DT2, EmbOff::DT1};
+    for (int L = 0; L < 2; ++L) {
+        const T h = L == 0 ? h2 : h1, xin = L == 0 ? x1 : x0;
+        T gz = T(0);
+        if (lane < E) {
+            g[offD[L] + lane] = gx * h;
+            gz = gx * w[offD[L] + lane] * (T(1) - h * h);
+            g[offB[L] + lane] = gz;
+            sg[lane] = gz;
+            sx[lane] = xin;
+        }
+        __syncwarp();
+        if (lane < E) {
+            T back = T(0);
+            for (int e = 0; e < E; ++e) {
+                g[offW[L] + e * E + lane] = sx[e] * gz;        // dW[e][lane] = xin[e] gz[lane]
+                back += w[offW[L] + lane * E + e] * sg[e];      // (W gz)[lane]
+            }
+            gx += back;
+        }
+        __syncwarp();
+    }
+    if (lane < E) {
+        const T gz0 = gx * (T(1) - x0 * x0);
+        g[EmbOff::B0 + lane] = gz0;
+        g[EmbOff::W0 + lane] = s * gz0;
+    }
+}
+
+int pad_params(const matpl_dp_model *md, int batch, int natoms, int nslots, PadParams &P) {
+    P.rows = batch * natoms; P.natoms = natoms; P.nslots = nslots;
+    P.ntypes = md->ntypes; P.m = md->m; P.npresent = md->npresent;
+    for (int q = 0; q < kMaxPresent; ++q) P.present[q] = q < md->npresent ? md->present[q] : 0;
+    P.inv_mT = 1.0 / ((double)md->m * (double)md->npresent);
+    return MATPL_OK;
+}
+
+template <typename T>
+int launch_pad(bool backward, const matpl_dp_model *md, int batch, int natoms, int nslots,
+               const int32_t *ln, const int32_t *tm, const void *in, void *out,
+               int32_t *n_empty, void *ws, cudaStream_t s) {
+    PadParams P;
+    pad_params(md, batch, natoms, nslots, P);
+    const int np = P.npresent, sms = device_sms();
+    if (!backward) {
+        T *prow = static_cast<T *>(ws);
+        {
+            ProfScope ps("dp_pad_rows", s);
+            dp_pad_rows<T><<<np * np, 32, 0, s>>>((const T *)md->params, (const T *)md->davg,
+                                                   (const T *)md->dstd, P, prow);
+        }
+        int st = check_launch("matpl_dp_pad_forward");
+        if (st) return st;
+        long long grid = ((long long)P.rows + 7) / 8;
+        if (grid > (long long)sms * 16) grid = (long long)sms * 16;
+        ProfScope ps("dp_pad_add", s);
+        dp_pad_add<T><<<(int)grid, 256, 0, s>>>(ln, tm, prow, P, (const T *)in, (T *)out,
+                                                n_empty);
+        return check_launch("matpl_dp_pad_forward");
+    }
+    double *gsum = static_cast<double *>(ws);
+    const size_t per = (size_t)np * np * NA * sizeof(double);
+    cudaMemsetAsync(gsum, 0, per * kPadReps, s);
+    cudaMemsetAsync(out, 0, (size_t)md->ntypes * md->ntypes * EmbOff::SIZE * sizeof(T), s);
+    const size_t sper = (size_t)np * np * NA * sizeof(T);   // one group's shared sums
+    int G = 4;                                       // row groups per CTA, as shared memory allows
+    while (G > 1 && sper * G > 100 * 1024) --G;
+    const long long nblk = (long long)sms * (16 / G);
+    const int chunk = (int)(((long long)P.rows + nblk - 1) / nblk);
+    const int grid = (P.rows + chunk - 1) / chunk;
+    cudaFuncSetAttribute(dp_pad_reduce<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(sper * G));
+    {
+        ProfScope ps("dp_pad_reduce", s);
+        dp_pad_reduce<T><<<grid, 128 * G, sper * G, s>>>(tm, n_empty, (const T *)in, P, chunk,
+                                                         gsum);
+    }
+    int st = check_launch("matpl_dp_pad_backward");
+    if (st) return st;
+    ProfScope ps("dp_pad_net_bwd", s);
+    dp_pad_net_bwd<T><<<np * np, 32, 0, s>>>((const T *)md->params, (const T *)md->davg,
+                                              (const T *)md->dstd, P, gsum, (T *)out);
+    return check_launch("matpl_dp_pad_backward");
+}
+
 int check_args(int dtype, int batch, int natoms, int nslots, int ntypes, int m) {
     MATPL_REQUIRE(dtype == MATPL_F32 || dtype == MATPL_F64, MATPL_ERR_DTYPE,
                   "the training kernels support MATPL_F32 and MATPL_F64");
@@ -721,6 +1028,69 @@ extern "C" int matpl_dp_dual_backward(int dtype, const matpl_dp_model *model, in
                : launch<float>(true, model, batch, natoms, nslots, list_neigh, image_dr,
                                type_map, grad_force, grad_virial, A_bar, A_dot_bar,
                                grad_embedding, nullptr, as_stream(stream));
+}
+
+extern "C" size_t matpl_dp_pad_workspace_bytes(int npresent) {
+    if (npresent < 1 || npresent > kMaxPresent) return 0;
+    return (size_t)kPadReps * npresent * npresent * NA * sizeof(double);
+}
+
+extern "C" int matpl_dp_pad_forward(int dtype, const matpl_dp_model *model, int batch,
+                                    int natoms, int nslots, const int32_t *list_neigh,
+                                    const int32_t *type_map, const void *A_occ, void *A,
+                                    int32_t *n_empty, void *workspace, size_t workspace_bytes,
+                                    void *stream) {
+    MATPL_REQUIRE(model != nullptr, MATPL_ERR_INVALID, "null model");
+    int st = check_args(dtype, batch, natoms, nslots, model->ntypes, model->m);
+    if (st) return st;
+    MATPL_REQUIRE(model->npresent >= 1 && model->npresent <= kMaxPresent, MATPL_ERR_INVALID,
+                  "npresent must be 1..8");
+    MATPL_REQUIRE((long long)batch * natoms < (1LL << 28), MATPL_ERR_INVALID,
+                  "batch * natoms must stay below 2^28");
+    for (int q = 0; q < model->npresent; ++q)
+        MATPL_REQUIRE(model->present[q] >= 0 && model->present[q] < model->ntypes,
+                      MATPL_ERR_INVALID, "present[] entry outside [0, ntypes)");
+    MATPL_REQUIRE(model->params && model->davg && model->dstd && list_neigh && type_map &&
+                      A_occ && A && n_empty,
+                  MATPL_ERR_INVALID, "null pointer argument");
+    MATPL_REQUIRE(workspace && workspace_bytes >= matpl_dp_pad_workspace_bytes(model->npresent),
+                  MATPL_ERR_WORKSPACE, "workspace smaller than matpl_dp_pad_workspace_bytes");
+    MATPL_REQUIRE_ON_DEVICE(A, "matpl_dp_pad_forward");
+    return dtype == MATPL_F64
+               ? launch_pad<double>(false, model, batch, natoms, nslots, list_neigh, type_map,
+                                    A_occ, A, n_empty, workspace, as_stream(stream))
+               : launch_pad<float>(false, model, batch, natoms, nslots, list_neigh, type_map,
+                                   A_occ, A, n_empty, workspace, as_stream(stream));
+}
+
+extern "C" int matpl_dp_pad_backward(int dtype, const matpl_dp_model *model, int batch,
+                                     int natoms, int nslots, const int32_t *type_map,
+                                     const int32_t *n_empty, const void *A_bar,
+                                     void *grad_embedding, void *workspace,
+                                     size_t workspace_bytes, void *stream) {
+    MATPL_REQUIRE(model != nullptr, MATPL_ERR_INVALID, "null model");
+    int st = check_args(dtype, batch, natoms, nslots, model->ntypes, model->m);
+    if (st) return st;
+    MATPL_REQUIRE(model->npresent >= 1 && model->npresent <= kMaxPresent, MATPL_ERR_INVALID,
+                  "npresent must be 1..8");
+    MATPL_REQUIRE((long long)batch * natoms < (1LL << 28), MATPL_ERR_INVALID,
+                  "batch * natoms must stay below 2^28");
+    for (int q = 0; q < model->npresent; ++q)
+        MATPL_REQUIRE(model->present[q] >= 0 && model->present[q] < model->ntypes,
+                      MATPL_ERR_INVALID, "present[] entry outside [0, ntypes)");
+    MATPL_REQUIRE(model->params && model->davg && model->dstd && type_map && n_empty && A_bar &&
+                      grad_embedding,
+                  MATPL_ERR_INVALID, "null pointer argument");
+    MATPL_REQUIRE(workspace && workspace_bytes >= matpl_dp_pad_workspace_bytes(model->npresent),
+                  MATPL_ERR_WORKSPACE, "workspace smaller than matpl_dp_pad_workspace_bytes");
+    MATPL_REQUIRE_ON_DEVICE(grad_embedding, "matpl_dp_pad_backward");
+    return dtype == MATPL_F64
+               ? launch_pad<double>(true, model, batch, natoms, nslots, nullptr, type_map, A_bar,
+                                    grad_embedding, const_cast<int32_t *>(n_empty), workspace,
+                                    as_stream(stream))
+               : launch_pad<float>(true, model, batch, natoms, nslots, nullptr, type_map, A_bar,
+                                   grad_embedding, const_cast<int32_t *>(n_empty), workspace,
+                                   as_stream(stream));
 }
 
 extern "C" int matpl_dp_desc_dual(int dtype, long long natoms, int m2, const long long *rows,

@@ -171,6 +171,19 @@ from . import _lib, dp as _dp  # noqa: E402
 from ._lib import check as _check, ptr as _ptr  # noqa: E402
 
 
+_CONSTS: Dict[tuple, torch.Tensor] = {}
+
+
+def _const(n: int, fill: float, like: torch.Tensor) -> torch.Tensor:
+    """A constant vector (an absent bias or resnet_dt) made once per device and dtype, so that
+    a training step spends no fill launch on it."""
+    key = (n, fill, like.dtype, like.device)
+    v = _CONSTS.get(key)
+    if v is None:
+        v = _CONSTS[key] = torch.full((n,), fill, dtype=like.dtype, device=like.device)
+    return v
+
+
 def _emb_flat(model: DPTrainModel) -> torch.Tensor:
     """Embedding parameters of every (t_i, t_j) net in the packed order of csrc/dp_layout.cuh,
     built from the model's Parameters with differentiable ops (gradients flow back to them)."""
@@ -182,10 +195,10 @@ def _emb_flat(model: DPTrainModel) -> torch.Tensor:
             w = model.param(pre + f"{l}.weight")
             b = model.param(pre + f"{l}.bias")
             parts.append(w.reshape(-1))
-            parts.append(b.reshape(-1) if b is not None else w.new_zeros(E))
+            parts.append(b.reshape(-1) if b is not None else _const(E, 0.0, w))
             if l > 0:
                 dt = model.param(pre + f"{l}.resnet_dt")
-                parts.append(dt.reshape(-1) if dt is not None else w.new_ones(E))
+                parts.append(dt.reshape(-1) if dt is not None else _const(E, 1.0, w))
     return torch.cat(parts)
 
 
@@ -199,12 +212,11 @@ def _pack_device(model: DPTrainModel) -> torch.Tensor:
 
             def g(name, n, fill):
                 v = model.param(pre + name)
-                return v.reshape(-1) if v is not None else torch.full(
-                    (n,), fill, dtype=model.dtype, device=model.davg.device)
+                return v.reshape(-1) if v is not None else _const(n, fill, model.davg)
             W0, W1, W2 = g("0.weight", 0, 0), g("1.weight", 0, 0), g("2.weight", 0, 0)
             parts += [W0, g("0.bias", F, 0.0), W1, g("1.bias", F, 0.0), g("1.resnet_dt", F, 1.0),
                       W2, g("2.bias", F, 0.0), g("2.resnet_dt", F, 1.0), g("3.weight", 0, 0),
-                      g("3.bias", 1, 0.0), W0.new_zeros(3),
+                      g("3.bias", 1, 0.0), _const(3, 0.0, model.davg),
                       W0.reshape(DIN, F).t().reshape(-1), W1.reshape(F, F).t().reshape(-1),
                       W2.reshape(F, F).t().reshape(-1)]
         return torch.cat(parts).contiguous()
@@ -247,6 +259,48 @@ class _EmbedDual(torch.autograd.Function):
             _ptr(gV) if ctx.has_gv else 0, _ptr(gA), _ptr(gAd), _ptr(grad),
             torch.cuda.current_stream(dev).cuda_stream), "matpl_dp_dual_backward")
         return grad, None, None, None, None, None, None
+
+
+class _EmptySlots(torch.autograd.Function):
+    """A = A_occ + the empty-slot term of A (matpl_dp_pad_forward: every empty slot of type
+    block t_j holds the normalised zero row, whose embedding is the same for all of them); the
+    backward passes dPhi/dA to A_occ unchanged and gives the embedding parameters' part through
+    the empty slots (matpl_dp_pad_backward)."""
+
+    @staticmethod
+    @_lib.on_device
+    def forward(ctx, A_occ, emb_flat, trainer, ln, tm):
+        B, N, S = ln.shape
+        dev = ln.device
+        A_occ = A_occ.contiguous()
+        flat = emb_flat.detach().contiguous()
+        m = trainer._struct(flat)
+        L = _lib.load()
+        np_ = len(trainer._present)
+        ws = torch.empty(L.matpl_dp_pad_workspace_bytes(np_), dtype=torch.uint8, device=dev)
+        ne = torch.empty(B * N, np_, dtype=torch.int32, device=dev)
+        A = torch.empty_like(A_occ)
+        _check(L.matpl_dp_pad_forward(
+            trainer.code, ctypes.byref(m), B, N, S, _ptr(ln), _ptr(tm), _ptr(A_occ), _ptr(A),
+            _ptr(ne), _ptr(ws), ws.numel(), torch.cuda.current_stream(dev).cuda_stream),
+            "matpl_dp_pad_forward")
+        ctx.trainer, ctx.shape = trainer, (B, N, S)
+        ctx.save_for_backward(flat, tm, ne, ws)
+        return A
+
+    @staticmethod
+    @_lib.on_device
+    def backward(ctx, gA):
+        flat, tm, ne, ws = ctx.saved_tensors
+        B, N, S = ctx.shape
+        gA = gA.contiguous()
+        grad = torch.empty_like(flat)
+        m = ctx.trainer._struct(flat)
+        _check(_lib.load().matpl_dp_pad_backward(
+            ctx.trainer.code, ctypes.byref(m), B, N, S, _ptr(tm), _ptr(ne), _ptr(gA),
+            _ptr(grad), _ptr(ws), ws.numel(), torch.cuda.current_stream(gA.device).cuda_stream),
+            "matpl_dp_pad_backward")
+        return gA, grad, None, None, None
 
 
 class _DescDual(torch.autograd.Function):
@@ -340,13 +394,13 @@ class _FitDualPhi(torch.autograd.Function):
     @torch.autograd.function.once_differentiable
     def backward(ctx, gphi):
         gD, gDd, gP = ctx.saved_tensors
+        torch._foreach_mul_([gD, gDd, gP], gphi)        # one launch for the three buffers
         grads = []
         k = len(_FIT_PARAMS)
         for q, shape in enumerate(ctx.shapes):
             _, off, size = _FIT_PARAMS[q % k]
-            grads.append(None if shape is None else
-                         (gP[q // k, off:off + size] * gphi).reshape(shape))
-        return (gD.mul_(gphi), gDd.mul_(gphi), None, None, None, None, *grads)
+            grads.append(None if shape is None else gP[q // k, off:off + size].reshape(shape))
+        return (gD, gDd, None, None, None, None, *grads)
 
 
 class FusedTrainer:
@@ -356,7 +410,8 @@ class FusedTrainer:
     1. E, F with the current parameters through the fused evaluation (``matpl_dp_eval``);
     2. gE = dL/dE, gF = dL/dF of the loss (dp_loss's MSE terms) on those values;
     3. A, A_dot = per-atom descriptor factor and its tangent along the seed gF
-       (``matpl_dp_dual_forward``), plus the empty-slot term of A in torch;
+       (``matpl_dp_dual_forward``), plus the empty-slot term of A
+       (``matpl_dp_pad_forward``);
     4. Ei = fitting nets on D = A^T A<, Edot = dEi/dA . A_dot;
     5. Phi = sum gE Etot + sum Edot; Phi.backward() gives dL/dtheta: the fitting part by
        ``matpl_dp_fit_dual`` (both streams and the closed-form reverse pass in one kernel, the
@@ -407,50 +462,6 @@ class FusedTrainer:
         m.params, m.davg, m.dstd = _ptr(flat), _ptr(self.davg4), _ptr(self.dstd4)
         m.err_dev = _ptr(self.evaluator.err)
         return m
-
-    def _pad_term(self, ln, present):
-        """Empty-slot term of A (before the 1/(mT) scale is applied): per atom
-        sum over present t_j of n_empty(t_j) R_pad(t_i) (x) G_{t_i t_j}(s_pad(t_i)).  Every
-        present pair's net is evaluated at its s_pad together (stacked weights, batched
-        products), and the per-atom weights onehot(t_i) n_empty(t_j) enter as one product over
-        the pairs (its gradient, a sum over the atoms, split like the fitting products)."""
-        model, cfg = self.model, self.model.cfg
-        B, N, S = ln.shape
-        T, m = cfg.ntypes, cfg.maxNeighborNum
-        dev, dt = ln.device, model.dtype
-        pairs = [(ti, tj) for ti in present for tj in present]
-        P = len(pairs)
-        key = (tuple(present), dev)
-        if getattr(self, "_pair_idx_key", None) != key:      # made outside graph capture
-            self._pair_idx = (torch.tensor([p[0] for p in pairs], device=dev),
-                              torch.tensor([p[1] for p in pairs], device=dev))
-            self._pair_idx_key = key
-        ti_idx, tj_idx = self._pair_idx
-        rpp = ((0.0 - self.davg4) / self.dstd4).index_select(0, ti_idx)      # [P, 4]
-
-        def stacked(l, name):
-            vals = [model.param(f"embedding_net.{ti * T + tj}.layers.{l}.{name}")
-                    for ti, tj in pairs]
-            if all(v is None for v in vals):
-                return None
-            return torch.stack([v if v is not None else
-                                (torch.ones_like(vals[0]) if name == "resnet_dt"
-                                 else torch.zeros_like(vals[0])) for v in vals])
-        # layer 0 (1 -> E): s W0 + b0; layers 1, 2 (E -> E, residual), as DPTrainModel._emb
-        x = rpp[:, 0].reshape(P, 1, 1) * stacked(0, "weight")                 # [P, 1, E]
-        b0 = stacked(0, "bias")
-        x = torch.tanh(x + b0 if b0 is not None else x)
-        for l in (1, 2):
-            h = torch.bmm(x, stacked(l, "weight"))
-            b = stacked(l, "bias")
-            h = torch.tanh(h + b if b is not None else h)
-            d = stacked(l, "resnet_dt")
-            x = (h * d if d is not None else h) + x
-        prow = (rpp.unsqueeze(-1) * x.reshape(P, 1, _dp.E)).reshape(P, 4 * _dp.E)
-        occ = (ln > 0).reshape(B, N, T, m).sum(-1).to(dt)                      # [B, N, T]
-        onehot = (self._tm_long.reshape(1, N, 1) == ti_idx.reshape(1, 1, P)).to(dt)
-        wts = onehot * (m - occ).index_select(2, tj_idx)                       # [B, N, P]
-        return splitk.mm(wts.reshape(B * N, P), prow).reshape(B, N, 4, _dp.E)
 
     def _fit_dual(self, t: int, x: torch.Tensor, xd: torch.Tensor):
         """Fitting net of element t (dp_embedding.py:140-163) on rows x and its tangent xd:
@@ -514,7 +525,6 @@ class FusedTrainer:
         tm32 = batch["type_map"]
         self._tm_src = tm32
         tm32 = tm32 if tm32.dtype == torch.int32 else tm32.to(device=dev, dtype=torch.int32).contiguous()
-        self._tm_long = tm32.long()
         present = [cfg.atom_type.index(int(a)) for a in batch["atom_type"]
                    if int(a) in cfg.atom_type]
         self._present = present
@@ -540,8 +550,9 @@ class FusedTrainer:
         gE, gF = torch.autograd.grad(loss, [Et, Fo])
         gF = gF.contiguous()
         # 3. descriptor factor and its tangent
-        A_occ, Ad = _EmbedDual.apply(_emb_flat(model), self, ln32, idr, tm32, gF, None)
-        A = A_occ.reshape(B, N, 4, _dp.E) + self._pad_term(ln, present) / (cfg.maxNeighborNum * len(present))
+        emb = _emb_flat(model)
+        A_occ, Ad = _EmbedDual.apply(emb, self, ln32, idr, tm32, gF, None)
+        A = _EmptySlots.apply(A_occ, emb, self, ln32, tm32).reshape(B, N, 4, _dp.E)
         Ad = Ad.reshape(B, N, 4, _dp.E)
         # 4. per-atom energies and their tangent (explicit forward-mode through D and the
         #    fitting net), 5. one first-order backward of Phi gives every parameter gradient

@@ -317,3 +317,31 @@ def test_ctypes_signatures_match_the_header_prototypes():
         assert len(argtypes) == len(params), name
         for i, (p, t) in enumerate(zip(params, argtypes)):
             assert _c_class(p) == _ctypes_class(t), f"{name} parameter {i}: {p!r} vs {t!r}"
+
+
+def test_empty_slot_entry_points_validate_on_the_host():
+    """The training empty-slot kernels refuse bad dtypes, present lists, NULL pointers and a
+    short workspace before any CUDA call."""
+    lib = _lib.load()
+    INVALID, DTYPE, WORKSPACE = 1, 2, 3
+    nb = lib.matpl_dp_pad_workspace_bytes(2)
+    assert nb >= 2 * 2 * 100 * 8 and nb % 16 == 0
+    assert lib.matpl_dp_pad_workspace_bytes(0) == 0 and lib.matpl_dp_pad_workspace_bytes(9) == 0
+    m = _lib.MatplDpModel()
+    m.ntypes, m.m, m.npresent, m.present[0], m.present[1] = 2, 100, 2, 0, 1
+    p = ctypes.c_void_p(16)            # never dereferenced: every call below fails first
+    m.params = m.davg = m.dstd = 16
+    fwd = lambda dt, md, ws, nb, a=p: lib.matpl_dp_pad_forward(  # noqa: E731
+        dt, ctypes.byref(md), 1, 10, 200, p, p, p, a, p, ws, nb, None)
+    bwd = lambda dt, md, ws, nb, g=p: lib.matpl_dp_pad_backward(  # noqa: E731
+        dt, ctypes.byref(md), 1, 10, 200, p, p, p, g, ws, nb, None)
+    for call in (fwd, bwd):
+        assert call(_lib.MATPL_MIXED, m, p, nb) == DTYPE
+        assert call(_lib.MATPL_F32, m, p, nb - 1) == WORKSPACE
+        assert call(_lib.MATPL_F32, m, None, nb) == WORKSPACE
+    assert fwd(_lib.MATPL_F32, m, p, nb, a=None) == INVALID
+    assert bwd(_lib.MATPL_F64, m, p, nb, g=None) == INVALID
+    m.present[1] = 2
+    assert fwd(_lib.MATPL_F32, m, p, nb) == INVALID and b"present" in lib.matpl_last_error()
+    m.present[1], m.npresent = 1, 9
+    assert bwd(_lib.MATPL_F32, m, p, nb) == INVALID
